@@ -1,0 +1,92 @@
+/*
+ * CPU oracle for the Dual Marching Cubes + manifold repair path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library restates the reference's algorithm
+ * (PhiliGuertler/ManifoldDMC, MarchingCubes/VisualDMC/src/DMC/) on the CPU so
+ * that the CUDA path can be checked against it.  Only tests/, the smoke test
+ * and bench.py's CPU-baseline leg may load it.  The product library never
+ * links or calls it.
+ *
+ * Parity pin: the oracle is checked against the reference's 28 golden meshes
+ * (Data-and-Results/Base-Results) in tests/test_oracle_golden.py.
+ *
+ * Ordering conventions (the reference's are atomic-order nondeterministic; the
+ * oracle and the CUDA path share these deterministic ones):
+ *   - vertices: by cell linear index, then contour index inside the cell;
+ *   - quads: by edge key 3*sample_index + axis, ascending;
+ *   - halfedge 4q+i belongs to quad q; halfedge ids inside an edge bucket are
+ *     sorted ascending before twins are formed;
+ *   - splitter working copies: non-manifold faces in ascending face order,
+ *     new elements per face in the reference's per-thread creation order.
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mdmc_oracle_options {
+    int surface_iteration;     /* m_enableSurfaceToVertexIteration (default 1) */
+    int simplify_3x3y_color;   /* m_simplifyP3x3yColor (default 0) */
+    int simplify_3x3y_old;     /* m_simplifyP3x3yOld (default 0) */
+    int simplify_3333;         /* m_simplifyP3333 (default 0) */
+    int split_non_manifold;    /* m_splitNonManifoldHalfedges (default 1) */
+    int detect_non_manifold_vertices; /* m_detectNonManifoldVertices (default 1) */
+    int splitting_step;        /* SplittingStep, 100 = All (default) */
+} mdmc_oracle_options;
+
+/* counts[] layout of mdmc_oracle_counts */
+enum {
+    MDMC_ORC_NUM_VERTICES = 0,
+    MDMC_ORC_NUM_FACES = 1,
+    MDMC_ORC_NUM_HALFEDGES = 2,
+    MDMC_ORC_NUM_DMC_VERTICES = 3,   /* before post-processing */
+    MDMC_ORC_NUM_DMC_QUADS = 4,
+    MDMC_ORC_NUM_COUNTS = 5
+};
+
+/* stats[] layout of mdmc_oracle_stats (mirrors the reference's getters) */
+enum {
+    MDMC_ORC_STAT_EDGES = 0,          /* getNumEdges */
+    MDMC_ORC_STAT_EDGES3 = 1,         /* getNumNonManifoldEdges3 */
+    MDMC_ORC_STAT_EDGES4 = 2,         /* getNumNonManifoldEdges4 */
+    MDMC_ORC_STAT_NM_VERTICES = 3,    /* getNumNonManifoldVertices (-1 if detection off) */
+    MDMC_ORC_STAT_QUADS_NM1 = 4,      /* getNumQuadsWithNonManifoldEdges(1..4) */
+    MDMC_ORC_STAT_QUADS_NM2 = 5,
+    MDMC_ORC_STAT_QUADS_NM3 = 6,
+    MDMC_ORC_STAT_QUADS_NM4 = 7,
+    MDMC_ORC_STAT_SPLIT_ITERATIONS = 8,
+    MDMC_ORC_STAT_ANOMALIES = 9,      /* bucket overflow, partner overflow, ... */
+    MDMC_ORC_NUM_STATS = 10
+};
+
+void mdmc_oracle_default_options(mdmc_oracle_options* o);
+
+/* Reads a reference .bin volume (int32 dims[3], float32 spacing[3], uint16
+ * samples, x fastest); origin = -(dims-1)/2 * spacing.  With out == NULL only
+ * the header is returned.  Returns 0 on success.  D/UniformGrid.inl:512-571 */
+int mdmc_oracle_read_bin(const char* path, int dims[3], float spacing[3], float origin[3], float* out);
+
+/* Trilinear refinement and/or replicate padding, D/UniformGrid.inl:279-319 and
+ * :575-608.  out must hold the refined dims' product; out_dims, out_origin and
+ * out_spacing receive the refined grid's geometry. */
+void mdmc_oracle_refine(const float* in, const int dims[3], const float origin[3],
+                        const float spacing[3], int refinement, int pad,
+                        float* out, int out_dims[3], float out_origin[3], float out_spacing[3]);
+
+void* mdmc_oracle_run(const float* grid, const int dims[3], const float origin[3],
+                      const float spacing[3], float iso, const mdmc_oracle_options* opt);
+void mdmc_oracle_counts(const void* result, int64_t counts[MDMC_ORC_NUM_COUNTS]);
+void mdmc_oracle_stats(const void* result, int64_t stats[MDMC_ORC_NUM_STATS]);
+/* Any pointer may be NULL.  halfedges: 4 ints per halfedge (origin, face, next, twin). */
+void mdmc_oracle_get(const void* result, float* positions, float* normals, int* halfedges,
+                     int* face_first, uint16_t* face_attr, uint8_t* vertex_flags, int* vertex_he);
+/* DMC stage only (before post-processing): vertices and quads (4 ids). */
+void mdmc_oracle_get_dmc(const void* result, float* positions, float* normals, int* quads,
+                         uint16_t* quad_attr);
+void mdmc_oracle_free(void* result);
+
+#ifdef __cplusplus
+}
+#endif

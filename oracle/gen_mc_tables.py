@@ -1,0 +1,106 @@
+"""Recipe: re-encode the reference's Marching Cubes polygon table.
+
+The Dual Marching Cubes path of the reference reads its cell polygons from
+``s_polygonPatterns`` (MarchingCubes/VisualDMC/src/DMC/DualMarchingCubes.cpp:564)
+and its ambiguity marks from ``s_triangleAmbiguities`` (same file, :301).
+The per-cell vertex positions are sums of edge crossings taken in the table's
+edge order, so bit-exact parity needs the same contour and edge order.  This
+script stores that order in the packed 64-bit layout that the reference builds
+at run time in ``Contour`` (D/CellIntersection.h:28-137): contour sizes in
+nibbles 0-3, the edges of all contours back to back in nibbles 4-15.  One
+8-byte word per case replaces a 17-byte row walk in the cell kernel.
+
+It writes the same words to the product header and to the oracle's header,
+and a SHA-256 digest of the words and of the ambiguity marks to
+``tests/golden/mc_tables_digest.json`` so that the tests can check both
+headers (and the ambiguity rule written in code) without the reference.
+
+Run from the repository root:  python3 oracle/gen_mc_tables.py [reference_root]
+"""
+import hashlib
+import json
+import os
+import re
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+SRC = os.path.join(REF, "MarchingCubes/VisualDMC/src/DMC/DualMarchingCubes.cpp")
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+def _array(src, name):
+    i = src.index(name)
+    j = src.index("{", i)
+    k = src.index("};", j)
+    body = re.sub(r"//[^\n]*", "", src[j + 1:k])
+    body = body.replace("MC_AMBIGUOUS", "105")
+    body = re.sub(r"static_cast<char>\((-?\d+)\)", r"\1", body)
+    return [int(t) for t in re.findall(r"-?\d+", body)]
+
+
+def pack_case(row):
+    n = row[0]
+    word = 0xFFFFFFFFFFFF0000
+    cursor = n + 1
+    total = 0
+    for t in range(n):
+        size = row[1 + t]
+        word &= ~(0xF << (4 * t))
+        word |= size << (4 * t)
+        for i in range(size):
+            bit = 16 + 4 * (total + i)
+            word &= ~(0xF << bit)
+            word |= row[cursor] << bit
+            cursor += 1
+        total += size
+    return word & 0xFFFFFFFFFFFFFFFF
+
+
+def main():
+    src = open(SRC, encoding="latin-1").read()
+    poly = _array(src, "s_polygonPatterns =")
+    amb = _array(src, "s_triangleAmbiguities =")
+    assert len(poly) == 256 * 17 and len(amb) == 256
+    words = [pack_case(poly[17 * c:17 * c + 17]) for c in range(256)]
+    ambiguous = [1 if amb[c] == 105 else 0 for c in range(256)]
+
+    lines = []
+    for c in range(0, 256, 4):
+        lines.append("    " + ", ".join("0x%016xULL" % w for w in words[c:c + 4]) + ",")
+    table = "\n".join(lines)
+    header = (
+        "// Generated by oracle/gen_mc_tables.py -- do not edit by hand.\n"
+        "// Per Marching Cubes case (bit i set <=> corner i >= iso), the cell's\n"
+        "// contours packed as: nibbles 0-3 = contour sizes, nibbles 4-15 = the\n"
+        "// intersected cell edges of all contours back to back (0xF = unused).\n"
+        "// Same contour/edge order as the reference's polygon table\n"
+        "// (MarchingCubes/VisualDMC/src/DMC/DualMarchingCubes.cpp:564), packed as\n"
+        "// its Contour class does (D/CellIntersection.h:28-137).  Ambiguous cases\n"
+        "// do not read this table.\n"
+    )
+    prod = os.path.join(ROOT, "manifolddmc_gb300", "csrc", "mc_contour_table.h")
+    with open(prod, "w") as f:
+        f.write("#pragma once\n" + header +
+                "namespace mdmc {\n// Lives in global memory; kernels stage it in shared memory (lanes index it\n// with divergent cases, which would serialise a __constant__ read).\n__device__ const unsigned long long kContourTable[256] = {\n"
+                + table + "\n};\n}  // namespace mdmc\n")
+    orc = os.path.join(ROOT, "oracle", "mc_contour_table_oracle.h")
+    with open(orc, "w") as f:
+        f.write("#pragma once\n" + header +
+                "namespace oracle {\nstatic const unsigned long long kContourTable[256] = {\n"
+                + table + "\n};\n}  // namespace oracle\n")
+    digest = {
+        "contour_words_sha256": hashlib.sha256(
+            b"".join(w.to_bytes(8, "little") for w in words)).hexdigest(),
+        "ambiguous_sha256": hashlib.sha256(bytes(ambiguous)).hexdigest(),
+        "num_ambiguous": sum(ambiguous),
+        "source": "MarchingCubes/VisualDMC/src/DMC/DualMarchingCubes.cpp:301,564",
+    }
+    with open(os.path.join(ROOT, "tests", "golden", "mc_tables_digest.json"), "w") as f:
+        json.dump(digest, f, indent=1)
+        f.write("\n")
+    print("wrote", prod, orc, digest)
+
+
+if __name__ == "__main__":
+    main()

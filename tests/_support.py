@@ -1,0 +1,208 @@
+"""Shared helpers for the test-suite: the CPU oracle's ctypes binding, golden
+fixtures and mesh canonicalisation.  The oracle is test infrastructure; the
+product library (manifolddmc_gb300) never loads it."""
+import ctypes
+import json
+import os
+import subprocess
+import threading
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[1]
+ORACLE_DIR = ROOT / "oracle"
+ORACLE_SO = ORACLE_DIR / "_build" / "libmdmc_oracle.so"
+GOLDEN_DIR = ROOT / "tests" / "golden"
+
+_lock = threading.Lock()
+_lib = None
+
+# SplittingStep, MarchingCubes/VisualDMC/src/DMC/PostProcesses/ManifoldSplitter.h:155-166
+STEP_NONE, STEP_SUBDIVIDE, STEP_COLLAPSE, STEP_MERGE, STEP_TWINS, STEP_MOVE, STEP_ITERATE = range(7)
+STEP_ALL = 100
+
+STAT_NAMES = ["edges", "edges3", "edges4", "nm_vertices", "quads_nm1", "quads_nm2",
+              "quads_nm3", "quads_nm4", "split_iterations", "anomalies"]
+
+
+class OracleOptions(ctypes.Structure):
+    _fields_ = [("surface_iteration", ctypes.c_int),
+                ("simplify_3x3y_color", ctypes.c_int),
+                ("simplify_3x3y_old", ctypes.c_int),
+                ("simplify_3333", ctypes.c_int),
+                ("split_non_manifold", ctypes.c_int),
+                ("detect_non_manifold_vertices", ctypes.c_int),
+                ("splitting_step", ctypes.c_int)]
+
+
+def build_oracle():
+    """Builds oracle/_build/libmdmc_oracle.so when it is missing or stale."""
+    srcs = [ORACLE_DIR / n for n in ("dmc_oracle.cpp", "dmc_oracle.h", "mc_contour_table_oracle.h")]
+    if ORACLE_SO.exists() and all(ORACLE_SO.stat().st_mtime >= s.stat().st_mtime for s in srcs):
+        return
+    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], check=True)
+
+
+def oracle():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build_oracle()
+            lib = ctypes.CDLL(str(ORACLE_SO))
+            lib.mdmc_oracle_run.restype = ctypes.c_void_p
+            lib.mdmc_oracle_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p]
+            for name in ("mdmc_oracle_counts", "mdmc_oracle_stats", "mdmc_oracle_free"):
+                getattr(lib, name).argtypes = [ctypes.c_void_p] + ([ctypes.c_void_p] if name != "mdmc_oracle_free" else [])
+            lib.mdmc_oracle_get.argtypes = [ctypes.c_void_p] * 8
+            lib.mdmc_oracle_get_dmc.argtypes = [ctypes.c_void_p] * 5
+            lib.mdmc_oracle_refine.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                               ctypes.c_void_p]
+            lib.mdmc_oracle_read_bin.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 4
+            _lib = lib
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def default_options(**kw):
+    o = OracleOptions(1, 0, 0, 0, 1, 1, STEP_ALL)
+    for k, v in kw.items():
+        setattr(o, k, int(v))
+    return o
+
+
+def refined_geometry(dims, spacing, origin, refinement, pad):
+    dims = np.asarray(dims, np.int64)
+    out = dims + (dims - 1) * refinement + (2 if pad else 0)
+    sp = (np.asarray(spacing, np.float32) * np.float32(1.0)) / (np.float32(refinement) + np.float32(1.0))
+    org = np.asarray(origin, np.float32).copy()
+    if pad:
+        org = (org - sp).astype(np.float32)
+    return [int(x) for x in out], sp.astype(np.float32), org.astype(np.float32)
+
+
+def oracle_refine(samples, dims, origin, spacing, refinement, pad):
+    """samples: float32 array with x fastest; returns (grid, dims, origin, spacing)."""
+    lib = oracle()
+    samples = np.ascontiguousarray(samples, np.float32).reshape(-1)
+    d = np.asarray(dims, np.int32)
+    od, _, _ = refined_geometry(dims, spacing, origin, refinement, pad)
+    out = np.empty(int(np.prod(od)), np.float32)
+    odims = np.zeros(3, np.int32)
+    oorg = np.zeros(3, np.float32)
+    osp = np.zeros(3, np.float32)
+    lib.mdmc_oracle_refine(_p(samples), _p(d), _p(np.asarray(origin, np.float32)),
+                           _p(np.asarray(spacing, np.float32)), int(refinement), int(pad),
+                           _p(out), _p(odims), _p(oorg), _p(osp))
+    return out, [int(x) for x in odims], oorg, osp
+
+
+def oracle_run(grid, dims, origin, spacing, iso, **opts):
+    """Runs the oracle; returns a dict with the DMC stage and the final mesh."""
+    lib = oracle()
+    grid = np.ascontiguousarray(grid, np.float32).reshape(-1)
+    assert grid.size == int(np.prod(dims))
+    o = default_options(**opts)
+    res = lib.mdmc_oracle_run(_p(grid), _p(np.asarray(dims, np.int32)),
+                              _p(np.asarray(origin, np.float32)), _p(np.asarray(spacing, np.float32)),
+                              ctypes.c_float(iso), ctypes.byref(o))
+    try:
+        counts = np.zeros(5, np.int64)
+        stats = np.zeros(10, np.int64)
+        lib.mdmc_oracle_counts(res, _p(counts))
+        lib.mdmc_oracle_stats(res, _p(stats))
+        V, F, H, DV, DQ = (int(x) for x in counts)
+        out = {
+            "positions": np.zeros((V, 3), np.float32), "normals": np.zeros((V, 3), np.float32),
+            "halfedges": np.zeros((H, 4), np.int32), "face_first": np.zeros(F, np.int32),
+            "face_attr": np.zeros(F, np.uint16), "vertex_flags": np.zeros(V, np.uint8),
+            "vertex_he": np.zeros(V, np.int32),
+            "dmc_positions": np.zeros((DV, 3), np.float32), "dmc_normals": np.zeros((DV, 3), np.float32),
+            "dmc_quads": np.zeros((DQ, 4), np.int32), "dmc_quad_attr": np.zeros(DQ, np.uint16),
+        }
+        lib.mdmc_oracle_get(res, _p(out["positions"]), _p(out["normals"]), _p(out["halfedges"]),
+                            _p(out["face_first"]), _p(out["face_attr"]), _p(out["vertex_flags"]),
+                            _p(out["vertex_he"]))
+        lib.mdmc_oracle_get_dmc(res, _p(out["dmc_positions"]), _p(out["dmc_normals"]),
+                                _p(out["dmc_quads"]), _p(out["dmc_quad_attr"]))
+        out["stats"] = dict(zip(STAT_NAMES, (int(x) for x in stats)))
+        return out
+    finally:
+        lib.mdmc_oracle_free(res)
+
+
+def face_vertices(halfedges, face_first):
+    """(F, 4) vertex ids of each face, walking next pointers from its first halfedge."""
+    he = np.asarray(halfedges)
+    h = np.asarray(face_first).astype(np.int64)
+    cols = []
+    for _ in range(4):
+        cols.append(he[h, 0])
+        h = he[h, 2]
+    return np.stack(cols, axis=1) if len(face_first) else np.zeros((0, 4), np.int32)
+
+
+# ---------------------------------------------------------------------------
+# golden fixtures
+# ---------------------------------------------------------------------------
+_goldens = None
+
+
+def reference_goldens():
+    global _goldens
+    if _goldens is None:
+        with open(GOLDEN_DIR / "reference_goldens.json") as f:
+            _goldens = json.load(f)
+    return _goldens
+
+
+LEVEL_OPTIONS = {
+    # level: (pad, options) -- Data-and-Results/README.md, LayerCUDA.cpp:575-636
+    0: (False, dict(split_non_manifold=0, splitting_step=STEP_NONE)),
+    1: (True, dict(split_non_manifold=0, splitting_step=STEP_NONE)),
+    2: (True, dict(split_non_manifold=1, splitting_step=STEP_MOVE)),
+    3: (True, dict(split_non_manifold=1, splitting_step=STEP_ALL)),
+}
+
+
+def golden_grid(case):
+    g = reference_goldens()[case]
+    dims = g["dims"]
+    spacing = np.asarray(g["spacing"], np.float32)
+    origin = ((np.float32(-0.5) * (np.asarray(dims, np.float32) - np.float32(1))) * spacing).astype(np.float32)
+    samples = np.asarray(g["samples"], np.float32)
+    return samples, dims, origin, spacing, float(np.float32(g["iso"]))
+
+
+def canonical_faces(faces):
+    """Rotates each face to start at its smallest id (orientation kept) and sorts."""
+    out = []
+    for f in faces:
+        f = list(int(x) for x in f)
+        k = f.index(min(f))
+        out.append(tuple(f[k:] + f[:k]))
+    return sorted(out)
+
+
+def match_to_golden(positions, faces, golden, tol):
+    """Maps referenced vertices onto the golden mesh's vertices by position.
+    Returns (mapped canonical faces, golden canonical faces, max distance, mapping)."""
+    gv = np.asarray(golden["v"], np.float64)
+    gf = np.asarray(golden["f"], np.int64).reshape(-1, 4)
+    used = np.unique(np.asarray(faces).reshape(-1)) if len(faces) else np.zeros(0, np.int64)
+    mapping = {}
+    maxd = 0.0
+    gref = np.unique(gf.reshape(-1)) if len(gf) else np.zeros(0, np.int64)
+    for v in used:
+        d = np.linalg.norm(gv[gref] - np.asarray(positions[v], np.float64)[None, :], axis=1)
+        j = int(np.argmin(d))
+        maxd = max(maxd, float(d[j]))
+        mapping[int(v)] = int(gref[j])
+    mapped = [[mapping[int(x)] for x in f] for f in faces]
+    return canonical_faces(mapped), canonical_faces(gf), maxd, mapping
