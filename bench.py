@@ -1,0 +1,367 @@
+#!/usr/bin/env python3
+"""Benchmark: Dual Marching Cubes + non-manifold repair on GB300.
+
+One step = one pass of the reference's DMC entry point over one grid: grid
+refinement (UniformGridHost::readFromFile's refine, minus file IO), then
+DualMarchingCubes::run with the reference's default flags (vertex-to-surface
+iteration, non-manifold split with all steps, non-manifold vertex detection).
+
+Default workload ("blobs129_refine4"): a 129^3 fp32 grid of 64 seeded Gaussian
+blobs (sigma 3-12 cells) refined x4 to 513^3 samples = 512^3 cells, iso 0.4.
+Metric: Mcells/s = processed cells / step time.  `value` is timed with the
+input already resident in HBM; `e2e` goes through the C ABI from pinned host
+memory (upload of the 129^3 input, run, download of the whole mesh).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config NAME]
+
+With --gpus N > 1 (launched under torch.distributed.run) every rank runs an
+independent replica on its own grid (different seed); value = all ranks' cells
+/ the slowest rank's time ("replicas only": the path has no exchange step).
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", default="blobs129_refine4")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def peaks():
+    try:
+        p = json.loads(PEAKS_FILE.read_text())
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed loop runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(kernel, s):
+    """Bytes a kernel must move, per launch (each datum read or written once)."""
+    S_in, S, rows = s["samples_in"], s["samples"], s["rows"]
+    A, V, Q, cap = s["active"], s["dmc_vertices"], s["dmc_quads"], s["table_buckets"]
+    if kernel == "refine":
+        return 4 * S_in + 4 * S
+    if kernel == "count":  # grid read once, per-row counts written
+        return 4 * S + 16 * rows
+    if kernel == "emit":  # grid read once, row offsets read, vertices + records written
+        return 4 * S + 16 * rows + 24 * V + 16 * A
+    if kernel == "quads":  # records read; halfedges, faces, attributes and edge keys written
+        return 16 * A + 64 * Q + 4 * Q + 2 * Q + 4 * Q * 8
+    if kernel == "table":  # buckets read once; twins written
+        return 32 * cap + 16 * Q
+    raise KeyError(kernel)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    import manifolddmc_gb300 as mdmc
+    from manifolddmc_gb300.workloads import CONFIGS
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    desc, gen, iso, refine, pad = CONFIGS[args.config]
+    vol = gen() if rank == 0 else gen(seed=100 + rank)  # replicas get their own grid
+    dims_in = [vol.shape[2], vol.shape[1], vol.shape[0]]
+    origin = np.zeros(3, np.float32)
+    spacing = np.ones(3, np.float32)
+    lib = mdmc.library()
+    ctx = ctypes.c_void_p()
+    assert lib.mdmc_create(ctypes.byref(ctx), None) == 0
+    stream = torch.cuda.current_stream(dev)
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    d_in = torch.from_numpy(vol).to(dev)
+    dims_c = np.asarray(dims_in, np.int32)
+    grid = mdmc.Grid()
+    stats = mdmc.Stats()
+    mesh = mdmc.Mesh()
+
+    def check(st):
+        if st != 0:
+            raise RuntimeError(lib.mdmc_last_error(ctx).decode())
+
+    def step(host=None):
+        src, on_host = (host.data_ptr(), 1) if host is not None else (d_in.data_ptr(), 0)
+        check(lib.mdmc_prepare_grid(ctx, ctypes.c_void_p(src), on_host, dims_c.ctypes.data_as(ctypes.c_void_p),
+                                    origin.ctypes.data_as(ctypes.c_void_p), spacing.ctypes.data_as(ctypes.c_void_p),
+                                    refine, int(pad), ctypes.byref(grid), sh))
+        st = lib.mdmc_run(ctx, ctypes.byref(grid), ctypes.c_float(iso), ctypes.byref(mesh), ctypes.byref(stats), sh)
+        if st not in (0, 4):
+            check(st)
+
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize(dev)
+    cells = (grid.dims[0] - 1) * (grid.dims[1] - 1) * (grid.dims[2] - 1)
+    samples = grid.dims[0] * grid.dims[1] * grid.dims[2]
+
+    per_step, kernel_ms, launches = [], {k: [] for k in ("refine", "count", "emit", "quads", "table")}, 0
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clocks:
+        for _ in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps (outside the step's events)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step()
+            e1.record(stream)
+            e1.synchronize()
+            per_step.append(e0.elapsed_time(e1))
+            for k, f in (("refine", "ms_refine"), ("count", "ms_count"), ("emit", "ms_emit"), ("quads", "ms_quads"),
+                         ("table", "ms_table")):
+                kernel_ms[k].append(getattr(stats, f))
+            launches += int(stats.kernel_launches)
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    ms = float(np.mean(per_step))
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * cells / (ms / 1e3) / 1e6
+
+    sizes = {"samples_in": int(np.prod(dims_in)), "samples": samples, "rows": (grid.dims[1] - 1) * (grid.dims[2] - 1),
+             "active": int(stats.num_active_cells), "dmc_vertices": int(stats.num_dmc_vertices),
+             "dmc_quads": int(stats.num_dmc_quads), "table_buckets": ((3 * int(stats.num_dmc_quads) + 31) // 32) * 32}
+    kavg = {k: float(np.mean(v)) for k, v in kernel_ms.items()}
+    dominant = max(kavg, key=kavg.get)
+    peak, peak_kind = peaks()
+    ab = algorithmic_bytes(dominant, sizes)
+    achieved = ab / (kavg[dominant] / 1e3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(args.config, {}).get(dominant)
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": traffic,
+                "algorithmic_bytes": ab, "kernel_ms": {k: round(v, 4) for k, v in kavg.items()},
+                "whole_step_gbs": round(sum(algorithmic_bytes(k, sizes) for k in kavg) / (ms / 1e3) / 1e9, 1)}
+
+    e2e = None
+    if not args.no_e2e:
+        host_in = torch.from_numpy(vol).pin_memory()
+        V, F, H = int(mesh.num_vertices), int(mesh.num_faces), int(mesh.num_halfedges)
+        bufs = {"positions": torch.empty((V, 3), dtype=torch.float32).pin_memory(),
+                "normals": torch.empty((V, 3), dtype=torch.float32).pin_memory(),
+                "quads": torch.empty((F, 4), dtype=torch.int32).pin_memory(),
+                "halfedges": torch.empty((H, 4), dtype=torch.int32).pin_memory(),
+                "face_first": torch.empty(F, dtype=torch.int32).pin_memory(),
+                "face_attr": torch.empty(F, dtype=torch.int16).pin_memory(),
+                "vertex_he": torch.empty(V, dtype=torch.int32).pin_memory(),
+                "vertex_flags": torch.empty(V, dtype=torch.uint8).pin_memory()}
+        d2h = sum(b.numel() * b.element_size() for b in bufs.values())
+        e2e_ms = []
+        for i in range(args.steps + 1):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            step(host=host_in)
+            if int(mesh.num_vertices) != V or int(mesh.num_faces) != F:
+                raise RuntimeError("mesh size changed between runs")
+            check(lib.mdmc_download_mesh(ctx, *[ctypes.c_void_p(b.data_ptr()) for b in bufs.values()], sh))
+            e1.record(stream)
+            e1.synchronize()
+            if i:
+                e2e_ms.append(e0.elapsed_time(e1))
+        m = float(np.mean(e2e_ms))
+        if world > 1:
+            t = torch.tensor([m], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            m = float(t.item())
+        e2e = {"value": round(world * cells / (m / 1e3) / 1e6, 2), "unit": "Mcells/s", "ms_per_step": round(m, 4),
+               "h2d_bytes_per_step": int(host_in.numel() * 4), "d2h_bytes_per_step": int(d2h)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args.config)
+    lib.mdmc_destroy(ctx)
+    if rank == 0:
+        line = {
+            "metric": "Mcells/s (DMC + manifold repair, 512^3-cell refined grid)",
+            "value": round(value, 2), "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian blobs)",
+            "config": {"workload": args.config, "description": desc, "cells": cells,
+                       "grid_in": dims_in, "grid_processed": list(grid.dims), "iso": iso, "refinement": refine,
+                       "pad": bool(pad), "l2": "flushed between timed steps (256 MB write)",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "dmc_vertices": int(stats.num_dmc_vertices), "dmc_quads": int(stats.num_dmc_quads),
+                       "final_vertices": int(mesh.num_vertices), "final_faces": int(mesh.num_faces),
+                       "split_iterations": int(stats.split_iterations), "edges4": int(stats.num_edges4)},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_sample(config):
+    """A bounded slab of the workload for the CPU timings: the first quarter of
+    the input's z-planes (refined as in the full workload)."""
+    from manifolddmc_gb300.workloads import CONFIGS
+    desc, gen, iso, refine, pad = CONFIGS[config]
+    vol = gen()
+    nz = max(2, vol.shape[0] // 4 + 1)
+    sub = np.ascontiguousarray(vol[:nz])
+    return sub, [sub.shape[2], sub.shape[1], sub.shape[0]], iso, refine, pad
+
+
+def time_oracle(sub, dims, iso, refine, pad):
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _support import oracle_refine, oracle_run
+    o = np.zeros(3, np.float32)
+    s = np.ones(3, np.float32)
+    t0 = time.perf_counter()
+    g, d, oo, ss = oracle_refine(sub.reshape(-1), dims, o, s, refine, pad)
+    r = oracle_run(g, d, oo, ss, iso)
+    dt = time.perf_counter() - t0
+    cells = (d[0] - 1) * (d[1] - 1) * (d[2] - 1)
+    return cells, dt, r
+
+
+def cpu_baseline(config):
+    sub, dims, iso, refine, pad = cpu_sample(config)
+    cells, dt, _ = time_oracle(sub, dims, iso, refine, pad)
+    return {"value": round(cells / dt / 1e6, 3), "unit": "Mcells/s", "cores": 1, "kind": "port",
+            "sample": "CPU oracle (C++ restatement, 1 thread) on the first %d of %d input z-planes: %d cells, %.2f s"
+                      % (dims[2], dims[0], cells, dt)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    sub, dims, iso, refine, pad = cpu_sample(args.config)
+    times = []
+    cells = 0
+    for i in range(max(args.warmup, 3) + args.steps):
+        cells, dt, _ = time_oracle(sub, dims, iso, refine, pad)
+        if i >= max(args.warmup, 3):
+            times.append(dt)
+    ms = float(np.mean(times)) * 1e3
+    value = cells / (ms / 1e3) / 1e6
+    sample = ("the reference's path has no CPU implementation and does not build on this image (CUDA-only, "
+              "MSVC/OpenGL dependencies); its C++ restatement (oracle/) runs on 1 host thread over the first %d of "
+              "%d input z-planes (%d cells per step)" % (dims[2], dims[0], cells))
+    from manifolddmc_gb300.workloads import CONFIGS
+    line = {"impl": "reference", "metric": "Mcells/s (DMC + manifold repair, 512^3-cell refined grid)",
+            "value": round(value, 3), "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 2), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian blobs)",
+            "config": {"workload": args.config, "description": CONFIGS[args.config][0]},
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mcells/s", "cores": 1, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 3), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

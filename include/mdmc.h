@@ -1,0 +1,204 @@
+/*
+ * mdmc: Dual Marching Cubes with non-manifold repair on sm_103a (GB300).
+ *
+ * C ABI of the drop-in boundary for the reference's DMC entry point,
+ * PhiliGuertler/ManifoldDMC MarchingCubes/VisualDMC/src/DMC/DualMarchingCubes.h
+ * (class DMC::DualMarchingCubes).  Plain pointers and sizes only.  Streams are
+ * passed as `void*` holding a cudaStream_t (NULL = the legacy default stream).
+ *
+ * Citations use the reference's paths relative to
+ * MarchingCubes/VisualDMC/src/DMC/.
+ *
+ * Ownership: every device pointer returned in an mdmc_mesh belongs to the
+ * context and stays valid until the next mdmc_run / mdmc_prepare_grid on that
+ * context or mdmc_destroy (the reference's algorithm object likewise owns its
+ * halfedge mesh until the next run, DualMarchingCubes.h:170-178).
+ * A context is used by one host thread at a time.
+ */
+#ifndef MDMC_H_
+#define MDMC_H_
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define MDMC_API __attribute__((visibility("default")))
+#else
+#define MDMC_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mdmc_context mdmc_context;
+
+typedef enum mdmc_status {
+    MDMC_OK = 0,
+    MDMC_ERROR_INVALID_ARGUMENT = 1,
+    MDMC_ERROR_CUDA = 2,
+    MDMC_ERROR_OUT_OF_MEMORY = 3,
+    /* a device-side limit was hit (hash probe limit, partner list overflow,
+     * iteration cap); the mesh is still written, see mdmc_last_error */
+    MDMC_ERROR_LIMIT = 4,
+    MDMC_ERROR_IO = 5,
+    MDMC_ERROR_NO_DEVICE = 6
+} mdmc_status;
+
+/* SplittingStep, PostProcesses/ManifoldSplitter.h:155-166 */
+enum {
+    MDMC_STEP_NONE = 0,
+    MDMC_STEP_SUBDIVIDE_QUADS = 1,
+    MDMC_STEP_COLLAPSE_NON_MANIFOLD_EDGES = 2,
+    MDMC_STEP_MERGE_VERTICES = 3,
+    MDMC_STEP_UPDATE_HALFEDGE_TWINS = 4,
+    MDMC_STEP_MOVE_VERTICES_TO_SURFACE = 5,
+    MDMC_STEP_ENABLE_ITERATIVE_REFINEMENT = 6,
+    MDMC_STEP_ALL = 100
+};
+
+/* Vertex flag bits, Halfedges/Halfedge.h:14-111 */
+enum {
+    MDMC_VERTEX_NON_MANIFOLD = 1,   /* origin of a 4-face edge's halfedge */
+    MDMC_VERTEX_BOUNDARY = 2,       /* origin of a 1-face edge's halfedge */
+    MDMC_VERTEX_WEIRD = 4,          /* origin of a 3-face edge's halfedge */
+    MDMC_VERTEX_MULTIPLE_FANS = 8   /* non-manifold vertex (more than one face fan) */
+};
+
+/* Face attribute bits, DeviceVectors.h:334-450 (QuadrilateralAttribute) */
+enum {
+    MDMC_FACE_COLOR_MASK = 0x1F,
+    MDMC_FACE_NON_MANIFOLD = 0x20,
+    MDMC_FACE_PATTERN = 0x40,
+    MDMC_FACE_REMOVE = 0x80,
+    MDMC_FACE_BOUNDARY = 0x100
+};
+
+/* Algorithm flags of DualMarchingCubes (DualMarchingCubes.h:167-185, defaults
+ * DualMarchingCubes.cu:110-133) and setSplittingStep (:143-145). */
+typedef struct mdmc_options {
+    int enable_surface_to_vertex_iteration; /* m_enableSurfaceToVertexIteration, default 1 */
+    int simplify_p3x3y_color;                /* m_simplifyP3x3yColor, default 0 */
+    int simplify_p3x3y_old;                  /* m_simplifyP3x3yOld, default 0 */
+    int simplify_p3333;                      /* m_simplifyP3333, default 0 */
+    int split_non_manifold_halfedges;        /* m_splitNonManifoldHalfedges, default 1 */
+    int detect_non_manifold_vertices;        /* m_detectNonManifoldVertices, default 1 */
+    int splitting_step;                      /* SplittingStep, default MDMC_STEP_ALL */
+} mdmc_options;
+
+/* A uniform grid on the device (UniformGrid<float>, UniformGrid.h:44-262):
+ * samples x fastest, sample (x,y,z) at origin + (x,y,z) * spacing. */
+typedef struct mdmc_grid {
+    const float* samples;
+    int32_t dims[3];
+    float origin[3];
+    float spacing[3];
+} mdmc_grid;
+
+/* The halfedge mesh after post-processing (HalfedgeMesh, Halfedges/HalfedgeMesh.h)
+ * as device arrays owned by the context. */
+typedef struct mdmc_mesh {
+    int64_t num_vertices;   /* vertices, unreferenced ones included */
+    int64_t num_faces;
+    int64_t num_halfedges;
+    float* positions;       /* 3 per vertex */
+    float* normals;         /* 3 per vertex */
+    int32_t* quads;         /* 4 vertex ids per face, walking next from the first halfedge */
+    int32_t* halfedges;     /* 4 per halfedge: origin vertex, face, next, twin (-1 = none) */
+    int32_t* face_first_halfedge;
+    uint16_t* face_attributes;
+    int32_t* vertex_halfedge; /* smallest halfedge leaving the vertex, -1 if none */
+    uint8_t* vertex_flags;
+} mdmc_mesh;
+
+/* Counters of DualMarchingCubes (DualMarchingCubes.h:87-118) plus timings. */
+typedef struct mdmc_stats {
+    int64_t num_dmc_vertices;      /* getNumVertices: DMC vertices before repair */
+    int64_t num_dmc_quads;         /* getNumQuads */
+    int64_t num_active_cells;
+    int64_t num_edges;             /* getNumEdges */
+    int64_t num_edges3;            /* getNumNonManifoldEdges3 */
+    int64_t num_edges4;            /* getNumNonManifoldEdges4 */
+    int64_t num_non_manifold_vertices; /* getNumNonManifoldVertices, -1 when detection is off */
+    int64_t quads_with_non_manifold_edges[4]; /* getNumQuadsWithNonManifoldEdges(1..4) */
+    int64_t split_iterations;
+    int64_t anomalies;             /* device-side limit hits, 0 on well-formed input */
+    float ms_dmc;                  /* GPU time per stage (CUDA events) */
+    float ms_halfedge;
+    float ms_repair;
+    float ms_detect;
+    float ms_total;
+    /* per-kernel GPU times of the last run (CUDA events on the run's stream) */
+    float ms_refine;               /* grid refinement of the last mdmc_prepare_grid */
+    float ms_count;                /* per-row counting pass over the grid */
+    float ms_emit;                 /* vertex / active-cell emission pass */
+    float ms_quads;                /* quads, halfedges and edge-table inserts */
+    float ms_table;                /* edge-table twins and flags */
+    int64_t kernel_launches;       /* kernels launched by the last run and prepare */
+} mdmc_stats;
+
+MDMC_API void mdmc_default_options(mdmc_options* options);
+
+/* DualMarchingCubes::DualMarchingCubes, DualMarchingCubes.cu:110-133
+ * (+ MarchingCubes::MarchingCubes table upload, :91-98).  options may be NULL. */
+MDMC_API mdmc_status mdmc_create(mdmc_context** context, const mdmc_options* options);
+/* DualMarchingCubes::~DualMarchingCubes, DualMarchingCubes.cu:135-140 */
+MDMC_API void mdmc_destroy(mdmc_context* context);
+/* the flag setters of DualMarchingCubes (renderImGui, DualMarchingCubes.cu:150-182;
+ * setSplittingStep, DualMarchingCubes.h:143-145) */
+MDMC_API mdmc_status mdmc_set_options(mdmc_context* context, const mdmc_options* options);
+MDMC_API mdmc_status mdmc_get_options(const mdmc_context* context, mdmc_options* options);
+
+/* Reads a .bin volume (int32 dims[3], float32 spacing[3], uint16 samples)
+ * into host memory as float; origin = -(dims-1)/2 * spacing.  With
+ * host_samples == NULL only the header is read.
+ * UniformGridHost::readFromFile<unsigned short>, UniformGrid.inl:512-571 */
+MDMC_API mdmc_status mdmc_read_bin(const char* path, int32_t dims[3], float spacing[3], float origin[3],
+                          float* host_samples);
+
+/* Trilinear refinement by (refinement+1) and/or one layer of replicated
+ * boundary samples ("zero boundary"), into a context-owned device grid.
+ * samples may be a device pointer (samples_on_host = 0) or host memory, which
+ * is then copied in on the stream.  UniformGridHost::readFromFile(file,
+ * refinement, addZeroBoundary), UniformGrid.inl:575-608, kernel refineGrid :279-319 */
+MDMC_API mdmc_status mdmc_prepare_grid(mdmc_context* context, const float* samples, int samples_on_host,
+                              const int32_t dims[3], const float origin[3], const float spacing[3],
+                              int32_t refinement, int32_t add_zero_boundary, mdmc_grid* out_grid,
+                              void* stream);
+
+/* DualMarchingCubes::run, DualMarchingCubes.cu:220-289: DMC, halfedge mesh,
+ * twin repair, non-manifold split and non-manifold vertex detection as the
+ * options say.  mesh and stats may be NULL.  The call returns when the mesh
+ * is complete on the stream (it synchronizes on host-side counts). */
+MDMC_API mdmc_status mdmc_run(mdmc_context* context, const mdmc_grid* grid, float iso_value, mdmc_mesh* mesh,
+                     mdmc_stats* stats, void* stream);
+
+/* The last run's mesh and counters (DualMarchingCubes::getHalfedgeMesh,
+ * getVertices and the statistics getters, DualMarchingCubes.h:87-141). */
+MDMC_API mdmc_status mdmc_get_mesh(const mdmc_context* context, mdmc_mesh* mesh);
+MDMC_API mdmc_status mdmc_get_stats(const mdmc_context* context, mdmc_stats* stats);
+
+/* Copies the last run's mesh to host memory; any pointer may be NULL.  Sizes
+ * follow mdmc_mesh.  Synchronous with respect to the stream. */
+MDMC_API mdmc_status mdmc_download_mesh(mdmc_context* context, float* positions, float* normals, int32_t* quads,
+                               int32_t* halfedges, int32_t* face_first_halfedge,
+                               uint16_t* face_attributes, int32_t* vertex_halfedge,
+                               uint8_t* vertex_flags, void* stream);
+
+/* Writes the last run's mesh as OBJ the way Mesh::writeToFile does
+ * (Mesh.cu:446-510): v, vn, then one "f a//a b//b c//c d//d" line per face. */
+MDMC_API mdmc_status mdmc_write_obj(mdmc_context* context, const char* path);
+
+/* Human-readable description of the context's last error ("" if none). */
+MDMC_API const char* mdmc_last_error(const mdmc_context* context);
+
+/* Build-time tables, for tests: the packed contour word of every Marching
+ * Cubes case and whether the case takes the asymptotic-decider path.  No
+ * reference counterpart (the reference keeps them in s_polygonPatterns and
+ * s_triangleAmbiguities, DualMarchingCubes.cpp:301,564). */
+MDMC_API void mdmc_case_tables(uint64_t contour_words[256], uint8_t ambiguous[256]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MDMC_H_ */

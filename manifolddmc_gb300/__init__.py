@@ -1,0 +1,331 @@
+"""manifolddmc_gb300: Dual Marching Cubes with non-manifold repair on GB300.
+
+Python mirror of the reference's DMC interface (PhiliGuertler/ManifoldDMC,
+MarchingCubes/VisualDMC/src/DMC/DualMarchingCubes.h, UniformGrid.h) over the
+C ABI of the in-tree CUDA library (include/mdmc.h).  Names follow the
+reference in snake_case: ``DualMarchingCubes.run(iso_value, grid)``,
+``get_num_non_manifold_edges4()``, ``set_splitting_step(...)``,
+``UniformGrid.read_from_file(path, refinement, add_zero_boundary)``.
+
+The compute path is the CUDA library only; when it cannot be loaded every
+entry point raises ``RuntimeError`` (there is no CPU fallback).
+"""
+import ctypes
+import threading
+from pathlib import Path
+
+import numpy as np
+
+from .build import LIB as _LIB_PATH
+from .build import build
+
+__all__ = ["DualMarchingCubes", "UniformGrid", "HalfedgeMesh", "SplittingStep", "Options", "Stats",
+           "library", "build", "MDMCError"]
+
+# SplittingStep, PostProcesses/ManifoldSplitter.h:155-166
+class SplittingStep:
+    NONE = 0
+    SUBDIVIDE_QUADS = 1
+    COLLAPSE_NON_MANIFOLD_EDGES = 2
+    MERGE_VERTICES = 3
+    UPDATE_HALFEDGE_TWINS = 4
+    MOVE_VERTICES_TO_SURFACE = 5
+    ENABLE_ITERATIVE_REFINEMENT = 6
+    ALL = 100
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("enable_surface_to_vertex_iteration", ctypes.c_int),
+                ("simplify_p3x3y_color", ctypes.c_int),
+                ("simplify_p3x3y_old", ctypes.c_int),
+                ("simplify_p3333", ctypes.c_int),
+                ("split_non_manifold_halfedges", ctypes.c_int),
+                ("detect_non_manifold_vertices", ctypes.c_int),
+                ("splitting_step", ctypes.c_int)]
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("samples", ctypes.c_void_p),
+                ("dims", ctypes.c_int32 * 3),
+                ("origin", ctypes.c_float * 3),
+                ("spacing", ctypes.c_float * 3)]
+
+
+class Mesh(ctypes.Structure):
+    _fields_ = [("num_vertices", ctypes.c_int64), ("num_faces", ctypes.c_int64),
+                ("num_halfedges", ctypes.c_int64),
+                ("positions", ctypes.c_void_p), ("normals", ctypes.c_void_p), ("quads", ctypes.c_void_p),
+                ("halfedges", ctypes.c_void_p), ("face_first_halfedge", ctypes.c_void_p),
+                ("face_attributes", ctypes.c_void_p), ("vertex_halfedge", ctypes.c_void_p),
+                ("vertex_flags", ctypes.c_void_p)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("num_dmc_vertices", ctypes.c_int64), ("num_dmc_quads", ctypes.c_int64),
+                ("num_active_cells", ctypes.c_int64), ("num_edges", ctypes.c_int64),
+                ("num_edges3", ctypes.c_int64), ("num_edges4", ctypes.c_int64),
+                ("num_non_manifold_vertices", ctypes.c_int64),
+                ("quads_with_non_manifold_edges", ctypes.c_int64 * 4),
+                ("split_iterations", ctypes.c_int64), ("anomalies", ctypes.c_int64),
+                ("ms_dmc", ctypes.c_float), ("ms_halfedge", ctypes.c_float), ("ms_repair", ctypes.c_float),
+                ("ms_detect", ctypes.c_float), ("ms_total", ctypes.c_float),
+                ("ms_refine", ctypes.c_float), ("ms_count", ctypes.c_float), ("ms_emit", ctypes.c_float),
+                ("ms_quads", ctypes.c_float), ("ms_table", ctypes.c_float), ("kernel_launches", ctypes.c_int64)]
+
+    def as_dict(self):
+        d = {k: getattr(self, k) for k, _ in self._fields_ if k != "quads_with_non_manifold_edges"}
+        d["quads_with_non_manifold_edges"] = list(self.quads_with_non_manifold_edges)
+        return d
+
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "cuda error", 3: "out of memory", 4: "device limit hit",
+          5: "io error", 6: "no cuda device"}
+
+
+class MDMCError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s (%d): %s" % (STATUS.get(status, "error"), status, message))
+        self.status = status
+
+
+_lock = threading.Lock()
+_lib = None
+P = ctypes.c_void_p
+
+
+def library():
+    """Loads libmdmc.so (building it when missing).  Raises when it cannot."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not _LIB_PATH.exists():
+            build()
+        if not _LIB_PATH.exists():
+            raise RuntimeError("libmdmc.so is missing; run manifolddmc_gb300.build.build()")
+        lib = ctypes.CDLL(str(_LIB_PATH))
+        sig = {
+            "mdmc_default_options": (None, [P]),
+            "mdmc_create": (ctypes.c_int, [P, P]),
+            "mdmc_destroy": (None, [P]),
+            "mdmc_set_options": (ctypes.c_int, [P, P]),
+            "mdmc_get_options": (ctypes.c_int, [P, P]),
+            "mdmc_read_bin": (ctypes.c_int, [ctypes.c_char_p, P, P, P, P]),
+            "mdmc_prepare_grid": (ctypes.c_int, [P, P, ctypes.c_int, P, P, P, ctypes.c_int32, ctypes.c_int32, P, P]),
+            "mdmc_run": (ctypes.c_int, [P, P, ctypes.c_float, P, P, P]),
+            "mdmc_get_mesh": (ctypes.c_int, [P, P]),
+            "mdmc_get_stats": (ctypes.c_int, [P, P]),
+            "mdmc_download_mesh": (ctypes.c_int, [P] * 10),
+            "mdmc_write_obj": (ctypes.c_int, [P, ctypes.c_char_p]),
+            "mdmc_last_error": (ctypes.c_char_p, [P]),
+            "mdmc_case_tables": (None, [P, P]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(P) if a is not None else None
+
+
+def _stream_handle(stream):
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return int(getattr(stream, "cuda_stream", stream))
+
+
+class _Context:
+    def __init__(self, options=None):
+        self.lib = library()
+        self.handle = P()
+        st = self.lib.mdmc_create(ctypes.byref(self.handle), ctypes.byref(options) if options is not None else None)
+        if st != 0:
+            raise MDMCError(st, "mdmc_create failed")
+
+    def check(self, st):
+        if st != 0:
+            raise MDMCError(st, self.lib.mdmc_last_error(self.handle).decode())
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            self.lib.mdmc_destroy(h)
+            self.handle = None
+
+
+def read_bin(path):
+    """UniformGridHost::readFromFile<unsigned short> (UniformGrid.inl:512-571) on the host.
+    Returns (samples float32 [z,y,x], dims, spacing, origin)."""
+    lib = library()
+    dims = np.zeros(3, np.int32)
+    sp = np.zeros(3, np.float32)
+    org = np.zeros(3, np.float32)
+    st = lib.mdmc_read_bin(str(path).encode(), _ptr(dims), _ptr(sp), _ptr(org), None)
+    if st != 0:
+        raise MDMCError(st, "cannot read %s" % path)
+    out = np.empty(int(np.prod(dims)), np.float32)
+    lib.mdmc_read_bin(str(path).encode(), _ptr(dims), _ptr(sp), _ptr(org), _ptr(out))
+    return out.reshape(dims[2], dims[1], dims[0]), [int(d) for d in dims], sp, org
+
+
+class UniformGrid:
+    """A uniform float grid on the device (UniformGridHost<float>, UniformGrid.h:264-430).
+
+    ``samples`` may be a numpy array (host, copied in) or a CUDA torch tensor
+    / integer device pointer (used in place when no refinement or padding is
+    asked for)."""
+
+    def __init__(self, samples, dims=None, origin=(0.0, 0.0, 0.0), spacing=(1.0, 1.0, 1.0), refinement=0,
+                 add_zero_boundary=False, stream=None):
+        self._ctx = _Context()
+        self._keep = samples
+        if isinstance(samples, np.ndarray):
+            arr = np.ascontiguousarray(samples, np.float32)
+            if dims is None:
+                dims = [arr.shape[2], arr.shape[1], arr.shape[0]]
+            self._keep = arr
+            ptr, on_host = arr.ctypes.data, 1
+        elif hasattr(samples, "data_ptr"):
+            if dims is None:
+                dims = [samples.shape[2], samples.shape[1], samples.shape[0]]
+            ptr, on_host = samples.data_ptr(), 0
+        else:
+            ptr, on_host = int(samples), 0
+        d = np.asarray(dims, np.int32)
+        o = np.asarray(origin, np.float32)
+        s = np.asarray(spacing, np.float32)
+        self.grid = Grid()
+        self._ctx.check(self._ctx.lib.mdmc_prepare_grid(self._ctx.handle, P(ptr), on_host, _ptr(d), _ptr(o), _ptr(s),
+                                                        int(refinement), int(bool(add_zero_boundary)),
+                                                        ctypes.byref(self.grid), _stream_handle(stream)))
+
+    @classmethod
+    def read_from_file(cls, path, refinement=0, add_zero_boundary=False):
+        """UniformGridHost::readFromFile(file, refinement, addZeroBoundary), UniformGrid.inl:575-608"""
+        samples, dims, sp, org = read_bin(path)
+        return cls(samples, dims, org, sp, refinement, add_zero_boundary)
+
+    @property
+    def dimensions(self):
+        return [int(x) for x in self.grid.dims]
+
+    @property
+    def origin(self):
+        return np.array(list(self.grid.origin), np.float32)
+
+    @property
+    def deltas(self):
+        return np.array(list(self.grid.spacing), np.float32)
+
+    def get_cell_count(self):
+        d = self.dimensions
+        return d[0] * d[1] * d[2]
+
+
+class HalfedgeMesh:
+    """Host copy of the halfedge mesh (HalfedgeMesh, Halfedges/HalfedgeMesh.h)."""
+
+    def __init__(self, positions, normals, quads, halfedges, face_first_halfedge, face_attributes, vertex_halfedge,
+                 vertex_flags):
+        self.positions = positions
+        self.normals = normals
+        self.quads = quads
+        self.halfedges = halfedges
+        self.face_first_halfedge = face_first_halfedge
+        self.face_attributes = face_attributes
+        self.vertex_halfedge = vertex_halfedge
+        self.vertex_flags = vertex_flags
+
+
+class DualMarchingCubes:
+    """DMC::DualMarchingCubes (DualMarchingCubes.h:68-186) on the GPU."""
+
+    def __init__(self, **flags):
+        lib = library()
+        self.options = Options()
+        lib.mdmc_default_options(ctypes.byref(self.options))
+        for k, v in flags.items():
+            setattr(self.options, k, int(v))
+        self._ctx = _Context(self.options)
+        self.stats = Stats()
+        self.mesh = Mesh()
+
+    # flags (DualMarchingCubes.h:167-185, defaults DualMarchingCubes.cu:110-133)
+    def _set(self, name, value):
+        setattr(self.options, name, int(value))
+        self._ctx.check(self._ctx.lib.mdmc_set_options(self._ctx.handle, ctypes.byref(self.options)))
+
+    def set_splitting_step(self, step):
+        """DualMarchingCubes::setSplittingStep, DualMarchingCubes.h:143-145"""
+        self._set("splitting_step", step)
+
+    def set_option(self, name, value):
+        self._set(name, value)
+
+    def run(self, iso_value, grid, stream=None):
+        """DualMarchingCubes::run, DualMarchingCubes.cu:220-289.  Returns the
+        per-stage GPU times in milliseconds (the reference returns its
+        Performance tree)."""
+        g = grid.grid if isinstance(grid, UniformGrid) else grid
+        self._ctx.check(self._ctx.lib.mdmc_run(self._ctx.handle, ctypes.byref(g), ctypes.c_float(iso_value),
+                                               ctypes.byref(self.mesh), ctypes.byref(self.stats),
+                                               _stream_handle(stream)))
+        s = self.stats
+        return {"DMC": s.ms_dmc, "HalfedgeMesh": s.ms_halfedge, "Repair": s.ms_repair,
+                "DetectNonManifoldVertices": s.ms_detect, "Total": s.ms_total}
+
+    # statistics getters (DualMarchingCubes.h:87-118)
+    def get_num_vertices(self):
+        return int(self.stats.num_dmc_vertices)
+
+    def get_num_quads(self):
+        return int(self.stats.num_dmc_quads)
+
+    def get_num_non_manifold_edges4(self):
+        return int(self.stats.num_edges4)
+
+    def get_num_non_manifold_edges3(self):
+        return int(self.stats.num_edges3)
+
+    def get_num_edges(self):
+        return int(self.stats.num_edges)
+
+    def get_num_non_manifold_vertices(self):
+        return int(self.stats.num_non_manifold_vertices)
+
+    def get_num_quads_with_non_manifold_edges(self, k):
+        if not 1 <= k <= 4:
+            return 0
+        return int(self.stats.quads_with_non_manifold_edges[k - 1])
+
+    def get_halfedge_mesh(self):
+        """The last run's mesh copied to host numpy arrays."""
+        m = self.mesh
+        V, F, H = int(m.num_vertices), int(m.num_faces), int(m.num_halfedges)
+        out = HalfedgeMesh(np.empty((V, 3), np.float32), np.empty((V, 3), np.float32), np.empty((F, 4), np.int32),
+                           np.empty((H, 4), np.int32), np.empty(F, np.int32), np.empty(F, np.uint16),
+                           np.empty(V, np.int32), np.empty(V, np.uint8))
+        self._ctx.check(self._ctx.lib.mdmc_download_mesh(
+            self._ctx.handle, _ptr(out.positions), _ptr(out.normals), _ptr(out.quads), _ptr(out.halfedges),
+            _ptr(out.face_first_halfedge), _ptr(out.face_attributes), _ptr(out.vertex_halfedge),
+            _ptr(out.vertex_flags), None))
+        return out
+
+    def write_obj(self, path):
+        """Mesh::writeToFile, Mesh.cu:446-510"""
+        self._ctx.check(self._ctx.lib.mdmc_write_obj(self._ctx.handle, str(path).encode()))
+
+
+def case_tables():
+    """(contour words [256] uint64, ambiguous [256] uint8) as built into the library."""
+    lib = library()
+    w = np.zeros(256, np.uint64)
+    a = np.zeros(256, np.uint8)
+    lib.mdmc_case_tables(_ptr(w), _ptr(a))
+    return w, a

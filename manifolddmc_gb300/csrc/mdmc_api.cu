@@ -1,0 +1,695 @@
+// C ABI of the library and the host-side orchestration of one run.
+//
+// Reference: DualMarchingCubes::run and runPostProcesses
+// (D/DualMarchingCubes.cu:220-380), ManifoldSplitter::run
+// (D/PostProcesses/ManifoldSplitter.cu:96-208), UniformGridHost::readFromFile
+// (D/UniformGrid.inl:512-608), Mesh::writeToFile (D/Mesh.cu:446-510).
+//
+// Buffers are grow-only and owned by the context, so repeated runs on one
+// context allocate nothing once the sizes have been seen.  A run reads back
+// the row-count totals once (to size its outputs), one count per splitter
+// iteration (as the reference's count_if loop does) and the counters at the
+// end.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mdmc.h"
+#include "mdmc_kernels.h"
+#include "mdmc_scan.cuh"
+
+namespace mdmc {
+
+std::atomic<long long> g_kernelLaunches{0};
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    ~DevBuf() {
+        if (p) cudaFree(p);
+    }
+    template <typename T>
+    T* as() const {
+        return static_cast<T*>(p);
+    }
+    // grows without keeping the contents
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        size_t nb = std::max<size_t>(need + need / 4, 256);
+        cudaError_t e = cudaMalloc(&p, nb);
+        if (e == cudaSuccess) bytes = nb;
+        return e;
+    }
+    // grows and keeps the first `keep` bytes
+    cudaError_t grow(size_t need, size_t keep, cudaStream_t s) {
+        if (need <= bytes) return cudaSuccess;
+        void* q = nullptr;
+        size_t nb = std::max<size_t>(need + need / 2, 256);
+        cudaError_t e = cudaMalloc(&q, nb);
+        if (e != cudaSuccess) return e;
+        if (p && keep) cudaMemcpyAsync(q, p, std::min(keep, bytes), cudaMemcpyDeviceToDevice, s);
+        if (p) {
+            cudaStreamSynchronize(s);
+            cudaFree(p);
+        }
+        p = q;
+        bytes = nb;
+        return cudaSuccess;
+    }
+};
+
+static inline size_t roundUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace mdmc
+
+using namespace mdmc;
+
+struct mdmc_context {
+    mdmc_options opt;
+    std::string err;
+    // grid preparation
+    DevBuf gridBuf, stageBuf;
+    // DMC stage
+    DevBuf rows, scanScratch, act;
+    // mesh
+    DevBuf pos, nrm, he, faceFirst, faceAttr, vflags, vertexHE, quads;
+    int64_t V = 0, F = 0, H = 0;
+    // edge table
+    DevBuf table, nmList;
+    unsigned long long cap = 0;
+    // counters
+    DevBuf counters;
+    DevCounters* hostCounters = nullptr;  // pinned
+    int32_t* hostInts = nullptr;          // pinned scratch for small reads
+    // splitter
+    DevBuf nmFlags, nmOffsets, nmFaces;
+    DevBuf wPos, wNrm, wVfl, wHfl, wFfl, wVC2O, wHC2O, wFC2O, wOrigV, wOrigH, wHe, wFirst, wAttr, wVNum, wVSlots,
+        wHNum, wHSlots;
+    DevBuf vO2C, hO2C, fO2C;
+    size_t vO2CCount = 0, hO2CCount = 0, fO2CCount = 0;
+    DevBuf appV, appH, appF;
+    // fan detection
+    DevBuf isKey, fans;
+    // events: start, dmc, halfedge, repair, detect, end
+    cudaEvent_t ev[6] = {};
+    // per-kernel events: refine begin/end, count, emit, quads, table (begin/end each)
+    cudaEvent_t kev[10] = {};
+    float msRefine = 0.f;
+    long long prepareLaunches = 0;
+    bool haveMesh = false;
+    mdmc_stats stats;
+};
+
+namespace {
+
+mdmc_status fail(mdmc_context* c, mdmc_status st, const std::string& msg) {
+    if (c) c->err = msg;
+    return st;
+}
+
+mdmc_status cudaFail(mdmc_context* c, cudaError_t e, const char* where) {
+    std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+    return fail(c, e == cudaErrorMemoryAllocation ? MDMC_ERROR_OUT_OF_MEMORY : MDMC_ERROR_CUDA, m);
+}
+
+#define MDMC_CHECK(ctx, expr)                              \
+    do {                                                   \
+        cudaError_t e_ = (expr);                           \
+        if (e_ != cudaSuccess) return cudaFail(ctx, e_, #expr); \
+    } while (0)
+
+void defaultOptions(mdmc_options* o) {
+    o->enable_surface_to_vertex_iteration = 1;
+    o->simplify_p3x3y_color = 0;
+    o->simplify_p3x3y_old = 0;
+    o->simplify_p3333 = 0;
+    o->split_non_manifold_halfedges = 1;
+    o->detect_non_manifold_vertices = 1;
+    o->splitting_step = MDMC_STEP_ALL;
+}
+
+std::string statusText(uint32_t s) {
+    std::string t;
+    auto add = [&](uint32_t bit, const char* name) {
+        if (s & bit) t += std::string(t.empty() ? "" : ", ") + name;
+    };
+    add(kStatusProbeLimit, "edge table probe limit");
+    add(kStatusSlotConflict, "quad slot conflict");
+    add(kStatusBucketOverflow, "more than four faces on an edge");
+    add(kStatusPartnerOverflow, "merge partner overflow");
+    add(kStatusWalkLimit, "face-fan walk limit");
+    add(kStatusBadTwin, "non-manifold twin outside the working copy");
+    add(kStatusIterationCap, "splitter iteration cap");
+    add(kStatusWallOutOfGrid, "cell wall outside the grid");
+    add(kStatusMissingCell, "quad neighbour cell missing");
+    add(kStatusMappingSwap, "unexpected working-copy mapping");
+    return t;
+}
+
+template <typename T>
+mdmc_status scan(mdmc_context* c, const T* in, T* out, int64_t n, cudaStream_t s) {
+    MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(n)));
+    if (!exclusiveScan<T>(in, out, n, c->scanScratch.as<T>(), s))
+        return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
+    return MDMC_OK;
+}
+
+// reads n int32 values from device memory (synchronizes the stream)
+mdmc_status readInts(mdmc_context* c, const void* src, int n, cudaStream_t s) {
+    MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, src, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+    MDMC_CHECK(c, cudaStreamSynchronize(s));
+    return MDMC_OK;
+}
+
+unsigned long long tableCapacity(int64_t faces) { return (unsigned long long)roundUp((size_t)std::max<int64_t>(3 * faces, 64), 32); }
+
+SplitWork splitWork(mdmc_context* c) {
+    SplitWork w;
+    w.pos = c->wPos.as<float>();
+    w.nrm = c->wNrm.as<float>();
+    w.vfl = c->wVfl.as<uint32_t>();
+    w.hfl = c->wHfl.as<uint32_t>();
+    w.ffl = c->wFfl.as<uint32_t>();
+    w.vC2O = c->wVC2O.as<int>();
+    w.hC2O = c->wHC2O.as<int>();
+    w.fC2O = c->wFC2O.as<int>();
+    w.vO2C = c->vO2C.as<int>();
+    w.hO2C = c->hO2C.as<int>();
+    w.fO2C = c->fO2C.as<int>();
+    w.origV = c->wOrigV.as<int>();
+    w.origH = c->wOrigH.as<int>();
+    w.he = c->wHe.as<int4>();
+    w.first = c->wFirst.as<int>();
+    w.attr = c->wAttr.as<uint16_t>();
+    w.vNum = c->wVNum.as<int>();
+    w.vSlots = c->wVSlots.as<int>();
+    w.hNum = c->wHNum.as<int>();
+    w.hSlots = c->wHSlots.as<int>();
+    return w;
+}
+
+// dense original->copy maps: sized to the mesh, all "none" between iterations
+mdmc_status ensureMaps(mdmc_context* c, cudaStream_t s) {
+    if ((size_t)c->V > c->vO2CCount) {
+        size_t n = (size_t)c->V * 2;
+        MDMC_CHECK(c, c->vO2C.ensure(sizeof(int) * n));
+        launchFillInt(c->vO2C.as<int>(), (int64_t)(c->vO2C.bytes / sizeof(int)), 0x7FFFFFFF, s);
+        c->vO2CCount = c->vO2C.bytes / sizeof(int);
+    }
+    if ((size_t)c->H > c->hO2CCount) {
+        size_t n = (size_t)c->H * 2;
+        MDMC_CHECK(c, c->hO2C.ensure(sizeof(int) * n));
+        MDMC_CHECK(c, cudaMemsetAsync(c->hO2C.p, 0xFF, c->hO2C.bytes, s));
+        c->hO2CCount = c->hO2C.bytes / sizeof(int);
+    }
+    if ((size_t)c->F > c->fO2CCount) {
+        size_t n = (size_t)c->F * 2;
+        MDMC_CHECK(c, c->fO2C.ensure(sizeof(int) * n));
+        MDMC_CHECK(c, cudaMemsetAsync(c->fO2C.p, 0xFF, c->fO2C.bytes, s));
+        c->fO2CCount = c->fO2C.bytes / sizeof(int);
+    }
+    return MDMC_OK;
+}
+
+// rebuilds the edge table from all faces and refreshes the flags
+// (HalfedgeMesh::refreshHashTable, D/Halfedges/HalfedgeMesh.cu:1063-1100)
+mdmc_status refreshTable(mdmc_context* c, uint32_t* status, cudaStream_t s) {
+    c->cap = tableCapacity(c->F);
+    MDMC_CHECK(c, c->table.ensure(sizeof(Bucket) * c->cap));
+    MDMC_CHECK(c, cudaMemsetAsync(c->table.p, 0xFF, sizeof(Bucket) * c->cap, s));
+    MDMC_CHECK(c, c->nmList.ensure(sizeof(int) * (size_t)(c->H / 4 + 1)));
+    launchInsertFaces(c->he.as<int4>(), c->faceFirst.as<int>(), (int)c->F, c->table.as<Bucket>(), c->cap, status, s);
+    launchResetFaceFlags(c->faceAttr.as<uint16_t>(), (int)c->F, s);
+    MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, (size_t)c->V, s));
+    MDMC_CHECK(c, cudaMemsetAsync((char*)c->counters.p + 8, 0, sizeof(DevCounters) - 8, s));
+    launchBuckets(c->table.as<Bucket>(), c->cap, c->he.as<int4>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(),
+                  0, c->nmList.as<int>(), c->counters.as<DevCounters>(), s);
+    return MDMC_OK;
+}
+
+// ManifoldSplitter::run, D/PostProcesses/ManifoldSplitter.cu:96-208
+mdmc_status runSplitter(mdmc_context* c, const GridView& g, float iso, int64_t& iterations, cudaStream_t s) {
+    DevCounters* ctr = c->counters.as<DevCounters>();
+    uint32_t* status = &ctr->status;
+    const int step = c->opt.splitting_step;
+    iterations = 0;
+    while (true) {
+        // countNonManifoldFaces + the list of non-manifold faces
+        MDMC_CHECK(c, c->nmFlags.ensure(sizeof(int) * (size_t)(c->F + 1)));
+        MDMC_CHECK(c, c->nmOffsets.ensure(sizeof(int) * (size_t)(c->F + 1)));
+        launchFlagNMFaces(c->faceAttr.as<uint16_t>(), (int)c->F, c->nmFlags.as<int>(), s);
+        mdmc_status st = scan<int>(c, c->nmFlags.as<int>(), c->nmOffsets.as<int>(), c->F, s);
+        if (st != MDMC_OK) return st;
+        if ((st = readInts(c, c->nmOffsets.as<int>() + c->F, 1, s)) != MDMC_OK) return st;
+        const int n = (int)c->hostInts[0];
+        if (n == 0) break;
+        MDMC_CHECK(c, c->nmFaces.ensure(sizeof(int) * (size_t)n));
+        launchCompactNMFaces(c->nmFlags.as<int>(), c->nmOffsets.as<int>(), (int)c->F, c->nmFaces.as<int>(), s);
+
+        const bool doSub = step >= MDMC_STEP_SUBDIVIDE_QUADS;
+        const int nv = 4 * n + (doSub ? 4 * n : 0);
+        const int nh = 4 * n + (doSub ? 16 * n : 0);
+        const int nf = n + (doSub ? 4 * n : 0);
+        MDMC_CHECK(c, c->wPos.ensure(sizeof(float) * 3 * (size_t)nv));
+        MDMC_CHECK(c, c->wNrm.ensure(sizeof(float) * 3 * (size_t)nv));
+        MDMC_CHECK(c, c->wVfl.ensure(sizeof(uint32_t) * (size_t)nv));
+        MDMC_CHECK(c, c->wHfl.ensure(sizeof(uint32_t) * (size_t)nh));
+        MDMC_CHECK(c, c->wFfl.ensure(sizeof(uint32_t) * (size_t)nf));
+        MDMC_CHECK(c, c->wVC2O.ensure(sizeof(int) * (size_t)nv));
+        MDMC_CHECK(c, c->wHC2O.ensure(sizeof(int) * (size_t)nh));
+        MDMC_CHECK(c, c->wFC2O.ensure(sizeof(int) * (size_t)nf));
+        MDMC_CHECK(c, c->wOrigV.ensure(sizeof(int) * 4 * (size_t)n));
+        MDMC_CHECK(c, c->wOrigH.ensure(sizeof(int) * 4 * (size_t)n));
+        MDMC_CHECK(c, c->wHe.ensure(sizeof(int4) * (size_t)nh));
+        MDMC_CHECK(c, c->wFirst.ensure(sizeof(int) * (size_t)nf));
+        MDMC_CHECK(c, c->wAttr.ensure(roundUp(sizeof(uint16_t) * (size_t)nf, 4)));
+        MDMC_CHECK(c, c->wVNum.ensure(sizeof(int) * (size_t)nv));
+        MDMC_CHECK(c, c->wVSlots.ensure(sizeof(int) * 4 * (size_t)nv));
+        MDMC_CHECK(c, c->wHNum.ensure(sizeof(int) * (size_t)nh));
+        MDMC_CHECK(c, c->wHSlots.ensure(sizeof(int) * 4 * (size_t)nh));
+        if ((st = ensureMaps(c, s)) != MDMC_OK) return st;
+        MDMC_CHECK(c, cudaMemsetAsync(c->wVfl.p, 0, sizeof(uint32_t) * (size_t)nv, s));
+        MDMC_CHECK(c, cudaMemsetAsync(c->wHfl.p, 0, sizeof(uint32_t) * (size_t)nh, s));
+        MDMC_CHECK(c, cudaMemsetAsync(c->wFfl.p, 0, sizeof(uint32_t) * (size_t)nf, s));
+        MDMC_CHECK(c, cudaMemsetAsync(c->wVC2O.p, 0xFF, sizeof(int) * (size_t)nv, s));
+        MDMC_CHECK(c, cudaMemsetAsync(c->wHC2O.p, 0xFF, sizeof(int) * (size_t)nh, s));
+        MDMC_CHECK(c, cudaMemsetAsync(c->wFC2O.p, 0xFF, sizeof(int) * (size_t)nf, s));
+        MDMC_CHECK(c, cudaMemsetAsync(c->wHe.p, 0xFF, sizeof(int4) * (size_t)nh, s));
+        MDMC_CHECK(c, cudaMemsetAsync(c->wVSlots.p, 0xFF, sizeof(int) * 4 * (size_t)nv, s));
+        MDMC_CHECK(c, cudaMemsetAsync(c->wHSlots.p, 0xFF, sizeof(int) * 4 * (size_t)nh, s));
+        launchFillInt(c->wVNum.as<int>(), nv, 1, s);
+        launchFillInt(c->wHNum.as<int>(), nh, 1, s);
+        const SplitWork w = splitWork(c);
+
+        // createWorkingCopies (:273-301)
+        launchSplitCopy(c->nmFaces.as<int>(), n, c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(),
+                        c->pos.as<float>(), c->nrm.as<float>(), w, s);
+        launchSplitMarkNM(c->table.as<Bucket>(), c->nmList.as<int>(), ctr, w, status, s);
+        if (doSub) launchSplitSubdivide(n, w, status, s);
+        if (step >= MDMC_STEP_COLLAPSE_NON_MANIFOLD_EDGES) {
+            launchSplitCollapse(nh, nv, w, status, s);
+            if (step >= MDMC_STEP_MERGE_VERTICES) launchSplitMerge(nv, nh, w, status, s);
+            if (step >= MDMC_STEP_UPDATE_HALFEDGE_TWINS) launchSplitMergeHalfedges(nh, w, status, s);
+        }
+        if (step >= MDMC_STEP_MOVE_VERTICES_TO_SURFACE) launchSplitMove(nv, g, iso, w, s);
+
+        // copyWorkingCopiesBack (:1297-1387): kept elements without an
+        // original are appended in working-copy order
+        MDMC_CHECK(c, c->appV.ensure(sizeof(int) * (size_t)(nv + 1)));
+        MDMC_CHECK(c, c->appH.ensure(sizeof(int) * (size_t)(nh + 1)));
+        MDMC_CHECK(c, c->appF.ensure(sizeof(int) * (size_t)(nf + 1)));
+        launchSplitFlagAppends(nv, w.vfl, w.vC2O, c->appV.as<int>(), s);
+        launchSplitFlagAppends(nh, w.hfl, w.hC2O, c->appH.as<int>(), s);
+        launchSplitFlagAppends(nf, w.ffl, w.fC2O, c->appF.as<int>(), s);
+        if ((st = scan<int>(c, c->appV.as<int>(), c->appV.as<int>(), nv, s)) != MDMC_OK) return st;
+        if ((st = scan<int>(c, c->appH.as<int>(), c->appH.as<int>(), nh, s)) != MDMC_OK) return st;
+        if ((st = scan<int>(c, c->appF.as<int>(), c->appF.as<int>(), nf, s)) != MDMC_OK) return st;
+        MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, c->appV.as<int>() + nv, sizeof(int), cudaMemcpyDeviceToHost, s));
+        MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts + 1, c->appH.as<int>() + nh, sizeof(int), cudaMemcpyDeviceToHost, s));
+        MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts + 2, c->appF.as<int>() + nf, sizeof(int), cudaMemcpyDeviceToHost, s));
+        MDMC_CHECK(c, cudaStreamSynchronize(s));
+        const int64_t addV = c->hostInts[0], addH = c->hostInts[1], addF = c->hostInts[2];
+        const int64_t V2 = c->V + addV, H2 = c->H + addH, F2 = c->F + addF;
+        MDMC_CHECK(c, c->pos.grow(sizeof(float) * 3 * (size_t)V2, sizeof(float) * 3 * (size_t)c->V, s));
+        MDMC_CHECK(c, c->nrm.grow(sizeof(float) * 3 * (size_t)V2, sizeof(float) * 3 * (size_t)c->V, s));
+        MDMC_CHECK(c, c->vflags.grow(roundUp((size_t)V2, 4), (size_t)c->V, s));
+        MDMC_CHECK(c, c->he.grow(sizeof(int4) * (size_t)H2, sizeof(int4) * (size_t)c->H, s));
+        MDMC_CHECK(c, c->faceFirst.grow(sizeof(int) * (size_t)F2, sizeof(int) * (size_t)c->F, s));
+        MDMC_CHECK(c, c->faceAttr.grow(roundUp(sizeof(uint16_t) * (size_t)F2, 4), sizeof(uint16_t) * (size_t)c->F, s));
+        launchSplitCopyBack(nv, nh, nf, w, c->appV.as<int>(), c->appH.as<int>(), c->appF.as<int>(), (int)c->V,
+                            (int)c->H, (int)c->F, c->pos.as<float>(), c->nrm.as<float>(), c->he.as<int4>(),
+                            c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(), s);
+        launchSplitResetMaps(n, c->nmFaces.as<int>(), w, s);
+        c->V = V2;
+        c->H = H2;
+        c->F = F2;
+        if ((st = refreshTable(c, status, s)) != MDMC_OK) return st;
+        ++iterations;
+        if (step < MDMC_STEP_ENABLE_ITERATIVE_REFINEMENT) break;
+        if (iterations >= 64) {  // the reference loops without a cap
+            uint32_t bit = kStatusIterationCap;
+            MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+            MDMC_CHECK(c, cudaStreamSynchronize(s));
+            bit |= (uint32_t)c->hostInts[0];
+            MDMC_CHECK(c, cudaMemcpyAsync(status, &bit, sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+            MDMC_CHECK(c, cudaStreamSynchronize(s));
+            break;
+        }
+    }
+    return MDMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void mdmc_default_options(mdmc_options* options) {
+    if (options) defaultOptions(options);
+}
+
+mdmc_status mdmc_create(mdmc_context** context, const mdmc_options* options) {
+    if (!context) return MDMC_ERROR_INVALID_ARGUMENT;
+    *context = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return MDMC_ERROR_NO_DEVICE;
+    mdmc_context* c = new mdmc_context();
+    if (options) c->opt = *options;
+    else defaultOptions(&c->opt);
+    std::memset(&c->stats, 0, sizeof c->stats);
+    if (cudaMallocHost(&c->hostCounters, sizeof(DevCounters)) != cudaSuccess ||
+        cudaMallocHost(&c->hostInts, 64 * sizeof(int32_t)) != cudaSuccess || c->counters.ensure(sizeof(DevCounters)) != cudaSuccess) {
+        mdmc_destroy(c);
+        return MDMC_ERROR_OUT_OF_MEMORY;
+    }
+    for (auto& e : c->ev) cudaEventCreate(&e);
+    for (auto& e : c->kev) cudaEventCreate(&e);
+    *context = c;
+    return MDMC_OK;
+}
+
+void mdmc_destroy(mdmc_context* c) {
+    if (!c) return;
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : c->kev)
+        if (e) cudaEventDestroy(e);
+    if (c->hostCounters) cudaFreeHost(c->hostCounters);
+    if (c->hostInts) cudaFreeHost(c->hostInts);
+    delete c;
+}
+
+mdmc_status mdmc_set_options(mdmc_context* c, const mdmc_options* options) {
+    if (!c || !options) return MDMC_ERROR_INVALID_ARGUMENT;
+    c->opt = *options;
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_get_options(const mdmc_context* c, mdmc_options* options) {
+    if (!c || !options) return MDMC_ERROR_INVALID_ARGUMENT;
+    *options = c->opt;
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_read_bin(const char* path, int32_t dims[3], float spacing[3], float origin[3], float* host_samples) {
+    if (!path || !dims || !spacing || !origin) return MDMC_ERROR_INVALID_ARGUMENT;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return MDMC_ERROR_IO;
+    bool ok = std::fread(dims, sizeof(int32_t), 3, f) == 3 && std::fread(spacing, sizeof(float), 3, f) == 3;
+    if (!ok || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) {
+        std::fclose(f);
+        return MDMC_ERROR_IO;
+    }
+    for (int a = 0; a < 3; ++a) origin[a] = (-0.5f * (float)(dims[a] - 1)) * spacing[a];
+    if (host_samples) {
+        const size_t n = (size_t)dims[0] * dims[1] * dims[2];
+        std::vector<uint16_t> raw(n);
+        if (std::fread(raw.data(), sizeof(uint16_t), n, f) != n) {
+            std::fclose(f);
+            return MDMC_ERROR_IO;
+        }
+        for (size_t i = 0; i < n; ++i) host_samples[i] = (float)raw[i];
+    }
+    std::fclose(f);
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_prepare_grid(mdmc_context* c, const float* samples, int samples_on_host, const int32_t dims[3],
+                              const float origin[3], const float spacing[3], int32_t refinement,
+                              int32_t add_zero_boundary, mdmc_grid* out, void* stream) {
+    if (!c || !samples || !dims || !origin || !spacing || !out) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "null argument");
+    if (refinement < 0 || dims[0] < 1 || dims[1] < 1 || dims[2] < 1)
+        return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "invalid dims or refinement");
+    cudaStream_t s = (cudaStream_t)stream;
+    const int pad = add_zero_boundary ? 1 : 0;
+    int32_t od[3];
+    float osp[3], oor[3];
+    size_t outN = 1, inN = 1;
+    for (int a = 0; a < 3; ++a) {
+        // D/UniformGrid.inl:585-598
+        const int64_t d = (int64_t)dims[a] + (int64_t)(dims[a] - 1) * refinement + 2 * pad;
+        if (d > (1 << 30)) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "refined grid too large");
+        od[a] = (int32_t)d;
+        osp[a] = (spacing[a] * 1.f) / ((float)refinement + 1.f);
+        oor[a] = origin[a];
+        if (pad) oor[a] = oor[a] - osp[a];
+        outN *= (size_t)od[a];
+        inN *= (size_t)dims[a];
+    }
+    if (outN >= 0xFFFFFFFFull) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "grid has 2^32 samples or more");
+    const float* src = samples;
+    c->prepareLaunches = 0;
+    cudaEventRecord(c->kev[0], s);
+    cudaEventRecord(c->kev[1], s);
+    if (refinement == 0 && !pad) {
+        if (samples_on_host) {
+            MDMC_CHECK(c, c->gridBuf.ensure(sizeof(float) * outN));
+            MDMC_CHECK(c, cudaMemcpyAsync(c->gridBuf.p, samples, sizeof(float) * outN, cudaMemcpyHostToDevice, s));
+            src = c->gridBuf.as<float>();
+        }
+        out->samples = src;
+    } else {
+        if (samples_on_host) {
+            MDMC_CHECK(c, c->stageBuf.ensure(sizeof(float) * inN));
+            MDMC_CHECK(c, cudaMemcpyAsync(c->stageBuf.p, samples, sizeof(float) * inN, cudaMemcpyHostToDevice, s));
+            src = c->stageBuf.as<float>();
+        }
+        MDMC_CHECK(c, c->gridBuf.ensure(sizeof(float) * outN));
+        const long long l0 = g_kernelLaunches.load();
+        cudaEventRecord(c->kev[0], s);
+        launchRefine(src, make_int3(dims[0], dims[1], dims[2]), c->gridBuf.as<float>(), make_int3(od[0], od[1], od[2]),
+                     refinement, pad, s);
+        cudaEventRecord(c->kev[1], s);
+        c->prepareLaunches = g_kernelLaunches.load() - l0;
+        MDMC_CHECK(c, cudaGetLastError());
+        out->samples = c->gridBuf.as<float>();
+    }
+    for (int a = 0; a < 3; ++a) {
+        out->dims[a] = od[a];
+        out->origin[a] = oor[a];
+        out->spacing[a] = osp[a];
+    }
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mesh* mesh, mdmc_stats* stats,
+                     void* stream) {
+    if (!c || !grid || !grid->samples) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "null argument");
+    c->err.clear();
+    const int X = grid->dims[0], Y = grid->dims[1], Z = grid->dims[2];
+    if (X < 1 || Y < 1 || Z < 1) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "invalid grid dims");
+    if ((uint64_t)X * Y * Z >= 0xFFFFFFFFull) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "grid has 2^32 samples or more");
+    cudaStream_t s = (cudaStream_t)stream;
+    c->haveMesh = false;
+    std::memset(&c->stats, 0, sizeof c->stats);
+    GridView g{grid->samples, X, Y, Z, grid->origin[0], grid->origin[1], grid->origin[2],
+               grid->spacing[0], grid->spacing[1], grid->spacing[2]};
+    DevCounters* ctr = c->counters.as<DevCounters>();
+    uint32_t* status = &ctr->status;
+    MDMC_CHECK(c, cudaMemsetAsync(ctr, 0, sizeof(DevCounters), s));
+    const long long launches0 = g_kernelLaunches.load();
+    cudaEventRecord(c->ev[0], s);
+
+    // ---- DMC: count, scan, emit (performDualMarchingCubes) --------------------
+    const int64_t numRows = (X > 1 && Y > 1 && Z > 1) ? (int64_t)(Y - 1) * (Z - 1) : 0;
+    MDMC_CHECK(c, c->rows.ensure(sizeof(int4) * (size_t)(numRows + 1)));
+    cudaEventRecord(c->kev[2], s);
+    if (numRows > 0) launchRowCount(g, iso, c->rows.as<int4>(), (int)numRows, s);
+    cudaEventRecord(c->kev[3], s);
+    mdmc_status st = scan<int4>(c, c->rows.as<int4>(), c->rows.as<int4>(), numRows, s);
+    if (st != MDMC_OK) return st;
+    if ((st = readInts(c, c->rows.as<int4>() + numRows, 4, s)) != MDMC_OK) return st;
+    const int* tot = reinterpret_cast<const int*>(c->hostInts);
+    const int64_t A = tot[0], Vd = tot[1], Q = tot[2];
+    c->stats.num_active_cells = A;
+    c->stats.num_dmc_vertices = Vd;
+    c->stats.num_dmc_quads = Q;
+    if (Vd == 0) {
+        // "DMC: No Vertices have been produced!" (D/DualMarchingCubes.cu:256-261)
+        c->V = c->F = c->H = 0;
+        c->stats.num_edges = c->stats.num_edges3 = c->stats.num_edges4 = -1;
+        c->stats.num_non_manifold_vertices = -1;
+        for (int k = 0; k < 4; ++k) c->stats.quads_with_non_manifold_edges[k] = -1;
+        c->haveMesh = true;
+        if (mesh) mdmc_get_mesh(c, mesh);
+        if (stats) *stats = c->stats;
+        return MDMC_OK;
+    }
+    if (4 * Q >= (int64_t)0x7FFFFFFF) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "more than 2^31 halfedges");
+    c->V = Vd;
+    c->F = Q;
+    c->H = 4 * Q;
+    c->cap = tableCapacity(Q);
+    MDMC_CHECK(c, c->act.ensure(sizeof(ActiveCell) * (size_t)A));
+    MDMC_CHECK(c, c->pos.ensure(sizeof(float) * 3 * (size_t)Vd));
+    MDMC_CHECK(c, c->nrm.ensure(sizeof(float) * 3 * (size_t)Vd));
+    MDMC_CHECK(c, c->vflags.ensure(roundUp((size_t)Vd, 4)));
+    MDMC_CHECK(c, c->he.ensure(sizeof(int4) * 4 * (size_t)Q));
+    MDMC_CHECK(c, c->faceFirst.ensure(sizeof(int) * (size_t)Q));
+    MDMC_CHECK(c, c->faceAttr.ensure(roundUp(sizeof(uint16_t) * (size_t)Q, 4)));
+    MDMC_CHECK(c, c->table.ensure(sizeof(Bucket) * c->cap));
+    MDMC_CHECK(c, c->nmList.ensure(sizeof(int) * (size_t)(Q + 1)));
+    MDMC_CHECK(c, cudaMemsetAsync(c->table.p, 0xFF, sizeof(Bucket) * c->cap, s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)Vd, 4), s));
+    cudaEventRecord(c->kev[4], s);
+    launchRowEmit(g, iso, c->opt.enable_surface_to_vertex_iteration, c->rows.as<int4>(), (int)numRows,
+                  c->act.as<ActiveCell>(), c->pos.as<float>(), c->nrm.as<float>(), s);
+    cudaEventRecord(c->kev[5], s);
+    // mapQuadrilaterals + collectHalfedgeElements
+    cudaEventRecord(c->kev[6], s);
+    launchQuads(c->act.as<ActiveCell>(), (int)A, c->rows.as<int4>(), X, Y, c->table.as<Bucket>(), c->cap,
+                c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(), status, s);
+    cudaEventRecord(c->kev[7], s);
+    cudaEventRecord(c->ev[1], s);
+
+    // ---- halfedge mesh: twins and flags (HalfedgeMesh::initialize) -----------
+    cudaEventRecord(c->kev[8], s);
+    launchBuckets(c->table.as<Bucket>(), c->cap, c->he.as<int4>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), 1,
+                  c->nmList.as<int>(), ctr, s);
+    cudaEventRecord(c->kev[9], s);
+    cudaEventRecord(c->ev[2], s);
+
+    // ---- repair: fixManifoldTwins, then the splitter ---------------------------
+    launchReconnect(g, iso, c->table.as<Bucket>(), c->nmList.as<int>(), ctr, c->he.as<int4>(), c->pos.as<float>(), status, s);
+    MDMC_CHECK(c, cudaGetLastError());
+    int64_t iterations = 0;
+    if (c->opt.split_non_manifold_halfedges) {
+        if ((st = runSplitter(c, g, iso, iterations, s)) != MDMC_OK) return st;
+    }
+    cudaEventRecord(c->ev[3], s);
+
+    // ---- non-manifold vertices ------------------------------------------------
+    if (c->opt.detect_non_manifold_vertices) {
+        MDMC_CHECK(c, c->isKey.ensure((size_t)c->H));
+        MDMC_CHECK(c, c->fans.ensure(sizeof(int) * (size_t)c->V));
+        MDMC_CHECK(c, cudaMemsetAsync(c->isKey.p, 0, (size_t)c->H, s));
+        MDMC_CHECK(c, cudaMemsetAsync(c->fans.p, 0, sizeof(int) * (size_t)c->V, s));
+        launchDetectFans(c->he.as<int4>(), (int)c->H, c->isKey.as<uint8_t>(), c->fans.as<int>(), c->vflags.as<uint8_t>(),
+                         (int)c->V, ctr, status, s);
+    }
+    cudaEventRecord(c->ev[4], s);
+
+    // ---- outputs and statistics -------------------------------------------------
+    MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)c->F));
+    MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)c->V));
+    launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), (int)c->F, (int)c->H, (int)c->V, c->table.as<Bucket>(),
+                 c->cap, c->quads.as<int4>(), c->vertexHE.as<int>(), ctr, s);
+    cudaEventRecord(c->ev[5], s);
+    MDMC_CHECK(c, cudaGetLastError());
+    MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
+    MDMC_CHECK(c, cudaStreamSynchronize(s));
+
+    const DevCounters& hc = *c->hostCounters;
+    c->stats.num_edges = (int64_t)hc.edges;
+    c->stats.num_edges3 = (int64_t)hc.edges3;
+    c->stats.num_edges4 = (int64_t)hc.edges4;
+    c->stats.num_non_manifold_vertices = c->opt.detect_non_manifold_vertices ? (int64_t)hc.nmVertices : -1;
+    for (int k = 0; k < 4; ++k) c->stats.quads_with_non_manifold_edges[k] = (int64_t)hc.quadsNM[k + 1];
+    c->stats.split_iterations = iterations;
+    c->stats.anomalies = (int64_t)hc.status;
+    float ms[5] = {0, 0, 0, 0, 0};
+    for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&ms[k], c->ev[k], c->ev[k + 1]);
+    cudaEventElapsedTime(&ms[4], c->ev[0], c->ev[5]);
+    c->stats.ms_dmc = ms[0];
+    c->stats.ms_halfedge = ms[1];
+    c->stats.ms_repair = ms[2];
+    c->stats.ms_detect = ms[3];
+    c->stats.ms_total = ms[4];
+    float km[5] = {0, 0, 0, 0, 0};
+    for (int k = 0; k < 5; ++k) cudaEventElapsedTime(&km[k], c->kev[2 * k], c->kev[2 * k + 1]);
+    c->stats.ms_refine = km[0];
+    c->stats.ms_count = km[1];
+    c->stats.ms_emit = km[2];
+    c->stats.ms_quads = km[3];
+    c->stats.ms_table = km[4];
+    c->stats.kernel_launches = (int64_t)(g_kernelLaunches.load() - launches0) + c->prepareLaunches;
+    c->haveMesh = true;
+    if (mesh) mdmc_get_mesh(c, mesh);
+    if (stats) *stats = c->stats;
+    if (hc.status) {
+        c->err = "device limits hit: " + statusText(hc.status);
+        if (hc.status & (kStatusProbeLimit | kStatusMissingCell)) return MDMC_ERROR_LIMIT;
+    }
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_get_mesh(const mdmc_context* c, mdmc_mesh* m) {
+    if (!c || !m) return MDMC_ERROR_INVALID_ARGUMENT;
+    std::memset(m, 0, sizeof *m);
+    if (!c->haveMesh) return MDMC_ERROR_INVALID_ARGUMENT;
+    m->num_vertices = c->V;
+    m->num_faces = c->F;
+    m->num_halfedges = c->H;
+    m->positions = c->pos.as<float>();
+    m->normals = c->nrm.as<float>();
+    m->quads = c->quads.as<int32_t>();
+    m->halfedges = c->he.as<int32_t>();
+    m->face_first_halfedge = c->faceFirst.as<int32_t>();
+    m->face_attributes = c->faceAttr.as<uint16_t>();
+    m->vertex_halfedge = c->vertexHE.as<int32_t>();
+    m->vertex_flags = c->vflags.as<uint8_t>();
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_get_stats(const mdmc_context* c, mdmc_stats* stats) {
+    if (!c || !stats) return MDMC_ERROR_INVALID_ARGUMENT;
+    *stats = c->stats;
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_download_mesh(mdmc_context* c, float* positions, float* normals, int32_t* quads, int32_t* halfedges,
+                               int32_t* face_first_halfedge, uint16_t* face_attributes, int32_t* vertex_halfedge,
+                               uint8_t* vertex_flags, void* stream) {
+    if (!c || !c->haveMesh) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "no mesh");
+    cudaStream_t s = (cudaStream_t)stream;
+    auto cp = [&](void* dst, const DevBuf& b, size_t bytes) -> cudaError_t {
+        if (!dst || bytes == 0) return cudaSuccess;
+        return cudaMemcpyAsync(dst, b.p, bytes, cudaMemcpyDeviceToHost, s);
+    };
+    MDMC_CHECK(c, cp(positions, c->pos, sizeof(float) * 3 * (size_t)c->V));
+    MDMC_CHECK(c, cp(normals, c->nrm, sizeof(float) * 3 * (size_t)c->V));
+    MDMC_CHECK(c, cp(quads, c->quads, sizeof(int4) * (size_t)c->F));
+    MDMC_CHECK(c, cp(halfedges, c->he, sizeof(int4) * (size_t)c->H));
+    MDMC_CHECK(c, cp(face_first_halfedge, c->faceFirst, sizeof(int) * (size_t)c->F));
+    MDMC_CHECK(c, cp(face_attributes, c->faceAttr, sizeof(uint16_t) * (size_t)c->F));
+    MDMC_CHECK(c, cp(vertex_halfedge, c->vertexHE, sizeof(int) * (size_t)c->V));
+    MDMC_CHECK(c, cp(vertex_flags, c->vflags, (size_t)c->V));
+    MDMC_CHECK(c, cudaStreamSynchronize(s));
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_write_obj(mdmc_context* c, const char* path) {
+    if (!c || !path || !c->haveMesh) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "no mesh or path");
+    std::vector<float> p(3 * (size_t)c->V), n(3 * (size_t)c->V);
+    std::vector<int32_t> q(4 * (size_t)c->F);
+    mdmc_status st = mdmc_download_mesh(c, p.data(), n.data(), q.data(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    if (st != MDMC_OK) return st;
+    FILE* f = std::fopen(path, "w");
+    if (!f) return fail(c, MDMC_ERROR_IO, std::string("cannot open ") + path);
+    // iostream's default float output: %g with 6 significant digits
+    for (int64_t v = 0; v < c->V; ++v) std::fprintf(f, "v %g %g %g\n", p[3 * v], p[3 * v + 1], p[3 * v + 2]);
+    for (int64_t v = 0; v < c->V; ++v) std::fprintf(f, "vn %g %g %g\n", n[3 * v], n[3 * v + 1], n[3 * v + 2]);
+    for (int64_t i = 0; i < c->F; ++i) {
+        const int a = q[4 * i] + 1, b = q[4 * i + 1] + 1, d = q[4 * i + 2] + 1, e = q[4 * i + 3] + 1;
+        std::fprintf(f, "f %d//%d %d//%d %d//%d %d//%d\n", a, a, b, b, d, d, e, e);
+    }
+    std::fclose(f);
+    return MDMC_OK;
+}
+
+const char* mdmc_last_error(const mdmc_context* c) { return c ? c->err.c_str() : "null context"; }
+
+void mdmc_case_tables(uint64_t contour_words[256], uint8_t ambiguous[256]) {
+    for (int i = 0; i < 256; ++i) {
+        if (contour_words) contour_words[i] = kContourTableHost[i];
+        if (ambiguous) ambiguous[i] = caseIsAmbiguous(i) ? 1 : 0;
+    }
+}
+
+}  // extern "C"

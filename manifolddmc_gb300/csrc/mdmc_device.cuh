@@ -1,0 +1,319 @@
+// Device-side building blocks of the Dual Marching Cubes path.
+//
+// Every float expression keeps the reference's operation order (glm
+// semantics) and the library is compiled with -fmad=false, so results are
+// rounded exactly as the reference's expressions are written; the CPU oracle
+// does the same and the two agree bit for bit.
+#pragma once
+
+#include <cstdint>
+
+#include "mc_contour_table.h"
+#include "mdmc_types.h"
+
+namespace mdmc {
+
+// ---------------------------------------------------------------------------
+// float3 helpers (glm::vec3 arithmetic, one rounding per operation)
+// ---------------------------------------------------------------------------
+struct F3 {
+    float x, y, z;
+};
+__host__ __device__ __forceinline__ F3 f3(float x, float y, float z) { return {x, y, z}; }
+__host__ __device__ __forceinline__ F3 operator+(F3 a, F3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__host__ __device__ __forceinline__ F3 operator-(F3 a, F3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__host__ __device__ __forceinline__ F3 operator*(F3 a, F3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__host__ __device__ __forceinline__ F3 operator/(F3 a, F3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+__host__ __device__ __forceinline__ F3 operator*(F3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__host__ __device__ __forceinline__ F3 operator*(float s, F3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__host__ __device__ __forceinline__ F3 operator/(F3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__host__ __device__ __forceinline__ float gmin(float x, float y) { return (y < x) ? y : x; }
+__host__ __device__ __forceinline__ float gmax(float x, float y) { return (x < y) ? y : x; }
+__host__ __device__ __forceinline__ float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+// glm::normalize: v * (1 / sqrt((x*x + y*y) + z*z))
+__device__ __forceinline__ F3 gnormalize(F3 v) {
+    float d = v.x * v.x + v.y * v.y;
+    d = d + v.z * v.z;
+    float inv = 1.0f / sqrtf(d);
+    return v * inv;
+}
+
+constexpr float kEpsilon = 0.0001f;  // LazyEngine::Constants::EPSILON
+
+// Interpolation<float>::interpolateTrilinearly, D/Utils/Interpolation.inl:76-84
+__device__ __forceinline__ float trilinear(const float s[8], F3 p) {
+    float a = s[0] + p.x * (s[1] - s[0]);
+    float b = s[2] + p.x * (s[3] - s[2]);
+    float c = s[4] + p.x * (s[5] - s[4]);
+    float e = s[6] + p.x * (s[7] - s[6]);
+    float lo = (1.f - p.y) * a + p.y * b;
+    float hi = (1.f - p.y) * c + p.y * e;
+    return (1.f - p.z) * lo + p.z * hi;
+}
+
+// ---------------------------------------------------------------------------
+// cell edges and the packed contour word (D/CellIntersection.h:28-137)
+// ---------------------------------------------------------------------------
+// corner pair of every cell edge; corner i sits at (i&1, (i>>1)&1, (i>>2)&1)
+__host__ __device__ __forceinline__ int edgeV0(int e) { return (int)((0x231046540210ULL >> (4 * e)) & 0xF); }
+__host__ __device__ __forceinline__ int edgeV1(int e) { return (int)((0x675467752331ULL >> (4 * e)) & 0xF); }
+// axis of every edge (0 = x, 1 = y, 2 = z)
+__host__ __device__ __forceinline__ int edgeAxis(int e) { return (int)((0xAA4444u >> (2 * e)) & 0x3); }
+
+__host__ __device__ __forceinline__ int nib(uint64_t w, int i) { return (int)((w >> (4 * i)) & 0xF); }
+__device__ __forceinline__ int contourSize(uint64_t c, int t) { return nib(c, t); }
+__device__ __forceinline__ int contourEdge(uint64_t c, int t, int pos) {
+    int before = 0;
+    for (int k = 0; k < t; ++k) before += nib(c, k);
+    return (int)((c >> (16 + 4 * (before + pos))) & 0xF);
+}
+__device__ __forceinline__ int numContours(uint64_t c) {
+    int n = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) n += nib(c, t) > 0 ? 1 : 0;
+    return n;
+}
+
+// quad slot of an edge (computeVertexPosition, D/CellIntersection.inl:361-366)
+__host__ __device__ __forceinline__ int quadSlot(int e, int edgyBit) {
+    return (int)((240177437832960ULL >> (4 * e + 2 * edgyBit)) & 3);
+}
+
+// cell faces in the flattened orientation (D/CellIntersection.inl:290-292)
+__device__ __forceinline__ int faceEdge(int f, int i) {
+    const unsigned short fe[6] = {0x0123, 0x4765, 0x4908, 0x2A6B, 0x83B7, 0x95A1};
+    return (fe[f] >> (4 * i)) & 0xF;
+}
+__device__ __forceinline__ int faceCorner(int f, int i) {
+    const unsigned short fc[6] = {0x3120, 0x6475, 0x1504, 0x7362, 0x2064, 0x7531};
+    return (fc[f] >> (4 * i)) & 0xF;
+}
+
+// The reference takes the asymptotic-decider path for a case
+// (s_triangleAmbiguities == MC_AMBIGUOUS, D/DualMarchingCubes.cpp:301) exactly
+// when a face of the cell has the diagonal sign pattern, or when the inside
+// corners are just the two ends of one cell diagonal (or all but those two).
+__host__ __device__ inline bool caseIsAmbiguous(int c) {
+    const unsigned short fc[6] = {0x3120, 0x6475, 0x1504, 0x7362, 0x2064, 0x7531};
+    for (int f = 0; f < 6; ++f) {
+        int m = 0;
+        for (int i = 0; i < 4; ++i) m |= ((c >> ((fc[f] >> (4 * i)) & 0xF)) & 1) << i;
+        if (m == 6 || m == 9) return true;
+    }
+    for (int i = 0; i < 4; ++i) {
+        int pair = (1 << i) | (1 << (7 - i));
+        if (c == pair || c == (255 ^ pair)) return true;
+    }
+    return false;
+}
+
+// marchingCubesAsymptoticPolygon, D/CellIntersection.inl:202-338.  Faces are
+// classified, their oriented segments connected, ambiguous faces decided by
+// the bilinear saddle value, and the segments chained into contours starting
+// from the lowest unused edge.
+__device__ inline uint64_t asymptoticContours(const float s[8], float iso) {
+    uint32_t seg[12];
+#pragma unroll
+    for (int i = 0; i < 12; ++i) seg[i] = 0xFF;
+    auto connect = [&](int in, int out) {
+        seg[in] = (seg[in] & 0xF0u) | (uint32_t)(out & 0xF);
+        seg[out] = (seg[out] & 0x0Fu) | (uint32_t)(in << 4);
+    };
+    for (int f = 0; f < 6; ++f) {
+        int e[4];
+        float val[4];
+        unsigned fc = 0;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            e[i] = faceEdge(f, i);
+            val[i] = s[faceCorner(f, i)];
+            fc |= (unsigned)(val[i] >= iso) << i;
+        }
+        switch (fc) {
+            case 1: connect(e[0], e[3]); break;
+            case 2: connect(e[1], e[0]); break;
+            case 3: connect(e[1], e[3]); break;
+            case 4: connect(e[3], e[2]); break;
+            case 5: connect(e[0], e[2]); break;
+            case 7: connect(e[1], e[2]); break;
+            case 8: connect(e[2], e[1]); break;
+            case 10: connect(e[2], e[0]); break;
+            case 11: connect(e[2], e[3]); break;
+            case 12: connect(e[3], e[1]); break;
+            case 13: connect(e[0], e[1]); break;
+            case 14: connect(e[3], e[0]); break;
+            case 6:
+            case 9: {
+                float num = val[0] * val[3] - val[1] * val[2];
+                float den = val[0] + val[3];
+                den = den - val[1];
+                den = den - val[2];
+                float decision = num / den;
+                bool hi = decision >= iso;
+                if (fc == 6) {
+                    if (hi) { connect(e[3], e[0]); connect(e[1], e[2]); }
+                    else { connect(e[1], e[0]); connect(e[3], e[2]); }
+                } else {
+                    if (hi) { connect(e[0], e[1]); connect(e[2], e[3]); }
+                    else { connect(e[0], e[3]); connect(e[2], e[1]); }
+                }
+            } break;
+            default: break;
+        }
+    }
+    uint64_t c = 0xFFFFFFFFFFFF0000ULL;
+    int n = 0;
+    int used = 0;  // edges already written, across contours
+    for (int edge = 0; edge < 12; ++edge) {
+        if (seg[edge] == 0xFF) continue;
+        const int start = edge;
+        int out = (int)(seg[edge] & 0xF);
+        int pos = 0;
+        int bit = 16 + 4 * used;
+        c = (c & ~(0xFULL << bit)) | ((uint64_t)start << bit);
+        int guard = 0;
+        while (out != start && guard < 12) {
+            ++pos;
+            bit = 16 + 4 * (used + pos);
+            if (bit <= 60) c = (c & ~(0xFULL << bit)) | ((uint64_t)out << bit);
+            int in = out;
+            if (in < 12) {
+                out = (int)(seg[in] & 0xF);
+                seg[in] = 0xFF;
+            } else {
+                out = start;
+            }
+            ++guard;
+        }
+        if (n < 4) c = (c & ~(0xFULL << (4 * n))) | ((uint64_t)(pos + 1) << (4 * n));
+        used += pos + 1;
+        ++n;
+    }
+    return c;
+}
+
+// contours of an active cell: table word or asymptotic decider
+__device__ __forceinline__ uint64_t cellContours(int cs, const float s[8], float iso, const uint64_t* table) {
+    if (caseIsAmbiguous(cs)) return asymptoticContours(s, iso);
+    return table[cs];
+}
+
+// VertexToSurfaceIterator, D/CellIntersection.inl:12-122
+struct SurfaceIterator {
+    const float* s;
+    float iso;
+
+    __device__ F3 gradient(F3 p) const {
+        float gx = (1 - p.z) * ((1 - p.y) * (s[1] - s[0]) + p.y * (s[3] - s[2])) +
+                   p.z * ((1 - p.y) * (s[5] - s[4]) + p.y * (s[7] - s[6]));
+        float gy = (1 - p.z) * ((1 - p.x) * (s[2] - s[0]) + p.x * (s[3] - s[1])) +
+                   p.z * ((1 - p.x) * (s[6] - s[4]) + p.x * (s[7] - s[5]));
+        float gz = (1 - p.y) * ((1 - p.x) * (s[4] - s[0]) + p.x * (s[5] - s[1])) +
+                   p.y * ((1 - p.x) * (s[6] - s[2]) + p.x * (s[7] - s[3]));
+        return f3(gx, gy, gz);
+    }
+    __device__ bool update(F3& point, F3& grad, F3 in1, F3& in2, float v1, float& v2, bool cl[3]) const {
+        grad = gnormalize(grad);
+        in2 = in1 + 0.05f * grad;
+        cl[0] = in2.x <= 0.f || in2.x >= 1.f;
+        cl[1] = in2.y <= 0.f || in2.y >= 1.f;
+        cl[2] = in2.z <= 0.f || in2.z >= 1.f;
+        in2 = f3(gclamp(in2.x, 0.f, 1.f), gclamp(in2.y, 0.f, 1.f), gclamp(in2.z, 0.f, 1.f));
+        v2 = trilinear(s, in2);
+        if ((v1 <= iso && iso <= v2) || (v2 <= iso && iso <= v1)) {
+            float e = v1;
+            if (v1 != v2) e = (iso - v1) / (v2 - v1);
+            point = in1 + e * (in2 - in1);
+            return true;
+        }
+        return false;
+    }
+    __device__ void move(F3& point) const {
+        F3 in1 = point;
+        float v1 = trilinear(s, in1);
+        float v2 = 0.f;
+        for (int i = 0; i < 30; ++i) {
+            F3 g = gradient(in1);
+            if (v1 > iso) g = f3(-g.x, -g.y, -g.z);
+            F3 in2 = in1;
+            bool cl[3];
+            if (update(point, g, in1, in2, v1, v2, cl)) break;
+            if (cl[0] || cl[1] || cl[2]) {
+                if (cl[0]) g.x = 0.f;
+                else if (cl[1]) g.y = 0.f;
+                else g.z = 0.f;
+                bool cl2[3];
+                if (update(point, g, in1, in2, v1, v2, cl2)) break;
+            }
+            in1 = in2;
+            v1 = v2;
+        }
+        const float lo = kEpsilon, hi = 1.f - kEpsilon;
+        point = f3(gclamp(point.x, lo, hi), gclamp(point.y, lo, hi), gclamp(point.z, lo, hi));
+    }
+};
+
+// ---------------------------------------------------------------------------
+// grid access
+// ---------------------------------------------------------------------------
+struct GridView {
+    const float* v;
+    int X, Y, Z;
+    float ox, oy, oz;  // origin
+    float dx, dy, dz;  // spacing
+    __device__ __forceinline__ float at(int x, int y, int z) const {
+        return __ldg(v + ((size_t)z * Y + y) * X + x);
+    }
+    __device__ __forceinline__ float atClamped(int x, int y, int z) const {
+        x = x < 0 ? 0 : (x > X - 1 ? X - 1 : x);
+        y = y < 0 ? 0 : (y > Y - 1 ? Y - 1 : y);
+        z = z < 0 ? 0 : (z > Z - 1 ? Z - 1 : z);
+        return at(x, y, z);
+    }
+    __device__ __forceinline__ F3 origin() const { return f3(ox, oy, oz); }
+    __device__ __forceinline__ F3 deltas() const { return f3(dx, dy, dz); }
+    // UniformGrid::evaluateCellCornerValues, D/UniformGrid.inl:414-427
+    __device__ __forceinline__ void corners(int x, int y, int z, float s[8]) const {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) s[i] = atClamped(x + (i & 1), y + ((i >> 1) & 1), z + ((i >> 2) & 1));
+    }
+    // getIndex3DFromPosition, D/UniformGrid.inl:441-448
+    __device__ __forceinline__ void cellOf(F3 p, int c[3]) const {
+        F3 off = (p - origin()) / deltas();
+        c[0] = (int)floorf(off.x);
+        c[1] = (int)floorf(off.y);
+        c[2] = (int)floorf(off.z);
+    }
+};
+
+// UniformGrid::computeGradients, D/UniformGrid.inl:325-379
+__device__ inline void cornerGradients(const GridView& g, int x, int y, int z, const float s[8], F3 out[8]) {
+    auto cl = [](int dim, int ii) { return ii < 0 ? 0 : (ii >= dim ? dim - 1 : ii); };
+    const int X = g.X, Y = g.Y, Z = g.Z;
+    F3 gr[8];
+    gr[0] = f3(s[1] - g.at(cl(X, x - 1), y, z), s[2] - g.at(x, cl(Y, y - 1), z), s[4] - g.at(x, y, cl(Z, z - 1)));
+    gr[1] = f3(g.at(cl(X, x + 2), y, z) - s[0], s[3] - g.at(x + 1, cl(Y, y - 1), z), s[5] - g.at(x + 1, y, cl(Z, z - 1)));
+    gr[2] = f3(s[3] - g.at(cl(X, x - 1), y + 1, z), g.at(x, cl(Y, y + 2), z) - s[0], s[6] - g.at(x, y + 1, cl(Z, z - 1)));
+    gr[3] = f3(g.at(cl(X, x + 2), y + 1, z) - s[2], g.at(x + 1, cl(Y, y + 2), z) - s[1],
+               s[7] - g.at(x + 1, y + 1, cl(Z, z - 1)));
+    gr[4] = f3(s[5] - g.at(cl(X, x - 1), y, z + 1), s[6] - g.at(x, cl(Y, y - 1), z + 1), g.at(x, y, cl(Z, z + 2)) - s[0]);
+    gr[5] = f3(g.at(cl(X, x + 2), y, z + 1) - s[4], s[7] - g.at(x + 1, cl(Y, y - 1), z + 1),
+               g.at(x + 1, y, cl(Z, z + 2)) - s[1]);
+    gr[6] = f3(s[7] - g.at(cl(X, x - 1), y + 1, z + 1), g.at(x, cl(Y, y + 2), z + 1) - s[4],
+               g.at(x, y + 1, cl(Z, z + 2)) - s[2]);
+    gr[7] = f3(g.at(cl(X, x + 2), y + 1, z + 1) - s[6], g.at(x + 1, cl(Y, y + 2), z + 1) - s[5],
+               g.at(x + 1, y + 1, cl(Z, z + 2)) - s[3]);
+    const F3 dl = g.deltas();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) out[i] = (0.5f * gr[i]) / dl;
+}
+
+// Interpolation<glm::vec3>::interpolateTrilinearly of the corner gradients
+__device__ __forceinline__ F3 trilinear3(const F3 n[8], F3 p) {
+    float xs[8], ys[8], zs[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) { xs[i] = n[i].x; ys[i] = n[i].y; zs[i] = n[i].z; }
+    return f3(trilinear(xs, p), trilinear(ys, p), trilinear(zs, p));
+}
+
+}  // namespace mdmc

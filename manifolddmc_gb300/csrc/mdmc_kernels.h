@@ -1,0 +1,82 @@
+// Kernel launchers of the library (one stream per call, no host syncs).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mdmc_device.cuh"
+#include "mdmc_types.h"
+
+#include <atomic>
+
+namespace mdmc {
+
+// kernels launched by this library in the process (read per run for stats)
+extern std::atomic<long long> g_kernelLaunches;
+inline void countLaunch(int n = 1) { g_kernelLaunches.fetch_add(n, std::memory_order_relaxed); }
+
+__device__ __forceinline__ void setTwinOut(int4* he, int h, int t) { reinterpret_cast<int*>(he)[4 * (int64_t)h + 3] = t; }
+
+// splitter working copies (device pointers)
+struct SplitWork {
+    float* pos;
+    float* nrm;
+    uint32_t* vfl;
+    uint32_t* hfl;
+    uint32_t* ffl;
+    int* vC2O;
+    int* hC2O;
+    int* fC2O;
+    int* vO2C;  // dense over the mesh's vertices, 0x7FFFFFFF = none
+    int* hO2C;  // dense over halfedges, -1 = none
+    int* fO2C;  // dense over faces, -1 = none
+    int* origV;
+    int* origH;
+    int4* he;
+    int* first;
+    uint16_t* attr;
+    int* vNum;
+    int* vSlots;
+    int* hNum;
+    int* hSlots;
+};
+
+void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int pad, cudaStream_t s);
+void launchRowCount(const GridView& g, float iso, int4* rowCounts, int numRows, cudaStream_t s);
+void launchRowEmit(const GridView& g, float iso, int surfaceIteration, const int4* rowOffsets, int numRows,
+                   ActiveCell* act, float* pos, float* nrm, cudaStream_t s);
+void launchQuads(const ActiveCell* act, int numActive, const int4* rowOffsets, int X, int Y, Bucket* table,
+                 unsigned long long cap, int4* he, int* faceFirst, uint16_t* faceAttr, uint32_t* status,
+                 cudaStream_t s);
+
+void launchBuckets(Bucket* table, unsigned long long cap, int4* he, uint16_t* faceAttr, uint8_t* vflags,
+                   int connectTwins, int* nmList, DevCounters* ctr, cudaStream_t s);
+void launchInsertFaces(const int4* he, const int* faceFirst, int numFaces, Bucket* table, unsigned long long cap,
+                       uint32_t* status, cudaStream_t s);
+void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s);
+void launchReconnect(const GridView& g, float iso, const Bucket* table, const int* nmList, const DevCounters* ctr,
+                     int4* he, const float* pos, uint32_t* status, cudaStream_t s);
+void launchDetectFans(const int4* he, int numHalfedges, uint8_t* isKey, int* fans, uint8_t* vflags, int numVertices,
+                      DevCounters* ctr, uint32_t* status, cudaStream_t s);
+void launchOutput(const int4* he, const int* faceFirst, int numFaces, int numHalfedges, int numVertices,
+                  const Bucket* table, unsigned long long cap, int4* quads, int* vertexHE, DevCounters* ctr,
+                  cudaStream_t s);
+
+void launchFlagNMFaces(const uint16_t* attr, int numFaces, int* flags, cudaStream_t s);
+void launchCompactNMFaces(const int* flags, const int* offsets, int numFaces, int* nmFaces, cudaStream_t s);
+void launchFillInt(int* p, int64_t n, int v, cudaStream_t s);
+void launchSplitCopy(const int* nmFaces, int n, const int4* he, const int* faceFirst, const uint16_t* faceAttr,
+                     const float* pos, const float* nrm, const SplitWork& w, cudaStream_t s);
+void launchSplitMarkNM(const Bucket* table, const int* nmList, const DevCounters* ctr, const SplitWork& w,
+                       uint32_t* status, cudaStream_t s);
+void launchSplitSubdivide(int n, const SplitWork& w, uint32_t* status, cudaStream_t s);
+void launchSplitCollapse(int nh, int nv, const SplitWork& w, uint32_t* status, cudaStream_t s);
+void launchSplitMerge(int nv, int nh, const SplitWork& w, uint32_t* status, cudaStream_t s);
+void launchSplitMergeHalfedges(int nh, const SplitWork& w, uint32_t* status, cudaStream_t s);
+void launchSplitMove(int nv, const GridView& g, float iso, const SplitWork& w, cudaStream_t s);
+void launchSplitFlagAppends(int count, const uint32_t* fl, const int* c2o, int* out, cudaStream_t s);
+void launchSplitCopyBack(int nv, int nh, int nf, const SplitWork& w, const int* appV, const int* appH,
+                         const int* appF, int V, int H, int F, float* pos, float* nrm, int4* he, int* faceFirst,
+                         uint16_t* faceAttr, cudaStream_t s);
+void launchSplitResetMaps(int n, const int* nmFaces, const SplitWork& w, cudaStream_t s);
+
+}  // namespace mdmc

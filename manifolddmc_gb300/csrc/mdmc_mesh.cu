@@ -1,0 +1,405 @@
+// Halfedge-mesh kernels: edge-table finishing (twins and flags), the
+// asymptotic-decider twin repair, face-fan detection and the output pass.
+//
+// Reference: connectHalfedgeTwins and refresh*Flags
+// (D/Halfedges/HalfedgeMesh.cu:92-291), reconnectHalfedges
+// (D/PostProcesses/ManifoldCreator.cu:39-312), detectNonManifoldVertices
+// (D/PostProcesses/ManifoldCreator.cu:319-536) and the statistics getters
+// (D/Halfedges/HalfedgeMesh.cu:1164-1239).
+//
+// The reference's bucket order is the order of atomic inserts; here the ids
+// of a bucket are sorted first, which makes every per-bucket decision (twin
+// pairing of 3- and 4-face edges, wall-side ties in the repair) deterministic.
+#include <cuda_runtime.h>
+
+#include "mdmc_device.cuh"
+#include "mdmc_edge_hash.cuh"
+#include "mdmc_kernels.h"
+
+namespace mdmc {
+
+__device__ __forceinline__ void setTwin(int4* he, int h, int t) { reinterpret_cast<int*>(he)[4 * (int64_t)h + 3] = t; }
+__device__ __forceinline__ void orFaceAttr(uint16_t* attr, int f, uint32_t bits) {
+    atomicOr(reinterpret_cast<uint32_t*>(attr) + (f >> 1), bits << ((f & 1) * 16));
+}
+__device__ __forceinline__ void orVertexFlag(uint8_t* flags, int v, uint32_t bits) {
+    atomicOr(reinterpret_cast<uint32_t*>(flags) + (v >> 2), bits << ((v & 3) * 8));
+}
+
+template <typename T>
+__device__ __forceinline__ void blockAddTo(unsigned long long* dst, T v) {
+    __shared__ unsigned long long acc;
+    if (threadIdx.x == 0) acc = 0;
+    __syncthreads();
+    unsigned long long w = (unsigned long long)v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&acc, w);
+    __syncthreads();
+    if (threadIdx.x == 0 && acc) atomicAdd(dst, acc);
+}
+
+// Sorts each bucket's ids, then (connectTwins) pairs twins as
+// connectHalfedgeTwins does, and sets the face and vertex flags of
+// refreshFaceFlagsGPU / refresh{NonManifold,Weird,Boundary}Flags.  Buckets
+// with at least four ids go to nmList (isHashTableEntryNonManifold).
+__global__ void kBuckets(Bucket* __restrict__ table, unsigned long long cap, int4* __restrict__ he, uint16_t* faceAttr,
+                         uint8_t* vflags, int connectTwins, int* __restrict__ nmList, DevCounters* ctr) {
+    int nE = 0, nE3 = 0, nE4 = 0;
+    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        Bucket b = table[i];
+        if (b.key == kEmptyKey) continue;
+        const int count = b.cnt + 1;
+        const int n = count < 4 ? count : 4;
+        int* e = b.ids;
+        // insertion sort of at most four ids
+        for (int a = 1; a < n; ++a) {
+            int v = e[a], k = a - 1;
+            while (k >= 0 && e[k] > v) { e[k + 1] = e[k]; --k; }
+            e[k + 1] = v;
+        }
+        if (n > 1) {
+            int4 ids = make_int4(e[0], e[1], e[2], e[3]);
+            *reinterpret_cast<int4*>(&table[i].ids[0]) = ids;
+        }
+        ++nE;
+        if (count == 3) ++nE3;
+        if (count == 4) ++nE4;
+        if (count >= 4) nmList[atomicAdd(&ctr->nmBuckets, 1ULL)] = (int)i;
+        if (connectTwins) {
+            if (count == 2) {
+                setTwin(he, e[0], e[1]);
+                setTwin(he, e[1], e[0]);
+            } else if (count == 3) {
+                setTwin(he, e[0], e[1]);
+                setTwin(he, e[1], e[2]);
+                setTwin(he, e[2], e[0]);
+            } else if (count == 4) {  // "HACKY_OLD_WAY", HalfedgeMesh.cu:250-281
+                const int v0 = he[e[0]].x, v1 = he[e[1]].x, v2 = he[e[2]].x;
+                if (v0 != v1) {
+                    setTwin(he, e[0], e[1]); setTwin(he, e[1], e[0]);
+                    setTwin(he, e[2], e[3]); setTwin(he, e[3], e[2]);
+                } else if (v0 != v2) {
+                    setTwin(he, e[0], e[2]); setTwin(he, e[2], e[0]);
+                    setTwin(he, e[1], e[3]); setTwin(he, e[3], e[1]);
+                } else {
+                    setTwin(he, e[0], e[3]); setTwin(he, e[3], e[0]);
+                    setTwin(he, e[1], e[2]); setTwin(he, e[2], e[1]);
+                }
+            }
+        }
+        if (count == 4)
+            for (int k = 0; k < 4; ++k) orFaceAttr(faceAttr, he[e[k]].y, MDMC_FACE_NON_MANIFOLD);
+        if (count == 4)
+            for (int k = 0; k < 4; ++k) orVertexFlag(vflags, he[e[k]].x, MDMC_VERTEX_NON_MANIFOLD);
+        if (count == 3)
+            for (int k = 0; k < 3; ++k) orVertexFlag(vflags, he[e[k]].x, MDMC_VERTEX_WEIRD);
+        if (count == 1) orVertexFlag(vflags, he[e[0]].x, MDMC_VERTEX_BOUNDARY);
+    }
+    blockAddTo(&ctr->edges, nE);
+    blockAddTo(&ctr->edges3, nE3);
+    blockAddTo(&ctr->edges4, nE4);
+}
+
+void launchBuckets(Bucket* table, unsigned long long cap, int4* he, uint16_t* faceAttr, uint8_t* vflags,
+                   int connectTwins, int* nmList, DevCounters* ctr, cudaStream_t s) {
+    unsigned long long blocks = (cap + 255) / 256;
+    if (blocks > 152ULL * 16) blocks = 152ULL * 16;
+    if (blocks == 0) blocks = 1;
+    countLaunch();
+    kBuckets<<<(unsigned)blocks, 256, 0, s>>>(table, cap, he, faceAttr, vflags, connectTwins, nmList, ctr);
+}
+
+// refreshHashTableGPU, D/Halfedges/HalfedgeMesh.cu:62-90
+__global__ void kInsertFaces(const int4* __restrict__ he, const int* __restrict__ faceFirst, int numFaces,
+                             Bucket* table, unsigned long long cap, uint32_t* status) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= numFaces) return;
+    int h = faceFirst[f];
+    int q[4], hs[4];
+    for (int i = 0; i < 4; ++i) {
+        int4 e = he[h];
+        q[i] = e.x;
+        hs[i] = h;
+        h = e.z;
+    }
+    for (int i = 0; i < 4; ++i) edgeInsert(table, cap, q[i], q[(i + 1) & 3], hs[i], status);
+}
+
+void launchInsertFaces(const int4* he, const int* faceFirst, int numFaces, Bucket* table, unsigned long long cap,
+                       uint32_t* status, cudaStream_t s) {
+    if (numFaces <= 0) return;
+    countLaunch();
+    kInsertFaces<<<(numFaces + 255) / 256, 256, 0, s>>>(he, faceFirst, numFaces, table, cap, status);
+}
+
+// face attributes: clearPatternFlags + unsetNonManifoldFlag (HalfedgeMesh.cu:1050-1055)
+__global__ void kResetFaceFlags(uint16_t* attr, int numFaces) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < numFaces) attr[f] = (uint16_t)(attr[f] & 0x1F);
+}
+void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s) {
+    if (numFaces > 0) {
+        countLaunch();
+        kResetFaceFlags<<<(numFaces + 255) / 256, 256, 0, s>>>(attr, numFaces);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// reconnectHalfedges, D/PostProcesses/ManifoldCreator.cu:39-312
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ F3 nudge(int it) {
+    F3 r = f3((it & 1) ? 1.f : 0.f, (it & 2) ? 1.f : 0.f, (it & 4) ? 1.f : 0.f);
+    if (it & 8) r.x = -r.x;
+    if (it & 16) r.y = -r.y;
+    if (it & 32) r.z = -r.z;
+    return r * kEpsilon;
+}
+
+__device__ __forceinline__ F3 loadP(const float* pos, int v) { return f3(pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]); }
+
+__global__ void kReconnect(GridView g, float iso, const Bucket* __restrict__ table, const int* __restrict__ nmList,
+                           const DevCounters* ctr, int4* he, const float* __restrict__ pos, uint32_t* status) {
+    const int count = (int)ctr->nmBuckets;
+    for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < count; w += gridDim.x * blockDim.x) {
+        const Bucket b = table[nmList[w]];
+        const int4 h0 = he[b.ids[0]];
+        const int n0 = h0.x, n1 = he[h0.z].x;
+        F3 p0 = loadP(pos, n0), p1 = loadP(pos, n1);
+        int c0[3], c1[3];
+        g.cellOf(p0, c0);
+        g.cellOf(p1, c1);
+        // nudge both vertices until their cells are face neighbours (:87-108)
+        for (int i = 0; i < 0x40; ++i) {
+            const F3 o0 = nudge(i);
+            F3 o1 = o0;
+            int finalK = -1;
+            for (int k = 0; k < 0x40; ++k) {
+                o1 = nudge(k);
+                int a[3], bb[3];
+                g.cellOf(p0 + o0, a);
+                g.cellOf(p1 + o1, bb);
+                int sum = abs(a[0] - bb[0]) + abs(a[1] - bb[1]) + abs(a[2] - bb[2]);
+                if (sum == 1) { finalK = k; break; }
+            }
+            if (finalK != -1) {
+                p0 = p0 + o0;
+                g.cellOf(p0, c0);
+                p1 = p1 + o1;
+                g.cellOf(p1, c1);
+                break;
+            }
+        }
+        const int64_t lin0 = ((int64_t)c0[2] * g.Y + c0[1]) * g.X + c0[0];
+        const int64_t lin1 = ((int64_t)c1[2] * g.Y + c1[1]) * g.X + c1[0];
+        int A[3], B[3];
+        for (int a = 0; a < 3; ++a) {
+            A[a] = lin0 < lin1 ? c0[a] : c1[a];
+            B[a] = lin0 < lin1 ? c1[a] : c0[a];
+        }
+        int nr[3], mn[3];
+        for (int a = 0; a < 3; ++a) {
+            nr[a] = max(A[a], B[a]) - min(A[a], B[a]);
+            mn[a] = max(A[a], B[a]);
+        }
+        int xo[3] = {0, 0, 0}, yo[3] = {0, 0, 0};
+        if (nr[0] == 0) {
+            xo[0] = 1;
+            if (nr[1] == 0) yo[1] = 1;
+            else yo[2] = 1;
+        } else {
+            xo[1] = 1;
+            yo[2] = 1;
+        }
+        if (mn[0] < 0 || mn[1] < 0 || mn[2] < 0 || mn[0] + 1 >= g.X || mn[1] + 1 >= g.Y || mn[2] + 1 >= g.Z)
+            atomicOr(status, kStatusWallOutOfGrid);
+        const float w0 = g.atClamped(mn[0], mn[1], mn[2]);
+        const float w1 = g.atClamped(mn[0] + xo[0], mn[1] + xo[1], mn[2] + xo[2]);
+        const float w2 = g.atClamped(mn[0] + xo[0] + yo[0], mn[1] + xo[1] + yo[1], mn[2] + xo[2] + yo[2]);
+        const float w3 = g.atClamped(mn[0] + yo[0], mn[1] + yo[1], mn[2] + yo[2]);
+        const F3 corner0 = g.origin() + g.deltas() * f3((float)mn[0], (float)mn[1], (float)mn[2]);
+        const F3 corner2 = g.origin() + g.deltas() * f3((float)(mn[0] + xo[0] + yo[0]), (float)(mn[1] + xo[1] + yo[1]),
+                                                        (float)(mn[2] + xo[2] + yo[2]));
+        const bool omitX = xo[0] == 0 && yo[0] == 0;
+        const bool omitY = xo[1] == 0 && yo[1] == 0;
+        auto down = [&](F3 p, float& u, float& v) {
+            if (omitX) { u = p.y; v = p.z; }
+            else if (omitY) { u = p.x; v = p.z; }
+            else { u = p.x; v = p.y; }
+        };
+        float minU, minV, maxU, maxV;
+        down(corner0, minU, minV);
+        down(corner2, maxU, maxV);
+        int sorted[4] = {-1, -1, -1, -1};
+        for (int i = 0; i < 4; ++i) {
+            const int hid = b.ids[i];
+            const int opp = he[he[he[hid].z].z].x;
+            float u, v;
+            down(loadP(pos, opp), u, v);
+            const float mnU = u - minU, mnV = v - minV, mxU = u - maxU, mxV = v - maxV;
+            if (mnV < 0.f) sorted[0] = hid;
+            if (mxU > 0.f) sorted[1] = hid;
+            if (mxV > 0.f) sorted[2] = hid;
+            if (mnU < 0.f) sorted[3] = hid;
+        }
+        if (sorted[0] < 0 || sorted[1] < 0 || sorted[2] < 0 || sorted[3] < 0) continue;
+        // AsymptoticDecider2D::quadrant0BelongsTogether, D/Utils/AsymptoticDecider.h:119-164
+        const float m00 = w0, m10 = w1, m11 = w2, m01 = w3;
+        float C = m00 - m10;
+        C = C - m01;
+        C = C + m11;
+        const float delta = (m00 * m11 - m10 * m01) / C;
+        const bool together = (m00 < iso && delta >= iso) || (m00 >= iso && delta < iso);
+        if (!together) {
+            setTwin(he, sorted[0], sorted[1]); setTwin(he, sorted[1], sorted[0]);
+            setTwin(he, sorted[2], sorted[3]); setTwin(he, sorted[3], sorted[2]);
+        } else {
+            setTwin(he, sorted[0], sorted[3]); setTwin(he, sorted[3], sorted[0]);
+            setTwin(he, sorted[1], sorted[2]); setTwin(he, sorted[2], sorted[1]);
+        }
+    }
+}
+
+void launchReconnect(const GridView& g, float iso, const Bucket* table, const int* nmList, const DevCounters* ctr,
+                     int4* he, const float* pos, uint32_t* status, cudaStream_t s) {
+    countLaunch();
+    kReconnect<<<152 * 2, 128, 0, s>>>(g, iso, table, nmList, ctr, he, pos, status);
+}
+
+// ---------------------------------------------------------------------------
+// detectNonManifoldVertices, D/PostProcesses/ManifoldCreator.cu:319-536
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int stepCW(const int4* he, int h) {
+    const int t = he[h].w;
+    return t != -1 ? he[t].z : -1;
+}
+__device__ __forceinline__ int stepCCW(const int4* he, int h) {
+    const int p = he[he[he[h].z].z].z;
+    const int t = he[p].w;
+    return t != -1 ? t : -1;
+}
+__device__ __forceinline__ int fanWalk(const int4* he, int start, bool cw, uint32_t* status) {
+    const int origin = he[start].x;
+    int result = start;
+    int cur = cw ? stepCW(he, start) : stepCCW(he, start);
+    int guard = 0;
+    while (cur != -1) {
+        if (cur == result) break;
+        if (origin != he[cur].x) break;
+        if (cur < result) result = cur;
+        cur = cw ? stepCW(he, cur) : stepCCW(he, cur);
+        if (++guard > 4096) {
+            atomicOr(status, kStatusWalkLimit);
+            break;
+        }
+    }
+    return result;
+}
+
+// A fan key is the smallest halfedge id of the fan and has the origin of the
+// halfedge it was found from, so "distinct (origin, key) pairs per origin"
+// (the reference's sort + unique) equals "halfedges named as key by some
+// halfedge, per origin".  No sort is needed.
+__global__ void kFanKeys(const int4* __restrict__ he, int numHalfedges, uint8_t* __restrict__ isKey, uint32_t* status) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= numHalfedges) return;
+    const int k = min(h, min(fanWalk(he, h, true, status), fanWalk(he, h, false, status)));
+    isKey[k] = 1;
+}
+
+__global__ void kFanCount(const int4* __restrict__ he, int numHalfedges, const uint8_t* __restrict__ isKey,
+                          int* __restrict__ fans) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= numHalfedges) return;
+    if (isKey[h]) atomicAdd(&fans[he[h].x], 1);
+}
+
+__global__ void kFanFlags(const int* __restrict__ fans, uint8_t* __restrict__ vflags, int numVertices, DevCounters* ctr) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    int nm = 0;
+    if (v < numVertices) {
+        uint8_t f = vflags[v];
+        if (fans[v] > 1) {
+            f |= MDMC_VERTEX_MULTIPLE_FANS;
+            nm = 1;
+        } else {
+            f &= (uint8_t)~MDMC_VERTEX_MULTIPLE_FANS;
+        }
+        vflags[v] = f;
+    }
+    blockAddTo(&ctr->nmVertices, nm);
+}
+
+void launchDetectFans(const int4* he, int numHalfedges, uint8_t* isKey, int* fans, uint8_t* vflags, int numVertices,
+                      DevCounters* ctr, uint32_t* status, cudaStream_t s) {
+    if (numHalfedges > 0) {
+        countLaunch();
+        kFanKeys<<<(numHalfedges + 255) / 256, 256, 0, s>>>(he, numHalfedges, isKey, status);
+        countLaunch();
+        kFanCount<<<(numHalfedges + 255) / 256, 256, 0, s>>>(he, numHalfedges, isKey, fans);
+    }
+    if (numVertices > 0) {
+        countLaunch();
+        kFanFlags<<<(numVertices + 255) / 256, 256, 0, s>>>(fans, vflags, numVertices, ctr);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// output pass: face vertex quads, getNumQuadsWithNonManifoldEdges, and the
+// smallest outgoing halfedge of every vertex
+// ---------------------------------------------------------------------------
+__global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__ faceFirst, int numFaces,
+                            const Bucket* __restrict__ table, unsigned long long cap, int4* __restrict__ quads,
+                            DevCounters* ctr) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    int cnt = -1;
+    if (f < numFaces) {
+        int h = faceFirst[f];
+        int q[4];
+        for (int i = 0; i < 4; ++i) {
+            int4 e = he[h];
+            q[i] = e.x;
+            h = e.z;
+        }
+        quads[f] = make_int4(q[0], q[1], q[2], q[3]);
+        cnt = 0;
+        for (int i = 0; i < 4; ++i)
+            if (edgeValence(table, cap, q[i], q[(i + 1) & 3]) > 2) ++cnt;
+    }
+    for (int k = 1; k <= 4; ++k) blockAddTo(&ctr->quadsNM[k], cnt == k ? 1 : 0);
+}
+
+__global__ void kVertexHalfedge(const int4* __restrict__ he, int numHalfedges, int* __restrict__ vertexHE) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h < numHalfedges) {
+        const int v = he[h].x;
+        if (v >= 0) atomicMin(&vertexHE[v], h);
+    }
+}
+
+__global__ void kVertexHalfedgeFix(int* vertexHE, int numVertices) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v < numVertices && vertexHE[v] == 0x7F7F7F7F) vertexHE[v] = -1;
+}
+
+void launchOutput(const int4* he, const int* faceFirst, int numFaces, int numHalfedges, int numVertices,
+                  const Bucket* table, unsigned long long cap, int4* quads, int* vertexHE, DevCounters* ctr,
+                  cudaStream_t s) {
+    if (numFaces > 0) {
+        countLaunch();
+        kFaceOutput<<<(numFaces + 255) / 256, 256, 0, s>>>(he, faceFirst, numFaces, table, cap, quads, ctr);
+    }
+    if (numVertices > 0) {
+        // 0x7F7F7F7F marks "none"; atomicMin lowers it
+        cudaMemsetAsync(vertexHE, 0x7F, sizeof(int) * (size_t)numVertices, s);
+        if (numHalfedges > 0) {
+            countLaunch();
+            kVertexHalfedge<<<(numHalfedges + 255) / 256, 256, 0, s>>>(he, numHalfedges, vertexHE);
+        }
+        countLaunch();
+        kVertexHalfedgeFix<<<(numVertices + 255) / 256, 256, 0, s>>>(vertexHE, numVertices);
+    }
+}
+
+}  // namespace mdmc

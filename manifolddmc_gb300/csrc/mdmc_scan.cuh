@@ -1,0 +1,167 @@
+// Exclusive prefix sums over int and int4 arrays, in three phases: per-tile
+// reduction, one-block scan of the tile sums, per-tile scan with the tile's
+// offset.  out has n+1 entries; out[n] is the total.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mdmc_kernels.h"
+
+namespace mdmc {
+
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+constexpr int kScanMaxTiles = 1024 * 16;  // largest tile-sum array one block scans
+
+template <typename T>
+struct ScanOps;
+template <>
+struct ScanOps<int> {
+    __device__ static int zero() { return 0; }
+    __device__ static int add(int a, int b) { return a + b; }
+};
+template <>
+struct ScanOps<int4> {
+    __device__ static int4 zero() { return make_int4(0, 0, 0, 0); }
+    __device__ static int4 add(int4 a, int4 b) { return make_int4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+};
+
+template <typename T>
+__device__ T warpInclusive(T v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        T u;
+        if constexpr (sizeof(T) == sizeof(int)) {
+            u = __shfl_up_sync(0xffffffffu, v, o);
+        } else {
+            u.x = __shfl_up_sync(0xffffffffu, v.x, o);
+            u.y = __shfl_up_sync(0xffffffffu, v.y, o);
+            u.z = __shfl_up_sync(0xffffffffu, v.z, o);
+            u.w = __shfl_up_sync(0xffffffffu, v.w, o);
+        }
+        if (lane >= o) v = ScanOps<T>::add(v, u);
+    }
+    return v;
+}
+
+// block-wide exclusive scan of one value per thread; returns the block total
+template <typename T>
+__device__ T blockExclusive(T v, T& total) {
+    __shared__ T warpSums[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+    T inc = warpInclusive(v);
+    if (lane == 31) warpSums[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        T w = lane < nw ? warpSums[lane] : ScanOps<T>::zero();
+        T wi = warpInclusive(w);
+        warpSums[lane] = wi;
+    }
+    __syncthreads();
+    T before = warp > 0 ? warpSums[warp - 1] : ScanOps<T>::zero();
+    total = warpSums[nw - 1];
+    __syncthreads();
+    T exc = inc;
+    // exclusive = inclusive - own value, computed additively
+    if constexpr (sizeof(T) == sizeof(int)) {
+        exc = inc - v;
+    } else {
+        exc = make_int4(inc.x - v.x, inc.y - v.y, inc.z - v.z, inc.w - v.w);
+    }
+    return ScanOps<T>::add(before, exc);
+}
+
+template <typename T>
+__global__ void kScanReduce(const T* __restrict__ in, int64_t n, T* __restrict__ tileSums) {
+    const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    T acc = ScanOps<T>::zero();
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t i = base + (int64_t)k * kScanThreads + threadIdx.x;
+        if (i < n) acc = ScanOps<T>::add(acc, in[i]);
+    }
+    T total;
+    blockExclusive(acc, total);
+    if (threadIdx.x == 0) tileSums[blockIdx.x] = total;
+}
+
+// one block: exclusive scan of the tile sums in place, total -> tileSums[numTiles]
+template <typename T>
+__global__ void kScanTiles(T* tileSums, int numTiles) {
+    constexpr int per = kScanMaxTiles / 1024;
+    T vals[per];
+    T acc = ScanOps<T>::zero();
+#pragma unroll
+    for (int k = 0; k < per; ++k) {
+        int i = threadIdx.x * per + k;
+        vals[k] = i < numTiles ? tileSums[i] : ScanOps<T>::zero();
+        acc = ScanOps<T>::add(acc, vals[k]);
+    }
+    T total;
+    T run = blockExclusive(acc, total);
+#pragma unroll
+    for (int k = 0; k < per; ++k) {
+        int i = threadIdx.x * per + k;
+        if (i < numTiles) tileSums[i] = run;
+        run = ScanOps<T>::add(run, vals[k]);
+    }
+    if (threadIdx.x == 0) tileSums[numTiles] = total;
+}
+
+template <typename T>
+__global__ void kScanApply(const T* __restrict__ in, int64_t n, const T* __restrict__ tileSums,
+                           T* __restrict__ out) {
+    const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    // each thread owns kScanItems consecutive elements
+    T vals[kScanItems];
+    T acc = ScanOps<T>::zero();
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t i = base + (int64_t)threadIdx.x * kScanItems + k;
+        vals[k] = i < n ? in[i] : ScanOps<T>::zero();
+        acc = ScanOps<T>::add(acc, vals[k]);
+    }
+    T total;
+    T run = ScanOps<T>::add(tileSums[blockIdx.x], blockExclusive(acc, total));
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        int64_t i = base + (int64_t)threadIdx.x * kScanItems + k;
+        if (i < n) out[i] = run;
+        run = ScanOps<T>::add(run, vals[k]);
+    }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = tileSums[gridDim.x];
+}
+
+// in and out may alias only if the caller accepts in being overwritten after
+// the reduction (kScanApply reads in[i] before writing out[i] of the same i).
+// scratch needs numTiles + 1 elements.  Returns false if n is too large.
+template <typename T>
+bool exclusiveScan(const T* in, T* out, int64_t n, T* scratch, cudaStream_t s) {
+    const int64_t tiles = (n + kScanTile - 1) / kScanTile;
+    if (tiles > kScanMaxTiles) return false;
+    const int nt = tiles > 0 ? (int)tiles : 1;
+    if (n > 0) {
+        countLaunch();
+        kScanReduce<T><<<nt, kScanThreads, 0, s>>>(in, n, scratch);
+    } else {
+        cudaMemsetAsync(scratch, 0, sizeof(T), s);
+    }
+    countLaunch();
+    kScanTiles<T><<<1, 1024, 0, s>>>(scratch, n > 0 ? nt : 0);
+    if (n > 0) {
+        countLaunch();
+        kScanApply<T><<<nt, kScanThreads, 0, s>>>(in, n, scratch, out);
+    } else {
+        cudaMemcpyAsync(out, scratch, sizeof(T), cudaMemcpyDeviceToDevice, s);
+    }
+    return true;
+}
+
+inline int64_t scanScratchElems(int64_t n) { return (n + kScanTile - 1) / kScanTile + 2; }
+
+}  // namespace mdmc

@@ -1,0 +1,518 @@
+// Non-manifold edge splitting (ManifoldSplitter, D/PostProcesses/ManifoldSplitter.cu).
+//
+// Working-copy layout (deterministic; the reference appends with atomics):
+// with n non-manifold faces taken in ascending face order, face k owns copy
+// vertices 4k..4k+3 and copy halfedges 4k..4k+3 (its corners and edges), copy
+// face k, and, once subdivided, new vertices 4n+4k..4n+4k+3, new halfedges
+// 4n+16k..4n+16k+15 (inner ring, then three per boundary quad) and new faces
+// n+4k..n+4k+3.  Merge-partner lists are sorted after the collapse so that
+// the partner closure and "first valid twin" do not depend on atomic order.
+#include <cuda_runtime.h>
+
+#include "mdmc_device.cuh"
+#include "mdmc_edge_hash.cuh"
+#include "mdmc_kernels.h"
+
+namespace mdmc {
+
+constexpr uint32_t kRemove = 16;      // Flags::setRemoveFlag
+constexpr uint32_t kNonManifold = 1;  // Flags::setNonManifoldFlag
+constexpr int kNone = -1;
+
+__global__ void kFlagNMFaces(const uint16_t* __restrict__ attr, int numFaces, int* __restrict__ flags) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < numFaces) flags[f] = (attr[f] & MDMC_FACE_NON_MANIFOLD) ? 1 : 0;
+}
+__global__ void kCompactNMFaces(const int* __restrict__ flags, const int* __restrict__ offsets, int numFaces,
+                                int* __restrict__ nmFaces) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f < numFaces && flags[f]) nmFaces[offsets[f]] = f;
+}
+void launchFlagNMFaces(const uint16_t* attr, int numFaces, int* flags, cudaStream_t s) {
+    if (numFaces > 0) {
+        countLaunch();
+        kFlagNMFaces<<<(numFaces + 255) / 256, 256, 0, s>>>(attr, numFaces, flags);
+    }
+}
+void launchCompactNMFaces(const int* flags, const int* offsets, int numFaces, int* nmFaces, cudaStream_t s) {
+    if (numFaces > 0) {
+        countLaunch();
+        kCompactNMFaces<<<(numFaces + 255) / 256, 256, 0, s>>>(flags, offsets, numFaces, nmFaces);
+    }
+}
+
+__global__ void kFillInt(int* p, int64_t n, int v) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+void launchFillInt(int* p, int64_t n, int v, cudaStream_t s) {
+    if (n <= 0) return;
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 16);
+    countLaunch();
+    kFillInt<<<blocks, 256, 0, s>>>(p, n, v);
+}
+
+// copyVerticesToWorkingCopy / copyHalfedgesToWorkingCopy / copyFacesToWorkingCopy
+// (:307-446).  Every original vertex maps to its smallest copy (the
+// reference keeps whichever copy wrote last; all copies hold the same data).
+__global__ void kCopyOut(const int* __restrict__ nmFaces, int n, const int4* __restrict__ he,
+                         const int* __restrict__ faceFirst, const uint16_t* __restrict__ faceAttr,
+                         const float* __restrict__ pos, const float* __restrict__ nrm, SplitWork w) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const int f = nmFaces[k];
+    int h = faceFirst[f];
+    for (int i = 0; i < 4; ++i) {
+        const int4 e = he[h];
+        const int c = 4 * k + i;
+        const int v = e.x;
+        for (int a = 0; a < 3; ++a) {
+            w.pos[3 * c + a] = pos[3 * (int64_t)v + a];
+            w.nrm[3 * c + a] = nrm[3 * (int64_t)v + a];
+        }
+        w.vC2O[c] = v;
+        w.origV[c] = v;
+        atomicMin(&w.vO2C[v], c);
+        w.he[c] = e;
+        w.hC2O[c] = h;
+        w.origH[c] = h;
+        w.hO2C[h] = c;
+        h = e.z;
+    }
+    w.first[k] = 4 * k;  // hO2C of the face's first halfedge
+    w.attr[k] = faceAttr[f];
+    w.fC2O[k] = f;
+    w.fO2C[f] = k;
+}
+
+// updateWorkingCopyHalfedges (:463-505); twins outside the copy become -twin-2
+__global__ void kUpdateRefs(int n, SplitWork w) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= 4 * n) return;
+    int4 e = w.he[c];
+    e.x = w.vO2C[e.x];
+    e.y = w.fO2C[e.y];
+    e.z = w.hO2C[e.z];
+    if (e.w >= 0) {
+        const int t = w.hO2C[e.w];
+        e.w = (t == kNone) ? -e.w - 2 : t;
+    }
+    w.he[c] = e;
+}
+
+// markHalfedgesAsNonManifold (:527-555)
+__global__ void kMarkNM(const Bucket* __restrict__ table, const int* __restrict__ nmList, const DevCounters* ctr,
+                        SplitWork w, uint32_t* status) {
+    const int count = (int)ctr->nmBuckets;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const Bucket b = table[nmList[i]];
+        for (int k = 0; k < 4; ++k) {
+            const int c = w.hO2C[b.ids[k]];
+            if (c < 0) {
+                atomicOr(status, kStatusBadTwin);
+                continue;
+            }
+            atomicOr(&w.hfl[c], kNonManifold);
+            atomicOr(&w.vfl[w.he[c].x], kNonManifold);
+        }
+    }
+}
+
+// performSubdivideQuads (:650-731): four inner vertices at (0.33|0.67)^2,
+// an inner quad that keeps the face's id and four boundary quads that take
+// the original edges.
+__global__ void kSubdivide(int n, SplitWork w, uint32_t* status) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float uvs[4][2] = {{0.33f, 0.33f}, {0.67f, 0.33f}, {0.67f, 0.67f}, {0.33f, 0.67f}};
+    int hid[4], vid[4];
+    int h = w.first[k];
+    for (int i = 0; i < 4; ++i) {
+        hid[i] = h;
+        const int4 e = w.he[h];
+        vid[i] = e.x;
+        h = e.z;
+    }
+    F3 P[4], N[4];
+    for (int i = 0; i < 4; ++i) {
+        P[i] = f3(w.pos[3 * vid[i]], w.pos[3 * vid[i] + 1], w.pos[3 * vid[i] + 2]);
+        N[i] = f3(w.nrm[3 * vid[i]], w.nrm[3 * vid[i] + 1], w.nrm[3 * vid[i] + 2]);
+    }
+    auto mix = [](F3 a, F3 b, float t) { return a * (1.f - t) + b * t; };
+    int inner[4];
+    for (int i = 0; i < 4; ++i) {
+        const float u = uvs[i][0], v = uvs[i][1];
+        const F3 pp = mix(mix(P[0], P[1], u), mix(P[3], P[2], u), v);
+        const F3 nn = mix(mix(N[0], N[1], u), mix(N[3], N[2], u), v);
+        const int c = 4 * n + 4 * k + i;
+        w.pos[3 * c] = pp.x; w.pos[3 * c + 1] = pp.y; w.pos[3 * c + 2] = pp.z;
+        w.nrm[3 * c] = nn.x; w.nrm[3 * c + 1] = nn.y; w.nrm[3 * c + 2] = nn.z;
+        inner[i] = c;
+    }
+    const int hb = 4 * n + 16 * k;
+    int ih[4];
+    for (int i = 0; i < 4; ++i) ih[i] = hb + i;
+    for (int i = 0; i < 4; ++i) w.he[ih[i]] = make_int4(inner[i], k, ih[(i + 1) & 3], -1);
+    w.first[k] = ih[0];
+    int of[4][4];
+    int prev = 3;
+    for (int j = 0; j < 4; ++j) {
+        const int qv[3] = {vid[j], inner[j], inner[prev]};
+        for (int t = 0; t < 3; ++t) of[j][t] = hb + 4 + 3 * j + t;
+        of[j][3] = hid[prev];
+        const int nf = n + 4 * k + j;
+        for (int t = 0; t < 3; ++t) w.he[of[j][t]] = make_int4(qv[t], nf, of[j][(t + 1) & 3], -1);
+        // the original edge keeps origin and twin, joins the boundary quad
+        int4 o = w.he[hid[prev]];
+        o.y = nf;
+        o.z = of[j][0];
+        w.he[hid[prev]] = o;
+        w.first[nf] = of[j][0];
+        w.attr[nf] = 0x1F;  // HalfedgeFace(): INVALID_COLOR
+        prev = j;
+    }
+    prev = 3;
+    for (int j = 0; j < 4; ++j) {
+        w.he[of[j][2]].w = of[prev][0];
+        w.he[of[prev][0]].w = of[j][2];
+        w.he[of[j][1]].w = ih[prev];
+        w.he[ih[prev]].w = of[j][1];
+        prev = j;
+    }
+    // swapHalfedgeMappings (:629-648): the inner ring takes over the original
+    // halfedge slots, the original edges become new halfedges
+    for (int i = 0; i < 4; ++i) {
+        const int a = hid[i], b = ih[i];
+        const int ao = w.hC2O[a], bo = w.hC2O[b];
+        w.hC2O[a] = bo;
+        w.hC2O[b] = ao;
+        if (ao != kNone && bo == kNone) w.hO2C[ao] = b;
+        else atomicOr(status, kStatusMappingSwap);
+    }
+}
+
+// DeviceMergeList::mark (:749-765); partner slots are sorted afterwards
+__device__ __forceinline__ void markPartner(int* num, int* slots, int a, int b, uint32_t* status) {
+    const int idx = atomicAdd(&num[a], 1);
+    if (idx - 1 < 4) slots[4 * a + idx - 1] = b;
+    if (idx > 2) atomicOr(status, kStatusPartnerOverflow);
+}
+
+// performCollapseNonManifoldHalfedges + collapseHalfedge (:767-868)
+__global__ void kCollapse(int nh, SplitWork w, uint32_t* status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nh) return;
+    if (!(w.hfl[t] & kNonManifold)) return;
+    const int tw = w.he[t].w;
+    if (tw < 0) {
+        atomicOr(status, kStatusBadTwin);
+        return;
+    }
+    if (tw < t) return;
+    int f0[4], f1[4];
+    int4 cur = w.he[t], ctw = w.he[tw];
+    f0[0] = t;
+    f1[0] = tw;
+    for (int i = 1; i < 4; ++i) {
+        f0[i] = cur.z;
+        f1[4 - i] = ctw.z;
+        cur = w.he[cur.z];
+        ctw = w.he[ctw.z];
+    }
+    for (int i = 0; i < 4; ++i) {
+        atomicOr(&w.hfl[f0[i]], kRemove);
+        atomicOr(&w.hfl[f1[i]], kRemove);
+    }
+    atomicOr(&w.ffl[w.he[f0[0]].y], kRemove);
+    atomicOr(&w.ffl[w.he[f1[0]].y], kRemove);
+    {
+        const int a = w.he[f0[2]].x, b = w.he[f1[1]].x;
+        markPartner(w.vNum, w.vSlots, a, b, status);
+        markPartner(w.vNum, w.vSlots, b, a, status);
+    }
+    {
+        const int a = w.he[f0[3]].x, b = w.he[f1[2]].x;
+        markPartner(w.vNum, w.vSlots, a, b, status);
+        markPartner(w.vNum, w.vSlots, b, a, status);
+    }
+    for (int i = 1; i < 4; ++i) {
+        const int a = f0[i], b = f1[i];
+        const int at = w.he[a].w, bt = w.he[b].w;
+        if (at < 0 || bt < 0) {
+            atomicOr(status, kStatusBadTwin);
+            continue;
+        }
+        markPartner(w.hNum, w.hSlots, a, bt, status);
+        markPartner(w.hNum, w.hSlots, bt, a, status);
+        markPartner(w.hNum, w.hSlots, b, at, status);
+        markPartner(w.hNum, w.hSlots, at, b, status);
+    }
+}
+
+__global__ void kSortPartners(int* num, int* slots, int count) {
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= count) return;
+    const int n = min(num[a] - 1, 4);
+    if (n < 2) return;
+    int s[4];
+    for (int i = 0; i < n; ++i) s[i] = slots[4 * a + i];
+    for (int i = 1; i < n; ++i) {
+        int v = s[i], j = i - 1;
+        while (j >= 0 && s[j] > v) { s[j + 1] = s[j]; --j; }
+        s[j + 1] = v;
+    }
+    for (int i = 0; i < n; ++i) slots[4 * a + i] = s[i];
+}
+
+// DeviceMergeList::getAllPartnersOf (:25-62): breadth-first closure, at most
+// 12 partners
+__device__ int closure(const int* num, const int* slots, int v, int out[12], uint32_t* status) {
+    auto cnt = [&](int x) { return min(num[x], 5); };
+    int np = cnt(v);
+    if (np <= 1) return np;
+    for (int i = 0; i < np - 1; ++i) out[i] = slots[4 * v + i];
+    for (int i = 0; i < np - 1; ++i) {
+        const int p = out[i];
+        const int npp = cnt(p);
+        for (int k = 0; k < npp - 1; ++k) {
+            const int pp = slots[4 * p + k];
+            bool contained = (pp == v);
+            for (int z = 0; z < np - 1; ++z) contained = contained || out[z] == pp;
+            if (!contained) {
+                if (np - 1 >= 12) {
+                    atomicOr(status, kStatusPartnerOverflow);
+                    continue;
+                }
+                out[np - 1] = pp;
+                ++np;
+            }
+        }
+    }
+    return np;
+}
+
+// mergeVertices (:936-990); the survivor's normal receives the averaged
+// position, as in the reference (:989)
+__global__ void kMergeVertices(int nv, SplitWork w, uint32_t* status) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    int part[12];
+    const int np = closure(w.vNum, w.vSlots, v, part, status);
+    if (np <= 1) return;
+    if (np > 12) {
+        atomicOr(status, kStatusPartnerOverflow);
+        return;
+    }
+    int smallest = v;
+    F3 p = f3(w.pos[3 * v], w.pos[3 * v + 1], w.pos[3 * v + 2]);
+    bool obsolete = false;
+    for (int i = 0; i < np - 1; ++i) {
+        const int q = part[i];
+        p = p + f3(w.pos[3 * q], w.pos[3 * q + 1], w.pos[3 * q + 2]);
+        if (q < smallest) {
+            obsolete = true;
+            smallest = q;
+        }
+    }
+    if (obsolete) {
+        atomicOr(&w.vfl[v], kRemove);
+        return;
+    }
+    p = p / (float)np;
+    w.pos[3 * smallest] = p.x; w.pos[3 * smallest + 1] = p.y; w.pos[3 * smallest + 2] = p.z;
+    w.nrm[3 * smallest] = p.x; w.nrm[3 * smallest + 1] = p.y; w.nrm[3 * smallest + 2] = p.z;
+}
+
+// updateHalfedgeVertexIDs (:992-1019)
+__global__ void kUpdateOrigins(int nh, SplitWork w, uint32_t* status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nh) return;
+    const int v = w.he[t].x;
+    if (v < 0) return;
+    int part[12];
+    const int np = closure(w.vNum, w.vSlots, v, part, status);
+    if (np <= 1) return;
+    int s = v;
+    for (int i = 0; i < np - 1; ++i) s = min(s, part[i]);
+    w.he[t].x = s;
+}
+
+// mergeHalfedges (:1021-1067): reads only removed partners' twins, which no
+// thread writes, so one pass is race-free
+__global__ void kMergeHalfedges(int nh, SplitWork w, uint32_t* status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nh) return;
+    if (w.hfl[t] & kRemove) return;
+    int part[12];
+    const int np = closure(w.hNum, w.hSlots, t, part, status);
+    if (np <= 1) return;
+    int valid = -1;
+    for (int i = 0; i < np - 1; ++i) {
+        const int tw = w.he[part[i]].w;
+        if (tw < 0) continue;
+        if (!(w.hfl[tw] & kRemove)) {
+            valid = tw;
+            break;
+        }
+    }
+    if (valid == -1 || valid < t) return;
+    w.he[t].w = valid;
+    w.he[valid].w = t;
+}
+
+// performMoveVerticesToSurface (:1130-1160)
+__global__ void kMoveVertices(int nv, GridView g, float iso, SplitWork w) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    if (w.vfl[v] & kRemove) return;
+    const F3 p = f3(w.pos[3 * v], w.pos[3 * v + 1], w.pos[3 * v + 2]);
+    int idx[3];
+    g.cellOf(p, idx);
+    float s[8];
+    g.corners(idx[0], idx[1], idx[2], s);
+    const F3 fi = f3((float)idx[0], (float)idx[1], (float)idx[2]);
+    const F3 fi1 = f3((float)(idx[0] + 1), (float)(idx[1] + 1), (float)(idx[2] + 1));
+    const F3 mn = g.origin() + fi * g.deltas();
+    const F3 mx = g.origin() + fi1 * g.deltas();
+    F3 local = (p - mn) / (mx - mn);
+    SurfaceIterator it{s, iso};
+    it.move(local);
+    const F3 q = g.origin() + (fi + local) * g.deltas();
+    w.pos[3 * v] = q.x; w.pos[3 * v + 1] = q.y; w.pos[3 * v + 2] = q.z;
+}
+
+// copy-back selection: elements kept and without an original get appended
+__global__ void kFlagAppends(int count, const uint32_t* __restrict__ fl, const int* __restrict__ c2o,
+                             int* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) out[i] = (!(fl[i] & kRemove) && c2o[i] == kNone) ? 1 : 0;
+}
+
+// copyVerticesBack / copyHalfedgesBack / copyFacesBack (:1176-1260)
+__global__ void kCopyBackVertices(int nv, SplitWork w, const int* __restrict__ app, int V, float* pos, float* nrm) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv) return;
+    if (w.vfl[v] & kRemove) return;
+    int o = w.vC2O[v];
+    if (o == kNone) {
+        o = V + app[v];
+        w.vC2O[v] = o;
+    }
+    for (int a = 0; a < 3; ++a) {
+        pos[3 * (int64_t)o + a] = w.pos[3 * v + a];
+        nrm[3 * (int64_t)o + a] = w.nrm[3 * v + a];
+    }
+}
+__global__ void kAssignHalfedges(int nh, SplitWork w, const int* __restrict__ app, int H) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nh) return;
+    if (w.hfl[t] & kRemove) return;
+    if (w.hC2O[t] == kNone) w.hC2O[t] = H + app[t];
+}
+__global__ void kCopyBackFaces(int nf, SplitWork w, const int* __restrict__ app, int F, int* faceFirst,
+                               uint16_t* faceAttr) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= nf) return;
+    if (w.ffl[f] & kRemove) return;
+    int o = w.fC2O[f];
+    if (o == kNone) {
+        o = F + app[f];
+        w.fC2O[f] = o;
+    }
+    faceFirst[o] = w.hC2O[w.first[f]];
+    faceAttr[o] = w.attr[f];
+}
+// copyHalfedgesBack + updateHalfedgesBack (:1205-1295)
+__global__ void kCopyBackHalfedges(int nh, SplitWork w, int4* he) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nh) return;
+    if (w.hfl[t] & kRemove) return;
+    int4 e = w.he[t];
+    const int self = w.hC2O[t];
+    e.z = w.hC2O[e.z];
+    e.y = w.fC2O[e.y];
+    e.x = w.vC2O[e.x];
+    if (e.w < 0) {
+        e.w = -e.w - 2;
+        if (e.w != -1) setTwinOut(he, e.w, self);
+    } else {
+        e.w = w.hC2O[e.w];
+    }
+    he[self] = e;
+}
+
+// after an iteration: clear the dense original->copy maps it touched
+__global__ void kResetMaps(int n, const int* __restrict__ nmFaces, SplitWork w) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= 4 * n) return;
+    w.vO2C[w.origV[c]] = 0x7FFFFFFF;
+    w.hO2C[w.origH[c]] = kNone;
+    if ((c & 3) == 0) w.fO2C[nmFaces[c >> 2]] = kNone;
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static inline int nb(int64_t n) { return (int)((n + 255) / 256); }
+
+void launchSplitCopy(const int* nmFaces, int n, const int4* he, const int* faceFirst, const uint16_t* faceAttr,
+                     const float* pos, const float* nrm, const SplitWork& w, cudaStream_t s) {
+    countLaunch();
+    kCopyOut<<<nb(n), 256, 0, s>>>(nmFaces, n, he, faceFirst, faceAttr, pos, nrm, w);
+    countLaunch();
+    kUpdateRefs<<<nb(4 * (int64_t)n), 256, 0, s>>>(n, w);
+}
+void launchSplitMarkNM(const Bucket* table, const int* nmList, const DevCounters* ctr, const SplitWork& w,
+                       uint32_t* status, cudaStream_t s) {
+    countLaunch();
+    kMarkNM<<<152, 256, 0, s>>>(table, nmList, ctr, w, status);
+}
+void launchSplitSubdivide(int n, const SplitWork& w, uint32_t* status, cudaStream_t s) {
+    countLaunch();
+    kSubdivide<<<nb(n), 128, 0, s>>>(n, w, status);
+}
+void launchSplitCollapse(int nh, int nv, const SplitWork& w, uint32_t* status, cudaStream_t s) {
+    countLaunch();
+    kCollapse<<<nb(nh), 256, 0, s>>>(nh, w, status);
+    countLaunch();
+    kSortPartners<<<nb(nv), 256, 0, s>>>(w.vNum, w.vSlots, nv);
+    countLaunch();
+    kSortPartners<<<nb(nh), 256, 0, s>>>(w.hNum, w.hSlots, nh);
+}
+void launchSplitMerge(int nv, int nh, const SplitWork& w, uint32_t* status, cudaStream_t s) {
+    countLaunch();
+    kMergeVertices<<<nb(nv), 128, 0, s>>>(nv, w, status);
+    countLaunch();
+    kUpdateOrigins<<<nb(nh), 128, 0, s>>>(nh, w, status);
+}
+void launchSplitMergeHalfedges(int nh, const SplitWork& w, uint32_t* status, cudaStream_t s) {
+    countLaunch();
+    kMergeHalfedges<<<nb(nh), 128, 0, s>>>(nh, w, status);
+}
+void launchSplitMove(int nv, const GridView& g, float iso, const SplitWork& w, cudaStream_t s) {
+    countLaunch();
+    kMoveVertices<<<nb(nv), 128, 0, s>>>(nv, g, iso, w);
+}
+void launchSplitFlagAppends(int count, const uint32_t* fl, const int* c2o, int* out, cudaStream_t s) {
+    if (count > 0) {
+        countLaunch();
+        kFlagAppends<<<nb(count), 256, 0, s>>>(count, fl, c2o, out);
+    }
+}
+void launchSplitCopyBack(int nv, int nh, int nf, const SplitWork& w, const int* appV, const int* appH,
+                         const int* appF, int V, int H, int F, float* pos, float* nrm, int4* he, int* faceFirst,
+                         uint16_t* faceAttr, cudaStream_t s) {
+    countLaunch();
+    kCopyBackVertices<<<nb(nv), 256, 0, s>>>(nv, w, appV, V, pos, nrm);
+    countLaunch();
+    kAssignHalfedges<<<nb(nh), 256, 0, s>>>(nh, w, appH, H);
+    countLaunch();
+    kCopyBackFaces<<<nb(nf), 256, 0, s>>>(nf, w, appF, F, faceFirst, faceAttr);
+    countLaunch();
+    kCopyBackHalfedges<<<nb(nh), 256, 0, s>>>(nh, w, he);
+}
+void launchSplitResetMaps(int n, const int* nmFaces, const SplitWork& w, cudaStream_t s) {
+    countLaunch();
+    kResetMaps<<<nb(4 * (int64_t)n), 256, 0, s>>>(n, nmFaces, w);
+}
+
+}  // namespace mdmc

@@ -1,0 +1,57 @@
+// Internal types shared by the library's translation units.
+#pragma once
+
+#include <cstdint>
+
+#include "mdmc.h"
+
+namespace mdmc {
+
+// Device status bits.  Kernels never trap: a hit limit sets a bit, the kernel
+// skips the offending element and the host reports the bits after the run.
+enum : uint32_t {
+    kStatusProbeLimit = 1u << 0,       // edge hash: probe limit reached
+    kStatusSlotConflict = 1u << 1,     // two cells claimed the same quad slot
+    kStatusBucketOverflow = 1u << 2,   // more than 4 halfedges on one edge
+    kStatusPartnerOverflow = 1u << 3,  // merge list longer than the reference's
+    kStatusWalkLimit = 1u << 4,        // fan walk did not close
+    kStatusBadTwin = 1u << 5,          // twin outside the working copy
+    kStatusIterationCap = 1u << 6,     // splitter iteration cap
+    kStatusWallOutOfGrid = 1u << 7,    // cell wall outside the grid (clamped)
+    kStatusMissingCell = 1u << 8,      // quad neighbour cell not found
+    kStatusMappingSwap = 1u << 9,      // unexpected working-copy mapping swap
+};
+
+// Edge hash bucket: 32 bytes, one sector.  key = concatenateKeys(min, max)
+// (D/Utils/Utilities.h:15-22); cnt stores count-1 so that an all-0xFF memset
+// yields an empty bucket (key ~0, count 0, ids -1).
+struct __align__(32) Bucket {
+    unsigned long long key;
+    int cnt;
+    int ids[4];
+    int pad;
+};
+constexpr unsigned long long kEmptyKey = ~0ULL;
+
+// Active cell record written by the DMC emit pass (16 bytes):
+//   cell  = linear sample index of the cell's corner 0
+//   vbase = index of the cell's first vertex
+//   qbase = index of the first quad the cell owns
+//   info  = case (8 bits) | edge -> contour map (2 bits per edge) << 8
+struct __align__(16) ActiveCell {
+    uint32_t cell;
+    int32_t vbase;
+    int32_t qbase;
+    uint32_t info;
+};
+
+// Device counters filled during a run and read back once at its end.
+struct DevCounters {
+    uint32_t status;
+    uint32_t pad;
+    unsigned long long edges, edges3, edges4, nmVertices;
+    unsigned long long quadsNM[5];
+    unsigned long long nmBuckets;  // length of the 4-face bucket list
+};
+
+}  // namespace mdmc

@@ -1,0 +1,37 @@
+"""Seeded synthetic grids for the benchmark configurations.
+
+No public dataset is involved: every grid is generated from a numpy
+default_rng seed with the shapes and value distributions of the benchmark
+configurations (sums of isotropic Gaussian blobs, or iid uniform noise).
+"""
+import numpy as np
+
+
+def gaussian_blobs(n, count, sigma_range, seed, amplitude=1.0):
+    """Sum of `count` isotropic Gaussians on an n^3 grid (x fastest in memory),
+    centres uniform in [0, n-1]^3, sigma uniform in sigma_range (cells)."""
+    rng = np.random.default_rng(seed)
+    ax = np.arange(n, dtype=np.float64)
+    out = np.zeros((n, n, n), np.float64)
+    for _ in range(count):
+        c = rng.uniform(0.0, n - 1.0, 3)
+        s = rng.uniform(sigma_range[0], sigma_range[1])
+        g = [np.exp(-((ax - c[k]) ** 2) / (2.0 * s * s)) for k in range(3)]
+        out += amplitude * (g[2][:, None, None] * g[1][None, :, None] * g[0][None, None, :])
+    return out.astype(np.float32)
+
+
+def uniform_noise(n, seed):
+    return np.random.default_rng(seed).random((n, n, n), dtype=np.float32)
+
+
+# name: (description, generator, iso, refinement, pad)
+CONFIGS = {
+    "blobs64_pad": ("64^3 fp32 grid, 8 Gaussian blobs (sigma 4-10), padded by 1, iso 0.5",
+                    lambda seed=0: gaussian_blobs(64, 8, (4.0, 10.0), seed), 0.5, 0, True),
+    "noise256": ("256^3 fp32 iid uniform[0,1] noise, iso 0.5",
+                 lambda seed=1: uniform_noise(256, seed), 0.5, 0, False),
+    "blobs129_refine4": ("129^3 fp32 grid, 64 Gaussian blobs (sigma 3-12), trilinearly refined x4 "
+                         "to 513^3 samples = 512^3 cells, iso 0.4",
+                         lambda seed=2: gaussian_blobs(129, 64, (3.0, 12.0), seed), 0.4, 3, False),
+}

@@ -1286,4 +1286,6 @@ void mdmc_oracle_get_dmc(const void* res, float* positions, float* normals, int*
 
 void mdmc_oracle_free(void* res) { delete (oracle::Result*)res; }
 
+int mdmc_oracle_case_ambiguous(int c) { return oracle::caseIsAmbiguous(c) ? 1 : 0; }
+
 }  // extern "C"

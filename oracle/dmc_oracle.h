@@ -87,6 +87,9 @@ void mdmc_oracle_get_dmc(const void* result, float* positions, float* normals, i
                          uint16_t* quad_attr);
 void mdmc_oracle_free(void* result);
 
+/* 1 if Marching Cubes case c takes the asymptotic-decider path. */
+int mdmc_oracle_case_ambiguous(int c);
+
 #ifdef __cplusplus
 }
 #endif

@@ -82,8 +82,12 @@ def main():
     prod = os.path.join(ROOT, "manifolddmc_gb300", "csrc", "mc_contour_table.h")
     with open(prod, "w") as f:
         f.write("#pragma once\n" + header +
-                "namespace mdmc {\n// Lives in global memory; kernels stage it in shared memory (lanes index it\n// with divergent cases, which would serialise a __constant__ read).\n__device__ const unsigned long long kContourTable[256] = {\n"
-                + table + "\n};\n}  // namespace mdmc\n")
+                "#define MDMC_CONTOUR_WORDS \\\n" + table.replace(",\n", ", \\\n").rstrip(",") + "\n\n"
+                "namespace mdmc {\n// Lives in global memory; kernels stage it in shared memory (lanes index it\n"
+                "// with divergent cases, which would serialise a __constant__ read).\n"
+                "__device__ const unsigned long long kContourTable[256] = {MDMC_CONTOUR_WORDS};\n"
+                "static const unsigned long long kContourTableHost[256] = {MDMC_CONTOUR_WORDS};\n"
+                "}  // namespace mdmc\n")
     orc = os.path.join(ROOT, "oracle", "mc_contour_table_oracle.h")
     with open(orc, "w") as f:
         f.write("#pragma once\n" + header +
