@@ -150,6 +150,7 @@ std::string statusText(uint32_t s) {
     add(kStatusWallOutOfGrid, "cell wall outside the grid");
     add(kStatusMissingCell, "quad neighbour cell missing");
     add(kStatusMappingSwap, "unexpected working-copy mapping");
+    add(kStatusCountMismatch, "emit pass disagreed with the count pass");
     return t;
 }
 
@@ -170,8 +171,14 @@ mdmc_status readInts(mdmc_context* c, const void* src, int n, cudaStream_t s) {
 
 unsigned long long tableCapacity(int64_t faces) { return (unsigned long long)roundUp((size_t)std::max<int64_t>(3 * faces, 64), 32); }
 
-SplitWork splitWork(mdmc_context* c) {
+SplitWork splitWork(mdmc_context* c, int nv, int nh, int nf) {
     SplitWork w;
+    w.nv = nv;
+    w.nh = nh;
+    w.nf = nf;
+    w.V = (int)c->V;
+    w.H = (int)c->H;
+    w.F = (int)c->F;
     w.pos = c->wPos.as<float>();
     w.nrm = c->wNrm.as<float>();
     w.vfl = c->wVfl.as<uint32_t>();
@@ -225,12 +232,13 @@ mdmc_status refreshTable(mdmc_context* c, uint32_t* status, cudaStream_t s) {
     MDMC_CHECK(c, c->table.ensure(sizeof(Bucket) * c->cap));
     MDMC_CHECK(c, cudaMemsetAsync(c->table.p, 0xFF, sizeof(Bucket) * c->cap, s));
     MDMC_CHECK(c, c->nmList.ensure(sizeof(int) * (size_t)(c->H / 4 + 1)));
-    launchInsertFaces(c->he.as<int4>(), c->faceFirst.as<int>(), (int)c->F, c->table.as<Bucket>(), c->cap, status, s);
+    const MeshDims md{(int)c->V, (int)c->F, (int)c->H};
+    launchInsertFaces(c->he.as<int4>(), c->faceFirst.as<int>(), md, c->table.as<Bucket>(), c->cap, status, s);
     launchResetFaceFlags(c->faceAttr.as<uint16_t>(), (int)c->F, s);
     MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, (size_t)c->V, s));
     MDMC_CHECK(c, cudaMemsetAsync((char*)c->counters.p + 8, 0, sizeof(DevCounters) - 8, s));
     launchBuckets(c->table.as<Bucket>(), c->cap, c->he.as<int4>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(),
-                  0, c->nmList.as<int>(), c->counters.as<DevCounters>(), s);
+                  0, c->nmList.as<int>(), c->counters.as<DevCounters>(), md, s);
     return MDMC_OK;
 }
 
@@ -247,9 +255,13 @@ mdmc_status runSplitter(mdmc_context* c, const GridView& g, float iso, int64_t& 
         launchFlagNMFaces(c->faceAttr.as<uint16_t>(), (int)c->F, c->nmFlags.as<int>(), s);
         mdmc_status st = scan<int>(c, c->nmFlags.as<int>(), c->nmOffsets.as<int>(), c->F, s);
         if (st != MDMC_OK) return st;
+        MDMC_CHECK(c, cudaGetLastError());
         if ((st = readInts(c, c->nmOffsets.as<int>() + c->F, 1, s)) != MDMC_OK) return st;
         const int n = (int)c->hostInts[0];
+        if (n < 0 || n > c->F) return fail(c, MDMC_ERROR_CUDA, "inconsistent non-manifold face count");
         if (n == 0) break;
+        if ((int64_t)c->H + 20 * (int64_t)n >= (int64_t)0x7FFFFFFF)
+            return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "splitting would exceed 2^31 halfedges");
         MDMC_CHECK(c, c->nmFaces.ensure(sizeof(int) * (size_t)n));
         launchCompactNMFaces(c->nmFlags.as<int>(), c->nmOffsets.as<int>(), (int)c->F, c->nmFaces.as<int>(), s);
 
@@ -286,19 +298,19 @@ mdmc_status runSplitter(mdmc_context* c, const GridView& g, float iso, int64_t& 
         MDMC_CHECK(c, cudaMemsetAsync(c->wHSlots.p, 0xFF, sizeof(int) * 4 * (size_t)nh, s));
         launchFillInt(c->wVNum.as<int>(), nv, 1, s);
         launchFillInt(c->wHNum.as<int>(), nh, 1, s);
-        const SplitWork w = splitWork(c);
+        const SplitWork w = splitWork(c, nv, nh, nf);
 
         // createWorkingCopies (:273-301)
         launchSplitCopy(c->nmFaces.as<int>(), n, c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(),
-                        c->pos.as<float>(), c->nrm.as<float>(), w, s);
+                        c->pos.as<float>(), c->nrm.as<float>(), w, status, s);
         launchSplitMarkNM(c->table.as<Bucket>(), c->nmList.as<int>(), ctr, w, status, s);
         if (doSub) launchSplitSubdivide(n, w, status, s);
         if (step >= MDMC_STEP_COLLAPSE_NON_MANIFOLD_EDGES) {
-            launchSplitCollapse(nh, nv, w, status, s);
-            if (step >= MDMC_STEP_MERGE_VERTICES) launchSplitMerge(nv, nh, w, status, s);
-            if (step >= MDMC_STEP_UPDATE_HALFEDGE_TWINS) launchSplitMergeHalfedges(nh, w, status, s);
+            launchSplitCollapse(w, status, s);
+            if (step >= MDMC_STEP_MERGE_VERTICES) launchSplitMerge(w, status, s);
+            if (step >= MDMC_STEP_UPDATE_HALFEDGE_TWINS) launchSplitMergeHalfedges(w, status, s);
         }
-        if (step >= MDMC_STEP_MOVE_VERTICES_TO_SURFACE) launchSplitMove(nv, g, iso, w, s);
+        if (step >= MDMC_STEP_MOVE_VERTICES_TO_SURFACE) launchSplitMove(g, iso, w, s);
 
         // copyWorkingCopiesBack (:1297-1387): kept elements without an
         // original are appended in working-copy order
@@ -315,7 +327,10 @@ mdmc_status runSplitter(mdmc_context* c, const GridView& g, float iso, int64_t& 
         MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts + 1, c->appH.as<int>() + nh, sizeof(int), cudaMemcpyDeviceToHost, s));
         MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts + 2, c->appF.as<int>() + nf, sizeof(int), cudaMemcpyDeviceToHost, s));
         MDMC_CHECK(c, cudaStreamSynchronize(s));
+        MDMC_CHECK(c, cudaGetLastError());
         const int64_t addV = c->hostInts[0], addH = c->hostInts[1], addF = c->hostInts[2];
+        if (addV < 0 || addV > nv || addH < 0 || addH > nh || addF < 0 || addF > nf)
+            return fail(c, MDMC_ERROR_CUDA, "inconsistent working-copy append counts");
         const int64_t V2 = c->V + addV, H2 = c->H + addH, F2 = c->F + addF;
         MDMC_CHECK(c, c->pos.grow(sizeof(float) * 3 * (size_t)V2, sizeof(float) * 3 * (size_t)c->V, s));
         MDMC_CHECK(c, c->nrm.grow(sizeof(float) * 3 * (size_t)V2, sizeof(float) * 3 * (size_t)c->V, s));
@@ -323,14 +338,15 @@ mdmc_status runSplitter(mdmc_context* c, const GridView& g, float iso, int64_t& 
         MDMC_CHECK(c, c->he.grow(sizeof(int4) * (size_t)H2, sizeof(int4) * (size_t)c->H, s));
         MDMC_CHECK(c, c->faceFirst.grow(sizeof(int) * (size_t)F2, sizeof(int) * (size_t)c->F, s));
         MDMC_CHECK(c, c->faceAttr.grow(roundUp(sizeof(uint16_t) * (size_t)F2, 4), sizeof(uint16_t) * (size_t)c->F, s));
-        launchSplitCopyBack(nv, nh, nf, w, c->appV.as<int>(), c->appH.as<int>(), c->appF.as<int>(), (int)c->V,
-                            (int)c->H, (int)c->F, c->pos.as<float>(), c->nrm.as<float>(), c->he.as<int4>(),
-                            c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(), s);
+        launchSplitCopyBack(w, c->appV.as<int>(), c->appH.as<int>(), c->appF.as<int>(), (int)V2, (int)H2, (int)F2,
+                            c->pos.as<float>(), c->nrm.as<float>(), c->he.as<int4>(), c->faceFirst.as<int>(),
+                            c->faceAttr.as<uint16_t>(), status, s);
         launchSplitResetMaps(n, c->nmFaces.as<int>(), w, s);
         c->V = V2;
         c->H = H2;
         c->F = F2;
         if ((st = refreshTable(c, status, s)) != MDMC_OK) return st;
+        MDMC_CHECK(c, cudaGetLastError());
         ++iterations;
         if (step < MDMC_STEP_ENABLE_ITERATIVE_REFINEMENT) break;
         if (iterations >= 64) {  // the reference loops without a cap
@@ -359,6 +375,7 @@ mdmc_status mdmc_create(mdmc_context** context, const mdmc_options* options) {
     *context = nullptr;
     int count = 0;
     if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return MDMC_ERROR_NO_DEVICE;
+    if (cudaFree(nullptr) != cudaSuccess) return MDMC_ERROR_CUDA;  // context unusable
     mdmc_context* c = new mdmc_context();
     if (options) c->opt = *options;
     else defaultOptions(&c->opt);
@@ -370,6 +387,14 @@ mdmc_status mdmc_create(mdmc_context** context, const mdmc_options* options) {
     }
     for (auto& e : c->ev) cudaEventCreate(&e);
     for (auto& e : c->kev) cudaEventCreate(&e);
+    // record every event once so that elapsed-time queries of stages a run
+    // skips (e.g. no refinement on this context) return 0 instead of failing
+    for (auto& e : c->ev) cudaEventRecord(e, 0);
+    for (auto& e : c->kev) cudaEventRecord(e, 0);
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        mdmc_destroy(c);
+        return MDMC_ERROR_CUDA;
+    }
     *context = c;
     return MDMC_OK;
 }
@@ -426,6 +451,7 @@ mdmc_status mdmc_prepare_grid(mdmc_context* c, const float* samples, int samples
     if (!c || !samples || !dims || !origin || !spacing || !out) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "null argument");
     if (refinement < 0 || dims[0] < 1 || dims[1] < 1 || dims[2] < 1)
         return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "invalid dims or refinement");
+    (void)cudaGetLastError();  // errors of earlier, unrelated runtime calls are not ours
     cudaStream_t s = (cudaStream_t)stream;
     const int pad = add_zero_boundary ? 1 : 0;
     int32_t od[3];
@@ -482,6 +508,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
                      void* stream) {
     if (!c || !grid || !grid->samples) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "null argument");
     c->err.clear();
+    (void)cudaGetLastError();  // errors of earlier, unrelated runtime calls are not ours
     const int X = grid->dims[0], Y = grid->dims[1], Z = grid->dims[2];
     if (X < 1 || Y < 1 || Z < 1) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "invalid grid dims");
     if ((uint64_t)X * Y * Z >= 0xFFFFFFFFull) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "grid has 2^32 samples or more");
@@ -504,9 +531,13 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     cudaEventRecord(c->kev[3], s);
     mdmc_status st = scan<int4>(c, c->rows.as<int4>(), c->rows.as<int4>(), numRows, s);
     if (st != MDMC_OK) return st;
+    MDMC_CHECK(c, cudaGetLastError());
     if ((st = readInts(c, c->rows.as<int4>() + numRows, 4, s)) != MDMC_OK) return st;
     const int* tot = reinterpret_cast<const int*>(c->hostInts);
     const int64_t A = tot[0], Vd = tot[1], Q = tot[2];
+    const int64_t cells = numRows * (int64_t)(X - 1);
+    if (A < 0 || A > cells || Vd < A || Vd > 4 * A || Q < 0 || Q > 3 * A)
+        return fail(c, MDMC_ERROR_CUDA, "inconsistent cell counts from the count pass");
     c->stats.num_active_cells = A;
     c->stats.num_dmc_vertices = Vd;
     c->stats.num_dmc_quads = Q;
@@ -539,24 +570,28 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)Vd, 4), s));
     cudaEventRecord(c->kev[4], s);
     launchRowEmit(g, iso, c->opt.enable_surface_to_vertex_iteration, c->rows.as<int4>(), (int)numRows,
-                  c->act.as<ActiveCell>(), c->pos.as<float>(), c->nrm.as<float>(), s);
+                  c->act.as<ActiveCell>(), c->pos.as<float>(), c->nrm.as<float>(), (int)A, (int)Vd, status, s);
     cudaEventRecord(c->kev[5], s);
     // mapQuadrilaterals + collectHalfedgeElements
     cudaEventRecord(c->kev[6], s);
     launchQuads(c->act.as<ActiveCell>(), (int)A, c->rows.as<int4>(), X, Y, c->table.as<Bucket>(), c->cap,
-                c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(), status, s);
+                c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(), (int)Q, (int)Vd, status, s);
+    MDMC_CHECK(c, cudaGetLastError());
     cudaEventRecord(c->kev[7], s);
     cudaEventRecord(c->ev[1], s);
 
     // ---- halfedge mesh: twins and flags (HalfedgeMesh::initialize) -----------
     cudaEventRecord(c->kev[8], s);
+    const MeshDims md0{(int)Vd, (int)Q, (int)(4 * Q)};
     launchBuckets(c->table.as<Bucket>(), c->cap, c->he.as<int4>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), 1,
-                  c->nmList.as<int>(), ctr, s);
+                  c->nmList.as<int>(), ctr, md0, s);
     cudaEventRecord(c->kev[9], s);
     cudaEventRecord(c->ev[2], s);
+    MDMC_CHECK(c, cudaGetLastError());
 
     // ---- repair: fixManifoldTwins, then the splitter ---------------------------
-    launchReconnect(g, iso, c->table.as<Bucket>(), c->nmList.as<int>(), ctr, c->he.as<int4>(), c->pos.as<float>(), status, s);
+    launchReconnect(g, iso, c->table.as<Bucket>(), c->nmList.as<int>(), ctr, c->he.as<int4>(), c->pos.as<float>(), md0,
+                    status, s);
     MDMC_CHECK(c, cudaGetLastError());
     int64_t iterations = 0;
     if (c->opt.split_non_manifold_halfedges) {
@@ -570,16 +605,16 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
         MDMC_CHECK(c, c->fans.ensure(sizeof(int) * (size_t)c->V));
         MDMC_CHECK(c, cudaMemsetAsync(c->isKey.p, 0, (size_t)c->H, s));
         MDMC_CHECK(c, cudaMemsetAsync(c->fans.p, 0, sizeof(int) * (size_t)c->V, s));
-        launchDetectFans(c->he.as<int4>(), (int)c->H, c->isKey.as<uint8_t>(), c->fans.as<int>(), c->vflags.as<uint8_t>(),
-                         (int)c->V, ctr, status, s);
+        launchDetectFans(c->he.as<int4>(), MeshDims{(int)c->V, (int)c->F, (int)c->H}, c->isKey.as<uint8_t>(),
+                         c->fans.as<int>(), c->vflags.as<uint8_t>(), ctr, status, s);
     }
     cudaEventRecord(c->ev[4], s);
 
     // ---- outputs and statistics -------------------------------------------------
     MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)c->F));
     MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)c->V));
-    launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), (int)c->F, (int)c->H, (int)c->V, c->table.as<Bucket>(),
-                 c->cap, c->quads.as<int4>(), c->vertexHE.as<int>(), ctr, s);
+    launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), MeshDims{(int)c->V, (int)c->F, (int)c->H},
+                 c->table.as<Bucket>(), c->cap, c->quads.as<int4>(), c->vertexHE.as<int>(), ctr, status, s);
     cudaEventRecord(c->ev[5], s);
     MDMC_CHECK(c, cudaGetLastError());
     MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
@@ -594,15 +629,18 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->stats.split_iterations = iterations;
     c->stats.anomalies = (int64_t)hc.status;
     float ms[5] = {0, 0, 0, 0, 0};
-    for (int k = 0; k < 4; ++k) cudaEventElapsedTime(&ms[k], c->ev[k], c->ev[k + 1]);
-    cudaEventElapsedTime(&ms[4], c->ev[0], c->ev[5]);
+    for (int k = 0; k < 4; ++k)
+        if (cudaEventElapsedTime(&ms[k], c->ev[k], c->ev[k + 1]) != cudaSuccess) ms[k] = 0.f;
+    if (cudaEventElapsedTime(&ms[4], c->ev[0], c->ev[5]) != cudaSuccess) ms[4] = 0.f;
     c->stats.ms_dmc = ms[0];
     c->stats.ms_halfedge = ms[1];
     c->stats.ms_repair = ms[2];
     c->stats.ms_detect = ms[3];
     c->stats.ms_total = ms[4];
     float km[5] = {0, 0, 0, 0, 0};
-    for (int k = 0; k < 5; ++k) cudaEventElapsedTime(&km[k], c->kev[2 * k], c->kev[2 * k + 1]);
+    for (int k = 0; k < 5; ++k)
+        if (cudaEventElapsedTime(&km[k], c->kev[2 * k], c->kev[2 * k + 1]) != cudaSuccess) km[k] = 0.f;
+    (void)cudaGetLastError();  // elapsed-time queries leave no error behind
     c->stats.ms_refine = km[0];
     c->stats.ms_count = km[1];
     c->stats.ms_emit = km[2];

@@ -192,7 +192,8 @@ __device__ void emitCell(const GridView& g, int x, int y, int z, float iso, bool
 __global__ void __launch_bounds__(256) kRowEmit(GridView g, float iso, int surfaceIteration,
                                                 const int4* __restrict__ rowOffsets, int numRows,
                                                 ActiveCell* __restrict__ act, float* __restrict__ pos,
-                                                float* __restrict__ nrm) {
+                                                float* __restrict__ nrm, int numActive, int numVertices,
+                                                uint32_t* status) {
     __shared__ uint64_t table[256];
     stageTable(table);
     const int lane = threadIdx.x & 31;
@@ -220,9 +221,14 @@ __global__ void __launch_bounds__(256) kRowEmit(GridView g, float iso, int surfa
         }
         const int vTot = __shfl_sync(0xffffffffu, vInc, 31);
         const int qTot = __shfl_sync(0xffffffffu, qInc, 31);
-        if (active)
-            emitCell(g, x, y, z, iso, surfaceIteration != 0, s, cc, vRun + vInc - cc.nv, qRun + qInc - cc.nq, act,
-                     aRun + __popc(ballot & ltMask), pos, nrm);
+        if (active) {
+            const int aIdx = aRun + __popc(ballot & ltMask), vIdx = vRun + vInc - cc.nv;
+            // the counts of the first pass bound every write of this one
+            if (aIdx < numActive && vIdx + cc.nv <= numVertices)
+                emitCell(g, x, y, z, iso, surfaceIteration != 0, s, cc, vIdx, qRun + qInc - cc.nq, act, aIdx, pos, nrm);
+            else
+                atomicOr(status, kStatusCountMismatch);
+        }
         aRun += __popc(ballot);
         vRun += vTot;
         qRun += qTot;
@@ -230,9 +236,11 @@ __global__ void __launch_bounds__(256) kRowEmit(GridView g, float iso, int surfa
 }
 
 void launchRowEmit(const GridView& g, float iso, int surfaceIteration, const int4* rowOffsets, int numRows,
-                   ActiveCell* act, float* pos, float* nrm, cudaStream_t s) {
+                   ActiveCell* act, float* pos, float* nrm, int numActive, int numVertices, uint32_t* status,
+                   cudaStream_t s) {
     countLaunch();
-    kRowEmit<<<(numRows + 7) / 8, 256, 0, s>>>(g, iso, surfaceIteration, rowOffsets, numRows, act, pos, nrm);
+    kRowEmit<<<(numRows + 7) / 8, 256, 0, s>>>(g, iso, surfaceIteration, rowOffsets, numRows, act, pos, nrm, numActive,
+                                                numVertices, status);
 }
 
 // ---------------------------------------------------------------------------
@@ -272,7 +280,8 @@ __device__ __forceinline__ void cellsAroundEdge(int axis, int d[4][3], int e[4])
 
 __global__ void kQuads(const ActiveCell* __restrict__ act, int numActive, const int4* __restrict__ rowOffsets, int X,
                        int Y, Bucket* __restrict__ table, unsigned long long cap, int4* __restrict__ he,
-                       int* __restrict__ faceFirst, uint16_t* __restrict__ faceAttr, uint32_t* status) {
+                       int* __restrict__ faceFirst, uint16_t* __restrict__ faceAttr, int numQuads, int numVertices,
+                       uint32_t* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= numActive) return;
     const ActiveCell rec = act[i];
@@ -281,9 +290,9 @@ __global__ void kQuads(const ActiveCell* __restrict__ act, int numActive, const 
     const int y = (int)((rec.cell / (uint32_t)X) % (uint32_t)Y);
     const int z = (int)(rec.cell / ((uint32_t)X * (uint32_t)Y));
     int qi = rec.qbase;
-    const int other[3] = {1, 2, 4};  // corner at the far end of edges 0, 3, 8
     for (int axis = 0; axis < 3; ++axis) {
-        if (!(((cs ^ (cs >> (other[axis] == 1 ? 1 : (other[axis] == 2 ? 2 : 4)))) & 1))) continue;
+        // edges 0, 3, 8 run from corner 0 to corners 1, 2, 4
+        if (!((cs ^ (cs >> (1 << axis))) & 1)) continue;
         if (axis == 0 && !(y >= 1 && z >= 1)) continue;
         if (axis == 1 && !(x >= 1 && z >= 1)) continue;
         if (axis == 2 && !(x >= 1 && y >= 1)) continue;
@@ -309,6 +318,11 @@ __global__ void kQuads(const ActiveCell* __restrict__ act, int numActive, const 
             if (quad[slot] != -1) atomicOr(status, kStatusSlotConflict);
             quad[slot] = r2.vbase + t;
         }
+        if (qi >= numQuads || quad[0] < 0 || quad[1] < 0 || quad[2] < 0 || quad[3] < 0 || quad[0] >= numVertices ||
+            quad[1] >= numVertices || quad[2] >= numVertices || quad[3] >= numVertices) {
+            atomicOr(status, kStatusCountMismatch);
+            return;
+        }
         const int h0 = 4 * qi;
 #pragma unroll
         for (int k = 0; k < 4; ++k) he[h0 + k] = make_int4(quad[k], qi, h0 + ((k + 1) & 3), -1);
@@ -322,12 +336,12 @@ __global__ void kQuads(const ActiveCell* __restrict__ act, int numActive, const 
 }
 
 void launchQuads(const ActiveCell* act, int numActive, const int4* rowOffsets, int X, int Y, Bucket* table,
-                 unsigned long long cap, int4* he, int* faceFirst, uint16_t* faceAttr, uint32_t* status,
-                 cudaStream_t s) {
+                 unsigned long long cap, int4* he, int* faceFirst, uint16_t* faceAttr, int numQuads, int numVertices,
+                 uint32_t* status, cudaStream_t s) {
     if (numActive <= 0) return;
     countLaunch();
     kQuads<<<(numActive + 255) / 256, 256, 0, s>>>(act, numActive, rowOffsets, X, Y, table, cap, he, faceFirst,
-                                                   faceAttr, status);
+                                                   faceAttr, numQuads, numVertices, status);
 }
 
 }  // namespace mdmc

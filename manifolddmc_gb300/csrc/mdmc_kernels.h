@@ -38,45 +38,48 @@ struct SplitWork {
     int* vSlots;
     int* hNum;
     int* hSlots;
+    // sizes: copies (nv, nh, nf) and the mesh (V, H, F)
+    int nv, nh, nf;
+    int V, H, F;
 };
 
 void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int pad, cudaStream_t s);
 void launchRowCount(const GridView& g, float iso, int4* rowCounts, int numRows, cudaStream_t s);
 void launchRowEmit(const GridView& g, float iso, int surfaceIteration, const int4* rowOffsets, int numRows,
-                   ActiveCell* act, float* pos, float* nrm, cudaStream_t s);
+                   ActiveCell* act, float* pos, float* nrm, int numActive, int numVertices, uint32_t* status,
+                   cudaStream_t s);
 void launchQuads(const ActiveCell* act, int numActive, const int4* rowOffsets, int X, int Y, Bucket* table,
-                 unsigned long long cap, int4* he, int* faceFirst, uint16_t* faceAttr, uint32_t* status,
-                 cudaStream_t s);
+                 unsigned long long cap, int4* he, int* faceFirst, uint16_t* faceAttr, int numQuads, int numVertices,
+                 uint32_t* status, cudaStream_t s);
 
 void launchBuckets(Bucket* table, unsigned long long cap, int4* he, uint16_t* faceAttr, uint8_t* vflags,
-                   int connectTwins, int* nmList, DevCounters* ctr, cudaStream_t s);
-void launchInsertFaces(const int4* he, const int* faceFirst, int numFaces, Bucket* table, unsigned long long cap,
+                   int connectTwins, int* nmList, DevCounters* ctr, MeshDims md, cudaStream_t s);
+void launchInsertFaces(const int4* he, const int* faceFirst, MeshDims md, Bucket* table, unsigned long long cap,
                        uint32_t* status, cudaStream_t s);
 void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s);
 void launchReconnect(const GridView& g, float iso, const Bucket* table, const int* nmList, const DevCounters* ctr,
-                     int4* he, const float* pos, uint32_t* status, cudaStream_t s);
-void launchDetectFans(const int4* he, int numHalfedges, uint8_t* isKey, int* fans, uint8_t* vflags, int numVertices,
-                      DevCounters* ctr, uint32_t* status, cudaStream_t s);
-void launchOutput(const int4* he, const int* faceFirst, int numFaces, int numHalfedges, int numVertices,
-                  const Bucket* table, unsigned long long cap, int4* quads, int* vertexHE, DevCounters* ctr,
-                  cudaStream_t s);
+                     int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s);
+void launchDetectFans(const int4* he, MeshDims md, uint8_t* isKey, int* fans, uint8_t* vflags, DevCounters* ctr,
+                      uint32_t* status, cudaStream_t s);
+void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const Bucket* table, unsigned long long cap,
+                  int4* quads, int* vertexHE, DevCounters* ctr, uint32_t* status, cudaStream_t s);
 
 void launchFlagNMFaces(const uint16_t* attr, int numFaces, int* flags, cudaStream_t s);
 void launchCompactNMFaces(const int* flags, const int* offsets, int numFaces, int* nmFaces, cudaStream_t s);
 void launchFillInt(int* p, int64_t n, int v, cudaStream_t s);
 void launchSplitCopy(const int* nmFaces, int n, const int4* he, const int* faceFirst, const uint16_t* faceAttr,
-                     const float* pos, const float* nrm, const SplitWork& w, cudaStream_t s);
+                     const float* pos, const float* nrm, const SplitWork& w, uint32_t* status, cudaStream_t s);
 void launchSplitMarkNM(const Bucket* table, const int* nmList, const DevCounters* ctr, const SplitWork& w,
                        uint32_t* status, cudaStream_t s);
 void launchSplitSubdivide(int n, const SplitWork& w, uint32_t* status, cudaStream_t s);
-void launchSplitCollapse(int nh, int nv, const SplitWork& w, uint32_t* status, cudaStream_t s);
-void launchSplitMerge(int nv, int nh, const SplitWork& w, uint32_t* status, cudaStream_t s);
-void launchSplitMergeHalfedges(int nh, const SplitWork& w, uint32_t* status, cudaStream_t s);
-void launchSplitMove(int nv, const GridView& g, float iso, const SplitWork& w, cudaStream_t s);
+void launchSplitCollapse(const SplitWork& w, uint32_t* status, cudaStream_t s);
+void launchSplitMerge(const SplitWork& w, uint32_t* status, cudaStream_t s);
+void launchSplitMergeHalfedges(const SplitWork& w, uint32_t* status, cudaStream_t s);
+void launchSplitMove(const GridView& g, float iso, const SplitWork& w, cudaStream_t s);
 void launchSplitFlagAppends(int count, const uint32_t* fl, const int* c2o, int* out, cudaStream_t s);
-void launchSplitCopyBack(int nv, int nh, int nf, const SplitWork& w, const int* appV, const int* appH,
-                         const int* appF, int V, int H, int F, float* pos, float* nrm, int4* he, int* faceFirst,
-                         uint16_t* faceAttr, cudaStream_t s);
+void launchSplitCopyBack(const SplitWork& w, const int* appV, const int* appH, const int* appF, int V2, int H2, int F2,
+                         float* pos, float* nrm, int4* he, int* faceFirst, uint16_t* faceAttr, uint32_t* status,
+                         cudaStream_t s);
 void launchSplitResetMaps(int n, const int* nmFaces, const SplitWork& w, cudaStream_t s);
 
 }  // namespace mdmc

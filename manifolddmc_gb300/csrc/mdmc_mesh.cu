@@ -44,7 +44,7 @@ __device__ __forceinline__ void blockAddTo(unsigned long long* dst, T v) {
 // refreshFaceFlagsGPU / refresh{NonManifold,Weird,Boundary}Flags.  Buckets
 // with at least four ids go to nmList (isHashTableEntryNonManifold).
 __global__ void kBuckets(Bucket* __restrict__ table, unsigned long long cap, int4* __restrict__ he, uint16_t* faceAttr,
-                         uint8_t* vflags, int connectTwins, int* __restrict__ nmList, DevCounters* ctr) {
+                         uint8_t* vflags, int connectTwins, int* __restrict__ nmList, DevCounters* ctr, MeshDims md) {
     int nE = 0, nE3 = 0, nE4 = 0;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap;
          i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -63,10 +63,26 @@ __global__ void kBuckets(Bucket* __restrict__ table, unsigned long long cap, int
             int4 ids = make_int4(e[0], e[1], e[2], e[3]);
             *reinterpret_cast<int4*>(&table[i].ids[0]) = ids;
         }
+        bool ok = true;
+        for (int k = 0; k < n; ++k) {
+            ok = ok && inb(e[k], md.H);
+            if (ok) {
+                const int4 h = he[e[k]];
+                ok = inb(h.x, md.V) && inb(h.y, md.F);
+            }
+        }
+        if (!ok) {
+            atomicOr(&ctr->status, kStatusBadIndex);
+            continue;
+        }
         ++nE;
         if (count == 3) ++nE3;
         if (count == 4) ++nE4;
-        if (count >= 4) nmList[atomicAdd(&ctr->nmBuckets, 1ULL)] = (int)i;
+        if (count >= 4) {
+            const unsigned long long slot = atomicAdd(&ctr->nmBuckets, 1ULL);
+            if (slot < (unsigned long long)(md.H / 4 + 1)) nmList[slot] = (int)i;
+            else atomicOr(&ctr->status, kStatusBadIndex);
+        }
         if (connectTwins) {
             if (count == 2) {
                 setTwin(he, e[0], e[1]);
@@ -103,22 +119,26 @@ __global__ void kBuckets(Bucket* __restrict__ table, unsigned long long cap, int
 }
 
 void launchBuckets(Bucket* table, unsigned long long cap, int4* he, uint16_t* faceAttr, uint8_t* vflags,
-                   int connectTwins, int* nmList, DevCounters* ctr, cudaStream_t s) {
+                   int connectTwins, int* nmList, DevCounters* ctr, MeshDims md, cudaStream_t s) {
     unsigned long long blocks = (cap + 255) / 256;
     if (blocks > 152ULL * 16) blocks = 152ULL * 16;
     if (blocks == 0) blocks = 1;
     countLaunch();
-    kBuckets<<<(unsigned)blocks, 256, 0, s>>>(table, cap, he, faceAttr, vflags, connectTwins, nmList, ctr);
+    kBuckets<<<(unsigned)blocks, 256, 0, s>>>(table, cap, he, faceAttr, vflags, connectTwins, nmList, ctr, md);
 }
 
 // refreshHashTableGPU, D/Halfedges/HalfedgeMesh.cu:62-90
-__global__ void kInsertFaces(const int4* __restrict__ he, const int* __restrict__ faceFirst, int numFaces,
+__global__ void kInsertFaces(const int4* __restrict__ he, const int* __restrict__ faceFirst, MeshDims md,
                              Bucket* table, unsigned long long cap, uint32_t* status) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= numFaces) return;
+    if (f >= md.F) return;
     int h = faceFirst[f];
     int q[4], hs[4];
     for (int i = 0; i < 4; ++i) {
+        if (!inb(h, md.H)) {
+            atomicOr(status, kStatusBadIndex);
+            return;
+        }
         int4 e = he[h];
         q[i] = e.x;
         hs[i] = h;
@@ -127,11 +147,11 @@ __global__ void kInsertFaces(const int4* __restrict__ he, const int* __restrict_
     for (int i = 0; i < 4; ++i) edgeInsert(table, cap, q[i], q[(i + 1) & 3], hs[i], status);
 }
 
-void launchInsertFaces(const int4* he, const int* faceFirst, int numFaces, Bucket* table, unsigned long long cap,
+void launchInsertFaces(const int4* he, const int* faceFirst, MeshDims md, Bucket* table, unsigned long long cap,
                        uint32_t* status, cudaStream_t s) {
-    if (numFaces <= 0) return;
+    if (md.F <= 0) return;
     countLaunch();
-    kInsertFaces<<<(numFaces + 255) / 256, 256, 0, s>>>(he, faceFirst, numFaces, table, cap, status);
+    kInsertFaces<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, table, cap, status);
 }
 
 // face attributes: clearPatternFlags + unsetNonManifoldFlag (HalfedgeMesh.cu:1050-1055)
@@ -160,10 +180,24 @@ __device__ __forceinline__ F3 nudge(int it) {
 __device__ __forceinline__ F3 loadP(const float* pos, int v) { return f3(pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]); }
 
 __global__ void kReconnect(GridView g, float iso, const Bucket* __restrict__ table, const int* __restrict__ nmList,
-                           const DevCounters* ctr, int4* he, const float* __restrict__ pos, uint32_t* status) {
-    const int count = (int)ctr->nmBuckets;
+                           const DevCounters* ctr, int4* he, const float* __restrict__ pos, MeshDims md,
+                           uint32_t* status) {
+    const int count = min((int)ctr->nmBuckets, md.H / 4 + 1);
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < count; w += gridDim.x * blockDim.x) {
         const Bucket b = table[nmList[w]];
+        // every id, its next, next.next and their origins must be in range
+        bool ok = true;
+        for (int k = 0; k < 4 && ok; ++k) {
+            int h = b.ids[k];
+            for (int d = 0; d < 3 && ok; ++d) {
+                ok = inb(h, md.H) && inb(he[h].x, md.V);
+                if (ok) h = he[h].z;
+            }
+        }
+        if (!ok) {
+            atomicOr(status, kStatusBadIndex);
+            continue;
+        }
         const int4 h0 = he[b.ids[0]];
         const int n0 = h0.x, n1 = he[h0.z].x;
         F3 p0 = loadP(pos, n0), p1 = loadP(pos, n1);
@@ -262,38 +296,48 @@ __global__ void kReconnect(GridView g, float iso, const Bucket* __restrict__ tab
 }
 
 void launchReconnect(const GridView& g, float iso, const Bucket* table, const int* nmList, const DevCounters* ctr,
-                     int4* he, const float* pos, uint32_t* status, cudaStream_t s) {
+                     int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s) {
     countLaunch();
-    kReconnect<<<152 * 2, 128, 0, s>>>(g, iso, table, nmList, ctr, he, pos, status);
+    kReconnect<<<152 * 2, 128, 0, s>>>(g, iso, table, nmList, ctr, he, pos, md, status);
 }
 
 // ---------------------------------------------------------------------------
 // detectNonManifoldVertices, D/PostProcesses/ManifoldCreator.cu:319-536
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int stepCW(const int4* he, int h) {
+// stepping around a vertex; any id outside the arrays ends the walk
+__device__ __forceinline__ int stepCW(const int4* he, int h, int H) {
     const int t = he[h].w;
-    return t != -1 ? he[t].z : -1;
+    if (t == -1) return -1;
+    if (!inb(t, H)) return -2;
+    const int n = he[t].z;
+    return inb(n, H) ? n : -2;
 }
-__device__ __forceinline__ int stepCCW(const int4* he, int h) {
-    const int p = he[he[he[h].z].z].z;
+__device__ __forceinline__ int stepCCW(const int4* he, int h, int H) {
+    int p = h;
+    for (int i = 0; i < 3; ++i) {
+        p = he[p].z;
+        if (!inb(p, H)) return -2;
+    }
     const int t = he[p].w;
-    return t != -1 ? t : -1;
+    if (t == -1) return -1;
+    return inb(t, H) ? t : -2;
 }
-__device__ __forceinline__ int fanWalk(const int4* he, int start, bool cw, uint32_t* status) {
+__device__ __forceinline__ int fanWalk(const int4* he, int start, bool cw, int H, uint32_t* status) {
     const int origin = he[start].x;
     int result = start;
-    int cur = cw ? stepCW(he, start) : stepCCW(he, start);
+    int cur = cw ? stepCW(he, start, H) : stepCCW(he, start, H);
     int guard = 0;
-    while (cur != -1) {
+    while (cur >= 0) {
         if (cur == result) break;
         if (origin != he[cur].x) break;
         if (cur < result) result = cur;
-        cur = cw ? stepCW(he, cur) : stepCCW(he, cur);
+        cur = cw ? stepCW(he, cur, H) : stepCCW(he, cur, H);
         if (++guard > 4096) {
             atomicOr(status, kStatusWalkLimit);
             break;
         }
     }
+    if (cur == -2) atomicOr(status, kStatusBadIndex);
     return result;
 }
 
@@ -301,18 +345,22 @@ __device__ __forceinline__ int fanWalk(const int4* he, int start, bool cw, uint3
 // halfedge it was found from, so "distinct (origin, key) pairs per origin"
 // (the reference's sort + unique) equals "halfedges named as key by some
 // halfedge, per origin".  No sort is needed.
-__global__ void kFanKeys(const int4* __restrict__ he, int numHalfedges, uint8_t* __restrict__ isKey, uint32_t* status) {
+__global__ void kFanKeys(const int4* __restrict__ he, MeshDims md, uint8_t* __restrict__ isKey, uint32_t* status) {
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= numHalfedges) return;
-    const int k = min(h, min(fanWalk(he, h, true, status), fanWalk(he, h, false, status)));
+    if (h >= md.H) return;
+    const int k = min(h, min(fanWalk(he, h, true, md.H, status), fanWalk(he, h, false, md.H, status)));
     isKey[k] = 1;
 }
 
-__global__ void kFanCount(const int4* __restrict__ he, int numHalfedges, const uint8_t* __restrict__ isKey,
-                          int* __restrict__ fans) {
+__global__ void kFanCount(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ isKey,
+                          int* __restrict__ fans, uint32_t* status) {
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= numHalfedges) return;
-    if (isKey[h]) atomicAdd(&fans[he[h].x], 1);
+    if (h >= md.H) return;
+    if (isKey[h]) {
+        const int v = he[h].x;
+        if (inb(v, md.V)) atomicAdd(&fans[v], 1);
+        else atomicOr(status, kStatusBadIndex);
+    }
 }
 
 __global__ void kFanFlags(const int* __restrict__ fans, uint8_t* __restrict__ vflags, int numVertices, DevCounters* ctr) {
@@ -331,17 +379,17 @@ __global__ void kFanFlags(const int* __restrict__ fans, uint8_t* __restrict__ vf
     blockAddTo(&ctr->nmVertices, nm);
 }
 
-void launchDetectFans(const int4* he, int numHalfedges, uint8_t* isKey, int* fans, uint8_t* vflags, int numVertices,
-                      DevCounters* ctr, uint32_t* status, cudaStream_t s) {
-    if (numHalfedges > 0) {
+void launchDetectFans(const int4* he, MeshDims md, uint8_t* isKey, int* fans, uint8_t* vflags, DevCounters* ctr,
+                      uint32_t* status, cudaStream_t s) {
+    if (md.H > 0) {
         countLaunch();
-        kFanKeys<<<(numHalfedges + 255) / 256, 256, 0, s>>>(he, numHalfedges, isKey, status);
+        kFanKeys<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, isKey, status);
         countLaunch();
-        kFanCount<<<(numHalfedges + 255) / 256, 256, 0, s>>>(he, numHalfedges, isKey, fans);
+        kFanCount<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, isKey, fans, status);
     }
-    if (numVertices > 0) {
+    if (md.V > 0) {
         countLaunch();
-        kFanFlags<<<(numVertices + 255) / 256, 256, 0, s>>>(fans, vflags, numVertices, ctr);
+        kFanFlags<<<(md.V + 255) / 256, 256, 0, s>>>(fans, vflags, md.V, ctr);
     }
 }
 
@@ -349,32 +397,40 @@ void launchDetectFans(const int4* he, int numHalfedges, uint8_t* isKey, int* fan
 // output pass: face vertex quads, getNumQuadsWithNonManifoldEdges, and the
 // smallest outgoing halfedge of every vertex
 // ---------------------------------------------------------------------------
-__global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__ faceFirst, int numFaces,
+__global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__ faceFirst, MeshDims md,
                             const Bucket* __restrict__ table, unsigned long long cap, int4* __restrict__ quads,
                             DevCounters* ctr) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     int cnt = -1;
-    if (f < numFaces) {
+    if (f < md.F) {
         int h = faceFirst[f];
-        int q[4];
-        for (int i = 0; i < 4; ++i) {
-            int4 e = he[h];
-            q[i] = e.x;
-            h = e.z;
+        int q[4] = {-1, -1, -1, -1};
+        bool ok = true;
+        for (int i = 0; i < 4 && ok; ++i) {
+            ok = inb(h, md.H);
+            if (ok) {
+                const int4 e = he[h];
+                q[i] = e.x;
+                h = e.z;
+            }
         }
         quads[f] = make_int4(q[0], q[1], q[2], q[3]);
-        cnt = 0;
-        for (int i = 0; i < 4; ++i)
-            if (edgeValence(table, cap, q[i], q[(i + 1) & 3]) > 2) ++cnt;
+        if (ok) {
+            cnt = 0;
+            for (int i = 0; i < 4; ++i)
+                if (edgeValence(table, cap, q[i], q[(i + 1) & 3]) > 2) ++cnt;
+        } else {
+            atomicOr(&ctr->status, kStatusBadIndex);
+        }
     }
     for (int k = 1; k <= 4; ++k) blockAddTo(&ctr->quadsNM[k], cnt == k ? 1 : 0);
 }
 
-__global__ void kVertexHalfedge(const int4* __restrict__ he, int numHalfedges, int* __restrict__ vertexHE) {
+__global__ void kVertexHalfedge(const int4* __restrict__ he, MeshDims md, int* __restrict__ vertexHE) {
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h < numHalfedges) {
+    if (h < md.H) {
         const int v = he[h].x;
-        if (v >= 0) atomicMin(&vertexHE[v], h);
+        if (inb(v, md.V)) atomicMin(&vertexHE[v], h);
     }
 }
 
@@ -383,22 +439,22 @@ __global__ void kVertexHalfedgeFix(int* vertexHE, int numVertices) {
     if (v < numVertices && vertexHE[v] == 0x7F7F7F7F) vertexHE[v] = -1;
 }
 
-void launchOutput(const int4* he, const int* faceFirst, int numFaces, int numHalfedges, int numVertices,
-                  const Bucket* table, unsigned long long cap, int4* quads, int* vertexHE, DevCounters* ctr,
-                  cudaStream_t s) {
-    if (numFaces > 0) {
+void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const Bucket* table, unsigned long long cap,
+                  int4* quads, int* vertexHE, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
+    (void)status;
+    if (md.F > 0) {
         countLaunch();
-        kFaceOutput<<<(numFaces + 255) / 256, 256, 0, s>>>(he, faceFirst, numFaces, table, cap, quads, ctr);
+        kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, table, cap, quads, ctr);
     }
-    if (numVertices > 0) {
+    if (md.V > 0) {
         // 0x7F7F7F7F marks "none"; atomicMin lowers it
-        cudaMemsetAsync(vertexHE, 0x7F, sizeof(int) * (size_t)numVertices, s);
-        if (numHalfedges > 0) {
+        cudaMemsetAsync(vertexHE, 0x7F, sizeof(int) * (size_t)md.V, s);
+        if (md.H > 0) {
             countLaunch();
-            kVertexHalfedge<<<(numHalfedges + 255) / 256, 256, 0, s>>>(he, numHalfedges, vertexHE);
+            kVertexHalfedge<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, vertexHE);
         }
         countLaunch();
-        kVertexHalfedgeFix<<<(numVertices + 255) / 256, 256, 0, s>>>(vertexHE, numVertices);
+        kVertexHalfedgeFix<<<(md.V + 255) / 256, 256, 0, s>>>(vertexHE, md.V);
     }
 }
 

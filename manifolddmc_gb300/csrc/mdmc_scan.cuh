@@ -77,7 +77,7 @@ __device__ T blockExclusive(T v, T& total) {
 }
 
 template <typename T>
-__global__ void kScanReduce(const T* __restrict__ in, int64_t n, T* __restrict__ tileSums) {
+__global__ void __launch_bounds__(kScanThreads) kScanReduce(const T* __restrict__ in, int64_t n, T* __restrict__ tileSums) {
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     T acc = ScanOps<T>::zero();
 #pragma unroll
@@ -90,31 +90,31 @@ __global__ void kScanReduce(const T* __restrict__ in, int64_t n, T* __restrict__
     if (threadIdx.x == 0) tileSums[blockIdx.x] = total;
 }
 
-// one block: exclusive scan of the tile sums in place, total -> tileSums[numTiles]
+// one block: exclusive scan of the tile sums in place, total -> tileSums[numTiles].
+// Chunks of 1024 sums are scanned one after the other with a running carry,
+// one value per thread and chunk (the block launches with 1024 threads, so a
+// thread may hold at most 64 registers).
 template <typename T>
-__global__ void kScanTiles(T* tileSums, int numTiles) {
-    constexpr int per = kScanMaxTiles / 1024;
-    T vals[per];
-    T acc = ScanOps<T>::zero();
-#pragma unroll
-    for (int k = 0; k < per; ++k) {
-        int i = threadIdx.x * per + k;
-        vals[k] = i < numTiles ? tileSums[i] : ScanOps<T>::zero();
-        acc = ScanOps<T>::add(acc, vals[k]);
+__global__ void __launch_bounds__(1024) kScanTiles(T* tileSums, int numTiles) {
+    __shared__ T carryShared;
+    if (threadIdx.x == 0) carryShared = ScanOps<T>::zero();
+    __syncthreads();
+    for (int base = 0; base < numTiles; base += 1024) {
+        const int i = base + threadIdx.x;
+        const T v = i < numTiles ? tileSums[i] : ScanOps<T>::zero();
+        T total;
+        const T exc = blockExclusive(v, total);
+        const T carry = carryShared;
+        if (i < numTiles) tileSums[i] = ScanOps<T>::add(carry, exc);
+        __syncthreads();
+        if (threadIdx.x == 0) carryShared = ScanOps<T>::add(carry, total);
+        __syncthreads();
     }
-    T total;
-    T run = blockExclusive(acc, total);
-#pragma unroll
-    for (int k = 0; k < per; ++k) {
-        int i = threadIdx.x * per + k;
-        if (i < numTiles) tileSums[i] = run;
-        run = ScanOps<T>::add(run, vals[k]);
-    }
-    if (threadIdx.x == 0) tileSums[numTiles] = total;
+    if (threadIdx.x == 0) tileSums[numTiles] = carryShared;
 }
 
 template <typename T>
-__global__ void kScanApply(const T* __restrict__ in, int64_t n, const T* __restrict__ tileSums,
+__global__ void __launch_bounds__(kScanThreads) kScanApply(const T* __restrict__ in, int64_t n, const T* __restrict__ tileSums,
                            T* __restrict__ out) {
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     // each thread owns kScanItems consecutive elements

@@ -56,12 +56,20 @@ void launchFillInt(int* p, int64_t n, int v, cudaStream_t s) {
 // reference keeps whichever copy wrote last; all copies hold the same data).
 __global__ void kCopyOut(const int* __restrict__ nmFaces, int n, const int4* __restrict__ he,
                          const int* __restrict__ faceFirst, const uint16_t* __restrict__ faceAttr,
-                         const float* __restrict__ pos, const float* __restrict__ nrm, SplitWork w) {
+                         const float* __restrict__ pos, const float* __restrict__ nrm, SplitWork w, uint32_t* status) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int f = nmFaces[k];
+    if (!inb(f, w.F)) {
+        atomicOr(status, kStatusBadIndex);
+        return;
+    }
     int h = faceFirst[f];
     for (int i = 0; i < 4; ++i) {
+        if (!inb(h, w.H) || !inb(he[h].x, w.V)) {
+            atomicOr(status, kStatusBadIndex);
+            return;
+        }
         const int4 e = he[h];
         const int c = 4 * k + i;
         const int v = e.x;
@@ -85,10 +93,14 @@ __global__ void kCopyOut(const int* __restrict__ nmFaces, int n, const int4* __r
 }
 
 // updateWorkingCopyHalfedges (:463-505); twins outside the copy become -twin-2
-__global__ void kUpdateRefs(int n, SplitWork w) {
+__global__ void kUpdateRefs(int n, SplitWork w, uint32_t* status) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= 4 * n) return;
     int4 e = w.he[c];
+    if (!inb(e.x, w.V) || !inb(e.y, w.F) || !inb(e.z, w.H) || (e.w >= 0 && !inb(e.w, w.H))) {
+        atomicOr(status, kStatusBadIndex);
+        return;
+    }
     e.x = w.vO2C[e.x];
     e.y = w.fO2C[e.y];
     e.z = w.hO2C[e.z];
@@ -96,18 +108,20 @@ __global__ void kUpdateRefs(int n, SplitWork w) {
         const int t = w.hO2C[e.w];
         e.w = (t == kNone) ? -e.w - 2 : t;
     }
+    if (!inb(e.x, w.nv) || !inb(e.y, w.nf) || !inb(e.z, w.nh)) atomicOr(status, kStatusBadIndex);
     w.he[c] = e;
 }
 
 // markHalfedgesAsNonManifold (:527-555)
 __global__ void kMarkNM(const Bucket* __restrict__ table, const int* __restrict__ nmList, const DevCounters* ctr,
                         SplitWork w, uint32_t* status) {
-    const int count = (int)ctr->nmBuckets;
+    const int count = min((int)ctr->nmBuckets, w.H / 4 + 1);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const Bucket b = table[nmList[i]];
         for (int k = 0; k < 4; ++k) {
-            const int c = w.hO2C[b.ids[k]];
-            if (c < 0) {
+            const int id = b.ids[k];
+            const int c = inb(id, w.H) ? w.hO2C[id] : kNone;
+            if (!inb(c, w.nh) || !inb(w.he[c].x, w.nv)) {
                 atomicOr(status, kStatusBadTwin);
                 continue;
             }
@@ -127,6 +141,10 @@ __global__ void kSubdivide(int n, SplitWork w, uint32_t* status) {
     int hid[4], vid[4];
     int h = w.first[k];
     for (int i = 0; i < 4; ++i) {
+        if (!inb(h, w.nh) || !inb(w.he[h].x, w.nv)) {
+            atomicOr(status, kStatusBadIndex);
+            return;
+        }
         hid[i] = h;
         const int4 e = w.he[h];
         vid[i] = e.x;
@@ -185,25 +203,29 @@ __global__ void kSubdivide(int n, SplitWork w, uint32_t* status) {
         const int ao = w.hC2O[a], bo = w.hC2O[b];
         w.hC2O[a] = bo;
         w.hC2O[b] = ao;
-        if (ao != kNone && bo == kNone) w.hO2C[ao] = b;
+        if (ao != kNone && bo == kNone && inb(ao, w.H)) w.hO2C[ao] = b;
         else atomicOr(status, kStatusMappingSwap);
     }
 }
 
 // DeviceMergeList::mark (:749-765); partner slots are sorted afterwards
-__device__ __forceinline__ void markPartner(int* num, int* slots, int a, int b, uint32_t* status) {
+__device__ __forceinline__ void markPartner(int* num, int* slots, int count, int a, int b, uint32_t* status) {
+    if (!inb(a, count) || !inb(b, count)) {
+        atomicOr(status, kStatusBadIndex);
+        return;
+    }
     const int idx = atomicAdd(&num[a], 1);
     if (idx - 1 < 4) slots[4 * a + idx - 1] = b;
     if (idx > 2) atomicOr(status, kStatusPartnerOverflow);
 }
 
 // performCollapseNonManifoldHalfedges + collapseHalfedge (:767-868)
-__global__ void kCollapse(int nh, SplitWork w, uint32_t* status) {
+__global__ void kCollapse(SplitWork w, uint32_t* status) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nh) return;
+    if (t >= w.nh) return;
     if (!(w.hfl[t] & kNonManifold)) return;
     const int tw = w.he[t].w;
-    if (tw < 0) {
+    if (!inb(tw, w.nh)) {
         atomicOr(status, kStatusBadTwin);
         return;
     }
@@ -213,26 +235,35 @@ __global__ void kCollapse(int nh, SplitWork w, uint32_t* status) {
     f0[0] = t;
     f1[0] = tw;
     for (int i = 1; i < 4; ++i) {
+        if (!inb(cur.z, w.nh) || !inb(ctw.z, w.nh)) {
+            atomicOr(status, kStatusBadIndex);
+            return;
+        }
         f0[i] = cur.z;
         f1[4 - i] = ctw.z;
         cur = w.he[cur.z];
         ctw = w.he[ctw.z];
     }
+    const int fa = w.he[f0[0]].y, fb = w.he[f1[0]].y;
+    if (!inb(fa, w.nf) || !inb(fb, w.nf)) {
+        atomicOr(status, kStatusBadIndex);
+        return;
+    }
     for (int i = 0; i < 4; ++i) {
         atomicOr(&w.hfl[f0[i]], kRemove);
         atomicOr(&w.hfl[f1[i]], kRemove);
     }
-    atomicOr(&w.ffl[w.he[f0[0]].y], kRemove);
-    atomicOr(&w.ffl[w.he[f1[0]].y], kRemove);
+    atomicOr(&w.ffl[fa], kRemove);
+    atomicOr(&w.ffl[fb], kRemove);
     {
         const int a = w.he[f0[2]].x, b = w.he[f1[1]].x;
-        markPartner(w.vNum, w.vSlots, a, b, status);
-        markPartner(w.vNum, w.vSlots, b, a, status);
+        markPartner(w.vNum, w.vSlots, w.nv, a, b, status);
+        markPartner(w.vNum, w.vSlots, w.nv, b, a, status);
     }
     {
         const int a = w.he[f0[3]].x, b = w.he[f1[2]].x;
-        markPartner(w.vNum, w.vSlots, a, b, status);
-        markPartner(w.vNum, w.vSlots, b, a, status);
+        markPartner(w.vNum, w.vSlots, w.nv, a, b, status);
+        markPartner(w.vNum, w.vSlots, w.nv, b, a, status);
     }
     for (int i = 1; i < 4; ++i) {
         const int a = f0[i], b = f1[i];
@@ -241,10 +272,10 @@ __global__ void kCollapse(int nh, SplitWork w, uint32_t* status) {
             atomicOr(status, kStatusBadTwin);
             continue;
         }
-        markPartner(w.hNum, w.hSlots, a, bt, status);
-        markPartner(w.hNum, w.hSlots, bt, a, status);
-        markPartner(w.hNum, w.hSlots, b, at, status);
-        markPartner(w.hNum, w.hSlots, at, b, status);
+        markPartner(w.hNum, w.hSlots, w.nh, a, bt, status);
+        markPartner(w.hNum, w.hSlots, w.nh, bt, a, status);
+        markPartner(w.hNum, w.hSlots, w.nh, b, at, status);
+        markPartner(w.hNum, w.hSlots, w.nh, at, b, status);
     }
 }
 
@@ -264,7 +295,7 @@ __global__ void kSortPartners(int* num, int* slots, int count) {
 }
 
 // DeviceMergeList::getAllPartnersOf (:25-62): breadth-first closure, at most
-// 12 partners
+// 12 partners.  Slots only hold ids checked by markPartner.
 __device__ int closure(const int* num, const int* slots, int v, int out[12], uint32_t* status) {
     auto cnt = [&](int x) { return min(num[x], 5); };
     int np = cnt(v);
@@ -292,9 +323,9 @@ __device__ int closure(const int* num, const int* slots, int v, int out[12], uin
 
 // mergeVertices (:936-990); the survivor's normal receives the averaged
 // position, as in the reference (:989)
-__global__ void kMergeVertices(int nv, SplitWork w, uint32_t* status) {
+__global__ void kMergeVertices(SplitWork w, uint32_t* status) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nv) return;
+    if (v >= w.nv) return;
     int part[12];
     const int np = closure(w.vNum, w.vSlots, v, part, status);
     if (np <= 1) return;
@@ -323,11 +354,11 @@ __global__ void kMergeVertices(int nv, SplitWork w, uint32_t* status) {
 }
 
 // updateHalfedgeVertexIDs (:992-1019)
-__global__ void kUpdateOrigins(int nh, SplitWork w, uint32_t* status) {
+__global__ void kUpdateOrigins(SplitWork w, uint32_t* status) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nh) return;
+    if (t >= w.nh) return;
     const int v = w.he[t].x;
-    if (v < 0) return;
+    if (!inb(v, w.nv)) return;
     int part[12];
     const int np = closure(w.vNum, w.vSlots, v, part, status);
     if (np <= 1) return;
@@ -338,9 +369,9 @@ __global__ void kUpdateOrigins(int nh, SplitWork w, uint32_t* status) {
 
 // mergeHalfedges (:1021-1067): reads only removed partners' twins, which no
 // thread writes, so one pass is race-free
-__global__ void kMergeHalfedges(int nh, SplitWork w, uint32_t* status) {
+__global__ void kMergeHalfedges(SplitWork w, uint32_t* status) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nh) return;
+    if (t >= w.nh) return;
     if (w.hfl[t] & kRemove) return;
     int part[12];
     const int np = closure(w.hNum, w.hSlots, t, part, status);
@@ -348,7 +379,7 @@ __global__ void kMergeHalfedges(int nh, SplitWork w, uint32_t* status) {
     int valid = -1;
     for (int i = 0; i < np - 1; ++i) {
         const int tw = w.he[part[i]].w;
-        if (tw < 0) continue;
+        if (!inb(tw, w.nh)) continue;
         if (!(w.hfl[tw] & kRemove)) {
             valid = tw;
             break;
@@ -360,9 +391,9 @@ __global__ void kMergeHalfedges(int nh, SplitWork w, uint32_t* status) {
 }
 
 // performMoveVerticesToSurface (:1130-1160)
-__global__ void kMoveVertices(int nv, GridView g, float iso, SplitWork w) {
+__global__ void kMoveVertices(GridView g, float iso, SplitWork w) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nv) return;
+    if (v >= w.nv) return;
     if (w.vfl[v] & kRemove) return;
     const F3 p = f3(w.pos[3 * v], w.pos[3 * v + 1], w.pos[3 * v + 2]);
     int idx[3];
@@ -387,56 +418,76 @@ __global__ void kFlagAppends(int count, const uint32_t* __restrict__ fl, const i
     if (i < count) out[i] = (!(fl[i] & kRemove) && c2o[i] == kNone) ? 1 : 0;
 }
 
-// copyVerticesBack / copyHalfedgesBack / copyFacesBack (:1176-1260)
-__global__ void kCopyBackVertices(int nv, SplitWork w, const int* __restrict__ app, int V, float* pos, float* nrm) {
+// copyVerticesBack / copyHalfedgesBack / copyFacesBack (:1176-1260); V2, H2
+// and F2 are the mesh sizes after the appends
+__global__ void kCopyBackVertices(SplitWork w, const int* __restrict__ app, int V2, float* pos, float* nrm,
+                                  uint32_t* status) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nv) return;
+    if (v >= w.nv) return;
     if (w.vfl[v] & kRemove) return;
     int o = w.vC2O[v];
     if (o == kNone) {
-        o = V + app[v];
+        o = w.V + app[v];
         w.vC2O[v] = o;
+    }
+    if (!inb(o, V2)) {
+        atomicOr(status, kStatusBadIndex);
+        return;
     }
     for (int a = 0; a < 3; ++a) {
         pos[3 * (int64_t)o + a] = w.pos[3 * v + a];
         nrm[3 * (int64_t)o + a] = w.nrm[3 * v + a];
     }
 }
-__global__ void kAssignHalfedges(int nh, SplitWork w, const int* __restrict__ app, int H) {
+__global__ void kAssignHalfedges(SplitWork w, const int* __restrict__ app) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nh) return;
+    if (t >= w.nh) return;
     if (w.hfl[t] & kRemove) return;
-    if (w.hC2O[t] == kNone) w.hC2O[t] = H + app[t];
+    if (w.hC2O[t] == kNone) w.hC2O[t] = w.H + app[t];
 }
-__global__ void kCopyBackFaces(int nf, SplitWork w, const int* __restrict__ app, int F, int* faceFirst,
-                               uint16_t* faceAttr) {
+__global__ void kCopyBackFaces(SplitWork w, const int* __restrict__ app, int H2, int F2, int* faceFirst,
+                               uint16_t* faceAttr, uint32_t* status) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= nf) return;
+    if (f >= w.nf) return;
     if (w.ffl[f] & kRemove) return;
     int o = w.fC2O[f];
     if (o == kNone) {
-        o = F + app[f];
+        o = w.F + app[f];
         w.fC2O[f] = o;
     }
-    faceFirst[o] = w.hC2O[w.first[f]];
+    const int fh = w.first[f];
+    const int first = inb(fh, w.nh) ? w.hC2O[fh] : kNone;
+    if (!inb(o, F2) || !inb(first, H2)) {
+        atomicOr(status, kStatusBadIndex);
+        return;
+    }
+    faceFirst[o] = first;
     faceAttr[o] = w.attr[f];
 }
 // copyHalfedgesBack + updateHalfedgesBack (:1205-1295)
-__global__ void kCopyBackHalfedges(int nh, SplitWork w, int4* he) {
+__global__ void kCopyBackHalfedges(SplitWork w, int V2, int H2, int F2, int4* he, uint32_t* status) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nh) return;
+    if (t >= w.nh) return;
     if (w.hfl[t] & kRemove) return;
     int4 e = w.he[t];
     const int self = w.hC2O[t];
+    if (!inb(self, H2) || !inb(e.z, w.nh) || !inb(e.y, w.nf) || !inb(e.x, w.nv) || (e.w >= 0 && !inb(e.w, w.nh))) {
+        atomicOr(status, kStatusBadIndex);
+        return;
+    }
     e.z = w.hC2O[e.z];
     e.y = w.fC2O[e.y];
     e.x = w.vC2O[e.x];
     if (e.w < 0) {
         e.w = -e.w - 2;
-        if (e.w != -1) setTwinOut(he, e.w, self);
+        if (e.w != -1) {
+            if (inb(e.w, w.H)) setTwinOut(he, e.w, self);
+            else atomicOr(status, kStatusBadIndex);
+        }
     } else {
         e.w = w.hC2O[e.w];
     }
+    if (!inb(e.z, H2) || !inb(e.y, F2) || !inb(e.x, V2)) atomicOr(status, kStatusBadIndex);
     he[self] = e;
 }
 
@@ -444,22 +495,22 @@ __global__ void kCopyBackHalfedges(int nh, SplitWork w, int4* he) {
 __global__ void kResetMaps(int n, const int* __restrict__ nmFaces, SplitWork w) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= 4 * n) return;
-    w.vO2C[w.origV[c]] = 0x7FFFFFFF;
-    w.hO2C[w.origH[c]] = kNone;
-    if ((c & 3) == 0) w.fO2C[nmFaces[c >> 2]] = kNone;
+    if (inb(w.origV[c], w.V)) w.vO2C[w.origV[c]] = 0x7FFFFFFF;
+    if (inb(w.origH[c], w.H)) w.hO2C[w.origH[c]] = kNone;
+    if ((c & 3) == 0 && inb(nmFaces[c >> 2], w.F)) w.fO2C[nmFaces[c >> 2]] = kNone;
 }
 
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-static inline int nb(int64_t n) { return (int)((n + 255) / 256); }
+// blocks of `bs` threads covering n elements
+static inline int nb(int64_t n, int bs) { return (int)std::max<int64_t>((n + bs - 1) / bs, 1); }
 
 void launchSplitCopy(const int* nmFaces, int n, const int4* he, const int* faceFirst, const uint16_t* faceAttr,
-                     const float* pos, const float* nrm, const SplitWork& w, cudaStream_t s) {
-    countLaunch();
-    kCopyOut<<<nb(n), 256, 0, s>>>(nmFaces, n, he, faceFirst, faceAttr, pos, nrm, w);
-    countLaunch();
-    kUpdateRefs<<<nb(4 * (int64_t)n), 256, 0, s>>>(n, w);
+                     const float* pos, const float* nrm, const SplitWork& w, uint32_t* status, cudaStream_t s) {
+    countLaunch(2);
+    kCopyOut<<<nb(n, 256), 256, 0, s>>>(nmFaces, n, he, faceFirst, faceAttr, pos, nrm, w, status);
+    kUpdateRefs<<<nb(4 * (int64_t)n, 256), 256, 0, s>>>(n, w, status);
 }
 void launchSplitMarkNM(const Bucket* table, const int* nmList, const DevCounters* ctr, const SplitWork& w,
                        uint32_t* status, cudaStream_t s) {
@@ -468,51 +519,44 @@ void launchSplitMarkNM(const Bucket* table, const int* nmList, const DevCounters
 }
 void launchSplitSubdivide(int n, const SplitWork& w, uint32_t* status, cudaStream_t s) {
     countLaunch();
-    kSubdivide<<<nb(n), 128, 0, s>>>(n, w, status);
+    kSubdivide<<<nb(n, 128), 128, 0, s>>>(n, w, status);
 }
-void launchSplitCollapse(int nh, int nv, const SplitWork& w, uint32_t* status, cudaStream_t s) {
-    countLaunch();
-    kCollapse<<<nb(nh), 256, 0, s>>>(nh, w, status);
-    countLaunch();
-    kSortPartners<<<nb(nv), 256, 0, s>>>(w.vNum, w.vSlots, nv);
-    countLaunch();
-    kSortPartners<<<nb(nh), 256, 0, s>>>(w.hNum, w.hSlots, nh);
+void launchSplitCollapse(const SplitWork& w, uint32_t* status, cudaStream_t s) {
+    countLaunch(3);
+    kCollapse<<<nb(w.nh, 256), 256, 0, s>>>(w, status);
+    kSortPartners<<<nb(w.nv, 256), 256, 0, s>>>(w.vNum, w.vSlots, w.nv);
+    kSortPartners<<<nb(w.nh, 256), 256, 0, s>>>(w.hNum, w.hSlots, w.nh);
 }
-void launchSplitMerge(int nv, int nh, const SplitWork& w, uint32_t* status, cudaStream_t s) {
-    countLaunch();
-    kMergeVertices<<<nb(nv), 128, 0, s>>>(nv, w, status);
-    countLaunch();
-    kUpdateOrigins<<<nb(nh), 128, 0, s>>>(nh, w, status);
+void launchSplitMerge(const SplitWork& w, uint32_t* status, cudaStream_t s) {
+    countLaunch(2);
+    kMergeVertices<<<nb(w.nv, 128), 128, 0, s>>>(w, status);
+    kUpdateOrigins<<<nb(w.nh, 128), 128, 0, s>>>(w, status);
 }
-void launchSplitMergeHalfedges(int nh, const SplitWork& w, uint32_t* status, cudaStream_t s) {
+void launchSplitMergeHalfedges(const SplitWork& w, uint32_t* status, cudaStream_t s) {
     countLaunch();
-    kMergeHalfedges<<<nb(nh), 128, 0, s>>>(nh, w, status);
+    kMergeHalfedges<<<nb(w.nh, 128), 128, 0, s>>>(w, status);
 }
-void launchSplitMove(int nv, const GridView& g, float iso, const SplitWork& w, cudaStream_t s) {
+void launchSplitMove(const GridView& g, float iso, const SplitWork& w, cudaStream_t s) {
     countLaunch();
-    kMoveVertices<<<nb(nv), 128, 0, s>>>(nv, g, iso, w);
+    kMoveVertices<<<nb(w.nv, 128), 128, 0, s>>>(g, iso, w);
 }
 void launchSplitFlagAppends(int count, const uint32_t* fl, const int* c2o, int* out, cudaStream_t s) {
-    if (count > 0) {
-        countLaunch();
-        kFlagAppends<<<nb(count), 256, 0, s>>>(count, fl, c2o, out);
-    }
+    if (count <= 0) return;
+    countLaunch();
+    kFlagAppends<<<nb(count, 256), 256, 0, s>>>(count, fl, c2o, out);
 }
-void launchSplitCopyBack(int nv, int nh, int nf, const SplitWork& w, const int* appV, const int* appH,
-                         const int* appF, int V, int H, int F, float* pos, float* nrm, int4* he, int* faceFirst,
-                         uint16_t* faceAttr, cudaStream_t s) {
-    countLaunch();
-    kCopyBackVertices<<<nb(nv), 256, 0, s>>>(nv, w, appV, V, pos, nrm);
-    countLaunch();
-    kAssignHalfedges<<<nb(nh), 256, 0, s>>>(nh, w, appH, H);
-    countLaunch();
-    kCopyBackFaces<<<nb(nf), 256, 0, s>>>(nf, w, appF, F, faceFirst, faceAttr);
-    countLaunch();
-    kCopyBackHalfedges<<<nb(nh), 256, 0, s>>>(nh, w, he);
+void launchSplitCopyBack(const SplitWork& w, const int* appV, const int* appH, const int* appF, int V2, int H2, int F2,
+                         float* pos, float* nrm, int4* he, int* faceFirst, uint16_t* faceAttr, uint32_t* status,
+                         cudaStream_t s) {
+    countLaunch(4);
+    kCopyBackVertices<<<nb(w.nv, 256), 256, 0, s>>>(w, appV, V2, pos, nrm, status);
+    kAssignHalfedges<<<nb(w.nh, 256), 256, 0, s>>>(w, appH);
+    kCopyBackFaces<<<nb(w.nf, 256), 256, 0, s>>>(w, appF, H2, F2, faceFirst, faceAttr, status);
+    kCopyBackHalfedges<<<nb(w.nh, 256), 256, 0, s>>>(w, V2, H2, F2, he, status);
 }
 void launchSplitResetMaps(int n, const int* nmFaces, const SplitWork& w, cudaStream_t s) {
     countLaunch();
-    kResetMaps<<<nb(4 * (int64_t)n), 256, 0, s>>>(n, nmFaces, w);
+    kResetMaps<<<nb(4 * (int64_t)n, 256), 256, 0, s>>>(n, nmFaces, w);
 }
 
 }  // namespace mdmc

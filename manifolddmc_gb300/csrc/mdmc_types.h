@@ -1,6 +1,7 @@
 // Internal types shared by the library's translation units.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 
 #include "mdmc.h"
@@ -20,17 +21,31 @@ enum : uint32_t {
     kStatusWallOutOfGrid = 1u << 7,    // cell wall outside the grid (clamped)
     kStatusMissingCell = 1u << 8,      // quad neighbour cell not found
     kStatusMappingSwap = 1u << 9,      // unexpected working-copy mapping swap
+    kStatusCountMismatch = 1u << 10,   // a write outside the sizes the count pass gave
+    kStatusBadIndex = 1u << 11,        // an element id outside its array (skipped)
+};
+
+// unsigned range check used before every data-dependent access
+__host__ __device__ __forceinline__ bool inb(long long i, long long n) { return (unsigned long long)i < (unsigned long long)n; }
+
+// current element counts of the mesh arrays
+struct MeshDims {
+    int V, F, H;
 };
 
 // Edge hash bucket: 32 bytes, one sector.  key = concatenateKeys(min, max)
 // (D/Utils/Utilities.h:15-22); cnt stores count-1 so that an all-0xFF memset
-// yields an empty bucket (key ~0, count 0, ids -1).
+// yields an empty bucket (key ~0, count 0, ids -1).  The ids come first so
+// that they can be read and written as one 16-byte-aligned int4.
 struct __align__(32) Bucket {
+    int ids[4];
     unsigned long long key;
     int cnt;
-    int ids[4];
     int pad;
 };
+static_assert(sizeof(Bucket) == 32, "bucket is one 32-byte sector");
+static_assert(offsetof(Bucket, ids) == 0 && offsetof(Bucket, key) == 16 && offsetof(Bucket, cnt) == 24,
+              "bucket layout");
 constexpr unsigned long long kEmptyKey = ~0ULL;
 
 // Active cell record written by the DMC emit pass (16 bytes):

@@ -359,6 +359,12 @@ static const uint16_t kAttrNonManifold = 0x20;
 static const uint8_t kFlagNonManifold = 1, kFlagBoundary = 2, kFlagWeird = 4, kFlagMultiFan = 8,
                      kFlagRemove = 16;
 
+// anomaly bits (same meaning and values as the CUDA path's status word)
+enum : uint32_t {
+    kSSlot = 1u << 1, kSBucket = 1u << 2, kSPartner = 1u << 3, kSWalk = 1u << 4, kSBadTwin = 1u << 5,
+    kSIterCap = 1u << 6, kSWall = 1u << 7, kSMapping = 1u << 9
+};
+
 struct Bucket {
     int count = 0;
     int ids[4] = {-1, -1, -1, -1};
@@ -387,11 +393,11 @@ struct Result {
 
 struct EdgeTable {
     std::unordered_map<uint64_t, Bucket> map;
-    int64_t anomalies = 0;
+    uint32_t anomalies = 0;
     void insert(int a, int b, int h) {
         Bucket& bk = map[edgeKey(a, b)];
         if (bk.count < 4) bk.ids[bk.count] = h;
-        else ++anomalies;  // more than 4 faces on one edge
+        else anomalies |= kSBucket;  // more than 4 faces on one edge
         ++bk.count;
     }
     void finish() {
@@ -413,7 +419,7 @@ struct Mesh {
     std::vector<uint16_t> faceAttr;
     std::vector<uint8_t> vflags;
     EdgeTable table;
-    int64_t anomalies = 0;
+    uint32_t anomalies = 0;
 
     int numV() const { return (int)(pos.size() / 3); }
     V3 P(int v) const { return v3(pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]); }
@@ -507,7 +513,7 @@ struct QuadEntry {
 
 static void runDMC(const Grid& g, float iso, bool surfaceIteration, std::vector<float>& pos,
                    std::vector<float>& nrm, std::vector<int>& quads, std::vector<uint16_t>& attr,
-                   int64_t& anomalies) {
+                   uint32_t& anomalies) {
     const int X = g.d[0], Y = g.d[1], Z = g.d[2];
     std::unordered_map<uint64_t, QuadEntry> table;
     V3 origin = g.o(), dl = g.dl();
@@ -555,7 +561,7 @@ static void runDMC(const Grid& g, float iso, bool surfaceIteration, std::vector<
                         uint64_t key = 3ULL * ((uint64_t)sz2 * X * Y + (uint64_t)sy * X + sx) + kEdgeAxis[e];
                         int slot = quadSlot(e, (edgy >> e) & 1);
                         QuadEntry& q = table[key];
-                        if (q.slot[slot] != -1) ++anomalies;
+                        if (q.slot[slot] != -1) anomalies |= kSSlot;
                         q.slot[slot] = vid;
                         int base = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
                         if (e == 0) q.color = 3 * base;
@@ -649,7 +655,7 @@ static void reconnect(Mesh& m, const Grid& g, float iso) {
         // the grid only arise from broken input and are clamped here
         if (mn[0] < 0 || mn[1] < 0 || mn[2] < 0 || mn[0] + 1 >= g.d[0] || mn[1] + 1 >= g.d[1] ||
             mn[2] + 1 >= g.d[2])
-            ++m.anomalies;
+            m.anomalies |= kSWall;
         float w[4];
         w[0] = g.atClamped(mn[0], mn[1], mn[2]);
         w[1] = g.atClamped(mn[0] + xo[0], mn[1] + xo[1], mn[2] + xo[2]);
@@ -736,7 +742,7 @@ struct MergeList {
     int get(int a, int k) const { return slot[4 * a + k]; }
     int count(int a) const { return std::min(num[a], 5); }
     // getAllPartnersOf, :25-62 (breadth-first closure, at most 12 partners)
-    int closure(int v, int out[12], int64_t& anomalies) const {
+    int closure(int v, int out[12], uint32_t& anomalies) const {
         int np = count(v);
         if (np <= 1) return np;
         for (int i = 0; i < np - 1; ++i) out[i] = get(v, i);
@@ -748,7 +754,7 @@ struct MergeList {
                 bool contained = (pp == v);
                 for (int z = 0; z < np - 1; ++z) contained = contained || out[z] == pp;
                 if (!contained) {
-                    if (np - 1 >= 12) { ++anomalies; continue; }
+                    if (np - 1 >= 12) { anomalies |= kSPartner; continue; }
                     out[np - 1] = pp;
                     ++np;
                 }
@@ -827,7 +833,7 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
             if (b.count < 4) continue;
             for (int i = 0; i < 4; ++i) {
                 int c = hO2C[b.ids[i]];
-                if (c < 0) { ++m.anomalies; continue; }
+                if (c < 0) { m.anomalies |= kSBadTwin; continue; }
                 hfl[c] |= kFlagNonManifold;
                 vfl[ch[c].origin] |= kFlagNonManifold;
             }
@@ -888,7 +894,7 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
                     hC2O[a] = bo;
                     hC2O[b] = ao;
                     if (ao != -1 && bo == -1) hO2C[ao] = b;
-                    else ++m.anomalies;
+                    else m.anomalies |= kSMapping;
                 }
             }
         }
@@ -898,7 +904,7 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
             for (int t = 0; t < nh; ++t) {
                 if (!(hfl[t] & kFlagNonManifold)) continue;
                 int tw = ch[t].twin;
-                if (tw < 0) { ++m.anomalies; continue; }
+                if (tw < 0) { m.anomalies |= kSBadTwin; continue; }
                 if (tw < t) continue;
                 // collapseHalfedge :767-835
                 int f0[4], f1[4];
@@ -925,21 +931,21 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
                 for (int i = 1; i < 4; ++i) {
                     int a = f0[i], b = f1[i];
                     int at = ch[a].twin, bt = ch[b].twin;
-                    if (at < 0 || bt < 0) { ++m.anomalies; continue; }
+                    if (at < 0 || bt < 0) { m.anomalies |= kSBadTwin; continue; }
                     hml.mark(a, bt); hml.mark(bt, a);
                     hml.mark(b, at); hml.mark(at, b);
                 }
             }
             vml.finish();
             hml.finish();
-            m.anomalies += vml.overflow + hml.overflow;
+            if (vml.overflow + hml.overflow) m.anomalies |= kSPartner;
             if (step >= StepMerge) {
                 // mergeVertices :936-990
                 for (int v = 0; v < nv; ++v) {
                     int part[12];
                     int np = vml.closure(v, part, m.anomalies);
                     if (np <= 1) continue;
-                    if (np > 12) { ++m.anomalies; continue; }  // :954-958
+                    if (np > 12) { m.anomalies |= kSPartner; continue; }  // :954-958
                     int smallest = v;
                     V3 p = v3(cpos[3 * v], cpos[3 * v + 1], cpos[3 * v + 2]);
                     bool obsolete = false;
@@ -1064,7 +1070,7 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
         m.refresh();
         ++iterations;
         if (!(step >= StepIterate)) break;
-        if (iterations > 64) { ++m.anomalies; break; }  // the reference has no cap
+        if (iterations >= 64) { m.anomalies |= kSIterCap; break; }  // the reference has no cap
     }
     return iterations;
 }
@@ -1094,7 +1100,7 @@ static void detectNonManifoldVertices(Mesh& m) {
             if (origin != m.he[cur].origin) break;
             if (cur < result) result = cur;
             cur = cw ? stepCW(cur) : stepCCW(cur);
-            if (++guard > 4096) { ++m.anomalies; break; }
+            if (++guard > 4096) { m.anomalies |= kSWalk; break; }
         }
         return result;
     };
@@ -1118,7 +1124,7 @@ static void detectNonManifoldVertices(Mesh& m) {
 static Result* run(const Grid& g, float iso, const mdmc_oracle_options& opt) {
     Result* r = new Result();
     std::memset(r->stats, 0, sizeof r->stats);
-    int64_t anomalies = 0;
+    uint32_t anomalies = 0;
     runDMC(g, iso, opt.surface_iteration != 0, r->dmcPos, r->dmcNrm, r->dmcQuads, r->dmcAttr, anomalies);
 
     Mesh m;
@@ -1146,7 +1152,7 @@ static Result* run(const Grid& g, float iso, const mdmc_oracle_options& opt) {
             r->stats[MDMC_ORC_STAT_SPLIT_ITERATIONS] = runSplitter(m, g, iso, opt.splitting_step);
         if (opt.detect_non_manifold_vertices) detectNonManifoldVertices(m);
     }
-    anomalies += m.table.anomalies + m.anomalies;
+    anomalies |= m.table.anomalies | m.anomalies;
     if (m.numV() == 0) {  // the reference logs and returns before post-processing
         for (int k = 0; k < MDMC_ORC_NUM_STATS; ++k) r->stats[k] = -1;
         r->stats[MDMC_ORC_STAT_SPLIT_ITERATIONS] = 0;

@@ -57,7 +57,9 @@ enum {
     MDMC_ORC_STAT_QUADS_NM3 = 6,
     MDMC_ORC_STAT_QUADS_NM4 = 7,
     MDMC_ORC_STAT_SPLIT_ITERATIONS = 8,
-    MDMC_ORC_STAT_ANOMALIES = 9,      /* bucket overflow, partner overflow, ... */
+    MDMC_ORC_STAT_ANOMALIES = 9,      /* bitmask: 2 slot conflict, 4 bucket overflow, 8 partner overflow,
+                                         16 fan-walk cap, 32 twin outside copy, 64 iteration cap,
+                                         128 wall outside grid, 512 mapping swap */
     MDMC_ORC_NUM_STATS = 10
 };
 

@@ -59,7 +59,8 @@ def assert_parity(dmc, m, ref):
     for k in range(1, 5):
         assert dmc.get_num_quads_with_non_manifold_edges(k) == st["quads_nm%d" % k]
     assert dmc.stats.split_iterations == st["split_iterations"]
-    assert dmc.stats.anomalies == 0 and st["anomalies"] == 0
+    # identical device status word (limits hit, e.g. the fan-walk cap)
+    assert dmc.stats.anomalies == st["anomalies"]
     # quads output = face walk
     if len(m.quads):
         he = m.halfedges
