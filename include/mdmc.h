@@ -86,12 +86,20 @@ typedef struct mdmc_options {
 } mdmc_options;
 
 /* A uniform grid on the device (UniformGrid<float>, UniformGrid.h:44-262):
- * samples x fastest, sample (x,y,z) at origin + (x,y,z) * spacing. */
+ * sample (x,y,z) at origin + (x,y,z) * spacing, x fastest in memory.
+ * Either dense (samples != NULL, coarse_samples == NULL) or refined and/or
+ * padded on demand from a coarse grid (coarse_samples != NULL): the library
+ * then evaluates refineGrid's samples where it needs them instead of storing
+ * the refined grid.  mdmc_prepare_grid fills this struct. */
 typedef struct mdmc_grid {
     const float* samples;
     int32_t dims[3];
     float origin[3];
     float spacing[3];
+    const float* coarse_samples;
+    int32_t coarse_dims[3];
+    int32_t refinement;
+    int32_t add_zero_boundary;
 } mdmc_grid;
 
 /* The halfedge mesh after post-processing (HalfedgeMesh, Halfedges/HalfedgeMesh.h)
@@ -130,7 +138,8 @@ typedef struct mdmc_stats {
     /* per-kernel GPU times of the last run (CUDA events on the run's stream) */
     float ms_refine;               /* grid refinement of the last mdmc_prepare_grid */
     float ms_count;                /* per-row counting pass over the grid */
-    float ms_emit;                 /* vertex / active-cell emission pass */
+    float ms_emit;                 /* active-cell compaction pass */
+    float ms_vertices;             /* dual vertices of the active cells */
     float ms_quads;                /* quads, halfedges and edge-table inserts */
     float ms_table;                /* edge-table twins and flags */
     int64_t kernel_launches;       /* kernels launched by the last run and prepare */
@@ -155,15 +164,22 @@ MDMC_API mdmc_status mdmc_get_options(const mdmc_context* context, mdmc_options*
 MDMC_API mdmc_status mdmc_read_bin(const char* path, int32_t dims[3], float spacing[3], float origin[3],
                           float* host_samples);
 
-/* Trilinear refinement by (refinement+1) and/or one layer of replicated
- * boundary samples ("zero boundary"), into a context-owned device grid.
- * samples may be a device pointer (samples_on_host = 0) or host memory, which
- * is then copied in on the stream.  UniformGridHost::readFromFile(file,
- * refinement, addZeroBoundary), UniformGrid.inl:575-608, kernel refineGrid :279-319 */
+/* Describes the grid of trilinear refinement by (refinement+1) and/or one
+ * layer of replicated boundary samples ("zero boundary") of the input.  The
+ * refined grid is evaluated on demand by mdmc_run (bit-identical to the
+ * reference's refineGrid output) and not stored.  samples may be a device
+ * pointer (samples_on_host = 0), used in place and required to stay valid
+ * while the grid is used, or host memory, copied into the context on the
+ * stream.  UniformGridHost::readFromFile(file, refinement, addZeroBoundary),
+ * UniformGrid.inl:575-608, kernel refineGrid :279-319 */
 MDMC_API mdmc_status mdmc_prepare_grid(mdmc_context* context, const float* samples, int samples_on_host,
                               const int32_t dims[3], const float origin[3], const float spacing[3],
                               int32_t refinement, int32_t add_zero_boundary, mdmc_grid* out_grid,
                               void* stream);
+
+/* Writes the dense samples of a grid (refined on demand or not) to a device
+ * buffer of dims[0]*dims[1]*dims[2] floats (refineGrid, UniformGrid.inl:279-319). */
+MDMC_API mdmc_status mdmc_materialize_grid(mdmc_context* context, const mdmc_grid* grid, float* out, void* stream);
 
 /* DualMarchingCubes::run, DualMarchingCubes.cu:220-289: DMC, halfedge mesh,
  * twin repair, non-manifold split and non-manifold vertex detection as the

@@ -48,7 +48,11 @@ class Grid(ctypes.Structure):
     _fields_ = [("samples", ctypes.c_void_p),
                 ("dims", ctypes.c_int32 * 3),
                 ("origin", ctypes.c_float * 3),
-                ("spacing", ctypes.c_float * 3)]
+                ("spacing", ctypes.c_float * 3),
+                ("coarse_samples", ctypes.c_void_p),
+                ("coarse_dims", ctypes.c_int32 * 3),
+                ("refinement", ctypes.c_int32),
+                ("add_zero_boundary", ctypes.c_int32)]
 
 
 class Mesh(ctypes.Structure):
@@ -70,6 +74,7 @@ class Stats(ctypes.Structure):
                 ("ms_dmc", ctypes.c_float), ("ms_halfedge", ctypes.c_float), ("ms_repair", ctypes.c_float),
                 ("ms_detect", ctypes.c_float), ("ms_total", ctypes.c_float),
                 ("ms_refine", ctypes.c_float), ("ms_count", ctypes.c_float), ("ms_emit", ctypes.c_float),
+                ("ms_vertices", ctypes.c_float),
                 ("ms_quads", ctypes.c_float), ("ms_table", ctypes.c_float), ("kernel_launches", ctypes.c_int64)]
 
     def as_dict(self):
@@ -113,6 +118,7 @@ def library():
             "mdmc_read_bin": (ctypes.c_int, [ctypes.c_char_p, P, P, P, P]),
             "mdmc_prepare_grid": (ctypes.c_int, [P, P, ctypes.c_int, P, P, P, ctypes.c_int32, ctypes.c_int32, P, P]),
             "mdmc_run": (ctypes.c_int, [P, P, ctypes.c_float, P, P, P]),
+            "mdmc_materialize_grid": (ctypes.c_int, [P, P, P, P]),
             "mdmc_get_mesh": (ctypes.c_int, [P, P]),
             "mdmc_get_stats": (ctypes.c_int, [P, P]),
             "mdmc_download_mesh": (ctypes.c_int, [P] * 10),
@@ -226,6 +232,11 @@ class UniformGrid:
     def get_cell_count(self):
         d = self.dimensions
         return d[0] * d[1] * d[2]
+
+    def materialize(self, out_device_ptr, stream=None):
+        """Writes the dense (refined) samples to a device buffer of get_cell_count() floats."""
+        self._ctx.check(self._ctx.lib.mdmc_materialize_grid(self._ctx.handle, ctypes.byref(self.grid),
+                                                            P(int(out_device_ptr)), _stream_handle(stream)))
 
 
 class HalfedgeMesh:

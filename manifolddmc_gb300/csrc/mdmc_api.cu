@@ -75,9 +75,9 @@ struct mdmc_context {
     mdmc_options opt;
     std::string err;
     // grid preparation
-    DevBuf gridBuf, stageBuf;
+    DevBuf gridBuf, stageBuf, mayCross;
     // DMC stage
-    DevBuf rows, scanScratch, act;
+    DevBuf rows, scanScratch, act, vbase;
     // mesh
     DevBuf pos, nrm, he, faceFirst, faceAttr, vflags, vertexHE, quads;
     int64_t V = 0, F = 0, H = 0;
@@ -99,10 +99,9 @@ struct mdmc_context {
     DevBuf isKey, fans;
     // events: start, dmc, halfedge, repair, detect, end
     cudaEvent_t ev[6] = {};
-    // per-kernel events: refine begin/end, count, emit, quads, table (begin/end each)
-    cudaEvent_t kev[10] = {};
+    // per-kernel events: refine, count, emit, quads, table, vertices (begin/end each)
+    cudaEvent_t kev[12] = {};
     float msRefine = 0.f;
-    long long prepareLaunches = 0;
     bool haveMesh = false;
     mdmc_stats stats;
 };
@@ -170,6 +169,58 @@ mdmc_status readInts(mdmc_context* c, const void* src, int n, cudaStream_t s) {
 }
 
 unsigned long long tableCapacity(int64_t faces) { return (unsigned long long)roundUp((size_t)std::max<int64_t>(3 * faces, 64), 32); }
+
+// the view of a grid the kernels read; refined grids get their coarse-cell
+// pre-pass for this iso-value (mayCross bits in the context)
+mdmc_status makeGridDesc(mdmc_context* c, const mdmc_grid* grid, float iso, GridDesc& d, cudaStream_t s) {
+    GridGeom geom;
+    geom.X = grid->dims[0];
+    geom.Y = grid->dims[1];
+    geom.Z = grid->dims[2];
+    geom.ox = grid->origin[0];
+    geom.oy = grid->origin[1];
+    geom.oz = grid->origin[2];
+    geom.dx = grid->spacing[0];
+    geom.dy = grid->spacing[1];
+    geom.dz = grid->spacing[2];
+    d.refined = grid->coarse_samples != nullptr && (grid->refinement > 0 || grid->add_zero_boundary);
+    static_cast<GridGeom&>(d.plain) = geom;
+    static_cast<GridGeom&>(d.ref) = geom;
+    d.plain.v = grid->samples;
+    d.ref.c = grid->coarse_samples;
+    d.ref.cX = grid->coarse_dims[0];
+    d.ref.cY = grid->coarse_dims[1];
+    d.ref.cZ = grid->coarse_dims[2];
+    d.ref.r = grid->refinement;
+    d.ref.pad = grid->add_zero_boundary ? 1 : 0;
+    d.ref.f = (float)(grid->refinement + 1);
+    {
+        const int f = grid->refinement + 1;
+        d.ref.fPow2 = (f & (f - 1)) == 0 ? 1 : 0;
+        d.ref.invf = 1.0f / (float)f;
+    }
+    d.ref.mayCross = nullptr;
+    if (!d.refined) {
+        if (!grid->samples) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "grid has no samples");
+        return MDMC_OK;
+    }
+    const int pad = d.ref.pad;
+    for (int a = 0; a < 3; ++a) {
+        const int cd = grid->coarse_dims[a];
+        if (cd < 1 || grid->refinement < 0 ||
+            (int64_t)cd + (int64_t)(cd - 1) * grid->refinement + 2 * pad != grid->dims[a])
+            return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "coarse dims do not match the refined dims");
+    }
+    if (d.ref.cX >= 2 && d.ref.cY >= 2 && d.ref.cZ >= 2) {
+        const int64_t cells = (int64_t)(d.ref.cX - 1) * (d.ref.cY - 1) * (d.ref.cZ - 1);
+        MDMC_CHECK(c, c->mayCross.ensure(sizeof(uint32_t) * (size_t)((cells + 31) / 32 + 1)));
+        d.ref.mayCross = c->mayCross.as<uint32_t>();
+        cudaEventRecord(c->kev[0], s);
+        launchCoarseMayCross(d.ref, iso, c->mayCross.as<uint32_t>(), s);
+        cudaEventRecord(c->kev[1], s);
+    }
+    return MDMC_OK;
+}
 
 SplitWork splitWork(mdmc_context* c, int nv, int nh, int nf) {
     SplitWork w;
@@ -243,7 +294,7 @@ mdmc_status refreshTable(mdmc_context* c, uint32_t* status, cudaStream_t s) {
 }
 
 // ManifoldSplitter::run, D/PostProcesses/ManifoldSplitter.cu:96-208
-mdmc_status runSplitter(mdmc_context* c, const GridView& g, float iso, int64_t& iterations, cudaStream_t s) {
+mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& iterations, cudaStream_t s) {
     DevCounters* ctr = c->counters.as<DevCounters>();
     uint32_t* status = &ctr->status;
     const int step = c->opt.splitting_step;
@@ -470,9 +521,10 @@ mdmc_status mdmc_prepare_grid(mdmc_context* c, const float* samples, int samples
     }
     if (outN >= 0xFFFFFFFFull) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "grid has 2^32 samples or more");
     const float* src = samples;
-    c->prepareLaunches = 0;
-    cudaEventRecord(c->kev[0], s);
-    cudaEventRecord(c->kev[1], s);
+    out->coarse_samples = nullptr;
+    out->coarse_dims[0] = out->coarse_dims[1] = out->coarse_dims[2] = 0;
+    out->refinement = refinement;
+    out->add_zero_boundary = pad;
     if (refinement == 0 && !pad) {
         if (samples_on_host) {
             MDMC_CHECK(c, c->gridBuf.ensure(sizeof(float) * outN));
@@ -481,20 +533,15 @@ mdmc_status mdmc_prepare_grid(mdmc_context* c, const float* samples, int samples
         }
         out->samples = src;
     } else {
+        // refined on demand from the coarse grid by the kernels that read it
         if (samples_on_host) {
             MDMC_CHECK(c, c->stageBuf.ensure(sizeof(float) * inN));
             MDMC_CHECK(c, cudaMemcpyAsync(c->stageBuf.p, samples, sizeof(float) * inN, cudaMemcpyHostToDevice, s));
             src = c->stageBuf.as<float>();
         }
-        MDMC_CHECK(c, c->gridBuf.ensure(sizeof(float) * outN));
-        const long long l0 = g_kernelLaunches.load();
-        cudaEventRecord(c->kev[0], s);
-        launchRefine(src, make_int3(dims[0], dims[1], dims[2]), c->gridBuf.as<float>(), make_int3(od[0], od[1], od[2]),
-                     refinement, pad, s);
-        cudaEventRecord(c->kev[1], s);
-        c->prepareLaunches = g_kernelLaunches.load() - l0;
-        MDMC_CHECK(c, cudaGetLastError());
-        out->samples = c->gridBuf.as<float>();
+        out->samples = nullptr;
+        out->coarse_samples = src;
+        for (int a = 0; a < 3; ++a) out->coarse_dims[a] = dims[a];
     }
     for (int a = 0; a < 3; ++a) {
         out->dims[a] = od[a];
@@ -504,9 +551,26 @@ mdmc_status mdmc_prepare_grid(mdmc_context* c, const float* samples, int samples
     return MDMC_OK;
 }
 
+mdmc_status mdmc_materialize_grid(mdmc_context* c, const mdmc_grid* grid, float* out, void* stream) {
+    if (!c || !grid || !out) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "null argument");
+    (void)cudaGetLastError();
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t n = (size_t)grid->dims[0] * grid->dims[1] * grid->dims[2];
+    if (grid->coarse_samples && (grid->refinement > 0 || grid->add_zero_boundary)) {
+        launchRefine(grid->coarse_samples, make_int3(grid->coarse_dims[0], grid->coarse_dims[1], grid->coarse_dims[2]),
+                     out, make_int3(grid->dims[0], grid->dims[1], grid->dims[2]), grid->refinement,
+                     grid->add_zero_boundary ? 1 : 0, s);
+        MDMC_CHECK(c, cudaGetLastError());
+    } else {
+        if (!grid->samples) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "grid has no samples");
+        MDMC_CHECK(c, cudaMemcpyAsync(out, grid->samples, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    }
+    return MDMC_OK;
+}
+
 mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mesh* mesh, mdmc_stats* stats,
                      void* stream) {
-    if (!c || !grid || !grid->samples) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "null argument");
+    if (!c || !grid) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "null argument");
     c->err.clear();
     (void)cudaGetLastError();  // errors of earlier, unrelated runtime calls are not ours
     const int X = grid->dims[0], Y = grid->dims[1], Z = grid->dims[2];
@@ -515,13 +579,16 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     cudaStream_t s = (cudaStream_t)stream;
     c->haveMesh = false;
     std::memset(&c->stats, 0, sizeof c->stats);
-    GridView g{grid->samples, X, Y, Z, grid->origin[0], grid->origin[1], grid->origin[2],
-               grid->spacing[0], grid->spacing[1], grid->spacing[2]};
     DevCounters* ctr = c->counters.as<DevCounters>();
     uint32_t* status = &ctr->status;
     MDMC_CHECK(c, cudaMemsetAsync(ctr, 0, sizeof(DevCounters), s));
     const long long launches0 = g_kernelLaunches.load();
     cudaEventRecord(c->ev[0], s);
+    cudaEventRecord(c->kev[0], s);
+    cudaEventRecord(c->kev[1], s);
+    GridDesc g;
+    mdmc_status st0 = makeGridDesc(c, grid, iso, g, s);
+    if (st0 != MDMC_OK) return st0;
 
     // ---- DMC: count, scan, emit (performDualMarchingCubes) --------------------
     const int64_t numRows = (X > 1 && Y > 1 && Z > 1) ? (int64_t)(Y - 1) * (Z - 1) : 0;
@@ -534,13 +601,28 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, cudaGetLastError());
     if ((st = readInts(c, c->rows.as<int4>() + numRows, 4, s)) != MDMC_OK) return st;
     const int* tot = reinterpret_cast<const int*>(c->hostInts);
-    const int64_t A = tot[0], Vd = tot[1], Q = tot[2];
+    const int64_t A = tot[0], Q = tot[1];
     const int64_t cells = numRows * (int64_t)(X - 1);
-    if (A < 0 || A > cells || Vd < A || Vd > 4 * A || Q < 0 || Q > 3 * A)
+    if (A < 0 || A > cells || Q < 0 || Q > 3 * A)
         return fail(c, MDMC_ERROR_CUDA, "inconsistent cell counts from the count pass");
     c->stats.num_active_cells = A;
-    c->stats.num_dmc_vertices = Vd;
     c->stats.num_dmc_quads = Q;
+    if (4 * Q >= (int64_t)0x7FFFFFFF) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "more than 2^31 halfedges");
+
+    // compaction of the active cells and their contour counts
+    MDMC_CHECK(c, c->act.ensure(sizeof(ActiveCell) * (size_t)std::max<int64_t>(A, 1)));
+    MDMC_CHECK(c, c->vbase.ensure(sizeof(int) * (size_t)(A + 1)));
+    cudaEventRecord(c->kev[4], s);
+    if (numRows > 0)
+        launchRowEmit(g, iso, c->rows.as<int4>(), (int)numRows, c->act.as<ActiveCell>(), c->vbase.as<int>(), (int)A,
+                      status, s);
+    cudaEventRecord(c->kev[5], s);
+    if ((st = scan<int>(c, c->vbase.as<int>(), c->vbase.as<int>(), A, s)) != MDMC_OK) return st;
+    MDMC_CHECK(c, cudaGetLastError());
+    if ((st = readInts(c, c->vbase.as<int>() + A, 1, s)) != MDMC_OK) return st;
+    const int64_t Vd = c->hostInts[0];
+    if (Vd < A || Vd > 4 * A) return fail(c, MDMC_ERROR_CUDA, "inconsistent vertex count from the emit pass");
+    c->stats.num_dmc_vertices = Vd;
     if (Vd == 0) {
         // "DMC: No Vertices have been produced!" (D/DualMarchingCubes.cu:256-261)
         c->V = c->F = c->H = 0;
@@ -552,32 +634,30 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
         if (stats) *stats = c->stats;
         return MDMC_OK;
     }
-    if (4 * Q >= (int64_t)0x7FFFFFFF) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "more than 2^31 halfedges");
     c->V = Vd;
     c->F = Q;
     c->H = 4 * Q;
     c->cap = tableCapacity(Q);
-    MDMC_CHECK(c, c->act.ensure(sizeof(ActiveCell) * (size_t)A));
     MDMC_CHECK(c, c->pos.ensure(sizeof(float) * 3 * (size_t)Vd));
     MDMC_CHECK(c, c->nrm.ensure(sizeof(float) * 3 * (size_t)Vd));
     MDMC_CHECK(c, c->vflags.ensure(roundUp((size_t)Vd, 4)));
-    MDMC_CHECK(c, c->he.ensure(sizeof(int4) * 4 * (size_t)Q));
-    MDMC_CHECK(c, c->faceFirst.ensure(sizeof(int) * (size_t)Q));
-    MDMC_CHECK(c, c->faceAttr.ensure(roundUp(sizeof(uint16_t) * (size_t)Q, 4)));
+    MDMC_CHECK(c, c->he.ensure(sizeof(int4) * 4 * (size_t)std::max<int64_t>(Q, 1)));
+    MDMC_CHECK(c, c->faceFirst.ensure(sizeof(int) * (size_t)std::max<int64_t>(Q, 1)));
+    MDMC_CHECK(c, c->faceAttr.ensure(roundUp(sizeof(uint16_t) * (size_t)std::max<int64_t>(Q, 1), 4)));
     MDMC_CHECK(c, c->table.ensure(sizeof(Bucket) * c->cap));
     MDMC_CHECK(c, c->nmList.ensure(sizeof(int) * (size_t)(Q + 1)));
     MDMC_CHECK(c, cudaMemsetAsync(c->table.p, 0xFF, sizeof(Bucket) * c->cap, s));
     MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)Vd, 4), s));
-    cudaEventRecord(c->kev[4], s);
-    launchRowEmit(g, iso, c->opt.enable_surface_to_vertex_iteration, c->rows.as<int4>(), (int)numRows,
-                  c->act.as<ActiveCell>(), c->pos.as<float>(), c->nrm.as<float>(), (int)A, (int)Vd, status, s);
-    cudaEventRecord(c->kev[5], s);
+    cudaEventRecord(c->kev[10], s);
+    launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), c->vbase.as<int>(), (int)A,
+                   (int)Vd, c->pos.as<float>(), c->nrm.as<float>(), status, s);
+    cudaEventRecord(c->kev[11], s);
     // mapQuadrilaterals + collectHalfedgeElements
     cudaEventRecord(c->kev[6], s);
-    launchQuads(c->act.as<ActiveCell>(), (int)A, c->rows.as<int4>(), X, Y, c->table.as<Bucket>(), c->cap,
-                c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(), (int)Q, (int)Vd, status, s);
-    MDMC_CHECK(c, cudaGetLastError());
+    launchQuads(c->act.as<ActiveCell>(), c->vbase.as<int>(), (int)A, c->rows.as<int4>(), X, Y, c->table.as<Bucket>(),
+                c->cap, c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(), (int)Q, (int)Vd, status, s);
     cudaEventRecord(c->kev[7], s);
+    MDMC_CHECK(c, cudaGetLastError());
     cudaEventRecord(c->ev[1], s);
 
     // ---- halfedge mesh: twins and flags (HalfedgeMesh::initialize) -----------
@@ -637,8 +717,8 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->stats.ms_repair = ms[2];
     c->stats.ms_detect = ms[3];
     c->stats.ms_total = ms[4];
-    float km[5] = {0, 0, 0, 0, 0};
-    for (int k = 0; k < 5; ++k)
+    float km[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = 0; k < 6; ++k)
         if (cudaEventElapsedTime(&km[k], c->kev[2 * k], c->kev[2 * k + 1]) != cudaSuccess) km[k] = 0.f;
     (void)cudaGetLastError();  // elapsed-time queries leave no error behind
     c->stats.ms_refine = km[0];
@@ -646,7 +726,8 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->stats.ms_emit = km[2];
     c->stats.ms_quads = km[3];
     c->stats.ms_table = km[4];
-    c->stats.kernel_launches = (int64_t)(g_kernelLaunches.load() - launches0) + c->prepareLaunches;
+    c->stats.ms_vertices = km[5];
+    c->stats.kernel_launches = (int64_t)(g_kernelLaunches.load() - launches0);
     c->haveMesh = true;
     if (mesh) mdmc_get_mesh(c, mesh);
     if (stats) *stats = c->stats;

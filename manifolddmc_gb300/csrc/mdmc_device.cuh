@@ -254,29 +254,18 @@ struct SurfaceIterator {
 };
 
 // ---------------------------------------------------------------------------
-// grid access
+// grid access.  Two views share the geometry: PlainView reads a dense grid;
+// RefinedView evaluates the refined and/or padded grid of refineGrid
+// (D/UniformGrid.inl:279-319) from the coarse input on demand, with the same
+// float operations, so it returns exactly the values the dense refined grid
+// would hold without that grid ever being written.
 // ---------------------------------------------------------------------------
-struct GridView {
-    const float* v;
-    int X, Y, Z;
+struct GridGeom {
+    int X, Y, Z;       // samples of the (refined) grid
     float ox, oy, oz;  // origin
     float dx, dy, dz;  // spacing
-    __device__ __forceinline__ float at(int x, int y, int z) const {
-        return __ldg(v + ((size_t)z * Y + y) * X + x);
-    }
-    __device__ __forceinline__ float atClamped(int x, int y, int z) const {
-        x = x < 0 ? 0 : (x > X - 1 ? X - 1 : x);
-        y = y < 0 ? 0 : (y > Y - 1 ? Y - 1 : y);
-        z = z < 0 ? 0 : (z > Z - 1 ? Z - 1 : z);
-        return at(x, y, z);
-    }
     __device__ __forceinline__ F3 origin() const { return f3(ox, oy, oz); }
     __device__ __forceinline__ F3 deltas() const { return f3(dx, dy, dz); }
-    // UniformGrid::evaluateCellCornerValues, D/UniformGrid.inl:414-427
-    __device__ __forceinline__ void corners(int x, int y, int z, float s[8]) const {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) s[i] = atClamped(x + (i & 1), y + ((i >> 1) & 1), z + ((i >> 2) & 1));
-    }
     // getIndex3DFromPosition, D/UniformGrid.inl:441-448
     __device__ __forceinline__ void cellOf(F3 p, int c[3]) const {
         F3 off = (p - origin()) / deltas();
@@ -286,8 +275,73 @@ struct GridView {
     }
 };
 
+struct PlainView : GridGeom {
+    const float* v;
+    static constexpr bool kRefined = false;
+    __device__ __forceinline__ float at(int x, int y, int z) const { return __ldg(v + ((size_t)z * Y + y) * X + x); }
+};
+
+struct RefinedView : GridGeom {
+    const float* c;            // coarse samples
+    int cX, cY, cZ;            // coarse dims
+    int r, pad;                // refinement, replicated boundary layer
+    float f;                   // r + 1
+    const uint32_t* mayCross;  // per coarse cell: may a refined cell inside cross iso (bitmask, x fastest)
+    static constexpr bool kRefined = true;
+
+    float invf;                // 1 / f when f is a power of two (then i * invf == i / f exactly)
+    int fPow2;
+
+    // sample index of the unpadded refined grid (refineGrid's clamp and shift)
+    __device__ __forceinline__ int unpad(int i, int n) const { return pad ? min(max(i, 1), n - 2) - 1 : i; }
+    // (float)i / f, computed by a multiplication when that is exact
+    __device__ __forceinline__ float divf(int i) const { return fPow2 ? (float)i * invf : (float)i / f; }
+    __device__ __forceinline__ float at(int x, int y, int z) const {
+        x = unpad(x, X);
+        y = unpad(y, Y);
+        z = unpad(z, Z);
+        const float qx = divf(x), qy = divf(y), qz = divf(z);
+        const int mx = (int)floorf(qx), my = (int)floorf(qy), mz = (int)floorf(qz);
+        const F3 diff = f3(qx - (float)mx, qy - (float)my, qz - (float)mz);
+        float s[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const int cx = min(max(mx + (k & 1), 0), cX - 1);
+            const int cy = min(max(my + ((k >> 1) & 1), 0), cY - 1);
+            const int cz = min(max(mz + ((k >> 2) & 1), 0), cZ - 1);
+            s[k] = __ldg(c + ((size_t)cz * cY + cy) * cX + cx);
+        }
+        return trilinear(s, diff);
+    }
+    // coarse cell containing the refined cell whose lowest corner is i
+    __device__ __forceinline__ int coarseCell(int i, int n, int cn) const {
+        const int u = unpad(i, n);
+        return min((int)floorf(divf(u)), cn - 2);
+    }
+    __device__ __forceinline__ bool coarseMayCross(int mx, int my, int mz) const {
+        const size_t bit = ((size_t)mz * (cY - 1) + my) * (size_t)(cX - 1) + mx;
+        return (__ldg(mayCross + (bit >> 5)) >> (bit & 31)) & 1u;
+    }
+};
+
+template <class View>
+__device__ __forceinline__ float atClamped(const View& g, int x, int y, int z) {
+    x = x < 0 ? 0 : (x > g.X - 1 ? g.X - 1 : x);
+    y = y < 0 ? 0 : (y > g.Y - 1 ? g.Y - 1 : y);
+    z = z < 0 ? 0 : (z > g.Z - 1 ? g.Z - 1 : z);
+    return g.at(x, y, z);
+}
+
+// UniformGrid::evaluateCellCornerValues, D/UniformGrid.inl:414-427
+template <class View>
+__device__ __forceinline__ void corners(const View& g, int x, int y, int z, float s[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s[i] = atClamped(g, x + (i & 1), y + ((i >> 1) & 1), z + ((i >> 2) & 1));
+}
+
 // UniformGrid::computeGradients, D/UniformGrid.inl:325-379
-__device__ inline void cornerGradients(const GridView& g, int x, int y, int z, const float s[8], F3 out[8]) {
+template <class View>
+__device__ inline void cornerGradients(const View& g, int x, int y, int z, const float s[8], F3 out[8]) {
     auto cl = [](int dim, int ii) { return ii < 0 ? 0 : (ii >= dim ? dim - 1 : ii); };
     const int X = g.X, Y = g.Y, Z = g.Z;
     F3 gr[8];

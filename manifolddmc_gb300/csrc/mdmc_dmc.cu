@@ -5,16 +5,18 @@
 // (D/CellIntersection.inl:368-439), collectHalfedgeElements
 // (D/Halfedges/HalfedgeMesh.cu:14-60), refineGrid (D/UniformGrid.inl:279-319).
 //
-// GB300 design: one warp per x-row of cells.  Two streaming passes over the
-// grid (count, emit) replace the reference's single global atomic vertex
+// GB300 design: one warp per x-row of cells.  Two lean streaming passes over
+// the grid (count, emit) replace the reference's single global atomic vertex
 // counter and its 20M-bucket quad hash table: the count pass gives per-row
-// (active cells, vertices, owned quads), an exclusive scan turns them into
-// row offsets, and the emit pass writes vertices and active-cell records at
-// deterministic offsets using warp ballots and shuffles.  Each quad is then
-// built by the cell that owns its grid edge (the cell at the edge's origin),
-// which looks up the three other cells' records by row, so no quad hash is
-// needed; the same thread writes the quad's four halfedges and inserts its
-// edges into the edge table.
+// (active cells, owned quads), an exclusive scan turns them into row offsets,
+// and the emit pass writes the active cells' records at deterministic offsets
+// using warp ballots and shuffles.  The vertices are then computed by a dense
+// kernel over the active-cell list (no lane idles behind a neighbour's
+// surface iteration), at offsets from a scan of the cells' contour counts.
+// Each quad is built by the cell that owns its grid edge (the cell at the
+// edge's origin), which looks up the three other cells' records by row, so no
+// quad hash is needed; the same thread writes the quad's four halfedges and
+// inserts its edges into the edge table.
 #include <cuda_runtime.h>
 
 #include "mdmc_device.cuh"
@@ -24,156 +26,494 @@
 namespace mdmc {
 
 // ---------------------------------------------------------------------------
-// refineGrid, D/UniformGrid.inl:279-319
+// refineGrid, D/UniformGrid.inl:279-319.  One block row per output row
+// (blockIdx.y, blockIdx.z = y, z), so no per-sample index division.
 // ---------------------------------------------------------------------------
-__global__ void kRefine(const float* __restrict__ in, int3 din, float* __restrict__ out, int3 dout, int r,
-                        int pad) {
-    const int64_t n = (int64_t)dout.x * dout.y * dout.z;
-    const float f = (float)(r + 1);
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        int x = (int)(i % dout.x);
-        int y = (int)((i / dout.x) % dout.y);
-        int z = (int)(i / ((int64_t)dout.x * dout.y));
-        if (pad) {
-            x = min(max(x, 1), dout.x - 2) - 1;
-            y = min(max(y, 1), dout.y - 2) - 1;
-            z = min(max(z, 1), dout.z - 2) - 1;
-        }
-        float qx = (float)x / f, qy = (float)y / f, qz = (float)z / f;
-        int mx = (int)floorf(qx), my = (int)floorf(qy), mz = (int)floorf(qz);
-        F3 diff = f3(qx - (float)mx, qy - (float)my, qz - (float)mz);
-        float s[8];
-#pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            int cx = min(max(mx + (c & 1), 0), din.x - 1);
-            int cy = min(max(my + ((c >> 1) & 1), 0), din.y - 1);
-            int cz = min(max(mz + ((c >> 2) & 1), 0), din.z - 1);
-            s[c] = __ldg(in + ((int64_t)cz * din.y + cy) * din.x + cx);
-        }
-        out[i] = trilinear(s, diff);
+__global__ void __launch_bounds__(128) kRefine(const float* __restrict__ in, int3 din, float* __restrict__ out,
+                                               int3 dout, int r, int pad) {
+    const int x0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x0 >= dout.x) return;
+    int x = x0, y = blockIdx.y, z = blockIdx.z;
+    if (pad) {
+        x = min(max(x, 1), dout.x - 2) - 1;
+        y = min(max(y, 1), dout.y - 2) - 1;
+        z = min(max(z, 1), dout.z - 2) - 1;
     }
+    const float f = (float)(r + 1);
+    const float qx = (float)x / f, qy = (float)y / f, qz = (float)z / f;
+    const int mx = (int)floorf(qx), my = (int)floorf(qy), mz = (int)floorf(qz);
+    const F3 diff = f3(qx - (float)mx, qy - (float)my, qz - (float)mz);
+    float s[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+        const int cx = min(max(mx + (c & 1), 0), din.x - 1);
+        const int cy = min(max(my + ((c >> 1) & 1), 0), din.y - 1);
+        const int cz = min(max(mz + ((c >> 2) & 1), 0), din.z - 1);
+        s[c] = __ldg(in + ((int64_t)cz * din.y + cy) * din.x + cx);
+    }
+    out[((int64_t)blockIdx.z * dout.y + blockIdx.y) * dout.x + x0] = trilinear(s, diff);
 }
 
 void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int pad, cudaStream_t s) {
-    const int64_t n = (int64_t)dout.x * dout.y * dout.z;
-    int blocks = (int)std::min<int64_t>((n + 255) / 256, 152 * 32);
+    dim3 grid((dout.x + 127) / 128, dout.y, dout.z);
     countLaunch();
-    kRefine<<<blocks, 256, 0, s>>>(in, din, out, dout, r, pad);
+    kRefine<<<grid, 128, 0, s>>>(in, din, out, dout, r, pad);
 }
 
 // ---------------------------------------------------------------------------
-// cell classification
+// coarse-cell pre-pass for refined grids.  A refined cell lies inside one
+// coarse cell and its samples are trilinear interpolations of that cell's
+// eight corners: in exact arithmetic they stay within [min, max] of the
+// corners, and the rounding of refineGrid's expression (three lerp levels,
+// at most ~15 unit roundings of max|corner|) stays below delta = 32 * 2^-24 *
+// max|corner|.  A coarse cell whose corners are all below iso - delta, or all
+// at or above iso + delta, therefore holds only case-0 / case-255 refined
+// cells, and its refined cells need not be evaluated at all.
 // ---------------------------------------------------------------------------
-struct CellClass {
-    int cs;      // case
-    int nv;      // vertices (contours)
-    int nq;      // quads owned
-    uint64_t c;  // contour word
+__global__ void kCoarseMayCross(const float* __restrict__ c, int cX, int cY, int cZ, float iso, uint32_t* __restrict__ bits,
+                                int64_t numCells) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool may = false;
+    if (i < numCells) {
+        const int x = (int)(i % (cX - 1));
+        const int y = (int)((i / (cX - 1)) % (cY - 1));
+        const int z = (int)(i / ((int64_t)(cX - 1) * (cY - 1)));
+        float lo = INFINITY, hi = -INFINITY, mag = 0.f;
+        bool nan = false;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const float v = __ldg(c + ((int64_t)(z + ((k >> 2) & 1)) * cY + (y + ((k >> 1) & 1))) * cX + (x + (k & 1)));
+            nan = nan || (v != v);
+            lo = fminf(lo, v);
+            hi = fmaxf(hi, v);
+            mag = fmaxf(mag, fabsf(v));
+        }
+        const double delta = 32.0 * 5.9604644775390625e-8 * (double)mag;
+        const bool allBelow = (double)hi < (double)iso - delta;
+        const bool allAbove = (double)lo >= (double)iso + delta;
+        may = nan || !(allBelow || allAbove);
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, may);
+    if ((threadIdx.x & 31) == 0 && i < numCells) bits[i >> 5] = b;
+}
+
+void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, cudaStream_t s) {
+    const int64_t n = (int64_t)(g.cX - 1) * (g.cY - 1) * (g.cZ - 1);
+    if (n <= 0) return;
+    countLaunch();
+    kCoarseMayCross<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g.c, g.cX, g.cY, g.cZ, iso, bits, n);
+}
+
+// ---------------------------------------------------------------------------
+// row streaming.  A warp walks one x-row of cells in chunks of 32.  Each lane
+// holds the four samples of its column (y/y+1 x z/z+1); the x+1 column comes
+// from the next lane by shuffle, the last lane's from the next chunk.
+// ---------------------------------------------------------------------------
+template <class View>
+struct RowWalker;
+
+template <>
+struct RowWalker<PlainView> {
+    const float* r[4];  // sample rows (y,z) (y+1,z) (y,z+1) (y+1,z+1)
+    int X;
+    __device__ RowWalker(const PlainView& g, int y, int z) : X(g.X) {
+        const size_t sy = g.X, sz = (size_t)g.X * g.Y;
+        const float* b = g.v + (size_t)z * sz + (size_t)y * sy;
+        r[0] = b;
+        r[1] = b + sy;
+        r[2] = b + sz;
+        r[3] = b + sz + sy;
+    }
+    __device__ __forceinline__ void load(int x, float v[4]) const {
+        if (x < X) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) v[k] = __ldg(r[k] + x);
+        } else {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) v[k] = 0.f;
+        }
+    }
+    __device__ __forceinline__ bool chunkMayCross(int) const { return true; }
 };
 
-// cells are interior (x <= X-2, ...), so the reference's clamped corner fetch
-// (D/UniformGrid.inl:414-427) reads the unclamped corners
-__device__ __forceinline__ void classify(const GridView& g, int x, int y, int z, float iso,
-                                         const uint64_t* table, float s[8], CellClass& cc) {
-    const float* p = g.v + ((size_t)z * g.Y + y) * g.X + x;
-    const size_t sy = g.X, sz = (size_t)g.X * g.Y;
-    s[0] = __ldg(p);
-    s[1] = __ldg(p + 1);
-    s[2] = __ldg(p + sy);
-    s[3] = __ldg(p + sy + 1);
-    s[4] = __ldg(p + sz);
-    s[5] = __ldg(p + sz + 1);
-    s[6] = __ldg(p + sz + sy);
-    s[7] = __ldg(p + sz + sy + 1);
+// Refined rows: the four samples of a column (x; y, y+1; z, z+1) are
+// refineGrid's trilinear interpolations.  They share the column's x position
+// in the coarse grid and, per coarse row (cy, cz), the same x-lerp
+// s(mx) + dx * (s(mx+1) - s(mx)); refineGrid computes exactly these lerps
+// (a, b, c, e in Interpolation::interpolateTrilinearly) before its y and z
+// lerps, so evaluating each distinct row lerp once gives bit-identical values.
+// The rows needed are cy in {j0, j1, j2} x cz in {k0, k1, k2}, the third
+// only when y+1 (z+1) falls into the next coarse cell.
+template <>
+struct RowWalker<RefinedView> {
+    const RefinedView& g;
+    int my, mz;          // coarse cell of the row (for chunk skipping)
+    int J[3], K[3];      // clamped coarse row indices my, my+1, my+2 (and z)
+    int ySecond[2];      // per sample row y, y+1: 0 -> rows (J0, J1), 1 -> rows (J1, J2)
+    int zSecond[2];
+    float dy[2], dz[2];  // in-cell weights of y, y+1 and z, z+1
+    const float* rowPtr[3][3];
+    __device__ RowWalker(const RefinedView& view, int y, int z) : g(view) {
+        int myy[2], mzz[2];
+        for (int t = 0; t < 2; ++t) {
+            const float qy = g.divf(g.unpad(y + t, g.Y));
+            myy[t] = (int)floorf(qy);
+            dy[t] = qy - (float)myy[t];
+            const float qz = g.divf(g.unpad(z + t, g.Z));
+            mzz[t] = (int)floorf(qz);
+            dz[t] = qz - (float)mzz[t];
+        }
+        for (int t = 0; t < 3; ++t) {
+            J[t] = min(max(myy[0] + t, 0), g.cY - 1);
+            K[t] = min(max(mzz[0] + t, 0), g.cZ - 1);
+        }
+        for (int t = 0; t < 2; ++t) {
+            ySecond[t] = myy[t] != myy[0] ? 1 : 0;
+            zSecond[t] = mzz[t] != mzz[0] ? 1 : 0;
+        }
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) rowPtr[a][b] = g.c + ((size_t)K[b] * g.cY + J[a]) * g.cX;
+        my = g.coarseCell(y, g.Y, g.cY);
+        mz = g.coarseCell(z, g.Z, g.cZ);
+    }
+    __device__ __forceinline__ void load(int x, float v[4]) const {
+        if (x >= g.X) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) v[k] = 0.f;
+            return;
+        }
+        const float qx = g.divf(g.unpad(x, g.X));
+        const int mx = (int)floorf(qx);
+        const float dx = qx - (float)mx;
+        const int x0 = min(max(mx, 0), g.cX - 1), x1 = min(max(mx + 1, 0), g.cX - 1);
+        auto lerpX = [&](int a, int b) {
+            const float* p = rowPtr[a][b];
+            const float s0 = __ldg(p + x0), s1 = __ldg(p + x1);
+            return s0 + dx * (s1 - s0);
+        };
+        const bool y2 = ySecond[1], z2 = zSecond[1];
+        const float L00 = lerpX(0, 0), L10 = lerpX(1, 0), L01 = lerpX(0, 1), L11 = lerpX(1, 1);
+        float L20 = 0.f, L21 = 0.f, L02 = 0.f, L12 = 0.f, L22 = 0.f;
+        if (y2) {
+            L20 = lerpX(2, 0);
+            L21 = lerpX(2, 1);
+        }
+        if (z2) {
+            L02 = lerpX(0, 2);
+            L12 = lerpX(1, 2);
+            if (y2) L22 = lerpX(2, 2);
+        }
+        // row lerp (j, k) by warp-uniform selects (no local-memory array)
+        auto pick = [&](int j, int k) -> float {
+            const float r0 = k == 0 ? L00 : (k == 1 ? L01 : L02);
+            const float r1 = k == 0 ? L10 : (k == 1 ? L11 : L12);
+            const float r2 = k == 0 ? L20 : (k == 1 ? L21 : L22);
+            return j == 0 ? r0 : (j == 1 ? r1 : r2);
+        };
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int ys = t & 1, zs = t >> 1;  // v[0] (y,z) v[1] (y+1,z) v[2] (y,z+1) v[3] (y+1,z+1)
+            const int ja = ySecond[ys], kb = zSecond[zs];
+            const float a = pick(ja, kb), b = pick(ja + 1, kb), c = pick(ja, kb + 1), e = pick(ja + 1, kb + 1);
+            const float wy = dy[ys], wz = dz[zs];
+            const float lo = (1.f - wy) * a + wy * b;
+            const float hi = (1.f - wy) * c + wy * e;
+            v[t] = (1.f - wz) * lo + wz * hi;
+        }
+    }
+    // refined cells x in [start(m), end(m)) lie in coarse cell m (along x)
+    __device__ __forceinline__ int coarseStart(int m) const { return g.pad ? (m == 0 ? 0 : m * (g.r + 1) + 1) : m * (g.r + 1); }
+    __device__ __forceinline__ int coarseEnd(int m) const { return m == g.cX - 2 ? g.X - 1 : coarseStart(m + 1); }
+    // may any cell x0..x0+31 of the row cross iso (uniform over the warp)
+    __device__ __forceinline__ bool chunkMayCross(int x0) const {
+        if (!g.mayCross) return true;
+        const int lastCell = min(x0 + 31, g.X - 2);
+        const int m0 = g.coarseCell(x0, g.X, g.cX), m1 = g.coarseCell(lastCell, g.X, g.cX);
+        for (int m = m0; m <= m1; ++m)
+            if (g.coarseMayCross(m, my, mz)) return true;
+        return false;
+    }
+};
+
+// the eight corner values of the lane's cell: own column and the next one
+template <class View>
+__device__ __forceinline__ void chunkCorners(const RowWalker<View>& w, int x0, int lane, float s[8]) {
+    float cur[4], ext[4];
+    w.load(x0 + lane, cur);
+    if (lane == 31) w.load(x0 + 32, ext);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float right = __shfl_down_sync(0xffffffffu, cur[k], 1);
+        s[2 * k] = cur[k];
+        s[2 * k + 1] = lane == 31 ? ext[k] : right;
+    }
+}
+
+// the same with the next chunk's columns already loaded (plain grids)
+__device__ __forceinline__ void cellCorners(const float cur[4], const float nxt[4], int lane, float s[8]) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float right = __shfl_down_sync(0xffffffffu, cur[k], 1);
+        const float wrap = __shfl_sync(0xffffffffu, nxt[k], 0);
+        s[2 * k] = cur[k];
+        s[2 * k + 1] = lane == 31 ? wrap : right;
+    }
+}
+
+__device__ __forceinline__ int caseOf(const float s[8], float iso) {
     int cs = 0;
 #pragma unroll
     for (int i = 0; i < 8; ++i) cs |= (s[i] >= iso ? 1 : 0) << i;
-    cc.cs = cs;
-    cc.nv = 0;
-    cc.nq = 0;
-    cc.c = 0;
-    if (cs == 0 || cs == 255) return;
-    cc.c = cellContours(cs, s, iso, table);
-    cc.nv = numContours(cc.c);
-    // quads owned: the three edges leaving corner 0 (local edges 0, 3, 8),
-    // when all four cells around the edge exist
-    cc.nq = ((((cs ^ (cs >> 1)) & 1) && y >= 1 && z >= 1) ? 1 : 0) +
-            ((((cs ^ (cs >> 2)) & 1) && x >= 1 && z >= 1) ? 1 : 0) +
-            ((((cs ^ (cs >> 4)) & 1) && x >= 1 && y >= 1) ? 1 : 0);
+    return cs;
 }
 
-__device__ __forceinline__ void stageTable(uint64_t* sh) {
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) sh[i] = kContourTable[i];
-    __syncthreads();
+// quads owned by a cell: the three edges leaving corner 0 (local edges 0, 3,
+// 8), when all four cells around the edge exist
+__device__ __forceinline__ int ownedQuads(int cs, int x, int y, int z) {
+    return ((((cs ^ (cs >> 1)) & 1) && y >= 1 && z >= 1) ? 1 : 0) +
+           ((((cs ^ (cs >> 2)) & 1) && x >= 1 && z >= 1) ? 1 : 0) +
+           ((((cs ^ (cs >> 4)) & 1) && x >= 1 && y >= 1) ? 1 : 0);
 }
 
-// per-row (active cells, vertices, owned quads)
-__global__ void __launch_bounds__(256) kRowCount(GridView g, float iso, int4* __restrict__ rowCounts, int numRows) {
-    __shared__ uint64_t table[256];
-    stageTable(table);
+// Visits the cells of one row and calls f(x, s[8]) once per lane and step
+// (warp-uniform calls; lanes without a cell get x = X, which every caller
+// rejects).  Plain grids: chunks of 32 consecutive cells, the next chunk's
+// columns loaded ahead.  Refined grids: only the cells of coarse cells that
+// may cross iso, packed into the lanes (the g-th candidate coarse cell of a
+// 32-cell mask word fills lanes g*W .. g*W+W-1, W = widest coarse cell), in
+// increasing x.
+template <class View, class F>
+__device__ __forceinline__ void walkRow(const View& g, int y, int z, int lane, F&& f) {
+    const RowWalker<View> w(g, y, z);
+    if constexpr (View::kRefined) {
+        const int nc = g.cX - 1;  // coarse cells along x
+        if (!g.mayCross || nc < 1) {
+            for (int x0 = 0; x0 < g.X - 1; x0 += 32) {
+                float s[8];
+                chunkCorners(w, x0, lane, s);
+                f(x0 + lane, s);
+            }
+            return;
+        }
+        const int W = (g.r + 1) + (g.pad ? 2 : 0);
+        const size_t rowBit = ((size_t)w.mz * (g.cY - 1) + w.my) * (size_t)nc;
+        for (int wb = 0; wb < nc; wb += 32) {
+            // the 32 coarse cells wb .. wb+31 of this row (the bits may straddle two words)
+            const size_t b0 = rowBit + wb;
+            const uint32_t lo = __ldg(g.mayCross + (b0 >> 5)), hi = __ldg(g.mayCross + (b0 >> 5) + 1);
+            uint32_t word = (b0 & 31) ? ((lo >> (b0 & 31)) | (hi << (32 - (b0 & 31)))) : lo;
+            if (nc - wb < 32) word &= (1u << (nc - wb)) - 1u;
+            const int nset = __popc(word);
+            if (W <= 32) {
+                const int G = 32 / W;
+                for (int g0 = 0; g0 < nset; g0 += G) {
+                    const int gi = g0 + lane / W, k = lane % W;
+                    int x = g.X;
+                    if (lane < G * W && gi < nset) {
+                        const int m = wb + (int)__fns(word, 0, gi + 1);
+                        const int xs = w.coarseStart(m);
+                        if (xs + k < w.coarseEnd(m)) x = xs + k;
+                    }
+                    float cur[4], nxt[4], s[8];
+                    w.load(x, cur);
+                    w.load(x + 1, nxt);
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        s[2 * t] = cur[t];
+                        s[2 * t + 1] = nxt[t];
+                    }
+                    f(x, s);
+                }
+            } else {
+                for (int gi = 0; gi < nset; ++gi) {
+                    const int m = wb + (int)__fns(word, 0, gi + 1);
+                    const int xs = w.coarseStart(m), xe = w.coarseEnd(m);
+                    for (int k0 = 0; k0 < xe - xs; k0 += 32) {
+                        const int x = (xs + k0 + lane < xe) ? xs + k0 + lane : g.X;
+                        float cur[4], nxt[4], s[8];
+                        w.load(x, cur);
+                        w.load(x + 1, nxt);
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) {
+                            s[2 * t] = cur[t];
+                            s[2 * t + 1] = nxt[t];
+                        }
+                        f(x, s);
+                    }
+                }
+            }
+        }
+    } else {
+        float cur[4], nxt[4];
+        w.load(lane, cur);
+        for (int x0 = 0; x0 < g.X - 1; x0 += 32) {
+            w.load(x0 + 32 + lane, nxt);
+            float s[8];
+            cellCorners(cur, nxt, lane, s);
+            f(x0 + lane, s);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) cur[k] = nxt[k];
+        }
+    }
+}
+
+// per-row (active cells, owned quads)
+template <class View>
+__global__ void __launch_bounds__(256) kRowCount(View g, float iso, int4* __restrict__ rowCounts, int numRows) {
     const int lane = threadIdx.x & 31;
     const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (row >= numRows) return;
     const int y = row % (g.Y - 1), z = row / (g.Y - 1);
-    int a = 0, v = 0, q = 0;
-    for (int x0 = 0; x0 < g.X - 1; x0 += 32) {
-        const int x = x0 + lane;
+    int a = 0, q = 0;
+    walkRow(g, y, z, lane, [&](int x, const float s[8]) {
         if (x < g.X - 1) {
-            float s[8];
-            CellClass cc;
-            classify(g, x, y, z, iso, table, s, cc);
-            a += cc.nv > 0 ? 1 : 0;
-            v += cc.nv;
-            q += cc.nq;
+            const int cs = caseOf(s, iso);
+            if (cs != 0 && cs != 255) {
+                ++a;
+                q += ownedQuads(cs, x, y, z);
+            }
         }
-    }
+    });
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         a += __shfl_down_sync(0xffffffffu, a, o);
-        v += __shfl_down_sync(0xffffffffu, v, o);
         q += __shfl_down_sync(0xffffffffu, q, o);
     }
-    if (lane == 0) rowCounts[row] = make_int4(a, v, q, 0);
+    if (lane == 0) rowCounts[row] = make_int4(a, q, 0, 0);
 }
 
-void launchRowCount(const GridView& g, float iso, int4* rowCounts, int numRows, cudaStream_t s) {
+void launchRowCount(const GridDesc& g, float iso, int4* rowCounts, int numRows, cudaStream_t s) {
     countLaunch();
-    kRowCount<<<(numRows + 7) / 8, 256, 0, s>>>(g, iso, rowCounts, numRows);
+    if (g.refined) kRowCount<RefinedView><<<(numRows + 7) / 8, 256, 0, s>>>(g.ref, iso, rowCounts, numRows);
+    else kRowCount<PlainView><<<(numRows + 7) / 8, 256, 0, s>>>(g.plain, iso, rowCounts, numRows);
 }
 
-// one active cell: vertices (sliceP, D/CellIntersection.inl:368-439) and record
-__device__ void emitCell(const GridView& g, int x, int y, int z, float iso, bool surfaceIteration,
-                         const float s[8], const CellClass& cc, int vbase, int qbase, ActiveCell* act, int aIdx,
-                         float* __restrict__ pos, float* __restrict__ nrm) {
+// compaction: the active cells of the row in x order, with the number of
+// contours (= vertices) of each cell and its edge -> contour map.  Rows
+// without active cells (known from the count pass) are skipped.
+template <class View>
+__global__ void __launch_bounds__(256) kRowEmit(View g, float iso, const int4* __restrict__ rowOffsets, int numRows,
+                                                ActiveCell* __restrict__ act, int* __restrict__ numVerts,
+                                                int numActive, uint32_t* status) {
+    __shared__ uint64_t table[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kContourTable[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (row >= numRows) return;
+    const int4 base = rowOffsets[row];
+    if (rowOffsets[row + 1].x == base.x) return;
+    const int y = row % (g.Y - 1), z = row / (g.Y - 1);
+    int aRun = base.x, qRun = base.y;
+    const unsigned ltMask = (1u << lane) - 1u;
+    walkRow(g, y, z, lane, [&](int x, const float s[8]) {
+        int cs = 0, nq = 0;
+        if (x < g.X - 1) {
+            cs = caseOf(s, iso);
+            if (cs != 0 && cs != 255) nq = ownedQuads(cs, x, y, z);
+        }
+        const bool active = cs != 0 && cs != 255;
+        const unsigned ballot = __ballot_sync(0xffffffffu, active);
+        int qInc = nq;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int u = __shfl_up_sync(0xffffffffu, qInc, o);
+            if (lane >= o) qInc += u;
+        }
+        const int qTot = __shfl_sync(0xffffffffu, qInc, 31);
+        if (active) {
+            const int aIdx = aRun + __popc(ballot & ltMask);
+            if (aIdx < numActive) {
+                const uint64_t c = cellContours(cs, s, iso, table);
+                uint32_t emap = 0;
+                int before = 0;
+                const int n = numContours(c);
+                for (int t = 0; t < n; ++t) {
+                    const int sz = nib(c, t);
+                    for (int i = 0; i < sz; ++i) emap |= (uint32_t)t << (2 * (int)((c >> (16 + 4 * (before + i))) & 0xF));
+                    before += sz;
+                }
+                ActiveCell rec;
+                rec.cell = (uint32_t)(((size_t)z * g.Y + y) * g.X + x);
+                rec.qbase = qRun + qInc - nq;
+                rec.info = (uint32_t)cs | (emap << 8);
+                rec.pad = 0;
+                act[aIdx] = rec;
+                numVerts[aIdx] = n;
+            } else {
+                atomicOr(status, kStatusCountMismatch);
+            }
+        }
+        aRun += __popc(ballot);
+        qRun += qTot;
+    });
+}
+
+void launchRowEmit(const GridDesc& g, float iso, const int4* rowOffsets, int numRows, ActiveCell* act, int* numVerts,
+                   int numActive, uint32_t* status, cudaStream_t s) {
+    countLaunch();
+    if (g.refined)
+        kRowEmit<RefinedView><<<(numRows + 7) / 8, 256, 0, s>>>(g.ref, iso, rowOffsets, numRows, act, numVerts, numActive,
+                                                                status);
+    else
+        kRowEmit<PlainView><<<(numRows + 7) / 8, 256, 0, s>>>(g.plain, iso, rowOffsets, numRows, act, numVerts, numActive,
+                                                              status);
+}
+
+// ---------------------------------------------------------------------------
+// vertices of the active cells (sliceP's vertex part, D/CellIntersection.inl:
+// 368-439), one thread per active cell
+// ---------------------------------------------------------------------------
+template <class View>
+__global__ void __launch_bounds__(128) kVertices(View g, float iso, int surfaceIteration,
+                                                 const ActiveCell* __restrict__ act, const int* __restrict__ vbase,
+                                                 int numActive, int numVertices, float* __restrict__ pos,
+                                                 float* __restrict__ nrm, uint32_t* status) {
+    __shared__ uint64_t table[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kContourTable[i];
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= numActive) return;
+    const ActiveCell rec = act[i];
+    const int x = (int)(rec.cell % (uint32_t)g.X);
+    const int y = (int)((rec.cell / (uint32_t)g.X) % (uint32_t)g.Y);
+    const int z = (int)(rec.cell / ((uint32_t)g.X * (uint32_t)g.Y));
+    const int vb = vbase[i];
+    const int cs = (int)(rec.info & 255u);
+    float s[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s[k] = g.at(x + (k & 1), y + ((k >> 1) & 1), z + ((k >> 2) & 1));
+    const uint64_t c = cellContours(cs, s, iso, table);
+    const int n = numContours(c);
+    if (vb < 0 || vb + n > numVertices) {
+        atomicOr(status, kStatusCountMismatch);
+        return;
+    }
     F3 normals[8];
     cornerGradients(g, x, y, z, s, normals);
-    const int n = cc.nv;
-    uint32_t emap = 0;
     int before = 0;
     for (int t = 0; t < n; ++t) {
-        const int sz = nib(cc.c, t);
-        F3 p = f3(0.f, 0.f, 0.f);
-        for (int i = 0; i < sz; ++i) {
-            const int e = (int)((cc.c >> (16 + 4 * (before + i))) & 0xF);
+        const int csz = nib(c, t);
+        F3 q = f3(0.f, 0.f, 0.f);
+        for (int k = 0; k < csz; ++k) {
+            const int e = (int)((c >> (16 + 4 * (before + k))) & 0xF);
             const int a0 = edgeV0(e), a1 = edgeV1(e);
             const float w = (iso - s[a0]) / (s[a1] - s[a0]);
             // computeLocalCoordinateOffset (:176-200): the edge's axis gets the
             // crossing, the other two axes corner a0's coordinate
             const int ax = edgeAxis(e);
-            F3 off = f3(ax == 0 ? w : (float)(a0 & 1), ax == 1 ? w : (float)((a0 >> 1) & 1),
-                        ax == 2 ? w : (float)((a0 >> 2) & 1));
-            p = p + off;
-            emap |= (uint32_t)t << (2 * e);
+            q = q + f3(ax == 0 ? w : (float)(a0 & 1), ax == 1 ? w : (float)((a0 >> 1) & 1),
+                       ax == 2 ? w : (float)((a0 >> 2) & 1));
         }
-        before += sz;
-        p = p / (float)sz;
+        before += csz;
+        q = q / (float)csz;
         if (surfaceIteration) {
             SurfaceIterator it{s, iso};
-            it.move(p);
+            it.move(q);
         }
-        F3 nm = gnormalize(trilinear3(normals, p));
-        F3 wp = g.origin() + (f3((float)x, (float)y, (float)z) + p) * g.deltas();
-        const int64_t vi = (int64_t)vbase + t;
+        const F3 nm = gnormalize(trilinear3(normals, q));
+        const F3 wp = g.origin() + (f3((float)x, (float)y, (float)z) + q) * g.deltas();
+        const int64_t vi = (int64_t)vb + t;
         pos[3 * vi] = wp.x;
         pos[3 * vi + 1] = wp.y;
         pos[3 * vi + 2] = wp.z;
@@ -181,66 +521,19 @@ __device__ void emitCell(const GridView& g, int x, int y, int z, float iso, bool
         nrm[3 * vi + 1] = nm.y;
         nrm[3 * vi + 2] = nm.z;
     }
-    ActiveCell rec;
-    rec.cell = (uint32_t)(((size_t)z * g.Y + y) * g.X + x);
-    rec.vbase = vbase;
-    rec.qbase = qbase;
-    rec.info = (uint32_t)cc.cs | (emap << 8);
-    act[aIdx] = rec;
 }
 
-__global__ void __launch_bounds__(256) kRowEmit(GridView g, float iso, int surfaceIteration,
-                                                const int4* __restrict__ rowOffsets, int numRows,
-                                                ActiveCell* __restrict__ act, float* __restrict__ pos,
-                                                float* __restrict__ nrm, int numActive, int numVertices,
-                                                uint32_t* status) {
-    __shared__ uint64_t table[256];
-    stageTable(table);
-    const int lane = threadIdx.x & 31;
-    const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (row >= numRows) return;
-    const int y = row % (g.Y - 1), z = row / (g.Y - 1);
-    const int4 base = rowOffsets[row];
-    int aRun = base.x, vRun = base.y, qRun = base.z;
-    const unsigned ltMask = (1u << lane) - 1u;
-    for (int x0 = 0; x0 < g.X - 1; x0 += 32) {
-        const int x = x0 + lane;
-        float s[8];
-        CellClass cc;
-        cc.nv = 0;
-        cc.nq = 0;
-        if (x < g.X - 1) classify(g, x, y, z, iso, table, s, cc);
-        const bool active = cc.nv > 0;
-        const unsigned ballot = __ballot_sync(0xffffffffu, active);
-        int vInc = cc.nv, qInc = cc.nq;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int u = __shfl_up_sync(0xffffffffu, vInc, o);
-            int w = __shfl_up_sync(0xffffffffu, qInc, o);
-            if (lane >= o) { vInc += u; qInc += w; }
-        }
-        const int vTot = __shfl_sync(0xffffffffu, vInc, 31);
-        const int qTot = __shfl_sync(0xffffffffu, qInc, 31);
-        if (active) {
-            const int aIdx = aRun + __popc(ballot & ltMask), vIdx = vRun + vInc - cc.nv;
-            // the counts of the first pass bound every write of this one
-            if (aIdx < numActive && vIdx + cc.nv <= numVertices)
-                emitCell(g, x, y, z, iso, surfaceIteration != 0, s, cc, vIdx, qRun + qInc - cc.nq, act, aIdx, pos, nrm);
-            else
-                atomicOr(status, kStatusCountMismatch);
-        }
-        aRun += __popc(ballot);
-        vRun += vTot;
-        qRun += qTot;
-    }
-}
-
-void launchRowEmit(const GridView& g, float iso, int surfaceIteration, const int4* rowOffsets, int numRows,
-                   ActiveCell* act, float* pos, float* nrm, int numActive, int numVertices, uint32_t* status,
-                   cudaStream_t s) {
+void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, const int* vbase,
+                    int numActive, int numVertices, float* pos, float* nrm, uint32_t* status, cudaStream_t s) {
+    if (numActive <= 0) return;
     countLaunch();
-    kRowEmit<<<(numRows + 7) / 8, 256, 0, s>>>(g, iso, surfaceIteration, rowOffsets, numRows, act, pos, nrm, numActive,
-                                                numVertices, status);
+    const unsigned blocks = (unsigned)((numActive + 127) / 128);
+    if (g.refined)
+        kVertices<RefinedView><<<blocks, 128, 0, s>>>(g.ref, iso, surfaceIteration, act, vbase, numActive, numVertices, pos,
+                                                      nrm, status);
+    else
+        kVertices<PlainView><<<blocks, 128, 0, s>>>(g.plain, iso, surfaceIteration, act, vbase, numActive, numVertices,
+                                                    pos, nrm, status);
 }
 
 // ---------------------------------------------------------------------------
@@ -278,10 +571,10 @@ __device__ __forceinline__ void cellsAroundEdge(int axis, int d[4][3], int e[4])
     }
 }
 
-__global__ void kQuads(const ActiveCell* __restrict__ act, int numActive, const int4* __restrict__ rowOffsets, int X,
-                       int Y, Bucket* __restrict__ table, unsigned long long cap, int4* __restrict__ he,
-                       int* __restrict__ faceFirst, uint16_t* __restrict__ faceAttr, int numQuads, int numVertices,
-                       uint32_t* status) {
+__global__ void kQuads(const ActiveCell* __restrict__ act, const int* __restrict__ vbase, int numActive,
+                       const int4* __restrict__ rowOffsets, int X, int Y, Bucket* __restrict__ table,
+                       unsigned long long cap, int4* __restrict__ he, int* __restrict__ faceFirst,
+                       uint16_t* __restrict__ faceAttr, int numQuads, int numVertices, uint32_t* status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= numActive) return;
     const ActiveCell rec = act[i];
@@ -301,6 +594,7 @@ __global__ void kQuads(const ActiveCell* __restrict__ act, int numActive, const 
         int quad[4] = {-1, -1, -1, -1};
         for (int k = 0; k < 4; ++k) {
             ActiveCell r2 = rec;
+            int vb2 = vbase[i];
             if (k > 0) {
                 const int cx = x + d[k][0], cy = y + d[k][1], cz = z + d[k][2];
                 const uint32_t cell = (uint32_t)(((size_t)cz * Y + cy) * X + cx);
@@ -310,13 +604,14 @@ __global__ void kQuads(const ActiveCell* __restrict__ act, int numActive, const 
                     continue;
                 }
                 r2 = act[j];
+                vb2 = vbase[j];
             }
             const int e = le[k];
             const int t = (int)((r2.info >> (8 + 2 * e)) & 3u);
             const int edgy = ((r2.info >> edgeV0(e)) & 1u) ? 0 : 1;  // s[v0] < iso
             const int slot = quadSlot(e, edgy);
             if (quad[slot] != -1) atomicOr(status, kStatusSlotConflict);
-            quad[slot] = r2.vbase + t;
+            quad[slot] = vb2 + t;
         }
         if (qi >= numQuads || quad[0] < 0 || quad[1] < 0 || quad[2] < 0 || quad[3] < 0 || quad[0] >= numVertices ||
             quad[1] >= numVertices || quad[2] >= numVertices || quad[3] >= numVertices) {
@@ -335,12 +630,12 @@ __global__ void kQuads(const ActiveCell* __restrict__ act, int numActive, const 
     }
 }
 
-void launchQuads(const ActiveCell* act, int numActive, const int4* rowOffsets, int X, int Y, Bucket* table,
-                 unsigned long long cap, int4* he, int* faceFirst, uint16_t* faceAttr, int numQuads, int numVertices,
-                 uint32_t* status, cudaStream_t s) {
+void launchQuads(const ActiveCell* act, const int* vbase, int numActive, const int4* rowOffsets, int X, int Y,
+                 Bucket* table, unsigned long long cap, int4* he, int* faceFirst, uint16_t* faceAttr, int numQuads,
+                 int numVertices, uint32_t* status, cudaStream_t s) {
     if (numActive <= 0) return;
     countLaunch();
-    kQuads<<<(numActive + 255) / 256, 256, 0, s>>>(act, numActive, rowOffsets, X, Y, table, cap, he, faceFirst,
+    kQuads<<<(numActive + 255) / 256, 256, 0, s>>>(act, vbase, numActive, rowOffsets, X, Y, table, cap, he, faceFirst,
                                                    faceAttr, numQuads, numVertices, status);
 }
 

@@ -16,6 +16,14 @@ inline void countLaunch(int n = 1) { g_kernelLaunches.fetch_add(n, std::memory_o
 
 __device__ __forceinline__ void setTwinOut(int4* he, int h, int t) { reinterpret_cast<int*>(he)[4 * (int64_t)h + 3] = t; }
 
+// the grid a run reads: dense, or refined/padded on demand from a coarse grid
+struct GridDesc {
+    bool refined;
+    PlainView plain;
+    RefinedView ref;
+    const GridGeom& geom() const { return refined ? static_cast<const GridGeom&>(ref) : static_cast<const GridGeom&>(plain); }
+};
+
 // splitter working copies (device pointers)
 struct SplitWork {
     float* pos;
@@ -44,20 +52,22 @@ struct SplitWork {
 };
 
 void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int pad, cudaStream_t s);
-void launchRowCount(const GridView& g, float iso, int4* rowCounts, int numRows, cudaStream_t s);
-void launchRowEmit(const GridView& g, float iso, int surfaceIteration, const int4* rowOffsets, int numRows,
-                   ActiveCell* act, float* pos, float* nrm, int numActive, int numVertices, uint32_t* status,
-                   cudaStream_t s);
-void launchQuads(const ActiveCell* act, int numActive, const int4* rowOffsets, int X, int Y, Bucket* table,
-                 unsigned long long cap, int4* he, int* faceFirst, uint16_t* faceAttr, int numQuads, int numVertices,
-                 uint32_t* status, cudaStream_t s);
+void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, cudaStream_t s);
+void launchRowCount(const GridDesc& g, float iso, int4* rowCounts, int numRows, cudaStream_t s);
+void launchRowEmit(const GridDesc& g, float iso, const int4* rowOffsets, int numRows, ActiveCell* act, int* numVerts,
+                   int numActive, uint32_t* status, cudaStream_t s);
+void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, const int* vbase,
+                    int numActive, int numVertices, float* pos, float* nrm, uint32_t* status, cudaStream_t s);
+void launchQuads(const ActiveCell* act, const int* vbase, int numActive, const int4* rowOffsets, int X, int Y,
+                 Bucket* table, unsigned long long cap, int4* he, int* faceFirst, uint16_t* faceAttr, int numQuads,
+                 int numVertices, uint32_t* status, cudaStream_t s);
 
 void launchBuckets(Bucket* table, unsigned long long cap, int4* he, uint16_t* faceAttr, uint8_t* vflags,
                    int connectTwins, int* nmList, DevCounters* ctr, MeshDims md, cudaStream_t s);
 void launchInsertFaces(const int4* he, const int* faceFirst, MeshDims md, Bucket* table, unsigned long long cap,
                        uint32_t* status, cudaStream_t s);
 void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s);
-void launchReconnect(const GridView& g, float iso, const Bucket* table, const int* nmList, const DevCounters* ctr,
+void launchReconnect(const GridDesc& g, float iso, const Bucket* table, const int* nmList, const DevCounters* ctr,
                      int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s);
 void launchDetectFans(const int4* he, MeshDims md, uint8_t* isKey, int* fans, uint8_t* vflags, DevCounters* ctr,
                       uint32_t* status, cudaStream_t s);
@@ -75,7 +85,7 @@ void launchSplitSubdivide(int n, const SplitWork& w, uint32_t* status, cudaStrea
 void launchSplitCollapse(const SplitWork& w, uint32_t* status, cudaStream_t s);
 void launchSplitMerge(const SplitWork& w, uint32_t* status, cudaStream_t s);
 void launchSplitMergeHalfedges(const SplitWork& w, uint32_t* status, cudaStream_t s);
-void launchSplitMove(const GridView& g, float iso, const SplitWork& w, cudaStream_t s);
+void launchSplitMove(const GridDesc& g, float iso, const SplitWork& w, cudaStream_t s);
 void launchSplitFlagAppends(int count, const uint32_t* fl, const int* c2o, int* out, cudaStream_t s);
 void launchSplitCopyBack(const SplitWork& w, const int* appV, const int* appH, const int* appF, int V2, int H2, int F2,
                          float* pos, float* nrm, int4* he, int* faceFirst, uint16_t* faceAttr, uint32_t* status,

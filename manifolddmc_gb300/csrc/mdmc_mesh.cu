@@ -179,7 +179,8 @@ __device__ __forceinline__ F3 nudge(int it) {
 
 __device__ __forceinline__ F3 loadP(const float* pos, int v) { return f3(pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]); }
 
-__global__ void kReconnect(GridView g, float iso, const Bucket* __restrict__ table, const int* __restrict__ nmList,
+template <class View>
+__global__ void kReconnect(View g, float iso, const Bucket* __restrict__ table, const int* __restrict__ nmList,
                            const DevCounters* ctr, int4* he, const float* __restrict__ pos, MeshDims md,
                            uint32_t* status) {
     const int count = min((int)ctr->nmBuckets, md.H / 4 + 1);
@@ -248,10 +249,10 @@ __global__ void kReconnect(GridView g, float iso, const Bucket* __restrict__ tab
         }
         if (mn[0] < 0 || mn[1] < 0 || mn[2] < 0 || mn[0] + 1 >= g.X || mn[1] + 1 >= g.Y || mn[2] + 1 >= g.Z)
             atomicOr(status, kStatusWallOutOfGrid);
-        const float w0 = g.atClamped(mn[0], mn[1], mn[2]);
-        const float w1 = g.atClamped(mn[0] + xo[0], mn[1] + xo[1], mn[2] + xo[2]);
-        const float w2 = g.atClamped(mn[0] + xo[0] + yo[0], mn[1] + xo[1] + yo[1], mn[2] + xo[2] + yo[2]);
-        const float w3 = g.atClamped(mn[0] + yo[0], mn[1] + yo[1], mn[2] + yo[2]);
+        const float w0 = atClamped(g, mn[0], mn[1], mn[2]);
+        const float w1 = atClamped(g, mn[0] + xo[0], mn[1] + xo[1], mn[2] + xo[2]);
+        const float w2 = atClamped(g, mn[0] + xo[0] + yo[0], mn[1] + xo[1] + yo[1], mn[2] + xo[2] + yo[2]);
+        const float w3 = atClamped(g, mn[0] + yo[0], mn[1] + yo[1], mn[2] + yo[2]);
         const F3 corner0 = g.origin() + g.deltas() * f3((float)mn[0], (float)mn[1], (float)mn[2]);
         const F3 corner2 = g.origin() + g.deltas() * f3((float)(mn[0] + xo[0] + yo[0]), (float)(mn[1] + xo[1] + yo[1]),
                                                         (float)(mn[2] + xo[2] + yo[2]));
@@ -295,10 +296,11 @@ __global__ void kReconnect(GridView g, float iso, const Bucket* __restrict__ tab
     }
 }
 
-void launchReconnect(const GridView& g, float iso, const Bucket* table, const int* nmList, const DevCounters* ctr,
+void launchReconnect(const GridDesc& g, float iso, const Bucket* table, const int* nmList, const DevCounters* ctr,
                      int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s) {
     countLaunch();
-    kReconnect<<<152 * 2, 128, 0, s>>>(g, iso, table, nmList, ctr, he, pos, md, status);
+    if (g.refined) kReconnect<RefinedView><<<152 * 2, 128, 0, s>>>(g.ref, iso, table, nmList, ctr, he, pos, md, status);
+    else kReconnect<PlainView><<<152 * 2, 128, 0, s>>>(g.plain, iso, table, nmList, ctr, he, pos, md, status);
 }
 
 // ---------------------------------------------------------------------------

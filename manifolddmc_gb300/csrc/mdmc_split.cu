@@ -391,7 +391,8 @@ __global__ void kMergeHalfedges(SplitWork w, uint32_t* status) {
 }
 
 // performMoveVerticesToSurface (:1130-1160)
-__global__ void kMoveVertices(GridView g, float iso, SplitWork w) {
+template <class View>
+__global__ void kMoveVertices(View g, float iso, SplitWork w) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= w.nv) return;
     if (w.vfl[v] & kRemove) return;
@@ -399,7 +400,7 @@ __global__ void kMoveVertices(GridView g, float iso, SplitWork w) {
     int idx[3];
     g.cellOf(p, idx);
     float s[8];
-    g.corners(idx[0], idx[1], idx[2], s);
+    corners(g, idx[0], idx[1], idx[2], s);
     const F3 fi = f3((float)idx[0], (float)idx[1], (float)idx[2]);
     const F3 fi1 = f3((float)(idx[0] + 1), (float)(idx[1] + 1), (float)(idx[2] + 1));
     const F3 mn = g.origin() + fi * g.deltas();
@@ -536,9 +537,10 @@ void launchSplitMergeHalfedges(const SplitWork& w, uint32_t* status, cudaStream_
     countLaunch();
     kMergeHalfedges<<<nb(w.nh, 128), 128, 0, s>>>(w, status);
 }
-void launchSplitMove(const GridView& g, float iso, const SplitWork& w, cudaStream_t s) {
+void launchSplitMove(const GridDesc& g, float iso, const SplitWork& w, cudaStream_t s) {
     countLaunch();
-    kMoveVertices<<<nb(w.nv, 128), 128, 0, s>>>(g, iso, w);
+    if (g.refined) kMoveVertices<RefinedView><<<nb(w.nv, 128), 128, 0, s>>>(g.ref, iso, w);
+    else kMoveVertices<PlainView><<<nb(w.nv, 128), 128, 0, s>>>(g.plain, iso, w);
 }
 void launchSplitFlagAppends(int count, const uint32_t* fl, const int* c2o, int* out, cudaStream_t s) {
     if (count <= 0) return;

@@ -50,14 +50,15 @@ constexpr unsigned long long kEmptyKey = ~0ULL;
 
 // Active cell record written by the DMC emit pass (16 bytes):
 //   cell  = linear sample index of the cell's corner 0
-//   vbase = index of the cell's first vertex
 //   qbase = index of the first quad the cell owns
 //   info  = case (8 bits) | edge -> contour map (2 bits per edge) << 8
+// The index of a cell's first vertex lives in a separate array (a prefix sum
+// over the cells' contour counts).
 struct __align__(16) ActiveCell {
     uint32_t cell;
-    int32_t vbase;
     int32_t qbase;
     uint32_t info;
+    int32_t pad;
 };
 
 // Device counters filled during a run and read back once at its end.

@@ -193,3 +193,22 @@ def test_write_obj_matches_reference_format(tmp_path):
     assert len(v) == len(m.positions) and len(f) == len(m.quads)
     first = [int(t.split("//")[0]) - 1 for t in f[0].split()[1:]]
     assert first == list(m.quads[0])
+
+
+@pytest.mark.parametrize("refinement,pad", [(0, True), (1, False), (2, False), (3, True)])
+def test_materialized_refinement_bit_exact(refinement, pad):
+    # the kernels read refined grids on demand; the dense form written by
+    # mdmc_materialize_grid must equal refineGrid's output (oracle)
+    import torch
+    vol = blobs(11, 4, 31)
+    dims = [11, 11, 11]
+    origin = np.array([0.5, -2.0, 1.0], np.float32)
+    spacing = np.array([0.3, 0.7, 1.1], np.float32)
+    grid = mdmc.UniformGrid(vol, dims, origin, spacing, refinement, pad)
+    out = torch.empty(grid.get_cell_count(), dtype=torch.float32, device="cuda")
+    grid.materialize(out.data_ptr())
+    torch.cuda.synchronize()
+    ref, d, o, s = oracle_refine(vol.reshape(-1), dims, origin, spacing, refinement, pad)
+    assert grid.dimensions == d
+    assert np.array_equal(grid.origin, o) and np.array_equal(grid.deltas, s)
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), ref.view(np.uint32))
