@@ -213,6 +213,25 @@ MDMC_API const char* mdmc_last_error(const mdmc_context* context);
  * s_triangleAmbiguities, DualMarchingCubes.cpp:301,564). */
 MDMC_API void mdmc_case_tables(uint64_t contour_words[256], uint8_t ambiguous[256]);
 
+/* The count pass of mdmc_run without a context and without allocating:
+ * writes {active cells, DMC quads} of the grid at iso_value to totals, two
+ * int64 in DEVICE memory, asynchronously on the stream (equal to
+ * mdmc_stats.num_active_cells and num_dmc_quads of an mdmc_run).  This entry
+ * point has no counterpart in the reference.  It is for callers that cannot
+ * allocate device memory: code that sizes its buffers inside a stream or frame
+ * loop with a fixed device-memory pool, or that must not stall the device
+ * (cudaMalloc/cudaFree synchronize it, and mdmc_run grows its buffers with
+ * them).  Its scratch is a fixed device array shared by every call on a
+ * device: at most 2^18 x-rows of cells ((dims[1]-1)*(dims[2]-1)) and, for a
+ * refined grid, 2^24 coarse cells; larger grids return MDMC_ERROR_LIMIT before
+ * any work.  Calls that overlap on the GPU race on the scratch: serialize
+ * them.  The first call on a device (with that device current) looks up the
+ * scratch there, which loads this code onto the device; make it before any
+ * stream capture.  message (may be NULL) receives an error description of at
+ * most message_len bytes. */
+MDMC_API mdmc_status mdmc_count_cells_noalloc(const mdmc_grid* grid, float iso_value, int64_t* totals, void* stream,
+                                              char* message, int message_len);
+
 #ifdef __cplusplus
 }
 #endif
