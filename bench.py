@@ -126,7 +126,7 @@ def algorithmic_bytes(kernel, s):
     over them read only the coarse samples (S_in)."""
     S_in, rows = s["samples_in"], s["rows"]
     S = s["samples_in"] if s["refined"] else s["samples"]
-    A, V, Q, cap = s["active"], s["dmc_vertices"], s["dmc_quads"], s["table_buckets"]
+    A, V, Q = s["active"], s["dmc_vertices"], s["dmc_quads"]
     if kernel == "refine":  # coarse-cell pre-pass: coarse samples read, one bit per coarse cell written
         return 4 * S_in + S_in // 8
     if kernel == "count":  # grid read once, per-row counts written
@@ -135,10 +135,8 @@ def algorithmic_bytes(kernel, s):
         return 4 * S + 16 * rows + 16 * A + 4 * A
     if kernel == "vertices":  # records and offsets read, positions + normals written
         return 16 * A + 4 * A + 24 * V
-    if kernel == "quads":  # records read; halfedges, faces, attributes and edge keys written
-        return 16 * A + 64 * Q + 4 * Q + 2 * Q + 4 * Q * 8
-    if kernel == "table":  # buckets read once; twins written
-        return 32 * cap + 16 * Q
+    if kernel == "quads":  # records + vertex offsets read; halfedges (with twins), faces, attributes, valences written
+        return 16 * A + 4 * A + 64 * Q + 4 * Q + 2 * Q + 4 * Q
     raise KeyError(kernel)
 
 
@@ -197,7 +195,7 @@ def run_ours(args, rank, world, local):
     cells = (grid.dims[0] - 1) * (grid.dims[1] - 1) * (grid.dims[2] - 1)
     samples = grid.dims[0] * grid.dims[1] * grid.dims[2]
 
-    per_step, kernel_ms, launches = [], {k: [] for k in ("refine", "count", "emit", "vertices", "quads", "table")}, 0
+    per_step, kernel_ms, launches = [], {k: [] for k in ("refine", "count", "emit", "vertices", "quads")}, 0
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
@@ -212,7 +210,7 @@ def run_ours(args, rank, world, local):
             e1.synchronize()
             per_step.append(e0.elapsed_time(e1))
             for k, f in (("refine", "ms_refine"), ("count", "ms_count"), ("emit", "ms_emit"),
-                         ("vertices", "ms_vertices"), ("quads", "ms_quads"), ("table", "ms_table")):
+                         ("vertices", "ms_vertices"), ("quads", "ms_quads")):
                 kernel_ms[k].append(getattr(stats, f))
             launches += int(stats.kernel_launches)
     torch.cuda.synchronize(dev)
@@ -228,7 +226,7 @@ def run_ours(args, rank, world, local):
     sizes = {"samples_in": int(np.prod(dims_in)), "samples": samples, "rows": (grid.dims[1] - 1) * (grid.dims[2] - 1),
              "refined": bool(refine or pad),
              "active": int(stats.num_active_cells), "dmc_vertices": int(stats.num_dmc_vertices),
-             "dmc_quads": int(stats.num_dmc_quads), "table_buckets": ((3 * int(stats.num_dmc_quads) + 31) // 32) * 32}
+             "dmc_quads": int(stats.num_dmc_quads)}
     kavg = {k: float(np.mean(v)) for k, v in kernel_ms.items()}
     dominant = max(kavg, key=kavg.get)
     peak, peak_kind = peaks()

@@ -140,8 +140,8 @@ typedef struct mdmc_stats {
     float ms_count;                /* per-row counting pass over the grid */
     float ms_emit;                 /* active-cell compaction pass */
     float ms_vertices;             /* dual vertices of the active cells */
-    float ms_quads;                /* quads, halfedges and edge-table inserts */
-    float ms_table;                /* edge-table twins and flags */
+    float ms_quads;                /* quads, halfedges, twins and edge flags (one pass) */
+    float ms_table;                /* edge-table rebuilds of the splitter (0: not timed separately) */
     int64_t kernel_launches;       /* kernels launched by the last run and prepare */
 } mdmc_stats;
 

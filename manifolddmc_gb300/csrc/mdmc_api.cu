@@ -82,7 +82,8 @@ struct mdmc_context {
     DevBuf pos, nrm, he, faceFirst, faceAttr, vflags, vertexHE, quads;
     int64_t V = 0, F = 0, H = 0;
     // edge table
-    DevBuf table, nmList;
+    DevBuf table, nmList, heValence;
+    bool tableValid = false;  // the edge table holds the current mesh (after a splitter refresh)
     unsigned long long cap = 0;
     // counters
     DevBuf counters;
@@ -282,14 +283,16 @@ mdmc_status refreshTable(mdmc_context* c, uint32_t* status, cudaStream_t s) {
     c->cap = tableCapacity(c->F);
     MDMC_CHECK(c, c->table.ensure(sizeof(Bucket) * c->cap));
     MDMC_CHECK(c, cudaMemsetAsync(c->table.p, 0xFF, sizeof(Bucket) * c->cap, s));
-    MDMC_CHECK(c, c->nmList.ensure(sizeof(int) * (size_t)(c->H / 4 + 1)));
+    MDMC_CHECK(c, c->nmList.ensure(sizeof(int4) * (size_t)(c->H / 4 + 1)));
+    MDMC_CHECK(c, c->heValence.ensure((size_t)std::max<int64_t>(c->H, 1)));
     const MeshDims md{(int)c->V, (int)c->F, (int)c->H};
     launchInsertFaces(c->he.as<int4>(), c->faceFirst.as<int>(), md, c->table.as<Bucket>(), c->cap, status, s);
     launchResetFaceFlags(c->faceAttr.as<uint16_t>(), (int)c->F, s);
     MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, (size_t)c->V, s));
     MDMC_CHECK(c, cudaMemsetAsync((char*)c->counters.p + 8, 0, sizeof(DevCounters) - 8, s));
     launchBuckets(c->table.as<Bucket>(), c->cap, c->he.as<int4>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(),
-                  0, c->nmList.as<int>(), c->counters.as<DevCounters>(), md, s);
+                  0, c->heValence.as<uint8_t>(), c->nmList.as<int4>(), c->counters.as<DevCounters>(), md, s);
+    c->tableValid = true;
     return MDMC_OK;
 }
 
@@ -354,7 +357,7 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         // createWorkingCopies (:273-301)
         launchSplitCopy(c->nmFaces.as<int>(), n, c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(),
                         c->pos.as<float>(), c->nrm.as<float>(), w, status, s);
-        launchSplitMarkNM(c->table.as<Bucket>(), c->nmList.as<int>(), ctr, w, status, s);
+        launchSplitMarkNM(c->nmList.as<int4>(), ctr, w, status, s);
         if (doSub) launchSplitSubdivide(n, w, status, s);
         if (step >= MDMC_STEP_COLLAPSE_NON_MANIFOLD_EDGES) {
             launchSplitCollapse(w, status, s);
@@ -637,40 +640,36 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->V = Vd;
     c->F = Q;
     c->H = 4 * Q;
-    c->cap = tableCapacity(Q);
+    c->tableValid = false;
     MDMC_CHECK(c, c->pos.ensure(sizeof(float) * 3 * (size_t)Vd));
     MDMC_CHECK(c, c->nrm.ensure(sizeof(float) * 3 * (size_t)Vd));
     MDMC_CHECK(c, c->vflags.ensure(roundUp((size_t)Vd, 4)));
     MDMC_CHECK(c, c->he.ensure(sizeof(int4) * 4 * (size_t)std::max<int64_t>(Q, 1)));
     MDMC_CHECK(c, c->faceFirst.ensure(sizeof(int) * (size_t)std::max<int64_t>(Q, 1)));
     MDMC_CHECK(c, c->faceAttr.ensure(roundUp(sizeof(uint16_t) * (size_t)std::max<int64_t>(Q, 1), 4)));
-    MDMC_CHECK(c, c->table.ensure(sizeof(Bucket) * c->cap));
-    MDMC_CHECK(c, c->nmList.ensure(sizeof(int) * (size_t)(Q + 1)));
-    MDMC_CHECK(c, cudaMemsetAsync(c->table.p, 0xFF, sizeof(Bucket) * c->cap, s));
+    MDMC_CHECK(c, c->nmList.ensure(sizeof(int4) * (size_t)(Q + 1)));
+    MDMC_CHECK(c, c->heValence.ensure((size_t)std::max<int64_t>(4 * Q, 1)));
     MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)Vd, 4), s));
     cudaEventRecord(c->kev[10], s);
     launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), c->vbase.as<int>(), (int)A,
                    (int)Vd, c->pos.as<float>(), c->nrm.as<float>(), status, s);
     cudaEventRecord(c->kev[11], s);
-    // mapQuadrilaterals + collectHalfedgeElements
+    // mapQuadrilaterals + collectHalfedgeElements, and the halfedge mesh's
+    // twins and flags (HalfedgeMesh::initialize) in the same pass
     cudaEventRecord(c->kev[6], s);
-    launchQuads(c->act.as<ActiveCell>(), c->vbase.as<int>(), (int)A, c->rows.as<int4>(), X, Y, c->table.as<Bucket>(),
-                c->cap, c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(), (int)Q, (int)Vd, status, s);
+    launchQuads(c->act.as<ActiveCell>(), c->vbase.as<int>(), (int)A, c->rows.as<int4>(), X, Y, Z, c->he.as<int4>(),
+                c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(),
+                c->nmList.as<int4>(), (int)(Q + 1), (int)Q, (int)Vd, ctr, s);
     cudaEventRecord(c->kev[7], s);
     MDMC_CHECK(c, cudaGetLastError());
     cudaEventRecord(c->ev[1], s);
-
-    // ---- halfedge mesh: twins and flags (HalfedgeMesh::initialize) -----------
     cudaEventRecord(c->kev[8], s);
     const MeshDims md0{(int)Vd, (int)Q, (int)(4 * Q)};
-    launchBuckets(c->table.as<Bucket>(), c->cap, c->he.as<int4>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), 1,
-                  c->nmList.as<int>(), ctr, md0, s);
     cudaEventRecord(c->kev[9], s);
     cudaEventRecord(c->ev[2], s);
-    MDMC_CHECK(c, cudaGetLastError());
 
     // ---- repair: fixManifoldTwins, then the splitter ---------------------------
-    launchReconnect(g, iso, c->table.as<Bucket>(), c->nmList.as<int>(), ctr, c->he.as<int4>(), c->pos.as<float>(), md0,
+    launchReconnect(g, iso, c->nmList.as<int4>(), ctr, c->he.as<int4>(), c->pos.as<float>(), md0,
                     status, s);
     MDMC_CHECK(c, cudaGetLastError());
     int64_t iterations = 0;
@@ -694,7 +693,8 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)c->F));
     MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)c->V));
     launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), MeshDims{(int)c->V, (int)c->F, (int)c->H},
-                 c->table.as<Bucket>(), c->cap, c->quads.as<int4>(), c->vertexHE.as<int>(), ctr, status, s);
+                 c->tableValid ? c->table.as<Bucket>() : nullptr, c->cap, c->heValence.as<uint8_t>(),
+                 c->quads.as<int4>(), c->vertexHE.as<int>(), ctr, status, s);
     cudaEventRecord(c->ev[5], s);
     MDMC_CHECK(c, cudaGetLastError());
     MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));

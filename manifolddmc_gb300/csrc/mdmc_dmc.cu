@@ -571,72 +571,242 @@ __device__ __forceinline__ void cellsAroundEdge(int axis, int d[4][3], int e[4])
     }
 }
 
-__global__ void kQuads(const ActiveCell* __restrict__ act, const int* __restrict__ vbase, int numActive,
-                       const int4* __restrict__ rowOffsets, int X, int Y, Bucket* __restrict__ table,
-                       unsigned long long cap, int4* __restrict__ he, int* __restrict__ faceFirst,
-                       uint16_t* __restrict__ faceAttr, int numQuads, int numVertices, uint32_t* status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= numActive) return;
-    const ActiveCell rec = act[i];
-    const int cs = (int)(rec.info & 255u);
-    const int x = (int)(rec.cell % (uint32_t)X);
-    const int y = (int)((rec.cell / (uint32_t)X) % (uint32_t)Y);
-    const int z = (int)(rec.cell / ((uint32_t)X * (uint32_t)Y));
-    int qi = rec.qbase;
-    for (int axis = 0; axis < 3; ++axis) {
-        // edges 0, 3, 8 run from corner 0 to corners 1, 2, 4
-        if (!((cs ^ (cs >> (1 << axis))) & 1)) continue;
-        if (axis == 0 && !(y >= 1 && z >= 1)) continue;
-        if (axis == 1 && !(x >= 1 && z >= 1)) continue;
-        if (axis == 2 && !(x >= 1 && y >= 1)) continue;
-        int d[4][3], le[4];
-        cellsAroundEdge(axis, d, le);
-        int quad[4] = {-1, -1, -1, -1};
-        for (int k = 0; k < 4; ++k) {
-            ActiveCell r2 = rec;
-            int vb2 = vbase[i];
-            if (k > 0) {
-                const int cx = x + d[k][0], cy = y + d[k][1], cz = z + d[k][2];
-                const uint32_t cell = (uint32_t)(((size_t)cz * Y + cy) * X + cx);
-                const int j = findActive(act, rowOffsets, cz * (Y - 1) + cy, cell);
-                if (j < 0) {
-                    atomicOr(status, kStatusMissingCell);
-                    continue;
-                }
-                r2 = act[j];
-                vb2 = vbase[j];
-            }
-            const int e = le[k];
-            const int t = (int)((r2.info >> (8 + 2 * e)) & 3u);
-            const int edgy = ((r2.info >> edgeV0(e)) & 1u) ? 0 : 1;  // s[v0] < iso
-            const int slot = quadSlot(e, edgy);
-            if (quad[slot] != -1) atomicOr(status, kStatusSlotConflict);
-            quad[slot] = vb2 + t;
-        }
-        if (qi >= numQuads || quad[0] < 0 || quad[1] < 0 || quad[2] < 0 || quad[3] < 0 || quad[0] >= numVertices ||
-            quad[1] >= numVertices || quad[2] >= numVertices || quad[3] >= numVertices) {
-            atomicOr(status, kStatusCountMismatch);
-            return;
-        }
-        const int h0 = 4 * qi;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) he[h0 + k] = make_int4(quad[k], qi, h0 + ((k + 1) & 3), -1);
-        faceFirst[qi] = h0;
-        const int baseColor = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
-        faceAttr[qi] = (uint16_t)(3 * baseColor + axis);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) edgeInsert(table, cap, quad[k], quad[(k + 1) & 3], h0 + k, status);
-        ++qi;
-    }
+// local index of the cell edge leaving corner `corner` along `axis` (-1: none)
+__device__ __forceinline__ int localEdge(int corner, int axis) {
+    if (axis == 0) return (corner & 1) ? -1 : corner;                          // 0, 2, 4, 6
+    if (axis == 1) return (corner & 2) ? -1 : ((0x5713 >> (4 * ((corner & 1) | ((corner >> 1) & 2)))) & 0xF);  // 3,1,7,5
+    return (corner & 4) ? -1 : ((0xAB98 >> (4 * corner)) & 0xF);              // 8, 9, 11, 10
 }
 
-void launchQuads(const ActiveCell* act, const int* vbase, int numActive, const int4* rowOffsets, int X, int Y,
-                 Bucket* table, unsigned long long cap, int4* he, int* faceFirst, uint16_t* faceAttr, int numQuads,
-                 int numVertices, uint32_t* status, cudaStream_t s) {
+// does the cell at (x,y,z) with case cs own the quad of its corner-0 edge along axis
+__device__ __forceinline__ bool ownsAxis(int cs, int axis, int x, int y, int z) {
+    if (!((cs ^ (cs >> (1 << axis))) & 1)) return false;
+    if (axis == 0) return y >= 1 && z >= 1;
+    if (axis == 1) return x >= 1 && z >= 1;
+    return x >= 1 && y >= 1;
+}
+
+struct CellRec {
+    int c[3];       // coordinates
+    uint32_t info;  // case | edge -> contour map << 8
+    int vbase;
+};
+
+// Quad id of the grid edge (origin o, axis al), or -1 if that edge has no quad
+// (a cell around it is outside the grid, or no sign change / owner record).
+__device__ int quadOfEdge(const int o[3], int al, const ActiveCell* __restrict__ act, const int4* __restrict__ rowOffsets,
+                          int X, int Y, int Z) {
+    const int dims[3] = {X, Y, Z};
+    for (int k = 0; k < 3; ++k) {
+        if (o[k] < 0 || o[k] > dims[k] - 2) return -1;  // the owner cell must exist
+        if (k != al && o[k] < 1) return -1;             // and the cells behind it
+    }
+    const uint32_t cell = (uint32_t)(((size_t)o[2] * Y + o[1]) * X + o[0]);
+    const int j = findActive(act, rowOffsets, o[2] * (Y - 1) + o[1], cell);
+    if (j < 0) return -1;
+    const ActiveCell r = act[j];
+    const int cs = (int)(r.info & 255u);
+    if (!ownsAxis(cs, al, o[0], o[1], o[2])) return -1;
+    int rank = 0;
+    for (int a = 0; a < al; ++a) rank += ownsAxis(cs, a, o[0], o[1], o[2]) ? 1 : 0;
+    return r.qbase + rank;
+}
+
+// The quads (mapQuadrilaterals, D/DualMarchingCubes.cu:72-85), their halfedges
+// (collectHalfedgeElements, D/Halfedges/HalfedgeMesh.cu:14-60) and the twins
+// and flags of connectHalfedgeTwins / refresh*Flags (:92-291), without an edge
+// table.  Halfedge i of quad q runs between the vertices of the face-adjacent
+// cells A (slot i) and B (slot i+1); the only quads that can hold the same
+// vertex pair are those of the four grid edges of the A|B face, and each of
+// them does exactly when its edge lies in the same contours of A and of B.
+// That set is the reference's edge-table bucket; sorted, it gives the twins
+// by the reference's rules.
+__global__ void kQuads(const ActiveCell* __restrict__ act, const int* __restrict__ vbase, int numActive,
+                       const int4* __restrict__ rowOffsets, int X, int Y, int Z, int4* __restrict__ he,
+                       int* __restrict__ faceFirst, uint16_t* __restrict__ faceAttr, uint8_t* vflags,
+                       uint8_t* __restrict__ heValence, int4* __restrict__ nmList, int nmCapacity, int numQuads,
+                       int numVertices, DevCounters* ctr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int nE = 0, nE3 = 0, nE4 = 0;
+    if (i < numActive) {
+        const ActiveCell rec = act[i];
+        const int cs = (int)(rec.info & 255u);
+        const int x = (int)(rec.cell % (uint32_t)X);
+        const int y = (int)((rec.cell / (uint32_t)X) % (uint32_t)Y);
+        const int z = (int)(rec.cell / ((uint32_t)X * (uint32_t)Y));
+        const int p[3] = {x, y, z};
+        int qi = rec.qbase;
+        for (int axis = 0; axis < 3; ++axis) {
+            if (!ownsAxis(cs, axis, x, y, z)) continue;
+            int d[4][3], le[4];
+            cellsAroundEdge(axis, d, le);
+            CellRec cells[4];
+            int slotOf[4];
+            int kOfSlot[4] = {-1, -1, -1, -1};
+            bool ok = true;
+            for (int k = 0; k < 4; ++k) {
+                ActiveCell r2 = rec;
+                int vb2 = vbase[i];
+                if (k > 0) {
+                    const int cx = x + d[k][0], cy = y + d[k][1], cz = z + d[k][2];
+                    const uint32_t cell = (uint32_t)(((size_t)cz * Y + cy) * X + cx);
+                    const int j = findActive(act, rowOffsets, cz * (Y - 1) + cy, cell);
+                    if (j < 0) {
+                        ok = false;
+                        continue;
+                    }
+                    r2 = act[j];
+                    vb2 = vbase[j];
+                }
+                cells[k].c[0] = x + d[k][0];
+                cells[k].c[1] = y + d[k][1];
+                cells[k].c[2] = z + d[k][2];
+                cells[k].info = r2.info;
+                cells[k].vbase = vb2;
+                const int e = le[k];
+                const int edgy = ((r2.info >> edgeV0(e)) & 1u) ? 0 : 1;  // s[v0] < iso
+                slotOf[k] = quadSlot(e, edgy);
+                if (kOfSlot[slotOf[k]] != -1) ok = false;
+                kOfSlot[slotOf[k]] = k;
+            }
+            if (!ok || qi >= numQuads) {
+                atomicOr(&ctr->status, kStatusMissingCell);
+                return;
+            }
+            int quad[4];
+            for (int sl = 0; sl < 4; ++sl) {
+                const CellRec& cr = cells[kOfSlot[sl]];
+                quad[sl] = cr.vbase + (int)((cr.info >> (8 + 2 * le[kOfSlot[sl]])) & 3u);
+                if (!inb(quad[sl], numVertices)) {
+                    atomicOr(&ctr->status, kStatusCountMismatch);
+                    return;
+                }
+            }
+            const int h0 = 4 * qi;
+            faceFirst[qi] = h0;
+            const int baseColor = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
+            uint16_t attr = (uint16_t)(3 * baseColor + axis);
+            for (int hi = 0; hi < 4; ++hi) {
+                const CellRec& A = cells[kOfSlot[hi]];
+                const CellRec& B = cells[kOfSlot[(hi + 1) & 3]];
+                // the axis t along which A and B differ, the third axis u
+                int t = -1;
+                for (int k = 0; k < 3; ++k)
+                    if (A.c[k] != B.c[k]) t = k;
+                const int u = 3 - axis - t;
+                const int tA = (int)((A.info >> (8 + 2 * le[kOfSlot[hi]])) & 3u);
+                const int tB = (int)((B.info >> (8 + 2 * le[kOfSlot[(hi + 1) & 3]])) & 3u);
+                int ids[4], org[4];
+                int n = 0;
+                ids[n] = h0 + hi;
+                org[n] = quad[hi];
+                ++n;
+                // the other three grid edges of the A|B face
+                const int uLo = A.c[u];
+                for (int cand = 0; cand < 3; ++cand) {
+                    int o[3] = {p[0], p[1], p[2]};
+                    int al;
+                    if (cand == 0) {  // parallel to the quad's edge, other side of the face
+                        al = axis;
+                        o[u] = (p[u] == uLo) ? uLo + 1 : uLo;
+                    } else {  // across the face, at either end of the quad's edge
+                        al = u;
+                        o[u] = uLo;
+                        o[axis] = p[axis] + (cand == 2 ? 1 : 0);
+                    }
+                    // its local index, sign change and contours in A and in B
+                    const int ca = (o[0] - A.c[0]) | ((o[1] - A.c[1]) << 1) | ((o[2] - A.c[2]) << 2);
+                    const int cb = (o[0] - B.c[0]) | ((o[1] - B.c[1]) << 1) | ((o[2] - B.c[2]) << 2);
+                    const int eA = localEdge(ca, al), eB = localEdge(cb, al);
+                    if (eA < 0 || eB < 0) {
+                        atomicOr(&ctr->status, kStatusBadIndex);
+                        continue;
+                    }
+                    const int csA = (int)(A.info & 255u);
+                    if (!(((csA >> edgeV0(eA)) ^ (csA >> edgeV1(eA))) & 1)) continue;  // no crossing
+                    if ((int)((A.info >> (8 + 2 * eA)) & 3u) != tA) continue;
+                    if ((int)((B.info >> (8 + 2 * eB)) & 3u) != tB) continue;
+                    const int q2 = quadOfEdge(o, al, act, rowOffsets, X, Y, Z);
+                    if (q2 < 0) continue;
+                    const int edgy = ((csA >> edgeV0(eA)) & 1) ? 0 : 1;
+                    const int sA = quadSlot(eA, edgy), sB = quadSlot(eB, edgy);
+                    if (((sA + 1) & 3) == sB) {
+                        ids[n] = 4 * q2 + sA;
+                        org[n] = A.vbase + tA;
+                    } else if (((sB + 1) & 3) == sA) {
+                        ids[n] = 4 * q2 + sB;
+                        org[n] = B.vbase + tB;
+                    } else {
+                        atomicOr(&ctr->status, kStatusBadIndex);
+                        continue;
+                    }
+                    ++n;
+                }
+                // sort the bucket (<= 4 ids) with their origins
+                for (int a = 1; a < n; ++a) {
+                    const int vi = ids[a], vo = org[a];
+                    int b = a - 1;
+                    while (b >= 0 && ids[b] > vi) {
+                        ids[b + 1] = ids[b];
+                        org[b + 1] = org[b];
+                        --b;
+                    }
+                    ids[b + 1] = vi;
+                    org[b + 1] = vo;
+                }
+                int me = 0;
+                for (int a = 0; a < n; ++a)
+                    if (ids[a] == h0 + hi) me = a;
+                int twin = -1;
+                if (n == 2) {
+                    twin = ids[1 - me];
+                } else if (n == 3) {
+                    twin = ids[(me + 1) % 3];
+                } else if (n == 4) {  // "HACKY_OLD_WAY", HalfedgeMesh.cu:250-281
+                    int partner;
+                    if (org[0] != org[1]) partner = me ^ 1;            // (0,1) (2,3)
+                    else if (org[0] != org[2]) partner = me ^ 2;       // (0,2) (1,3)
+                    else partner = 3 - me;                             // (0,3) (1,2)
+                    twin = ids[partner];
+                }
+                he[h0 + hi] = make_int4(quad[hi], qi, h0 + ((hi + 1) & 3), twin);
+                heValence[h0 + hi] = (uint8_t)n;
+                const int origin = quad[hi];
+                if (n == 4) {
+                    attr |= MDMC_FACE_NON_MANIFOLD;
+                    orVertexFlag(vflags, origin, MDMC_VERTEX_NON_MANIFOLD);
+                } else if (n == 3) {
+                    orVertexFlag(vflags, origin, MDMC_VERTEX_WEIRD);
+                } else if (n == 1) {
+                    orVertexFlag(vflags, origin, MDMC_VERTEX_BOUNDARY);
+                }
+                if (me == 0) {  // the bucket's smallest halfedge counts it
+                    ++nE;
+                    if (n == 3) ++nE3;
+                    if (n == 4) {
+                        ++nE4;
+                        const unsigned long long slot = atomicAdd(&ctr->nmBuckets, 1ULL);
+                        if (slot < (unsigned long long)nmCapacity) nmList[slot] = make_int4(ids[0], ids[1], ids[2], ids[3]);
+                        else atomicOr(&ctr->status, kStatusBadIndex);
+                    }
+                }
+            }
+            faceAttr[qi] = attr;
+            ++qi;
+        }
+    }
+    blockAddTo(&ctr->edges, nE);
+    blockAddTo(&ctr->edges3, nE3);
+    blockAddTo(&ctr->edges4, nE4);
+}
+
+void launchQuads(const ActiveCell* act, const int* vbase, int numActive, const int4* rowOffsets, int X, int Y, int Z,
+                 int4* he, int* faceFirst, uint16_t* faceAttr, uint8_t* vflags, uint8_t* heValence, int4* nmList,
+                 int nmCapacity, int numQuads, int numVertices, DevCounters* ctr, cudaStream_t s) {
     if (numActive <= 0) return;
     countLaunch();
-    kQuads<<<(numActive + 255) / 256, 256, 0, s>>>(act, vbase, numActive, rowOffsets, X, Y, table, cap, he, faceFirst,
-                                                   faceAttr, numQuads, numVertices, status);
+    kQuads<<<(numActive + 127) / 128, 128, 0, s>>>(act, vbase, numActive, rowOffsets, X, Y, Z, he, faceFirst, faceAttr,
+                                                   vflags, heValence, nmList, nmCapacity, numQuads, numVertices, ctr);
 }
 
 }  // namespace mdmc

@@ -16,12 +16,46 @@ inline void countLaunch(int n = 1) { g_kernelLaunches.fetch_add(n, std::memory_o
 
 __device__ __forceinline__ void setTwinOut(int4* he, int h, int t) { reinterpret_cast<int*>(he)[4 * (int64_t)h + 3] = t; }
 
+// packed 16-bit face attributes / 8-bit vertex flags, or-ed through 32-bit words
+// (the arrays are padded to a multiple of 4 bytes)
+__device__ __forceinline__ void orFaceAttr(uint16_t* attr, int f, uint32_t bits) {
+    atomicOr(reinterpret_cast<uint32_t*>(attr) + (f >> 1), bits << ((f & 1) * 16));
+}
+__device__ __forceinline__ void orVertexFlag(uint8_t* flags, int v, uint32_t bits) {
+    atomicOr(reinterpret_cast<uint32_t*>(flags) + (v >> 2), bits << ((v & 3) * 8));
+}
+
+template <typename T>
+__device__ __forceinline__ void blockAddTo(unsigned long long* dst, T v) {
+    __shared__ unsigned long long acc;
+    if (threadIdx.x == 0) acc = 0;
+    __syncthreads();
+    unsigned long long w = (unsigned long long)v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&acc, w);
+    __syncthreads();
+    if (threadIdx.x == 0 && acc) atomicAdd(dst, acc);
+}
+
 // the grid a run reads: dense, or refined/padded on demand from a coarse grid
 struct GridDesc {
     bool refined;
     PlainView plain;
     RefinedView ref;
     const GridGeom& geom() const { return refined ? static_cast<const GridGeom&>(ref) : static_cast<const GridGeom&>(plain); }
+};
+
+// the (sorted) ids of one edge bucket with four or more halfedges, as listed
+// in the non-manifold edge list
+struct NMIds {
+    int ids[4];
+    __device__ __forceinline__ explicit NMIds(int4 q) {
+        ids[0] = q.x;
+        ids[1] = q.y;
+        ids[2] = q.z;
+        ids[3] = q.w;
+    }
 };
 
 // splitter working copies (device pointers)
@@ -58,28 +92,28 @@ void launchRowEmit(const GridDesc& g, float iso, const int4* rowOffsets, int num
                    int numActive, uint32_t* status, cudaStream_t s);
 void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, const int* vbase,
                     int numActive, int numVertices, float* pos, float* nrm, uint32_t* status, cudaStream_t s);
-void launchQuads(const ActiveCell* act, const int* vbase, int numActive, const int4* rowOffsets, int X, int Y,
-                 Bucket* table, unsigned long long cap, int4* he, int* faceFirst, uint16_t* faceAttr, int numQuads,
-                 int numVertices, uint32_t* status, cudaStream_t s);
+void launchQuads(const ActiveCell* act, const int* vbase, int numActive, const int4* rowOffsets, int X, int Y, int Z,
+                 int4* he, int* faceFirst, uint16_t* faceAttr, uint8_t* vflags, uint8_t* heValence, int4* nmList,
+                 int nmCapacity, int numQuads, int numVertices, DevCounters* ctr, cudaStream_t s);
 
 void launchBuckets(Bucket* table, unsigned long long cap, int4* he, uint16_t* faceAttr, uint8_t* vflags,
-                   int connectTwins, int* nmList, DevCounters* ctr, MeshDims md, cudaStream_t s);
+                   int connectTwins, uint8_t* heValence, int4* nmList, DevCounters* ctr, MeshDims md, cudaStream_t s);
 void launchInsertFaces(const int4* he, const int* faceFirst, MeshDims md, Bucket* table, unsigned long long cap,
                        uint32_t* status, cudaStream_t s);
 void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s);
-void launchReconnect(const GridDesc& g, float iso, const Bucket* table, const int* nmList, const DevCounters* ctr,
+void launchReconnect(const GridDesc& g, float iso, const int4* nmList, const DevCounters* ctr,
                      int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s);
 void launchDetectFans(const int4* he, MeshDims md, uint8_t* isKey, int* fans, uint8_t* vflags, DevCounters* ctr,
                       uint32_t* status, cudaStream_t s);
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const Bucket* table, unsigned long long cap,
-                  int4* quads, int* vertexHE, DevCounters* ctr, uint32_t* status, cudaStream_t s);
+                  const uint8_t* heValence, int4* quads, int* vertexHE, DevCounters* ctr, uint32_t* status, cudaStream_t s);
 
 void launchFlagNMFaces(const uint16_t* attr, int numFaces, int* flags, cudaStream_t s);
 void launchCompactNMFaces(const int* flags, const int* offsets, int numFaces, int* nmFaces, cudaStream_t s);
 void launchFillInt(int* p, int64_t n, int v, cudaStream_t s);
 void launchSplitCopy(const int* nmFaces, int n, const int4* he, const int* faceFirst, const uint16_t* faceAttr,
                      const float* pos, const float* nrm, const SplitWork& w, uint32_t* status, cudaStream_t s);
-void launchSplitMarkNM(const Bucket* table, const int* nmList, const DevCounters* ctr, const SplitWork& w,
+void launchSplitMarkNM(const int4* nmList, const DevCounters* ctr, const SplitWork& w,
                        uint32_t* status, cudaStream_t s);
 void launchSplitSubdivide(int n, const SplitWork& w, uint32_t* status, cudaStream_t s);
 void launchSplitCollapse(const SplitWork& w, uint32_t* status, cudaStream_t s);

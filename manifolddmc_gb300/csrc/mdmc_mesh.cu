@@ -19,32 +19,14 @@
 namespace mdmc {
 
 __device__ __forceinline__ void setTwin(int4* he, int h, int t) { reinterpret_cast<int*>(he)[4 * (int64_t)h + 3] = t; }
-__device__ __forceinline__ void orFaceAttr(uint16_t* attr, int f, uint32_t bits) {
-    atomicOr(reinterpret_cast<uint32_t*>(attr) + (f >> 1), bits << ((f & 1) * 16));
-}
-__device__ __forceinline__ void orVertexFlag(uint8_t* flags, int v, uint32_t bits) {
-    atomicOr(reinterpret_cast<uint32_t*>(flags) + (v >> 2), bits << ((v & 3) * 8));
-}
-
-template <typename T>
-__device__ __forceinline__ void blockAddTo(unsigned long long* dst, T v) {
-    __shared__ unsigned long long acc;
-    if (threadIdx.x == 0) acc = 0;
-    __syncthreads();
-    unsigned long long w = (unsigned long long)v;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
-    if ((threadIdx.x & 31) == 0 && w) atomicAdd(&acc, w);
-    __syncthreads();
-    if (threadIdx.x == 0 && acc) atomicAdd(dst, acc);
-}
 
 // Sorts each bucket's ids, then (connectTwins) pairs twins as
 // connectHalfedgeTwins does, and sets the face and vertex flags of
 // refreshFaceFlagsGPU / refresh{NonManifold,Weird,Boundary}Flags.  Buckets
 // with at least four ids go to nmList (isHashTableEntryNonManifold).
 __global__ void kBuckets(Bucket* __restrict__ table, unsigned long long cap, int4* __restrict__ he, uint16_t* faceAttr,
-                         uint8_t* vflags, int connectTwins, int* __restrict__ nmList, DevCounters* ctr, MeshDims md) {
+                         uint8_t* vflags, int connectTwins, uint8_t* __restrict__ heValence, int4* __restrict__ nmList,
+                         DevCounters* ctr, MeshDims md) {
     int nE = 0, nE3 = 0, nE4 = 0;
     for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap;
          i += (unsigned long long)gridDim.x * blockDim.x) {
@@ -75,12 +57,13 @@ __global__ void kBuckets(Bucket* __restrict__ table, unsigned long long cap, int
             atomicOr(&ctr->status, kStatusBadIndex);
             continue;
         }
+        for (int k = 0; k < n; ++k) heValence[e[k]] = (uint8_t)(count < 255 ? count : 255);
         ++nE;
         if (count == 3) ++nE3;
         if (count == 4) ++nE4;
         if (count >= 4) {
             const unsigned long long slot = atomicAdd(&ctr->nmBuckets, 1ULL);
-            if (slot < (unsigned long long)(md.H / 4 + 1)) nmList[slot] = (int)i;
+            if (slot < (unsigned long long)(md.H / 4 + 1)) nmList[slot] = make_int4(e[0], e[1], e[2], e[3]);
             else atomicOr(&ctr->status, kStatusBadIndex);
         }
         if (connectTwins) {
@@ -119,12 +102,12 @@ __global__ void kBuckets(Bucket* __restrict__ table, unsigned long long cap, int
 }
 
 void launchBuckets(Bucket* table, unsigned long long cap, int4* he, uint16_t* faceAttr, uint8_t* vflags,
-                   int connectTwins, int* nmList, DevCounters* ctr, MeshDims md, cudaStream_t s) {
+                   int connectTwins, uint8_t* heValence, int4* nmList, DevCounters* ctr, MeshDims md, cudaStream_t s) {
     unsigned long long blocks = (cap + 255) / 256;
     if (blocks > 152ULL * 16) blocks = 152ULL * 16;
     if (blocks == 0) blocks = 1;
     countLaunch();
-    kBuckets<<<(unsigned)blocks, 256, 0, s>>>(table, cap, he, faceAttr, vflags, connectTwins, nmList, ctr, md);
+    kBuckets<<<(unsigned)blocks, 256, 0, s>>>(table, cap, he, faceAttr, vflags, connectTwins, heValence, nmList, ctr, md);
 }
 
 // refreshHashTableGPU, D/Halfedges/HalfedgeMesh.cu:62-90
@@ -180,12 +163,12 @@ __device__ __forceinline__ F3 nudge(int it) {
 __device__ __forceinline__ F3 loadP(const float* pos, int v) { return f3(pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]); }
 
 template <class View>
-__global__ void kReconnect(View g, float iso, const Bucket* __restrict__ table, const int* __restrict__ nmList,
+__global__ void kReconnect(View g, float iso, const int4* __restrict__ nmList,
                            const DevCounters* ctr, int4* he, const float* __restrict__ pos, MeshDims md,
                            uint32_t* status) {
     const int count = min((int)ctr->nmBuckets, md.H / 4 + 1);
     for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < count; w += gridDim.x * blockDim.x) {
-        const Bucket b = table[nmList[w]];
+        const NMIds b(nmList[w]);
         // every id, its next, next.next and their origins must be in range
         bool ok = true;
         for (int k = 0; k < 4 && ok; ++k) {
@@ -296,11 +279,11 @@ __global__ void kReconnect(View g, float iso, const Bucket* __restrict__ table, 
     }
 }
 
-void launchReconnect(const GridDesc& g, float iso, const Bucket* table, const int* nmList, const DevCounters* ctr,
+void launchReconnect(const GridDesc& g, float iso, const int4* nmList, const DevCounters* ctr,
                      int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s) {
     countLaunch();
-    if (g.refined) kReconnect<RefinedView><<<152 * 2, 128, 0, s>>>(g.ref, iso, table, nmList, ctr, he, pos, md, status);
-    else kReconnect<PlainView><<<152 * 2, 128, 0, s>>>(g.plain, iso, table, nmList, ctr, he, pos, md, status);
+    if (g.refined) kReconnect<RefinedView><<<152 * 2, 128, 0, s>>>(g.ref, iso, nmList, ctr, he, pos, md, status);
+    else kReconnect<PlainView><<<152 * 2, 128, 0, s>>>(g.plain, iso, nmList, ctr, he, pos, md, status);
 }
 
 // ---------------------------------------------------------------------------
@@ -400,19 +383,20 @@ void launchDetectFans(const int4* he, MeshDims md, uint8_t* isKey, int* fans, ui
 // smallest outgoing halfedge of every vertex
 // ---------------------------------------------------------------------------
 __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__ faceFirst, MeshDims md,
-                            const Bucket* __restrict__ table, unsigned long long cap, int4* __restrict__ quads,
-                            DevCounters* ctr) {
+                            const Bucket* __restrict__ table, unsigned long long cap,
+                            const uint8_t* __restrict__ heValence, int4* __restrict__ quads, DevCounters* ctr) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     int cnt = -1;
     if (f < md.F) {
         int h = faceFirst[f];
-        int q[4] = {-1, -1, -1, -1};
+        int q[4] = {-1, -1, -1, -1}, hs[4] = {-1, -1, -1, -1};
         bool ok = true;
         for (int i = 0; i < 4 && ok; ++i) {
             ok = inb(h, md.H);
             if (ok) {
                 const int4 e = he[h];
                 q[i] = e.x;
+                hs[i] = h;
                 h = e.z;
             }
         }
@@ -420,7 +404,7 @@ __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__
         if (ok) {
             cnt = 0;
             for (int i = 0; i < 4; ++i)
-                if (edgeValence(table, cap, q[i], q[(i + 1) & 3]) > 2) ++cnt;
+                if ((table ? edgeValence(table, cap, q[i], q[(i + 1) & 3]) : (int)heValence[hs[i]]) > 2) ++cnt;
         } else {
             atomicOr(&ctr->status, kStatusBadIndex);
         }
@@ -442,11 +426,11 @@ __global__ void kVertexHalfedgeFix(int* vertexHE, int numVertices) {
 }
 
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const Bucket* table, unsigned long long cap,
-                  int4* quads, int* vertexHE, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
+                  const uint8_t* heValence, int4* quads, int* vertexHE, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
     (void)status;
     if (md.F > 0) {
         countLaunch();
-        kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, table, cap, quads, ctr);
+        kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, table, cap, heValence, quads, ctr);
     }
     if (md.V > 0) {
         // 0x7F7F7F7F marks "none"; atomicMin lowers it

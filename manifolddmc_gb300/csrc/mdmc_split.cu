@@ -113,11 +113,11 @@ __global__ void kUpdateRefs(int n, SplitWork w, uint32_t* status) {
 }
 
 // markHalfedgesAsNonManifold (:527-555)
-__global__ void kMarkNM(const Bucket* __restrict__ table, const int* __restrict__ nmList, const DevCounters* ctr,
+__global__ void kMarkNM(const int4* __restrict__ nmList, const DevCounters* ctr,
                         SplitWork w, uint32_t* status) {
     const int count = min((int)ctr->nmBuckets, w.H / 4 + 1);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
-        const Bucket b = table[nmList[i]];
+        const NMIds b(nmList[i]);
         for (int k = 0; k < 4; ++k) {
             const int id = b.ids[k];
             const int c = inb(id, w.H) ? w.hO2C[id] : kNone;
@@ -513,10 +513,10 @@ void launchSplitCopy(const int* nmFaces, int n, const int4* he, const int* faceF
     kCopyOut<<<nb(n, 256), 256, 0, s>>>(nmFaces, n, he, faceFirst, faceAttr, pos, nrm, w, status);
     kUpdateRefs<<<nb(4 * (int64_t)n, 256), 256, 0, s>>>(n, w, status);
 }
-void launchSplitMarkNM(const Bucket* table, const int* nmList, const DevCounters* ctr, const SplitWork& w,
+void launchSplitMarkNM(const int4* nmList, const DevCounters* ctr, const SplitWork& w,
                        uint32_t* status, cudaStream_t s) {
     countLaunch();
-    kMarkNM<<<152, 256, 0, s>>>(table, nmList, ctr, w, status);
+    kMarkNM<<<152, 256, 0, s>>>(nmList, ctr, w, status);
 }
 void launchSplitSubdivide(int n, const SplitWork& w, uint32_t* status, cudaStream_t s) {
     countLaunch();
