@@ -131,12 +131,12 @@ def algorithmic_bytes(kernel, s):
         return 4 * S_in + S_in // 8
     if kernel == "count":  # grid read once, per-row counts written
         return 4 * S + 16 * rows
-    if kernel == "emit":  # grid read once, row offsets read, records + contour counts written
-        return 4 * S + 16 * rows + 16 * A + 4 * A
+    if kernel == "emit":  # grid read once, row offsets read, records + contour counts + quad owners written
+        return 4 * S + 16 * rows + 16 * A + 4 * A + 4 * Q
     if kernel == "vertices":  # records and offsets read, positions + normals written
         return 16 * A + 4 * A + 24 * V
-    if kernel == "quads":  # records + vertex offsets read; halfedges (with twins), faces, attributes, valences written
-        return 16 * A + 4 * A + 64 * Q + 4 * Q + 2 * Q + 4 * Q
+    if kernel == "quads":  # records + vertex offsets + quad owners read; halfedges (with twins), faces, attributes, valences written
+        return 16 * A + 4 * A + 4 * Q + 64 * Q + 4 * Q + 2 * Q + 4 * Q
     raise KeyError(kernel)
 
 

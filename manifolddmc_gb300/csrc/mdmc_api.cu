@@ -83,6 +83,8 @@ struct mdmc_context {
     int64_t V = 0, F = 0, H = 0;
     // edge table
     DevBuf table, nmList, heValence;
+    // quad -> owner cell, and the per-row cell index (mask + first active id per 32 cells)
+    DevBuf quadOwner, cellMask, cellFirst;
     bool tableValid = false;  // the edge table holds the current mesh (after a splitter refresh)
     unsigned long long cap = 0;
     // counters
@@ -615,10 +617,11 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     // compaction of the active cells and their contour counts
     MDMC_CHECK(c, c->act.ensure(sizeof(ActiveCell) * (size_t)std::max<int64_t>(A, 1)));
     MDMC_CHECK(c, c->vbase.ensure(sizeof(int) * (size_t)(A + 1)));
+    MDMC_CHECK(c, c->quadOwner.ensure(sizeof(int) * (size_t)std::max<int64_t>(Q, 1)));
     cudaEventRecord(c->kev[4], s);
     if (numRows > 0)
-        launchRowEmit(g, iso, c->rows.as<int4>(), (int)numRows, c->act.as<ActiveCell>(), c->vbase.as<int>(), (int)A,
-                      status, s);
+        launchRowEmit(g, iso, c->rows.as<int4>(), (int)numRows, c->act.as<ActiveCell>(), c->vbase.as<int>(),
+                      c->quadOwner.as<int>(), (int)A, (int)Q, status, s);
     cudaEventRecord(c->kev[5], s);
     if ((st = scan<int>(c, c->vbase.as<int>(), c->vbase.as<int>(), A, s)) != MDMC_OK) return st;
     MDMC_CHECK(c, cudaGetLastError());
@@ -657,9 +660,19 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     // mapQuadrilaterals + collectHalfedgeElements, and the halfedge mesh's
     // twins and flags (HalfedgeMesh::initialize) in the same pass
     cudaEventRecord(c->kev[6], s);
-    launchQuads(c->act.as<ActiveCell>(), c->vbase.as<int>(), (int)A, c->rows.as<int4>(), X, Y, Z, c->he.as<int4>(),
-                c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(),
-                c->nmList.as<int4>(), (int)(Q + 1), (int)Q, (int)Vd, ctr, s);
+    {
+        const int W = (X - 1 + 31) / 32;
+        const size_t words = (size_t)numRows * (size_t)W;
+        MDMC_CHECK(c, c->cellMask.ensure(sizeof(uint32_t) * std::max<size_t>(words, 1)));
+        MDMC_CHECK(c, c->cellFirst.ensure(sizeof(int) * std::max<size_t>(words, 1)));
+        MDMC_CHECK(c, cudaMemsetAsync(c->cellMask.p, 0, sizeof(uint32_t) * words, s));
+        launchIndexCells(c->act.as<ActiveCell>(), c->vbase.as<int>(), (int)A, X, Y, W, c->cellMask.as<uint32_t>(),
+                         c->cellFirst.as<int>(), s);
+        launchQuads(c->act.as<ActiveCell>(), c->quadOwner.as<int>(), (int)A, c->cellMask.as<uint32_t>(),
+                    c->cellFirst.as<int>(), X, Y, Z, W, c->he.as<int4>(), c->faceFirst.as<int>(),
+                    c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(),
+                    c->nmList.as<int4>(), (int)(Q + 1), (int)Q, (int)Vd, ctr, s);
+    }
     cudaEventRecord(c->kev[7], s);
     MDMC_CHECK(c, cudaGetLastError());
     cudaEventRecord(c->ev[1], s);

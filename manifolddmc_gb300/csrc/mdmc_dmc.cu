@@ -394,7 +394,8 @@ void launchRowCount(const GridDesc& g, float iso, int4* rowCounts, int numRows, 
 template <class View>
 __global__ void __launch_bounds__(256) kRowEmit(View g, float iso, const int4* __restrict__ rowOffsets, int numRows,
                                                 ActiveCell* __restrict__ act, int* __restrict__ numVerts,
-                                                int numActive, uint32_t* status) {
+                                                int* __restrict__ quadOwner, int numActive, int numQuads,
+                                                uint32_t* status) {
     __shared__ uint64_t table[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kContourTable[i];
     __syncthreads();
@@ -440,6 +441,10 @@ __global__ void __launch_bounds__(256) kRowEmit(View g, float iso, const int4* _
                 rec.pad = 0;
                 act[aIdx] = rec;
                 numVerts[aIdx] = n;
+                for (int r = 0; r < nq; ++r) {
+                    if (inb(rec.qbase + r, numQuads)) quadOwner[rec.qbase + r] = aIdx;
+                    else atomicOr(status, kStatusCountMismatch);
+                }
             } else {
                 atomicOr(status, kStatusCountMismatch);
             }
@@ -450,14 +455,14 @@ __global__ void __launch_bounds__(256) kRowEmit(View g, float iso, const int4* _
 }
 
 void launchRowEmit(const GridDesc& g, float iso, const int4* rowOffsets, int numRows, ActiveCell* act, int* numVerts,
-                   int numActive, uint32_t* status, cudaStream_t s) {
+                   int* quadOwner, int numActive, int numQuads, uint32_t* status, cudaStream_t s) {
     countLaunch();
     if (g.refined)
-        kRowEmit<RefinedView><<<(numRows + 7) / 8, 256, 0, s>>>(g.ref, iso, rowOffsets, numRows, act, numVerts, numActive,
-                                                                status);
+        kRowEmit<RefinedView><<<(numRows + 7) / 8, 256, 0, s>>>(g.ref, iso, rowOffsets, numRows, act, numVerts, quadOwner,
+                                                                numActive, numQuads, status);
     else
-        kRowEmit<PlainView><<<(numRows + 7) / 8, 256, 0, s>>>(g.plain, iso, rowOffsets, numRows, act, numVerts, numActive,
-                                                              status);
+        kRowEmit<PlainView><<<(numRows + 7) / 8, 256, 0, s>>>(g.plain, iso, rowOffsets, numRows, act, numVerts, quadOwner,
+                                                              numActive, numQuads, status);
 }
 
 // ---------------------------------------------------------------------------
@@ -537,46 +542,53 @@ void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const Ac
 }
 
 // ---------------------------------------------------------------------------
-// quads, halfedges and edge-table inserts
+// cell index: for every x-row of cells and every 32 cells of it, the mask of
+// the active ones and the index (in the active-cell list) of the first, so a
+// cell's record is one load away.  Also stores each cell's first vertex id in
+// its record.  Built once per run, one thread per active cell.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ int findActive(const ActiveCell* __restrict__ act, const int4* __restrict__ rowOffsets,
-                                          int row, uint32_t cell) {
-    int lo = rowOffsets[row].x, hi = rowOffsets[row + 1].x;
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        uint32_t c = act[mid].cell;
-        if (c < cell) lo = mid + 1;
-        else hi = mid;
+__global__ void kIndexCells(ActiveCell* __restrict__ act, const int* __restrict__ vbase, int numActive, int X, int Y,
+                            int W, uint32_t* __restrict__ mask, int* __restrict__ first) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= numActive) return;
+    const uint32_t cell = act[i].cell;
+    const uint32_t line = cell / (uint32_t)X;  // z * Y + y
+    const int x = (int)(cell - line * (uint32_t)X);
+    const int y = (int)(line % (uint32_t)Y), z = (int)(line / (uint32_t)Y);
+    const int64_t w = ((int64_t)z * (Y - 1) + y) * W + (x >> 5);
+    atomicOr(&mask[w], 1u << (x & 31));
+    bool lead = i == 0;
+    if (!lead) {
+        const uint32_t pc = act[i - 1].cell;
+        const uint32_t pl = pc / (uint32_t)X;
+        lead = pl != line || ((int)(pc - pl * (uint32_t)X) >> 5) != (x >> 5);
     }
-    if (lo < rowOffsets[row + 1].x && act[lo].cell == cell) return lo;
-    return -1;
+    if (lead) first[w] = i;
+    act[i].pad = vbase[i];
 }
 
-// The four cells around the grid edge leaving cell (x,y,z)'s corner 0 along
-// `axis`, each with the local index of that edge inside the cell.  The slot
-// each contributes follows from the edge index and its orientation
-// (computeVertexPosition, D/CellIntersection.inl:361-366).
-__device__ __forceinline__ void cellsAroundEdge(int axis, int d[4][3], int e[4]) {
-    // axis 0: cells p, p-y, p-z, p-y-z with local edges 0, 2, 4, 6
-    // axis 1: cells p, p-x, p-z, p-x-z with local edges 3, 1, 7, 5
-    // axis 2: cells p, p-x, p-y, p-x-y with local edges 8, 9, 11, 10
-    const int b = axis == 0 ? 1 : 0;  // first other axis
-    const int c = axis == 2 ? 1 : 2;  // second other axis
-    const int le[3][4] = {{0, 2, 4, 6}, {3, 1, 7, 5}, {8, 9, 11, 10}};
-    for (int k = 0; k < 4; ++k) {
-        d[k][0] = d[k][1] = d[k][2] = 0;
-        if (k & 1) d[k][b] = -1;
-        if (k & 2) d[k][c] = -1;
-        e[k] = le[axis][k];
-    }
+void launchIndexCells(ActiveCell* act, const int* vbase, int numActive, int X, int Y, int W, uint32_t* mask, int* first,
+                      cudaStream_t s) {
+    if (numActive <= 0) return;
+    countLaunch();
+    kIndexCells<<<(numActive + 255) / 256, 256, 0, s>>>(act, vbase, numActive, X, Y, W, mask, first);
 }
 
-// local index of the cell edge leaving corner `corner` along `axis` (-1: none)
-__device__ __forceinline__ int localEdge(int corner, int axis) {
-    if (axis == 0) return (corner & 1) ? -1 : corner;                          // 0, 2, 4, 6
-    if (axis == 1) return (corner & 2) ? -1 : ((0x5713 >> (4 * ((corner & 1) | ((corner >> 1) & 2)))) & 0xF);  // 3,1,7,5
-    return (corner & 4) ? -1 : ((0xAB98 >> (4 * corner)) & 0xF);              // 8, 9, 11, 10
-}
+struct CellIndex {
+    const uint32_t* mask;
+    const int* first;
+    int X, Y, Z, W;
+    // index of cell (x,y,z) in the active-cell list, -1 if inactive or outside
+    __device__ __forceinline__ int find(int x, int y, int z) const {
+        if ((unsigned)x > (unsigned)(X - 2) || (unsigned)y > (unsigned)(Y - 2) || (unsigned)z > (unsigned)(Z - 2))
+            return -1;
+        const int64_t w = ((int64_t)z * (Y - 1) + y) * W + (x >> 5);
+        const uint32_t m = __ldg(mask + w);
+        const int f = __ldg(first + w);
+        const uint32_t bit = 1u << (x & 31);
+        return (m & bit) ? f + __popc(m & (bit - 1u)) : -1;
+    }
+};
 
 // does the cell at (x,y,z) with case cs own the quad of its corner-0 edge along axis
 __device__ __forceinline__ bool ownsAxis(int cs, int axis, int x, int y, int z) {
@@ -586,213 +598,258 @@ __device__ __forceinline__ bool ownsAxis(int cs, int axis, int x, int y, int z) 
     return x >= 1 && y >= 1;
 }
 
-struct CellRec {
-    int c[3];       // coordinates
-    uint32_t info;  // case | edge -> contour map << 8
-    int vbase;
-};
-
-// Quad id of the grid edge (origin o, axis al), or -1 if that edge has no quad
-// (a cell around it is outside the grid, or no sign change / owner record).
-__device__ int quadOfEdge(const int o[3], int al, const ActiveCell* __restrict__ act, const int4* __restrict__ rowOffsets,
-                          int X, int Y, int Z) {
-    const int dims[3] = {X, Y, Z};
-    for (int k = 0; k < 3; ++k) {
-        if (o[k] < 0 || o[k] > dims[k] - 2) return -1;  // the owner cell must exist
-        if (k != al && o[k] < 1) return -1;             // and the cells behind it
-    }
-    const uint32_t cell = (uint32_t)(((size_t)o[2] * Y + o[1]) * X + o[0]);
-    const int j = findActive(act, rowOffsets, o[2] * (Y - 1) + o[1], cell);
-    if (j < 0) return -1;
-    const ActiveCell r = act[j];
-    const int cs = (int)(r.info & 255u);
-    if (!ownsAxis(cs, al, o[0], o[1], o[2])) return -1;
-    int rank = 0;
-    for (int a = 0; a < al; ++a) rank += ownsAxis(cs, a, o[0], o[1], o[2]) ? 1 : 0;
-    return r.qbase + rank;
+// local index of the cell edge leaving corner `corner` (bit 0 x, 1 y, 2 z)
+// along `axis`; the corner's bit for that axis is 0
+__device__ __forceinline__ int localEdge(int corner, int axis) {
+    if (axis == 0) return corner;                                                        // 0, 2, 4, 6
+    if (axis == 1) return (0x5713 >> (4 * ((corner & 1) | ((corner >> 1) & 2)))) & 0xF;  // 3, 1, 7, 5
+    return (0xAB98 >> (4 * corner)) & 0xF;                                               // 8, 9, 11, 10
 }
+
+__device__ __forceinline__ int axisBit(int a) { return 1 << a; }
+
+// one cell around a quad's grid edge, in registers
+struct AroundCell {
+    uint32_t info;  // case | edge -> contour map << 8
+    int vbase;      // first vertex id
+    int le;         // local index of the quad's edge in this cell
+    int contour;    // contour of that edge in this cell
+};
 
 // The quads (mapQuadrilaterals, D/DualMarchingCubes.cu:72-85), their halfedges
 // (collectHalfedgeElements, D/Halfedges/HalfedgeMesh.cu:14-60) and the twins
 // and flags of connectHalfedgeTwins / refresh*Flags (:92-291), without an edge
-// table.  Halfedge i of quad q runs between the vertices of the face-adjacent
-// cells A (slot i) and B (slot i+1); the only quads that can hold the same
-// vertex pair are those of the four grid edges of the A|B face, and each of
-// them does exactly when its edge lies in the same contours of A and of B.
-// That set is the reference's edge-table bucket; sorted, it gives the twins
-// by the reference's rules.
-__global__ void kQuads(const ActiveCell* __restrict__ act, const int* __restrict__ vbase, int numActive,
-                       const int4* __restrict__ rowOffsets, int X, int Y, int Z, int4* __restrict__ he,
-                       int* __restrict__ faceFirst, uint16_t* __restrict__ faceAttr, uint8_t* vflags,
-                       uint8_t* __restrict__ heValence, int4* __restrict__ nmList, int nmCapacity, int numQuads,
-                       int numVertices, DevCounters* ctr) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// table, one thread per quad.  Halfedge i of quad q runs between the vertices
+// of the face-adjacent cells A (slot i) and B (slot i+1); the only quads that
+// can hold the same vertex pair are those of the four grid edges of the A|B
+// face, and each of them does exactly when its edge lies in the same contours
+// of A and of B.  That set is the reference's edge-table bucket; sorted, it
+// gives the twins by the reference's rules.
+__global__ void __launch_bounds__(256) kQuads(const ActiveCell* __restrict__ act, const int* __restrict__ quadOwner,
+                                              int numActive, CellIndex ix, int4* __restrict__ he,
+                                              int* __restrict__ faceFirst, uint16_t* __restrict__ faceAttr,
+                                              uint8_t* vflags, uint32_t* __restrict__ heValence4,
+                                              int4* __restrict__ nmList, int nmCapacity, int numQuads, int numVertices,
+                                              DevCounters* ctr) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
     int nE = 0, nE3 = 0, nE4 = 0;
-    if (i < numActive) {
-        const ActiveCell rec = act[i];
+    bool ok = q < numQuads;
+    const int j = ok ? quadOwner[q] : 0;
+    if (ok && !inb(j, numActive)) {
+        atomicOr(&ctr->status, kStatusBadIndex);
+        ok = false;
+    }
+    if (ok) {
+        const ActiveCell rec = act[j];
         const int cs = (int)(rec.info & 255u);
-        const int x = (int)(rec.cell % (uint32_t)X);
-        const int y = (int)((rec.cell / (uint32_t)X) % (uint32_t)Y);
-        const int z = (int)(rec.cell / ((uint32_t)X * (uint32_t)Y));
-        const int p[3] = {x, y, z};
-        int qi = rec.qbase;
-        for (int axis = 0; axis < 3; ++axis) {
-            if (!ownsAxis(cs, axis, x, y, z)) continue;
-            int d[4][3], le[4];
-            cellsAroundEdge(axis, d, le);
-            CellRec cells[4];
-            int slotOf[4];
-            int kOfSlot[4] = {-1, -1, -1, -1};
-            bool ok = true;
+        const uint32_t line = rec.cell / (uint32_t)ix.X;
+        const int px = (int)(rec.cell - line * (uint32_t)ix.X), py = (int)(line % (uint32_t)ix.Y),
+                  pz = (int)(line / (uint32_t)ix.Y);
+        // the rank-th owned axis of the owner
+        int axis = -1, rank = q - rec.qbase;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            if (axis < 0 && ownsAxis(cs, a, px, py, pz) && rank-- == 0) axis = a;
+        if (axis < 0) {
+            atomicOr(&ctr->status, kStatusBadIndex);
+            ok = false;
+        }
+        if (ok) {
+            // the other axes b < c; cell k = p - (k&1) e_b - (k>>1) e_c
+            const int b = axis == 0 ? 1 : 0, c = axis == 2 ? 1 : 2;
+            const uint32_t leWord = axis == 0 ? 0x6420u : (axis == 1 ? 0x5713u : 0xAB98u);
+            AroundCell cell[4];
+            cell[0].info = rec.info;
+            cell[0].vbase = rec.pad;
+            int jk[4];
+            jk[0] = j;
+#pragma unroll
+            for (int k = 1; k < 4; ++k) {
+                const int db = k & 1, dc = k >> 1;
+                jk[k] = ix.find(px - (b == 0 ? db : 0) - (c == 0 ? dc : 0), py - (b == 1 ? db : 0) - (c == 1 ? dc : 0),
+                                pz - (c == 2 ? dc : 0));
+            }
+#pragma unroll
+            for (int k = 1; k < 4; ++k) {
+                if (jk[k] < 0 || jk[k] >= numActive) {
+                    ok = false;
+                    cell[k].info = 0;
+                    cell[k].vbase = 0;
+                } else {
+                    const ActiveCell r2 = act[jk[k]];
+                    cell[k].info = r2.info;
+                    cell[k].vbase = r2.pad;
+                }
+            }
+#pragma unroll
             for (int k = 0; k < 4; ++k) {
-                ActiveCell r2 = rec;
-                int vb2 = vbase[i];
-                if (k > 0) {
-                    const int cx = x + d[k][0], cy = y + d[k][1], cz = z + d[k][2];
-                    const uint32_t cell = (uint32_t)(((size_t)cz * Y + cy) * X + cx);
-                    const int j = findActive(act, rowOffsets, cz * (Y - 1) + cy, cell);
-                    if (j < 0) {
-                        ok = false;
-                        continue;
-                    }
-                    r2 = act[j];
-                    vb2 = vbase[j];
-                }
-                cells[k].c[0] = x + d[k][0];
-                cells[k].c[1] = y + d[k][1];
-                cells[k].c[2] = z + d[k][2];
-                cells[k].info = r2.info;
-                cells[k].vbase = vb2;
-                const int e = le[k];
-                const int edgy = ((r2.info >> edgeV0(e)) & 1u) ? 0 : 1;  // s[v0] < iso
-                slotOf[k] = quadSlot(e, edgy);
-                if (kOfSlot[slotOf[k]] != -1) ok = false;
-                kOfSlot[slotOf[k]] = k;
+                cell[k].le = (int)((leWord >> (4 * k)) & 0xF);
+                cell[k].contour = (int)((cell[k].info >> (8 + 2 * cell[k].le)) & 3u);
             }
-            if (!ok || qi >= numQuads) {
-                atomicOr(&ctr->status, kStatusMissingCell);
-                return;
+            if (!ok) atomicOr(&ctr->status, kStatusMissingCell);
+            // slot -> cell: edges with v0 inside take the reverse cycle
+            // (quadSlot, computeVertexPosition, D/CellIntersection.inl:361-366)
+            const int edgy = (cs & 1) ? 0 : 1;
+            int quadK[4] = {0, 0, 0, 0};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int sl = quadSlot(cell[k].le, edgy);
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (sl == t) quadK[t] = k;
             }
-            int quad[4];
+            int quadV[4];
+#pragma unroll
             for (int sl = 0; sl < 4; ++sl) {
-                const CellRec& cr = cells[kOfSlot[sl]];
-                quad[sl] = cr.vbase + (int)((cr.info >> (8 + 2 * le[kOfSlot[sl]])) & 3u);
-                if (!inb(quad[sl], numVertices)) {
-                    atomicOr(&ctr->status, kStatusCountMismatch);
-                    return;
-                }
+                const int k = quadK[sl];
+                int v = 0;
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    if (k == t) v = cell[t].vbase + cell[t].contour;
+                quadV[sl] = v;
+                if (!inb(v, numVertices)) ok = false;
             }
-            const int h0 = 4 * qi;
-            faceFirst[qi] = h0;
-            const int baseColor = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
-            uint16_t attr = (uint16_t)(3 * baseColor + axis);
-            for (int hi = 0; hi < 4; ++hi) {
-                const CellRec& A = cells[kOfSlot[hi]];
-                const CellRec& B = cells[kOfSlot[(hi + 1) & 3]];
-                // the axis t along which A and B differ, the third axis u
-                int t = -1;
-                for (int k = 0; k < 3; ++k)
-                    if (A.c[k] != B.c[k]) t = k;
-                const int u = 3 - axis - t;
-                const int tA = (int)((A.info >> (8 + 2 * le[kOfSlot[hi]])) & 3u);
-                const int tB = (int)((B.info >> (8 + 2 * le[kOfSlot[(hi + 1) & 3]])) & 3u);
-                int ids[4], org[4];
-                int n = 0;
-                ids[n] = h0 + hi;
-                org[n] = quad[hi];
-                ++n;
-                // the other three grid edges of the A|B face
-                const int uLo = A.c[u];
-                for (int cand = 0; cand < 3; ++cand) {
-                    int o[3] = {p[0], p[1], p[2]};
-                    int al;
-                    if (cand == 0) {  // parallel to the quad's edge, other side of the face
-                        al = axis;
-                        o[u] = (p[u] == uLo) ? uLo + 1 : uLo;
-                    } else {  // across the face, at either end of the quad's edge
-                        al = u;
-                        o[u] = uLo;
-                        o[axis] = p[axis] + (cand == 2 ? 1 : 0);
+            if (!ok) {
+                atomicOr(&ctr->status, kStatusCountMismatch);
+            } else {
+                const int h0 = 4 * q;
+                const int baseColor = (px & 1) | ((py & 1) << 1) | ((pz & 1) << 2);
+                uint32_t attr = (uint32_t)(3 * baseColor + axis);
+                uint32_t valences = 0;
+                int4 out[4];
+#pragma unroll
+                for (int hi = 0; hi < 4; ++hi) {
+                    const int kA = quadK[hi], kB = quadK[(hi + 1) & 3];
+                    uint32_t infoA = 0, infoB = 0;
+                    int vbA = 0, vbB = 0;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        if (kA == t) {
+                            infoA = cell[t].info;
+                            vbA = cell[t].vbase;
+                        }
+                        if (kB == t) {
+                            infoB = cell[t].info;
+                            vbB = cell[t].vbase;
+                        }
                     }
-                    // its local index, sign change and contours in A and in B
-                    const int ca = (o[0] - A.c[0]) | ((o[1] - A.c[1]) << 1) | ((o[2] - A.c[2]) << 2);
-                    const int cb = (o[0] - B.c[0]) | ((o[1] - B.c[1]) << 1) | ((o[2] - B.c[2]) << 2);
-                    const int eA = localEdge(ca, al), eB = localEdge(cb, al);
-                    if (eA < 0 || eB < 0) {
-                        atomicOr(&ctr->status, kStatusBadIndex);
-                        continue;
+                    const int tA = (int)((infoA >> (8 + 2 * ((leWord >> (4 * kA)) & 0xF))) & 3u);
+                    const int tB = (int)((infoB >> (8 + 2 * ((leWord >> (4 * kB)) & 0xF))) & 3u);
+                    // A and B differ along t; u is the remaining axis.  diffB:
+                    // A and B differ in bit 0 of k (along b) or bit 1 (along c)
+                    const bool alongB = ((kA ^ kB) & 1) != 0;
+                    const int t = alongB ? b : c, u = alongB ? c : b;
+                    const int aMinusT = alongB ? (kA & 1) : (kA >> 1);   // A = p - e_t ?
+                    const int aMinusU = alongB ? (kA >> 1) : (kA & 1);   // A = p - e_u ?
+                    // A's corner offsets (relative to A) of the face's grid edges:
+                    // the t offset is 1 where A lies below the face
+                    const int cT = aMinusT, cTB = 1 - aMinusT;
+                    const uint32_t csA = infoA & 255u;
+                    int ids[4], org[4];
+                    ids[0] = h0 + hi;
+                    org[0] = quadV[hi];
+#pragma unroll
+                    for (int cand = 0; cand < 3; ++cand) {
+                        ids[cand + 1] = 0x7FFFFFFF;
+                        org[cand + 1] = -1;
+                        // cand 0: parallel to the quad's edge on the face's other side;
+                        // cand 1, 2: across the face at the edge's lower / upper end
+                        const int al = cand == 0 ? axis : u;
+                        const int offU = cand == 0 ? (aMinusU ? 0 : 1) : 0;
+                        const int offA = cand == 2 ? 1 : 0;
+                        const int ca = (cT << t) | (offU << u) | (offA << axis);
+                        const int cb = (cTB << t) | (offU << u) | (offA << axis);
+                        const int eA = localEdge(ca, al), eB = localEdge(cb, al);
+                        const bool cross = ((csA >> edgeV0(eA)) ^ (csA >> edgeV1(eA))) & 1u;
+                        if (!cross) continue;
+                        if ((int)((infoA >> (8 + 2 * eA)) & 3u) != tA) continue;
+                        if ((int)((infoB >> (8 + 2 * eB)) & 3u) != tB) continue;
+                        // the grid edge's origin and the quad its owner holds
+                        const int du = offU - aMinusU;
+                        const int ox = px + (u == 0 ? du : 0) + (axis == 0 ? offA : 0);
+                        const int oy = py + (u == 1 ? du : 0) + (axis == 1 ? offA : 0);
+                        const int oz = pz + (u == 2 ? du : 0) + (axis == 2 ? offA : 0);
+                        if (((al != 0 && ox < 1) || (al != 1 && oy < 1) || (al != 2 && oz < 1))) continue;
+                        const int jo = ix.find(ox, oy, oz);
+                        if (jo < 0 || jo >= numActive) continue;
+                        const ActiveCell ro = act[jo];
+                        const int cso = (int)(ro.info & 255u);
+                        if (!ownsAxis(cso, al, ox, oy, oz)) continue;
+                        int r = 0;
+#pragma unroll
+                        for (int a2 = 0; a2 < 2; ++a2)
+                            if (a2 < al && ownsAxis(cso, a2, ox, oy, oz)) ++r;
+                        const int q2 = ro.qbase + r;
+                        const int edgyO = ((csA >> edgeV0(eA)) & 1u) ? 0 : 1;
+                        const int sA = quadSlot(eA, edgyO), sB = quadSlot(eB, edgyO);
+                        if (((sA + 1) & 3) == sB) {
+                            ids[cand + 1] = 4 * q2 + sA;
+                            org[cand + 1] = vbA + tA;
+                        } else if (((sB + 1) & 3) == sA) {
+                            ids[cand + 1] = 4 * q2 + sB;
+                            org[cand + 1] = vbB + tB;
+                        } else {
+                            atomicOr(&ctr->status, kStatusBadIndex);
+                        }
                     }
-                    const int csA = (int)(A.info & 255u);
-                    if (!(((csA >> edgeV0(eA)) ^ (csA >> edgeV1(eA))) & 1)) continue;  // no crossing
-                    if ((int)((A.info >> (8 + 2 * eA)) & 3u) != tA) continue;
-                    if ((int)((B.info >> (8 + 2 * eB)) & 3u) != tB) continue;
-                    const int q2 = quadOfEdge(o, al, act, rowOffsets, X, Y, Z);
-                    if (q2 < 0) continue;
-                    const int edgy = ((csA >> edgeV0(eA)) & 1) ? 0 : 1;
-                    const int sA = quadSlot(eA, edgy), sB = quadSlot(eB, edgy);
-                    if (((sA + 1) & 3) == sB) {
-                        ids[n] = 4 * q2 + sA;
-                        org[n] = A.vbase + tA;
-                    } else if (((sB + 1) & 3) == sA) {
-                        ids[n] = 4 * q2 + sB;
-                        org[n] = B.vbase + tB;
-                    } else {
-                        atomicOr(&ctr->status, kStatusBadIndex);
-                        continue;
+                    // sort the bucket (absent entries last) with its origins
+#define MDMC_CX(i0, i1)                                   \
+    if (ids[i1] < ids[i0]) {                              \
+        const int ti = ids[i0], to = org[i0];             \
+        ids[i0] = ids[i1];                                \
+        org[i0] = org[i1];                                \
+        ids[i1] = ti;                                     \
+        org[i1] = to;                                     \
+    }
+                    MDMC_CX(0, 1) MDMC_CX(2, 3) MDMC_CX(0, 2) MDMC_CX(1, 3) MDMC_CX(1, 2)
+#undef MDMC_CX
+                    const int self = h0 + hi;
+                    const int n = 1 + (ids[1] != 0x7FFFFFFF) + (ids[2] != 0x7FFFFFFF) + (ids[3] != 0x7FFFFFFF);
+                    const int me = (ids[1] == self) ? 1 : (ids[2] == self) ? 2 : (ids[3] == self) ? 3 : 0;
+                    int partner = -1;
+                    if (n == 2) {
+                        partner = 1 - me;
+                    } else if (n == 3) {
+                        partner = me == 2 ? 0 : me + 1;
+                    } else if (n == 4) {  // "HACKY_OLD_WAY", HalfedgeMesh.cu:250-281
+                        if (org[0] != org[1]) partner = me ^ 1;       // (0,1) (2,3)
+                        else if (org[0] != org[2]) partner = me ^ 2;  // (0,2) (1,3)
+                        else partner = 3 - me;                        // (0,3) (1,2)
                     }
-                    ++n;
-                }
-                // sort the bucket (<= 4 ids) with their origins
-                for (int a = 1; a < n; ++a) {
-                    const int vi = ids[a], vo = org[a];
-                    int b = a - 1;
-                    while (b >= 0 && ids[b] > vi) {
-                        ids[b + 1] = ids[b];
-                        org[b + 1] = org[b];
-                        --b;
-                    }
-                    ids[b + 1] = vi;
-                    org[b + 1] = vo;
-                }
-                int me = 0;
-                for (int a = 0; a < n; ++a)
-                    if (ids[a] == h0 + hi) me = a;
-                int twin = -1;
-                if (n == 2) {
-                    twin = ids[1 - me];
-                } else if (n == 3) {
-                    twin = ids[(me + 1) % 3];
-                } else if (n == 4) {  // "HACKY_OLD_WAY", HalfedgeMesh.cu:250-281
-                    int partner;
-                    if (org[0] != org[1]) partner = me ^ 1;            // (0,1) (2,3)
-                    else if (org[0] != org[2]) partner = me ^ 2;       // (0,2) (1,3)
-                    else partner = 3 - me;                             // (0,3) (1,2)
-                    twin = ids[partner];
-                }
-                he[h0 + hi] = make_int4(quad[hi], qi, h0 + ((hi + 1) & 3), twin);
-                heValence[h0 + hi] = (uint8_t)n;
-                const int origin = quad[hi];
-                if (n == 4) {
-                    attr |= MDMC_FACE_NON_MANIFOLD;
-                    orVertexFlag(vflags, origin, MDMC_VERTEX_NON_MANIFOLD);
-                } else if (n == 3) {
-                    orVertexFlag(vflags, origin, MDMC_VERTEX_WEIRD);
-                } else if (n == 1) {
-                    orVertexFlag(vflags, origin, MDMC_VERTEX_BOUNDARY);
-                }
-                if (me == 0) {  // the bucket's smallest halfedge counts it
-                    ++nE;
-                    if (n == 3) ++nE3;
+                    int twin = -1;
+#pragma unroll
+                    for (int t2 = 0; t2 < 4; ++t2)
+                        if (partner == t2) twin = ids[t2];
+                    out[hi] = make_int4(quadV[hi], q, h0 + ((hi + 1) & 3), twin);
+                    valences |= (uint32_t)n << (8 * hi);
+                    const int origin = quadV[hi];
                     if (n == 4) {
-                        ++nE4;
-                        const unsigned long long slot = atomicAdd(&ctr->nmBuckets, 1ULL);
-                        if (slot < (unsigned long long)nmCapacity) nmList[slot] = make_int4(ids[0], ids[1], ids[2], ids[3]);
-                        else atomicOr(&ctr->status, kStatusBadIndex);
+                        attr |= MDMC_FACE_NON_MANIFOLD;
+                        orVertexFlag(vflags, origin, MDMC_VERTEX_NON_MANIFOLD);
+                    } else if (n == 3) {
+                        orVertexFlag(vflags, origin, MDMC_VERTEX_WEIRD);
+                    } else if (n == 1) {
+                        orVertexFlag(vflags, origin, MDMC_VERTEX_BOUNDARY);
+                    }
+                    if (me == 0) {  // the bucket's smallest halfedge counts it
+                        ++nE;
+                        if (n == 3) ++nE3;
+                        if (n == 4) {
+                            ++nE4;
+                            const unsigned long long slot = atomicAdd(&ctr->nmBuckets, 1ULL);
+                            if (slot < (unsigned long long)nmCapacity)
+                                nmList[slot] = make_int4(ids[0], ids[1], ids[2], ids[3]);
+                            else
+                                atomicOr(&ctr->status, kStatusBadIndex);
+                        }
                     }
                 }
+#pragma unroll
+                for (int hi = 0; hi < 4; ++hi) he[h0 + hi] = out[hi];
+                heValence4[q] = valences;
+                faceFirst[q] = h0;
+                faceAttr[q] = (uint16_t)attr;
             }
-            faceAttr[qi] = attr;
-            ++qi;
         }
     }
     blockAddTo(&ctr->edges, nE);
@@ -800,13 +857,22 @@ __global__ void kQuads(const ActiveCell* __restrict__ act, const int* __restrict
     blockAddTo(&ctr->edges4, nE4);
 }
 
-void launchQuads(const ActiveCell* act, const int* vbase, int numActive, const int4* rowOffsets, int X, int Y, int Z,
-                 int4* he, int* faceFirst, uint16_t* faceAttr, uint8_t* vflags, uint8_t* heValence, int4* nmList,
-                 int nmCapacity, int numQuads, int numVertices, DevCounters* ctr, cudaStream_t s) {
-    if (numActive <= 0) return;
+void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, const uint32_t* cellMask,
+                 const int* cellFirst, int X, int Y, int Z, int W, int4* he, int* faceFirst, uint16_t* faceAttr,
+                 uint8_t* vflags, uint8_t* heValence, int4* nmList, int nmCapacity, int numQuads, int numVertices,
+                 DevCounters* ctr, cudaStream_t s) {
+    if (numQuads <= 0) return;
     countLaunch();
-    kQuads<<<(numActive + 127) / 128, 128, 0, s>>>(act, vbase, numActive, rowOffsets, X, Y, Z, he, faceFirst, faceAttr,
-                                                   vflags, heValence, nmList, nmCapacity, numQuads, numVertices, ctr);
+    CellIndex ix;
+    ix.mask = cellMask;
+    ix.first = cellFirst;
+    ix.X = X;
+    ix.Y = Y;
+    ix.Z = Z;
+    ix.W = W;
+    kQuads<<<(numQuads + 255) / 256, 256, 0, s>>>(act, quadOwner, numActive, ix, he, faceFirst, faceAttr, vflags,
+                                                   reinterpret_cast<uint32_t*>(heValence), nmList, nmCapacity,
+                                                   numQuads, numVertices, ctr);
 }
 
 }  // namespace mdmc

@@ -89,12 +89,15 @@ void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int p
 void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, cudaStream_t s);
 void launchRowCount(const GridDesc& g, float iso, int4* rowCounts, int numRows, cudaStream_t s);
 void launchRowEmit(const GridDesc& g, float iso, const int4* rowOffsets, int numRows, ActiveCell* act, int* numVerts,
-                   int numActive, uint32_t* status, cudaStream_t s);
+                   int* quadOwner, int numActive, int numQuads, uint32_t* status, cudaStream_t s);
+void launchIndexCells(ActiveCell* act, const int* vbase, int numActive, int X, int Y, int W, uint32_t* mask, int* first,
+                      cudaStream_t s);
 void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, const int* vbase,
                     int numActive, int numVertices, float* pos, float* nrm, uint32_t* status, cudaStream_t s);
-void launchQuads(const ActiveCell* act, const int* vbase, int numActive, const int4* rowOffsets, int X, int Y, int Z,
-                 int4* he, int* faceFirst, uint16_t* faceAttr, uint8_t* vflags, uint8_t* heValence, int4* nmList,
-                 int nmCapacity, int numQuads, int numVertices, DevCounters* ctr, cudaStream_t s);
+void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, const uint32_t* cellMask,
+                 const int* cellFirst, int X, int Y, int Z, int W, int4* he, int* faceFirst, uint16_t* faceAttr,
+                 uint8_t* vflags, uint8_t* heValence, int4* nmList, int nmCapacity, int numQuads, int numVertices,
+                 DevCounters* ctr, cudaStream_t s);
 
 void launchBuckets(Bucket* table, unsigned long long cap, int4* he, uint16_t* faceAttr, uint8_t* vflags,
                    int connectTwins, uint8_t* heValence, int4* nmList, DevCounters* ctr, MeshDims md, cudaStream_t s);
