@@ -129,14 +129,16 @@ def algorithmic_bytes(kernel, s):
     A, V, Q = s["active"], s["dmc_vertices"], s["dmc_quads"]
     if kernel == "refine":  # coarse-cell pre-pass: coarse samples read, one bit per coarse cell written
         return 4 * S_in + S_in // 8
-    if kernel == "count":  # grid read once, per-row counts written
-        return 4 * S + 16 * rows
-    if kernel == "emit":  # grid read once, row offsets read, records + contour counts + quad owners written
-        return 4 * S + 16 * rows + 16 * A + 4 * A + 4 * Q
-    if kernel == "vertices":  # records and offsets read, positions + normals written
-        return 16 * A + 4 * A + 24 * V
-    if kernel == "quads":  # records + vertex offsets + quad owners read; halfedges (with twins), faces, attributes, valences written
-        return 16 * A + 4 * A + 4 * Q + 64 * Q + 4 * Q + 2 * Q + 4 * Q
+    words = s["mask_words"]
+    if kernel == "count":  # grid read once; active-cell mask words and their first-cell offsets written
+        return 4 * S + 8 * words
+    if kernel == "emit":  # mask + offsets read; records and {contours, quads} counts written, counts scanned in place
+        return 8 * words + 16 * A + 8 * A + 16 * A
+    if kernel == "vertices":  # records read, positions + normals written
+        return 16 * A + 24 * V
+    if kernel == "quads":  # offsets -> records + quad owners; records + owners read, halfedges (with twins),
+        # faces, attributes, valences written
+        return (8 * A + 8 * A + 4 * Q) + (4 * Q + 16 * A + 64 * Q + 4 * Q + 2 * Q + 4 * Q)
     raise KeyError(kernel)
 
 
@@ -224,6 +226,7 @@ def run_ours(args, rank, world, local):
     value = world * cells / (ms / 1e3) / 1e6
 
     sizes = {"samples_in": int(np.prod(dims_in)), "samples": samples, "rows": (grid.dims[1] - 1) * (grid.dims[2] - 1),
+             "mask_words": (grid.dims[1] - 1) * (grid.dims[2] - 1) * ((grid.dims[0] - 1 + 31) // 32),
              "refined": bool(refine or pad),
              "active": int(stats.num_active_cells), "dmc_vertices": int(stats.num_dmc_vertices),
              "dmc_quads": int(stats.num_dmc_quads)}

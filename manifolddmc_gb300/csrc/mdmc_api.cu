@@ -77,14 +77,15 @@ struct mdmc_context {
     // grid preparation
     DevBuf gridBuf, stageBuf, mayCross;
     // DMC stage
-    DevBuf rows, scanScratch, act, vbase;
+    DevBuf scanScratch, act;
     // mesh
     DevBuf pos, nrm, he, faceFirst, faceAttr, vflags, vertexHE, quads;
     int64_t V = 0, F = 0, H = 0;
     // edge table
     DevBuf table, nmList, heValence;
-    // quad -> owner cell, and the per-row cell index (mask + first active id per 32 cells)
-    DevBuf quadOwner, cellMask, cellFirst;
+    // quad -> owner cell; per-row active-cell mask (32 cells per word) and the
+    // index of each word's first active cell; per active cell {contours, quads}
+    DevBuf quadOwner, cellMask, cellFirst, cellCounts, cellIds;
     bool tableValid = false;  // the edge table holds the current mesh (after a splitter refresh)
     unsigned long long cap = 0;
     // counters
@@ -595,40 +596,47 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     mdmc_status st0 = makeGridDesc(c, grid, iso, g, s);
     if (st0 != MDMC_OK) return st0;
 
-    // ---- DMC: count, scan, emit (performDualMarchingCubes) --------------------
+    // ---- DMC (performDualMarchingCubes) -----------------------------------------
+    // active-cell mask per x-row of cells, word counts -> index of every
+    // word's first active cell (the cell index the quad pass reads too)
     const int64_t numRows = (X > 1 && Y > 1 && Z > 1) ? (int64_t)(Y - 1) * (Z - 1) : 0;
-    MDMC_CHECK(c, c->rows.ensure(sizeof(int4) * (size_t)(numRows + 1)));
+    const int W = (X - 1 + 31) / 32;
+    const int64_t numWords = numRows * (int64_t)W;
+    MDMC_CHECK(c, c->cellMask.ensure(sizeof(uint32_t) * (size_t)std::max<int64_t>(numWords, 1)));
+    MDMC_CHECK(c, c->cellFirst.ensure(sizeof(int) * (size_t)(numWords + 1)));
     cudaEventRecord(c->kev[2], s);
-    if (numRows > 0) launchRowCount(g, iso, c->rows.as<int4>(), (int)numRows, s);
-    cudaEventRecord(c->kev[3], s);
-    mdmc_status st = scan<int4>(c, c->rows.as<int4>(), c->rows.as<int4>(), numRows, s);
+    if (g.refined && numWords > 0) MDMC_CHECK(c, cudaMemsetAsync(c->cellMask.p, 0, sizeof(uint32_t) * (size_t)numWords, s));
+    launchRowMask(g, iso, c->cellMask.as<uint32_t>(), (int)numRows, W, s);
+    launchWordCounts(c->cellMask.as<uint32_t>(), numWords, c->cellFirst.as<int>(), s);
+    mdmc_status st = scan<int>(c, c->cellFirst.as<int>(), c->cellFirst.as<int>(), numWords, s);
     if (st != MDMC_OK) return st;
+    cudaEventRecord(c->kev[3], s);
     MDMC_CHECK(c, cudaGetLastError());
-    if ((st = readInts(c, c->rows.as<int4>() + numRows, 4, s)) != MDMC_OK) return st;
-    const int* tot = reinterpret_cast<const int*>(c->hostInts);
-    const int64_t A = tot[0], Q = tot[1];
+    if ((st = readInts(c, c->cellFirst.as<int>() + numWords, 1, s)) != MDMC_OK) return st;
+    const int64_t A = c->hostInts[0];
     const int64_t cells = numRows * (int64_t)(X - 1);
-    if (A < 0 || A > cells || Q < 0 || Q > 3 * A)
-        return fail(c, MDMC_ERROR_CUDA, "inconsistent cell counts from the count pass");
+    if (A < 0 || A > cells) return fail(c, MDMC_ERROR_CUDA, "inconsistent cell count from the mask pass");
     c->stats.num_active_cells = A;
+
+    // the active cells' records, contour and quad counts, and their offsets
+    MDMC_CHECK(c, c->act.ensure(sizeof(ActiveCell) * (size_t)std::max<int64_t>(A, 1)));
+    MDMC_CHECK(c, c->cellCounts.ensure(sizeof(int2) * (size_t)(A + 1)));
+    MDMC_CHECK(c, c->cellIds.ensure(sizeof(uint32_t) * (size_t)std::max<int64_t>(A, 1)));
+    cudaEventRecord(c->kev[4], s);
+    launchScatterCells(c->cellMask.as<uint32_t>(), c->cellFirst.as<int>(), numWords, W, X, Y, c->cellIds.as<uint32_t>(),
+                       (int)A, status, s);
+    launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A, status,
+                     s);
+    if ((st = scan<int2>(c, c->cellCounts.as<int2>(), c->cellCounts.as<int2>(), A, s)) != MDMC_OK) return st;
+    cudaEventRecord(c->kev[5], s);
+    MDMC_CHECK(c, cudaGetLastError());
+    if ((st = readInts(c, c->cellCounts.as<int2>() + A, 2, s)) != MDMC_OK) return st;
+    const int64_t Vd = c->hostInts[0], Q = c->hostInts[1];
+    if (Vd < A || Vd > 4 * A || Q < 0 || Q > 3 * A)
+        return fail(c, MDMC_ERROR_CUDA, "inconsistent vertex or quad count from the emit pass");
+    c->stats.num_dmc_vertices = Vd;
     c->stats.num_dmc_quads = Q;
     if (4 * Q >= (int64_t)0x7FFFFFFF) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "more than 2^31 halfedges");
-
-    // compaction of the active cells and their contour counts
-    MDMC_CHECK(c, c->act.ensure(sizeof(ActiveCell) * (size_t)std::max<int64_t>(A, 1)));
-    MDMC_CHECK(c, c->vbase.ensure(sizeof(int) * (size_t)(A + 1)));
-    MDMC_CHECK(c, c->quadOwner.ensure(sizeof(int) * (size_t)std::max<int64_t>(Q, 1)));
-    cudaEventRecord(c->kev[4], s);
-    if (numRows > 0)
-        launchRowEmit(g, iso, c->rows.as<int4>(), (int)numRows, c->act.as<ActiveCell>(), c->vbase.as<int>(),
-                      c->quadOwner.as<int>(), (int)A, (int)Q, status, s);
-    cudaEventRecord(c->kev[5], s);
-    if ((st = scan<int>(c, c->vbase.as<int>(), c->vbase.as<int>(), A, s)) != MDMC_OK) return st;
-    MDMC_CHECK(c, cudaGetLastError());
-    if ((st = readInts(c, c->vbase.as<int>() + A, 1, s)) != MDMC_OK) return st;
-    const int64_t Vd = c->hostInts[0];
-    if (Vd < A || Vd > 4 * A) return fail(c, MDMC_ERROR_CUDA, "inconsistent vertex count from the emit pass");
-    c->stats.num_dmc_vertices = Vd;
     if (Vd == 0) {
         // "DMC: No Vertices have been produced!" (D/DualMarchingCubes.cu:256-261)
         c->V = c->F = c->H = 0;
@@ -644,6 +652,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->F = Q;
     c->H = 4 * Q;
     c->tableValid = false;
+    MDMC_CHECK(c, c->quadOwner.ensure(sizeof(int) * (size_t)std::max<int64_t>(Q, 1)));
     MDMC_CHECK(c, c->pos.ensure(sizeof(float) * 3 * (size_t)Vd));
     MDMC_CHECK(c, c->nrm.ensure(sizeof(float) * 3 * (size_t)Vd));
     MDMC_CHECK(c, c->vflags.ensure(roundUp((size_t)Vd, 4)));
@@ -653,27 +662,22 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, c->nmList.ensure(sizeof(int4) * (size_t)(Q + 1)));
     MDMC_CHECK(c, c->heValence.ensure((size_t)std::max<int64_t>(4 * Q, 1)));
     MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)Vd, 4), s));
-    cudaEventRecord(c->kev[10], s);
-    launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), c->vbase.as<int>(), (int)A,
-                   (int)Vd, c->pos.as<float>(), c->nrm.as<float>(), status, s);
-    cudaEventRecord(c->kev[11], s);
+
     // mapQuadrilaterals + collectHalfedgeElements, and the halfedge mesh's
     // twins and flags (HalfedgeMesh::initialize) in the same pass
     cudaEventRecord(c->kev[6], s);
-    {
-        const int W = (X - 1 + 31) / 32;
-        const size_t words = (size_t)numRows * (size_t)W;
-        MDMC_CHECK(c, c->cellMask.ensure(sizeof(uint32_t) * std::max<size_t>(words, 1)));
-        MDMC_CHECK(c, c->cellFirst.ensure(sizeof(int) * std::max<size_t>(words, 1)));
-        MDMC_CHECK(c, cudaMemsetAsync(c->cellMask.p, 0, sizeof(uint32_t) * words, s));
-        launchIndexCells(c->act.as<ActiveCell>(), c->vbase.as<int>(), (int)A, X, Y, W, c->cellMask.as<uint32_t>(),
-                         c->cellFirst.as<int>(), s);
-        launchQuads(c->act.as<ActiveCell>(), c->quadOwner.as<int>(), (int)A, c->cellMask.as<uint32_t>(),
-                    c->cellFirst.as<int>(), X, Y, Z, W, c->he.as<int4>(), c->faceFirst.as<int>(),
-                    c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(),
-                    c->nmList.as<int4>(), (int)(Q + 1), (int)Q, (int)Vd, ctr, s);
-    }
+    launchFinishCells(c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A, X, Y, c->quadOwner.as<int>(), (int)Q,
+                      status, s);
+    launchQuads(c->act.as<ActiveCell>(), c->quadOwner.as<int>(), (int)A, c->cellMask.as<uint32_t>(),
+                c->cellFirst.as<int>(), X, Y, Z, W, c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(),
+                c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(), c->nmList.as<int4>(), (int)(Q + 1), (int)Q,
+                (int)Vd, ctr, s);
     cudaEventRecord(c->kev[7], s);
+    // vertex positions and normals (sliceP's vertex part)
+    cudaEventRecord(c->kev[10], s);
+    launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), (int)A, (int)Vd,
+                   c->pos.as<float>(), c->nrm.as<float>(), status, s);
+    cudaEventRecord(c->kev[11], s);
     MDMC_CHECK(c, cudaGetLastError());
     cudaEventRecord(c->ev[1], s);
     cudaEventRecord(c->kev[8], s);

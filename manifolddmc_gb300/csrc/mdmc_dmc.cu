@@ -388,81 +388,169 @@ void launchRowCount(const GridDesc& g, float iso, int4* rowCounts, int numRows, 
     else kRowCount<PlainView><<<(numRows + 7) / 8, 256, 0, s>>>(g.plain, iso, rowCounts, numRows);
 }
 
-// compaction: the active cells of the row in x order, with the number of
-// contours (= vertices) of each cell and its edge -> contour map.  Rows
-// without active cells (known from the count pass) are skipped.
+// The active-cell mask: bit x of word (row, x / 32) is set when cell x of the
+// row is active (case neither 0 nor 255).  Plain rows store whole ballots;
+// refined rows visit only candidate cells and OR their bits into words
+// cleared beforehand.
 template <class View>
-__global__ void __launch_bounds__(256) kRowEmit(View g, float iso, const int4* __restrict__ rowOffsets, int numRows,
-                                                ActiveCell* __restrict__ act, int* __restrict__ numVerts,
-                                                int* __restrict__ quadOwner, int numActive, int numQuads,
-                                                uint32_t* status) {
-    __shared__ uint64_t table[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kContourTable[i];
-    __syncthreads();
+__global__ void __launch_bounds__(256) kRowMask(View g, float iso, uint32_t* __restrict__ mask, int numRows, int W) {
     const int lane = threadIdx.x & 31;
     const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (row >= numRows) return;
-    const int4 base = rowOffsets[row];
-    if (rowOffsets[row + 1].x == base.x) return;
     const int y = row % (g.Y - 1), z = row / (g.Y - 1);
-    int aRun = base.x, qRun = base.y;
-    const unsigned ltMask = (1u << lane) - 1u;
+    uint32_t* words = mask + (int64_t)row * W;
     walkRow(g, y, z, lane, [&](int x, const float s[8]) {
-        int cs = 0, nq = 0;
+        bool active = false;
         if (x < g.X - 1) {
-            cs = caseOf(s, iso);
-            if (cs != 0 && cs != 255) nq = ownedQuads(cs, x, y, z);
+            const int cs = caseOf(s, iso);
+            active = cs != 0 && cs != 255;
         }
-        const bool active = cs != 0 && cs != 255;
-        const unsigned ballot = __ballot_sync(0xffffffffu, active);
-        int qInc = nq;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int u = __shfl_up_sync(0xffffffffu, qInc, o);
-            if (lane >= o) qInc += u;
+        if constexpr (View::kRefined) {
+            if (active) atomicOr(&words[x >> 5], 1u << (x & 31));
+        } else {
+            const unsigned ballot = __ballot_sync(0xffffffffu, active);
+            if (lane == 0 && x < g.X - 1) words[x >> 5] = ballot;
         }
-        const int qTot = __shfl_sync(0xffffffffu, qInc, 31);
-        if (active) {
-            const int aIdx = aRun + __popc(ballot & ltMask);
-            if (aIdx < numActive) {
-                const uint64_t c = cellContours(cs, s, iso, table);
-                uint32_t emap = 0;
-                int before = 0;
-                const int n = numContours(c);
-                for (int t = 0; t < n; ++t) {
-                    const int sz = nib(c, t);
-                    for (int i = 0; i < sz; ++i) emap |= (uint32_t)t << (2 * (int)((c >> (16 + 4 * (before + i))) & 0xF));
-                    before += sz;
-                }
-                ActiveCell rec;
-                rec.cell = (uint32_t)(((size_t)z * g.Y + y) * g.X + x);
-                rec.qbase = qRun + qInc - nq;
-                rec.info = (uint32_t)cs | (emap << 8);
-                rec.pad = 0;
-                act[aIdx] = rec;
-                numVerts[aIdx] = n;
-                for (int r = 0; r < nq; ++r) {
-                    if (inb(rec.qbase + r, numQuads)) quadOwner[rec.qbase + r] = aIdx;
-                    else atomicOr(status, kStatusCountMismatch);
-                }
-            } else {
-                atomicOr(status, kStatusCountMismatch);
-            }
-        }
-        aRun += __popc(ballot);
-        qRun += qTot;
     });
 }
 
-void launchRowEmit(const GridDesc& g, float iso, const int4* rowOffsets, int numRows, ActiveCell* act, int* numVerts,
-                   int* quadOwner, int numActive, int numQuads, uint32_t* status, cudaStream_t s) {
+void launchRowMask(const GridDesc& g, float iso, uint32_t* mask, int numRows, int W, cudaStream_t s) {
+    if (numRows <= 0) return;
     countLaunch();
+    if (g.refined) kRowMask<RefinedView><<<(numRows + 7) / 8, 256, 0, s>>>(g.ref, iso, mask, numRows, W);
+    else kRowMask<PlainView><<<(numRows + 7) / 8, 256, 0, s>>>(g.plain, iso, mask, numRows, W);
+}
+
+__global__ void kWordCounts(const uint32_t* __restrict__ mask, int64_t numWords, int* __restrict__ counts) {
+    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w < numWords) counts[w] = __popc(mask[w]);
+}
+
+void launchWordCounts(const uint32_t* mask, int64_t numWords, int* counts, cudaStream_t s) {
+    if (numWords <= 0) return;
+    countLaunch();
+    kWordCounts<<<(unsigned)((numWords + 255) / 256), 256, 0, s>>>(mask, numWords, counts);
+}
+
+// The linear cell id of every active cell, in row-major order: one thread
+// per mask word; the index of the word's first active cell comes from the
+// scan of the word counts.
+__global__ void kScatterCells(const uint32_t* __restrict__ mask, const int* __restrict__ first, int64_t numWords, int W,
+                              int X, int Y, uint32_t* __restrict__ cellIds, int numActive, uint32_t* status) {
+    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= numWords) return;
+    uint32_t m = mask[w];
+    if (!m) return;
+    const int row = (int)(w / W);
+    const int x0 = (int)(w - (int64_t)row * W) * 32;
+    const int y = row % (Y - 1), z = row / (Y - 1);
+    const uint32_t base = (uint32_t)(((size_t)z * Y + y) * X + x0);
+    int j = first[w];
+    while (m) {
+        const int b = __ffs(m) - 1;
+        m &= m - 1;
+        if (inb(j, numActive)) cellIds[j] = base + (uint32_t)b;
+        else atomicOr(status, kStatusCountMismatch);
+        ++j;
+    }
+}
+
+void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords, int W, int X, int Y, uint32_t* cellIds,
+                        int numActive, uint32_t* status, cudaStream_t s) {
+    if (numWords <= 0) return;
+    countLaunch();
+    kScatterCells<<<(unsigned)((numWords + 255) / 256), 256, 0, s>>>(mask, first, numWords, W, X, Y, cellIds, numActive,
+                                                                     status);
+}
+
+// Records of the active cells: the cell, its case and edge -> contour map,
+// and its number of contours (= vertices) and owned quads.  One thread per
+// active cell; the corner samples come from the same column evaluation as
+// the mask pass, so the case is the one that set the cell's mask bit.
+template <class View>
+__global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint32_t* __restrict__ cellIds,
+                                                   ActiveCell* __restrict__ act, int2* __restrict__ counts,
+                                                   int numActive, uint32_t* status) {
+    __shared__ uint64_t table[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kContourTable[i];
+    __syncthreads();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= numActive) return;
+    const uint32_t cell = cellIds[j];
+    const uint32_t line = cell / (uint32_t)g.X;
+    const int x = (int)(cell - line * (uint32_t)g.X), y = (int)(line % (uint32_t)g.Y), z = (int)(line / (uint32_t)g.Y);
+    if (x >= g.X - 1 || y >= g.Y - 1 || z >= g.Z - 1) {
+        atomicOr(status, kStatusCountMismatch);
+        return;
+    }
+    const RowWalker<View> walker(g, y, z);
+    float cur[4], nxt[4];
+    walker.load(x, cur);
+    walker.load(x + 1, nxt);
+    float s[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        s[2 * k] = cur[k];
+        s[2 * k + 1] = nxt[k];
+    }
+    const int cs = caseOf(s, iso);
+    if (cs == 0 || cs == 255) {
+        atomicOr(status, kStatusCountMismatch);
+        return;
+    }
+    const uint64_t c = cellContours(cs, s, iso, table);
+    uint32_t emap = 0;
+    int before = 0;
+    const int n = numContours(c);
+    for (int t = 0; t < n; ++t) {
+        const int sz = nib(c, t);
+        for (int i = 0; i < sz; ++i) emap |= (uint32_t)t << (2 * (int)((c >> (16 + 4 * (before + i))) & 0xF));
+        before += sz;
+    }
+    ActiveCell rec;
+    rec.cell = cell;
+    rec.qbase = 0;
+    rec.info = (uint32_t)cs | (emap << 8);
+    rec.pad = 0;
+    act[j] = rec;
+    counts[j] = make_int2(n, ownedQuads(cs, x, y, z));
+}
+
+void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, ActiveCell* act, int2* counts,
+                      int numActive, uint32_t* status, cudaStream_t s) {
+    if (numActive <= 0) return;
+    countLaunch();
+    const unsigned blocks = (unsigned)((numActive + 127) / 128);
     if (g.refined)
-        kRowEmit<RefinedView><<<(numRows + 7) / 8, 256, 0, s>>>(g.ref, iso, rowOffsets, numRows, act, numVerts, quadOwner,
-                                                                numActive, numQuads, status);
+        kEmitActive<RefinedView><<<blocks, 128, 0, s>>>(g.ref, iso, cellIds, act, counts, numActive, status);
     else
-        kRowEmit<PlainView><<<(numRows + 7) / 8, 256, 0, s>>>(g.plain, iso, rowOffsets, numRows, act, numVerts, quadOwner,
-                                                              numActive, numQuads, status);
+        kEmitActive<PlainView><<<blocks, 128, 0, s>>>(g.plain, iso, cellIds, act, counts, numActive, status);
+}
+
+// Each active cell's first vertex id (kept in its record's spare word) and
+// first quad id, and the owner of every quad.
+__global__ void kFinishCells(ActiveCell* __restrict__ act, const int2* __restrict__ offsets, int numActive, int X, int Y,
+                             int* __restrict__ quadOwner, int numQuads, uint32_t* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= numActive) return;
+    const ActiveCell rec = act[i];
+    const int2 off = offsets[i];
+    const uint32_t line = rec.cell / (uint32_t)X;
+    const int x = (int)(rec.cell - line * (uint32_t)X), y = (int)(line % (uint32_t)Y), z = (int)(line / (uint32_t)Y);
+    const int nq = ownedQuads((int)(rec.info & 255u), x, y, z);
+    act[i].qbase = off.y;
+    act[i].pad = off.x;
+    for (int r = 0; r < nq; ++r) {
+        if (inb(off.y + r, numQuads)) quadOwner[off.y + r] = i;
+        else atomicOr(status, kStatusCountMismatch);
+    }
+}
+
+void launchFinishCells(ActiveCell* act, const int2* offsets, int numActive, int X, int Y, int* quadOwner, int numQuads,
+                       uint32_t* status, cudaStream_t s) {
+    if (numActive <= 0) return;
+    countLaunch();
+    kFinishCells<<<(numActive + 255) / 256, 256, 0, s>>>(act, offsets, numActive, X, Y, quadOwner, numQuads, status);
 }
 
 // ---------------------------------------------------------------------------
@@ -471,8 +559,8 @@ void launchRowEmit(const GridDesc& g, float iso, const int4* rowOffsets, int num
 // ---------------------------------------------------------------------------
 template <class View>
 __global__ void __launch_bounds__(128) kVertices(View g, float iso, int surfaceIteration,
-                                                 const ActiveCell* __restrict__ act, const int* __restrict__ vbase,
-                                                 int numActive, int numVertices, float* __restrict__ pos,
+                                                 const ActiveCell* __restrict__ act, int numActive,
+                                                 int numVertices, float* __restrict__ pos,
                                                  float* __restrict__ nrm, uint32_t* status) {
     __shared__ uint64_t table[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kContourTable[i];
@@ -483,7 +571,7 @@ __global__ void __launch_bounds__(128) kVertices(View g, float iso, int surfaceI
     const int x = (int)(rec.cell % (uint32_t)g.X);
     const int y = (int)((rec.cell / (uint32_t)g.X) % (uint32_t)g.Y);
     const int z = (int)(rec.cell / ((uint32_t)g.X * (uint32_t)g.Y));
-    const int vb = vbase[i];
+    const int vb = rec.pad;  // first vertex id
     const int cs = (int)(rec.info & 255u);
     float s[8];
 #pragma unroll
@@ -528,52 +616,24 @@ __global__ void __launch_bounds__(128) kVertices(View g, float iso, int surfaceI
     }
 }
 
-void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, const int* vbase,
-                    int numActive, int numVertices, float* pos, float* nrm, uint32_t* status, cudaStream_t s) {
+void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, int numActive,
+                    int numVertices, float* pos, float* nrm, uint32_t* status, cudaStream_t s) {
     if (numActive <= 0) return;
     countLaunch();
     const unsigned blocks = (unsigned)((numActive + 127) / 128);
     if (g.refined)
-        kVertices<RefinedView><<<blocks, 128, 0, s>>>(g.ref, iso, surfaceIteration, act, vbase, numActive, numVertices, pos,
-                                                      nrm, status);
+        kVertices<RefinedView><<<blocks, 128, 0, s>>>(g.ref, iso, surfaceIteration, act, numActive, numVertices, pos, nrm,
+                                                      status);
     else
-        kVertices<PlainView><<<blocks, 128, 0, s>>>(g.plain, iso, surfaceIteration, act, vbase, numActive, numVertices,
-                                                    pos, nrm, status);
+        kVertices<PlainView><<<blocks, 128, 0, s>>>(g.plain, iso, surfaceIteration, act, numActive, numVertices, pos, nrm,
+                                                    status);
 }
 
 // ---------------------------------------------------------------------------
-// cell index: for every x-row of cells and every 32 cells of it, the mask of
-// the active ones and the index (in the active-cell list) of the first, so a
-// cell's record is one load away.  Also stores each cell's first vertex id in
-// its record.  Built once per run, one thread per active cell.
+// cell index: the active-cell mask of every x-row of cells (32 cells per word)
+// and, per word, the index of its first active cell in the active-cell list,
+// so a cell's record is one load away
 // ---------------------------------------------------------------------------
-__global__ void kIndexCells(ActiveCell* __restrict__ act, const int* __restrict__ vbase, int numActive, int X, int Y,
-                            int W, uint32_t* __restrict__ mask, int* __restrict__ first) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= numActive) return;
-    const uint32_t cell = act[i].cell;
-    const uint32_t line = cell / (uint32_t)X;  // z * Y + y
-    const int x = (int)(cell - line * (uint32_t)X);
-    const int y = (int)(line % (uint32_t)Y), z = (int)(line / (uint32_t)Y);
-    const int64_t w = ((int64_t)z * (Y - 1) + y) * W + (x >> 5);
-    atomicOr(&mask[w], 1u << (x & 31));
-    bool lead = i == 0;
-    if (!lead) {
-        const uint32_t pc = act[i - 1].cell;
-        const uint32_t pl = pc / (uint32_t)X;
-        lead = pl != line || ((int)(pc - pl * (uint32_t)X) >> 5) != (x >> 5);
-    }
-    if (lead) first[w] = i;
-    act[i].pad = vbase[i];
-}
-
-void launchIndexCells(ActiveCell* act, const int* vbase, int numActive, int X, int Y, int W, uint32_t* mask, int* first,
-                      cudaStream_t s) {
-    if (numActive <= 0) return;
-    countLaunch();
-    kIndexCells<<<(numActive + 255) / 256, 256, 0, s>>>(act, vbase, numActive, X, Y, W, mask, first);
-}
-
 struct CellIndex {
     const uint32_t* mask;
     const int* first;

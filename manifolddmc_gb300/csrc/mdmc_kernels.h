@@ -88,12 +88,16 @@ struct SplitWork {
 void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int pad, cudaStream_t s);
 void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, cudaStream_t s);
 void launchRowCount(const GridDesc& g, float iso, int4* rowCounts, int numRows, cudaStream_t s);
-void launchRowEmit(const GridDesc& g, float iso, const int4* rowOffsets, int numRows, ActiveCell* act, int* numVerts,
-                   int* quadOwner, int numActive, int numQuads, uint32_t* status, cudaStream_t s);
-void launchIndexCells(ActiveCell* act, const int* vbase, int numActive, int X, int Y, int W, uint32_t* mask, int* first,
-                      cudaStream_t s);
-void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, const int* vbase,
-                    int numActive, int numVertices, float* pos, float* nrm, uint32_t* status, cudaStream_t s);
+void launchRowMask(const GridDesc& g, float iso, uint32_t* mask, int numRows, int W, cudaStream_t s);
+void launchWordCounts(const uint32_t* mask, int64_t numWords, int* counts, cudaStream_t s);
+void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords, int W, int X, int Y, uint32_t* cellIds,
+                        int numActive, uint32_t* status, cudaStream_t s);
+void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, ActiveCell* act, int2* counts,
+                      int numActive, uint32_t* status, cudaStream_t s);
+void launchFinishCells(ActiveCell* act, const int2* offsets, int numActive, int X, int Y, int* quadOwner, int numQuads,
+                       uint32_t* status, cudaStream_t s);
+void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, int numActive,
+                    int numVertices, float* pos, float* nrm, uint32_t* status, cudaStream_t s);
 void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, const uint32_t* cellMask,
                  const int* cellFirst, int X, int Y, int Z, int W, int4* he, int* faceFirst, uint16_t* faceAttr,
                  uint8_t* vflags, uint8_t* heValence, int4* nmList, int nmCapacity, int numQuads, int numVertices,

@@ -6,8 +6,8 @@
 // simulator's pre-allocated pool, a process under a hard memory cap), or that
 // must not stall the device: cudaMalloc and cudaFree synchronize the whole
 // device, and mdmc_run grows its context buffers with them.  This entry point
-// needs no context, allocates nothing and does not synchronize; it runs the
-// same row-count kernel mdmc_run starts with.
+// needs no context, allocates nothing and does not synchronize; its per-row
+// count kernel classifies cells exactly as mdmc_run's mask pass does.
 //
 // Scratch: two file-scope device arrays, shared by every call in the process
 // on a device and keeping the last call's contents:

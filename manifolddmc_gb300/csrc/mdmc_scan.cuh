@@ -1,4 +1,4 @@
-// Exclusive prefix sums over int and int4 arrays, in three phases: per-tile
+// Exclusive prefix sums over int, int2 and int4 arrays, in three phases: per-tile
 // reduction, one-block scan of the tile sums, per-tile scan with the tile's
 // offset.  out has n+1 entries; out[n] is the total.
 #pragma once
@@ -24,25 +24,34 @@ struct ScanOps<int> {
     __device__ static int add(int a, int b) { return a + b; }
 };
 template <>
+struct ScanOps<int2> {
+    __device__ static int2 zero() { return make_int2(0, 0); }
+    __device__ static int2 add(int2 a, int2 b) { return make_int2(a.x + b.x, a.y + b.y); }
+};
+template <>
 struct ScanOps<int4> {
     __device__ static int4 zero() { return make_int4(0, 0, 0, 0); }
     __device__ static int4 add(int4 a, int4 b) { return make_int4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
 };
+
+__device__ __forceinline__ int shflUp(int v, int o) { return __shfl_up_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ int2 shflUp(int2 v, int o) {
+    return make_int2(__shfl_up_sync(0xffffffffu, v.x, o), __shfl_up_sync(0xffffffffu, v.y, o));
+}
+__device__ __forceinline__ int4 shflUp(int4 v, int o) {
+    return make_int4(__shfl_up_sync(0xffffffffu, v.x, o), __shfl_up_sync(0xffffffffu, v.y, o),
+                     __shfl_up_sync(0xffffffffu, v.z, o), __shfl_up_sync(0xffffffffu, v.w, o));
+}
+__device__ __forceinline__ int minus(int a, int b) { return a - b; }
+__device__ __forceinline__ int2 minus(int2 a, int2 b) { return make_int2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ int4 minus(int4 a, int4 b) { return make_int4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
 
 template <typename T>
 __device__ T warpInclusive(T v) {
     const int lane = threadIdx.x & 31;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        T u;
-        if constexpr (sizeof(T) == sizeof(int)) {
-            u = __shfl_up_sync(0xffffffffu, v, o);
-        } else {
-            u.x = __shfl_up_sync(0xffffffffu, v.x, o);
-            u.y = __shfl_up_sync(0xffffffffu, v.y, o);
-            u.z = __shfl_up_sync(0xffffffffu, v.z, o);
-            u.w = __shfl_up_sync(0xffffffffu, v.w, o);
-        }
+        const T u = shflUp(v, o);
         if (lane >= o) v = ScanOps<T>::add(v, u);
     }
     return v;
@@ -66,14 +75,8 @@ __device__ T blockExclusive(T v, T& total) {
     T before = warp > 0 ? warpSums[warp - 1] : ScanOps<T>::zero();
     total = warpSums[nw - 1];
     __syncthreads();
-    T exc = inc;
-    // exclusive = inclusive - own value, computed additively
-    if constexpr (sizeof(T) == sizeof(int)) {
-        exc = inc - v;
-    } else {
-        exc = make_int4(inc.x - v.x, inc.y - v.y, inc.z - v.z, inc.w - v.w);
-    }
-    return ScanOps<T>::add(before, exc);
+    // exclusive = inclusive - own value
+    return ScanOps<T>::add(before, minus(inc, v));
 }
 
 template <typename T>
