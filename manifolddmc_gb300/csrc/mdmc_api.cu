@@ -75,7 +75,7 @@ struct mdmc_context {
     mdmc_options opt;
     std::string err;
     // grid preparation
-    DevBuf gridBuf, stageBuf, mayCross;
+    DevBuf gridBuf, stageBuf, mayCross, candidates;
     // DMC stage
     DevBuf scanScratch, act;
     // mesh
@@ -218,9 +218,11 @@ mdmc_status makeGridDesc(mdmc_context* c, const mdmc_grid* grid, float iso, Grid
     if (d.ref.cX >= 2 && d.ref.cY >= 2 && d.ref.cZ >= 2) {
         const int64_t cells = (int64_t)(d.ref.cX - 1) * (d.ref.cY - 1) * (d.ref.cZ - 1);
         MDMC_CHECK(c, c->mayCross.ensure(sizeof(uint32_t) * (size_t)((cells + 31) / 32 + 1)));
+        MDMC_CHECK(c, c->candidates.ensure(sizeof(uint32_t) * (size_t)cells));
         d.ref.mayCross = c->mayCross.as<uint32_t>();
         cudaEventRecord(c->kev[0], s);
-        launchCoarseMayCross(d.ref, iso, c->mayCross.as<uint32_t>(), s);
+        launchCoarseMayCross(d.ref, iso, c->mayCross.as<uint32_t>(), c->candidates.as<uint32_t>(),
+                             &c->counters.as<DevCounters>()->candidates, s);
         cudaEventRecord(c->kev[1], s);
     }
     return MDMC_OK;
@@ -606,7 +608,11 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, c->cellFirst.ensure(sizeof(int) * (size_t)(numWords + 1)));
     cudaEventRecord(c->kev[2], s);
     if (g.refined && numWords > 0) MDMC_CHECK(c, cudaMemsetAsync(c->cellMask.p, 0, sizeof(uint32_t) * (size_t)numWords, s));
-    launchRowMask(g, iso, c->cellMask.as<uint32_t>(), (int)numRows, W, s);
+    if (g.refined && g.ref.mayCross && (g.ref.r + 4) * (g.ref.r + 4) <= 512 && numWords > 0)
+        launchBlockMask(g.ref, iso, c->candidates.as<uint32_t>(), &ctr->candidates, c->cellMask.as<uint32_t>(), W, status,
+                        s);
+    else
+        launchRowMask(g, iso, c->cellMask.as<uint32_t>(), (int)numRows, W, s);
     launchWordCounts(c->cellMask.as<uint32_t>(), numWords, c->cellFirst.as<int>(), s);
     mdmc_status st = scan<int>(c, c->cellFirst.as<int>(), c->cellFirst.as<int>(), numWords, s);
     if (st != MDMC_OK) return st;

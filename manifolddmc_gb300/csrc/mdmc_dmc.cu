@@ -71,7 +71,7 @@ void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int p
 // cells, and its refined cells need not be evaluated at all.
 // ---------------------------------------------------------------------------
 __global__ void kCoarseMayCross(const float* __restrict__ c, int cX, int cY, int cZ, float iso, uint32_t* __restrict__ bits,
-                                int64_t numCells) {
+                                int64_t numCells, uint32_t* __restrict__ list, unsigned long long* listCount) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool may = false;
     if (i < numCells) {
@@ -94,15 +94,28 @@ __global__ void kCoarseMayCross(const float* __restrict__ c, int cX, int cY, int
         may = nan || !(allBelow || allAbove);
     }
     const unsigned b = __ballot_sync(0xffffffffu, may);
-    if ((threadIdx.x & 31) == 0 && i < numCells) bits[i >> 5] = b;
+    const int lane = threadIdx.x & 31;
+    if (lane == 0 && i < numCells) bits[i >> 5] = b;
+    if (list && b) {  // the candidates, in any order
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(listCount, (unsigned long long)__popc(b));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (may) list[base + __popc(b & ((1u << lane) - 1u))] = (uint32_t)i;
+    }
 }
 
 void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, cudaStream_t s) {
+    launchCoarseMayCross(g, iso, bits, nullptr, nullptr, s);
+}
+
+void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, uint32_t* list, unsigned long long* listCount,
+                          cudaStream_t s) {
     const int64_t n = (int64_t)(g.cX - 1) * (g.cY - 1) * (g.cZ - 1);
     if (n <= 0) return;
     countLaunch();
-    kCoarseMayCross<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g.c, g.cX, g.cY, g.cZ, iso, bits, n);
+    kCoarseMayCross<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g.c, g.cX, g.cY, g.cZ, iso, bits, n, list, listCount);
 }
+
 
 // ---------------------------------------------------------------------------
 // row streaming.  A warp walks one x-row of cells in chunks of 32.  Each lane
@@ -273,6 +286,91 @@ __device__ __forceinline__ int ownedQuads(int cs, int x, int y, int z) {
     return ((((cs ^ (cs >> 1)) & 1) && y >= 1 && z >= 1) ? 1 : 0) +
            ((((cs ^ (cs >> 2)) & 1) && x >= 1 && z >= 1) ? 1 : 0) +
            ((((cs ^ (cs >> 4)) & 1) && x >= 1 && y >= 1) ? 1 : 0);
+}
+
+// ---------------------------------------------------------------------------
+// the active-cell mask of a refined grid, one warp per candidate coarse cell:
+// the refined samples of the coarse cell's block of refined cells, one z
+// plane at a time (each sample is RefinedView::at, i.e. refineGrid's value),
+// the cases of the block's cells, and their active bits OR-ed into the row
+// words (cleared beforehand; refined cells of the other coarse cells are
+// inactive, see kCoarseMayCross)
+// ---------------------------------------------------------------------------
+constexpr int kBlockMaskWarps = 8;
+constexpr int kBlockPlaneMax = 512;  // samples of one z plane of a block: (r + 4)^2
+
+__device__ __forceinline__ int blockStart(const RefinedView& g, int m) { return g.pad ? (m == 0 ? 0 : m * (g.r + 1) + 1) : m * (g.r + 1); }
+__device__ __forceinline__ int blockEnd(const RefinedView& g, int m, int n, int cn) {
+    return m == cn - 2 ? n - 1 : blockStart(g, m + 1);
+}
+
+__global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g, float iso, const uint32_t* __restrict__ list,
+                                                                 const unsigned long long* listCount,
+                                                                 uint32_t* __restrict__ mask, int W, uint32_t* status) {
+    __shared__ float planes[kBlockMaskWarps][2][kBlockPlaneMax];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t count = (int64_t)*listCount;
+    const int64_t nc = (int64_t)(g.cX - 1) * (g.cY - 1) * (g.cZ - 1);
+    for (int64_t li = (int64_t)blockIdx.x * kBlockMaskWarps + warp; li < count;
+         li += (int64_t)gridDim.x * kBlockMaskWarps) {
+        const int64_t ci = list[li];
+        if (ci < 0 || ci >= nc) {
+            if (lane == 0) atomicOr(status, kStatusBadIndex);
+            continue;
+        }
+        const int mx = (int)(ci % (g.cX - 1));
+        const int my = (int)((ci / (g.cX - 1)) % (g.cY - 1));
+        const int mz = (int)(ci / ((int64_t)(g.cX - 1) * (g.cY - 1)));
+        const int xs = blockStart(g, mx), xe = blockEnd(g, mx, g.X, g.cX);
+        const int ys = blockStart(g, my), ye = blockEnd(g, my, g.Y, g.cY);
+        const int zs = blockStart(g, mz), ze = blockEnd(g, mz, g.Z, g.cZ);
+        const int ex = xe - xs, ey = ye - ys;
+        const int px = ex + 1, plane = px * (ey + 1);
+        if (plane > kBlockPlaneMax || ex < 1 || ey < 1 || ze <= zs) {
+            if (lane == 0) atomicOr(status, kStatusBadIndex);
+            continue;
+        }
+        float* p0 = planes[warp][0];
+        float* p1 = planes[warp][1];
+        for (int k = lane; k < plane; k += 32) p0[k] = g.at(xs + k % px, ys + k / px, zs);
+        for (int z = zs; z < ze; ++z) {
+            for (int k = lane; k < plane; k += 32) p1[k] = g.at(xs + k % px, ys + k / px, z + 1);
+            __syncwarp();
+            for (int k0 = 0; k0 < ex * ey; k0 += 32) {
+                const int k = k0 + lane;
+                bool active = false;
+                int x = 0, y = 0;
+                if (k < ex * ey) {
+                    const int lx = k % ex, ly = k / ex;
+                    x = xs + lx;
+                    y = ys + ly;
+                    const int o = ly * px + lx;
+                    const float s[8] = {p0[o], p0[o + 1], p0[o + px], p0[o + px + 1],
+                                        p1[o], p1[o + 1], p1[o + px], p1[o + px + 1]};
+                    const int cs = caseOf(s, iso);
+                    active = cs != 0 && cs != 255;
+                }
+                const unsigned act = __ballot_sync(0xffffffffu, active);
+                if (active) {
+                    const int64_t w = ((int64_t)z * (g.Y - 1) + y) * W + (x >> 5);
+                    const unsigned peers = __match_any_sync(act, w);
+                    const unsigned bits = __reduce_or_sync(peers, 1u << (x & 31));
+                    if (lane == __ffs(peers) - 1) atomicOr(&mask[w], bits);
+                }
+            }
+            __syncwarp();
+            float* t = p0;
+            p0 = p1;
+            p1 = t;
+        }
+        __syncwarp();
+    }
+}
+
+void launchBlockMask(const RefinedView& g, float iso, const uint32_t* list, const unsigned long long* listCount,
+                     uint32_t* mask, int W, uint32_t* status, cudaStream_t s) {
+    countLaunch();
+    kBlockMask<<<152 * 6, 32 * kBlockMaskWarps, 0, s>>>(g, iso, list, listCount, mask, W, status);
 }
 
 // Visits the cells of one row and calls f(x, s[8]) once per lane and step

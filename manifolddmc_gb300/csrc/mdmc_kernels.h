@@ -87,6 +87,11 @@ struct SplitWork {
 
 void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int pad, cudaStream_t s);
 void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, cudaStream_t s);
+// also appends the candidate coarse cells to list (count in *listCount)
+void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, uint32_t* list, unsigned long long* listCount,
+                          cudaStream_t s);
+void launchBlockMask(const RefinedView& g, float iso, const uint32_t* list, const unsigned long long* listCount,
+                     uint32_t* mask, int W, uint32_t* status, cudaStream_t s);
 void launchRowCount(const GridDesc& g, float iso, int4* rowCounts, int numRows, cudaStream_t s);
 void launchRowMask(const GridDesc& g, float iso, uint32_t* mask, int numRows, int W, cudaStream_t s);
 void launchWordCounts(const uint32_t* mask, int64_t numWords, int* counts, cudaStream_t s);

@@ -68,6 +68,7 @@ struct DevCounters {
     unsigned long long edges, edges3, edges4, nmVertices;
     unsigned long long quadsNM[5];
     unsigned long long nmBuckets;  // length of the 4-face bucket list
+    unsigned long long candidates; // coarse cells that may cross iso (refined grids)
 };
 
 }  // namespace mdmc
