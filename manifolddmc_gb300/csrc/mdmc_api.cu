@@ -608,7 +608,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, c->cellFirst.ensure(sizeof(int) * (size_t)(numWords + 1)));
     cudaEventRecord(c->kev[2], s);
     if (g.refined && numWords > 0) MDMC_CHECK(c, cudaMemsetAsync(c->cellMask.p, 0, sizeof(uint32_t) * (size_t)numWords, s));
-    if (g.refined && g.ref.mayCross && (g.ref.r + 4) * (g.ref.r + 4) <= 512 && numWords > 0)
+    if (g.refined && g.ref.mayCross && 2 * (g.ref.r + 4) * (g.ref.r + 4) <= 512 && numWords > 0)
         launchBlockMask(g.ref, iso, c->candidates.as<uint32_t>(), &ctr->candidates, c->cellMask.as<uint32_t>(), W, status,
                         s);
     else

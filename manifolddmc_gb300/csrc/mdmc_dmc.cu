@@ -297,18 +297,31 @@ __device__ __forceinline__ int ownedQuads(int cs, int x, int y, int z) {
 // inactive, see kCoarseMayCross)
 // ---------------------------------------------------------------------------
 constexpr int kBlockMaskWarps = 8;
-constexpr int kBlockPlaneMax = 512;  // samples of one z plane of a block: (r + 4)^2
+constexpr int kBlockSamplesMax = 512;  // per warp: a whole block's samples, or two z planes of (r + 4)^2
 
 __device__ __forceinline__ int blockStart(const RefinedView& g, int m) { return g.pad ? (m == 0 ? 0 : m * (g.r + 1) + 1) : m * (g.r + 1); }
 __device__ __forceinline__ int blockEnd(const RefinedView& g, int m, int n, int cn) {
     return m == cn - 2 ? n - 1 : blockStart(g, m + 1);
 }
 
+// ORs the active bit of the lane's cell (x, y, z) into its row word; lanes of
+// the same word combine their bits first
+__device__ __forceinline__ void orActive(uint32_t* mask, int W, int Y, bool active, int x, int y, int z) {
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (active) {
+        const int64_t w = ((int64_t)z * (Y - 1) + y) * W + (x >> 5);
+        const unsigned peers = __match_any_sync(act, w);
+        const unsigned bits = __reduce_or_sync(peers, 1u << (x & 31));
+        if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicOr(&mask[w], bits);
+    }
+}
+
 __global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g, float iso, const uint32_t* __restrict__ list,
                                                                  const unsigned long long* listCount,
                                                                  uint32_t* __restrict__ mask, int W, uint32_t* status) {
-    __shared__ float planes[kBlockMaskWarps][2][kBlockPlaneMax];
+    __shared__ float samples[kBlockMaskWarps][kBlockSamplesMax];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    float* buf = samples[warp];
     const int64_t count = (int64_t)*listCount;
     const int64_t nc = (int64_t)(g.cX - 1) * (g.cY - 1) * (g.cZ - 1);
     for (int64_t li = (int64_t)blockIdx.x * kBlockMaskWarps + warp; li < count;
@@ -324,14 +337,54 @@ __global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g
         const int xs = blockStart(g, mx), xe = blockEnd(g, mx, g.X, g.cX);
         const int ys = blockStart(g, my), ye = blockEnd(g, my, g.Y, g.cY);
         const int zs = blockStart(g, mz), ze = blockEnd(g, mz, g.Z, g.cZ);
-        const int ex = xe - xs, ey = ye - ys;
+        const int ex = xe - xs, ey = ye - ys, ez = ze - zs;
         const int px = ex + 1, plane = px * (ey + 1);
-        if (plane > kBlockPlaneMax || ex < 1 || ey < 1 || ze <= zs) {
+        if (ex < 1 || ey < 1 || ez < 1 || 2 * plane > kBlockSamplesMax) {
             if (lane == 0) atomicOr(status, kStatusBadIndex);
             continue;
         }
-        float* p0 = planes[warp][0];
-        float* p1 = planes[warp][1];
+        if (plane * (ez + 1) <= kBlockSamplesMax) {
+            // every sample of the block at once (loads of four rounds in flight)
+            const int total = plane * (ez + 1);
+            for (int k0 = 0; k0 < total; k0 += 128) {
+                float v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int k = k0 + 32 * u + lane;
+                    const int kk = k < total ? k : 0;
+                    v[u] = g.at(xs + kk % px, ys + (kk % plane) / px, zs + kk / plane);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int k = k0 + 32 * u + lane;
+                    if (k < total) buf[k] = v[u];
+                }
+            }
+            __syncwarp();
+            const int cells = ex * ey * ez;
+            for (int k0 = 0; k0 < cells; k0 += 32) {
+                const int k = k0 + lane;
+                bool active = false;
+                int x = 0, y = 0, z = 0;
+                if (k < cells) {
+                    const int lx = k % ex, ly = (k / ex) % ey, lz = k / (ex * ey);
+                    x = xs + lx;
+                    y = ys + ly;
+                    z = zs + lz;
+                    const int o = lz * plane + ly * px + lx;
+                    const float s[8] = {buf[o],         buf[o + 1],         buf[o + px],         buf[o + px + 1],
+                                        buf[o + plane], buf[o + plane + 1], buf[o + plane + px], buf[o + plane + px + 1]};
+                    const int cs = caseOf(s, iso);
+                    active = cs != 0 && cs != 255;
+                }
+                orActive(mask, W, g.Y, active, x, y, z);
+            }
+            __syncwarp();
+            continue;
+        }
+        // large blocks: two z planes at a time
+        float* p0 = buf;
+        float* p1 = buf + plane;
         for (int k = lane; k < plane; k += 32) p0[k] = g.at(xs + k % px, ys + k / px, zs);
         for (int z = zs; z < ze; ++z) {
             for (int k = lane; k < plane; k += 32) p1[k] = g.at(xs + k % px, ys + k / px, z + 1);
@@ -350,13 +403,7 @@ __global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g
                     const int cs = caseOf(s, iso);
                     active = cs != 0 && cs != 255;
                 }
-                const unsigned act = __ballot_sync(0xffffffffu, active);
-                if (active) {
-                    const int64_t w = ((int64_t)z * (g.Y - 1) + y) * W + (x >> 5);
-                    const unsigned peers = __match_any_sync(act, w);
-                    const unsigned bits = __reduce_or_sync(peers, 1u << (x & 31));
-                    if (lane == __ffs(peers) - 1) atomicOr(&mask[w], bits);
-                }
+                orActive(mask, W, g.Y, active, x, y, z);
             }
             __syncwarp();
             float* t = p0;
@@ -370,7 +417,7 @@ __global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g
 void launchBlockMask(const RefinedView& g, float iso, const uint32_t* list, const unsigned long long* listCount,
                      uint32_t* mask, int W, uint32_t* status, cudaStream_t s) {
     countLaunch();
-    kBlockMask<<<152 * 6, 32 * kBlockMaskWarps, 0, s>>>(g, iso, list, listCount, mask, W, status);
+    kBlockMask<<<152 * 8, 32 * kBlockMaskWarps, 0, s>>>(g, iso, list, listCount, mask, W, status);
 }
 
 // Visits the cells of one row and calls f(x, s[8]) once per lane and step

@@ -105,9 +105,10 @@ RANDOM_CASES = [
     ("noise14_nodetect", lambda: np.random.default_rng(8).random((14, 14, 14), dtype=np.float32), 0.5, 0, False,
      {"detect_non_manifold_vertices": 0}),
     ("noise12x17x9", lambda: np.random.default_rng(9).random((9, 17, 12), dtype=np.float32), 0.5, 0, False, {}),
-    # large refinement factors: coarse blocks of 19^3 (+ padding) refined cells,
-    # and beyond the block pass's plane size (the row walk takes over)
-    ("blobs6_refine18_pad", lambda: blobs(6, 3, 13, (1.0, 2.0)), 0.45, 18, True, {}),
+    # large refinement factors: coarse blocks of 13^3 (+ padding) refined cells
+    # (evaluated two planes at a time), and beyond the block pass's plane size
+    # (the row walk takes over)
+    ("blobs7_refine12_pad", lambda: blobs(7, 3, 13, (1.0, 2.0)), 0.45, 12, True, {}),
     ("blobs7_refine19", lambda: blobs(7, 3, 12, (1.0, 2.5)), 0.4, 19, False, {}),
 ]
 
