@@ -100,7 +100,7 @@ struct mdmc_context {
     size_t vO2CCount = 0, hO2CCount = 0, fO2CCount = 0;
     DevBuf appV, appH, appF;
     // fan detection
-    DevBuf isKey, fans;
+    DevBuf isKey, fans, degree, slowFan;
     // events: start, dmc, halfedge, repair, detect, end
     cudaEvent_t ev[6] = {};
     // per-kernel events: refine, count, emit, quads, table, vertices (begin/end each)
@@ -702,22 +702,25 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     cudaEventRecord(c->ev[3], s);
 
     // ---- non-manifold vertices ------------------------------------------------
+    MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
+    const MeshDims mdF{(int)c->V, (int)c->F, (int)c->H};
     if (c->opt.detect_non_manifold_vertices) {
-        MDMC_CHECK(c, c->isKey.ensure((size_t)c->H));
-        MDMC_CHECK(c, c->fans.ensure(sizeof(int) * (size_t)c->V));
+        MDMC_CHECK(c, c->isKey.ensure((size_t)std::max<int64_t>(c->H, 1)));
+        MDMC_CHECK(c, c->fans.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
+        MDMC_CHECK(c, c->degree.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
+        MDMC_CHECK(c, c->slowFan.ensure((size_t)std::max<int64_t>(c->V, 1)));
         MDMC_CHECK(c, cudaMemsetAsync(c->isKey.p, 0, (size_t)c->H, s));
-        MDMC_CHECK(c, cudaMemsetAsync(c->fans.p, 0, sizeof(int) * (size_t)c->V, s));
-        launchDetectFans(c->he.as<int4>(), MeshDims{(int)c->V, (int)c->F, (int)c->H}, c->isKey.as<uint8_t>(),
-                         c->fans.as<int>(), c->vflags.as<uint8_t>(), ctr, status, s);
+        launchVertexStar(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), s);
+        launchDetectFans(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), c->slowFan.as<uint8_t>(),
+                         c->isKey.as<uint8_t>(), c->fans.as<int>(), c->vflags.as<uint8_t>(), ctr, status, s);
     }
     cudaEventRecord(c->ev[4], s);
 
     // ---- outputs and statistics -------------------------------------------------
-    MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)c->F));
-    MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)c->V));
-    launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), MeshDims{(int)c->V, (int)c->F, (int)c->H},
-                 c->tableValid ? c->table.as<Bucket>() : nullptr, c->cap, c->heValence.as<uint8_t>(),
-                 c->quads.as<int4>(), c->vertexHE.as<int>(), ctr, status, s);
+    MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)std::max<int64_t>(c->F, 1)));
+    launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), mdF, c->tableValid ? c->table.as<Bucket>() : nullptr, c->cap,
+                 c->heValence.as<uint8_t>(), c->quads.as<int4>(), c->vertexHE.as<int>(),
+                 c->opt.detect_non_manifold_vertices != 0, ctr, status, s);
     cudaEventRecord(c->ev[5], s);
     MDMC_CHECK(c, cudaGetLastError());
     MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));

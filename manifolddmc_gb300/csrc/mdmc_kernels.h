@@ -115,10 +115,13 @@ void launchInsertFaces(const int4* he, const int* faceFirst, MeshDims md, Bucket
 void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s);
 void launchReconnect(const GridDesc& g, float iso, const int4* nmList, const DevCounters* ctr,
                      int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s);
-void launchDetectFans(const int4* he, MeshDims md, uint8_t* isKey, int* fans, uint8_t* vflags, DevCounters* ctr,
+void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cudaStream_t s);
+void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, uint8_t* slow, uint8_t* isKey,
+                      int* fans, uint8_t* vflags, DevCounters* ctr,
                       uint32_t* status, cudaStream_t s);
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const Bucket* table, unsigned long long cap,
-                  const uint8_t* heValence, int4* quads, int* vertexHE, DevCounters* ctr, uint32_t* status, cudaStream_t s);
+                  const uint8_t* heValence, int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr,
+                  uint32_t* status, cudaStream_t s);
 
 void launchFlagNMFaces(const uint16_t* attr, int numFaces, int* flags, cudaStream_t s);
 void launchCompactNMFaces(const int* flags, const int* offsets, int numFaces, int* nmFaces, cudaStream_t s);

@@ -326,25 +326,87 @@ __device__ __forceinline__ int fanWalk(const int4* he, int start, bool cw, int H
     return result;
 }
 
+// The smallest outgoing halfedge (0x7F7F7F7F: none yet) and the number of
+// outgoing halfedges of every vertex.
+__global__ void kVertexStar(const int4* __restrict__ he, MeshDims md, int* __restrict__ vertexHE, int* __restrict__ deg) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h < md.H) {
+        const int v = he[h].x;
+        if (inb(v, md.V)) {
+            atomicMin(&vertexHE[v], h);
+            if (deg) atomicAdd(&deg[v], 1);
+        }
+    }
+}
+
+// One walk per vertex.  When the clockwise walk from the vertex's smallest
+// outgoing halfedge returns to it after visiting exactly all of the vertex's
+// outgoing halfedges, every step through a symmetric twin pair (and faces are
+// 4-cycles), the counter-clockwise step is the inverse of the clockwise one
+// on that cycle: every outgoing halfedge's own walks cover the same cycle,
+// its key is the cycle's smallest id, and the vertex has one fan with no
+// limit hit.  Every other vertex (boundary, non-manifold or asymmetric twins)
+// takes the per-halfedge walks.  Also turns "no outgoing halfedge" into -1.
+__global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restrict__ vertexHE,
+                         const int* __restrict__ deg, int* __restrict__ fans, uint8_t* __restrict__ slow) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= md.V) return;
+    const int d = deg[v];
+    if (d == 0) {
+        vertexHE[v] = -1;
+        fans[v] = 0;
+        slow[v] = 0;
+        return;
+    }
+    const int start = vertexHE[v];
+    bool ok = inb(start, md.H) && d <= 1024;
+    int x = start, steps = 0;
+    while (ok) {
+        const int4 hx = he[x];
+        if (hx.x != v || !inb(hx.w, md.H)) {
+            ok = false;
+            break;
+        }
+        const int4 ht = he[hx.w];
+        if (ht.w != x || !inb(ht.z, md.H)) {
+            ok = false;
+            break;
+        }
+        x = ht.z;
+        if (++steps > d) ok = false;
+        if (x == start) break;
+    }
+    ok = ok && steps == d;
+    fans[v] = ok ? 1 : 0;
+    slow[v] = ok ? 0 : 1;
+}
+
 // A fan key is the smallest halfedge id of the fan and has the origin of the
 // halfedge it was found from, so "distinct (origin, key) pairs per origin"
 // (the reference's sort + unique) equals "halfedges named as key by some
-// halfedge, per origin".  No sort is needed.
-__global__ void kFanKeys(const int4* __restrict__ he, MeshDims md, uint8_t* __restrict__ isKey, uint32_t* status) {
+// halfedge, per origin".  No sort is needed.  Only the halfedges of vertices
+// the single walk did not settle.
+__global__ void kFanKeys(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ slow,
+                         uint8_t* __restrict__ isKey, uint32_t* status) {
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= md.H) return;
+    const int v = he[h].x;
+    if (!inb(v, md.V) || !slow[v]) return;
     const int k = min(h, min(fanWalk(he, h, true, md.H, status), fanWalk(he, h, false, md.H, status)));
     isKey[k] = 1;
 }
 
-__global__ void kFanCount(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ isKey,
-                          int* __restrict__ fans, uint32_t* status) {
+__global__ void kFanCount(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ slow,
+                          const uint8_t* __restrict__ isKey, int* __restrict__ fans, uint32_t* status) {
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
     if (h >= md.H) return;
     if (isKey[h]) {
         const int v = he[h].x;
-        if (inb(v, md.V)) atomicAdd(&fans[v], 1);
-        else atomicOr(status, kStatusBadIndex);
+        if (inb(v, md.V)) {
+            if (slow[v]) atomicAdd(&fans[v], 1);
+        } else {
+            atomicOr(status, kStatusBadIndex);
+        }
     }
 }
 
@@ -364,13 +426,28 @@ __global__ void kFanFlags(const int* __restrict__ fans, uint8_t* __restrict__ vf
     blockAddTo(&ctr->nmVertices, nm);
 }
 
-void launchDetectFans(const int4* he, MeshDims md, uint8_t* isKey, int* fans, uint8_t* vflags, DevCounters* ctr,
-                      uint32_t* status, cudaStream_t s) {
+void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cudaStream_t s) {
+    if (md.V <= 0) return;
+    // 0x7F7F7F7F marks "none"; atomicMin lowers it
+    cudaMemsetAsync(vertexHE, 0x7F, sizeof(int) * (size_t)md.V, s);
+    if (deg) cudaMemsetAsync(deg, 0, sizeof(int) * (size_t)md.V, s);
     if (md.H > 0) {
         countLaunch();
-        kFanKeys<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, isKey, status);
+        kVertexStar<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, vertexHE, deg);
+    }
+}
+
+void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, uint8_t* slow, uint8_t* isKey,
+                      int* fans, uint8_t* vflags, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
+    if (md.V > 0) {
         countLaunch();
-        kFanCount<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, isKey, fans, status);
+        kFanFast<<<(md.V + 255) / 256, 256, 0, s>>>(he, md, vertexHE, deg, fans, slow);
+    }
+    if (md.H > 0) {
+        countLaunch();
+        kFanKeys<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, slow, isKey, status);
+        countLaunch();
+        kFanCount<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, slow, isKey, fans, status);
     }
     if (md.V > 0) {
         countLaunch();
@@ -412,33 +489,21 @@ __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__
     for (int k = 1; k <= 4; ++k) blockAddTo(&ctr->quadsNM[k], cnt == k ? 1 : 0);
 }
 
-__global__ void kVertexHalfedge(const int4* __restrict__ he, MeshDims md, int* __restrict__ vertexHE) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h < md.H) {
-        const int v = he[h].x;
-        if (inb(v, md.V)) atomicMin(&vertexHE[v], h);
-    }
-}
-
 __global__ void kVertexHalfedgeFix(int* vertexHE, int numVertices) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v < numVertices && vertexHE[v] == 0x7F7F7F7F) vertexHE[v] = -1;
 }
 
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const Bucket* table, unsigned long long cap,
-                  const uint8_t* heValence, int4* quads, int* vertexHE, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
+                  const uint8_t* heValence, int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr,
+                  uint32_t* status, cudaStream_t s) {
     (void)status;
     if (md.F > 0) {
         countLaunch();
         kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, table, cap, heValence, quads, ctr);
     }
-    if (md.V > 0) {
-        // 0x7F7F7F7F marks "none"; atomicMin lowers it
-        cudaMemsetAsync(vertexHE, 0x7F, sizeof(int) * (size_t)md.V, s);
-        if (md.H > 0) {
-            countLaunch();
-            kVertexHalfedge<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, vertexHE);
-        }
+    if (md.V > 0 && !vertexHEDone) {
+        launchVertexStar(he, md, vertexHE, nullptr, s);
         countLaunch();
         kVertexHalfedgeFix<<<(md.V + 255) / 256, 256, 0, s>>>(vertexHE, md.V);
     }
