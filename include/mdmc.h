@@ -204,6 +204,22 @@ MDMC_API mdmc_status mdmc_download_mesh(mdmc_context* context, float* positions,
  * (Mesh.cu:446-510): v, vn, then one "f a//a b//b c//c d//d" line per face. */
 MDMC_API mdmc_status mdmc_write_obj(mdmc_context* context, const char* path);
 
+/* Adjoint of the last mdmc_run on the context (no counterpart in the
+ * reference, which is not differentiable).  Given dL/dpositions (device, 3
+ * floats per vertex of the last mesh), writes dL/dsamples for the grid samples
+ * the run read: the coarse input for a refined or padded grid, the dense grid
+ * otherwise (device, one float per sample; added to the buffer's contents when
+ * accumulate != 0, else the buffer is overwritten).  The topology is held
+ * fixed; a DMC vertex is origin + (cell + mean of its edge points) * spacing,
+ * so the run must have had enable_surface_to_vertex_iteration = 0 (else
+ * MDMC_ERROR_INVALID_ARGUMENT).  Vertices appended by the non-manifold split
+ * pass their gradient to the DMC vertex they descend from (vertex copies: the
+ * copied vertex; subdivision vertices: the face corner they are nearest).
+ * The grid's sample buffers must still hold the run's input.  Sums use float
+ * atomics, so the last bits can differ from call to call. */
+MDMC_API mdmc_status mdmc_backward(mdmc_context* context, const float* dl_dpositions, float* dl_dsamples,
+                                   int accumulate, void* stream);
+
 /* Human-readable description of the context's last error ("" if none). */
 MDMC_API const char* mdmc_last_error(const mdmc_context* context);
 

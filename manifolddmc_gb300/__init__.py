@@ -125,6 +125,7 @@ def library():
             "mdmc_write_obj": (ctypes.c_int, [P, ctypes.c_char_p]),
             "mdmc_last_error": (ctypes.c_char_p, [P]),
             "mdmc_case_tables": (None, [P, P]),
+            "mdmc_backward": (ctypes.c_int, [P, P, P, ctypes.c_int, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -136,6 +137,23 @@ def library():
 
 def _ptr(a):
     return a.ctypes.data_as(P) if a is not None else None
+
+
+def _dev_ptr(a):
+    """Device address of a CUDA tensor, an integer, or None."""
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return int(a)
+
+
+class _DeviceArray:
+    """A view of library-owned device memory for torch.as_tensor (CUDA array interface)."""
+
+    def __init__(self, ptr, shape, typestr):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(ptr or 0), False),
+                                         "version": 2, "strides": None}
 
 
 def _stream_handle(stream):
@@ -266,6 +284,7 @@ class DualMarchingCubes:
         self._ctx = _Context(self.options)
         self.stats = Stats()
         self.mesh = Mesh()
+        self._run_id = 0
 
     # flags (DualMarchingCubes.h:167-185, defaults DualMarchingCubes.cu:110-133)
     def _set(self, name, value):
@@ -284,6 +303,7 @@ class DualMarchingCubes:
         per-stage GPU times in milliseconds (the reference returns its
         Performance tree)."""
         g = grid.grid if isinstance(grid, UniformGrid) else grid
+        self._run_id += 1
         self._ctx.check(self._ctx.lib.mdmc_run(self._ctx.handle, ctypes.byref(g), ctypes.c_float(iso_value),
                                                ctypes.byref(self.mesh), ctypes.byref(self.stats),
                                                _stream_handle(stream)))
@@ -327,6 +347,34 @@ class DualMarchingCubes:
             _ptr(out.face_first_halfedge), _ptr(out.face_attributes), _ptr(out.vertex_halfedge),
             _ptr(out.vertex_flags), None))
         return out
+
+    def device_arrays(self):
+        """The last run's mesh as CUDA torch tensors viewing the library's
+        buffers (valid until the next run on this object)."""
+        import torch
+        m = self.mesh
+        V, F, H = int(m.num_vertices), int(m.num_faces), int(m.num_halfedges)
+        views = {"positions": (m.positions, (V, 3), "<f4"), "normals": (m.normals, (V, 3), "<f4"),
+                 "quads": (m.quads, (F, 4), "<i4"), "halfedges": (m.halfedges, (H, 4), "<i4"),
+                 "face_first_halfedge": (m.face_first_halfedge, (F,), "<i4"),
+                 "vertex_halfedge": (m.vertex_halfedge, (V,), "<i4"), "vertex_flags": (m.vertex_flags, (V,), "|u1")}
+        out = {}
+        for k, (ptr, shape, ts) in views.items():
+            addr = int(ptr) if ptr else 0
+            if not addr or 0 in shape:
+                out[k] = torch.empty(shape, dtype={"<f4": torch.float32, "<i4": torch.int32, "|u1": torch.uint8}[ts],
+                                     device="cuda")
+            else:
+                out[k] = torch.as_tensor(_DeviceArray(addr, shape, ts), device="cuda")
+        return out
+
+    def backward(self, dl_dpositions, dl_dsamples, accumulate=False, stream=None):
+        """Adjoint of the last run (no counterpart in the reference): writes
+        dL/dsamples of the grid the run read (the coarse input of a refined
+        grid) from dL/dpositions (3 floats per vertex), topology held fixed.
+        Needs a run with enable_surface_to_vertex_iteration = 0."""
+        self._ctx.check(self._ctx.lib.mdmc_backward(self._ctx.handle, _dev_ptr(dl_dpositions), _dev_ptr(dl_dsamples),
+                                                    int(bool(accumulate)), _stream_handle(stream)))
 
     def write_obj(self, path):
         """Mesh::writeToFile, Mesh.cu:446-510"""

@@ -81,6 +81,13 @@ struct mdmc_context {
     // mesh
     DevBuf pos, nrm, he, faceFirst, faceAttr, vflags, vertexHE, quads;
     int64_t V = 0, F = 0, H = 0;
+    // differentiable path: the last run's grid, iso, DMC vertex and active-cell
+    // counts, and the parents of the vertices the splitter appended
+    mdmc_grid lastGrid{};
+    float lastIso = 0.f;
+    int lastSurfaceIteration = 1;
+    int64_t dmcV = 0, activeCells = 0;
+    DevBuf appParent, vertexGrad;
     // edge table
     DevBuf table, nmList, heValence;
     // quad -> owner cell; per-row active-cell mask (32 cells per word) and the
@@ -176,7 +183,8 @@ unsigned long long tableCapacity(int64_t faces) { return (unsigned long long)rou
 
 // the view of a grid the kernels read; refined grids get their coarse-cell
 // pre-pass for this iso-value (mayCross bits in the context)
-mdmc_status makeGridDesc(mdmc_context* c, const mdmc_grid* grid, float iso, GridDesc& d, cudaStream_t s) {
+mdmc_status makeGridDesc(mdmc_context* c, const mdmc_grid* grid, float iso, GridDesc& d, cudaStream_t s,
+                         bool prepass = true) {
     GridGeom geom;
     geom.X = grid->dims[0];
     geom.Y = grid->dims[1];
@@ -215,7 +223,7 @@ mdmc_status makeGridDesc(mdmc_context* c, const mdmc_grid* grid, float iso, Grid
             (int64_t)cd + (int64_t)(cd - 1) * grid->refinement + 2 * pad != grid->dims[a])
             return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "coarse dims do not match the refined dims");
     }
-    if (d.ref.cX >= 2 && d.ref.cY >= 2 && d.ref.cZ >= 2) {
+    if (prepass && d.ref.cX >= 2 && d.ref.cY >= 2 && d.ref.cZ >= 2) {
         const int64_t cells = (int64_t)(d.ref.cX - 1) * (d.ref.cY - 1) * (d.ref.cZ - 1);
         MDMC_CHECK(c, c->mayCross.ensure(sizeof(uint32_t) * (size_t)((cells + 31) / 32 + 1)));
         MDMC_CHECK(c, c->candidates.ensure(sizeof(uint32_t) * (size_t)cells));
@@ -248,6 +256,8 @@ SplitWork splitWork(mdmc_context* c, int nv, int nh, int nf) {
     w.hO2C = c->hO2C.as<int>();
     w.fO2C = c->fO2C.as<int>();
     w.origV = c->wOrigV.as<int>();
+    w.appParent = c->appParent.as<int>();
+    w.dmcV = (int)c->dmcV;
     w.origH = c->wOrigH.as<int>();
     w.he = c->wHe.as<int4>();
     w.first = c->wFirst.as<int>();
@@ -336,7 +346,7 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         MDMC_CHECK(c, c->wVC2O.ensure(sizeof(int) * (size_t)nv));
         MDMC_CHECK(c, c->wHC2O.ensure(sizeof(int) * (size_t)nh));
         MDMC_CHECK(c, c->wFC2O.ensure(sizeof(int) * (size_t)nf));
-        MDMC_CHECK(c, c->wOrigV.ensure(sizeof(int) * 4 * (size_t)n));
+        MDMC_CHECK(c, c->wOrigV.ensure(sizeof(int) * (size_t)nv));
         MDMC_CHECK(c, c->wOrigH.ensure(sizeof(int) * 4 * (size_t)n));
         MDMC_CHECK(c, c->wHe.ensure(sizeof(int4) * (size_t)nh));
         MDMC_CHECK(c, c->wFirst.ensure(sizeof(int) * (size_t)nf));
@@ -347,6 +357,7 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         MDMC_CHECK(c, c->wHSlots.ensure(sizeof(int) * 4 * (size_t)nh));
         if ((st = ensureMaps(c, s)) != MDMC_OK) return st;
         MDMC_CHECK(c, cudaMemsetAsync(c->wVfl.p, 0, sizeof(uint32_t) * (size_t)nv, s));
+        MDMC_CHECK(c, cudaMemsetAsync(c->wOrigV.p, 0xFF, sizeof(int) * (size_t)nv, s));
         MDMC_CHECK(c, cudaMemsetAsync(c->wHfl.p, 0, sizeof(uint32_t) * (size_t)nh, s));
         MDMC_CHECK(c, cudaMemsetAsync(c->wFfl.p, 0, sizeof(uint32_t) * (size_t)nf, s));
         MDMC_CHECK(c, cudaMemsetAsync(c->wVC2O.p, 0xFF, sizeof(int) * (size_t)nv, s));
@@ -394,10 +405,14 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         MDMC_CHECK(c, c->pos.grow(sizeof(float) * 3 * (size_t)V2, sizeof(float) * 3 * (size_t)c->V, s));
         MDMC_CHECK(c, c->nrm.grow(sizeof(float) * 3 * (size_t)V2, sizeof(float) * 3 * (size_t)c->V, s));
         MDMC_CHECK(c, c->vflags.grow(roundUp((size_t)V2, 4), (size_t)c->V, s));
+        MDMC_CHECK(c, c->appParent.grow(sizeof(int) * (size_t)std::max<int64_t>(V2 - c->dmcV, 1),
+                                        sizeof(int) * (size_t)(c->V - c->dmcV), s));
+        SplitWork wb = w;
+        wb.appParent = c->appParent.as<int>();
         MDMC_CHECK(c, c->he.grow(sizeof(int4) * (size_t)H2, sizeof(int4) * (size_t)c->H, s));
         MDMC_CHECK(c, c->faceFirst.grow(sizeof(int) * (size_t)F2, sizeof(int) * (size_t)c->F, s));
         MDMC_CHECK(c, c->faceAttr.grow(roundUp(sizeof(uint16_t) * (size_t)F2, 4), sizeof(uint16_t) * (size_t)c->F, s));
-        launchSplitCopyBack(w, c->appV.as<int>(), c->appH.as<int>(), c->appF.as<int>(), (int)V2, (int)H2, (int)F2,
+        launchSplitCopyBack(wb, c->appV.as<int>(), c->appH.as<int>(), c->appF.as<int>(), (int)V2, (int)H2, (int)F2,
                             c->pos.as<float>(), c->nrm.as<float>(), c->he.as<int4>(), c->faceFirst.as<int>(),
                             c->faceAttr.as<uint16_t>(), status, s);
         launchSplitResetMaps(n, c->nmFaces.as<int>(), w, s);
@@ -586,6 +601,10 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     if ((uint64_t)X * Y * Z >= 0xFFFFFFFFull) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "grid has 2^32 samples or more");
     cudaStream_t s = (cudaStream_t)stream;
     c->haveMesh = false;
+    c->lastGrid = *grid;
+    c->lastIso = iso;
+    c->lastSurfaceIteration = c->opt.enable_surface_to_vertex_iteration;
+    c->dmcV = c->activeCells = 0;
     std::memset(&c->stats, 0, sizeof c->stats);
     DevCounters* ctr = c->counters.as<DevCounters>();
     uint32_t* status = &ctr->status;
@@ -657,6 +676,8 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->V = Vd;
     c->F = Q;
     c->H = 4 * Q;
+    c->dmcV = Vd;
+    c->activeCells = A;
     c->tableValid = false;
     MDMC_CHECK(c, c->quadOwner.ensure(sizeof(int) * (size_t)std::max<int64_t>(Q, 1)));
     MDMC_CHECK(c, c->pos.ensure(sizeof(float) * 3 * (size_t)Vd));
@@ -806,6 +827,36 @@ mdmc_status mdmc_download_mesh(mdmc_context* c, float* positions, float* normals
     MDMC_CHECK(c, cp(vertex_halfedge, c->vertexHE, sizeof(int) * (size_t)c->V));
     MDMC_CHECK(c, cp(vertex_flags, c->vflags, (size_t)c->V));
     MDMC_CHECK(c, cudaStreamSynchronize(s));
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_backward(mdmc_context* c, const float* dl_dpositions, float* dl_dsamples, int accumulate,
+                          void* stream) {
+    if (!c || !dl_dsamples || (!dl_dpositions && c->V > 0)) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "null argument");
+    c->err.clear();
+    (void)cudaGetLastError();
+    if (!c->haveMesh) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "no forward run to differentiate");
+    if (c->lastSurfaceIteration)
+        return fail(c, MDMC_ERROR_INVALID_ARGUMENT,
+                    "the adjoint needs a forward run with enable_surface_to_vertex_iteration = 0");
+    cudaStream_t s = (cudaStream_t)stream;
+    const mdmc_grid& grid = c->lastGrid;
+    GridDesc g;
+    mdmc_status st = makeGridDesc(c, &grid, c->lastIso, g, s, false);
+    if (st != MDMC_OK) return st;
+    const int64_t outCount = g.refined ? (int64_t)grid.coarse_dims[0] * grid.coarse_dims[1] * grid.coarse_dims[2]
+                                       : (int64_t)grid.dims[0] * grid.dims[1] * grid.dims[2];
+    if (!accumulate) MDMC_CHECK(c, cudaMemsetAsync(dl_dsamples, 0, sizeof(float) * (size_t)outCount, s));
+    if (c->dmcV == 0) return MDMC_OK;
+    MDMC_CHECK(c, c->vertexGrad.ensure(sizeof(float) * 3 * (size_t)c->dmcV));
+    MDMC_CHECK(c, cudaMemcpyAsync(c->vertexGrad.p, dl_dpositions, sizeof(float) * 3 * (size_t)c->dmcV,
+                                  cudaMemcpyDeviceToDevice, s));
+    launchGatherParents(dl_dpositions, (int)c->V, (int)c->dmcV, c->appParent.as<int>(), c->vertexGrad.as<float>(), s);
+    DevCounters* ctr = c->counters.as<DevCounters>();
+    MDMC_CHECK(c, cudaMemsetAsync(&ctr->status, 0, sizeof(uint32_t), s));
+    launchBackwardCells(g, c->lastIso, c->act.as<ActiveCell>(), (int)c->activeCells, c->vertexGrad.as<float>(),
+                        (int)c->dmcV, dl_dsamples, &ctr->status, s);
+    MDMC_CHECK(c, cudaGetLastError());
     return MDMC_OK;
 }
 

@@ -83,6 +83,9 @@ struct SplitWork {
     // sizes: copies (nv, nh, nf) and the mesh (V, H, F)
     int nv, nh, nf;
     int V, H, F;
+    // DMC vertex each appended mesh vertex descends from (index o - dmcV)
+    int* appParent;
+    int dmcV;
 };
 
 void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int pad, cudaStream_t s);
@@ -122,6 +125,12 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const Bucket* table, unsigned long long cap,
                   const uint8_t* heValence, int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr,
                   uint32_t* status, cudaStream_t s);
+
+// adjoint of the vertex positions (surface iteration off)
+void launchGatherParents(const float* dlDpos, int numVertices, int dmcVertices, const int* appParent, float* vertexGrad,
+                         cudaStream_t s);
+void launchBackwardCells(const GridDesc& g, float iso, const ActiveCell* act, int numActive, const float* vertexGrad,
+                         int dmcVertices, float* dlDsamples, uint32_t* status, cudaStream_t s);
 
 void launchFlagNMFaces(const uint16_t* attr, int numFaces, int* flags, cudaStream_t s);
 void launchCompactNMFaces(const int* flags, const int* offsets, int numFaces, int* nmFaces, cudaStream_t s);

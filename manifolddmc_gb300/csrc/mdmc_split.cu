@@ -162,6 +162,7 @@ __global__ void kSubdivide(int n, SplitWork w, uint32_t* status) {
         const F3 pp = mix(mix(P[0], P[1], u), mix(P[3], P[2], u), v);
         const F3 nn = mix(mix(N[0], N[1], u), mix(N[3], N[2], u), v);
         const int c = 4 * n + 4 * k + i;
+        w.origV[c] = w.vC2O[vid[i]];  // the differentiable path's parent: corner i
         w.pos[3 * c] = pp.x; w.pos[3 * c + 1] = pp.y; w.pos[3 * c + 2] = pp.z;
         w.nrm[3 * c] = nn.x; w.nrm[3 * c + 1] = nn.y; w.nrm[3 * c + 2] = nn.z;
         inner[i] = c;
@@ -430,6 +431,10 @@ __global__ void kCopyBackVertices(SplitWork w, const int* __restrict__ app, int 
     if (o == kNone) {
         o = w.V + app[v];
         w.vC2O[v] = o;
+        // the DMC vertex it descends from (parents of earlier appends resolved)
+        const int p = w.origV[v];
+        const int parent = !inb(p, w.V) ? -1 : (p < w.dmcV ? p : w.appParent[p - w.dmcV]);
+        if (inb(o - w.dmcV, V2 - w.dmcV)) w.appParent[o - w.dmcV] = parent;
     }
     if (!inb(o, V2)) {
         atomicOr(status, kStatusBadIndex);

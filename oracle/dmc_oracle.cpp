@@ -381,6 +381,11 @@ struct Result {
     std::vector<float> dmcPos, dmcNrm;
     std::vector<int> dmcQuads;
     std::vector<uint16_t> dmcAttr;
+    // per DMC vertex: its cell (3 ints) and the cell edges of its contour (12-bit mask)
+    std::vector<int> dmcCell;
+    std::vector<uint16_t> dmcEdges;
+    // per final vertex: the DMC vertex it descends from (-1: none)
+    std::vector<int> parent;
     // final mesh
     std::vector<float> pos, nrm;  // 3 per vertex
     std::vector<HE> he;
@@ -418,6 +423,7 @@ struct Mesh {
     std::vector<int> faceFirst;
     std::vector<uint16_t> faceAttr;
     std::vector<uint8_t> vflags;
+    std::vector<int> parent;  // DMC vertex each vertex descends from
     EdgeTable table;
     uint32_t anomalies = 0;
 
@@ -513,7 +519,7 @@ struct QuadEntry {
 
 static void runDMC(const Grid& g, float iso, bool surfaceIteration, std::vector<float>& pos,
                    std::vector<float>& nrm, std::vector<int>& quads, std::vector<uint16_t>& attr,
-                   uint32_t& anomalies) {
+                   std::vector<int>& cells, std::vector<uint16_t>& edgeMasks, uint32_t& anomalies) {
     const int X = g.d[0], Y = g.d[1], Z = g.d[2];
     std::unordered_map<uint64_t, QuadEntry> table;
     V3 origin = g.o(), dl = g.dl();
@@ -554,6 +560,10 @@ static void runDMC(const Grid& g, float iso, bool surfaceIteration, std::vector<
                     int vid = (int)(pos.size() / 3);
                     pos.push_back(wp.x); pos.push_back(wp.y); pos.push_back(wp.z);
                     nrm.push_back(nm.x); nrm.push_back(nm.y); nrm.push_back(nm.z);
+                    cells.push_back(x); cells.push_back(y); cells.push_back(z);
+                    uint16_t mask = 0;
+                    for (int i = 0; i < sz; ++i) mask |= (uint16_t)(1u << contourEdge(c, t, i));
+                    edgeMasks.push_back(mask);
                     for (int i = 0; i < sz; ++i) {
                         int e = contourEdge(c, t, i);
                         int a0 = kEdgeV0[e];
@@ -781,6 +791,7 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
         std::vector<float> cpos(3 * (size_t)nv, 0.f), cnrm(3 * (size_t)nv, 0.f);
         std::vector<uint8_t> vfl(nv, 0), hfl(nh, 0), ffl(nf, 0);
         std::vector<int> vC2O(nv, -1), hC2O(nh, -1), fC2O(nf, -1);
+        std::vector<int> cparent(nv, -1);  // mesh vertex each working vertex comes from
         std::vector<int> vO2C(V, -1), hO2C(H, -1), fO2C(F, -1);
         std::vector<HE> ch(nh, HE{-1, -1, -1, -1});
         std::vector<int> cfirst(nf, -1);
@@ -794,6 +805,7 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
                 int v = m.he[h].origin, c = 4 * k + i;
                 for (int a = 0; a < 3; ++a) { cpos[3 * c + a] = m.pos[3 * v + a]; cnrm[3 * c + a] = m.nrm[3 * v + a]; }
                 vC2O[c] = v;
+                cparent[c] = v;
                 if (vO2C[v] == -1) vO2C[v] = c;
                 h = m.he[h].next;
             }
@@ -858,6 +870,7 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
                     V3 pa = mix(P[0], P[1], u), pb = mix(P[3], P[2], u), pp = mix(pa, pb, v);
                     V3 na = mix(N[0], N[1], u), nb = mix(N[3], N[2], u), nn = mix(na, nb, v);
                     int c = 4 * n + 4 * k + i;
+                    cparent[c] = vC2O[vid[i]];  // inner vertex i comes from corner i
                     cpos[3 * c] = pp.x; cpos[3 * c + 1] = pp.y; cpos[3 * c + 2] = pp.z;
                     cnrm[3 * c] = nn.x; cnrm[3 * c + 1] = nn.y; cnrm[3 * c + 2] = nn.z;
                     inner[i] = c;
@@ -1021,6 +1034,7 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
                     o = m.numV();
                     for (int a = 0; a < 3; ++a) { m.pos.push_back(cpos[3 * v + a]); m.nrm.push_back(cnrm[3 * v + a]); }
                     m.vflags.push_back(0);
+                    m.parent.push_back(cparent[v] >= 0 && cparent[v] < V ? m.parent[cparent[v]] : -1);
                     vC2O[v] = o;
                 } else {
                     for (int a = 0; a < 3; ++a) { m.pos[3 * o + a] = cpos[3 * v + a]; m.nrm[3 * o + a] = cnrm[3 * v + a]; }
@@ -1125,11 +1139,14 @@ static Result* run(const Grid& g, float iso, const mdmc_oracle_options& opt) {
     Result* r = new Result();
     std::memset(r->stats, 0, sizeof r->stats);
     uint32_t anomalies = 0;
-    runDMC(g, iso, opt.surface_iteration != 0, r->dmcPos, r->dmcNrm, r->dmcQuads, r->dmcAttr, anomalies);
+    runDMC(g, iso, opt.surface_iteration != 0, r->dmcPos, r->dmcNrm, r->dmcQuads, r->dmcAttr, r->dmcCell,
+           r->dmcEdges, anomalies);
 
     Mesh m;
     m.pos = r->dmcPos;
     m.nrm = r->dmcNrm;
+    m.parent.resize(m.numV());
+    for (int v = 0; v < m.numV(); ++v) m.parent[v] = v;
     const int Q = (int)r->dmcAttr.size();
     if (m.numV() > 0) {
         // HalfedgeMesh::initialize, D/Halfedges/HalfedgeMesh.cu:14-60, :848-857
@@ -1187,6 +1204,7 @@ static Result* run(const Grid& g, float iso, const mdmc_oracle_options& opt) {
     for (int k = 1; k <= 4; ++k) r->stats[MDMC_ORC_STAT_QUADS_NM1 + k - 1] = qk[k];
     r->stats[MDMC_ORC_STAT_ANOMALIES] = anomalies;
 
+    r->parent = std::move(m.parent);
     r->pos = std::move(m.pos);
     r->nrm = std::move(m.nrm);
     r->he = std::move(m.he);
@@ -1291,6 +1309,142 @@ void mdmc_oracle_get_dmc(const void* res, float* positions, float* normals, int*
 }
 
 void mdmc_oracle_free(void* res) { delete (oracle::Result*)res; }
+
+void mdmc_oracle_get_topology(const void* res, int* cells, uint16_t* edges, int* parents) {
+    const oracle::Result* r = (const oracle::Result*)res;
+    if (cells) std::memcpy(cells, r->dmcCell.data(), r->dmcCell.size() * sizeof(int));
+    if (edges) std::memcpy(edges, r->dmcEdges.data(), r->dmcEdges.size() * sizeof(uint16_t));
+    if (parents) {
+        const size_t V = r->pos.size() / 3;
+        for (size_t v = 0; v < V; ++v) parents[v] = v < r->parent.size() ? r->parent[v] : (int)v;
+    }
+}
+
+// FP64 restatement of the differentiable vertex position (surface iteration
+// off): origin + (cell + mean of the contour's edge points) * spacing, the edge
+// point taking w = (iso - s0) / (s1 - s0) on the edge's axis
+// (computeLocalCoordinateOffset, D/CellIntersection.inl:176-200)
+static double gridAt(const double* g, const int d[3], int x, int y, int z) {
+    x = x < 0 ? 0 : (x > d[0] - 1 ? d[0] - 1 : x);
+    y = y < 0 ? 0 : (y > d[1] - 1 ? d[1] - 1 : y);
+    z = z < 0 ? 0 : (z > d[2] - 1 ? d[2] - 1 : z);
+    return g[((size_t)z * d[1] + y) * d[0] + x];
+}
+
+void mdmc_oracle_positions_f64(const void* res, const double* grid, const int dims[3], const double origin[3],
+                               const double spacing[3], double iso, double* out) {
+    const oracle::Result* r = (const oracle::Result*)res;
+    const size_t Vd = r->dmcEdges.size();
+    for (size_t v = 0; v < Vd; ++v) {
+        const int* c = &r->dmcCell[3 * v];
+        double s[8];
+        for (int k = 0; k < 8; ++k) s[k] = gridAt(grid, dims, c[0] + (k & 1), c[1] + ((k >> 1) & 1), c[2] + ((k >> 2) & 1));
+        double q[3] = {0, 0, 0};
+        int n = 0;
+        for (int e = 0; e < 12; ++e) {
+            if (!((r->dmcEdges[v] >> e) & 1)) continue;
+            const int a0 = oracle::kEdgeV0[e], a1 = oracle::kEdgeV1[e], ax = oracle::kEdgeAxis[e];
+            double p[3] = {(double)(a0 & 1), (double)((a0 >> 1) & 1), (double)((a0 >> 2) & 1)};
+            p[ax] = (iso - s[a0]) / (s[a1] - s[a0]);
+            for (int a = 0; a < 3; ++a) q[a] += p[a];
+            ++n;
+        }
+        for (int a = 0; a < 3; ++a) out[3 * v + a] = origin[a] + ((double)c[a] + q[a] / n) * spacing[a];
+    }
+}
+
+// FP64 gradient of sum_v dLdpos[v] . pos[v] with respect to the grid samples,
+// added to out.  Final vertices that the splitter made pass their gradient to
+// the DMC vertex they descend from.
+void mdmc_oracle_backward(const void* res, const double* grid, const int dims[3], const double spacing[3], double iso,
+                          const double* dLdpos, double* out) {
+    const oracle::Result* r = (const oracle::Result*)res;
+    const size_t Vd = r->dmcEdges.size(), V = r->pos.size() / 3;
+    std::vector<double> gs(3 * Vd, 0.0);
+    for (size_t v = 0; v < V; ++v) {
+        const int p = v < Vd ? (int)v : (v < r->parent.size() ? r->parent[v] : -1);
+        if (p < 0 || (size_t)p >= Vd) continue;
+        for (int a = 0; a < 3; ++a) gs[3 * p + a] += dLdpos[3 * v + a];
+    }
+    for (size_t v = 0; v < Vd; ++v) {
+        const int* c = &r->dmcCell[3 * v];
+        int idx[8];
+        double s[8];
+        for (int k = 0; k < 8; ++k) {
+            int x = c[0] + (k & 1), y = c[1] + ((k >> 1) & 1), z = c[2] + ((k >> 2) & 1);
+            x = x > dims[0] - 1 ? dims[0] - 1 : x;
+            y = y > dims[1] - 1 ? dims[1] - 1 : y;
+            z = z > dims[2] - 1 ? dims[2] - 1 : z;
+            idx[k] = (int)(((size_t)z * dims[1] + y) * dims[0] + x);
+            s[k] = grid[idx[k]];
+        }
+        int n = 0;
+        for (int e = 0; e < 12; ++e) n += (r->dmcEdges[v] >> e) & 1;
+        for (int e = 0; e < 12; ++e) {
+            if (!((r->dmcEdges[v] >> e) & 1)) continue;
+            const int a0 = oracle::kEdgeV0[e], a1 = oracle::kEdgeV1[e], ax = oracle::kEdgeAxis[e];
+            const double d = s[a1] - s[a0];
+            const double coef = gs[3 * v + ax] * spacing[ax] / n;
+            out[idx[a0]] += coef * (iso - s[a1]) / (d * d);
+            out[idx[a1]] += coef * (-(iso - s[a0]) / (d * d));
+        }
+    }
+}
+
+// refineGrid's weights (D/UniformGrid.inl:279-319) applied in FP64, and their
+// adjoint: every refined sample is a fixed trilinear combination of 8 coarse
+// samples (clamped indices; the padded layer repeats the boundary)
+static void refineWeights(const int in[3], int r, int pad, int x, int y, int z, int idx[8], double w[8]) {
+    int od[3];
+    for (int a = 0; a < 3; ++a) od[a] = in[a] + (in[a] - 1) * r + (pad ? 2 : 0);
+    int ix = x, iy = y, iz = z;
+    if (pad) {
+        ix = std::min(std::max(ix, 1), od[0] - 2) - 1;
+        iy = std::min(std::max(iy, 1), od[1] - 2) - 1;
+        iz = std::min(std::max(iz, 1), od[2] - 2) - 1;
+    }
+    const float f = (float)(r + 1);
+    const float qx = (float)ix / f, qy = (float)iy / f, qz = (float)iz / f;
+    const int mx = (int)std::floor(qx), my = (int)std::floor(qy), mz = (int)std::floor(qz);
+    const double dx = (double)(qx - (float)mx), dy = (double)(qy - (float)my), dz = (double)(qz - (float)mz);
+    for (int k = 0; k < 8; ++k) {
+        int cx = mx + (k & 1), cy = my + ((k >> 1) & 1), cz = mz + ((k >> 2) & 1);
+        cx = cx < 0 ? 0 : (cx > in[0] - 1 ? in[0] - 1 : cx);
+        cy = cy < 0 ? 0 : (cy > in[1] - 1 ? in[1] - 1 : cy);
+        cz = cz < 0 ? 0 : (cz > in[2] - 1 ? in[2] - 1 : cz);
+        idx[k] = (int)(((size_t)cz * in[1] + cy) * in[0] + cx);
+        w[k] = ((k & 1) ? dx : 1.0 - dx) * (((k >> 1) & 1) ? dy : 1.0 - dy) * (((k >> 2) & 1) ? dz : 1.0 - dz);
+    }
+}
+
+void mdmc_oracle_refine_f64(const double* in, const int dims[3], int r, int pad, double* out) {
+    int od[3];
+    for (int a = 0; a < 3; ++a) od[a] = dims[a] + (dims[a] - 1) * r + (pad ? 2 : 0);
+    for (int z = 0; z < od[2]; ++z)
+        for (int y = 0; y < od[1]; ++y)
+            for (int x = 0; x < od[0]; ++x) {
+                int idx[8];
+                double w[8], v = 0.0;
+                refineWeights(dims, r, pad, x, y, z, idx, w);
+                for (int k = 0; k < 8; ++k) v += w[k] * in[idx[k]];
+                out[((size_t)z * od[1] + y) * od[0] + x] = v;
+            }
+}
+
+void mdmc_oracle_refine_backward(const double* dout, const int dims[3], int r, int pad, double* din) {
+    int od[3];
+    for (int a = 0; a < 3; ++a) od[a] = dims[a] + (dims[a] - 1) * r + (pad ? 2 : 0);
+    for (int z = 0; z < od[2]; ++z)
+        for (int y = 0; y < od[1]; ++y)
+            for (int x = 0; x < od[0]; ++x) {
+                const double g = dout[((size_t)z * od[1] + y) * od[0] + x];
+                if (g == 0.0) continue;
+                int idx[8];
+                double w[8];
+                refineWeights(dims, r, pad, x, y, z, idx, w);
+                for (int k = 0; k < 8; ++k) din[idx[k]] += w[k] * g;
+            }
+}
 
 int mdmc_oracle_case_ambiguous(int c) { return oracle::caseIsAmbiguous(c) ? 1 : 0; }
 

@@ -89,6 +89,23 @@ void mdmc_oracle_get_dmc(const void* result, float* positions, float* normals, i
                          uint16_t* quad_attr);
 void mdmc_oracle_free(void* result);
 
+/* Differentiable path (no reference counterpart; surface iteration off).
+ * Topology of a result: per DMC vertex its cell (x, y, z) and the 12-bit mask
+ * of its contour's cell edges; per final vertex the DMC vertex it descends
+ * from (itself for DMC vertices, the corner vertex for split vertices, -1 if
+ * none).  Any pointer may be NULL. */
+void mdmc_oracle_get_topology(const void* result, int* cells, uint16_t* edges, int* parents);
+/* FP64 DMC vertex positions for a grid of the same dims, topology held fixed */
+void mdmc_oracle_positions_f64(const void* result, const double* grid, const int dims[3], const double origin[3],
+                               const double spacing[3], double iso, double* out);
+/* FP64 gradient of sum(dLdpos . positions) (3 per final vertex) with respect to
+ * the grid samples, added to out */
+void mdmc_oracle_backward(const void* result, const double* grid, const int dims[3], const double spacing[3],
+                          double iso, const double* dLdpos, double* out);
+/* refineGrid as a linear map in FP64 (coarse dims in), and its adjoint (added to din) */
+void mdmc_oracle_refine_f64(const double* in, const int dims[3], int r, int pad, double* out);
+void mdmc_oracle_refine_backward(const double* dout, const int dims[3], int r, int pad, double* din);
+
 /* 1 if Marching Cubes case c takes the asymptotic-decider path. */
 int mdmc_oracle_case_ambiguous(int c);
 

@@ -62,6 +62,14 @@ def oracle():
                                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                                ctypes.c_void_p]
             lib.mdmc_oracle_read_bin.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 4
+            lib.mdmc_oracle_get_topology.argtypes = [ctypes.c_void_p] * 4
+            lib.mdmc_oracle_positions_f64.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_double, ctypes.c_void_p]
+            lib.mdmc_oracle_backward.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_double, ctypes.c_void_p,
+                                                                         ctypes.c_void_p]
+            lib.mdmc_oracle_refine_f64.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                                   ctypes.c_void_p]
+            lib.mdmc_oracle_refine_backward.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                        ctypes.c_int, ctypes.c_void_p]
             _lib = lib
     return _lib
 
@@ -206,3 +214,79 @@ def match_to_golden(positions, faces, golden, tol):
         mapping[int(v)] = int(gref[j])
     mapped = [[mapping[int(x)] for x in f] for f in faces]
     return canonical_faces(mapped), canonical_faces(gf), maxd, mapping
+
+
+class OracleRun:
+    """One oracle run kept open for the differentiable path: the DMC vertex
+    topology (cell, contour edges), the parent DMC vertex of every final
+    vertex, FP64 positions for a perturbed grid of the same dims and the FP64
+    gradient of sum(dL/dpos . pos) with respect to the grid samples."""
+
+    def __init__(self, grid, dims, origin, spacing, iso, **opts):
+        self.lib = oracle()
+        self.dims = np.asarray(dims, np.int32)
+        self.origin = np.asarray(origin, np.float64)
+        self.spacing = np.asarray(spacing, np.float64)
+        self.iso = float(np.float32(iso))
+        grid = np.ascontiguousarray(grid, np.float32).reshape(-1)
+        o = default_options(**opts)
+        self.res = self.lib.mdmc_oracle_run(_p(grid), _p(self.dims), _p(np.asarray(origin, np.float32)),
+                                            _p(np.asarray(spacing, np.float32)), ctypes.c_float(iso),
+                                            ctypes.byref(o))
+        counts = np.zeros(5, np.int64)
+        self.lib.mdmc_oracle_counts(self.res, _p(counts))
+        self.num_vertices, self.num_dmc_vertices = int(counts[0]), int(counts[3])
+        self.cells = np.zeros((self.num_dmc_vertices, 3), np.int32)
+        self.edges = np.zeros(self.num_dmc_vertices, np.uint16)
+        self.parents = np.zeros(self.num_vertices, np.int32)
+        self.lib.mdmc_oracle_get_topology(self.res, _p(self.cells), _p(self.edges), _p(self.parents))
+        self.positions = np.zeros((self.num_vertices, 3), np.float32)
+        self.lib.mdmc_oracle_get(self.res, _p(self.positions), None, None, None, None, None, None)
+
+    def positions_f64(self, grid64):
+        out = np.zeros((self.num_dmc_vertices, 3), np.float64)
+        g = np.ascontiguousarray(grid64, np.float64).reshape(-1)
+        self.lib.mdmc_oracle_positions_f64(self.res, _p(g), _p(self.dims), _p(self.origin), _p(self.spacing),
+                                           self.iso, _p(out))
+        return out
+
+    def backward(self, grid64, dLdpos):
+        out = np.zeros(int(np.prod(self.dims)), np.float64)
+        g = np.ascontiguousarray(grid64, np.float64).reshape(-1)
+        d = np.ascontiguousarray(dLdpos, np.float64).reshape(-1)
+        assert d.size == 3 * self.num_vertices
+        self.lib.mdmc_oracle_backward(self.res, _p(g), _p(self.dims), _p(self.spacing), self.iso, _p(d), _p(out))
+        return out
+
+    def close(self):
+        if self.res:
+            self.lib.mdmc_oracle_free(self.res)
+            self.res = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def refine_f64(coarse, dims, refinement, pad):
+    od, _, _ = refined_geometry(dims, [1, 1, 1], [0, 0, 0], refinement, pad)
+    out = np.zeros(int(np.prod(od)), np.float64)
+    c = np.ascontiguousarray(coarse, np.float64).reshape(-1)
+    oracle().mdmc_oracle_refine_f64(_p(c), _p(np.asarray(dims, np.int32)), int(refinement), int(pad), _p(out))
+    return out
+
+
+def refine_backward(dout, dims, refinement, pad):
+    out = np.zeros(int(np.prod(dims)), np.float64)
+    d = np.ascontiguousarray(dout, np.float64).reshape(-1)
+    oracle().mdmc_oracle_refine_backward(_p(d), _p(np.asarray(dims, np.int32)), int(refinement), int(pad), _p(out))
+    return out
+
+
+def sphere_sdf(n, radius, center=None):
+    """Signed distance to a sphere (cells), float32, x fastest."""
+    c = (n - 1) / 2.0 if center is None else center
+    z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    return (np.sqrt((x - c) ** 2 + (y - c) ** 2 + (z - c) ** 2) - radius).astype(np.float32)
