@@ -47,6 +47,9 @@ def parse():
     ap.add_argument("--config", default="blobs129_refine4")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--fit", action="store_true",
+                    help="also time 200 Adam steps of the sphere-to-torus fit (brute-force Chamfer in torch)")
     return ap.parse_args()
 
 
@@ -284,6 +287,9 @@ def run_ours(args, rank, world, local):
         e2e = {"value": round(world * cells / (m / 1e3) / 1e6, 2), "unit": "Mcells/s", "ms_per_step": round(m, 4),
                "h2d_bytes_per_step": int(host_in.numel() * 4), "d2h_bytes_per_step": int(d2h)}
 
+    adjoint = None
+    if rank == 0 and not args.no_adjoint:
+        adjoint = measure_adjoint(args, dev, stream, flush)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args.config)
@@ -304,12 +310,66 @@ def run_ours(args, rank, world, local):
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
+            "adjoint": adjoint,
             "gpu_launches": launches,
             "clocks": clocks.summary(),
         }
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def measure_adjoint(args, dev, stream, flush):
+    """Forward (surface iteration off) and forward + adjoint on the 128^3
+    sphere SDF with the grid resident in HBM; CUDA events on the run's stream,
+    L2 flushed before every timed pass.  The gradient's accuracy is checked by
+    tests/test_gpu_adjoint.py, not here."""
+    import torch
+
+    import manifolddmc_gb300 as mdmc
+    from manifolddmc_gb300.workloads import CONFIGS
+    name = "sphere128_sdf"
+    desc, gen, iso, refine, pad = CONFIGS[name]
+    vol = gen()
+    d_in = torch.from_numpy(vol).to(dev)
+    dmc = mdmc.DualMarchingCubes(enable_surface_to_vertex_iteration=0)
+    grid = mdmc.UniformGrid(d_in, [vol.shape[2], vol.shape[1], vol.shape[0]], stream=stream)
+    dmc.run(iso, grid, stream=stream)
+    V = int(dmc.mesh.num_vertices)
+    dl = torch.randn((V, 3), device=dev, generator=torch.Generator(device=dev).manual_seed(0))
+    dgrid = torch.empty_like(d_in)
+    fwd, both = [], []
+    for i in range(max(args.warmup, 3) + args.steps):
+        for with_adjoint in (False, True):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dmc.run(iso, grid, stream=stream)
+            if with_adjoint:
+                dmc.backward(dl, dgrid, stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            if int(dmc.mesh.num_vertices) != V:
+                raise RuntimeError("mesh size changed between runs")
+            if i >= max(args.warmup, 3):
+                (both if with_adjoint else fwd).append(e0.elapsed_time(e1))
+    f, b = float(np.mean(fwd)), float(np.mean(both))
+    fit = None
+    if args.fit:
+        # 200 Adam steps of forward + adjoint + one-sided Chamfer to 200k points
+        # on a torus (R = 40, r = 15 cells) around the grid's centre
+        from manifolddmc_gb300.optimize import fit_to_points
+        from manifolddmc_gb300.workloads import torus_points
+        c = (vol.shape[0] - 1) / 2.0
+        pts = torch.from_numpy(torus_points(200000, 40.0, 15.0, (c, c, c), seed=5)).to(dev)
+        _, losses, seconds = fit_to_points(d_in, pts, iso, steps=200, lr=0.1)
+        fit = {"steps": 200, "points": 200000, "seconds": round(seconds, 3), "ms_per_step": round(1e3 * seconds / 200, 3),
+               "loss_first": round(losses[0], 4), "loss_last": round(losses[-1], 4)}
+    return {"workload": name, "description": desc, "vertices": V, "fwd_ms": round(f, 4), "fit": fit,
+            "fwd_adjoint_ms": round(b, 4), "ratio": round(b / f, 3),
+            "gradient_check": "max |gpu - FP64 oracle| <= 1e-5 * max |FP64| (tests/test_gpu_adjoint.py); "
+                              "FP64 oracle vs FP64 central differences h=1e-4 (tests/test_adjoint_oracle.py)"}
 
 
 def cpu_sample(config):

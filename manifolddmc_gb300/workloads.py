@@ -25,6 +25,31 @@ def uniform_noise(n, seed):
     return np.random.default_rng(seed).random((n, n, n), dtype=np.float32)
 
 
+def sphere_sdf(n, radius, seed=0):
+    """Signed distance (cells) to a sphere of `radius` centred in an n^3 grid;
+    `seed` is unused (the field is deterministic)."""
+    ax = np.arange(n, dtype=np.float64) - (n - 1) / 2.0
+    d = np.sqrt(ax[None, None, :] ** 2 + ax[None, :, None] ** 2 + ax[:, None, None] ** 2)
+    return (d - radius).astype(np.float32)
+
+
+def torus_points(count, major, minor, centre, seed):
+    """`count` points uniform in area on a torus (radii in cells) around the z
+    axis through `centre`, by rejection sampling of the tube angle."""
+    rng = np.random.default_rng(seed)
+    pts = []
+    need = count
+    while need > 0:
+        u = rng.uniform(0, 2 * np.pi, 2 * need)
+        v = rng.uniform(0, 2 * np.pi, 2 * need)
+        keep = rng.uniform(0, 1, 2 * need) < (major + minor * np.cos(v)) / (major + minor)
+        u, v = u[keep][:need], v[keep][:need]
+        r = major + minor * np.cos(v)
+        pts.append(np.stack([r * np.cos(u), r * np.sin(u), minor * np.sin(v)], 1))
+        need -= len(u)
+    return (np.concatenate(pts)[:count] + np.asarray(centre)).astype(np.float32)
+
+
 # name: (description, generator, iso, refinement, pad)
 CONFIGS = {
     "blobs64_pad": ("64^3 fp32 grid, 8 Gaussian blobs (sigma 4-10), padded by 1, iso 0.5",
@@ -34,4 +59,7 @@ CONFIGS = {
     "blobs129_refine4": ("129^3 fp32 grid, 64 Gaussian blobs (sigma 3-12), trilinearly refined x4 "
                          "to 513^3 samples = 512^3 cells, iso 0.4",
                          lambda seed=2: gaussian_blobs(129, 64, (3.0, 12.0), seed), 0.4, 3, False),
+    "sphere128_sdf": ("128^3 fp32 signed distance to a sphere of radius 40 cells, iso 0, surface iteration off "
+                      "(the differentiable form)",
+                      lambda seed=0: sphere_sdf(128, 40.0, seed), 0.0, 0, False),
 }

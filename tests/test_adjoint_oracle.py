@@ -102,3 +102,26 @@ def test_oracle_gradient_through_refinement(refinement, pad):
         f = lambda cc: _loss(run, refine_f64(cc, dims, refinement, pad), geff)
         nodes = list(rng.choice(np.flatnonzero(np.abs(grad) > 0), size=60, replace=False)) + [0, 5]
         _check_fd(grad, f, c64, nodes)
+
+
+def test_oracle_gradient_on_the_differentiable_workload_1k_nodes():
+    # the 128^3 signed distance to a sphere of radius 40 cells at iso 0 (the
+    # differentiable form's grid): FP64 central differences (h = 1e-4) on 1000
+    # random grid nodes, most of them at corners of cells holding vertices
+    import sys
+    sys.path.insert(0, str(__import__("pathlib").Path(__file__).resolve().parents[1]))
+    from manifolddmc_gb300.workloads import CONFIGS
+    desc, gen, iso, refine, pad = CONFIGS["sphere128_sdf"]
+    vol = gen()
+    n = vol.shape[0]
+    dims = [n, n, n]
+    rng = np.random.default_rng(123)
+    with OracleRun(vol, dims, np.zeros(3, np.float32), np.ones(3, np.float32), iso, surface_iteration=0) as run:
+        assert run.num_dmc_vertices > 10000
+        dL = rng.standard_normal((run.num_vertices, 3))
+        g64 = vol.astype(np.float64).reshape(-1)
+        grad = run.backward(g64, dL)
+        geff = _effective(run, dL)
+        touched = np.flatnonzero(grad != 0)
+        nodes = list(rng.choice(touched, size=900, replace=False)) + list(rng.integers(0, vol.size, size=100))
+        _check_fd(grad, lambda gg: _loss(run, gg, geff), g64, nodes)

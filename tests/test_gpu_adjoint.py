@@ -115,3 +115,18 @@ def test_autograd_function_and_optimisation_step():
         opt.step()
         losses.append(float(loss.detach()))
     assert losses[-1] < losses[0]
+
+
+def test_fit_sphere_to_torus_points():
+    # the differentiable workload at a smaller size: a 48^3 sphere SDF pulled
+    # toward points on a torus by Adam through forward + adjoint
+    torch = pytest.importorskip("torch")
+    from manifolddmc_gb300.optimize import fit_to_points
+    from manifolddmc_gb300.workloads import sphere_sdf, torus_points
+    n = 48
+    c = (n - 1) / 2.0
+    grid0 = torch.from_numpy(sphere_sdf(n, 15.0)).cuda()
+    pts = torch.from_numpy(torus_points(20000, 15.0, 6.0, (c, c, c), seed=3)).cuda()
+    _, losses, seconds = fit_to_points(grid0, pts, steps=30, lr=0.1)
+    assert all(np.isfinite(losses))
+    assert np.mean(losses[-5:]) < 0.9 * np.mean(losses[:5]), losses[::5]
