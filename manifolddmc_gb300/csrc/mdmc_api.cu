@@ -88,6 +88,9 @@ struct mdmc_context {
     int lastSurfaceIteration = 1;
     int64_t dmcV = 0, activeCells = 0;
     DevBuf appParent, vertexGrad;
+    bool simplified = false;  // a simplification renumbered the DMC vertices
+    // simplification scratch
+    DevBuf sVal, sCount, sType, sTarget, sClaimA, sClaimC, sMerge, sKeepV, sKeepF, sPos, sNrm, sQuads, sAttr;
     // edge table
     DevBuf table, nmList, heValence;
     // quad -> owner cell; per-row active-cell mask (32 cells per word) and the
@@ -308,6 +311,86 @@ mdmc_status refreshTable(mdmc_context* c, uint32_t* status, cudaStream_t s) {
     launchBuckets(c->table.as<Bucket>(), c->cap, c->he.as<int4>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(),
                   0, c->heValence.as<uint8_t>(), c->nmList.as<int4>(), c->counters.as<DevCounters>(), md, s);
     c->tableValid = true;
+    return MDMC_OK;
+}
+
+// simplify3X3Y (kind 0), simplify3X3YOld (kind 1), simplify3333 (kind 2),
+// D/Halfedges/HalfedgeMesh.cu:859-1048: mark and merge, compact the vertex
+// and quad lists, rebuild the halfedge mesh from the quads (initialize)
+mdmc_status runSimplification(mdmc_context* c, int kind, cudaStream_t s) {
+    DevCounters* ctr = c->counters.as<DevCounters>();
+    uint32_t* status = &ctr->status;
+    const int V = (int)c->V, F = (int)c->F;
+    const MeshDims md{V, F, (int)c->H};
+    if (V <= 0 || F <= 0) return MDMC_OK;
+    MDMC_CHECK(c, c->sVal.ensure(sizeof(int) * (size_t)V));
+    MDMC_CHECK(c, c->sCount.ensure(sizeof(int) * (size_t)V));
+    MDMC_CHECK(c, c->sType.ensure(sizeof(int) * (size_t)V));
+    MDMC_CHECK(c, c->sTarget.ensure(sizeof(int) * (size_t)V));
+    MDMC_CHECK(c, c->sClaimA.ensure(sizeof(int) * (size_t)V));
+    MDMC_CHECK(c, c->sClaimC.ensure(sizeof(int) * (size_t)V));
+    MDMC_CHECK(c, c->sMerge.ensure(sizeof(int4) * (size_t)F));
+    MDMC_CHECK(c, c->sKeepV.ensure(sizeof(int) * (size_t)(V + 1)));
+    MDMC_CHECK(c, c->sKeepF.ensure(sizeof(int) * (size_t)(F + 1)));
+    MDMC_CHECK(c, cudaMemsetAsync(c->sVal.p, 0, sizeof(int) * (size_t)V, s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->sCount.p, 0, sizeof(int) * (size_t)V, s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->sType.p, 0, sizeof(int) * (size_t)V, s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->sTarget.p, 0xFF, sizeof(int) * (size_t)V, s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->sClaimA.p, 0xFF, sizeof(int) * (size_t)V, s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->sClaimC.p, 0xFF, sizeof(int) * (size_t)V, s));
+    launchValence(c->he.as<int4>(), md, c->sVal.as<int>(), s);
+    if (kind < 2)
+        launchSimplify3X3Y(c->he.as<int4>(), c->faceFirst.as<int>(), md, c->sVal.as<int>(), kind == 0 ? 1 : 0,
+                           c->faceAttr.as<uint16_t>(), c->sCount.as<int>(), c->sMerge.as<int4>(), c->sClaimA.as<int>(),
+                           c->sClaimC.as<int>(), c->pos.as<float>(), c->nrm.as<float>(), c->sType.as<int>(),
+                           c->sTarget.as<int>(), status, s);
+    else
+        launchSimplify3333(c->he.as<int4>(), c->faceFirst.as<int>(), md, c->sVal.as<int>(), c->faceAttr.as<uint16_t>(),
+                           c->sType.as<int>(), c->sTarget.as<int>(), s);
+    const int removedType = kind < 2 ? 3 : 1;
+    launchKeepFlags(c->sType.as<int>(), removedType, V, c->sKeepV.as<int>(), c->faceAttr.as<uint16_t>(), F,
+                    c->sKeepF.as<int>(), s);
+    mdmc_status st;
+    if ((st = scan<int>(c, c->sKeepV.as<int>(), c->sKeepV.as<int>(), V, s)) != MDMC_OK) return st;
+    if ((st = scan<int>(c, c->sKeepF.as<int>(), c->sKeepF.as<int>(), F, s)) != MDMC_OK) return st;
+    MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, c->sKeepV.as<int>() + V, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts + 1, c->sKeepF.as<int>() + F, sizeof(int), cudaMemcpyDeviceToHost, s));
+    MDMC_CHECK(c, cudaStreamSynchronize(s));
+    MDMC_CHECK(c, cudaGetLastError());
+    const int V2 = c->hostInts[0], F2 = c->hostInts[1];
+    if (V2 < 0 || V2 > V || F2 < 0 || F2 > F) return fail(c, MDMC_ERROR_CUDA, "inconsistent simplification counts");
+    MDMC_CHECK(c, c->sPos.ensure(sizeof(float) * 3 * (size_t)std::max(V2, 1)));
+    MDMC_CHECK(c, c->sNrm.ensure(sizeof(float) * 3 * (size_t)std::max(V2, 1)));
+    MDMC_CHECK(c, c->sQuads.ensure(sizeof(int4) * (size_t)std::max(F2, 1)));
+    MDMC_CHECK(c, c->sAttr.ensure(roundUp(sizeof(uint16_t) * (size_t)std::max(F2, 1), 4)));
+    launchCompactMesh(c->he.as<int4>(), c->faceFirst.as<int>(), md, c->faceAttr.as<uint16_t>(), c->sType.as<int>(),
+                      c->sTarget.as<int>(), removedType, kind == 2 ? 1 : 0, c->sKeepV.as<int>(), c->sKeepF.as<int>(), V2,
+                      c->pos.as<float>(), c->nrm.as<float>(), c->sPos.as<float>(), c->sNrm.as<float>(),
+                      c->sQuads.as<int4>(), c->sAttr.as<uint16_t>(), status, s);
+    if (V2 > 0) {
+        MDMC_CHECK(c, cudaMemcpyAsync(c->pos.p, c->sPos.p, sizeof(float) * 3 * (size_t)V2, cudaMemcpyDeviceToDevice, s));
+        MDMC_CHECK(c, cudaMemcpyAsync(c->nrm.p, c->sNrm.p, sizeof(float) * 3 * (size_t)V2, cudaMemcpyDeviceToDevice, s));
+    }
+    // HalfedgeMesh::initialize from the reduced quads
+    c->V = V2;
+    c->F = F2;
+    c->H = 4 * (int64_t)F2;
+    c->simplified = true;
+    launchCollectHalfedges(c->sQuads.as<int4>(), c->sAttr.as<uint16_t>(), F2, c->he.as<int4>(), c->faceFirst.as<int>(),
+                           c->faceAttr.as<uint16_t>(), s);
+    const MeshDims md2{V2, F2, 4 * F2};
+    c->cap = tableCapacity(F2);
+    MDMC_CHECK(c, c->table.ensure(sizeof(Bucket) * c->cap));
+    MDMC_CHECK(c, cudaMemsetAsync(c->table.p, 0xFF, sizeof(Bucket) * c->cap, s));
+    MDMC_CHECK(c, c->nmList.ensure(sizeof(int4) * (size_t)(F2 + 1)));
+    MDMC_CHECK(c, c->heValence.ensure((size_t)std::max(4 * F2, 1)));
+    MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)std::max(V2, 1), 4), s));
+    MDMC_CHECK(c, cudaMemsetAsync((char*)c->counters.p + 8, 0, sizeof(DevCounters) - 8, s));
+    launchInsertFaces(c->he.as<int4>(), c->faceFirst.as<int>(), md2, c->table.as<Bucket>(), c->cap, status, s);
+    launchBuckets(c->table.as<Bucket>(), c->cap, c->he.as<int4>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), 1,
+                  c->heValence.as<uint8_t>(), c->nmList.as<int4>(), ctr, md2, s);
+    c->tableValid = true;
+    MDMC_CHECK(c, cudaGetLastError());
     return MDMC_OK;
 }
 
@@ -605,6 +688,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->lastIso = iso;
     c->lastSurfaceIteration = c->opt.enable_surface_to_vertex_iteration;
     c->dmcV = c->activeCells = 0;
+    c->simplified = false;
     std::memset(&c->stats, 0, sizeof c->stats);
     DevCounters* ctr = c->counters.as<DevCounters>();
     uint32_t* status = &ctr->status;
@@ -708,7 +792,11 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, cudaGetLastError());
     cudaEventRecord(c->ev[1], s);
     cudaEventRecord(c->kev[8], s);
-    const MeshDims md0{(int)Vd, (int)Q, (int)(4 * Q)};
+    // runPostProcesses, D/DualMarchingCubes.cu:335-380: simplifications first
+    if (c->opt.simplify_p3x3y_color && (st = runSimplification(c, 0, s)) != MDMC_OK) return st;
+    if (c->opt.simplify_p3x3y_old && (st = runSimplification(c, 1, s)) != MDMC_OK) return st;
+    if (c->opt.simplify_p3333 && (st = runSimplification(c, 2, s)) != MDMC_OK) return st;
+    const MeshDims md0{(int)c->V, (int)c->F, (int)c->H};
     cudaEventRecord(c->kev[9], s);
     cudaEventRecord(c->ev[2], s);
 
@@ -839,6 +927,8 @@ mdmc_status mdmc_backward(mdmc_context* c, const float* dl_dpositions, float* dl
     if (c->lastSurfaceIteration)
         return fail(c, MDMC_ERROR_INVALID_ARGUMENT,
                     "the adjoint needs a forward run with enable_surface_to_vertex_iteration = 0");
+    if (c->simplified)
+        return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "the adjoint is not defined after a simplification pass");
     cudaStream_t s = (cudaStream_t)stream;
     const mdmc_grid& grid = c->lastGrid;
     GridDesc g;

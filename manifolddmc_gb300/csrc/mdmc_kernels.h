@@ -126,6 +126,22 @@ void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const Bucke
                   const uint8_t* heValence, int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr,
                   uint32_t* status, cudaStream_t s);
 
+// valence-pattern simplifications
+void launchValence(const int4* he, MeshDims md, int* val, cudaStream_t s);
+void launchSimplify3X3Y(const int4* he, const int* faceFirst, MeshDims md, const int* val, int color, uint16_t* attr,
+                        int* count, int4* merge, int* claimA, int* claimC, float* pos, float* nrm, int* type,
+                        int* target, uint32_t* status, cudaStream_t s);
+void launchSimplify3333(const int4* he, const int* faceFirst, MeshDims md, const int* val, uint16_t* attr, int* type,
+                        int* target, cudaStream_t s);
+void launchKeepFlags(const int* type, int removedType, int numVertices, int* keepV, const uint16_t* attr, int numFaces,
+                     int* keepF, cudaStream_t s);
+void launchCompactMesh(const int4* he, const int* faceFirst, MeshDims md, const uint16_t* attr, const int* type,
+                       const int* target, int removedType, int remapPattern, const int* vAddr, const int* fAddr,
+                       int newVertices, const float* pos, const float* nrm, float* pos2, float* nrm2, int4* quads,
+                       uint16_t* attr2, uint32_t* status, cudaStream_t s);
+void launchCollectHalfedges(const int4* quads, const uint16_t* attr2, int numFaces, int4* he, int* faceFirst,
+                            uint16_t* attr, cudaStream_t s);
+
 // adjoint of the vertex positions (surface iteration off)
 void launchGatherParents(const float* dlDpos, int numVertices, int dmcVertices, const int* appParent, float* vertexGrad,
                          cudaStream_t s);

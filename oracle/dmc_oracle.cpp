@@ -1135,6 +1135,214 @@ static void detectNonManifoldVertices(Mesh& m) {
     }
 }
 
+// ------------------------------------------------------------------------ //
+// HalfedgeMesh::initialize from a quad list, D/Halfedges/HalfedgeMesh.cu:14-60,
+// :173-291, :848-857: halfedge i of quad q is 4q+i, twins and flags from the
+// edge table, face attributes from the quads'
+// ------------------------------------------------------------------------ //
+static void initializeFromQuads(Mesh& m, const std::vector<int>& quads, const std::vector<uint16_t>& attr) {
+    const int Q = (int)attr.size();
+    m.he.resize(4 * (size_t)Q);
+    m.faceFirst.resize(Q);
+    m.faceAttr = attr;
+    m.vflags.assign(m.numV(), 0);
+    for (int q = 0; q < Q; ++q) {
+        for (int i = 0; i < 4; ++i) m.he[4 * q + i] = HE{quads[4 * q + i], q, 4 * q + ((i + 1) & 3), -1};
+        m.faceFirst[q] = 4 * q;
+    }
+    m.buildTable();
+    m.connectTwins();
+    m.vertexFlagsFromTable();
+}
+
+// ------------------------------------------------------------------------ //
+// Valence-pattern simplifications, D/Halfedges/HalfedgeMesh.cu:296-683 and
+// :859-1048.  They run right after the halfedge mesh is built, on its vertex
+// and quad lists, and end with a rebuild from the reduced lists.  Where the
+// reference is not deterministic or reads outside its arrays, this
+// restatement fixes one behaviour:
+//  - a quad edge without a twin (the reference then reads halfedges[-1])
+//    makes the quad ineligible;
+//  - vertices and quads are compacted in their order (the reference appends
+//    with atomics);
+//  - in the 3333 pass every face's pattern bits are cleared before any face
+//    sets a neighbour's remove flag (the reference's threads race there).
+// ------------------------------------------------------------------------ //
+static const uint16_t kAttrPattern = 0x40, kAttrRemove = 0x80, kAttrBoundary = 0x100;
+enum { kTypeNeutral = 0, kTypePattern = 1, kTypeRemovable = 3 };
+
+// computeVertexValence, :296-312: outgoing halfedges, plus one per halfedge
+// without twin for the vertex it points to
+static std::vector<int> vertexValence(const Mesh& m) {
+    std::vector<int> val(m.numV(), 0);
+    for (const HE& e : m.he) {
+        val[e.origin]++;
+        if (e.twin == -1) val[m.he[e.next].origin]++;
+    }
+    return val;
+}
+
+static void faceVertices(const Mesh& m, int f, int q[4], int hs[4]) {
+    int h = m.faceFirst[f];
+    for (int i = 0; i < 4; ++i) {
+        hs[i] = h;
+        q[i] = m.he[h].origin;
+        h = m.he[h].next;
+    }
+}
+
+// removeVertices*, removeQuadrilaterals* / removeQuads*: keep the vertices that
+// are not removed (in order), remap the kept quads, then rebuild
+static void compactAndRebuild(Mesh& m, const std::vector<int>& type, int removedType, const std::vector<int>& target,
+                              bool remapPatternQuads) {
+    const int V = m.numV(), F = (int)m.faceFirst.size();
+    std::vector<int> addr(V, -1);
+    std::vector<float> pos, nrm;
+    std::vector<int> parent;
+    for (int v = 0; v < V; ++v) {
+        if (type[v] == removedType) continue;
+        addr[v] = (int)(pos.size() / 3);
+        for (int a = 0; a < 3; ++a) {
+            pos.push_back(m.pos[3 * v + a]);
+            nrm.push_back(m.nrm[3 * v + a]);
+        }
+        parent.push_back(v < (int)m.parent.size() ? m.parent[v] : -1);
+    }
+    std::vector<int> quads;
+    std::vector<uint16_t> attr;
+    for (int f = 0; f < F; ++f) {
+        const uint16_t a = m.faceAttr[f];
+        if (a & kAttrRemove) continue;
+        int q[4], hs[4];
+        faceVertices(m, f, q, hs);
+        for (int i = 0; i < 4; ++i) {
+            int v = q[i];
+            if (remapPatternQuads ? (a & kAttrPattern) != 0 : type[v] == removedType) v = target[v];
+            const int n = (v >= 0 && v < V) ? addr[v] : -1;
+            if (n < 0) m.anomalies |= kSMapping;
+            quads.push_back(n < 0 ? 0 : n);
+        }
+        // a new QuadrilateralAttribute (INVALID_COLOR) keeps the NM and boundary bits
+        attr.push_back((uint16_t)(kAttrInvalidColor | (a & kAttrNonManifold) | (a & kAttrBoundary)));
+    }
+    m.pos = std::move(pos);
+    m.nrm = std::move(nrm);
+    m.parent = std::move(parent);
+    initializeFromQuads(m, quads, attr);
+}
+
+// handleMerge, :358-378: vertex a takes the midpoint of b and d (position and
+// normalized normal), c is removed in favour of a
+static void handleMerge(Mesh& m, int a, int b, int c, int d, std::vector<int>& type, std::vector<int>& target,
+                        uint16_t& attr) {
+    V3 p = m.P(b);
+    p = add(p, smul(0.5f, sub(m.P(d), p)));
+    V3 n = v3(m.nrm[3 * b], m.nrm[3 * b + 1], m.nrm[3 * b + 2]);
+    const V3 nd = v3(m.nrm[3 * d], m.nrm[3 * d + 1], m.nrm[3 * d + 2]);
+    n = normalize(add(n, smul(0.5f, sub(nd, n))));
+    m.pos[3 * a] = p.x; m.pos[3 * a + 1] = p.y; m.pos[3 * a + 2] = p.z;
+    m.nrm[3 * a] = n.x; m.nrm[3 * a + 1] = n.y; m.nrm[3 * a + 2] = n.z;
+    type[c] = kTypeRemovable;
+    target[c] = a;
+    attr |= kAttrRemove;
+}
+
+// simplify3X3Y (color based, :859-921; markElementsP3X3Y :318-340,
+// mergeVerticesP3X3YColor :381-442) and simplify3X3YOld (:923-985;
+// countVerticesP3X3Y :342-364, mergeVerticesP3X3Y :448-496)
+static void simplify3X3Y(Mesh& m, bool color) {
+    const int V = m.numV(), F = (int)m.faceFirst.size();
+    const std::vector<int> val = vertexValence(m);
+    std::vector<int> count(V, 0), type(V, kTypeNeutral), target(V, -1);
+    std::vector<uint16_t>& attr = m.faceAttr;
+    auto patternA = [&](const int q[4]) { return val[q[0]] == 3 && val[q[1]] >= 5 && val[q[2]] == 3 && val[q[3]] >= 5; };
+    auto patternB = [&](const int q[4]) { return val[q[0]] >= 5 && val[q[1]] == 3 && val[q[2]] >= 5 && val[q[3]] == 3; };
+    for (int f = 0; f < F; ++f) {
+        int q[4], hs[4];
+        faceVertices(m, f, q, hs);
+        if (color) {
+            if (attr[f] & (kAttrNonManifold | kAttrBoundary)) continue;
+            attr[f] &= 0x3F;
+            if (patternA(q) || patternB(q)) attr[f] |= kAttrPattern;
+        } else {
+            attr[f] &= 0x3F;
+            if (patternA(q)) {
+                count[q[0]]++;
+                count[q[2]]++;
+                attr[f] |= kAttrPattern;
+            } else if (patternB(q)) {
+                count[q[1]]++;
+                count[q[3]]++;
+                attr[f] |= kAttrPattern;
+            }
+        }
+    }
+    for (int f = 0; f < F; ++f) {
+        if (!color && (attr[f] & (kAttrNonManifold | kAttrBoundary))) continue;
+        if (!(attr[f] & kAttrPattern)) continue;
+        int q[4], hs[4];
+        faceVertices(m, f, q, hs);
+        int nb[4];
+        bool ok = true;
+        for (int i = 0; i < 4 && ok; ++i) {
+            const int t = m.he[hs[i]].twin;
+            if (t < 0) { ok = false; break; }
+            nb[i] = m.he[t].face;
+            // the reference tests the neighbour's NM flag and its own boundary flag
+            if ((attr[nb[i]] & kAttrNonManifold) || (attr[f] & kAttrBoundary)) ok = false;
+        }
+        if (!ok) continue;
+        if (color) {
+            const int c = attr[f] & 0x1F;
+            for (int i = 0; i < 4; ++i)
+                if ((attr[nb[i]] & kAttrPattern) && (attr[nb[i]] & 0x1F) <= c) ok = false;
+            if (!ok) continue;
+        }
+        if (patternA(q) && (color || (count[q[0]] == 1 && count[q[2]] == 1)))
+            handleMerge(m, q[0], q[1], q[2], q[3], type, target, attr[f]);
+        else if (patternB(q) && (color || (count[q[1]] == 1 && count[q[3]] == 1)))
+            handleMerge(m, q[1], q[0], q[3], q[2], type, target, attr[f]);
+    }
+    compactAndRebuild(m, type, kTypeRemovable, target, false);
+}
+
+// simplify3333 (:987-1048; markElementsP3333 :544-625)
+static void simplify3333(Mesh& m) {
+    const int V = m.numV(), F = (int)m.faceFirst.size();
+    const std::vector<int> val = vertexValence(m);
+    std::vector<int> type(V, kTypeNeutral), target(V, -1);
+    std::vector<uint16_t>& attr = m.faceAttr;
+    for (int f = 0; f < F; ++f)
+        if (!(attr[f] & (kAttrNonManifold | kAttrBoundary))) attr[f] &= 0x3F;
+    for (int f = 0; f < F; ++f) {
+        if (attr[f] & (kAttrNonManifold | kAttrBoundary)) continue;
+        int q[4], hs[4];
+        faceVertices(m, f, q, hs);
+        bool ok = true;
+        for (int i = 0; i < 4; ++i) ok = ok && val[q[i]] == 3;
+        if (!ok) continue;
+        int nb[4], nv[4], nval[4];
+        for (int i = 0; i < 4 && ok; ++i) {
+            const int t = m.he[hs[i]].twin;
+            if (t < 0) { ok = false; break; }
+            nb[i] = m.he[t].face;
+            if (attr[nb[i]] & (kAttrNonManifold | kAttrBoundary)) { ok = false; break; }
+            nv[i] = m.he[m.he[m.he[t].next].next].origin;
+            nval[i] = val[nv[i]];
+            if (nval[i] == 3) ok = false;
+        }
+        if (!ok) continue;
+        if (nval[0] == 4 && nval[1] == 4 && nval[2] == 4 && nval[3] == 4) continue;
+        attr[f] |= kAttrPattern;
+        for (int i = 0; i < 4; ++i) {
+            attr[nb[i]] |= kAttrRemove;
+            type[q[i]] = kTypePattern;
+            target[q[i]] = nv[i];
+        }
+    }
+    compactAndRebuild(m, type, kTypePattern, target, true);
+}
+
 static Result* run(const Grid& g, float iso, const mdmc_oracle_options& opt) {
     Result* r = new Result();
     std::memset(r->stats, 0, sizeof r->stats);
@@ -1149,21 +1357,12 @@ static Result* run(const Grid& g, float iso, const mdmc_oracle_options& opt) {
     for (int v = 0; v < m.numV(); ++v) m.parent[v] = v;
     const int Q = (int)r->dmcAttr.size();
     if (m.numV() > 0) {
-        // HalfedgeMesh::initialize, D/Halfedges/HalfedgeMesh.cu:14-60, :848-857
-        m.he.resize(4 * (size_t)Q);
-        m.faceFirst.resize(Q);
-        m.faceAttr.resize(Q);
-        m.vflags.assign(m.numV(), 0);
-        for (int q = 0; q < Q; ++q) {
-            for (int i = 0; i < 4; ++i)
-                m.he[4 * q + i] = HE{r->dmcQuads[4 * q + i], q, 4 * q + ((i + 1) & 3), -1};
-            m.faceFirst[q] = 4 * q;
-            m.faceAttr[q] = r->dmcAttr[q];
-        }
-        m.buildTable();
-        m.connectTwins();
-        m.vertexFlagsFromTable();
-        // runPostProcesses, D/DualMarchingCubes.cu:335-380
+        initializeFromQuads(m, r->dmcQuads, r->dmcAttr);
+        (void)Q;
+        // runPostProcesses, D/DualMarchingCubes.cu:335-380: simplifications, then repair
+        if (opt.simplify_3x3y_color) simplify3X3Y(m, true);
+        if (opt.simplify_3x3y_old) simplify3X3Y(m, false);
+        if (opt.simplify_3333) simplify3333(m);
         reconnect(m, g, iso);  // fixManifoldTwins
         if (opt.split_non_manifold)
             r->stats[MDMC_ORC_STAT_SPLIT_ITERATIONS] = runSplitter(m, g, iso, opt.splitting_step);

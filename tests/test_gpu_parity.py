@@ -20,6 +20,9 @@ OPTION_MAP = {
     "split_non_manifold": "split_non_manifold_halfedges",
     "detect_non_manifold_vertices": "detect_non_manifold_vertices",
     "splitting_step": "splitting_step",
+    "simplify_3x3y_color": "simplify_p3x3y_color",
+    "simplify_3x3y_old": "simplify_p3x3y_old",
+    "simplify_3333": "simplify_p3333",
 }
 
 
@@ -80,6 +83,16 @@ def test_golden_cases_bit_exact(case, level):
     assert_parity(dmc, m, ref)
 
 
+@pytest.mark.parametrize("case", list(reference_goldens().keys()))
+def test_golden_grids_with_all_simplifications(case):
+    # the reference's grids, padded, with every simplification before the repair
+    samples, dims, origin, spacing, iso = golden_grid(case)
+    opts = dict(simplify_3x3y_color=1, simplify_3x3y_old=1, simplify_3333=1)
+    dmc, m, _ = gpu_run(samples, dims, origin, spacing, iso, 0, True, **opts)
+    ref, _ = oracle_for(samples, dims, origin, spacing, iso, 0, True, **opts)
+    assert_parity(dmc, m, ref)
+
+
 def blobs(n, count, seed, sigma=(2.0, 5.0)):
     rng = np.random.default_rng(seed)
     z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
@@ -110,6 +123,16 @@ RANDOM_CASES = [
     # (the row walk takes over)
     ("blobs7_refine12_pad", lambda: blobs(7, 3, 13, (1.0, 2.0)), 0.45, 12, True, {}),
     ("blobs7_refine19", lambda: blobs(7, 3, 12, (1.0, 2.5)), 0.4, 19, False, {}),
+    # valence-pattern simplifications (HalfedgeMesh.cu:859-1048), alone and chained
+    ("noise16_3x3y_color", lambda: np.random.default_rng(21).random((16, 16, 16), dtype=np.float32), 0.5, 0, False,
+     {"simplify_3x3y_color": 1}),
+    ("blobs32_3x3y_old_pad", lambda: blobs(32, 6, 3), 0.4, 0, True, {"simplify_3x3y_old": 1}),
+    ("noise16_3333", lambda: np.random.default_rng(22).random((16, 16, 16), dtype=np.float32), 0.5, 0, False,
+     {"simplify_3333": 1}),
+    ("blobs28_all_simplify", lambda: blobs(28, 5, 23, (3.0, 7.0)), 0.3, 0, False,
+     {"simplify_3x3y_color": 1, "simplify_3x3y_old": 1, "simplify_3333": 1}),
+    ("blobs13_refine2_simplify", lambda: blobs(13, 4, 24), 0.4, 2, True,
+     {"simplify_3x3y_color": 1, "simplify_3333": 1, "surface_iteration": 0}),
 ]
 
 
