@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--fit", action="store_true",
                     help="also time 200 Adam steps of the sphere-to-torus fit (brute-force Chamfer in torch)")
     return ap.parse_args()
@@ -287,6 +288,9 @@ def run_ours(args, rank, world, local):
         e2e = {"value": round(world * cells / (m / 1e3) / 1e6, 2), "unit": "Mcells/s", "ms_per_step": round(m, 4),
                "h2d_bytes_per_step": int(host_in.numel() * 4), "d2h_bytes_per_step": int(d2h)}
 
+    batched = None
+    if rank == 0 and not args.no_batch:
+        batched = measure_batch(args, dev)
     adjoint = None
     if rank == 0 and not args.no_adjoint:
         adjoint = measure_adjoint(args, dev, stream, flush)
@@ -311,6 +315,7 @@ def run_ours(args, rank, world, local):
             "cpu_baseline": cpu,
             "e2e": e2e,
             "adjoint": adjoint,
+            "batch": batched,
             "gpu_launches": launches,
             "clocks": clocks.summary(),
         }
@@ -370,6 +375,47 @@ def measure_adjoint(args, dev, stream, flush):
             "fwd_adjoint_ms": round(b, 4), "ratio": round(b / f, 3),
             "gradient_check": "max |gpu - FP64 oracle| <= 1e-5 * max |FP64| (tests/test_gpu_adjoint.py); "
                               "FP64 oracle vs FP64 central differences h=1e-4 (tests/test_adjoint_oracle.py)"}
+
+
+def measure_batch(args, dev):
+    """The batched workload (96 seeded grids of uneven dims, blobs or noise,
+    iso in [0.3, 0.7]), resident in HBM: one mdmc_run_batch call (workers
+    autotuned on the warm-up call) against 96 sequential mdmc_run calls on one
+    context.  Both calls are synchronous; wall-clock over each whole call.
+    Inputs total far more than L2."""
+    import torch
+
+    import manifolddmc_gb300 as mdmc
+    from manifolddmc_gb300.workloads import batch_grids
+    items = batch_grids(96, seed=4)
+    tensors = [torch.from_numpy(v).to(dev) for v, _ in items]
+    grids = [mdmc.UniformGrid(t, [t.shape[2], t.shape[1], t.shape[0]]) for t in tensors]
+    isos = [iso for _, iso in items]
+    cells = sum((g.grid.dims[0] - 1) * (g.grid.dims[1] - 1) * (g.grid.dims[2] - 1) for g in grids)
+    torch.cuda.synchronize(dev)
+    batch = mdmc.BatchedDualMarchingCubes(streams=0)
+    batch.run(grids, isos)  # warm-up: grows the slots and picks the worker count
+    single = mdmc.DualMarchingCubes()
+    for g, iso in zip(grids, isos):
+        single.run(iso, g)
+    seq, bat = [], []
+    for _ in range(max(1, min(args.steps, 3))):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for g, iso in zip(grids, isos):
+            single.run(iso, g)
+        torch.cuda.synchronize(dev)
+        seq.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        batch.run(grids, isos)
+        torch.cuda.synchronize(dev)
+        bat.append(time.perf_counter() - t0)
+    s, b = float(np.mean(seq)), float(np.mean(bat))
+    return {"workload": "96 grids, dims uniform in [24,192] per axis, 4-32 Gaussian blobs or uniform noise (50/50), "
+                        "iso uniform in [0.3,0.7], seed 4",
+            "cells": int(cells), "streams": batch.streams, "sequential_ms": round(1e3 * s, 3),
+            "batch_ms": round(1e3 * b, 3), "speedup": round(s / b, 3),
+            "batch_mcells_s": round(cells / b / 1e6, 1), "sequential_mcells_s": round(cells / s / 1e6, 1)}
 
 
 def cpu_sample(config):

@@ -220,6 +220,25 @@ MDMC_API mdmc_status mdmc_write_obj(mdmc_context* context, const char* path);
 MDMC_API mdmc_status mdmc_backward(mdmc_context* context, const float* dl_dpositions, float* dl_dsamples,
                                    int accumulate, void* stream);
 
+/* Batched form (no counterpart in the reference, whose run takes one grid):
+ * n grids of uneven size, each with its iso-value, in one call.  The batch
+ * owns one context per grid slot; grid i's mesh and statistics (meshes[i],
+ * stats[i], either array may be NULL) stay valid until the next batch run, and
+ * mdmc_batch_context(batch, i) gives its context for the other getters.  The
+ * pipelines run concurrently on `streams` worker streams; streams = 0 lets the
+ * first mdmc_run_batch time 1, 2, 4, 8 and 16 workers on its grids and keep the
+ * fastest (mdmc_batch_streams reports the choice).  The call waits for the
+ * caller's stream (the grids' inputs) first and returns when every mesh is
+ * complete.  Grids keep the options given at creation. */
+typedef struct mdmc_batch mdmc_batch;
+MDMC_API mdmc_status mdmc_batch_create(mdmc_batch** batch, const mdmc_options* options, int streams);
+MDMC_API void mdmc_batch_destroy(mdmc_batch* batch);
+MDMC_API mdmc_status mdmc_run_batch(mdmc_batch* batch, const mdmc_grid* grids, const float* iso_values, int n,
+                                    mdmc_mesh* meshes, mdmc_stats* stats, void* stream);
+MDMC_API int mdmc_batch_streams(const mdmc_batch* batch);
+MDMC_API mdmc_context* mdmc_batch_context(mdmc_batch* batch, int i);
+MDMC_API const char* mdmc_batch_last_error(const mdmc_batch* batch);
+
 /* Human-readable description of the context's last error ("" if none). */
 MDMC_API const char* mdmc_last_error(const mdmc_context* context);
 

@@ -126,6 +126,12 @@ def library():
             "mdmc_last_error": (ctypes.c_char_p, [P]),
             "mdmc_case_tables": (None, [P, P]),
             "mdmc_backward": (ctypes.c_int, [P, P, P, ctypes.c_int, P]),
+            "mdmc_batch_create": (ctypes.c_int, [P, P, ctypes.c_int]),
+            "mdmc_batch_destroy": (None, [P]),
+            "mdmc_run_batch": (ctypes.c_int, [P, P, P, ctypes.c_int, P, P, P]),
+            "mdmc_batch_streams": (ctypes.c_int, [P]),
+            "mdmc_batch_context": (P, [P, ctypes.c_int]),
+            "mdmc_batch_last_error": (ctypes.c_char_p, [P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -379,6 +385,62 @@ class DualMarchingCubes:
     def write_obj(self, path):
         """Mesh::writeToFile, Mesh.cu:446-510"""
         self._ctx.check(self._ctx.lib.mdmc_write_obj(self._ctx.handle, str(path).encode()))
+
+
+class BatchedDualMarchingCubes:
+    """Many grids per call (mdmc_run_batch; no counterpart in the reference).
+    streams = 0 lets the first run pick the number of concurrent workers."""
+
+    def __init__(self, streams=0, **flags):
+        self.lib = library()
+        self.options = Options()
+        self.lib.mdmc_default_options(ctypes.byref(self.options))
+        for k, v in flags.items():
+            setattr(self.options, k, int(v))
+        self.handle = P()
+        st = self.lib.mdmc_batch_create(ctypes.byref(self.handle), ctypes.byref(self.options), int(streams))
+        if st != 0:
+            raise MDMCError(st, "mdmc_batch_create failed")
+        self.meshes = []
+        self.stats = []
+
+    def run(self, grids, iso_values, stream=None):
+        n = len(grids)
+        gs = (Grid * n)(*[g.grid if isinstance(g, UniformGrid) else g for g in grids])
+        isos = np.ascontiguousarray(iso_values, np.float32)
+        meshes = (Mesh * n)()
+        stats = (Stats * n)()
+        st = self.lib.mdmc_run_batch(self.handle, gs, _ptr(isos), n, meshes, stats, _stream_handle(stream))
+        if st != 0:
+            raise MDMCError(st, self.lib.mdmc_batch_last_error(self.handle).decode())
+        self.meshes, self.stats = list(meshes), list(stats)
+        return self.stats
+
+    @property
+    def streams(self):
+        return int(self.lib.mdmc_batch_streams(self.handle))
+
+    def get_halfedge_mesh(self, i):
+        """Grid i's mesh of the last batch, copied to host numpy arrays."""
+        ctx = self.lib.mdmc_batch_context(self.handle, int(i))
+        m = self.meshes[i]
+        V, F, H = int(m.num_vertices), int(m.num_faces), int(m.num_halfedges)
+        out = HalfedgeMesh(np.empty((V, 3), np.float32), np.empty((V, 3), np.float32), np.empty((F, 4), np.int32),
+                           np.empty((H, 4), np.int32), np.empty(F, np.int32), np.empty(F, np.uint16),
+                           np.empty(V, np.int32), np.empty(V, np.uint8))
+        st = self.lib.mdmc_download_mesh(ctx, _ptr(out.positions), _ptr(out.normals), _ptr(out.quads),
+                                         _ptr(out.halfedges), _ptr(out.face_first_halfedge),
+                                         _ptr(out.face_attributes), _ptr(out.vertex_halfedge), _ptr(out.vertex_flags),
+                                         None)
+        if st != 0:
+            raise MDMCError(st, self.lib.mdmc_last_error(ctx).decode())
+        return out
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            self.lib.mdmc_batch_destroy(h)
+            self.handle = None
 
 
 def case_tables():

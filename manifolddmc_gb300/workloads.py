@@ -21,6 +21,38 @@ def gaussian_blobs(n, count, sigma_range, seed, amplitude=1.0):
     return out.astype(np.float32)
 
 
+def gaussian_blobs_xyz(dims, count, sigma_range, seed, amplitude=1.0):
+    """Sum of `count` isotropic Gaussians on a grid of dims (X, Y, Z), array [Z, Y, X]."""
+    rng = np.random.default_rng(seed)
+    axes = [np.arange(d, dtype=np.float64) for d in dims]
+    out = np.zeros((dims[2], dims[1], dims[0]), np.float64)
+    for _ in range(count):
+        c = [rng.uniform(0.0, d - 1.0) for d in dims]
+        s = rng.uniform(sigma_range[0], sigma_range[1])
+        g = [np.exp(-((axes[k] - c[k]) ** 2) / (2.0 * s * s)) for k in range(3)]
+        out += amplitude * (g[2][:, None, None] * g[1][None, :, None] * g[0][None, None, :])
+    return out.astype(np.float32)
+
+
+def batch_grids(count=96, seed=4, dim_range=(24, 192)):
+    """The batched workload: `count` grids with dims drawn per axis uniformly
+    from dim_range, values 4-32 Gaussian blobs (sigma 2-8 cells) or iid
+    uniform noise (50/50), iso-values uniform in [0.3, 0.7].  Returns a list
+    of (array [Z, Y, X] float32, iso)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        dims = [int(x) for x in rng.integers(dim_range[0], dim_range[1] + 1, 3)]
+        iso = float(np.float32(rng.uniform(0.3, 0.7)))
+        sub = int(rng.integers(0, 2**31))
+        if rng.random() < 0.5:
+            vol = gaussian_blobs_xyz(dims, int(rng.integers(4, 33)), (2.0, 8.0), sub)
+        else:
+            vol = np.random.default_rng(sub).random((dims[2], dims[1], dims[0]), dtype=np.float32)
+        out.append((vol, iso))
+    return out
+
+
 def uniform_noise(n, seed):
     return np.random.default_rng(seed).random((n, n, n), dtype=np.float32)
 
