@@ -91,13 +91,12 @@ struct mdmc_context {
     bool simplified = false;  // a simplification renumbered the DMC vertices
     // simplification scratch
     DevBuf sVal, sCount, sType, sTarget, sClaimA, sClaimC, sMerge, sKeepV, sKeepF, sPos, sNrm, sQuads, sAttr;
-    // edge table
-    DevBuf table, nmList, heValence;
+    // edge buckets: per-vertex adjacency rows (destination, halfedge), the
+    // 4-face edge list, per-halfedge valence
+    DevBuf adjRow, adjCursor, adj, nmList, heValence;
     // quad -> owner cell; per-row active-cell mask (32 cells per word) and the
     // index of each word's first active cell; per active cell {contours, quads}
     DevBuf quadOwner, cellMask, cellFirst, cellCounts, cellIds;
-    bool tableValid = false;  // the edge table holds the current mesh (after a splitter refresh)
-    unsigned long long cap = 0;
     // counters
     DevBuf counters;
     DevCounters* hostCounters = nullptr;  // pinned
@@ -182,7 +181,6 @@ mdmc_status readInts(mdmc_context* c, const void* src, int n, cudaStream_t s) {
     return MDMC_OK;
 }
 
-unsigned long long tableCapacity(int64_t faces) { return (unsigned long long)roundUp((size_t)std::max<int64_t>(3 * faces, 64), 32); }
 
 // the view of a grid the kernels read; refined grids get their coarse-cell
 // pre-pass for this iso-value (mayCross bits in the context)
@@ -295,23 +293,36 @@ mdmc_status ensureMaps(mdmc_context* c, cudaStream_t s) {
     return MDMC_OK;
 }
 
-// rebuilds the edge table from all faces and refreshes the flags
-// (HalfedgeMesh::refreshHashTable, D/Halfedges/HalfedgeMesh.cu:1063-1100)
-mdmc_status refreshTable(mdmc_context* c, uint32_t* status, cudaStream_t s) {
-    c->cap = tableCapacity(c->F);
-    MDMC_CHECK(c, c->table.ensure(sizeof(Bucket) * c->cap));
-    MDMC_CHECK(c, cudaMemsetAsync(c->table.p, 0xFF, sizeof(Bucket) * c->cap, s));
+// Edge buckets of the current mesh from per-vertex adjacency rows: valences,
+// vertex and face flags, edge counters, the 4-face edge list, and (connect)
+// the twins of connectHalfedgeTwins (D/Halfedges/HalfedgeMesh.cu:92-291)
+mdmc_status edgeBuckets(mdmc_context* c, int connect, cudaStream_t s) {
+    DevCounters* ctr = c->counters.as<DevCounters>();
+    const MeshDims md{(int)c->V, (int)c->F, (int)c->H};
     MDMC_CHECK(c, c->nmList.ensure(sizeof(int4) * (size_t)(c->H / 4 + 1)));
     MDMC_CHECK(c, c->heValence.ensure((size_t)std::max<int64_t>(c->H, 1)));
-    const MeshDims md{(int)c->V, (int)c->F, (int)c->H};
-    launchInsertFaces(c->he.as<int4>(), c->faceFirst.as<int>(), md, c->table.as<Bucket>(), c->cap, status, s);
-    launchResetFaceFlags(c->faceAttr.as<uint16_t>(), (int)c->F, s);
-    MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, (size_t)c->V, s));
+    MDMC_CHECK(c, c->adjRow.ensure(sizeof(int) * (size_t)(c->V + 1)));
+    MDMC_CHECK(c, c->adjCursor.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
+    MDMC_CHECK(c, c->adj.ensure(sizeof(int2) * (size_t)std::max<int64_t>(c->H, 1)));
+    MDMC_CHECK(c, cudaMemsetAsync(c->adjRow.p, 0, sizeof(int) * (size_t)c->V, s));
+    launchDegree(c->he.as<int4>(), md, c->adjRow.as<int>(), &ctr->status, s);
+    mdmc_status st = scan<int>(c, c->adjRow.as<int>(), c->adjRow.as<int>(), c->V, s);
+    if (st != MDMC_OK) return st;
+    MDMC_CHECK(c, cudaMemsetAsync(c->adjCursor.p, 0, sizeof(int) * (size_t)c->V, s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)std::max<int64_t>(c->V, 1), 4), s));
     MDMC_CHECK(c, cudaMemsetAsync((char*)c->counters.p + 8, 0, sizeof(DevCounters) - 8, s));
-    launchBuckets(c->table.as<Bucket>(), c->cap, c->he.as<int4>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(),
-                  0, c->heValence.as<uint8_t>(), c->nmList.as<int4>(), c->counters.as<DevCounters>(), md, s);
-    c->tableValid = true;
+    launchEdgeBuckets(c->he.as<int4>(), md, c->adjRow.as<int>(), c->adjCursor.as<int>(), c->adj.as<int2>(), connect,
+                      c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(),
+                      c->nmList.as<int4>(), ctr, s);
     return MDMC_OK;
+}
+
+// HalfedgeMesh::refreshHashTable, D/Halfedges/HalfedgeMesh.cu:1063-1100: the
+// face flags are reset and every bucket and flag recomputed (twins kept)
+mdmc_status refreshTable(mdmc_context* c, uint32_t* status, cudaStream_t s) {
+    (void)status;
+    launchResetFaceFlags(c->faceAttr.as<uint16_t>(), (int)c->F, s);
+    return edgeBuckets(c, 0, s);
 }
 
 // simplify3X3Y (kind 0), simplify3X3YOld (kind 1), simplify3333 (kind 2),
@@ -378,18 +389,7 @@ mdmc_status runSimplification(mdmc_context* c, int kind, cudaStream_t s) {
     c->simplified = true;
     launchCollectHalfedges(c->sQuads.as<int4>(), c->sAttr.as<uint16_t>(), F2, c->he.as<int4>(), c->faceFirst.as<int>(),
                            c->faceAttr.as<uint16_t>(), s);
-    const MeshDims md2{V2, F2, 4 * F2};
-    c->cap = tableCapacity(F2);
-    MDMC_CHECK(c, c->table.ensure(sizeof(Bucket) * c->cap));
-    MDMC_CHECK(c, cudaMemsetAsync(c->table.p, 0xFF, sizeof(Bucket) * c->cap, s));
-    MDMC_CHECK(c, c->nmList.ensure(sizeof(int4) * (size_t)(F2 + 1)));
-    MDMC_CHECK(c, c->heValence.ensure((size_t)std::max(4 * F2, 1)));
-    MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)std::max(V2, 1), 4), s));
-    MDMC_CHECK(c, cudaMemsetAsync((char*)c->counters.p + 8, 0, sizeof(DevCounters) - 8, s));
-    launchInsertFaces(c->he.as<int4>(), c->faceFirst.as<int>(), md2, c->table.as<Bucket>(), c->cap, status, s);
-    launchBuckets(c->table.as<Bucket>(), c->cap, c->he.as<int4>(), c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), 1,
-                  c->heValence.as<uint8_t>(), c->nmList.as<int4>(), ctr, md2, s);
-    c->tableValid = true;
+    if ((st = edgeBuckets(c, 1, s)) != MDMC_OK) return st;
     MDMC_CHECK(c, cudaGetLastError());
     return MDMC_OK;
 }
@@ -762,7 +762,6 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->H = 4 * Q;
     c->dmcV = Vd;
     c->activeCells = A;
-    c->tableValid = false;
     MDMC_CHECK(c, c->quadOwner.ensure(sizeof(int) * (size_t)std::max<int64_t>(Q, 1)));
     MDMC_CHECK(c, c->pos.ensure(sizeof(float) * 3 * (size_t)Vd));
     MDMC_CHECK(c, c->nrm.ensure(sizeof(float) * 3 * (size_t)Vd));
@@ -827,8 +826,8 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
 
     // ---- outputs and statistics -------------------------------------------------
     MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)std::max<int64_t>(c->F, 1)));
-    launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), mdF, c->tableValid ? c->table.as<Bucket>() : nullptr, c->cap,
-                 c->heValence.as<uint8_t>(), c->quads.as<int4>(), c->vertexHE.as<int>(),
+    launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), mdF, c->heValence.as<uint8_t>(), c->quads.as<int4>(),
+                 c->vertexHE.as<int>(),
                  c->opt.detect_non_manifold_vertices != 0, ctr, status, s);
     cudaEventRecord(c->ev[5], s);
     MDMC_CHECK(c, cudaGetLastError());

@@ -20,7 +20,6 @@
 #include <cuda_runtime.h>
 
 #include "mdmc_device.cuh"
-#include "mdmc_edge_hash.cuh"
 #include "mdmc_kernels.h"
 
 namespace mdmc {

@@ -111,10 +111,10 @@ void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, con
                  uint8_t* vflags, uint8_t* heValence, int4* nmList, int nmCapacity, int numQuads, int numVertices,
                  DevCounters* ctr, cudaStream_t s);
 
-void launchBuckets(Bucket* table, unsigned long long cap, int4* he, uint16_t* faceAttr, uint8_t* vflags,
-                   int connectTwins, uint8_t* heValence, int4* nmList, DevCounters* ctr, MeshDims md, cudaStream_t s);
-void launchInsertFaces(const int4* he, const int* faceFirst, MeshDims md, Bucket* table, unsigned long long cap,
-                       uint32_t* status, cudaStream_t s);
+void launchDegree(const int4* he, MeshDims md, int* deg, uint32_t* status, cudaStream_t s);
+void launchEdgeBuckets(int4* he, MeshDims md, const int* rowStart, int* cursor, int2* adj, int connectTwins,
+                       uint16_t* faceAttr, uint8_t* vflags, uint8_t* heValence, int4* nmList, DevCounters* ctr,
+                       cudaStream_t s);
 void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s);
 void launchReconnect(const GridDesc& g, float iso, const int4* nmList, const DevCounters* ctr,
                      int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s);
@@ -122,9 +122,8 @@ void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cuda
 void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, uint8_t* slow, uint8_t* isKey,
                       int* fans, uint8_t* vflags, DevCounters* ctr,
                       uint32_t* status, cudaStream_t s);
-void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const Bucket* table, unsigned long long cap,
-                  const uint8_t* heValence, int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr,
-                  uint32_t* status, cudaStream_t s);
+void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, int4* quads,
+                  int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s);
 
 // valence-pattern simplifications
 void launchValence(const int4* he, MeshDims md, int* val, cudaStream_t s);

@@ -13,129 +13,11 @@
 #include <cuda_runtime.h>
 
 #include "mdmc_device.cuh"
-#include "mdmc_edge_hash.cuh"
 #include "mdmc_kernels.h"
 
 namespace mdmc {
 
 __device__ __forceinline__ void setTwin(int4* he, int h, int t) { reinterpret_cast<int*>(he)[4 * (int64_t)h + 3] = t; }
-
-// Sorts each bucket's ids, then (connectTwins) pairs twins as
-// connectHalfedgeTwins does, and sets the face and vertex flags of
-// refreshFaceFlagsGPU / refresh{NonManifold,Weird,Boundary}Flags.  Buckets
-// with at least four ids go to nmList (isHashTableEntryNonManifold).
-__global__ void kBuckets(Bucket* __restrict__ table, unsigned long long cap, int4* __restrict__ he, uint16_t* faceAttr,
-                         uint8_t* vflags, int connectTwins, uint8_t* __restrict__ heValence, int4* __restrict__ nmList,
-                         DevCounters* ctr, MeshDims md) {
-    int nE = 0, nE3 = 0, nE4 = 0;
-    for (unsigned long long i = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; i < cap;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        Bucket b = table[i];
-        if (b.key == kEmptyKey) continue;
-        const int count = b.cnt + 1;
-        const int n = count < 4 ? count : 4;
-        int* e = b.ids;
-        // insertion sort of at most four ids
-        for (int a = 1; a < n; ++a) {
-            int v = e[a], k = a - 1;
-            while (k >= 0 && e[k] > v) { e[k + 1] = e[k]; --k; }
-            e[k + 1] = v;
-        }
-        if (n > 1) {
-            int4 ids = make_int4(e[0], e[1], e[2], e[3]);
-            *reinterpret_cast<int4*>(&table[i].ids[0]) = ids;
-        }
-        bool ok = true;
-        for (int k = 0; k < n; ++k) {
-            ok = ok && inb(e[k], md.H);
-            if (ok) {
-                const int4 h = he[e[k]];
-                ok = inb(h.x, md.V) && inb(h.y, md.F);
-            }
-        }
-        if (!ok) {
-            atomicOr(&ctr->status, kStatusBadIndex);
-            continue;
-        }
-        for (int k = 0; k < n; ++k) heValence[e[k]] = (uint8_t)(count < 255 ? count : 255);
-        ++nE;
-        if (count == 3) ++nE3;
-        if (count == 4) ++nE4;
-        if (count >= 4) {
-            const unsigned long long slot = atomicAdd(&ctr->nmBuckets, 1ULL);
-            if (slot < (unsigned long long)(md.H / 4 + 1)) nmList[slot] = make_int4(e[0], e[1], e[2], e[3]);
-            else atomicOr(&ctr->status, kStatusBadIndex);
-        }
-        if (connectTwins) {
-            if (count == 2) {
-                setTwin(he, e[0], e[1]);
-                setTwin(he, e[1], e[0]);
-            } else if (count == 3) {
-                setTwin(he, e[0], e[1]);
-                setTwin(he, e[1], e[2]);
-                setTwin(he, e[2], e[0]);
-            } else if (count == 4) {  // "HACKY_OLD_WAY", HalfedgeMesh.cu:250-281
-                const int v0 = he[e[0]].x, v1 = he[e[1]].x, v2 = he[e[2]].x;
-                if (v0 != v1) {
-                    setTwin(he, e[0], e[1]); setTwin(he, e[1], e[0]);
-                    setTwin(he, e[2], e[3]); setTwin(he, e[3], e[2]);
-                } else if (v0 != v2) {
-                    setTwin(he, e[0], e[2]); setTwin(he, e[2], e[0]);
-                    setTwin(he, e[1], e[3]); setTwin(he, e[3], e[1]);
-                } else {
-                    setTwin(he, e[0], e[3]); setTwin(he, e[3], e[0]);
-                    setTwin(he, e[1], e[2]); setTwin(he, e[2], e[1]);
-                }
-            }
-        }
-        if (count == 4)
-            for (int k = 0; k < 4; ++k) orFaceAttr(faceAttr, he[e[k]].y, MDMC_FACE_NON_MANIFOLD);
-        if (count == 4)
-            for (int k = 0; k < 4; ++k) orVertexFlag(vflags, he[e[k]].x, MDMC_VERTEX_NON_MANIFOLD);
-        if (count == 3)
-            for (int k = 0; k < 3; ++k) orVertexFlag(vflags, he[e[k]].x, MDMC_VERTEX_WEIRD);
-        if (count == 1) orVertexFlag(vflags, he[e[0]].x, MDMC_VERTEX_BOUNDARY);
-    }
-    blockAddTo(&ctr->edges, nE);
-    blockAddTo(&ctr->edges3, nE3);
-    blockAddTo(&ctr->edges4, nE4);
-}
-
-void launchBuckets(Bucket* table, unsigned long long cap, int4* he, uint16_t* faceAttr, uint8_t* vflags,
-                   int connectTwins, uint8_t* heValence, int4* nmList, DevCounters* ctr, MeshDims md, cudaStream_t s) {
-    unsigned long long blocks = (cap + 255) / 256;
-    if (blocks > 152ULL * 16) blocks = 152ULL * 16;
-    if (blocks == 0) blocks = 1;
-    countLaunch();
-    kBuckets<<<(unsigned)blocks, 256, 0, s>>>(table, cap, he, faceAttr, vflags, connectTwins, heValence, nmList, ctr, md);
-}
-
-// refreshHashTableGPU, D/Halfedges/HalfedgeMesh.cu:62-90
-__global__ void kInsertFaces(const int4* __restrict__ he, const int* __restrict__ faceFirst, MeshDims md,
-                             Bucket* table, unsigned long long cap, uint32_t* status) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= md.F) return;
-    int h = faceFirst[f];
-    int q[4], hs[4];
-    for (int i = 0; i < 4; ++i) {
-        if (!inb(h, md.H)) {
-            atomicOr(status, kStatusBadIndex);
-            return;
-        }
-        int4 e = he[h];
-        q[i] = e.x;
-        hs[i] = h;
-        h = e.z;
-    }
-    for (int i = 0; i < 4; ++i) edgeInsert(table, cap, q[i], q[(i + 1) & 3], hs[i], status);
-}
-
-void launchInsertFaces(const int4* he, const int* faceFirst, MeshDims md, Bucket* table, unsigned long long cap,
-                       uint32_t* status, cudaStream_t s) {
-    if (md.F <= 0) return;
-    countLaunch();
-    kInsertFaces<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, table, cap, status);
-}
 
 // face attributes: clearPatternFlags + unsetNonManifoldFlag (HalfedgeMesh.cu:1050-1055)
 __global__ void kResetFaceFlags(uint16_t* attr, int numFaces) {
@@ -147,6 +29,132 @@ void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s) {
         countLaunch();
         kResetFaceFlags<<<(numFaces + 255) / 256, 256, 0, s>>>(attr, numFaces);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Edge buckets without a hash table: the halfedges of the vertex pair {a, b}
+// all leave a or b, so with every vertex's outgoing halfedges listed as
+// (destination, id) rows, a halfedge finds its bucket by scanning two short
+// rows.  Same buckets, counts and flags as the edge table of
+// refreshHashTable / connectHalfedgeTwins (D/Halfedges/HalfedgeMesh.cu:62-291,
+// :1063-1100); a bucket keeps its 4 smallest ids.
+// ---------------------------------------------------------------------------
+__global__ void kDegree(const int4* __restrict__ he, MeshDims md, int* __restrict__ deg, uint32_t* status) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= md.H) return;
+    const int v = he[h].x;
+    if (inb(v, md.V)) atomicAdd(&deg[v], 1);
+    else atomicOr(status, kStatusBadIndex);
+}
+
+__global__ void kAdjScatter(const int4* __restrict__ he, MeshDims md, const int* __restrict__ rowStart,
+                            int* __restrict__ cursor, int2* __restrict__ adj, uint32_t* status) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= md.H) return;
+    const int4 e = he[h];
+    if (!inb(e.x, md.V)) return;
+    const int dest = inb(e.z, md.H) ? he[e.z].x : -1;
+    const int pos = rowStart[e.x] + atomicAdd(&cursor[e.x], 1);
+    if (pos < rowStart[e.x + 1]) adj[pos] = make_int2(dest, h);
+    else atomicOr(status, kStatusBadIndex);
+}
+
+__device__ __forceinline__ void keepSmallest(int ids[4], int g) {
+    if (g >= ids[3]) return;
+    int k = 3;
+    while (k > 0 && ids[k - 1] > g) {
+        ids[k] = ids[k - 1];
+        --k;
+    }
+    ids[k] = g;
+}
+
+__global__ void kEdgeBuckets(int4* __restrict__ he, MeshDims md, const int* __restrict__ rowStart,
+                             const int2* __restrict__ adj, int connectTwins, uint16_t* faceAttr, uint8_t* vflags,
+                             uint8_t* __restrict__ heValence, int4* __restrict__ nmList, DevCounters* ctr) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    int nE = 0, nE3 = 0, nE4 = 0;
+    if (h < md.H) {
+        const int4 e = he[h];
+        const int a = e.x;
+        const int b = (inb(e.z, md.H) && inb(a, md.V)) ? he[e.z].x : -1;
+        if (!inb(b, md.V)) {
+            atomicOr(&ctr->status, kStatusBadIndex);
+        } else {
+            int ids[4] = {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF};
+            int cnt = 0;
+            for (int j = rowStart[a], je = rowStart[a + 1]; j < je; ++j) {
+                const int2 r = adj[j];
+                if (r.x == b) {
+                    ++cnt;
+                    keepSmallest(ids, r.y);
+                }
+            }
+            if (a != b)
+                for (int j = rowStart[b], je = rowStart[b + 1]; j < je; ++j) {
+                    const int2 r = adj[j];
+                    if (r.x == a) {
+                        ++cnt;
+                        keepSmallest(ids, r.y);
+                    }
+                }
+            int me = 4;
+            for (int k = 3; k >= 0; --k)
+                if (ids[k] == h) me = k;
+            heValence[h] = (uint8_t)(cnt < 255 ? cnt : 255);
+            if (connectTwins && me < 4) {
+                int twin = -1;
+                if (cnt == 2) {
+                    twin = ids[1 - me];
+                } else if (cnt == 3) {
+                    twin = ids[me == 2 ? 0 : me + 1];
+                } else if (cnt == 4) {  // "HACKY_OLD_WAY", HalfedgeMesh.cu:250-281
+                    const int v0 = he[ids[0]].x, v1 = he[ids[1]].x, v2 = he[ids[2]].x;
+                    const int partner = v0 != v1 ? (me ^ 1) : (v0 != v2 ? (me ^ 2) : 3 - me);
+                    twin = ids[partner];
+                }
+                if (cnt >= 2 && cnt <= 4) setTwin(he, h, twin);
+            }
+            if (cnt == 4) {
+                orFaceAttr(faceAttr, e.y, MDMC_FACE_NON_MANIFOLD);
+                orVertexFlag(vflags, a, MDMC_VERTEX_NON_MANIFOLD);
+            } else if (cnt == 3) {
+                orVertexFlag(vflags, a, MDMC_VERTEX_WEIRD);
+            } else if (cnt == 1) {
+                orVertexFlag(vflags, a, MDMC_VERTEX_BOUNDARY);
+            }
+            if (me == 0) {  // the bucket's smallest halfedge counts it
+                ++nE;
+                if (cnt == 3) ++nE3;
+                if (cnt == 4) ++nE4;
+                if (cnt > 4) atomicOr(&ctr->status, kStatusBucketOverflow);
+                if (cnt >= 4) {
+                    const unsigned long long slot = atomicAdd(&ctr->nmBuckets, 1ULL);
+                    if (slot < (unsigned long long)(md.H / 4 + 1)) nmList[slot] = make_int4(ids[0], ids[1], ids[2], ids[3]);
+                    else atomicOr(&ctr->status, kStatusBadIndex);
+                }
+            }
+        }
+    }
+    blockAddTo(&ctr->edges, nE);
+    blockAddTo(&ctr->edges3, nE3);
+    blockAddTo(&ctr->edges4, nE4);
+}
+
+void launchDegree(const int4* he, MeshDims md, int* deg, uint32_t* status, cudaStream_t s) {
+    if (md.H <= 0) return;
+    countLaunch();
+    kDegree<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, deg, status);
+}
+
+void launchEdgeBuckets(int4* he, MeshDims md, const int* rowStart, int* cursor, int2* adj, int connectTwins,
+                       uint16_t* faceAttr, uint8_t* vflags, uint8_t* heValence, int4* nmList, DevCounters* ctr,
+                       cudaStream_t s) {
+    if (md.H <= 0) return;
+    countLaunch(2);
+    kAdjScatter<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, rowStart, cursor, adj, &ctr->status);
+    kEdgeBuckets<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, rowStart, adj, connectTwins, faceAttr, vflags, heValence,
+                                                    nmList, ctr);
 }
 
 // ---------------------------------------------------------------------------
@@ -460,7 +468,6 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
 // smallest outgoing halfedge of every vertex
 // ---------------------------------------------------------------------------
 __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__ faceFirst, MeshDims md,
-                            const Bucket* __restrict__ table, unsigned long long cap,
                             const uint8_t* __restrict__ heValence, int4* __restrict__ quads, DevCounters* ctr) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     int cnt = -1;
@@ -481,7 +488,7 @@ __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__
         if (ok) {
             cnt = 0;
             for (int i = 0; i < 4; ++i)
-                if ((table ? edgeValence(table, cap, q[i], q[(i + 1) & 3]) : (int)heValence[hs[i]]) > 2) ++cnt;
+                if (heValence[hs[i]] > 2) ++cnt;
         } else {
             atomicOr(&ctr->status, kStatusBadIndex);
         }
@@ -494,13 +501,12 @@ __global__ void kVertexHalfedgeFix(int* vertexHE, int numVertices) {
     if (v < numVertices && vertexHE[v] == 0x7F7F7F7F) vertexHE[v] = -1;
 }
 
-void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const Bucket* table, unsigned long long cap,
-                  const uint8_t* heValence, int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr,
-                  uint32_t* status, cudaStream_t s) {
+void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, int4* quads,
+                  int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
     (void)status;
     if (md.F > 0) {
         countLaunch();
-        kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, table, cap, heValence, quads, ctr);
+        kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, heValence, quads, ctr);
     }
     if (md.V > 0 && !vertexHEDone) {
         launchVertexStar(he, md, vertexHE, nullptr, s);

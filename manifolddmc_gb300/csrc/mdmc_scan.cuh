@@ -14,7 +14,7 @@ namespace mdmc {
 constexpr int kScanThreads = 512;
 constexpr int kScanItems = 4;
 constexpr int kScanTile = kScanThreads * kScanItems;
-constexpr int kScanMaxTiles = 1024 * 16;  // largest tile-sum array one block scans
+constexpr int kScanMaxTiles = 1 << 20;  // largest tile-sum array the one-block pass scans (2^31 elements)
 
 template <typename T>
 struct ScanOps;

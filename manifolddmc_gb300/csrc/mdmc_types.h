@@ -11,7 +11,7 @@ namespace mdmc {
 // Device status bits.  Kernels never trap: a hit limit sets a bit, the kernel
 // skips the offending element and the host reports the bits after the run.
 enum : uint32_t {
-    kStatusProbeLimit = 1u << 0,       // edge hash: probe limit reached
+    kStatusProbeLimit = 1u << 0,       // reserved (no probing structure is left)
     kStatusSlotConflict = 1u << 1,     // two cells claimed the same quad slot
     kStatusBucketOverflow = 1u << 2,   // more than 4 halfedges on one edge
     kStatusPartnerOverflow = 1u << 3,  // merge list longer than the reference's
@@ -32,21 +32,6 @@ __host__ __device__ __forceinline__ bool inb(long long i, long long n) { return 
 struct MeshDims {
     int V, F, H;
 };
-
-// Edge hash bucket: 32 bytes, one sector.  key = concatenateKeys(min, max)
-// (D/Utils/Utilities.h:15-22); cnt stores count-1 so that an all-0xFF memset
-// yields an empty bucket (key ~0, count 0, ids -1).  The ids come first so
-// that they can be read and written as one 16-byte-aligned int4.
-struct __align__(32) Bucket {
-    int ids[4];
-    unsigned long long key;
-    int cnt;
-    int pad;
-};
-static_assert(sizeof(Bucket) == 32, "bucket is one 32-byte sector");
-static_assert(offsetof(Bucket, ids) == 0 && offsetof(Bucket, key) == 16 && offsetof(Bucket, cnt) == 24,
-              "bucket layout");
-constexpr unsigned long long kEmptyKey = ~0ULL;
 
 // Active cell record written by the DMC emit pass (16 bytes):
 //   cell  = linear sample index of the cell's corner 0

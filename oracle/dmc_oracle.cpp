@@ -399,10 +399,17 @@ struct Result {
 struct EdgeTable {
     std::unordered_map<uint64_t, Bucket> map;
     uint32_t anomalies = 0;
+    // keeps the 4 smallest ids of a bucket (the reference keeps the first 4
+    // inserted, in atomic order); more than 4 faces on one edge is an anomaly
     void insert(int a, int b, int h) {
         Bucket& bk = map[edgeKey(a, b)];
-        if (bk.count < 4) bk.ids[bk.count] = h;
-        else anomalies |= kSBucket;  // more than 4 faces on one edge
+        if (bk.count < 4) {
+            bk.ids[bk.count] = h;
+        } else {
+            anomalies |= kSBucket;
+            int* mx = std::max_element(bk.ids, bk.ids + 4);
+            if (h < *mx) *mx = h;
+        }
         ++bk.count;
     }
     void finish() {
