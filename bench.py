@@ -418,15 +418,21 @@ def measure_batch(args, dev):
             "batch_mcells_s": round(cells / b / 1e6, 1), "sequential_mcells_s": round(cells / s / 1e6, 1)}
 
 
-def cpu_sample(config):
-    """A bounded slab of the workload for the CPU timings: the first quarter of
-    the input's z-planes (refined as in the full workload)."""
+def cpu_sample(config, fraction=1):
+    """The workload for the CPU timings: the whole input (fraction 1), or its
+    first 1/fraction of the z-planes, refined as in the GPU workload."""
     from manifolddmc_gb300.workloads import CONFIGS
     desc, gen, iso, refine, pad = CONFIGS[config]
     vol = gen()
-    nz = max(2, vol.shape[0] // 4 + 1)
+    nz = vol.shape[0] if fraction <= 1 else max(2, vol.shape[0] // fraction + 1)
     sub = np.ascontiguousarray(vol[:nz])
     return sub, [sub.shape[2], sub.shape[1], sub.shape[0]], iso, refine, pad
+
+
+def cpu_threads():
+    """Host threads the oracle's OpenMP regions use (OMP_NUM_THREADS, else every core)."""
+    env = os.environ.get("OMP_NUM_THREADS")
+    return int(env) if env and env.isdigit() else (os.cpu_count() or 1)
 
 
 def time_oracle(sub, dims, iso, refine, pad):
@@ -445,8 +451,9 @@ def time_oracle(sub, dims, iso, refine, pad):
 def cpu_baseline(config):
     sub, dims, iso, refine, pad = cpu_sample(config)
     cells, dt, _ = time_oracle(sub, dims, iso, refine, pad)
-    return {"value": round(cells / dt / 1e6, 3), "unit": "Mcells/s", "cores": 1, "kind": "port",
-            "sample": "CPU oracle (C++ restatement, 1 thread) on the first %d of %d input z-planes: %d cells, %.2f s"
+    return {"value": round(cells / dt / 1e6, 3), "unit": "Mcells/s", "cores": cpu_threads(), "kind": "port",
+            "sample": "CPU oracle (C++ restatement; OpenMP over z-slabs for refinement and DMC, the halfedge build and "
+                      "repair serial) on the whole workload: %d of %d input z-planes, %d cells, one run, %.2f s"
                       % (dims[2], dims[0], cells, dt)}
 
 
@@ -463,15 +470,16 @@ def run_reference(args, rank, world):
     ms = float(np.mean(times)) * 1e3
     value = cells / (ms / 1e3) / 1e6
     sample = ("the reference's path has no CPU implementation and does not build on this image (CUDA-only, "
-              "MSVC/OpenGL dependencies); its C++ restatement (oracle/) runs on 1 host thread over the first %d of "
-              "%d input z-planes (%d cells per step)" % (dims[2], dims[0], cells))
+              "MSVC/OpenGL dependencies); its C++ restatement (oracle/) runs with OpenMP on %d host threads "
+              "(refinement and DMC in z-slabs, halfedge build and repair serial) over the whole workload, %d of %d "
+              "input z-planes (%d cells per step)" % (cpu_threads(), dims[2], dims[0], cells))
     from manifolddmc_gb300.workloads import CONFIGS
     line = {"impl": "reference", "metric": "Mcells/s (DMC + manifold repair, 512^3-cell refined grid)",
             "value": round(value, 3), "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 2), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian blobs)",
             "config": {"workload": args.config, "description": CONFIGS[args.config][0]},
-            "cpu_baseline": {"value": round(value, 3), "unit": "Mcells/s", "cores": 1, "kind": "port",
+            "cpu_baseline": {"value": round(value, 3), "unit": "Mcells/s", "cores": cpu_threads(), "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 3), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))

@@ -200,6 +200,15 @@ MDMC_API mdmc_status mdmc_download_mesh(mdmc_context* context, float* positions,
                                uint16_t* face_attributes, int32_t* vertex_halfedge,
                                uint8_t* vertex_flags, void* stream);
 
+/* HalfedgeMesh::toVertexAndIndexBuffer (Halfedges/HalfedgeMesh.cu:1102-1146)
+ * into device arrays instead of GL buffers (either may be NULL): vertices gets
+ * 10 floats per vertex {position[3], normal[3], rgba[4]} with the reference's
+ * flag colours (insertVertices :716-760; a vertex without halfedges gets the
+ * default Vertex of Mesh.h:15-19: NaN position and normal, magenta), indices
+ * gets 6 per face, the triangles (x, y, z) and (z, w, x) of the face's quad
+ * (insertHalfedgeFaceIndices :690-714).  Asynchronous on the stream. */
+MDMC_API mdmc_status mdmc_render_buffers(mdmc_context* context, float* vertices, uint32_t* indices, void* stream);
+
 /* Writes the last run's mesh as OBJ the way Mesh::writeToFile does
  * (Mesh.cu:446-510): v, vn, then one "f a//a b//b c//c d//d" line per face. */
 MDMC_API mdmc_status mdmc_write_obj(mdmc_context* context, const char* path);

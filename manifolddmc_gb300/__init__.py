@@ -126,6 +126,7 @@ def library():
             "mdmc_last_error": (ctypes.c_char_p, [P]),
             "mdmc_case_tables": (None, [P, P]),
             "mdmc_backward": (ctypes.c_int, [P, P, P, ctypes.c_int, P]),
+            "mdmc_render_buffers": (ctypes.c_int, [P, P, P, P]),
             "mdmc_batch_create": (ctypes.c_int, [P, P, ctypes.c_int]),
             "mdmc_batch_destroy": (None, [P]),
             "mdmc_run_batch": (ctypes.c_int, [P, P, P, ctypes.c_int, P, P, P]),
@@ -381,6 +382,21 @@ class DualMarchingCubes:
         Needs a run with enable_surface_to_vertex_iteration = 0."""
         self._ctx.check(self._ctx.lib.mdmc_backward(self._ctx.handle, _dev_ptr(dl_dpositions), _dev_ptr(dl_dsamples),
                                                     int(bool(accumulate)), _stream_handle(stream)))
+
+    def render_buffers(self, vertices=None, indices=None, stream=None):
+        """HalfedgeMesh::toVertexAndIndexBuffer (HalfedgeMesh.cu:1102-1146) into
+        CUDA tensors: vertices [V, 10] float32 (position, normal, rgba) and
+        indices [F * 6] uint32 (two triangles per quad).  Allocates them when
+        not given."""
+        import torch
+        V, F = int(self.mesh.num_vertices), int(self.mesh.num_faces)
+        if vertices is None:
+            vertices = torch.empty((V, 10), dtype=torch.float32, device="cuda")
+        if indices is None:
+            indices = torch.empty(6 * F, dtype=torch.int32, device="cuda")
+        self._ctx.check(self._ctx.lib.mdmc_render_buffers(self._ctx.handle, _dev_ptr(vertices), _dev_ptr(indices),
+                                                          _stream_handle(stream)))
+        return vertices, indices
 
     def write_obj(self, path):
         """Mesh::writeToFile, Mesh.cu:446-510"""

@@ -949,6 +949,17 @@ mdmc_status mdmc_backward(mdmc_context* c, const float* dl_dpositions, float* dl
     return MDMC_OK;
 }
 
+mdmc_status mdmc_render_buffers(mdmc_context* c, float* vertices, uint32_t* indices, void* stream) {
+    if (!c) return MDMC_ERROR_INVALID_ARGUMENT;
+    c->err.clear();
+    (void)cudaGetLastError();
+    if (!c->haveMesh) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "no mesh: run first");
+    launchRenderBuffers(c->pos.as<float>(), c->nrm.as<float>(), c->vflags.as<uint8_t>(), c->vertexHE.as<int>(),
+                        (int)c->V, c->quads.as<int4>(), (int)c->F, vertices, indices, (cudaStream_t)stream);
+    MDMC_CHECK(c, cudaGetLastError());
+    return MDMC_OK;
+}
+
 mdmc_status mdmc_write_obj(mdmc_context* c, const char* path) {
     if (!c || !path || !c->haveMesh) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "no mesh or path");
     std::vector<float> p(3 * (size_t)c->V), n(3 * (size_t)c->V);

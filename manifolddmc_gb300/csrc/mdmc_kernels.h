@@ -147,6 +147,9 @@ void launchGatherParents(const float* dlDpos, int numVertices, int dmcVertices, 
 void launchBackwardCells(const GridDesc& g, float iso, const ActiveCell* act, int numActive, const float* vertexGrad,
                          int dmcVertices, float* dlDsamples, uint32_t* status, cudaStream_t s);
 
+void launchRenderBuffers(const float* pos, const float* nrm, const uint8_t* vflags, const int* vertexHE, int numVertices,
+                         const int4* quads, int numFaces, float* vertices, uint32_t* indices, cudaStream_t s);
+
 void launchFlagNMFaces(const uint16_t* attr, int numFaces, int* flags, cudaStream_t s);
 void launchCompactNMFaces(const int* flags, const int* offsets, int numFaces, int* nmFaces, cudaStream_t s);
 void launchFillInt(int* p, int64_t n, int v, cudaStream_t s);

@@ -515,4 +515,84 @@ void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8
     }
 }
 
+// ---------------------------------------------------------------------------
+// HalfedgeMesh::toVertexAndIndexBuffer, D/Halfedges/HalfedgeMesh.cu:1102-1146
+// (insertVertices :716-760, insertHalfedgeFaceIndices :690-714), with device
+// arrays in place of the GL buffers: per vertex {position, normal, rgba}
+// coloured by its flags, per quad the triangles (x, y, z) and (z, w, x)
+// ---------------------------------------------------------------------------
+// LazyEngine::Color::HSVtoRGB (Renderer/Materials/Colors.h:15-57)
+__device__ __forceinline__ F3 hsvToRgb(float h, float s, float v) {
+    float f = h / 60.0f;
+    const float hi = floorf(f);
+    f = f - hi;
+    const float p = v * (1 - s);
+    const float q = v * (1 - s * f);
+    const float t = v * (1 - s * (1 - f));
+    if (hi == 0.0f || hi == 6.0f) return f3(v, t, p);
+    if (hi == 1.0f) return f3(q, v, p);
+    if (hi == 2.0f) return f3(p, v, t);
+    if (hi == 3.0f) return f3(p, q, v);
+    if (hi == 4.0f) return f3(t, p, v);
+    return f3(v, p, q);
+}
+
+__global__ void kRenderVertices(const float* __restrict__ pos, const float* __restrict__ nrm,
+                                const uint8_t* __restrict__ vflags, const int* __restrict__ vertexHE, int numVertices,
+                                float* __restrict__ out) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= numVertices) return;
+    float* o = out + 10 * (int64_t)v;
+    if (vertexHE[v] < 0) {  // no halfedge writes it: the default Vertex (Mesh.h:15-19)
+        for (int a = 0; a < 6; ++a) o[a] = __int_as_float(0x7fc00000);
+        o[6] = 1.f;
+        o[7] = 0.f;
+        o[8] = 1.f;
+        o[9] = 1.f;
+        return;
+    }
+    const uint32_t fl = vflags[v];
+    const bool nm = fl & MDMC_VERTEX_NON_MANIFOLD, weird = fl & MDMC_VERTEX_WEIRD, fans = fl & MDMC_VERTEX_MULTIPLE_FANS;
+    float hue = 180.f;
+    if (nm) hue = 0.f;
+    if (weird) hue = 60.f;
+    if (fans) hue = 270.f;
+    if (weird && nm) hue = 300.f;
+    if (nm && fans) hue = 240.f;
+    const F3 c = hsvToRgb(hue, 0.8f, 0.8f);
+    for (int a = 0; a < 3; ++a) {
+        o[a] = pos[3 * (int64_t)v + a];
+        o[3 + a] = nrm[3 * (int64_t)v + a];
+    }
+    o[6] = c.x;
+    o[7] = c.y;
+    o[8] = c.z;
+    o[9] = 1.f;
+}
+
+__global__ void kRenderIndices(const int4* __restrict__ quads, int numFaces, uint32_t* __restrict__ out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= numFaces) return;
+    const int4 q = quads[f];
+    uint32_t* o = out + 6 * (int64_t)f;
+    o[0] = (uint32_t)q.x;
+    o[1] = (uint32_t)q.y;
+    o[2] = (uint32_t)q.z;
+    o[3] = (uint32_t)q.z;
+    o[4] = (uint32_t)q.w;
+    o[5] = (uint32_t)q.x;
+}
+
+void launchRenderBuffers(const float* pos, const float* nrm, const uint8_t* vflags, const int* vertexHE, int numVertices,
+                         const int4* quads, int numFaces, float* vertices, uint32_t* indices, cudaStream_t s) {
+    if (vertices && numVertices > 0) {
+        countLaunch();
+        kRenderVertices<<<(numVertices + 255) / 256, 256, 0, s>>>(pos, nrm, vflags, vertexHE, numVertices, vertices);
+    }
+    if (indices && numFaces > 0) {
+        countLaunch();
+        kRenderIndices<<<(numFaces + 255) / 256, 256, 0, s>>>(quads, numFaces, indices);
+    }
+}
+
 }  // namespace mdmc

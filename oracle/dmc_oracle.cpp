@@ -20,6 +20,9 @@
 #include <cstdio>
 #include <cstring>
 #include <unordered_map>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <vector>
 
 namespace oracle {
@@ -106,6 +109,7 @@ static void refine(const Grid& in, int r, bool pad, std::vector<float>& out, int
     }
     out.assign((size_t)od[0] * od[1] * od[2], 0.f);
     const float f = (float)(r + 1);
+#pragma omp parallel for schedule(static)
     for (int z = 0; z < od[2]; ++z)
         for (int y = 0; y < od[1]; ++y)
             for (int x = 0; x < od[0]; ++x) {
@@ -524,13 +528,20 @@ struct QuadEntry {
     int color = (int)kAttrInvalidColor;
 };
 
-static void runDMC(const Grid& g, float iso, bool surfaceIteration, std::vector<float>& pos,
-                   std::vector<float>& nrm, std::vector<int>& quads, std::vector<uint16_t>& attr,
-                   std::vector<int>& cells, std::vector<uint16_t>& edgeMasks, uint32_t& anomalies) {
-    const int X = g.d[0], Y = g.d[1], Z = g.d[2];
+// One z-slab of cells [z0, z1): vertices numbered from 0 within the slab,
+// quad slots keyed by the global edge key.
+struct SlabDMC {
+    std::vector<float> pos, nrm;
+    std::vector<int> cells;
+    std::vector<uint16_t> edgeMasks;
     std::unordered_map<uint64_t, QuadEntry> table;
+    uint32_t anomalies = 0;
+};
+
+static void runDMCSlab(const Grid& g, float iso, bool surfaceIteration, int z0, int z1, SlabDMC& out) {
+    const int X = g.d[0], Y = g.d[1];
     V3 origin = g.o(), dl = g.dl();
-    for (int z = 0; z + 1 < Z; ++z)
+    for (int z = z0; z < z1; ++z)
         for (int y = 0; y + 1 < Y; ++y)
             for (int x = 0; x + 1 < X; ++x) {
                 float s[8];
@@ -564,21 +575,21 @@ static void runDMC(const Grid& g, float iso, bool surfaceIteration, std::vector<
                     }
                     V3 nm = normalize(trilinear3(normals, p));
                     V3 wp = add(origin, mul(add(v3((float)x, (float)y, (float)z), p), dl));
-                    int vid = (int)(pos.size() / 3);
-                    pos.push_back(wp.x); pos.push_back(wp.y); pos.push_back(wp.z);
-                    nrm.push_back(nm.x); nrm.push_back(nm.y); nrm.push_back(nm.z);
-                    cells.push_back(x); cells.push_back(y); cells.push_back(z);
+                    int vid = (int)(out.pos.size() / 3);
+                    out.pos.push_back(wp.x); out.pos.push_back(wp.y); out.pos.push_back(wp.z);
+                    out.nrm.push_back(nm.x); out.nrm.push_back(nm.y); out.nrm.push_back(nm.z);
+                    out.cells.push_back(x); out.cells.push_back(y); out.cells.push_back(z);
                     uint16_t mask = 0;
                     for (int i = 0; i < sz; ++i) mask |= (uint16_t)(1u << contourEdge(c, t, i));
-                    edgeMasks.push_back(mask);
+                    out.edgeMasks.push_back(mask);
                     for (int i = 0; i < sz; ++i) {
                         int e = contourEdge(c, t, i);
                         int a0 = kEdgeV0[e];
                         int sx = x + (a0 & 1), sy = y + ((a0 >> 1) & 1), sz2 = z + ((a0 >> 2) & 1);
                         uint64_t key = 3ULL * ((uint64_t)sz2 * X * Y + (uint64_t)sy * X + sx) + kEdgeAxis[e];
                         int slot = quadSlot(e, (edgy >> e) & 1);
-                        QuadEntry& q = table[key];
-                        if (q.slot[slot] != -1) anomalies |= kSSlot;
+                        QuadEntry& q = out.table[key];
+                        if (q.slot[slot] != -1) out.anomalies |= kSSlot;
                         q.slot[slot] = vid;
                         int base = (x & 1) | ((y & 1) << 1) | ((z & 1) << 2);
                         if (e == 0) q.color = 3 * base;
@@ -587,6 +598,45 @@ static void runDMC(const Grid& g, float iso, bool surfaceIteration, std::vector<
                     }
                 }
             }
+}
+
+// performDualMarchingCubes + mapQuadrilaterals (D/DualMarchingCubes.cu:38-85):
+// z-slabs in parallel (OpenMP), joined in slab order, so vertex ids follow
+// the cells' (z, y, x) order as in a single pass
+static void runDMC(const Grid& g, float iso, bool surfaceIteration, std::vector<float>& pos,
+                   std::vector<float>& nrm, std::vector<int>& quads, std::vector<uint16_t>& attr,
+                   std::vector<int>& cells, std::vector<uint16_t>& edgeMasks, uint32_t& anomalies) {
+    const int Zc = std::max(g.d[2] - 1, 0);
+    int slabs = 1;
+#ifdef _OPENMP
+    slabs = std::max(1, std::min(Zc, 4 * omp_get_max_threads()));
+#endif
+    std::vector<SlabDMC> part(slabs);
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int k = 0; k < slabs; ++k)
+        runDMCSlab(g, iso, surfaceIteration, (int)((int64_t)Zc * k / slabs), (int)((int64_t)Zc * (k + 1) / slabs),
+                   part[k]);
+    std::unordered_map<uint64_t, QuadEntry> table;
+    int base = 0;
+    for (int k = 0; k < slabs; ++k) {
+        SlabDMC& sd = part[k];
+        anomalies |= sd.anomalies;
+        pos.insert(pos.end(), sd.pos.begin(), sd.pos.end());
+        nrm.insert(nrm.end(), sd.nrm.begin(), sd.nrm.end());
+        cells.insert(cells.end(), sd.cells.begin(), sd.cells.end());
+        edgeMasks.insert(edgeMasks.end(), sd.edgeMasks.begin(), sd.edgeMasks.end());
+        for (auto& kv : sd.table) {
+            QuadEntry& q = table[kv.first];
+            for (int i = 0; i < 4; ++i) {
+                if (kv.second.slot[i] == -1) continue;
+                if (q.slot[i] != -1) anomalies |= kSSlot;
+                q.slot[i] = kv.second.slot[i] + base;
+            }
+            if (kv.second.color != (int)kAttrInvalidColor) q.color = kv.second.color;
+        }
+        base += (int)(sd.pos.size() / 3);
+        SlabDMC().table.swap(sd.table);
+    }
     std::vector<uint64_t> keys;
     keys.reserve(table.size());
     for (auto& kv : table)

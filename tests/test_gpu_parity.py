@@ -240,3 +240,41 @@ def test_materialized_refinement_bit_exact(refinement, pad):
     assert grid.dimensions == d
     assert np.array_equal(grid.origin, o) and np.array_equal(grid.deltas, s)
     assert np.array_equal(out.cpu().numpy().view(np.uint32), ref.view(np.uint32))
+
+
+def _hsv(h, s=np.float32(0.8), v=np.float32(0.8)):
+    # LazyEngine::Color::HSVtoRGB in float32
+    f = np.float32(h) / np.float32(60.0)
+    hi = np.floor(f)
+    f = np.float32(f - hi)
+    one = np.float32(1)
+    p, q, t = v * (one - s), v * (one - s * f), v * (one - s * (one - f))
+    return {0: (v, t, p), 6: (v, t, p), 1: (q, v, p), 2: (p, v, t), 3: (p, q, v), 4: (t, p, v)}.get(int(hi), (v, p, q))
+
+
+def test_render_buffers_match_the_mesh():
+    import torch
+    # non-manifold edges and a non-manifold vertex left unrepaired: several flag colours
+    samples, dims, origin, spacing, iso = golden_grid("Non-Manifold-Vertex")
+    dmc, m, _ = gpu_run(samples, dims, origin, spacing, iso, 0, False, split_non_manifold=0)
+    assert len(set(int(f) for f in m.vertex_flags)) > 1
+    verts, idx = dmc.render_buffers()
+    torch.cuda.synchronize()
+    verts, idx = verts.cpu().numpy(), idx.cpu().numpy().view(np.uint32).reshape(-1, 6)
+    q = m.quads.astype(np.uint32)
+    assert np.array_equal(idx, np.stack([q[:, 0], q[:, 1], q[:, 2], q[:, 2], q[:, 3], q[:, 0]], 1))
+    used = m.vertex_halfedge >= 0
+    assert np.array_equal(verts[used, :3].view(np.uint32), m.positions[used].view(np.uint32))
+    assert np.array_equal(verts[used, 3:6].view(np.uint32), m.normals[used].view(np.uint32))
+    assert np.all(np.isnan(verts[~used, :6]))
+    for v in np.flatnonzero(used):
+        fl = int(m.vertex_flags[v])
+        nm, weird, fans = fl & 1, fl & 4, fl & 8
+        hue = 180.0
+        if nm: hue = 0.0
+        if weird: hue = 60.0
+        if fans: hue = 270.0
+        if weird and nm: hue = 300.0
+        if nm and fans: hue = 240.0
+        assert np.array_equal(verts[v, 6:9], np.array(_hsv(hue), np.float32)), (v, fl)
+        assert verts[v, 9] == 1.0
