@@ -1,0 +1,76 @@
+"""The benchmark configurations at their full sizes.  The 64^3 blob grid and
+the 512^3-cell refined headline grid are compared with the oracle bit for bit;
+uniform noise (the worst case for ambiguous cells and non-manifold edges) is
+compared at 128^3, and at its full 256^3 size checked for determinism and
+mesh consistency (the oracle's serial halfedge build takes minutes there)."""
+import numpy as np
+import pytest
+
+import manifolddmc_gb300 as mdmc
+from manifolddmc_gb300.workloads import CONFIGS, uniform_noise
+from test_gpu_parity import assert_parity, gpu_run, oracle_for
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_config(name):
+    desc, gen, iso, refine, pad = CONFIGS[name]
+    vol = gen()
+    dims = [vol.shape[2], vol.shape[1], vol.shape[0]]
+    o, s = np.zeros(3, np.float32), np.ones(3, np.float32)
+    dmc, m, _ = gpu_run(vol.reshape(-1), dims, o, s, iso, refine, pad)
+    ref, _ = oracle_for(vol.reshape(-1), dims, o, s, iso, refine, pad)
+    return dmc, m, ref
+
+
+def test_blobs64_padded_bit_exact():
+    dmc, m, ref = _run_config("blobs64_pad")
+    assert len(m.face_first_halfedge) > 5000
+    assert_parity(dmc, m, ref)
+
+
+def test_headline_refined_512_cubed_bit_exact():
+    dmc, m, ref = _run_config("blobs129_refine4")
+    assert len(m.face_first_halfedge) > 1_000_000
+    assert_parity(dmc, m, ref)
+
+
+def test_noise_128_bit_exact():
+    vol = uniform_noise(128, 1)
+    o, s = np.zeros(3, np.float32), np.ones(3, np.float32)
+    dmc, m, _ = gpu_run(vol.reshape(-1), [128, 128, 128], o, s, 0.5)
+    ref, _ = oracle_for(vol.reshape(-1), [128, 128, 128], o, s, 0.5)
+    assert dmc.stats.split_iterations >= 1
+    assert_parity(dmc, m, ref)
+
+
+def test_noise_256_deterministic_and_consistent():
+    desc, gen, iso, refine, pad = CONFIGS["noise256"]
+    vol = gen()
+    g = mdmc.UniformGrid(vol)
+    dmc = mdmc.DualMarchingCubes()
+    dmc.run(iso, g)
+    a = dmc.get_halfedge_mesh()
+    st = dmc.stats
+    dmc.run(iso, g)
+    b = dmc.get_halfedge_mesh()
+    for k in ("positions", "normals", "halfedges", "face_first_halfedge", "face_attributes", "vertex_flags",
+              "vertex_halfedge", "quads"):
+        assert np.array_equal(getattr(a, k).view(np.uint8), getattr(b, k).view(np.uint8)), k
+    V, F, H = len(a.positions), len(a.face_first_halfedge), len(a.halfedges)
+    assert H == 4 * F and int(st.num_dmc_quads) > 20_000_000
+    he = a.halfedges
+    # every face is a 4-cycle of its own halfedges
+    h = a.face_first_halfedge.astype(np.int64)
+    for _ in range(4):
+        assert np.all(he[h, 1] == np.arange(F))
+        h = he[h, 2]
+    assert np.array_equal(h, a.face_first_halfedge)
+    # the repair leaves no 4-face edge, and twins of 2-face edges join opposite directions
+    assert int(st.num_edges4) == 0
+    assert he[:, 0].min() >= 0 and he[:, 0].max() < V
+    t = he[:, 3]
+    ok = t >= 0
+    dest = he[he[:, 2], 0]
+    sym = ok & (he[np.where(ok, t, 0), 3] == np.arange(H))
+    assert np.all(he[t[sym], 0] == dest[sym])
