@@ -325,6 +325,38 @@ mdmc_status refreshTable(mdmc_context* c, uint32_t* status, cudaStream_t s) {
     return edgeBuckets(c, 0, s);
 }
 
+// Non-manifold vertex detection (detectNonManifoldVertices,
+// D/PostProcesses/ManifoldCreator.cu:488-536) and the outputs (quads by face
+// walk, getNumQuadsWithNonManifoldEdges, smallest outgoing halfedge per
+// vertex).  starsDone: the quad pass already wrote the vertex stars, quads and
+// face statistics of this mesh.
+mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaStream_t s) {
+    DevCounters* ctr = c->counters.as<DevCounters>();
+    MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
+    MDMC_CHECK(c, c->degree.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
+    MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)std::max<int64_t>(c->F, 1)));
+    const MeshDims mdF{(int)c->V, (int)c->F, (int)c->H};
+    const bool detect = c->opt.detect_non_manifold_vertices != 0;
+    if (detect) {
+        MDMC_CHECK(c, c->isKey.ensure((size_t)std::max<int64_t>(c->H, 1)));
+        MDMC_CHECK(c, c->fans.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
+        MDMC_CHECK(c, c->slowFan.ensure((size_t)std::max<int64_t>(c->V, 1)));
+        MDMC_CHECK(c, cudaMemsetAsync(c->isKey.p, 0, (size_t)c->H, s));
+        if (!starsDone) launchVertexStar(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), s);
+        launchDetectFans(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), c->slowFan.as<uint8_t>(),
+                         c->isKey.as<uint8_t>(), c->fans.as<int>(), c->vflags.as<uint8_t>(), ctr, status, s);
+    }
+    cudaEventRecord(c->ev[4], s);
+    if (!starsDone)
+        launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), mdF, c->heValence.as<uint8_t>(), c->quads.as<int4>(),
+                     c->vertexHE.as<int>(), detect, ctr, status, s);
+    else if (!detect)
+        launchVertexHalfedgeFix(c->vertexHE.as<int>(), (int)c->V, s);
+    cudaEventRecord(c->ev[5], s);
+    MDMC_CHECK(c, cudaGetLastError());
+    return MDMC_OK;
+}
+
 // simplify3X3Y (kind 0), simplify3X3YOld (kind 1), simplify3333 (kind 2),
 // D/Halfedges/HalfedgeMesh.cu:859-1048: mark and merge, compact the vertex
 // and quad lists, rebuild the halfedge mesh from the quads (initialize)
@@ -772,6 +804,11 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, c->nmList.ensure(sizeof(int4) * (size_t)(Q + 1)));
     MDMC_CHECK(c, c->heValence.ensure((size_t)std::max<int64_t>(4 * Q, 1)));
     MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)Vd, 4), s));
+    MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)std::max<int64_t>(Q, 1)));
+    MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)Vd));
+    MDMC_CHECK(c, c->degree.ensure(sizeof(int) * (size_t)Vd));
+    MDMC_CHECK(c, cudaMemsetAsync(c->vertexHE.p, 0x7F, sizeof(int) * (size_t)Vd, s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->degree.p, 0, sizeof(int) * (size_t)Vd, s));
 
     // mapQuadrilaterals + collectHalfedgeElements, and the halfedge mesh's
     // twins and flags (HalfedgeMesh::initialize) in the same pass
@@ -781,7 +818,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     launchQuads(c->act.as<ActiveCell>(), c->quadOwner.as<int>(), (int)A, c->cellMask.as<uint32_t>(),
                 c->cellFirst.as<int>(), X, Y, Z, W, c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(),
                 c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(), c->nmList.as<int4>(), (int)(Q + 1), (int)Q,
-                (int)Vd, ctr, s);
+                (int)Vd, c->quads.as<int4>(), c->vertexHE.as<int>(), c->degree.as<int>(), ctr, s);
     cudaEventRecord(c->kev[7], s);
     // vertex positions and normals (sliceP's vertex part)
     cudaEventRecord(c->kev[10], s);
@@ -804,35 +841,33 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
                     status, s);
     MDMC_CHECK(c, cudaGetLastError());
     int64_t iterations = 0;
-    if (c->opt.split_non_manifold_halfedges) {
-        if ((st = runSplitter(c, g, iso, iterations, s)) != MDMC_OK) return st;
+    // When no face is non-manifold the splitter does nothing and the mesh is
+    // final here, with its vertex stars, output quads and face statistics
+    // already written by the quad pass: detection and output run at once and
+    // one read-back decides.  Their status bits go to a side word, kept only if
+    // the splitter turns out not to run.
+    bool finished = false;
+    if (!c->simplified) {
+        cudaEventRecord(c->ev[3], s);
+        if ((st = finishMesh(c, true, &ctr->specStatus, s)) != MDMC_OK) return st;
+        MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
+        MDMC_CHECK(c, cudaStreamSynchronize(s));
+        finished = !(c->opt.split_non_manifold_halfedges && c->hostCounters->nmBuckets > 0);
+        if (finished) c->hostCounters->status |= c->hostCounters->specStatus;
     }
-    cudaEventRecord(c->ev[3], s);
-
-    // ---- non-manifold vertices ------------------------------------------------
-    MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
-    const MeshDims mdF{(int)c->V, (int)c->F, (int)c->H};
-    if (c->opt.detect_non_manifold_vertices) {
-        MDMC_CHECK(c, c->isKey.ensure((size_t)std::max<int64_t>(c->H, 1)));
-        MDMC_CHECK(c, c->fans.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
-        MDMC_CHECK(c, c->degree.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
-        MDMC_CHECK(c, c->slowFan.ensure((size_t)std::max<int64_t>(c->V, 1)));
-        MDMC_CHECK(c, cudaMemsetAsync(c->isKey.p, 0, (size_t)c->H, s));
-        launchVertexStar(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), s);
-        launchDetectFans(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), c->slowFan.as<uint8_t>(),
-                         c->isKey.as<uint8_t>(), c->fans.as<int>(), c->vflags.as<uint8_t>(), ctr, status, s);
+    if (!finished) {
+        if (c->opt.split_non_manifold_halfedges) {
+            if ((st = runSplitter(c, g, iso, iterations, s)) != MDMC_OK) return st;
+        }
+        cudaEventRecord(c->ev[3], s);
+        // the splitter's refresh reset the edge counters; detection and the
+        // face statistics start from zero again
+        MDMC_CHECK(c, cudaMemsetAsync(&ctr->nmVertices, 0, sizeof(unsigned long long), s));
+        MDMC_CHECK(c, cudaMemsetAsync(&ctr->quadsNM[0], 0, sizeof(ctr->quadsNM), s));
+        if ((st = finishMesh(c, false, status, s)) != MDMC_OK) return st;
+        MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
+        MDMC_CHECK(c, cudaStreamSynchronize(s));
     }
-    cudaEventRecord(c->ev[4], s);
-
-    // ---- outputs and statistics -------------------------------------------------
-    MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)std::max<int64_t>(c->F, 1)));
-    launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), mdF, c->heValence.as<uint8_t>(), c->quads.as<int4>(),
-                 c->vertexHE.as<int>(),
-                 c->opt.detect_non_manifold_vertices != 0, ctr, status, s);
-    cudaEventRecord(c->ev[5], s);
-    MDMC_CHECK(c, cudaGetLastError());
-    MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
-    MDMC_CHECK(c, cudaStreamSynchronize(s));
 
     const DevCounters& hc = *c->hostCounters;
     c->stats.num_edges = (int64_t)hc.edges;

@@ -834,9 +834,11 @@ __global__ void __launch_bounds__(256) kQuads(const ActiveCell* __restrict__ act
                                               int* __restrict__ faceFirst, uint16_t* __restrict__ faceAttr,
                                               uint8_t* vflags, uint32_t* __restrict__ heValence4,
                                               int4* __restrict__ nmList, int nmCapacity, int numQuads, int numVertices,
+                                              int4* __restrict__ quadsOut, int* vertexHE, int* degree,
                                               DevCounters* ctr) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     int nE = 0, nE3 = 0, nE4 = 0;
+    int nmEdges = -1;  // halfedges of this quad on edges of more than two faces
     bool ok = q < numQuads;
     const int j = ok ? quadOwner[q] : 0;
     if (ok && !inb(j, numActive)) {
@@ -1053,18 +1055,31 @@ __global__ void __launch_bounds__(256) kQuads(const ActiveCell* __restrict__ act
                 heValence4[q] = valences;
                 faceFirst[q] = h0;
                 faceAttr[q] = (uint16_t)attr;
+                // what the output pass reads off the finished mesh, valid while
+                // no later pass changes faces or vertices: the face's vertices,
+                // its count of edges with more than two faces, each vertex's
+                // smallest outgoing halfedge and out-degree
+                quadsOut[q] = make_int4(quadV[0], quadV[1], quadV[2], quadV[3]);
+                nmEdges = 0;
+#pragma unroll
+                for (int hi = 0; hi < 4; ++hi) {
+                    nmEdges += ((valences >> (8 * hi)) & 0xFFu) > 2 ? 1 : 0;
+                    atomicMin(&vertexHE[quadV[hi]], h0 + hi);
+                    atomicAdd(&degree[quadV[hi]], 1);
+                }
             }
         }
     }
     blockAddTo(&ctr->edges, nE);
     blockAddTo(&ctr->edges3, nE3);
     blockAddTo(&ctr->edges4, nE4);
+    for (int k = 1; k <= 4; ++k) blockAddTo(&ctr->quadsNM[k], nmEdges == k ? 1 : 0);
 }
 
 void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, const uint32_t* cellMask,
                  const int* cellFirst, int X, int Y, int Z, int W, int4* he, int* faceFirst, uint16_t* faceAttr,
                  uint8_t* vflags, uint8_t* heValence, int4* nmList, int nmCapacity, int numQuads, int numVertices,
-                 DevCounters* ctr, cudaStream_t s) {
+                 int4* quadsOut, int* vertexHE, int* degree, DevCounters* ctr, cudaStream_t s) {
     if (numQuads <= 0) return;
     countLaunch();
     CellIndex ix;
@@ -1076,7 +1091,7 @@ void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, con
     ix.W = W;
     kQuads<<<(numQuads + 255) / 256, 256, 0, s>>>(act, quadOwner, numActive, ix, he, faceFirst, faceAttr, vflags,
                                                    reinterpret_cast<uint32_t*>(heValence), nmList, nmCapacity,
-                                                   numQuads, numVertices, ctr);
+                                                   numQuads, numVertices, quadsOut, vertexHE, degree, ctr);
 }
 
 }  // namespace mdmc

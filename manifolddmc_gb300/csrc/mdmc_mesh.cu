@@ -501,6 +501,12 @@ __global__ void kVertexHalfedgeFix(int* vertexHE, int numVertices) {
     if (v < numVertices && vertexHE[v] == 0x7F7F7F7F) vertexHE[v] = -1;
 }
 
+void launchVertexHalfedgeFix(int* vertexHE, int numVertices, cudaStream_t s) {
+    if (numVertices <= 0) return;
+    countLaunch();
+    kVertexHalfedgeFix<<<(numVertices + 255) / 256, 256, 0, s>>>(vertexHE, numVertices);
+}
+
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, int4* quads,
                   int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
     (void)status;

@@ -49,7 +49,7 @@ struct __align__(16) ActiveCell {
 // Device counters filled during a run and read back once at its end.
 struct DevCounters {
     uint32_t status;
-    uint32_t pad;
+    uint32_t specStatus;  // status bits of work that may be discarded (merged by the host when kept)
     unsigned long long edges, edges3, edges4, nmVertices;
     unsigned long long quadsNM[5];
     unsigned long long nmBuckets;  // length of the 4-face bucket list
