@@ -342,6 +342,7 @@ mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaSt
         MDMC_CHECK(c, c->fans.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
         MDMC_CHECK(c, c->slowFan.ensure((size_t)std::max<int64_t>(c->V, 1)));
         MDMC_CHECK(c, cudaMemsetAsync(c->isKey.p, 0, (size_t)c->H, s));
+        MDMC_CHECK(c, cudaMemsetAsync(&ctr->slowFans, 0, sizeof(unsigned long long), s));
         if (!starsDone) launchVertexStar(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), s);
         launchDetectFans(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), c->slowFan.as<uint8_t>(),
                          c->isKey.as<uint8_t>(), c->fans.as<int>(), c->vflags.as<uint8_t>(), ctr, status, s);

@@ -347,46 +347,84 @@ __global__ void kVertexStar(const int4* __restrict__ he, MeshDims md, int* __res
     }
 }
 
-// One walk per vertex.  When the clockwise walk from the vertex's smallest
-// outgoing halfedge returns to it after visiting exactly all of the vertex's
-// outgoing halfedges, every step through a symmetric twin pair (and faces are
-// 4-cycles), the counter-clockwise step is the inverse of the clockwise one
-// on that cycle: every outgoing halfedge's own walks cover the same cycle,
-// its key is the cycle's smallest id, and the vertex has one fan with no
-// limit hit.  Every other vertex (boundary, non-manifold or asymmetric twins)
-// takes the per-halfedge walks.  Also turns "no outgoing halfedge" into -1.
+// One walk per vertex.  When the walks from the vertex's smallest outgoing
+// halfedge visit exactly all of the vertex's outgoing halfedges through
+// symmetric twin pairs (faces are 4-cycles) -- clockwise back to the start
+// (a closed fan), or clockwise to a boundary and counter-clockwise to the
+// other boundary (an open fan) -- the counter-clockwise step is the inverse of
+// the clockwise one on that fan: every outgoing halfedge's own walks cover the
+// same fan, its key is the fan's smallest id, and the vertex has one fan with
+// no limit hit.  Every other vertex (non-manifold, asymmetric twins) takes the
+// per-halfedge walks and is counted.  Also turns "no outgoing halfedge" into -1.
 __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restrict__ vertexHE,
-                         const int* __restrict__ deg, int* __restrict__ fans, uint8_t* __restrict__ slow) {
+                         const int* __restrict__ deg, int* __restrict__ fans, uint8_t* __restrict__ slow,
+                         unsigned long long* slowCount) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= md.V) return;
-    const int d = deg[v];
-    if (d == 0) {
-        vertexHE[v] = -1;
-        fans[v] = 0;
-        slow[v] = 0;
-        return;
-    }
-    const int start = vertexHE[v];
-    bool ok = inb(start, md.H) && d <= 1024;
-    int x = start, steps = 0;
-    while (ok) {
-        const int4 hx = he[x];
-        if (hx.x != v || !inb(hx.w, md.H)) {
-            ok = false;
-            break;
+    bool isSlow = false;
+    if (v < md.V) {
+        const int d = deg[v];
+        if (d == 0) {
+            vertexHE[v] = -1;
+            fans[v] = 0;
+            slow[v] = 0;
+        } else {
+            const int start = vertexHE[v];
+            bool ok = inb(start, md.H) && d <= 1024;
+            bool open = false;
+            int x = start, visited = 1;
+            while (ok) {  // clockwise: next(twin(x))
+                const int4 hx = he[x];
+                if (hx.x != v) {
+                    ok = false;
+                    break;
+                }
+                if (hx.w == -1) {
+                    open = true;
+                    break;
+                }
+                if (!inb(hx.w, md.H)) {
+                    ok = false;
+                    break;
+                }
+                const int4 ht = he[hx.w];
+                if (ht.w != x || !inb(ht.z, md.H)) {
+                    ok = false;
+                    break;
+                }
+                x = ht.z;
+                if (x == start) break;
+                if (++visited > d) ok = false;
+            }
+            x = start;
+            while (ok && open) {  // counter-clockwise: twin(next^3(x)), up to the other boundary
+                int p = x;
+                for (int k = 0; k < 3 && ok; ++k) {
+                    p = he[p].z;
+                    ok = inb(p, md.H);
+                }
+                if (!ok) break;
+                const int t = he[p].w;
+                if (t == -1) break;
+                if (!inb(t, md.H)) {
+                    ok = false;
+                    break;
+                }
+                const int4 htt = he[t];
+                if (htt.w != p || htt.x != v) {
+                    ok = false;
+                    break;
+                }
+                x = t;
+                if (x == start || ++visited > d) ok = false;
+            }
+            ok = ok && visited == d;
+            fans[v] = ok ? 1 : 0;
+            slow[v] = ok ? 0 : 1;
+            isSlow = !ok;
         }
-        const int4 ht = he[hx.w];
-        if (ht.w != x || !inb(ht.z, md.H)) {
-            ok = false;
-            break;
-        }
-        x = ht.z;
-        if (++steps > d) ok = false;
-        if (x == start) break;
     }
-    ok = ok && steps == d;
-    fans[v] = ok ? 1 : 0;
-    slow[v] = ok ? 0 : 1;
+    const unsigned b = __ballot_sync(0xffffffffu, isSlow);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(slowCount, (unsigned long long)__popc(b));
 }
 
 // A fan key is the smallest halfedge id of the fan and has the origin of the
@@ -395,9 +433,9 @@ __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restri
 // halfedge, per origin".  No sort is needed.  Only the halfedges of vertices
 // the single walk did not settle.
 __global__ void kFanKeys(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ slow,
-                         uint8_t* __restrict__ isKey, uint32_t* status) {
+                         const unsigned long long* slowCount, uint8_t* __restrict__ isKey, uint32_t* status) {
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= md.H) return;
+    if (h >= md.H || *slowCount == 0) return;
     const int v = he[h].x;
     if (!inb(v, md.V) || !slow[v]) return;
     const int k = min(h, min(fanWalk(he, h, true, md.H, status), fanWalk(he, h, false, md.H, status)));
@@ -405,9 +443,10 @@ __global__ void kFanKeys(const int4* __restrict__ he, MeshDims md, const uint8_t
 }
 
 __global__ void kFanCount(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ slow,
-                          const uint8_t* __restrict__ isKey, int* __restrict__ fans, uint32_t* status) {
+                          const unsigned long long* slowCount, const uint8_t* __restrict__ isKey,
+                          int* __restrict__ fans, uint32_t* status) {
     const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= md.H) return;
+    if (h >= md.H || *slowCount == 0) return;
     if (isKey[h]) {
         const int v = he[h].x;
         if (inb(v, md.V)) {
@@ -449,13 +488,13 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
                       int* fans, uint8_t* vflags, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
     if (md.V > 0) {
         countLaunch();
-        kFanFast<<<(md.V + 255) / 256, 256, 0, s>>>(he, md, vertexHE, deg, fans, slow);
+        kFanFast<<<(md.V + 255) / 256, 256, 0, s>>>(he, md, vertexHE, deg, fans, slow, &ctr->slowFans);
     }
     if (md.H > 0) {
         countLaunch();
-        kFanKeys<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, slow, isKey, status);
+        kFanKeys<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, slow, &ctr->slowFans, isKey, status);
         countLaunch();
-        kFanCount<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, slow, isKey, fans, status);
+        kFanCount<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, slow, &ctr->slowFans, isKey, fans, status);
     }
     if (md.V > 0) {
         countLaunch();

@@ -54,6 +54,7 @@ struct DevCounters {
     unsigned long long quadsNM[5];
     unsigned long long nmBuckets;  // length of the 4-face bucket list
     unsigned long long candidates; // coarse cells that may cross iso (refined grids)
+    unsigned long long slowFans;   // vertices the single fan walk did not settle
 };
 
 }  // namespace mdmc
