@@ -64,13 +64,20 @@ void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int p
 // coarse cell and its samples are trilinear interpolations of that cell's
 // eight corners: in exact arithmetic they stay within [min, max] of the
 // corners, and the rounding of refineGrid's expression (three lerp levels,
-// at most ~15 unit roundings of max|corner|) stays below delta = 32 * 2^-24 *
-// max|corner|.  A coarse cell whose corners are all below iso - delta, or all
-// at or above iso + delta, therefore holds only case-0 / case-255 refined
-// cells, and its refined cells need not be evaluated at all.
+// at most ~15 unit roundings of m = max|corner|) stays below 15u*m (u = 2^-24).
+// With D = 64u*m (exact: a power-of-two multiple), a coarse cell whose corners
+// all satisfy max < fl(iso - D), or min >= fl(iso + D), holds only case-0 /
+// case-255 refined cells.  The float rounding of iso -+ D is at most u/2 of
+// |iso - D|; while |iso| <= 97m that is below the 49u*m of slack, and when
+// |iso| > 97m no refined sample can reach iso at all, so the test never skips
+// a crossing cell.  D is at least 2^-120, which covers the absolute rounding
+// of subnormal values.  NaN corners keep the cell.
 // ---------------------------------------------------------------------------
-__global__ void kCoarseMayCross(const float* __restrict__ c, int cX, int cY, int cZ, float iso, uint32_t* __restrict__ bits,
-                                int64_t numCells, uint32_t* __restrict__ list, unsigned long long* listCount) {
+__global__ void __launch_bounds__(256) kCoarseMayCross(const float* __restrict__ c, int cX, int cY, int cZ, float iso,
+                                                       uint32_t* __restrict__ bits, int64_t numCells,
+                                                       uint32_t* __restrict__ list, unsigned long long* listCount) {
+    __shared__ unsigned warpCount[8];
+    __shared__ unsigned long long blockBase;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool may = false;
     if (i < numCells) {
@@ -87,20 +94,30 @@ __global__ void kCoarseMayCross(const float* __restrict__ c, int cX, int cY, int
             hi = fmaxf(hi, v);
             mag = fmaxf(mag, fabsf(v));
         }
-        const double delta = 32.0 * 5.9604644775390625e-8 * (double)mag;
-        const bool allBelow = (double)hi < (double)iso - delta;
-        const bool allAbove = (double)lo >= (double)iso + delta;
+        // 64 * 2^-24 * m, at least 2^-120 so that subnormal rounding stays covered
+        const float delta = fmaxf(mag * 3.814697265625e-06f, 7.52316384526264e-37f);
+        const bool allBelow = hi < iso - delta;
+        const bool allAbove = lo >= iso + delta;
         may = nan || !(allBelow || allAbove);
     }
     const unsigned b = __ballot_sync(0xffffffffu, may);
-    const int lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (lane == 0 && i < numCells) bits[i >> 5] = b;
-    if (list && b) {  // the candidates, in any order
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(listCount, (unsigned long long)__popc(b));
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (may) list[base + __popc(b & ((1u << lane) - 1u))] = (uint32_t)i;
+    if (!list) return;
+    // the candidates, in any order: one atomic per block
+    if (lane == 0) warpCount[warp] = __popc(b);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned total = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            const unsigned n = warpCount[w];
+            warpCount[w] = total;
+            total += n;
+        }
+        blockBase = total ? atomicAdd(listCount, (unsigned long long)total) : 0ULL;
     }
+    __syncthreads();
+    if (may) list[blockBase + warpCount[warp] + __popc(b & ((1u << lane) - 1u))] = (uint32_t)i;
 }
 
 void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, cudaStream_t s) {
