@@ -359,6 +359,38 @@ __global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g
             if (lane == 0) atomicOr(status, kStatusBadIndex);
             continue;
         }
+        if (ex == 4 && ey == 4 && ez == 4 && ((xs & 31) + 4) <= 32) {
+            // the standard block of a x4 refinement: 125 samples and 64 cells
+            // with compile-time strides; the 4 cells of a row lie in one mask
+            // word and occupy 4 aligned lanes, OR-ed by two shuffles
+            float v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int k = 32 * u + lane;
+                const int kk = k < 125 ? k : 0;
+                v[u] = g.at(xs + kk % 5, ys + (kk / 5) % 5, zs + kk / 25);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (32 * u + lane < 125) buf[32 * u + lane] = v[u];
+            __syncwarp();
+#pragma unroll
+            for (int k0 = 0; k0 < 64; k0 += 32) {
+                const int k = k0 + lane;
+                const int lx = k & 3, ly = (k >> 2) & 3, lz = k >> 4;
+                const int o = lz * 25 + ly * 5 + lx;
+                const float s[8] = {buf[o],      buf[o + 1],      buf[o + 5],      buf[o + 6],
+                                    buf[o + 25], buf[o + 26], buf[o + 30], buf[o + 31]};
+                const int cs = caseOf(s, iso);
+                const int x = xs + lx;
+                unsigned bitv = (cs != 0 && cs != 255) ? (1u << (x & 31)) : 0u;
+                bitv |= __shfl_xor_sync(0xffffffffu, bitv, 1);
+                bitv |= __shfl_xor_sync(0xffffffffu, bitv, 2);
+                if (lx == 0 && bitv) atomicOr(&mask[((int64_t)(zs + lz) * (g.Y - 1) + (ys + ly)) * W + (x >> 5)], bitv);
+            }
+            __syncwarp();
+            continue;
+        }
         if (plane * (ez + 1) <= kBlockSamplesMax) {
             // every sample of the block at once (loads of four rounds in flight)
             const int total = plane * (ez + 1);
