@@ -865,6 +865,7 @@ __device__ __forceinline__ int axisBit(int a) { return 1 << a; }
 struct AroundCell {
     uint32_t info;  // case | edge -> contour map << 8
     int vbase;      // first vertex id
+    int qbase;      // first quad id
     int le;         // local index of the quad's edge in this cell
     int contour;    // contour of that edge in this cell
 };
@@ -916,6 +917,7 @@ __global__ void __launch_bounds__(256) kQuads(const ActiveCell* __restrict__ act
             AroundCell cell[4];
             cell[0].info = rec.info;
             cell[0].vbase = rec.pad;
+            cell[0].qbase = rec.qbase;
             int jk[4];
             jk[0] = j;
 #pragma unroll
@@ -930,10 +932,12 @@ __global__ void __launch_bounds__(256) kQuads(const ActiveCell* __restrict__ act
                     ok = false;
                     cell[k].info = 0;
                     cell[k].vbase = 0;
+                    cell[k].qbase = 0;
                 } else {
                     const ActiveCell r2 = act[jk[k]];
                     cell[k].info = r2.info;
                     cell[k].vbase = r2.pad;
+                    cell[k].qbase = r2.qbase;
                 }
             }
 #pragma unroll
@@ -1025,16 +1029,28 @@ __global__ void __launch_bounds__(256) kQuads(const ActiveCell* __restrict__ act
                         const int oy = py + (u == 1 ? du : 0) + (axis == 1 ? offA : 0);
                         const int oz = pz + (u == 2 ? du : 0) + (axis == 2 ? offA : 0);
                         if (((al != 0 && ox < 1) || (al != 1 && oy < 1) || (al != 2 && oz < 1))) continue;
-                        const int jo = ix.find(ox, oy, oz);
-                        if (jo < 0 || jo >= numActive) continue;
-                        const ActiveCell ro = act[jo];
-                        const int cso = (int)(ro.info & 255u);
+                        // the owner is often a cell around the quad's edge (p, p - e_u),
+                        // whose record is loaded already
+                        uint32_t oinfo;
+                        int oqbase;
+                        if (offA == 0 && du <= 0) {
+                            const int ko = du == 0 ? 0 : (u == b ? 1 : 2);
+                            oinfo = ko == 0 ? cell[0].info : (ko == 1 ? cell[1].info : cell[2].info);
+                            oqbase = ko == 0 ? cell[0].qbase : (ko == 1 ? cell[1].qbase : cell[2].qbase);
+                        } else {
+                            const int jo = ix.find(ox, oy, oz);
+                            if (jo < 0 || jo >= numActive) continue;
+                            const ActiveCell ro = act[jo];
+                            oinfo = ro.info;
+                            oqbase = ro.qbase;
+                        }
+                        const int cso = (int)(oinfo & 255u);
                         if (!ownsAxis(cso, al, ox, oy, oz)) continue;
                         int r = 0;
 #pragma unroll
                         for (int a2 = 0; a2 < 2; ++a2)
                             if (a2 < al && ownsAxis(cso, a2, ox, oy, oz)) ++r;
-                        const int q2 = ro.qbase + r;
+                        const int q2 = oqbase + r;
                         const int edgyO = ((csA >> edgeV0(eA)) & 1u) ? 0 : 1;
                         const int sA = quadSlot(eA, edgyO), sB = quadSlot(eB, edgyO);
                         if (((sA + 1) & 3) == sB) {
