@@ -251,6 +251,26 @@ MDMC_API const char* mdmc_batch_last_error(const mdmc_batch* batch);
 /* Human-readable description of the context's last error ("" if none). */
 MDMC_API const char* mdmc_last_error(const mdmc_context* context);
 
+/* Volume generators (UniformGridHost::generateVolume / generateEdgeCase,
+ * UniformGrid.inl:20-269, :463-509).  surface_case follows SurfaceCase
+ * (UniformGrid.h:26-37): 0 sphere, 1 torus, 2 two-holed torus, 3 four-holed
+ * torus, 4 genus two, 5 iWP, 6 pwHybrid, 7 neovius, 8 Goursat, 9 Steiner's
+ * Roman surface.  Samples the surface on [-1, 1]^3 into a device buffer of
+ * dims[0]*dims[1]*dims[2] floats and reports the grid's origin and spacing.
+ * The edge cases (which = 0, 1: NonManifoldVertex0/1) are 4x4x3 grids of
+ * 850/950.  Asynchronous on the stream. */
+MDMC_API mdmc_status mdmc_generate_volume(int32_t surface_case, const int32_t dims[3], float* samples,
+                                          float origin[3], float spacing[3], void* stream);
+MDMC_API mdmc_status mdmc_generate_edge_case(int32_t which, float* samples, int32_t dims[3], float origin[3],
+                                             float spacing[3], void* stream);
+
+/* Writes a .bin volume (int32 dims[3], float32 spacing[3], then the samples
+ * cast to uint16, x fastest), the format mdmc_read_bin reads
+ * (UniformGridHost::writeSelectionToFile<unsigned short> over the whole grid,
+ * UniformGrid.inl:632-695).  host_samples is host memory. */
+MDMC_API mdmc_status mdmc_write_bin(const char* path, const int32_t dims[3], const float spacing[3],
+                                    const float* host_samples);
+
 /* Build-time tables, for tests: the packed contour word of every Marching
  * Cubes case and whether the case takes the asymptotic-decider path.  No
  * reference counterpart (the reference keeps them in s_polygonPatterns and

@@ -127,6 +127,9 @@ def library():
             "mdmc_case_tables": (None, [P, P]),
             "mdmc_backward": (ctypes.c_int, [P, P, P, ctypes.c_int, P]),
             "mdmc_render_buffers": (ctypes.c_int, [P, P, P, P]),
+            "mdmc_generate_volume": (ctypes.c_int, [ctypes.c_int32, P, P, P, P, P]),
+            "mdmc_generate_edge_case": (ctypes.c_int, [ctypes.c_int32, P, P, P, P, P]),
+            "mdmc_write_bin": (ctypes.c_int, [ctypes.c_char_p, P, P, P]),
             "mdmc_batch_create": (ctypes.c_int, [P, P, ctypes.c_int]),
             "mdmc_batch_destroy": (None, [P]),
             "mdmc_run_batch": (ctypes.c_int, [P, P, P, ctypes.c_int, P, P, P]),
@@ -457,6 +460,50 @@ class BatchedDualMarchingCubes:
         if h:
             self.lib.mdmc_batch_destroy(h)
             self.handle = None
+
+
+# SurfaceCase, UniformGrid.h:26-37
+SURFACES = {"sphere": 0, "torus": 1, "two_holed_torus": 2, "four_holed_torus": 3, "genus_two": 4, "iwp": 5,
+            "pw_hybrid": 6, "neovius": 7, "goursat": 8, "steiner_roman": 9}
+
+
+def generate_volume(surface, dims, stream=None):
+    """UniformGridHost::generateVolume (UniformGrid.inl:463-486) on the GPU:
+    the implicit surface `surface` (a SURFACES name or number) sampled on
+    [-1, 1]^3.  Returns (CUDA tensor [Z, Y, X] float32, origin, spacing)."""
+    import torch
+    lib = library()
+    case = SURFACES.get(surface, surface) if isinstance(surface, str) else int(surface)
+    d = np.asarray(dims, np.int32)
+    out = torch.empty((int(d[2]), int(d[1]), int(d[0])), dtype=torch.float32, device="cuda")
+    o, sp = np.zeros(3, np.float32), np.zeros(3, np.float32)
+    st = lib.mdmc_generate_volume(int(case), _ptr(d), out.data_ptr(), _ptr(o), _ptr(sp), _stream_handle(stream))
+    if st != 0:
+        raise MDMCError(st, "mdmc_generate_volume failed")
+    return out, o, sp
+
+
+def generate_edge_case(which, stream=None):
+    """UniformGridHost::generateEdgeCase (UniformGrid.inl:488-509): the 4x4x3
+    NonManifoldVertex0/1 grids.  Returns (CUDA tensor, dims, origin, spacing)."""
+    import torch
+    lib = library()
+    out = torch.empty((3, 4, 4), dtype=torch.float32, device="cuda")
+    d, o, sp = np.zeros(3, np.int32), np.zeros(3, np.float32), np.zeros(3, np.float32)
+    st = lib.mdmc_generate_edge_case(int(which), out.data_ptr(), _ptr(d), _ptr(o), _ptr(sp), _stream_handle(stream))
+    if st != 0:
+        raise MDMCError(st, "mdmc_generate_edge_case failed")
+    return out, [int(x) for x in d], o, sp
+
+
+def write_bin(path, samples, spacing):
+    """Writes a .bin volume (int32 dims, float32 spacing, uint16 samples) that
+    read_bin / UniformGridHost::readFromFile read back."""
+    arr = np.ascontiguousarray(samples, np.float32)
+    dims = np.asarray([arr.shape[2], arr.shape[1], arr.shape[0]], np.int32)
+    st = library().mdmc_write_bin(str(path).encode(), _ptr(dims), _ptr(np.asarray(spacing, np.float32)), _ptr(arr))
+    if st != 0:
+        raise MDMCError(st, "cannot write %s" % path)
 
 
 def case_tables():

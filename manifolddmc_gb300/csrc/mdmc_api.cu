@@ -996,6 +996,27 @@ mdmc_status mdmc_render_buffers(mdmc_context* c, float* vertices, uint32_t* indi
     return MDMC_OK;
 }
 
+mdmc_status mdmc_write_bin(const char* path, const int32_t dims[3], const float spacing[3], const float* host_samples) {
+    if (!path || !dims || !spacing || !host_samples || dims[0] < 1 || dims[1] < 1 || dims[2] < 1)
+        return MDMC_ERROR_INVALID_ARGUMENT;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return MDMC_ERROR_IO;
+    bool ok = std::fwrite(dims, sizeof(int32_t), 3, f) == 3 && std::fwrite(spacing, sizeof(float), 3, f) == 3;
+    const size_t n = (size_t)dims[0] * dims[1] * dims[2];
+    std::vector<uint16_t> buf(std::min<size_t>(n, (size_t)1 << 20));
+    for (size_t i = 0; ok && i < n; i += buf.size()) {
+        const size_t m = std::min(buf.size(), n - i);
+        for (size_t k = 0; k < m; ++k) {
+            // static_cast<unsigned short>(float): truncation; out-of-range values clamp here
+            const float v = host_samples[i + k];
+            buf[k] = v != v || v <= 0.f ? 0 : (v >= 65535.f ? 65535 : (uint16_t)v);
+        }
+        ok = std::fwrite(buf.data(), sizeof(uint16_t), m, f) == m;
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? MDMC_OK : MDMC_ERROR_IO;
+}
+
 mdmc_status mdmc_write_obj(mdmc_context* c, const char* path) {
     if (!c || !path || !c->haveMesh) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "no mesh or path");
     std::vector<float> p(3 * (size_t)c->V), n(3 * (size_t)c->V);
