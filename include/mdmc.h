@@ -213,6 +213,38 @@ MDMC_API mdmc_status mdmc_render_buffers(mdmc_context* context, float* vertices,
  * (Mesh.cu:446-510): v, vn, then one "f a//a b//b c//c d//d" line per face. */
 MDMC_API mdmc_status mdmc_write_obj(mdmc_context* context, const char* path);
 
+/* An indexed triangle mesh in device memory, owned by the context and valid
+ * until its next mdmc_run_standard_mc: positions and normals 3 floats per
+ * vertex, triangles 3 vertex ids each. */
+typedef struct mdmc_triangle_mesh {
+    int64_t num_vertices;
+    int64_t num_triangles;
+    float* positions;
+    float* normals;
+    int32_t* triangles;
+} mdmc_triangle_mesh;
+
+/* Standard Marching Cubes of the older CLI version (standard_mc and
+ * map_triangles, MarchingCubes/OriginalDMC/src/DualMarchingCubes.cu:201-328,
+ * its hash table VertexHashTable.h:81-113 replaced by an edge bit mask):
+ * one vertex per grid edge whose end samples lie on both sides of iso (a
+ * sample belongs to the inside when >= iso), at the linear crossing from the
+ * edge's low end, with the interpolated central-difference gradients
+ * (UniformGrid.h:279-321) divided by their length as its normal; triangles
+ * from the reference's t_pattern table.  Vertices are numbered by global edge
+ * id 3 * sample + axis, triangles by cell in (z, y, x) order and then table
+ * order (the reference numbers both in atomic order).  Refined or padded
+ * grids are read through the same on-demand view as mdmc_run.  The
+ * context's DMC mesh is left as it was.  Synchronous with respect to the
+ * stream; mesh may be NULL. */
+MDMC_API mdmc_status mdmc_run_standard_mc(mdmc_context* context, const mdmc_grid* grid, float iso_value,
+                                          mdmc_triangle_mesh* mesh, void* stream);
+
+/* Copies the last standard Marching Cubes mesh to host memory; any pointer
+ * may be NULL.  Synchronous with respect to the stream. */
+MDMC_API mdmc_status mdmc_download_triangle_mesh(mdmc_context* context, float* positions, float* normals,
+                                                 int32_t* triangles, void* stream);
+
 /* Adjoint of the last mdmc_run on the context (no counterpart in the
  * reference, which is not differentiable).  Given dL/dpositions (device, 3
  * floats per vertex of the last mesh), writes dL/dsamples for the grid samples

@@ -64,6 +64,11 @@ class Mesh(ctypes.Structure):
                 ("vertex_flags", ctypes.c_void_p)]
 
 
+class TriangleMesh(ctypes.Structure):
+    _fields_ = [("num_vertices", ctypes.c_int64), ("num_triangles", ctypes.c_int64),
+                ("positions", ctypes.c_void_p), ("normals", ctypes.c_void_p), ("triangles", ctypes.c_void_p)]
+
+
 class Stats(ctypes.Structure):
     _fields_ = [("num_dmc_vertices", ctypes.c_int64), ("num_dmc_quads", ctypes.c_int64),
                 ("num_active_cells", ctypes.c_int64), ("num_edges", ctypes.c_int64),
@@ -127,6 +132,8 @@ def library():
             "mdmc_case_tables": (None, [P, P]),
             "mdmc_backward": (ctypes.c_int, [P, P, P, ctypes.c_int, P]),
             "mdmc_render_buffers": (ctypes.c_int, [P, P, P, P]),
+            "mdmc_run_standard_mc": (ctypes.c_int, [P, P, ctypes.c_float, P, P]),
+            "mdmc_download_triangle_mesh": (ctypes.c_int, [P] * 5),
             "mdmc_generate_volume": (ctypes.c_int, [ctypes.c_int32, P, P, P, P, P]),
             "mdmc_generate_edge_case": (ctypes.c_int, [ctypes.c_int32, P, P, P, P, P]),
             "mdmc_write_bin": (ctypes.c_int, [ctypes.c_char_p, P, P, P]),
@@ -404,6 +411,23 @@ class DualMarchingCubes:
     def write_obj(self, path):
         """Mesh::writeToFile, Mesh.cu:446-510"""
         self._ctx.check(self._ctx.lib.mdmc_write_obj(self._ctx.handle, str(path).encode()))
+
+    def run_standard_mc(self, iso_value, grid, stream=None):
+        """Standard Marching Cubes of the older CLI version (standard_mc,
+        OriginalDMC/src/DualMarchingCubes.cu:201-328) on the same grid view as
+        run(); leaves the DMC mesh of the last run() as it was.  Returns host
+        arrays (positions [V, 3], normals [V, 3], triangles [T, 3] int32);
+        the device copies stay in self.triangle_mesh until the next call."""
+        g = grid.grid if isinstance(grid, UniformGrid) else grid
+        self.triangle_mesh = TriangleMesh()
+        self._ctx.check(self._ctx.lib.mdmc_run_standard_mc(self._ctx.handle, ctypes.byref(g), ctypes.c_float(iso_value),
+                                                           ctypes.byref(self.triangle_mesh), _stream_handle(stream)))
+        V, T = int(self.triangle_mesh.num_vertices), int(self.triangle_mesh.num_triangles)
+        pos, nrm = np.zeros((V, 3), np.float32), np.zeros((V, 3), np.float32)
+        tri = np.zeros((T, 3), np.int32)
+        self._ctx.check(self._ctx.lib.mdmc_download_triangle_mesh(self._ctx.handle, _ptr(pos), _ptr(nrm), _ptr(tri),
+                                                                  _stream_handle(stream)))
+        return pos, nrm, tri
 
 
 class BatchedDualMarchingCubes:

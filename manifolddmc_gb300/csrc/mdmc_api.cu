@@ -110,6 +110,11 @@ struct mdmc_context {
     DevBuf appV, appH, appF;
     // fan detection
     DevBuf isKey, fans, degree, slowFan;
+    // standard Marching Cubes: edge mask and the index of each word's first
+    // edge, per active cell its case and triangle offset, the vertices' edge
+    // ids, and the triangle mesh
+    DevBuf mcEdgeMask, mcEdgeFirst, mcCases, mcTriOffset, mcEdgeIds, mcPos, mcNrm, mcTris;
+    int64_t mcV = 0, mcT = 0;
     // events: start, dmc, halfedge, repair, detect, end
     cudaEvent_t ev[6] = {};
     // per-kernel events: refine, count, emit, quads, table, vertices (begin/end each)
@@ -552,6 +557,38 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
     return MDMC_OK;
 }
 
+// The DMC front end: the active-cell mask per x-row of cells (W words per
+// row, numWords in all) and the index of every word's first active cell
+// (cellFirst, the cell index the quad pass reads too); A = active cells.
+mdmc_status activeCells(mdmc_context* c, const GridDesc& g, float iso, int& W, int64_t& numWords, int64_t& A,
+                        cudaStream_t s) {
+    const GridGeom& geom = g.geom();
+    const int X = geom.X, Y = geom.Y, Z = geom.Z;
+    uint32_t* status = &c->counters.as<DevCounters>()->status;
+    const int64_t numRows = (X > 1 && Y > 1 && Z > 1) ? (int64_t)(Y - 1) * (Z - 1) : 0;
+    W = (X - 1 + 31) / 32;
+    numWords = numRows * (int64_t)W;
+    MDMC_CHECK(c, c->cellMask.ensure(sizeof(uint32_t) * (size_t)std::max<int64_t>(numWords, 1)));
+    MDMC_CHECK(c, c->cellFirst.ensure(sizeof(int) * (size_t)(numWords + 1)));
+    cudaEventRecord(c->kev[2], s);
+    if (g.refined && numWords > 0) MDMC_CHECK(c, cudaMemsetAsync(c->cellMask.p, 0, sizeof(uint32_t) * (size_t)numWords, s));
+    if (g.refined && g.ref.mayCross && 2 * (g.ref.r + 4) * (g.ref.r + 4) <= 512 && numWords > 0)
+        launchBlockMask(g.ref, iso, c->candidates.as<uint32_t>(), &c->counters.as<DevCounters>()->candidates,
+                        c->cellMask.as<uint32_t>(), W, status, s);
+    else
+        launchRowMask(g, iso, c->cellMask.as<uint32_t>(), (int)numRows, W, s);
+    launchWordCounts(c->cellMask.as<uint32_t>(), numWords, c->cellFirst.as<int>(), s);
+    mdmc_status st = scan<int>(c, c->cellFirst.as<int>(), c->cellFirst.as<int>(), numWords, s);
+    if (st != MDMC_OK) return st;
+    cudaEventRecord(c->kev[3], s);
+    MDMC_CHECK(c, cudaGetLastError());
+    if ((st = readInts(c, c->cellFirst.as<int>() + numWords, 1, s)) != MDMC_OK) return st;
+    A = c->hostInts[0];
+    const int64_t cells = numRows * (int64_t)(X - 1);
+    if (A < 0 || A > cells) return fail(c, MDMC_ERROR_CUDA, "inconsistent cell count from the mask pass");
+    return MDMC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -735,29 +772,10 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     if (st0 != MDMC_OK) return st0;
 
     // ---- DMC (performDualMarchingCubes) -----------------------------------------
-    // active-cell mask per x-row of cells, word counts -> index of every
-    // word's first active cell (the cell index the quad pass reads too)
-    const int64_t numRows = (X > 1 && Y > 1 && Z > 1) ? (int64_t)(Y - 1) * (Z - 1) : 0;
-    const int W = (X - 1 + 31) / 32;
-    const int64_t numWords = numRows * (int64_t)W;
-    MDMC_CHECK(c, c->cellMask.ensure(sizeof(uint32_t) * (size_t)std::max<int64_t>(numWords, 1)));
-    MDMC_CHECK(c, c->cellFirst.ensure(sizeof(int) * (size_t)(numWords + 1)));
-    cudaEventRecord(c->kev[2], s);
-    if (g.refined && numWords > 0) MDMC_CHECK(c, cudaMemsetAsync(c->cellMask.p, 0, sizeof(uint32_t) * (size_t)numWords, s));
-    if (g.refined && g.ref.mayCross && 2 * (g.ref.r + 4) * (g.ref.r + 4) <= 512 && numWords > 0)
-        launchBlockMask(g.ref, iso, c->candidates.as<uint32_t>(), &ctr->candidates, c->cellMask.as<uint32_t>(), W, status,
-                        s);
-    else
-        launchRowMask(g, iso, c->cellMask.as<uint32_t>(), (int)numRows, W, s);
-    launchWordCounts(c->cellMask.as<uint32_t>(), numWords, c->cellFirst.as<int>(), s);
-    mdmc_status st = scan<int>(c, c->cellFirst.as<int>(), c->cellFirst.as<int>(), numWords, s);
+    int64_t numWords = 0, A = 0;
+    int W = 0;
+    mdmc_status st = activeCells(c, g, iso, W, numWords, A, s);
     if (st != MDMC_OK) return st;
-    cudaEventRecord(c->kev[3], s);
-    MDMC_CHECK(c, cudaGetLastError());
-    if ((st = readInts(c, c->cellFirst.as<int>() + numWords, 1, s)) != MDMC_OK) return st;
-    const int64_t A = c->hostInts[0];
-    const int64_t cells = numRows * (int64_t)(X - 1);
-    if (A < 0 || A > cells) return fail(c, MDMC_ERROR_CUDA, "inconsistent cell count from the mask pass");
     c->stats.num_active_cells = A;
 
     // the active cells' records, contour and quad counts, and their offsets
@@ -905,6 +923,96 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
         c->err = "device limits hit: " + statusText(hc.status);
         if (hc.status & (kStatusProbeLimit | kStatusMissingCell)) return MDMC_ERROR_LIMIT;
     }
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_run_standard_mc(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_triangle_mesh* mesh,
+                                 void* stream) {
+    if (!c || !grid) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "null argument");
+    c->err.clear();
+    (void)cudaGetLastError();
+    const int X = grid->dims[0], Y = grid->dims[1], Z = grid->dims[2];
+    if (X < 1 || Y < 1 || Z < 1) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "invalid grid dims");
+    if (3 * (uint64_t)X * Y * Z >= 0xFFFFFFFFull)
+        return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "grid has 2^32 edges or more");
+    cudaStream_t s = (cudaStream_t)stream;
+    c->mcV = c->mcT = 0;
+    if (mesh) std::memset(mesh, 0, sizeof *mesh);
+    DevCounters* ctr = c->counters.as<DevCounters>();
+    uint32_t* status = &ctr->status;
+    MDMC_CHECK(c, cudaMemsetAsync(ctr, 0, sizeof(DevCounters), s));
+    GridDesc g;
+    mdmc_status st = makeGridDesc(c, grid, iso, g, s);
+    if (st != MDMC_OK) return st;
+    int64_t numWords = 0, A = 0;
+    int W = 0;
+    if ((st = activeCells(c, g, iso, W, numWords, A, s)) != MDMC_OK) return st;
+    if (A > 0) {
+        MDMC_CHECK(c, c->cellIds.ensure(sizeof(uint32_t) * (size_t)A));
+        launchScatterCells(c->cellMask.as<uint32_t>(), c->cellFirst.as<int>(), numWords, W, X, Y,
+                           c->cellIds.as<uint32_t>(), (int)A, status, s);
+        // intersected edges: bit 3x + axis of the words of sample row (y, z)
+        const int W3 = (3 * X + 31) / 32;
+        const int64_t nE = (int64_t)Y * Z * W3;
+        MDMC_CHECK(c, c->mcEdgeMask.ensure(sizeof(uint32_t) * (size_t)nE));
+        MDMC_CHECK(c, c->mcEdgeFirst.ensure(sizeof(int) * (size_t)(nE + 1)));
+        MDMC_CHECK(c, c->mcCases.ensure((size_t)A));
+        MDMC_CHECK(c, c->mcTriOffset.ensure(sizeof(int) * (size_t)(A + 1)));
+        MDMC_CHECK(c, cudaMemsetAsync(c->mcEdgeMask.p, 0, sizeof(uint32_t) * (size_t)nE, s));
+        launchMCMarkEdges(g, iso, c->cellIds.as<uint32_t>(), (int)A, W3, c->mcEdgeMask.as<uint32_t>(),
+                          c->mcCases.as<uint8_t>(), c->mcTriOffset.as<int>(), status, s);
+        launchWordCounts(c->mcEdgeMask.as<uint32_t>(), nE, c->mcEdgeFirst.as<int>(), s);
+        if ((st = scan<int>(c, c->mcEdgeFirst.as<int>(), c->mcEdgeFirst.as<int>(), nE, s)) != MDMC_OK) return st;
+        if ((st = scan<int>(c, c->mcTriOffset.as<int>(), c->mcTriOffset.as<int>(), A, s)) != MDMC_OK) return st;
+        MDMC_CHECK(c, cudaGetLastError());
+        if ((st = readInts(c, c->mcEdgeFirst.as<int>() + nE, 1, s)) != MDMC_OK) return st;
+        const int64_t V = c->hostInts[0];
+        if ((st = readInts(c, c->mcTriOffset.as<int>() + A, 1, s)) != MDMC_OK) return st;
+        const int64_t T = c->hostInts[0];
+        if (V < 3 || V > 12 * A || T < 1 || T > 5 * A)
+            return fail(c, MDMC_ERROR_CUDA, "inconsistent vertex or triangle count from the edge pass");
+        MDMC_CHECK(c, c->mcEdgeIds.ensure(sizeof(uint32_t) * (size_t)V));
+        MDMC_CHECK(c, c->mcPos.ensure(sizeof(float) * 3 * (size_t)V));
+        MDMC_CHECK(c, c->mcNrm.ensure(sizeof(float) * 3 * (size_t)V));
+        MDMC_CHECK(c, c->mcTris.ensure(sizeof(int) * 3 * (size_t)T));
+        launchMCScatterEdges(c->mcEdgeMask.as<uint32_t>(), c->mcEdgeFirst.as<int>(), nE, W3, X,
+                             c->mcEdgeIds.as<uint32_t>(), (int)V, status, s);
+        launchMCVertices(g, iso, c->mcEdgeIds.as<uint32_t>(), (int)V, c->mcPos.as<float>(), c->mcNrm.as<float>(), s);
+        launchMCTriangles(c->cellIds.as<uint32_t>(), c->mcCases.as<uint8_t>(), c->mcTriOffset.as<int>(), (int)A, X, Y, W3,
+                          c->mcEdgeMask.as<uint32_t>(), c->mcEdgeFirst.as<int>(), nE, c->mcTris.as<int>(), (int)T, status,
+                          s);
+        MDMC_CHECK(c, cudaGetLastError());
+        c->mcV = V;
+        c->mcT = T;
+    }
+    MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
+    MDMC_CHECK(c, cudaStreamSynchronize(s));
+    if (mesh) {
+        mesh->num_vertices = c->mcV;
+        mesh->num_triangles = c->mcT;
+        mesh->positions = c->mcPos.as<float>();
+        mesh->normals = c->mcNrm.as<float>();
+        mesh->triangles = c->mcTris.as<int32_t>();
+    }
+    const uint32_t hs = c->hostCounters->status;
+    if (hs) {
+        c->err = "device limits hit: " + statusText(hs);
+        return MDMC_ERROR_LIMIT;
+    }
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_download_triangle_mesh(mdmc_context* c, float* positions, float* normals, int32_t* triangles,
+                                        void* stream) {
+    if (!c) return MDMC_ERROR_INVALID_ARGUMENT;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (positions && c->mcV)
+        MDMC_CHECK(c, cudaMemcpyAsync(positions, c->mcPos.p, sizeof(float) * 3 * (size_t)c->mcV, cudaMemcpyDeviceToHost, s));
+    if (normals && c->mcV)
+        MDMC_CHECK(c, cudaMemcpyAsync(normals, c->mcNrm.p, sizeof(float) * 3 * (size_t)c->mcV, cudaMemcpyDeviceToHost, s));
+    if (triangles && c->mcT)
+        MDMC_CHECK(c, cudaMemcpyAsync(triangles, c->mcTris.p, sizeof(int) * 3 * (size_t)c->mcT, cudaMemcpyDeviceToHost, s));
+    MDMC_CHECK(c, cudaStreamSynchronize(s));
     return MDMC_OK;
 }
 

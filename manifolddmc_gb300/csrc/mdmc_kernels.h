@@ -102,6 +102,17 @@ void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords
                         int numActive, uint32_t* status, cudaStream_t s);
 void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, ActiveCell* act, int2* counts,
                       int numActive, uint32_t* status, cudaStream_t s);
+// standard Marching Cubes (edge mask over global edge ids 3 * sample + axis,
+// W3 words per sample row)
+void launchMCMarkEdges(const GridDesc& g, float iso, const uint32_t* cellIds, int numActive, int W3, uint32_t* edgeMask,
+                       uint8_t* cases, int* triCount, uint32_t* status, cudaStream_t s);
+void launchMCScatterEdges(const uint32_t* edgeMask, const int* first, int64_t numWords, int W3, int X, uint32_t* edgeIds,
+                          int numVertices, uint32_t* status, cudaStream_t s);
+void launchMCVertices(const GridDesc& g, float iso, const uint32_t* edgeIds, int numVertices, float* pos, float* nrm,
+                      cudaStream_t s);
+void launchMCTriangles(const uint32_t* cellIds, const uint8_t* cases, const int* triOffset, int numActive, int X, int Y,
+                       int W3, const uint32_t* edgeMask, const int* edgeFirst, int64_t numWords, int* tris,
+                       int numTriangles, uint32_t* status, cudaStream_t s);
 void launchFinishCells(ActiveCell* act, const int2* offsets, int numActive, int X, int Y, int* quadOwner, int numQuads,
                        uint32_t* status, cudaStream_t s);
 void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, int numActive,

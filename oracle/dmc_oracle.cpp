@@ -13,6 +13,7 @@
 
 #include "dmc_oracle.h"
 #include "mc_contour_table_oracle.h"
+#include "mc_triangle_table_oracle.h"
 
 #include <algorithm>
 #include <cmath>
@@ -1193,6 +1194,78 @@ static void detectNonManifoldVertices(Mesh& m) {
 }
 
 // ------------------------------------------------------------------------ //
+// Standard Marching Cubes (OriginalDMC standard_mc, O/DualMarchingCubes.cu:
+// 201-307, and map_triangles :316-328): one vertex per intersected grid edge,
+// at the linear crossing, with the interpolated corner gradient divided by its
+// length; triangles from the case table.  The reference numbers vertices and
+// triangles in atomic order; here vertices follow the global edge id
+// 3 * sample + axis and triangles the cells' (z, y, x) order, then the table.
+// ------------------------------------------------------------------------ //
+struct MCMesh {
+    std::vector<float> pos, nrm;
+    std::vector<int> tris;
+};
+
+// central-difference gradient at grid point (x, y, z) with clamped neighbours
+// (UniformGrid::gradient, O/UniformGrid.h:278-330: each corner's entry)
+static V3 pointGradient(const Grid& g, int x, int y, int z) {
+    V3 d = g.dl();
+    float gx = 0.5f * (g.atClamped(x + 1, y, z) - g.atClamped(x - 1, y, z)) / d.x;
+    float gy = 0.5f * (g.atClamped(x, y + 1, z) - g.atClamped(x, y - 1, z)) / d.y;
+    float gz = 0.5f * (g.atClamped(x, y, z + 1) - g.atClamped(x, y, z - 1)) / d.z;
+    return v3(gx, gy, gz);
+}
+
+static MCMesh* standardMC(const Grid& g, float iso) {
+    MCMesh* m = new MCMesh();
+    const int X = g.d[0], Y = g.d[1], Z = g.d[2];
+    if (X < 2 || Y < 2 || Z < 2) return m;  // no cells
+    const size_t S = (size_t)X * Y * Z;
+    std::vector<int> vid(3 * S, -1);
+    const V3 o = g.o(), dl = g.dl();
+    for (int z = 0; z < Z; ++z)
+        for (int y = 0; y < Y; ++y)
+            for (int x = 0; x < X; ++x)
+                for (int a = 0; a < 3; ++a) {
+                    const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
+                    if (x1 >= X || y1 >= Y || z1 >= Z) continue;
+                    const float u0 = g.at(x, y, z), u1 = g.at(x1, y1, z1);
+                    if ((u0 >= iso) == (u1 >= iso)) continue;
+                    const size_t e = 3 * (((size_t)z * Y + y) * X + x) + a;
+                    vid[e] = (int)(m->pos.size() / 3);
+                    const float l = (iso - u0) / (u1 - u0);
+                    const float p0[3] = {o.x + (float)x * dl.x, o.y + (float)y * dl.y, o.z + (float)z * dl.z};
+                    const float p1[3] = {o.x + (float)x1 * dl.x, o.y + (float)y1 * dl.y, o.z + (float)z1 * dl.z};
+                    const V3 n0 = pointGradient(g, x, y, z), n1 = pointGradient(g, x1, y1, z1);
+                    V3 ni = v3(n0.x + l * (n1.x - n0.x), n0.y + l * (n1.y - n0.y), n0.z + l * (n1.z - n0.z));
+                    const float f = std::sqrt(ni.x * ni.x + ni.y * ni.y + ni.z * ni.z);
+                    ni = v3(ni.x / f, ni.y / f, ni.z / f);
+                    for (int k = 0; k < 3; ++k) m->pos.push_back(p0[k] + l * (p1[k] - p0[k]));
+                    m->nrm.push_back(ni.x);
+                    m->nrm.push_back(ni.y);
+                    m->nrm.push_back(ni.z);
+                }
+    for (int z = 0; z + 1 < Z; ++z)
+        for (int y = 0; y + 1 < Y; ++y)
+            for (int x = 0; x + 1 < X; ++x) {
+                float sv[8];
+                cornerValues(g, x, y, z, sv);
+                int cs = 0;
+                for (int i = 0; i < 8; ++i) cs |= (sv[i] >= iso ? 1 : 0) << i;
+                const uint64_t w = kTriangleTable[cs];
+                const int n = (int)(w & 0xF);
+                for (int k = 0; k < 3 * n; ++k) {
+                    const int e = (int)((w >> (4 + 4 * k)) & 0xF);
+                    const int a0 = kEdgeV0[e];
+                    const size_t gid = 3 * (((size_t)(z + ((a0 >> 2) & 1)) * Y + (y + ((a0 >> 1) & 1))) * X +
+                                            (x + (a0 & 1))) + kEdgeAxis[e];
+                    m->tris.push_back(vid[gid]);
+                }
+            }
+    return m;
+}
+
+// ------------------------------------------------------------------------ //
 // HalfedgeMesh::initialize from a quad list, D/Halfedges/HalfedgeMesh.cu:14-60,
 // :173-291, :848-857: halfedge i of quad q is 4q+i, twins and flags from the
 // edge table, face attributes from the quads'
@@ -1565,6 +1638,26 @@ void mdmc_oracle_get_dmc(const void* res, float* positions, float* normals, int*
 }
 
 void mdmc_oracle_free(void* res) { delete (oracle::Result*)res; }
+
+void* mdmc_oracle_standard_mc(const float* grid, const int dims[3], const float origin[3], const float spacing[3],
+                              float iso, int64_t counts[2]) {
+    oracle::Grid g;
+    for (int a = 0; a < 3; ++a) { g.d[a] = dims[a]; g.origin[a] = origin[a]; g.deltas[a] = spacing[a]; }
+    g.v = grid;
+    oracle::MCMesh* m = oracle::standardMC(g, iso);
+    counts[0] = (int64_t)(m->pos.size() / 3);
+    counts[1] = (int64_t)(m->tris.size() / 3);
+    return m;
+}
+
+void mdmc_oracle_get_standard_mc(const void* mesh, float* positions, float* normals, int* triangles) {
+    const oracle::MCMesh* m = (const oracle::MCMesh*)mesh;
+    if (positions) std::memcpy(positions, m->pos.data(), m->pos.size() * sizeof(float));
+    if (normals) std::memcpy(normals, m->nrm.data(), m->nrm.size() * sizeof(float));
+    if (triangles) std::memcpy(triangles, m->tris.data(), m->tris.size() * sizeof(int));
+}
+
+void mdmc_oracle_free_standard_mc(void* mesh) { delete (oracle::MCMesh*)mesh; }
 
 void mdmc_oracle_get_topology(const void* res, int* cells, uint16_t* edges, int* parents) {
     const oracle::Result* r = (const oracle::Result*)res;

@@ -89,6 +89,14 @@ void mdmc_oracle_get_dmc(const void* result, float* positions, float* normals, i
                          uint16_t* quad_attr);
 void mdmc_oracle_free(void* result);
 
+/* Standard Marching Cubes of the older CLI version (OriginalDMC standard_mc,
+ * O/DualMarchingCubes.cu:201-328): vertices by global edge id 3 * sample +
+ * axis, triangles by cell then table order.  counts = {vertices, triangles}. */
+void* mdmc_oracle_standard_mc(const float* grid, const int dims[3], const float origin[3], const float spacing[3],
+                              float iso, int64_t counts[2]);
+void mdmc_oracle_get_standard_mc(const void* mesh, float* positions, float* normals, int* triangles);
+void mdmc_oracle_free_standard_mc(void* mesh);
+
 /* Differentiable path (no reference counterpart; surface iteration off).
  * Topology of a result: per DMC vertex its cell (x, y, z) and the 12-bit mask
  * of its contour's cell edges; per final vertex the DMC vertex it descends

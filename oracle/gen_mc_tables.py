@@ -15,6 +15,12 @@ and a SHA-256 digest of the words and of the ambiguity marks to
 ``tests/golden/mc_tables_digest.json`` so that the tests can check both
 headers (and the ambiguity rule written in code) without the reference.
 
+The standard Marching Cubes path reads the triangle table of the older CLI
+version (``t_pattern``, MarchingCubes/OriginalDMC/src/DualMarchingCubes.h:160)
+with its intersected-edge masks (``e_pattern``, :123).  Each case's triangles
+are packed into one 64-bit word: bits 0-3 the triangle count, then the cell
+edges of the triangles, three per triangle, one nibble each, in table order.
+
 Run from the repository root:  python3 oracle/gen_mc_tables.py [reference_root]
 """
 import hashlib
@@ -25,6 +31,7 @@ import sys
 
 REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 SRC = os.path.join(REF, "MarchingCubes/VisualDMC/src/DMC/DualMarchingCubes.cpp")
+SRC_MC = os.path.join(REF, "MarchingCubes/OriginalDMC/src/DualMarchingCubes.h")
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 
@@ -100,6 +107,44 @@ def main():
         "num_ambiguous": sum(ambiguous),
         "source": "MarchingCubes/VisualDMC/src/DMC/DualMarchingCubes.cpp:301,564",
     }
+    # standard Marching Cubes triangle table (OriginalDMC)
+    src_mc = open(SRC_MC, encoding="latin-1").read()
+    e_pat = _array(src_mc, "e_pattern = std::array")
+    t_pat = _array(src_mc, "t_pattern = std::array")
+    assert len(e_pat) == 256 and len(t_pat) == 4096
+    tri_words = []
+    for c in range(256):
+        row = t_pat[16 * c:16 * c + 16]
+        n = 0
+        while n < 5 and row[3 * n] != -1:
+            n += 1
+        w = n
+        for k in range(3 * n):
+            assert 0 <= row[k] < 12
+            w |= row[k] << (4 + 4 * k)
+        tri_words.append(w)
+    tlines = []
+    for c in range(0, 256, 4):
+        tlines.append("    " + ", ".join("0x%016xULL" % w for w in tri_words[c:c + 4]) + ",")
+    ttable = "\n".join(tlines)
+    theader = (
+        "// Generated by oracle/gen_mc_tables.py -- do not edit by hand.\n"
+        "// Standard Marching Cubes triangles per case (bit i set <=> corner i >= iso):\n"
+        "// bits 0-3 = number of triangles, then 3 cell edges per triangle, one nibble\n"
+        "// each, in the order of the reference's t_pattern\n"
+        "// (MarchingCubes/OriginalDMC/src/DualMarchingCubes.h:160).\n"
+    )
+    with open(os.path.join(ROOT, "manifolddmc_gb300", "csrc", "mc_triangle_table.h"), "w") as f:
+        f.write("#pragma once\n" + theader + "namespace mdmc {\n"
+                "__device__ const unsigned long long kTriangleTable[256] = {\n" + ttable + "\n};\n"
+                "static const unsigned long long kTriangleTableHost[256] = {\n" + ttable + "\n};\n"
+                "}  // namespace mdmc\n")
+    with open(os.path.join(ROOT, "oracle", "mc_triangle_table_oracle.h"), "w") as f:
+        f.write("#pragma once\n" + theader + "namespace oracle {\nstatic const unsigned long long kTriangleTable[256] = {\n"
+                + ttable + "\n};\n}  // namespace oracle\n")
+    digest["triangle_words_sha256"] = hashlib.sha256(b"".join(w.to_bytes(8, "little") for w in tri_words)).hexdigest()
+    digest["edge_patterns_sha256"] = hashlib.sha256(b"".join(v.to_bytes(2, "little") for v in e_pat)).hexdigest()
+    digest["triangle_source"] = "MarchingCubes/OriginalDMC/src/DualMarchingCubes.h:123,160"
     with open(os.path.join(ROOT, "tests", "golden", "mc_tables_digest.json"), "w") as f:
         json.dump(digest, f, indent=1)
         f.write("\n")

@@ -38,7 +38,8 @@ class OracleOptions(ctypes.Structure):
 
 def build_oracle():
     """Builds oracle/_build/libmdmc_oracle.so when it is missing or stale."""
-    srcs = [ORACLE_DIR / n for n in ("dmc_oracle.cpp", "dmc_oracle.h", "mc_contour_table_oracle.h")]
+    srcs = [ORACLE_DIR / n for n in ("dmc_oracle.cpp", "dmc_oracle.h", "mc_contour_table_oracle.h",
+                                     "mc_triangle_table_oracle.h")]
     if ORACLE_SO.exists() and all(ORACLE_SO.stat().st_mtime >= s.stat().st_mtime for s in srcs):
         return
     subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], check=True)
@@ -63,6 +64,10 @@ def oracle():
                                                ctypes.c_void_p]
             lib.mdmc_oracle_read_bin.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 4
             lib.mdmc_oracle_get_topology.argtypes = [ctypes.c_void_p] * 4
+            lib.mdmc_oracle_standard_mc.restype = ctypes.c_void_p
+            lib.mdmc_oracle_standard_mc.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_float, ctypes.c_void_p]
+            lib.mdmc_oracle_get_standard_mc.argtypes = [ctypes.c_void_p] * 4
+            lib.mdmc_oracle_free_standard_mc.argtypes = [ctypes.c_void_p]
             lib.mdmc_oracle_positions_f64.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_double, ctypes.c_void_p]
             lib.mdmc_oracle_backward.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_double, ctypes.c_void_p,
                                                                          ctypes.c_void_p]
@@ -290,3 +295,19 @@ def sphere_sdf(n, radius, center=None):
     c = (n - 1) / 2.0 if center is None else center
     z, y, x = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
     return (np.sqrt((x - c) ** 2 + (y - c) ** 2 + (z - c) ** 2) - radius).astype(np.float32)
+
+
+def oracle_standard_mc(grid, dims, origin, spacing, iso):
+    """The oracle's standard Marching Cubes: (positions [V,3], normals [V,3], triangles [T,3])."""
+    lib = oracle()
+    grid = np.ascontiguousarray(grid, np.float32).reshape(-1)
+    counts = np.zeros(2, np.int64)
+    m = lib.mdmc_oracle_standard_mc(_p(grid), _p(np.asarray(dims, np.int32)), _p(np.asarray(origin, np.float32)),
+                                    _p(np.asarray(spacing, np.float32)), ctypes.c_float(iso), _p(counts))
+    try:
+        V, T = int(counts[0]), int(counts[1])
+        pos, nrm, tri = np.zeros((V, 3), np.float32), np.zeros((V, 3), np.float32), np.zeros((T, 3), np.int32)
+        lib.mdmc_oracle_get_standard_mc(m, _p(pos), _p(nrm), _p(tri))
+        return pos, nrm, tri
+    finally:
+        lib.mdmc_oracle_free_standard_mc(m)
