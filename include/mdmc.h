@@ -245,6 +245,34 @@ MDMC_API mdmc_status mdmc_run_standard_mc(mdmc_context* context, const mdmc_grid
 MDMC_API mdmc_status mdmc_download_triangle_mesh(mdmc_context* context, float* positions, float* normals,
                                                  int32_t* triangles, void* stream);
 
+/* Face coloring of the older CLI version (FaceColoring::colorFaces,
+ * MarchingCubes/OriginalDMC/src/FaceColoring.cu:116-141, kernels :5-116) on
+ * the last run's mesh, in place: the color bits (0-4) of the face attributes
+ * go from the DMC's 24 grid-edge colors to 0-4.  Classes 5..23 in turn, each
+ * face takes the first color of 0..4 that no face across one of its edges
+ * holds (the test for 4 skips the fourth neighbour, as at :63); then every
+ * face of color 4 takes the first free color of 0..3.  A face whose
+ * neighbour has its own class sees that neighbour's color from before the
+ * class's pass (the reference reads it live; with a proper grid-edge
+ * coloring no two such faces touch).  Asynchronous on the stream. */
+MDMC_API mdmc_status mdmc_color_faces(mdmc_context* context, void* stream);
+
+/* quadrilateral_to_triangle (MarchingCubes/OriginalDMC/src/
+ * DualMarchingCubes.cu:51-60): quad q = (v0, v1, v2, v3) gives triangles
+ * 2q = (v0, v1, v3) and 2q + 1 = (v3, v2, v0).  Device arrays: quads
+ * 4 * num_quads ints, triangles 6 * num_quads ints.  Asynchronous. */
+MDMC_API mdmc_status mdmc_quads_to_triangles(const int32_t* quads, int64_t num_quads, int32_t* triangles,
+                                             void* stream);
+
+/* Mean-ratio element quality (mean_ratio_measure, MarchingCubes/OriginalDMC/
+ * src/DualMarchingCubes.cu:93-107; QualityMeasure::mean_ratio,
+ * QualityMeasure.h:45-66): per triangle 2 sqrt(3) |(p1-p0) x (p2-p0)| over the
+ * sum of its squared edge lengths.  Device arrays; a triangle with a vertex id
+ * outside [0, num_vertices) gets NaN and sets *bad_index to 1 (bad_index may
+ * be NULL).  Asynchronous on the stream. */
+MDMC_API mdmc_status mdmc_mean_ratio(const float* positions, int64_t num_vertices, const int32_t* triangles,
+                                     int64_t num_triangles, float* quality, uint32_t* bad_index, void* stream);
+
 /* Adjoint of the last mdmc_run on the context (no counterpart in the
  * reference, which is not differentiable).  Given dL/dpositions (device, 3
  * floats per vertex of the last mesh), writes dL/dsamples for the grid samples

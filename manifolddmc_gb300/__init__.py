@@ -134,6 +134,9 @@ def library():
             "mdmc_render_buffers": (ctypes.c_int, [P, P, P, P]),
             "mdmc_run_standard_mc": (ctypes.c_int, [P, P, ctypes.c_float, P, P]),
             "mdmc_download_triangle_mesh": (ctypes.c_int, [P] * 5),
+            "mdmc_color_faces": (ctypes.c_int, [P, P]),
+            "mdmc_quads_to_triangles": (ctypes.c_int, [P, ctypes.c_int64, P, P]),
+            "mdmc_mean_ratio": (ctypes.c_int, [P, ctypes.c_int64, P, ctypes.c_int64, P, P, P]),
             "mdmc_generate_volume": (ctypes.c_int, [ctypes.c_int32, P, P, P, P, P]),
             "mdmc_generate_edge_case": (ctypes.c_int, [ctypes.c_int32, P, P, P, P, P]),
             "mdmc_write_bin": (ctypes.c_int, [ctypes.c_char_p, P, P, P]),
@@ -412,6 +415,11 @@ class DualMarchingCubes:
         """Mesh::writeToFile, Mesh.cu:446-510"""
         self._ctx.check(self._ctx.lib.mdmc_write_obj(self._ctx.handle, str(path).encode()))
 
+    def color_faces(self, stream=None):
+        """FaceColoring::colorFaces (OriginalDMC/src/FaceColoring.cu:116-141) on
+        the last run's mesh: face colors 24 -> 5, in place."""
+        self._ctx.check(self._ctx.lib.mdmc_color_faces(self._ctx.handle, _stream_handle(stream)))
+
     def run_standard_mc(self, iso_value, grid, stream=None):
         """Standard Marching Cubes of the older CLI version (standard_mc,
         OriginalDMC/src/DualMarchingCubes.cu:201-328) on the same grid view as
@@ -537,3 +545,33 @@ def case_tables():
     a = np.zeros(256, np.uint8)
     lib.mdmc_case_tables(_ptr(w), _ptr(a))
     return w, a
+
+
+def quads_to_triangles(quads, stream=None):
+    """quadrilateral_to_triangle (OriginalDMC/src/DualMarchingCubes.cu:51-60):
+    CUDA int32 tensor [Q, 4] -> [2Q, 3], quad (v0, v1, v2, v3) giving
+    (v0, v1, v3) and (v3, v2, v0)."""
+    import torch
+    q = quads.contiguous()
+    out = torch.empty((2 * q.shape[0], 3), dtype=torch.int32, device=q.device)
+    st = library().mdmc_quads_to_triangles(_dev_ptr(q), int(q.shape[0]), _dev_ptr(out), _stream_handle(stream))
+    if st != 0:
+        raise MDMCError(st, "mdmc_quads_to_triangles failed")
+    return out
+
+
+def mean_ratio(positions, triangles, stream=None):
+    """Mean-ratio quality per triangle (QualityMeasure::mean_ratio,
+    OriginalDMC/src/QualityMeasure.h:45-66) of CUDA tensors positions [V, 3]
+    float32 and triangles [T, 3] int32; raises on a vertex id outside [0, V)."""
+    import torch
+    p, t = positions.contiguous(), triangles.contiguous()
+    q = torch.empty(t.shape[0], dtype=torch.float32, device=t.device)
+    bad = torch.zeros(1, dtype=torch.int32, device=t.device)
+    st = library().mdmc_mean_ratio(_dev_ptr(p), int(p.shape[0]), _dev_ptr(t), int(t.shape[0]), _dev_ptr(q),
+                                   _dev_ptr(bad), _stream_handle(stream))
+    if st != 0:
+        raise MDMCError(st, "mdmc_mean_ratio failed")
+    if int(bad.item()):
+        raise MDMCError(1, "triangle vertex id outside the vertex array")
+    return q

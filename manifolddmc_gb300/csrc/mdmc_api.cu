@@ -114,6 +114,8 @@ struct mdmc_context {
     // edge, per active cell its case and triangle offset, the vertices' edge
     // ids, and the triangle mesh
     DevBuf mcEdgeMask, mcEdgeFirst, mcCases, mcTriOffset, mcEdgeIds, mcPos, mcNrm, mcTris;
+    // face coloring scratch
+    DevBuf colorOrig;
     int64_t mcV = 0, mcT = 0;
     // events: start, dmc, halfedge, repair, detect, end
     cudaEvent_t ev[6] = {};
@@ -1100,6 +1102,19 @@ mdmc_status mdmc_render_buffers(mdmc_context* c, float* vertices, uint32_t* indi
     if (!c->haveMesh) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "no mesh: run first");
     launchRenderBuffers(c->pos.as<float>(), c->nrm.as<float>(), c->vflags.as<uint8_t>(), c->vertexHE.as<int>(),
                         (int)c->V, c->quads.as<int4>(), (int)c->F, vertices, indices, (cudaStream_t)stream);
+    MDMC_CHECK(c, cudaGetLastError());
+    return MDMC_OK;
+}
+
+mdmc_status mdmc_color_faces(mdmc_context* c, void* stream) {
+    if (!c) return MDMC_ERROR_INVALID_ARGUMENT;
+    c->err.clear();
+    (void)cudaGetLastError();
+    if (!c->haveMesh) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "no mesh: run first");
+    if (c->F == 0) return MDMC_OK;
+    MDMC_CHECK(c, c->colorOrig.ensure((size_t)c->F));
+    launchColorFaces(c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(), c->colorOrig.as<uint8_t>(),
+                     (int)c->F, (int)c->H, (cudaStream_t)stream);
     MDMC_CHECK(c, cudaGetLastError());
     return MDMC_OK;
 }

@@ -162,6 +162,9 @@ void launchBackwardCells(const GridDesc& g, float iso, const ActiveCell* act, in
 void launchRenderBuffers(const float* pos, const float* nrm, const uint8_t* vflags, const int* vertexHE, int numVertices,
                          const int4* quads, int numFaces, float* vertices, uint32_t* indices, cudaStream_t s);
 
+// face coloring 24 -> 5 colors in place (orig: one byte per face of scratch)
+void launchColorFaces(const int4* he, const int* faceFirst, uint16_t* attr, uint8_t* orig, int numFaces, int numHalfedges,
+                      cudaStream_t s);
 void launchFlagNMFaces(const uint16_t* attr, int numFaces, int* flags, cudaStream_t s);
 void launchCompactNMFaces(const int* flags, const int* offsets, int numFaces, int* nmFaces, cudaStream_t s);
 void launchFillInt(int* p, int64_t n, int v, cudaStream_t s);

@@ -1797,4 +1797,95 @@ void mdmc_oracle_refine_backward(const double* dout, const int dims[3], int r, i
 
 int mdmc_oracle_case_ambiguous(int c) { return oracle::caseIsAmbiguous(c) ? 1 : 0; }
 
+// FaceColoring::colorFaces (O/FaceColoring.cu:116-141; color_faces :13-66,
+// optimize_face_coloring :67-116): classes 5..23 in turn pick the first free
+// color of 0..4 (the test for 4 compares c2 twice and never c3, :63), then
+// the faces of color 4 the first free of 0..3.  Faces of the class being
+// recolored see each other with their color from before that pass.
+void mdmc_oracle_color_faces(const int32_t* halfedges, int64_t num_halfedges, const int32_t* face_first,
+                             uint16_t* face_attr, int64_t num_faces) {
+    std::vector<int> orig(num_faces);
+    auto neighbours = [&](int64_t f, int cls, const std::vector<int>& mark, int nc[4]) {
+        int e = face_first[f];
+        for (int k = 0; k < 4; ++k) {
+            nc[k] = -1;
+            if (e < 0 || e >= num_halfedges) continue;
+            const int t = halfedges[4 * (int64_t)e + 3];
+            if (t > -1 && t < num_halfedges) {
+                const int g = halfedges[4 * (int64_t)t + 1];
+                if (g >= 0 && g < num_faces) nc[k] = mark[g] == cls ? cls : (face_attr[g] & 0x1F);
+            }
+            e = halfedges[4 * (int64_t)e + 2];
+        }
+    };
+    auto setColor = [&](int64_t f, int c) { face_attr[f] = (uint16_t)((face_attr[f] & ~0x1F) | c); };
+    for (int64_t f = 0; f < num_faces; ++f) orig[f] = face_attr[f] & 0x1F;
+    for (int cls = 5; cls < 24; ++cls) {
+        std::vector<std::pair<int64_t, int>> next;
+        for (int64_t f = 0; f < num_faces; ++f) {
+            if (orig[f] != cls) continue;
+            int c[4];
+            neighbours(f, cls, orig, c);
+            int pick = -1;
+            for (int k = 0; k < 4 && pick < 0; ++k)
+                if (c[0] != k && c[1] != k && c[2] != k && c[3] != k) pick = k;
+            if (pick < 0 && c[0] != 4 && c[1] != 4 && c[2] != 4) pick = 4;
+            if (pick >= 0) next.push_back({f, pick});
+        }
+        for (auto& fc : next) setColor(fc.first, fc.second);
+    }
+    std::vector<int> four(num_faces);
+    for (int64_t f = 0; f < num_faces; ++f) four[f] = (face_attr[f] & 0x1F) == 4 ? 4 : 0xFF;
+    std::vector<std::pair<int64_t, int>> next;
+    for (int64_t f = 0; f < num_faces; ++f) {
+        if (four[f] != 4) continue;
+        int c[4];
+        neighbours(f, 4, four, c);
+        for (int k = 0; k < 4; ++k)
+            if (c[0] != k && c[1] != k && c[2] != k && c[3] != k) {
+                next.push_back({f, k});
+                break;
+            }
+    }
+    for (auto& fc : next) setColor(fc.first, fc.second);
+}
+
+// quadrilateral_to_triangle, O/DualMarchingCubes.cu:51-60
+void mdmc_oracle_quads_to_triangles(const int32_t* quads, int64_t num_quads, int32_t* tris) {
+    for (int64_t q = 0; q < num_quads; ++q) {
+        const int32_t* v = quads + 4 * q;
+        int32_t* t = tris + 6 * q;
+        t[0] = v[0];
+        t[1] = v[1];
+        t[2] = v[3];
+        t[3] = v[3];
+        t[4] = v[2];
+        t[5] = v[0];
+    }
+}
+
+// QualityMeasure::mean_ratio and area, O/QualityMeasure.h:45-66
+void mdmc_oracle_mean_ratio(const float* pos, const int32_t* tris, int64_t num_triangles, float* q) {
+    for (int64_t t = 0; t < num_triangles; ++t) {
+        const float* p0 = pos + 3 * (int64_t)tris[3 * t];
+        const float* p1 = pos + 3 * (int64_t)tris[3 * t + 1];
+        const float* p2 = pos + 3 * (int64_t)tris[3 * t + 2];
+        const float l0 = (p1[0] - p0[0]) * (p1[0] - p0[0]) + (p1[1] - p0[1]) * (p1[1] - p0[1]) +
+                         (p1[2] - p0[2]) * (p1[2] - p0[2]);
+        const float l1 = (p2[0] - p1[0]) * (p2[0] - p1[0]) + (p2[1] - p1[1]) * (p2[1] - p1[1]) +
+                         (p2[2] - p1[2]) * (p2[2] - p1[2]);
+        const float l2 = (p0[0] - p2[0]) * (p0[0] - p2[0]) + (p0[1] - p2[1]) * (p0[1] - p2[1]) +
+                         (p0[2] - p2[2]) * (p0[2] - p2[2]);
+        const float l = l0 + l1 + l2;
+        const float x1 = p1[0] - p0[0], x2 = p2[0] - p0[0];
+        const float y1 = p1[1] - p0[1], y2 = p2[1] - p0[1];
+        const float z1 = p1[2] - p0[2], z2 = p2[2] - p0[2];
+        const float a1 = (y1 * z2 - z1 * y2) * (y1 * z2 - z1 * y2);
+        const float a2 = (x1 * z2 - z1 * x2) * (x1 * z2 - z1 * x2);
+        const float a3 = (x1 * y2 - y1 * x2) * (x1 * y2 - y1 * x2);
+        const float a = std::sqrt(a1 + a2 + a3);
+        q[t] = 2.0f * std::sqrt(3.0f) * a / l;
+    }
+}
+
 }  // extern "C"

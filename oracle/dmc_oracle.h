@@ -97,6 +97,15 @@ void* mdmc_oracle_standard_mc(const float* grid, const int dims[3], const float 
 void mdmc_oracle_get_standard_mc(const void* mesh, float* positions, float* normals, int* triangles);
 void mdmc_oracle_free_standard_mc(void* mesh);
 
+/* Face coloring 24 -> 5 colors in place (O/FaceColoring.cu:5-141);
+ * halfedges 4 ints each {origin, face, next, twin}. */
+void mdmc_oracle_color_faces(const int32_t* halfedges, int64_t num_halfedges, const int32_t* face_first,
+                             uint16_t* face_attr, int64_t num_faces);
+/* quadrilateral_to_triangle (O/DualMarchingCubes.cu:51-60) */
+void mdmc_oracle_quads_to_triangles(const int32_t* quads, int64_t num_quads, int32_t* tris);
+/* mean-ratio quality per triangle (O/QualityMeasure.h:45-66) */
+void mdmc_oracle_mean_ratio(const float* pos, const int32_t* tris, int64_t num_triangles, float* q);
+
 /* Differentiable path (no reference counterpart; surface iteration off).
  * Topology of a result: per DMC vertex its cell (x, y, z) and the 12-bit mask
  * of its contour's cell edges; per final vertex the DMC vertex it descends

@@ -68,6 +68,10 @@ def oracle():
             lib.mdmc_oracle_standard_mc.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_float, ctypes.c_void_p]
             lib.mdmc_oracle_get_standard_mc.argtypes = [ctypes.c_void_p] * 4
             lib.mdmc_oracle_free_standard_mc.argtypes = [ctypes.c_void_p]
+            lib.mdmc_oracle_color_faces.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                                    ctypes.c_int64]
+            lib.mdmc_oracle_quads_to_triangles.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+            lib.mdmc_oracle_mean_ratio.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
             lib.mdmc_oracle_positions_f64.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_double, ctypes.c_void_p]
             lib.mdmc_oracle_backward.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_double, ctypes.c_void_p,
                                                                          ctypes.c_void_p]
@@ -311,3 +315,27 @@ def oracle_standard_mc(grid, dims, origin, spacing, iso):
         return pos, nrm, tri
     finally:
         lib.mdmc_oracle_free_standard_mc(m)
+
+
+def oracle_color_faces(halfedges, face_first, face_attr):
+    """The oracle's 24 -> 5 face coloring; returns the new face attributes."""
+    he = np.ascontiguousarray(halfedges, np.int32).reshape(-1, 4)
+    ff = np.ascontiguousarray(face_first, np.int32)
+    attr = np.array(face_attr, np.uint16, copy=True)
+    oracle().mdmc_oracle_color_faces(_p(he), len(he), _p(ff), _p(attr), len(attr))
+    return attr
+
+
+def oracle_quads_to_triangles(quads):
+    q = np.ascontiguousarray(quads, np.int32).reshape(-1, 4)
+    t = np.zeros((2 * len(q), 3), np.int32)
+    oracle().mdmc_oracle_quads_to_triangles(_p(q), len(q), _p(t))
+    return t
+
+
+def oracle_mean_ratio(positions, triangles):
+    pos = np.ascontiguousarray(positions, np.float32).reshape(-1, 3)
+    tri = np.ascontiguousarray(triangles, np.int32).reshape(-1, 3)
+    q = np.zeros(len(tri), np.float32)
+    oracle().mdmc_oracle_mean_ratio(_p(pos), _p(tri), len(tri), _p(q))
+    return q
