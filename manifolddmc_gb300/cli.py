@@ -3,6 +3,9 @@
   python -m manifolddmc_gb300.cli run volume.bin --iso 900 [--refine R] [--pad]
         [--no-split] [--no-detect] [--no-surface-iteration] [--simplify3x3y]
         [--simplify3x3y-old] [--simplify3333] --obj out.obj [--stats Statistics.json]
+        [--color-faces] [--quality qualityDMC.bin]
+  python -m manifolddmc_gb300.cli mc volume.bin --iso 900 [--refine R] [--pad] [--obj out.obj]
+        [--quality qualityMC.bin]
   python -m manifolddmc_gb300.cli generate sphere --dims 64 64 64 --bin out.bin [--scale 1000]
   python -m manifolddmc_gb300.cli check mesh.obj
   python -m manifolddmc_gb300.cli canonical in.obj out.obj
@@ -30,6 +33,15 @@ def main(argv=None):
     r.add_argument("--simplify3333", action="store_true")
     r.add_argument("--obj")
     r.add_argument("--stats")
+    r.add_argument("--color-faces", action="store_true", help="reduce the face colors to 5 (FaceColoring.cu)")
+    r.add_argument("--quality", help="mean-ratio quality of the quads' triangles, int32 count + float32 each")
+    m = sub.add_parser("mc")
+    m.add_argument("volume")
+    m.add_argument("--iso", type=float, required=True)
+    m.add_argument("--refine", type=int, default=0)
+    m.add_argument("--pad", action="store_true")
+    m.add_argument("--obj")
+    m.add_argument("--quality")
     g = sub.add_parser("generate")
     g.add_argument("surface")
     g.add_argument("--dims", type=int, nargs=3, default=[64, 64, 64])
@@ -57,14 +69,34 @@ def main(argv=None):
         vol, origin, spacing = mdmc.generate_volume(a.surface, a.dims)
         mdmc.write_bin(a.bin, vol.cpu().numpy() * np.float32(a.scale) + np.float32(a.offset), spacing)
         return 0
+    if a.cmd == "mc":
+        import torch
+        dmc = mdmc.DualMarchingCubes()
+        grid = mdmc.UniformGrid.read_from_file(a.volume, a.refine, a.pad)
+        pos, nrm, tri = dmc.run_standard_mc(a.iso, grid)
+        if a.obj:
+            # the older CLI's mesh copy negates the gradient normals
+            # (OriginalDMC/src/DualMarchingCubes.cu:1034)
+            meshtools.write_triangle_obj(a.obj, pos, -nrm, tri)
+        if a.quality:
+            q = mdmc.mean_ratio(torch.from_numpy(pos).cuda(), torch.from_numpy(tri).cuda())
+            meshtools.write_quality_bin(a.quality, q.cpu().numpy())
+        print(json.dumps({"vertices": len(pos), "triangles": len(tri)}))
+        return 0
     dmc = mdmc.DualMarchingCubes(
         split_non_manifold_halfedges=int(not a.no_split), detect_non_manifold_vertices=int(not a.no_detect),
         enable_surface_to_vertex_iteration=int(not a.no_surface_iteration), simplify_p3x3y_color=int(a.simplify3x3y),
         simplify_p3x3y_old=int(a.simplify3x3y_old), simplify_p3333=int(a.simplify3333))
     grid = mdmc.UniformGrid.read_from_file(a.volume, a.refine, a.pad)
     times = dmc.run(a.iso, grid)
+    if a.color_faces:
+        dmc.color_faces()
     if a.obj:
         dmc.write_obj(a.obj)
+    if a.quality:
+        dev = dmc.device_arrays()
+        q = mdmc.mean_ratio(dev["positions"], mdmc.quads_to_triangles(dev["quads"]))
+        meshtools.write_quality_bin(a.quality, q.cpu().numpy())
     if a.stats:
         meshtools.append_statistics(a.stats, meshtools.statistics_record(
             a.volume, grid.dimensions, a.iso, dmc.stats, int(dmc.mesh.num_vertices)))

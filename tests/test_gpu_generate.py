@@ -105,3 +105,23 @@ def test_cli_generated_sphere_is_manifold(tmp_path, capsys):
     assert rep["manifold"] and rep["edges_by_faces"] == {2: rep["edges"]}
     rec = json.loads("[" + st.read_text().rstrip().rstrip(",") + "]")[0]
     assert rec["quads"]["numQuads"] == len(quads) and rec["edges"]["4-Edges"] == 0
+
+
+def test_cli_standard_mc_and_quality_of_a_generated_torus(tmp_path, capsys):
+    b, obj, qb = tmp_path / "t.bin", tmp_path / "t.obj", tmp_path / "qualityMC.bin"
+    assert cli.main(["generate", "torus", "--dims", "48", "48", "48", "--bin", str(b)]) == 0
+    assert cli.main(["mc", str(b), "--iso", "1000", "--obj", str(obj), "--quality", str(qb)]) == 0
+    out = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    pos, tris = meshtools.read_obj(obj)
+    assert tris.shape[1] == 3 and len(tris) == out["triangles"] > 100
+    rep = meshtools.manifold_report(tris, len(pos))
+    assert rep["manifold"] and rep["edges_by_faces"] == {2: rep["edges"]}
+    # genus 1: V - E + F = 0
+    assert len(pos) - rep["edges"] + len(tris) == 0
+    q = meshtools.read_quality_bin(qb)
+    assert len(q) == len(tris) and np.all((q >= 0) & (q <= 1.0 + 1e-6))
+    # DMC run with the 5-coloring and the quality of its quads' triangles
+    qd, o2 = tmp_path / "qualityDMC.bin", tmp_path / "d.obj"
+    assert cli.main(["run", str(b), "--iso", "1000", "--color-faces", "--quality", str(qd), "--obj", str(o2)]) == 0
+    out = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert len(meshtools.read_quality_bin(qd)) == 2 * out["faces"]

@@ -71,3 +71,21 @@ def test_statistics_record_layout():
     assert r["numCells"] == 2 * 3 * 4
     assert list(r) == ["fileName", "dimensions", "numCells", "isoValue", "edges", "vertices", "quads"]
     assert r["quads"] == {"numQuads": 4, "1-Quads": 5, "2-Quads": 6, "3-Quads": 7, "4-Quads": 8}
+
+
+def test_triangle_obj_and_quality_bin(tmp_path):
+    pos = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32)
+    nrm = np.eye(4, 3, dtype=np.float32)
+    tri = np.array([[0, 1, 2], [0, 1, 3], [0, 2, 3], [1, 2, 3]], np.int32)
+    meshtools.write_triangle_obj(tmp_path / "t.obj", pos, nrm, tri)
+    p2, f2 = meshtools.read_obj(tmp_path / "t.obj")
+    assert np.array_equal(p2, pos) and np.array_equal(f2, tri)
+    rep = meshtools.manifold_report(f2, len(p2))
+    assert rep["manifold"] and rep["edges"] == 6 and rep["edges_by_faces"] == {2: 6}
+    cp, cf = meshtools.canonicalize(p2, f2[::-1])
+    assert cf.shape == (4, 3) and np.all(cf[:, 0] == cf.min(axis=1))
+    q = np.array([0.5, 1.0, 0.25], np.float32)
+    meshtools.write_quality_bin(tmp_path / "q.bin", q)
+    raw = (tmp_path / "q.bin").read_bytes()
+    assert len(raw) == 4 + 12 and np.frombuffer(raw[:4], np.int32)[0] == 3
+    assert np.array_equal(meshtools.read_quality_bin(tmp_path / "q.bin"), q)
