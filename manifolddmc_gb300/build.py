@@ -6,6 +6,7 @@ float operation separately rounded (the reference's expression order is kept
 in the source), which the bit-exact parity with the CPU oracle relies on.
 """
 import os
+import shlex
 import subprocess
 import sys
 from concurrent.futures import ThreadPoolExecutor
@@ -45,7 +46,7 @@ def build(force=False, verbose=False):
 
     def compile_one(src):
         obj = OUT_DIR / (Path(src).stem + ".o")
-        cmd = [cc] + ARCH + FLAGS + ["-c", str(CSRC / src), "-o", str(obj)]
+        cmd = [cc] + ARCH + FLAGS + shlex.split(os.environ.get("MDMC_NVCC_FLAGS", "")) + ["-c", str(CSRC / src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

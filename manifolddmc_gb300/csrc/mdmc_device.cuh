@@ -362,6 +362,91 @@ __device__ inline void cornerGradients(const View& g, int x, int y, int z, const
     for (int i = 0; i < 8; ++i) out[i] = (0.5f * gr[i]) / dl;
 }
 
+// The samples a cell's corners and corner gradients read: stencil sample
+// (i, j, k), i, j, k in 0..3, is View::at(clamp(x - 1 + i), clamp(y - 1 + j),
+// clamp(z - 1 + k)) with the same float operations.  The per-axis part of
+// each coordinate (clamped sample offset; for refined grids the coarse index
+// pair and fraction) is computed once per cell instead of once per sample.
+template <class View>
+struct CellStencil;
+
+template <>
+struct CellStencil<PlainView> {
+    const float* v;
+    int xo[4];
+    int64_t yo[4], zo[4];
+    __device__ __forceinline__ CellStencil(const PlainView& g, int x, int y, int z) : v(g.v) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            xo[k] = min(max(x - 1 + k, 0), g.X - 1);
+            yo[k] = (int64_t)min(max(y - 1 + k, 0), g.Y - 1) * g.X;
+            zo[k] = (int64_t)min(max(z - 1 + k, 0), g.Z - 1) * g.Y * g.X;
+        }
+    }
+    __device__ __forceinline__ float at(int i, int j, int k) const { return __ldg(v + zo[k] + yo[j] + xo[i]); }
+};
+
+// (refined grids have fewer than 2^32 samples, so their coarse grids too:
+// 32-bit element offsets suffice)
+template <>
+struct CellStencil<RefinedView> {
+    const float* c;
+    uint32_t x0[4], x1[4], y0[4], y1[4], z0[4], z1[4];
+    float dx[4], dy[4], dz[4];
+    __device__ __forceinline__ static void axis(const RefinedView& g, int p, int n, int cn, uint32_t stride, uint32_t& o0,
+                                                uint32_t& o1, float& d) {
+        const int u = g.unpad(min(max(p, 0), n - 1), n);
+        const float q = g.divf(u);
+        const int m = (int)floorf(q);
+        d = q - (float)m;
+        o0 = (uint32_t)min(max(m, 0), cn - 1) * stride;
+        o1 = (uint32_t)min(max(m + 1, 0), cn - 1) * stride;
+    }
+    __device__ __forceinline__ CellStencil(const RefinedView& g, int x, int y, int z) : c(g.c) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            axis(g, x - 1 + k, g.X, g.cX, 1u, x0[k], x1[k], dx[k]);
+            axis(g, y - 1 + k, g.Y, g.cY, (uint32_t)g.cX, y0[k], y1[k], dy[k]);
+            axis(g, z - 1 + k, g.Z, g.cZ, (uint32_t)g.cX * (uint32_t)g.cY, z0[k], z1[k], dz[k]);
+        }
+    }
+    __device__ __forceinline__ float at(int i, int j, int k) const {
+        float s[8];
+        s[0] = __ldg(c + (z0[k] + y0[j] + x0[i]));
+        s[1] = __ldg(c + (z0[k] + y0[j] + x1[i]));
+        s[2] = __ldg(c + (z0[k] + y1[j] + x0[i]));
+        s[3] = __ldg(c + (z0[k] + y1[j] + x1[i]));
+        s[4] = __ldg(c + (z1[k] + y0[j] + x0[i]));
+        s[5] = __ldg(c + (z1[k] + y0[j] + x1[i]));
+        s[6] = __ldg(c + (z1[k] + y1[j] + x0[i]));
+        s[7] = __ldg(c + (z1[k] + y1[j] + x1[i]));
+        return trilinear(s, f3(dx[i], dy[j], dz[k]));
+    }
+};
+
+// the cell's corner values (corner i at stencil (1 + bit0, 1 + bit1, 1 + bit2))
+template <class St>
+__device__ __forceinline__ void stencilCorners(const St& st, float s[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s[i] = st.at(1 + (i & 1), 1 + ((i >> 1) & 1), 1 + ((i >> 2) & 1));
+}
+
+// cornerGradients from the stencil: along axis a, corner i's neighbour is
+// the stencil sample one step outside the cell (index 0 below, 3 above)
+template <class St>
+__device__ __forceinline__ void stencilGradients(const St& st, const float s[8], F3 dl, F3 out[8]) {
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int bx = i & 1, by = (i >> 1) & 1, bz = (i >> 2) & 1;
+        const float nx = st.at(bx ? 3 : 0, 1 + by, 1 + bz);
+        const float ny = st.at(1 + bx, by ? 3 : 0, 1 + bz);
+        const float nz = st.at(1 + bx, 1 + by, bz ? 3 : 0);
+        const F3 gr = f3(bx ? nx - s[i ^ 1] : s[i ^ 1] - nx, by ? ny - s[i ^ 2] : s[i ^ 2] - ny,
+                         bz ? nz - s[i ^ 4] : s[i ^ 4] - nz);
+        out[i] = (0.5f * gr) / dl;
+    }
+}
+
 // Interpolation<glm::vec3>::interpolateTrilinearly of the corner gradients
 __device__ __forceinline__ F3 trilinear3(const F3 n[8], F3 p) {
     float xs[8], ys[8], zs[8];
