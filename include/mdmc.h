@@ -200,6 +200,38 @@ MDMC_API mdmc_status mdmc_download_mesh(mdmc_context* context, float* positions,
                                uint16_t* face_attributes, int32_t* vertex_halfedge,
                                uint8_t* vertex_flags, void* stream);
 
+/* Caller-owned host arrays for mdmc_run_to_host, laid out like mdmc_mesh
+ * (halfedges: 4 ints per halfedge, 4 halfedges per face), sized for up to
+ * capacity_vertices vertices and capacity_faces faces.  Any pointer may be
+ * NULL (that array is not copied).  Page-locked memory (cudaMallocHost or
+ * cudaHostRegister) lets the copies overlap the run; pageable memory works
+ * but copies without overlap. */
+typedef struct mdmc_host_mesh {
+    int64_t capacity_vertices;
+    int64_t capacity_faces;
+    float* positions;
+    float* normals;
+    int32_t* quads;
+    int32_t* halfedges;
+    int32_t* face_first_halfedge;
+    uint16_t* face_attributes;
+    int32_t* vertex_halfedge;
+    uint8_t* vertex_flags;
+} mdmc_host_mesh;
+
+/* DualMarchingCubes::run with the mesh delivered into caller-owned host
+ * arrays, the way the reference delivers it into caller-owned buffers
+ * (DualMarchingCubes.cu:382-406, there GL buffers): mdmc_run, plus the copies
+ * of mdmc_download_mesh, started as soon as each array is final so that they
+ * overlap the later stages (halfedges and faces after the quad pass,
+ * positions and normals after the vertex pass; arrays a repair stage rewrites
+ * are copied again at the end).  The device mesh, mesh and stats are those
+ * of mdmc_run.  A mesh larger than the capacities is left on the device and
+ * the call returns MDMC_ERROR_LIMIT naming its size.  Synchronous: the host
+ * arrays are complete when the call returns. */
+MDMC_API mdmc_status mdmc_run_to_host(mdmc_context* context, const mdmc_grid* grid, float iso_value,
+                                      const mdmc_host_mesh* out, mdmc_mesh* mesh, mdmc_stats* stats, void* stream);
+
 /* HalfedgeMesh::toVertexAndIndexBuffer (Halfedges/HalfedgeMesh.cu:1102-1146)
  * into device arrays instead of GL buffers (either may be NULL): vertices gets
  * 10 floats per vertex {position[3], normal[3], rgba[4]} with the reference's

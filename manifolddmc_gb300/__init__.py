@@ -64,6 +64,41 @@ class Mesh(ctypes.Structure):
                 ("vertex_flags", ctypes.c_void_p)]
 
 
+class HostMeshArrays(ctypes.Structure):
+    _fields_ = [("capacity_vertices", ctypes.c_int64), ("capacity_faces", ctypes.c_int64),
+                ("positions", ctypes.c_void_p), ("normals", ctypes.c_void_p), ("quads", ctypes.c_void_p),
+                ("halfedges", ctypes.c_void_p), ("face_first_halfedge", ctypes.c_void_p),
+                ("face_attributes", ctypes.c_void_p), ("vertex_halfedge", ctypes.c_void_p),
+                ("vertex_flags", ctypes.c_void_p)]
+
+
+class HostMesh:
+    """Page-locked host arrays for DualMarchingCubes.run_to_host, for meshes
+    of up to max_vertices vertices and max_faces faces."""
+
+    def __init__(self, max_vertices, max_faces):
+        import torch
+        V, F = int(max_vertices), int(max_faces)
+
+        def pinned(shape, dtype):
+            return torch.empty(shape, dtype=dtype).pin_memory()
+
+        self.tensors = {"positions": pinned((V, 3), torch.float32), "normals": pinned((V, 3), torch.float32),
+                        "quads": pinned((F, 4), torch.int32), "halfedges": pinned((4 * F, 4), torch.int32),
+                        "face_first_halfedge": pinned((F,), torch.int32),
+                        "face_attributes": pinned((F,), torch.int16),
+                        "vertex_halfedge": pinned((V,), torch.int32), "vertex_flags": pinned((V,), torch.uint8)}
+        self.arrays = HostMeshArrays(V, F, *[t.data_ptr() for t in self.tensors.values()])
+
+    def mesh(self, V, F):
+        """numpy views of the first V vertices and F faces"""
+        t = self.tensors
+        return HalfedgeMesh(t["positions"][:V].numpy(), t["normals"][:V].numpy(), t["quads"][:F].numpy(),
+                            t["halfedges"][:4 * F].numpy(), t["face_first_halfedge"][:F].numpy(),
+                            t["face_attributes"][:F].numpy().view(np.uint16), t["vertex_halfedge"][:V].numpy(),
+                            t["vertex_flags"][:V].numpy())
+
+
 class TriangleMesh(ctypes.Structure):
     _fields_ = [("num_vertices", ctypes.c_int64), ("num_triangles", ctypes.c_int64),
                 ("positions", ctypes.c_void_p), ("normals", ctypes.c_void_p), ("triangles", ctypes.c_void_p)]
@@ -133,6 +168,7 @@ def library():
             "mdmc_backward": (ctypes.c_int, [P, P, P, ctypes.c_int, P]),
             "mdmc_render_buffers": (ctypes.c_int, [P, P, P, P]),
             "mdmc_run_standard_mc": (ctypes.c_int, [P, P, ctypes.c_float, P, P]),
+            "mdmc_run_to_host": (ctypes.c_int, [P, P, ctypes.c_float, P, P, P, P]),
             "mdmc_download_triangle_mesh": (ctypes.c_int, [P] * 5),
             "mdmc_color_faces": (ctypes.c_int, [P, P]),
             "mdmc_quads_to_triangles": (ctypes.c_int, [P, ctypes.c_int64, P, P]),
@@ -330,6 +366,17 @@ class DualMarchingCubes:
         s = self.stats
         return {"DMC": s.ms_dmc, "HalfedgeMesh": s.ms_halfedge, "Repair": s.ms_repair,
                 "DetectNonManifoldVertices": s.ms_detect, "Total": s.ms_total}
+
+    def run_to_host(self, iso_value, grid, host, stream=None):
+        """run() with the mesh copied into the HostMesh `host` while the run
+        goes on (mdmc_run_to_host); returns numpy views of host's arrays
+        holding the mesh."""
+        g = grid.grid if isinstance(grid, UniformGrid) else grid
+        self._run_id += 1
+        self._ctx.check(self._ctx.lib.mdmc_run_to_host(self._ctx.handle, ctypes.byref(g), ctypes.c_float(iso_value),
+                                                       ctypes.byref(host.arrays), ctypes.byref(self.mesh),
+                                                       ctypes.byref(self.stats), _stream_handle(stream)))
+        return host.mesh(int(self.mesh.num_vertices), int(self.mesh.num_faces))
 
     # statistics getters (DualMarchingCubes.h:87-118)
     def get_num_vertices(self):

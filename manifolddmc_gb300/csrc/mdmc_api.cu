@@ -116,6 +116,13 @@ struct mdmc_context {
     DevBuf mcEdgeMask, mcEdgeFirst, mcCases, mcTriOffset, mcEdgeIds, mcPos, mcNrm, mcTris;
     // face coloring scratch
     DevBuf colorOrig;
+    // mdmc_run_to_host: the caller's host arrays during the call, a copy
+    // stream whose copies overlap the later stages, and which arrays went
+    // out early; lateChange = a stage after the quad pass rewrote the mesh
+    const mdmc_host_mesh* hostOut = nullptr;
+    cudaStream_t copyStream = nullptr;
+    cudaEvent_t copyEv[2] = {};
+    bool earlyFaces = false, earlyVertices = false, lateChange = false;
     int64_t mcV = 0, mcT = 0;
     // events: start, dmc, halfedge, repair, detect, end
     cudaEvent_t ev[6] = {};
@@ -559,6 +566,34 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
     return MDMC_OK;
 }
 
+// mdmc_run_to_host: once the quad pass (stage 0: halfedges, quads, face
+// arrays) or the vertex pass (stage 1: positions, normals) has written its
+// arrays, copy them to the caller's host arrays on the copy stream while the
+// run goes on.  Copies only what fits the host arrays; the end of the call
+// copies again whatever a later stage rewrote.
+mdmc_status earlyCopy(mdmc_context* c, int stage, cudaStream_t s) {
+    const mdmc_host_mesh* h = c->hostOut;
+    if (!h || c->V > h->capacity_vertices || c->F > h->capacity_faces) return MDMC_OK;
+    MDMC_CHECK(c, cudaEventRecord(c->copyEv[stage], s));
+    MDMC_CHECK(c, cudaStreamWaitEvent(c->copyStream, c->copyEv[stage], 0));
+    auto cp = [&](void* dst, const DevBuf& b, size_t bytes) -> cudaError_t {
+        if (!dst || bytes == 0) return cudaSuccess;
+        return cudaMemcpyAsync(dst, b.p, bytes, cudaMemcpyDeviceToHost, c->copyStream);
+    };
+    if (stage == 0) {
+        MDMC_CHECK(c, cp(h->halfedges, c->he, sizeof(int4) * (size_t)c->H));
+        MDMC_CHECK(c, cp(h->quads, c->quads, sizeof(int4) * (size_t)c->F));
+        MDMC_CHECK(c, cp(h->face_first_halfedge, c->faceFirst, sizeof(int) * (size_t)c->F));
+        MDMC_CHECK(c, cp(h->face_attributes, c->faceAttr, sizeof(uint16_t) * (size_t)c->F));
+        c->earlyFaces = true;
+    } else {
+        MDMC_CHECK(c, cp(h->positions, c->pos, sizeof(float) * 3 * (size_t)c->V));
+        MDMC_CHECK(c, cp(h->normals, c->nrm, sizeof(float) * 3 * (size_t)c->V));
+        c->earlyVertices = true;
+    }
+    return MDMC_OK;
+}
+
 // The DMC front end: the active-cell mask per x-row of cells (W words per
 // row, numWords in all) and the index of every word's first active cell
 // (cellFirst, the cell index the quad pass reads too); A = active cells.
@@ -616,6 +651,11 @@ mdmc_status mdmc_create(mdmc_context** context, const mdmc_options* options) {
     }
     for (auto& e : c->ev) cudaEventCreate(&e);
     for (auto& e : c->kev) cudaEventCreate(&e);
+    for (auto& e : c->copyEv) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+    if (cudaStreamCreateWithFlags(&c->copyStream, cudaStreamNonBlocking) != cudaSuccess) {
+        mdmc_destroy(c);
+        return MDMC_ERROR_CUDA;
+    }
     // record every event once so that elapsed-time queries of stages a run
     // skips (e.g. no refinement on this context) return 0 instead of failing
     for (auto& e : c->ev) cudaEventRecord(e, 0);
@@ -634,6 +674,9 @@ void mdmc_destroy(mdmc_context* c) {
         if (e) cudaEventDestroy(e);
     for (auto& e : c->kev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : c->copyEv)
+        if (e) cudaEventDestroy(e);
+    if (c->copyStream) cudaStreamDestroy(c->copyStream);
     if (c->hostCounters) cudaFreeHost(c->hostCounters);
     if (c->hostInts) cudaFreeHost(c->hostInts);
     delete c;
@@ -761,6 +804,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->lastSurfaceIteration = c->opt.enable_surface_to_vertex_iteration;
     c->dmcV = c->activeCells = 0;
     c->simplified = false;
+    c->earlyFaces = c->earlyVertices = c->lateChange = false;
     std::memset(&c->stats, 0, sizeof c->stats);
     DevCounters* ctr = c->counters.as<DevCounters>();
     uint32_t* status = &ctr->status;
@@ -841,11 +885,13 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
                 c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(), c->nmList.as<int4>(), (int)(Q + 1), (int)Q,
                 (int)Vd, c->quads.as<int4>(), c->vertexHE.as<int>(), c->degree.as<int>(), ctr, s);
     cudaEventRecord(c->kev[7], s);
+    if (c->hostOut && (st = earlyCopy(c, 0, s)) != MDMC_OK) return st;
     // vertex positions and normals (sliceP's vertex part)
     cudaEventRecord(c->kev[10], s);
     launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), (int)A, (int)Vd,
                    c->pos.as<float>(), c->nrm.as<float>(), status, s);
     cudaEventRecord(c->kev[11], s);
+    if (c->hostOut && (st = earlyCopy(c, 1, s)) != MDMC_OK) return st;
     MDMC_CHECK(c, cudaGetLastError());
     cudaEventRecord(c->ev[1], s);
     cudaEventRecord(c->kev[8], s);
@@ -874,9 +920,11 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
         MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
         MDMC_CHECK(c, cudaStreamSynchronize(s));
         finished = !(c->opt.split_non_manifold_halfedges && c->hostCounters->nmBuckets > 0);
+        c->lateChange = c->hostCounters->nmBuckets > 0;  // fixManifoldTwins rewrote twins
         if (finished) c->hostCounters->status |= c->hostCounters->specStatus;
     }
     if (!finished) {
+        c->lateChange = true;
         if (c->opt.split_non_manifold_halfedges) {
             if ((st = runSplitter(c, g, iso, iterations, s)) != MDMC_OK) return st;
         }
@@ -1061,6 +1109,48 @@ mdmc_status mdmc_download_mesh(mdmc_context* c, float* positions, float* normals
     MDMC_CHECK(c, cp(vertex_flags, c->vflags, (size_t)c->V));
     MDMC_CHECK(c, cudaStreamSynchronize(s));
     return MDMC_OK;
+}
+
+mdmc_status mdmc_run_to_host(mdmc_context* c, const mdmc_grid* grid, float iso, const mdmc_host_mesh* out,
+                             mdmc_mesh* mesh, mdmc_stats* stats, void* stream) {
+    if (!c || !grid || !out || out->capacity_vertices < 0 || out->capacity_faces < 0)
+        return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "null argument or negative capacity");
+    cudaStream_t s = (cudaStream_t)stream;
+    c->hostOut = out;
+    const mdmc_status st = mdmc_run(c, grid, iso, mesh, stats, stream);
+    c->hostOut = nullptr;
+    // the early copies write the caller's arrays: they end before this call does
+    const cudaError_t ce = cudaStreamSynchronize(c->copyStream);
+    if (st != MDMC_OK && st != MDMC_ERROR_LIMIT) return st;
+    if (ce != cudaSuccess) return cudaFail(c, ce, "early copies");
+    const std::string runMessage = c->err;
+    if (c->V > out->capacity_vertices || c->F > out->capacity_faces) {
+        char text[200];
+        std::snprintf(text, sizeof text, "the mesh has %lld vertices and %lld faces; the host arrays hold %lld and %lld",
+                      (long long)c->V, (long long)c->F, (long long)out->capacity_vertices,
+                      (long long)out->capacity_faces);
+        return fail(c, MDMC_ERROR_LIMIT, text);
+    }
+    auto cp = [&](void* dst, const DevBuf& b, size_t bytes) -> cudaError_t {
+        if (!dst || bytes == 0) return cudaSuccess;
+        return cudaMemcpyAsync(dst, b.p, bytes, cudaMemcpyDeviceToHost, s);
+    };
+    if (!c->earlyFaces || c->lateChange || c->simplified) {
+        MDMC_CHECK(c, cp(out->halfedges, c->he, sizeof(int4) * (size_t)c->H));
+        MDMC_CHECK(c, cp(out->quads, c->quads, sizeof(int4) * (size_t)c->F));
+        MDMC_CHECK(c, cp(out->face_first_halfedge, c->faceFirst, sizeof(int) * (size_t)c->F));
+        MDMC_CHECK(c, cp(out->face_attributes, c->faceAttr, sizeof(uint16_t) * (size_t)c->F));
+    }
+    if (!c->earlyVertices || c->lateChange || c->simplified) {
+        MDMC_CHECK(c, cp(out->positions, c->pos, sizeof(float) * 3 * (size_t)c->V));
+        MDMC_CHECK(c, cp(out->normals, c->nrm, sizeof(float) * 3 * (size_t)c->V));
+    }
+    // written by the fan detection at the end in every case
+    MDMC_CHECK(c, cp(out->vertex_halfedge, c->vertexHE, sizeof(int) * (size_t)c->V));
+    MDMC_CHECK(c, cp(out->vertex_flags, c->vflags, (size_t)c->V));
+    MDMC_CHECK(c, cudaStreamSynchronize(s));
+    c->err = runMessage;
+    return st;
 }
 
 mdmc_status mdmc_backward(mdmc_context* c, const float* dl_dpositions, float* dl_dsamples, int accumulate,
