@@ -882,7 +882,10 @@ struct AroundCell {
 // face, and each of them does exactly when its edge lies in the same contours
 // of A and of B.  That set is the reference's edge-table bucket; sorted, it
 // gives the twins by the reference's rules.
-__global__ void __launch_bounds__(256) kQuads(const ActiveCell* __restrict__ act, const int* __restrict__ quadOwner,
+#ifndef MDMC_QUADS_MIN_BLOCKS
+#define MDMC_QUADS_MIN_BLOCKS 3
+#endif
+__global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const ActiveCell* __restrict__ act, const int* __restrict__ quadOwner,
                                               int numActive, CellIndex ix, int4* __restrict__ he,
                                               int* __restrict__ faceFirst, uint16_t* __restrict__ faceAttr,
                                               uint8_t* vflags, uint32_t* __restrict__ heValence4,
@@ -921,13 +924,26 @@ __global__ void __launch_bounds__(256) kQuads(const ActiveCell* __restrict__ act
             cell[0].info = rec.info;
             cell[0].vbase = rec.pad;
             cell[0].qbase = rec.qbase;
-            int jk[4];
+            // the cells around the quad's edge (k = 1..3), and the five other
+            // cells that can own a quad of one of the face buckets:
+            // p + e_b, p + e_c, p + e_a, p - e_b + e_a, p - e_c + e_a.  All
+            // eight lookups are issued before any record is used.
+            int jk[4], jx[5];
             jk[0] = j;
 #pragma unroll
             for (int k = 1; k < 4; ++k) {
                 const int db = k & 1, dc = k >> 1;
                 jk[k] = ix.find(px - (b == 0 ? db : 0) - (c == 0 ? dc : 0), py - (b == 1 ? db : 0) - (c == 1 ? dc : 0),
                                 pz - (c == 2 ? dc : 0));
+            }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                const int dA = k >= 2 ? 1 : 0;
+                const int dB = k == 0 ? 1 : (k == 3 ? -1 : 0);
+                const int dC = k == 1 ? 1 : (k == 4 ? -1 : 0);
+                jx[k] = ix.find(px + (axis == 0 ? dA : 0) + (b == 0 ? dB : 0),
+                                py + (axis == 1 ? dA : 0) + (b == 1 ? dB : 0) + (c == 1 ? dC : 0),
+                                pz + (axis == 2 ? dA : 0) + (c == 2 ? dC : 0));
             }
 #pragma unroll
             for (int k = 1; k < 4; ++k) {
@@ -941,6 +957,18 @@ __global__ void __launch_bounds__(256) kQuads(const ActiveCell* __restrict__ act
                     cell[k].info = r2.info;
                     cell[k].vbase = r2.pad;
                     cell[k].qbase = r2.qbase;
+                }
+            }
+            uint32_t xinfo[5];
+            int xqbase[5];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) {
+                xinfo[k] = 0;
+                xqbase[k] = -1;  // no such active cell
+                if (inb(jx[k], numActive)) {
+                    const ActiveCell r2 = act[jx[k]];
+                    xinfo[k] = r2.info;
+                    xqbase[k] = r2.qbase;
                 }
             }
 #pragma unroll
@@ -1041,11 +1069,17 @@ __global__ void __launch_bounds__(256) kQuads(const ActiveCell* __restrict__ act
                             oinfo = ko == 0 ? cell[0].info : (ko == 1 ? cell[1].info : cell[2].info);
                             oqbase = ko == 0 ? cell[0].qbase : (ko == 1 ? cell[1].qbase : cell[2].qbase);
                         } else {
-                            const int jo = ix.find(ox, oy, oz);
-                            if (jo < 0 || jo >= numActive) continue;
-                            const ActiveCell ro = act[jo];
-                            oinfo = ro.info;
-                            oqbase = ro.qbase;
+                            // p + e_u (du = 1), p + e_a (du = 0) or p - e_u + e_a (du = -1)
+                            const int kx = offA == 0 ? (u == b ? 0 : 1) : (du == 0 ? 2 : (u == b ? 3 : 4));
+                            oinfo = 0;
+                            oqbase = -1;
+#pragma unroll
+                            for (int k = 0; k < 5; ++k)
+                                if (kx == k) {
+                                    oinfo = xinfo[k];
+                                    oqbase = xqbase[k];
+                                }
+                            if (oqbase < 0) continue;
                         }
                         const int cso = (int)(oinfo & 255u);
                         if (!ownsAxis(cso, al, ox, oy, oz)) continue;
