@@ -67,6 +67,10 @@ struct DevBuf {
 
 static inline size_t roundUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// quad ranges of mdmc_run_to_host (each range's arrays are copied out as soon
+// as the quad pass has written them)
+constexpr int kCopyRanges = 8;
+
 }  // namespace mdmc
 
 using namespace mdmc;
@@ -122,7 +126,7 @@ struct mdmc_context {
     const mdmc_host_mesh* hostOut = nullptr;
     cudaStream_t copyStream = nullptr;
     cudaEvent_t copyEv[2] = {};
-    bool earlyFaces = false, earlyVertices = false, lateChange = false;
+    bool earlyFaces = false, earlyVertices = false, earlyVertexMaps = false, lateChange = false;
     int64_t mcV = 0, mcT = 0;
     // events: start, dmc, halfedge, repair, detect, end
     cudaEvent_t ev[6] = {};
@@ -566,31 +570,59 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
     return MDMC_OK;
 }
 
-// mdmc_run_to_host: once the quad pass (stage 0: halfedges, quads, face
-// arrays) or the vertex pass (stage 1: positions, normals) has written its
-// arrays, copy them to the caller's host arrays on the copy stream while the
-// run goes on.  Copies only what fits the host arrays; the end of the call
-// copies again whatever a later stage rewrote.
-mdmc_status earlyCopy(mdmc_context* c, int stage, cudaStream_t s) {
+// mdmc_run_to_host: as soon as the quad pass has written a range of quads
+// (their halfedges, quads and face arrays) or the vertex pass the positions
+// and normals, copy them to the caller's host arrays on the copy stream while
+// the run goes on.  Only when the whole mesh fits the host arrays; the end of
+// the call copies again whatever a later stage rewrote.
+bool earlyFits(const mdmc_context* c) {
     const mdmc_host_mesh* h = c->hostOut;
-    if (!h || c->V > h->capacity_vertices || c->F > h->capacity_faces) return MDMC_OK;
-    MDMC_CHECK(c, cudaEventRecord(c->copyEv[stage], s));
-    MDMC_CHECK(c, cudaStreamWaitEvent(c->copyStream, c->copyEv[stage], 0));
-    auto cp = [&](void* dst, const DevBuf& b, size_t bytes) -> cudaError_t {
-        if (!dst || bytes == 0) return cudaSuccess;
-        return cudaMemcpyAsync(dst, b.p, bytes, cudaMemcpyDeviceToHost, c->copyStream);
-    };
-    if (stage == 0) {
-        MDMC_CHECK(c, cp(h->halfedges, c->he, sizeof(int4) * (size_t)c->H));
-        MDMC_CHECK(c, cp(h->quads, c->quads, sizeof(int4) * (size_t)c->F));
-        MDMC_CHECK(c, cp(h->face_first_halfedge, c->faceFirst, sizeof(int) * (size_t)c->F));
-        MDMC_CHECK(c, cp(h->face_attributes, c->faceAttr, sizeof(uint16_t) * (size_t)c->F));
-        c->earlyFaces = true;
-    } else {
-        MDMC_CHECK(c, cp(h->positions, c->pos, sizeof(float) * 3 * (size_t)c->V));
-        MDMC_CHECK(c, cp(h->normals, c->nrm, sizeof(float) * 3 * (size_t)c->V));
-        c->earlyVertices = true;
-    }
+    return h && c->V <= h->capacity_vertices && c->F <= h->capacity_faces;
+}
+
+mdmc_status copyAfter(mdmc_context* c, int k, cudaStream_t s) {
+    MDMC_CHECK(c, cudaEventRecord(c->copyEv[k], s));
+    MDMC_CHECK(c, cudaStreamWaitEvent(c->copyStream, c->copyEv[k], 0));
+    return MDMC_OK;
+}
+
+cudaError_t copyOut(mdmc_context* c, void* dst, const void* src, size_t bytes) {
+    if (!dst || bytes == 0) return cudaSuccess;
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->copyStream);
+}
+
+mdmc_status earlyCopyFaces(mdmc_context* c, int64_t q0, int64_t q1, cudaStream_t s) {
+    const mdmc_host_mesh* h = c->hostOut;
+    mdmc_status st = copyAfter(c, 0, s);
+    if (st != MDMC_OK) return st;
+    const size_t n = (size_t)(q1 - q0);
+    MDMC_CHECK(c, copyOut(c, h->halfedges ? h->halfedges + 16 * q0 : nullptr, c->he.as<int4>() + 4 * q0, 4 * sizeof(int4) * n));
+    MDMC_CHECK(c, copyOut(c, h->quads ? h->quads + 4 * q0 : nullptr, c->quads.as<int4>() + q0, sizeof(int4) * n));
+    MDMC_CHECK(c, copyOut(c, h->face_first_halfedge ? h->face_first_halfedge + q0 : nullptr, c->faceFirst.as<int>() + q0,
+                          sizeof(int) * n));
+    MDMC_CHECK(c, copyOut(c, h->face_attributes ? h->face_attributes + q0 : nullptr, c->faceAttr.as<uint16_t>() + q0,
+                          sizeof(uint16_t) * n));
+    return MDMC_OK;
+}
+
+// the vertex halfedges and flags, final once the fan detection has run
+mdmc_status earlyCopyVertexMaps(mdmc_context* c, cudaStream_t s) {
+    const mdmc_host_mesh* h = c->hostOut;
+    mdmc_status st = copyAfter(c, 0, s);
+    if (st != MDMC_OK) return st;
+    MDMC_CHECK(c, copyOut(c, h->vertex_halfedge, c->vertexHE.p, sizeof(int) * (size_t)c->V));
+    MDMC_CHECK(c, copyOut(c, h->vertex_flags, c->vflags.p, (size_t)c->V));
+    c->earlyVertexMaps = true;
+    return MDMC_OK;
+}
+
+mdmc_status earlyCopyVertices(mdmc_context* c, cudaStream_t s) {
+    const mdmc_host_mesh* h = c->hostOut;
+    mdmc_status st = copyAfter(c, 1, s);
+    if (st != MDMC_OK) return st;
+    MDMC_CHECK(c, copyOut(c, h->positions, c->pos.p, sizeof(float) * 3 * (size_t)c->V));
+    MDMC_CHECK(c, copyOut(c, h->normals, c->nrm.p, sizeof(float) * 3 * (size_t)c->V));
+    c->earlyVertices = true;
     return MDMC_OK;
 }
 
@@ -804,7 +836,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->lastSurfaceIteration = c->opt.enable_surface_to_vertex_iteration;
     c->dmcV = c->activeCells = 0;
     c->simplified = false;
-    c->earlyFaces = c->earlyVertices = c->lateChange = false;
+    c->earlyFaces = c->earlyVertices = c->earlyVertexMaps = c->lateChange = false;
     std::memset(&c->stats, 0, sizeof c->stats);
     DevCounters* ctr = c->counters.as<DevCounters>();
     uint32_t* status = &ctr->status;
@@ -880,18 +912,27 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     cudaEventRecord(c->kev[6], s);
     launchFinishCells(c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A, X, Y, c->quadOwner.as<int>(), (int)Q,
                       status, s);
-    launchQuads(c->act.as<ActiveCell>(), c->quadOwner.as<int>(), (int)A, c->cellMask.as<uint32_t>(),
-                c->cellFirst.as<int>(), X, Y, Z, W, c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(),
-                c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(), c->nmList.as<int4>(), (int)(Q + 1), (int)Q,
-                (int)Vd, c->quads.as<int4>(), c->vertexHE.as<int>(), c->degree.as<int>(), ctr, s);
+    // with host arrays to fill, the quads go in ranges, each copied out as
+    // soon as it is written, so that the copies start early
+    const bool early = earlyFits(c);
+    const int ranges = early ? kCopyRanges : 1;
+    for (int k = 0; k < ranges; ++k) {
+        const int64_t q0 = Q * k / ranges, q1 = Q * (k + 1) / ranges;
+        launchQuads(c->act.as<ActiveCell>(), c->quadOwner.as<int>(), (int)A, c->cellMask.as<uint32_t>(),
+                    c->cellFirst.as<int>(), X, Y, Z, W, c->he.as<int4>(), c->faceFirst.as<int>(),
+                    c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(),
+                    c->nmList.as<int4>(), (int)(Q + 1), (int)Q, (int)Vd, c->quads.as<int4>(), c->vertexHE.as<int>(),
+                    c->degree.as<int>(), ctr, (int)q0, (int)q1, s);
+        if (early && (st = earlyCopyFaces(c, q0, q1, s)) != MDMC_OK) return st;
+    }
+    c->earlyFaces = early;
     cudaEventRecord(c->kev[7], s);
-    if (c->hostOut && (st = earlyCopy(c, 0, s)) != MDMC_OK) return st;
     // vertex positions and normals (sliceP's vertex part)
     cudaEventRecord(c->kev[10], s);
     launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), (int)A, (int)Vd,
                    c->pos.as<float>(), c->nrm.as<float>(), status, s);
     cudaEventRecord(c->kev[11], s);
-    if (c->hostOut && (st = earlyCopy(c, 1, s)) != MDMC_OK) return st;
+    if (early && (st = earlyCopyVertices(c, s)) != MDMC_OK) return st;
     MDMC_CHECK(c, cudaGetLastError());
     cudaEventRecord(c->ev[1], s);
     cudaEventRecord(c->kev[8], s);
@@ -917,6 +958,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     if (!c->simplified) {
         cudaEventRecord(c->ev[3], s);
         if ((st = finishMesh(c, true, &ctr->specStatus, s)) != MDMC_OK) return st;
+        if (early && (st = earlyCopyVertexMaps(c, s)) != MDMC_OK) return st;
         MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
         MDMC_CHECK(c, cudaStreamSynchronize(s));
         finished = !(c->opt.split_non_manifold_halfedges && c->hostCounters->nmBuckets > 0);
@@ -1145,9 +1187,10 @@ mdmc_status mdmc_run_to_host(mdmc_context* c, const mdmc_grid* grid, float iso, 
         MDMC_CHECK(c, cp(out->positions, c->pos, sizeof(float) * 3 * (size_t)c->V));
         MDMC_CHECK(c, cp(out->normals, c->nrm, sizeof(float) * 3 * (size_t)c->V));
     }
-    // written by the fan detection at the end in every case
-    MDMC_CHECK(c, cp(out->vertex_halfedge, c->vertexHE, sizeof(int) * (size_t)c->V));
-    MDMC_CHECK(c, cp(out->vertex_flags, c->vflags, (size_t)c->V));
+    if (!c->earlyVertexMaps || c->lateChange || c->simplified) {
+        MDMC_CHECK(c, cp(out->vertex_halfedge, c->vertexHE, sizeof(int) * (size_t)c->V));
+        MDMC_CHECK(c, cp(out->vertex_flags, c->vflags, (size_t)c->V));
+    }
     MDMC_CHECK(c, cudaStreamSynchronize(s));
     c->err = runMessage;
     return st;

@@ -891,11 +891,11 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
                                               uint8_t* vflags, uint32_t* __restrict__ heValence4,
                                               int4* __restrict__ nmList, int nmCapacity, int numQuads, int numVertices,
                                               int4* __restrict__ quadsOut, int* vertexHE, int* degree,
-                                              DevCounters* ctr) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+                                              DevCounters* ctr, int qBegin, int qEnd) {
+    const int q = qBegin + blockIdx.x * blockDim.x + threadIdx.x;
     int nE = 0, nE3 = 0, nE4 = 0;
     int nmEdges = -1;  // halfedges of this quad on edges of more than two faces
-    bool ok = q < numQuads;
+    bool ok = q < qEnd && q < numQuads;
     const int j = ok ? quadOwner[q] : 0;
     if (ok && !inb(j, numActive)) {
         atomicOr(&ctr->status, kStatusBadIndex);
@@ -1181,8 +1181,8 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
 void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, const uint32_t* cellMask,
                  const int* cellFirst, int X, int Y, int Z, int W, int4* he, int* faceFirst, uint16_t* faceAttr,
                  uint8_t* vflags, uint8_t* heValence, int4* nmList, int nmCapacity, int numQuads, int numVertices,
-                 int4* quadsOut, int* vertexHE, int* degree, DevCounters* ctr, cudaStream_t s) {
-    if (numQuads <= 0) return;
+                 int4* quadsOut, int* vertexHE, int* degree, DevCounters* ctr, int qBegin, int qEnd, cudaStream_t s) {
+    if (qEnd <= qBegin) return;
     countLaunch();
     CellIndex ix;
     ix.mask = cellMask;
@@ -1191,9 +1191,10 @@ void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, con
     ix.Y = Y;
     ix.Z = Z;
     ix.W = W;
-    kQuads<<<(numQuads + 255) / 256, 256, 0, s>>>(act, quadOwner, numActive, ix, he, faceFirst, faceAttr, vflags,
-                                                   reinterpret_cast<uint32_t*>(heValence), nmList, nmCapacity,
-                                                   numQuads, numVertices, quadsOut, vertexHE, degree, ctr);
+    kQuads<<<(qEnd - qBegin + 255) / 256, 256, 0, s>>>(act, quadOwner, numActive, ix, he, faceFirst, faceAttr, vflags,
+                                                        reinterpret_cast<uint32_t*>(heValence), nmList, nmCapacity,
+                                                        numQuads, numVertices, quadsOut, vertexHE, degree, ctr, qBegin,
+                                                        qEnd);
 }
 
 }  // namespace mdmc

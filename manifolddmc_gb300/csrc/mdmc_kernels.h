@@ -120,7 +120,8 @@ void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const Ac
 void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, const uint32_t* cellMask,
                  const int* cellFirst, int X, int Y, int Z, int W, int4* he, int* faceFirst, uint16_t* faceAttr,
                  uint8_t* vflags, uint8_t* heValence, int4* nmList, int nmCapacity, int numQuads, int numVertices,
-                 int4* quadsOut, int* vertexHE, int* degree, DevCounters* ctr, cudaStream_t s);
+                 int4* quadsOut, int* vertexHE, int* degree, DevCounters* ctr, int qBegin, int qEnd,
+                 cudaStream_t s);
 void launchVertexHalfedgeFix(int* vertexHE, int numVertices, cudaStream_t s);
 
 void launchDegree(const int4* he, MeshDims md, int* deg, uint32_t* status, cudaStream_t s);
