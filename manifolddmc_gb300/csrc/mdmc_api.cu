@@ -192,6 +192,15 @@ mdmc_status scan(mdmc_context* c, const T* in, T* out, int64_t n, cudaStream_t s
     return MDMC_OK;
 }
 
+// index of every mask word's first set bit among all set bits (out has n + 1
+// entries, out[n] = all set bits)
+mdmc_status scanPopc(mdmc_context* c, const uint32_t* mask, int* out, int64_t n, cudaStream_t s) {
+    MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(n)));
+    if (!exclusiveScanPopc(mask, out, n, c->scanScratch.as<int>(), s))
+        return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
+    return MDMC_OK;
+}
+
 // reads n int32 values from device memory (synchronizes the stream)
 mdmc_status readInts(mdmc_context* c, const void* src, int n, cudaStream_t s) {
     MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, src, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
@@ -646,15 +655,25 @@ mdmc_status activeCells(mdmc_context* c, const GridDesc& g, float iso, int& W, i
                         c->cellMask.as<uint32_t>(), W, status, s);
     else
         launchRowMask(g, iso, c->cellMask.as<uint32_t>(), (int)numRows, W, s);
-    launchWordCounts(c->cellMask.as<uint32_t>(), numWords, c->cellFirst.as<int>(), s);
-    mdmc_status st = scan<int>(c, c->cellFirst.as<int>(), c->cellFirst.as<int>(), numWords, s);
-    if (st != MDMC_OK) return st;
+    // the scan also lists the active cells' ids, as many as the list holds
+    // already (all of them when the grid is like the last one)
+    MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(numWords)));
+    const int64_t capacity = (int64_t)(c->cellIds.bytes / sizeof(uint32_t));
+    if (!scanMaskScatter(c->cellMask.as<uint32_t>(), c->cellFirst.as<int>(), numWords, W, X, Y,
+                         c->cellIds.as<uint32_t>(), capacity, c->scanScratch.as<int>(), s))
+        return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
     cudaEventRecord(c->kev[3], s);
     MDMC_CHECK(c, cudaGetLastError());
-    if ((st = readInts(c, c->cellFirst.as<int>() + numWords, 1, s)) != MDMC_OK) return st;
+    mdmc_status st = readInts(c, c->cellFirst.as<int>() + numWords, 1, s);
+    if (st != MDMC_OK) return st;
     A = c->hostInts[0];
     const int64_t cells = numRows * (int64_t)(X - 1);
     if (A < 0 || A > cells) return fail(c, MDMC_ERROR_CUDA, "inconsistent cell count from the mask pass");
+    if (A > capacity) {
+        MDMC_CHECK(c, c->cellIds.ensure(sizeof(uint32_t) * (size_t)A));
+        launchScatterCells(c->cellMask.as<uint32_t>(), c->cellFirst.as<int>(), numWords, W, X, Y,
+                           c->cellIds.as<uint32_t>(), (int)A, status, s);
+    }
     return MDMC_OK;
 }
 
@@ -859,10 +878,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     // the active cells' records, contour and quad counts, and their offsets
     MDMC_CHECK(c, c->act.ensure(sizeof(ActiveCell) * (size_t)std::max<int64_t>(A, 1)));
     MDMC_CHECK(c, c->cellCounts.ensure(sizeof(int2) * (size_t)(A + 1)));
-    MDMC_CHECK(c, c->cellIds.ensure(sizeof(uint32_t) * (size_t)std::max<int64_t>(A, 1)));
     cudaEventRecord(c->kev[4], s);
-    launchScatterCells(c->cellMask.as<uint32_t>(), c->cellFirst.as<int>(), numWords, W, X, Y, c->cellIds.as<uint32_t>(),
-                       (int)A, status, s);
     launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A, status,
                      s);
     if ((st = scan<int2>(c, c->cellCounts.as<int2>(), c->cellCounts.as<int2>(), A, s)) != MDMC_OK) return st;
@@ -1040,9 +1056,6 @@ mdmc_status mdmc_run_standard_mc(mdmc_context* c, const mdmc_grid* grid, float i
     int W = 0;
     if ((st = activeCells(c, g, iso, W, numWords, A, s)) != MDMC_OK) return st;
     if (A > 0) {
-        MDMC_CHECK(c, c->cellIds.ensure(sizeof(uint32_t) * (size_t)A));
-        launchScatterCells(c->cellMask.as<uint32_t>(), c->cellFirst.as<int>(), numWords, W, X, Y,
-                           c->cellIds.as<uint32_t>(), (int)A, status, s);
         // intersected edges: bit 3x + axis of the words of sample row (y, z)
         const int W3 = (3 * X + 31) / 32;
         const int64_t nE = (int64_t)Y * Z * W3;
@@ -1053,8 +1066,7 @@ mdmc_status mdmc_run_standard_mc(mdmc_context* c, const mdmc_grid* grid, float i
         MDMC_CHECK(c, cudaMemsetAsync(c->mcEdgeMask.p, 0, sizeof(uint32_t) * (size_t)nE, s));
         launchMCMarkEdges(g, iso, c->cellIds.as<uint32_t>(), (int)A, W3, c->mcEdgeMask.as<uint32_t>(),
                           c->mcCases.as<uint8_t>(), c->mcTriOffset.as<int>(), status, s);
-        launchWordCounts(c->mcEdgeMask.as<uint32_t>(), nE, c->mcEdgeFirst.as<int>(), s);
-        if ((st = scan<int>(c, c->mcEdgeFirst.as<int>(), c->mcEdgeFirst.as<int>(), nE, s)) != MDMC_OK) return st;
+        if ((st = scanPopc(c, c->mcEdgeMask.as<uint32_t>(), c->mcEdgeFirst.as<int>(), nE, s)) != MDMC_OK) return st;
         if ((st = scan<int>(c, c->mcTriOffset.as<int>(), c->mcTriOffset.as<int>(), A, s)) != MDMC_OK) return st;
         MDMC_CHECK(c, cudaGetLastError());
         if ((st = readInts(c, c->mcEdgeFirst.as<int>() + nE, 1, s)) != MDMC_OK) return st;

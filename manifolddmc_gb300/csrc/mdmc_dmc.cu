@@ -21,6 +21,7 @@
 
 #include "mdmc_device.cuh"
 #include "mdmc_kernels.h"
+#include "mdmc_scan.cuh"
 
 namespace mdmc {
 
@@ -614,17 +615,6 @@ void launchRowMask(const GridDesc& g, float iso, uint32_t* mask, int numRows, in
     else kRowMask<PlainView><<<(numRows + 7) / 8, 256, 0, s>>>(g.plain, iso, mask, numRows, W);
 }
 
-__global__ void kWordCounts(const uint32_t* __restrict__ mask, int64_t numWords, int* __restrict__ counts) {
-    const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (w < numWords) counts[w] = __popc(mask[w]);
-}
-
-void launchWordCounts(const uint32_t* mask, int64_t numWords, int* counts, cudaStream_t s) {
-    if (numWords <= 0) return;
-    countLaunch();
-    kWordCounts<<<(unsigned)((numWords + 255) / 256), 256, 0, s>>>(mask, numWords, counts);
-}
-
 // The linear cell id of every active cell, in row-major order: one thread
 // per mask word; the index of the word's first active cell comes from the
 // scan of the word counts.
@@ -646,6 +636,37 @@ __global__ void kScatterCells(const uint32_t* __restrict__ mask, const int* __re
         else atomicOr(status, kStatusCountMismatch);
         ++j;
     }
+}
+
+// The same during the scan's apply pass, which has just computed the word's
+// first index: ids beyond `capacity` are not written (the caller then runs
+// kScatterCells once it knows the count and has the room).
+struct CellScatter {
+    const uint32_t* __restrict__ mask;
+    uint32_t* __restrict__ cellIds;
+    int64_t capacity;
+    int W, X, Y;
+    __device__ __forceinline__ void operator()(int64_t w, int first) const {
+        uint32_t m = mask[w];
+        if (!m) return;
+        const int row = (int)(w / W);
+        const int x0 = (int)(w - (int64_t)row * W) * 32;
+        const int y = row % (Y - 1), z = row / (Y - 1);
+        const uint32_t base = (uint32_t)(((size_t)z * Y + y) * X + x0);
+        int64_t j = first;
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            if (j < capacity) cellIds[j] = base + (uint32_t)b;
+            ++j;
+        }
+    }
+};
+
+bool scanMaskScatter(const uint32_t* mask, int* first, int64_t numWords, int W, int X, int Y, uint32_t* cellIds,
+                     int64_t capacity, int* scratch, cudaStream_t s) {
+    return exclusiveScanOf<int>(PopcRead{mask}, first, numWords, scratch, s,
+                                CellScatter{mask, cellIds, capacity, W, X, Y});
 }
 
 void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords, int W, int X, int Y, uint32_t* cellIds,

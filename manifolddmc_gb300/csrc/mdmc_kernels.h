@@ -97,7 +97,10 @@ void launchBlockMask(const RefinedView& g, float iso, const uint32_t* list, cons
                      uint32_t* mask, int W, uint32_t* status, cudaStream_t s);
 void launchRowCount(const GridDesc& g, float iso, int4* rowCounts, int numRows, cudaStream_t s);
 void launchRowMask(const GridDesc& g, float iso, uint32_t* mask, int numRows, int W, cudaStream_t s);
-void launchWordCounts(const uint32_t* mask, int64_t numWords, int* counts, cudaStream_t s);
+// exclusive scan of the mask words' popcounts into first (numWords + 1
+// entries) that also writes the active cells' ids, the first `capacity` of them
+bool scanMaskScatter(const uint32_t* mask, int* first, int64_t numWords, int W, int X, int Y, uint32_t* cellIds,
+                     int64_t capacity, int* scratch, cudaStream_t s);
 void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords, int W, int X, int Y, uint32_t* cellIds,
                         int numActive, uint32_t* status, cudaStream_t s);
 void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, ActiveCell* act, int2* counts,

@@ -79,8 +79,26 @@ __device__ T blockExclusive(T v, T& total) {
     return ScanOps<T>::add(before, minus(inc, v));
 }
 
+// element readers: an array, or the popcounts of a bit-mask's words (the
+// per-word counts are then never stored)
 template <typename T>
-__global__ void __launch_bounds__(kScanThreads) kScanReduce(const T* __restrict__ in, int64_t n, T* __restrict__ tileSums) {
+struct ArrayRead {
+    const T* __restrict__ p;
+    __device__ __forceinline__ T operator[](int64_t i) const { return p[i]; }
+};
+struct PopcRead {
+    const uint32_t* __restrict__ p;
+    __device__ __forceinline__ int operator[](int64_t i) const { return __popc(p[i]); }
+};
+
+// called by the apply pass with every element's exclusive prefix
+struct NoPost {
+    template <typename T>
+    __device__ __forceinline__ void operator()(int64_t, T) const {}
+};
+
+template <typename T, class In>
+__global__ void __launch_bounds__(kScanThreads) kScanReduce(In in, int64_t n, T* __restrict__ tileSums) {
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     T acc = ScanOps<T>::zero();
 #pragma unroll
@@ -116,9 +134,9 @@ __global__ void __launch_bounds__(1024) kScanTiles(T* tileSums, int numTiles) {
     if (threadIdx.x == 0) tileSums[numTiles] = carryShared;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kScanThreads) kScanApply(const T* __restrict__ in, int64_t n, const T* __restrict__ tileSums,
-                           T* __restrict__ out) {
+template <typename T, class In, class Post>
+__global__ void __launch_bounds__(kScanThreads) kScanApply(In in, int64_t n, const T* __restrict__ tileSums,
+                           T* __restrict__ out, Post post) {
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     // each thread owns kScanItems consecutive elements
     T vals[kScanItems];
@@ -134,7 +152,10 @@ __global__ void __launch_bounds__(kScanThreads) kScanApply(const T* __restrict__
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
         int64_t i = base + (int64_t)threadIdx.x * kScanItems + k;
-        if (i < n) out[i] = run;
+        if (i < n) {
+            out[i] = run;
+            post(i, run);
+        }
         run = ScanOps<T>::add(run, vals[k]);
     }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = tileSums[gridDim.x];
@@ -143,14 +164,14 @@ __global__ void __launch_bounds__(kScanThreads) kScanApply(const T* __restrict__
 // in and out may alias only if the caller accepts in being overwritten after
 // the reduction (kScanApply reads in[i] before writing out[i] of the same i).
 // scratch needs numTiles + 1 elements.  Returns false if n is too large.
-template <typename T>
-bool exclusiveScan(const T* in, T* out, int64_t n, T* scratch, cudaStream_t s) {
+template <typename T, class In, class Post = NoPost>
+bool exclusiveScanOf(In in, T* out, int64_t n, T* scratch, cudaStream_t s, Post post = Post()) {
     const int64_t tiles = (n + kScanTile - 1) / kScanTile;
     if (tiles > kScanMaxTiles) return false;
     const int nt = tiles > 0 ? (int)tiles : 1;
     if (n > 0) {
         countLaunch();
-        kScanReduce<T><<<nt, kScanThreads, 0, s>>>(in, n, scratch);
+        kScanReduce<T, In><<<nt, kScanThreads, 0, s>>>(in, n, scratch);
     } else {
         cudaMemsetAsync(scratch, 0, sizeof(T), s);
     }
@@ -158,11 +179,22 @@ bool exclusiveScan(const T* in, T* out, int64_t n, T* scratch, cudaStream_t s) {
     kScanTiles<T><<<1, 1024, 0, s>>>(scratch, n > 0 ? nt : 0);
     if (n > 0) {
         countLaunch();
-        kScanApply<T><<<nt, kScanThreads, 0, s>>>(in, n, scratch, out);
+        kScanApply<T, In, Post><<<nt, kScanThreads, 0, s>>>(in, n, scratch, out, post);
     } else {
         cudaMemcpyAsync(out, scratch, sizeof(T), cudaMemcpyDeviceToDevice, s);
     }
     return true;
+}
+
+template <typename T>
+bool exclusiveScan(const T* in, T* out, int64_t n, T* scratch, cudaStream_t s) {
+    return exclusiveScanOf<T>(ArrayRead<T>{in}, out, n, scratch, s);
+}
+
+// exclusive scan of the popcounts of n mask words: out[i] = set bits in
+// words 0..i-1, out[n] = all set bits
+inline bool exclusiveScanPopc(const uint32_t* mask, int* out, int64_t n, int* scratch, cudaStream_t s) {
+    return exclusiveScanOf<int>(PopcRead{mask}, out, n, scratch, s);
 }
 
 inline int64_t scanScratchElems(int64_t n) { return (n + kScanTile - 1) / kScanTile + 2; }

@@ -278,3 +278,28 @@ def test_render_buffers_match_the_mesh():
         if nm and fans: hue = 240.0
         assert np.array_equal(verts[v, 6:9], np.array(_hsv(hue), np.float32)), (v, fl)
         assert verts[v, 9] == 1.0
+
+
+def test_one_context_over_growing_and_shrinking_grids():
+    """Buffers sized by earlier runs (the active-cell list is written during
+    the scan when it already has room, after it otherwise) give the same
+    meshes as a fresh context, on plain and refined grids."""
+    o, s = np.zeros(3, np.float32), np.ones(3, np.float32)
+    grids = [
+        mdmc.UniformGrid(blobs(14, 3, 61), [14, 14, 14], o, s),
+        mdmc.UniformGrid(np.random.default_rng(62).random((22, 22, 22), dtype=np.float32), [22, 22, 22], o, s),
+        mdmc.UniformGrid(blobs(17, 5, 63), [17, 17, 17], o, s, 3, True),
+        mdmc.UniformGrid(blobs(14, 3, 61), [14, 14, 14], o, s),
+        mdmc.UniformGrid(np.random.default_rng(64).random((9, 12, 10), dtype=np.float32), [10, 12, 9], o, s, 1, False),
+    ]
+    isos = [0.5, 0.5, 0.4, 0.5, 0.5]
+    shared = mdmc.DualMarchingCubes()
+    for g, iso in zip(grids, isos):
+        fresh = mdmc.DualMarchingCubes()
+        fresh.run(iso, g)
+        shared.run(iso, g)
+        a, b = fresh.get_halfedge_mesh(), shared.get_halfedge_mesh()
+        assert np.array_equal(a.halfedges, b.halfedges)
+        assert np.array_equal(a.positions.view(np.uint32), b.positions.view(np.uint32))
+        assert np.array_equal(a.vertex_flags, b.vertex_flags)
+        assert fresh.stats.num_active_cells == shared.stats.num_active_cells
