@@ -333,10 +333,77 @@ __device__ __forceinline__ void orActive(uint32_t* mask, int W, int Y, bool acti
     }
 }
 
+// The 5x5x5 refined samples (xs..xs+4, ys..ys+4, zs..zs+4) of a standard
+// block into buf[kz*25 + ky*5 + kx], evaluated separably: every sample is
+// RefinedView::at's trilinear interpolation, whose x-lerps depend only on
+// (kx, coarse row) and whose y-lerps only on (kx, ky, coarse z), so the 27
+// coarse samples around the block are loaded once, the 45 distinct x-lerps and
+// 75 distinct y-lerps are computed once and the 125 z-lerps finish them, each
+// with the operations and operands at() uses.  Returns false (nothing
+// written) when the block's coarse indices do not lie within a 3x3x3 range.
+__device__ bool blockSamples5(const RefinedView& g, int xs, int ys, int zs, int lane, float* __restrict__ buf,
+                              float* __restrict__ sc, int* __restrict__ ax, float* __restrict__ ad) {
+    int i0 = 0, i1 = 0;
+    float d = 0.f;
+    if (lane < 15) {
+        const int a = lane / 5, k = lane - 5 * a;
+        const int n = a == 0 ? g.X : (a == 1 ? g.Y : g.Z);
+        const int cn = a == 0 ? g.cX : (a == 1 ? g.cY : g.cZ);
+        const int p = (a == 0 ? xs : (a == 1 ? ys : zs)) + k;
+        const float q = g.divf(g.unpad(p, n));
+        const int m = (int)floorf(q);
+        d = q - (float)m;
+        i0 = min(max(m, 0), cn - 1);
+        i1 = min(max(m + 1, 0), cn - 1);
+    }
+    const int bx = __shfl_sync(0xffffffffu, i0, 0), by = __shfl_sync(0xffffffffu, i0, 5),
+              bz = __shfl_sync(0xffffffffu, i0, 10);
+    const int b = lane < 5 ? bx : (lane < 10 ? by : bz);
+    const int r0 = i0 - b, r1 = i1 - b;
+    if (__ballot_sync(0xffffffffu, lane < 15 && (r0 < 0 || r1 > 2 || r0 > r1)) != 0u) return false;
+    if (lane < 15) {
+        ax[lane] = r0;
+        ax[15 + lane] = r1;
+        ad[lane] = d;
+    }
+    if (lane < 27) {
+        const int rx = lane % 3, ry = (lane / 3) % 3, rz = lane / 9;
+        const int cx = min(bx + rx, g.cX - 1), cy = min(by + ry, g.cY - 1), cz = min(bz + rz, g.cZ - 1);
+        sc[lane] = __ldg(g.c + ((size_t)cz * g.cY + cy) * g.cX + cx);
+    }
+    __syncwarp();
+    float* xl = sc + 27;  // [rz][ry][kx], 45
+    float* yl = sc + 72;  // [rz][ky][kx], 75
+    for (int i = lane; i < 45; i += 32) {
+        const int kx = i % 5, ry = (i / 5) % 3, rz = i / 15;
+        const float s0 = sc[rz * 9 + ry * 3 + ax[kx]], s1 = sc[rz * 9 + ry * 3 + ax[15 + kx]];
+        xl[i] = s0 + ad[kx] * (s1 - s0);
+    }
+    __syncwarp();
+    for (int i = lane; i < 75; i += 32) {
+        const int kx = i % 5, ky = (i / 5) % 5, rz = i / 25;
+        const float dy = ad[5 + ky];
+        const float a = xl[rz * 15 + ax[5 + ky] * 5 + kx], bb = xl[rz * 15 + ax[20 + ky] * 5 + kx];
+        yl[i] = (1.f - dy) * a + dy * bb;
+    }
+    __syncwarp();
+    for (int i = lane; i < 125; i += 32) {
+        const int kx = i % 5, ky = (i / 5) % 5, kz = i / 25;
+        const float dz = ad[10 + kz];
+        const float lo = yl[ax[10 + kz] * 25 + ky * 5 + kx], hi = yl[ax[25 + kz] * 25 + ky * 5 + kx];
+        buf[i] = (1.f - dz) * lo + dz * hi;
+    }
+    __syncwarp();
+    return true;
+}
+
 __global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g, float iso, const uint32_t* __restrict__ list,
                                                                  const unsigned long long* listCount,
                                                                  uint32_t* __restrict__ mask, int W, uint32_t* status) {
     __shared__ float samples[kBlockMaskWarps][kBlockSamplesMax];
+    __shared__ float sepSamples[kBlockMaskWarps][27 + 45 + 75];
+    __shared__ int sepIndex[kBlockMaskWarps][30];
+    __shared__ float sepFrac[kBlockMaskWarps][15];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float* buf = samples[warp];
     const int64_t count = (int64_t)*listCount;
@@ -364,17 +431,19 @@ __global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g
             // the standard block of a x4 refinement: 125 samples and 64 cells
             // with compile-time strides; the 4 cells of a row lie in one mask
             // word and occupy 4 aligned lanes, OR-ed by two shuffles
-            float v[4];
+            if (!blockSamples5(g, xs, ys, zs, lane, buf, sepSamples[warp], sepIndex[warp], sepFrac[warp])) {
+                float v[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int k = 32 * u + lane;
-                const int kk = k < 125 ? k : 0;
-                v[u] = g.at(xs + kk % 5, ys + (kk / 5) % 5, zs + kk / 25);
+                for (int u = 0; u < 4; ++u) {
+                    const int k = 32 * u + lane;
+                    const int kk = k < 125 ? k : 0;
+                    v[u] = g.at(xs + kk % 5, ys + (kk / 5) % 5, zs + kk / 25);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (32 * u + lane < 125) buf[32 * u + lane] = v[u];
+                __syncwarp();
             }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (32 * u + lane < 125) buf[32 * u + lane] = v[u];
-            __syncwarp();
 #pragma unroll
             for (int k0 = 0; k0 < 64; k0 += 32) {
                 const int k = k0 + lane;
