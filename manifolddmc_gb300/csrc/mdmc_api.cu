@@ -638,8 +638,11 @@ mdmc_status earlyCopyVertices(mdmc_context* c, cudaStream_t s) {
 // The DMC front end: the active-cell mask per x-row of cells (W words per
 // row, numWords in all) and the index of every word's first active cell
 // (cellFirst, the cell index the quad pass reads too); A = active cells.
-mdmc_status activeCells(mdmc_context* c, const GridDesc& g, float iso, int& W, int64_t& numWords, int64_t& A,
-                        cudaStream_t s) {
+// The mask and its scan, without reading the count back: the scan lists the
+// active cells' ids as far as the list holds (idsCapacity); cellFirst[numWords]
+// is the count.
+mdmc_status markActive(mdmc_context* c, const GridDesc& g, float iso, int& W, int64_t& numWords, int64_t& idsCapacity,
+                       cudaStream_t s) {
     const GridGeom& geom = g.geom();
     const int X = geom.X, Y = geom.Y, Z = geom.Z;
     uint32_t* status = &c->counters.as<DevCounters>()->status;
@@ -658,23 +661,40 @@ mdmc_status activeCells(mdmc_context* c, const GridDesc& g, float iso, int& W, i
     // the scan also lists the active cells' ids, as many as the list holds
     // already (all of them when the grid is like the last one)
     MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(numWords)));
-    const int64_t capacity = (int64_t)(c->cellIds.bytes / sizeof(uint32_t));
+    idsCapacity = (int64_t)(c->cellIds.bytes / sizeof(uint32_t));
     if (!scanMaskScatter(c->cellMask.as<uint32_t>(), c->cellFirst.as<int>(), numWords, W, X, Y,
-                         c->cellIds.as<uint32_t>(), capacity, c->scanScratch.as<int>(), s))
+                         c->cellIds.as<uint32_t>(), idsCapacity, c->scanScratch.as<int>(), s))
         return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
     cudaEventRecord(c->kev[3], s);
     MDMC_CHECK(c, cudaGetLastError());
-    mdmc_status st = readInts(c, c->cellFirst.as<int>() + numWords, 1, s);
-    if (st != MDMC_OK) return st;
-    A = c->hostInts[0];
-    const int64_t cells = numRows * (int64_t)(X - 1);
+    return MDMC_OK;
+}
+
+// With the count A known: checks it and lists the ids the scan had no room for.
+mdmc_status finishActive(mdmc_context* c, const GridDesc& g, int W, int64_t numWords, int64_t A, int64_t idsCapacity,
+                         cudaStream_t s) {
+    const GridGeom& geom = g.geom();
+    const int X = geom.X, Y = geom.Y, Z = geom.Z;
+    const int64_t cells = (X > 1 && Y > 1 && Z > 1) ? (int64_t)(X - 1) * (Y - 1) * (Z - 1) : 0;
     if (A < 0 || A > cells) return fail(c, MDMC_ERROR_CUDA, "inconsistent cell count from the mask pass");
-    if (A > capacity) {
+    if (A > idsCapacity) {
         MDMC_CHECK(c, c->cellIds.ensure(sizeof(uint32_t) * (size_t)A));
         launchScatterCells(c->cellMask.as<uint32_t>(), c->cellFirst.as<int>(), numWords, W, X, Y,
-                           c->cellIds.as<uint32_t>(), (int)A, status, s);
+                           c->cellIds.as<uint32_t>(), (int)A, &c->counters.as<DevCounters>()->status, s);
     }
     return MDMC_OK;
+}
+
+// The DMC front end with the count read back: mask, scan and the ids of all
+// active cells.
+mdmc_status activeCells(mdmc_context* c, const GridDesc& g, float iso, int& W, int64_t& numWords, int64_t& A,
+                        cudaStream_t s) {
+    int64_t idsCapacity = 0;
+    mdmc_status st = markActive(c, g, iso, W, numWords, idsCapacity, s);
+    if (st != MDMC_OK) return st;
+    if ((st = readInts(c, c->cellFirst.as<int>() + numWords, 1, s)) != MDMC_OK) return st;
+    A = c->hostInts[0];
+    return finishActive(c, g, W, numWords, A, idsCapacity, s);
 }
 
 }  // namespace
@@ -869,23 +889,50 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     if (st0 != MDMC_OK) return st0;
 
     // ---- DMC (performDualMarchingCubes) -----------------------------------------
-    int64_t numWords = 0, A = 0;
+    int64_t numWords = 0, idsCapacity = 0;
     int W = 0;
-    mdmc_status st = activeCells(c, g, iso, W, numWords, A, s);
+    mdmc_status st = markActive(c, g, iso, W, numWords, idsCapacity, s);
     if (st != MDMC_OK) return st;
-    c->stats.num_active_cells = A;
 
-    // the active cells' records, contour and quad counts, and their offsets
-    MDMC_CHECK(c, c->act.ensure(sizeof(ActiveCell) * (size_t)std::max<int64_t>(A, 1)));
-    MDMC_CHECK(c, c->cellCounts.ensure(sizeof(int2) * (size_t)(A + 1)));
+    // the active cells' records, their contour and quad counts and offsets.
+    // Without reading the active-cell count back first: the records are
+    // made for as many cells as the lists hold (all of them when the grid is
+    // like the last one), the count read on the device, and one read-back
+    // brings the cell, vertex and quad counts; only when the lists were too
+    // short is the pass repeated at the right size.
+    const int* numActiveDev = c->cellFirst.as<int>() + numWords;
+    int64_t capA = std::min<int64_t>(idsCapacity, (int64_t)(c->act.bytes / sizeof(ActiveCell)));
+    capA = std::min<int64_t>(capA, (int64_t)(c->cellCounts.bytes / sizeof(int2)) - 1);
+    capA = std::max<int64_t>(std::min<int64_t>(capA, 0x7FFFFFFF), 0);
     cudaEventRecord(c->kev[4], s);
-    launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A, status,
-                     s);
-    if ((st = scan<int2>(c, c->cellCounts.as<int2>(), c->cellCounts.as<int2>(), A, s)) != MDMC_OK) return st;
+    if (capA > 0) {
+        MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(capA)));
+        launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)capA,
+                         status, s, numActiveDev);
+        if (!exclusiveScanOf<int2>(ArrayRead<int2>{c->cellCounts.as<int2>()}, c->cellCounts.as<int2>(), capA,
+                                   c->scanScratch.as<int2>(), s, NoPost(), numActiveDev))
+            return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
+    }
+    launchGatherCounts(numActiveDev, capA > 0 ? c->cellCounts.as<int2>() : nullptr, capA > 0 ? (int)capA : -1,
+                       ctr->gathered, s);
     cudaEventRecord(c->kev[5], s);
     MDMC_CHECK(c, cudaGetLastError());
-    if ((st = readInts(c, c->cellCounts.as<int2>() + A, 2, s)) != MDMC_OK) return st;
-    const int64_t Vd = c->hostInts[0], Q = c->hostInts[1];
+    if ((st = readInts(c, ctr->gathered, 3, s)) != MDMC_OK) return st;
+    const int64_t A = c->hostInts[0];
+    int64_t Vd = c->hostInts[1], Q = c->hostInts[2];
+    if ((st = finishActive(c, g, W, numWords, A, idsCapacity, s)) != MDMC_OK) return st;
+    c->stats.num_active_cells = A;
+    if (A > capA || capA == 0) {
+        MDMC_CHECK(c, c->act.ensure(sizeof(ActiveCell) * (size_t)std::max<int64_t>(A, 1)));
+        MDMC_CHECK(c, c->cellCounts.ensure(sizeof(int2) * (size_t)(A + 1)));
+        launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A,
+                         status, s);
+        if ((st = scan<int2>(c, c->cellCounts.as<int2>(), c->cellCounts.as<int2>(), A, s)) != MDMC_OK) return st;
+        MDMC_CHECK(c, cudaGetLastError());
+        if ((st = readInts(c, c->cellCounts.as<int2>() + A, 2, s)) != MDMC_OK) return st;
+        Vd = c->hostInts[0];
+        Q = c->hostInts[1];
+    }
     if (Vd < A || Vd > 4 * A || Q < 0 || Q > 3 * A)
         return fail(c, MDMC_ERROR_CUDA, "inconsistent vertex or quad count from the emit pass");
     c->stats.num_dmc_vertices = Vd;

@@ -753,11 +753,12 @@ void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords
 template <class View>
 __global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint32_t* __restrict__ cellIds,
                                                    ActiveCell* __restrict__ act, int2* __restrict__ counts,
-                                                   int numActive, uint32_t* status) {
+                                                   int numActive, const int* numActiveDev, uint32_t* status) {
     __shared__ uint64_t table[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kContourTable[i];
     __syncthreads();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (numActiveDev) numActive = min(max(*numActiveDev, 0), numActive);
     if (j >= numActive) return;
     const uint32_t cell = cellIds[j];
     const uint32_t line = cell / (uint32_t)g.X;
@@ -800,14 +801,32 @@ __global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint
 }
 
 void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, ActiveCell* act, int2* counts,
-                      int numActive, uint32_t* status, cudaStream_t s) {
+                      int numActive, uint32_t* status, cudaStream_t s, const int* numActiveDev) {
     if (numActive <= 0) return;
     countLaunch();
     const unsigned blocks = (unsigned)((numActive + 127) / 128);
     if (g.refined)
-        kEmitActive<RefinedView><<<blocks, 128, 0, s>>>(g.ref, iso, cellIds, act, counts, numActive, status);
+        kEmitActive<RefinedView><<<blocks, 128, 0, s>>>(g.ref, iso, cellIds, act, counts, numActive, numActiveDev,
+                                                        status);
     else
-        kEmitActive<PlainView><<<blocks, 128, 0, s>>>(g.plain, iso, cellIds, act, counts, numActive, status);
+        kEmitActive<PlainView><<<blocks, 128, 0, s>>>(g.plain, iso, cellIds, act, counts, numActive, numActiveDev,
+                                                      status);
+}
+
+// the active-cell count and, when the emit pass covered them all, the
+// vertex and quad totals of its scan, into one place for one read-back
+__global__ void kGatherCounts(const int* numActiveDev, const int2* counts, int capacity, int* out) {
+    const int a = *numActiveDev;
+    out[0] = a;
+    const bool all = a >= 0 && a <= capacity;
+    const int2 t = all ? counts[a] : make_int2(-1, -1);
+    out[1] = t.x;
+    out[2] = t.y;
+}
+
+void launchGatherCounts(const int* numActiveDev, const int2* counts, int capacity, int* out, cudaStream_t s) {
+    countLaunch();
+    kGatherCounts<<<1, 1, 0, s>>>(numActiveDev, counts, capacity, out);
 }
 
 // Each active cell's first vertex id (kept in its record's spare word) and

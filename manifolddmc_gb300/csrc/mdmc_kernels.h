@@ -103,8 +103,10 @@ bool scanMaskScatter(const uint32_t* mask, int* first, int64_t numWords, int W, 
                      int64_t capacity, int* scratch, cudaStream_t s);
 void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords, int W, int X, int Y, uint32_t* cellIds,
                         int numActive, uint32_t* status, cudaStream_t s);
+// numActiveDev != nullptr: the count is read on the device, at most numActive
 void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, ActiveCell* act, int2* counts,
-                      int numActive, uint32_t* status, cudaStream_t s);
+                      int numActive, uint32_t* status, cudaStream_t s, const int* numActiveDev = nullptr);
+void launchGatherCounts(const int* numActiveDev, const int2* counts, int capacity, int* out, cudaStream_t s);
 // standard Marching Cubes (edge mask over global edge ids 3 * sample + axis,
 // W3 words per sample row)
 void launchMCMarkEdges(const GridDesc& g, float iso, const uint32_t* cellIds, int numActive, int W3, uint32_t* edgeMask,

@@ -97,8 +97,24 @@ struct NoPost {
     __device__ __forceinline__ void operator()(int64_t, T) const {}
 };
 
+// the element count: known on the host (dev == nullptr), or read on the
+// device from *dev and capped at max (the launch covers max elements)
+struct ScanCount {
+    int64_t max;
+    const int* dev;
+    __device__ __forceinline__ int64_t get() const {
+        if (!dev) return max;
+        const int64_t n = *dev;
+        return n < 0 ? 0 : (n < max ? n : max);
+    }
+};
+
+__device__ __forceinline__ int64_t scanTiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
+
 template <typename T, class In>
-__global__ void __launch_bounds__(kScanThreads) kScanReduce(In in, int64_t n, T* __restrict__ tileSums) {
+__global__ void __launch_bounds__(kScanThreads) kScanReduce(In in, ScanCount cnt, T* __restrict__ tileSums) {
+    const int64_t n = cnt.get();
+    if (blockIdx.x > 0 && blockIdx.x >= scanTiles(n)) return;
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     T acc = ScanOps<T>::zero();
 #pragma unroll
@@ -116,7 +132,8 @@ __global__ void __launch_bounds__(kScanThreads) kScanReduce(In in, int64_t n, T*
 // one value per thread and chunk (the block launches with 1024 threads, so a
 // thread may hold at most 64 registers).
 template <typename T>
-__global__ void __launch_bounds__(1024) kScanTiles(T* tileSums, int numTiles) {
+__global__ void __launch_bounds__(1024) kScanTiles(T* tileSums, ScanCount cnt) {
+    const int numTiles = (int)scanTiles(cnt.get());
     __shared__ T carryShared;
     if (threadIdx.x == 0) carryShared = ScanOps<T>::zero();
     __syncthreads();
@@ -135,8 +152,12 @@ __global__ void __launch_bounds__(1024) kScanTiles(T* tileSums, int numTiles) {
 }
 
 template <typename T, class In, class Post>
-__global__ void __launch_bounds__(kScanThreads) kScanApply(In in, int64_t n, const T* __restrict__ tileSums,
+__global__ void __launch_bounds__(kScanThreads) kScanApply(In in, ScanCount cnt, const T* __restrict__ tileSums,
                            T* __restrict__ out, Post post) {
+    const int64_t n = cnt.get();
+    const int nTiles = (int)scanTiles(n);
+    const int lastBlock = nTiles > 0 ? nTiles - 1 : 0;
+    if ((int)blockIdx.x > lastBlock) return;
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     // each thread owns kScanItems consecutive elements
     T vals[kScanItems];
@@ -158,28 +179,32 @@ __global__ void __launch_bounds__(kScanThreads) kScanApply(In in, int64_t n, con
         }
         run = ScanOps<T>::add(run, vals[k]);
     }
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = tileSums[gridDim.x];
+    if ((int)blockIdx.x == lastBlock && threadIdx.x == 0) out[n] = tileSums[nTiles];
 }
 
 // in and out may alias only if the caller accepts in being overwritten after
 // the reduction (kScanApply reads in[i] before writing out[i] of the same i).
 // scratch needs numTiles + 1 elements.  Returns false if n is too large.
+// nDev != nullptr: the element count is read on the device from *nDev,
+// at most n (the capacity the launches cover).
 template <typename T, class In, class Post = NoPost>
-bool exclusiveScanOf(In in, T* out, int64_t n, T* scratch, cudaStream_t s, Post post = Post()) {
+bool exclusiveScanOf(In in, T* out, int64_t n, T* scratch, cudaStream_t s, Post post = Post(),
+                     const int* nDev = nullptr) {
     const int64_t tiles = (n + kScanTile - 1) / kScanTile;
     if (tiles > kScanMaxTiles) return false;
     const int nt = tiles > 0 ? (int)tiles : 1;
-    if (n > 0) {
+    const ScanCount cnt{n, nDev};
+    if (n > 0 || nDev) {
         countLaunch();
-        kScanReduce<T, In><<<nt, kScanThreads, 0, s>>>(in, n, scratch);
+        kScanReduce<T, In><<<nt, kScanThreads, 0, s>>>(in, cnt, scratch);
     } else {
         cudaMemsetAsync(scratch, 0, sizeof(T), s);
     }
     countLaunch();
-    kScanTiles<T><<<1, 1024, 0, s>>>(scratch, n > 0 ? nt : 0);
-    if (n > 0) {
+    kScanTiles<T><<<1, 1024, 0, s>>>(scratch, cnt);
+    if (n > 0 || nDev) {
         countLaunch();
-        kScanApply<T, In, Post><<<nt, kScanThreads, 0, s>>>(in, n, scratch, out, post);
+        kScanApply<T, In, Post><<<nt, kScanThreads, 0, s>>>(in, cnt, scratch, out, post);
     } else {
         cudaMemcpyAsync(out, scratch, sizeof(T), cudaMemcpyDeviceToDevice, s);
     }

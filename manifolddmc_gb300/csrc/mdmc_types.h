@@ -55,6 +55,7 @@ struct DevCounters {
     unsigned long long nmBuckets;  // length of the 4-face bucket list
     unsigned long long candidates; // coarse cells that may cross iso (refined grids)
     unsigned long long slowFans;   // vertices the single fan walk did not settle
+    int gathered[4];               // active cells, DMC vertices, quads (one read-back)
 };
 
 }  // namespace mdmc
