@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(128) kBackwardCells(View g, float iso, const A
     for (int t = 0; t < n; ++t) {
         const int csz = nib(c, t);
         const int64_t v = rec.pad + t;
-        const float gv[3] = {vertexGrad[3 * v], vertexGrad[3 * v + 1], vertexGrad[3 * v + 2]};
+        const float gv[3] = {vertexGrad[3 * (int64_t)v], vertexGrad[3 * (int64_t)v + 1], vertexGrad[3 * (int64_t)v + 2]};
         for (int k = 0; k < csz; ++k) {
             const int e = (int)((c >> (16 + 4 * (before + k))) & 0xF);
             const int a0 = edgeV0(e), a1 = edgeV1(e), ax = edgeAxis(e);

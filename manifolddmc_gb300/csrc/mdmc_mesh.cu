@@ -168,7 +168,9 @@ __device__ __forceinline__ F3 nudge(int it) {
     return r * kEpsilon;
 }
 
-__device__ __forceinline__ F3 loadP(const float* pos, int v) { return f3(pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]); }
+__device__ __forceinline__ F3 loadP(const float* pos, int v) {
+    return f3(pos[3 * (int64_t)v], pos[3 * (int64_t)v + 1], pos[3 * (int64_t)v + 2]);
+}
 
 template <class View>
 __global__ void kReconnect(View g, float iso, const int4* __restrict__ nmList,

@@ -73,8 +73,8 @@ __global__ void kCopyOut(const int* __restrict__ nmFaces, int n, const int4* __r
         const int c = 4 * k + i;
         const int v = e.x;
         for (int a = 0; a < 3; ++a) {
-            w.pos[3 * c + a] = pos[3 * (int64_t)v + a];
-            w.nrm[3 * c + a] = nrm[3 * (int64_t)v + a];
+            w.pos[3 * (int64_t)c + a] = pos[3 * (int64_t)v + a];
+            w.nrm[3 * (int64_t)c + a] = nrm[3 * (int64_t)v + a];
         }
         w.vC2O[c] = v;
         w.origV[c] = v;
@@ -151,8 +151,8 @@ __global__ void kSubdivide(int n, SplitWork w, uint32_t* status) {
     }
     F3 P[4], N[4];
     for (int i = 0; i < 4; ++i) {
-        P[i] = f3(w.pos[3 * vid[i]], w.pos[3 * vid[i] + 1], w.pos[3 * vid[i] + 2]);
-        N[i] = f3(w.nrm[3 * vid[i]], w.nrm[3 * vid[i] + 1], w.nrm[3 * vid[i] + 2]);
+        P[i] = f3(w.pos[3 * (int64_t)vid[i]], w.pos[3 * (int64_t)vid[i] + 1], w.pos[3 * (int64_t)vid[i] + 2]);
+        N[i] = f3(w.nrm[3 * (int64_t)vid[i]], w.nrm[3 * (int64_t)vid[i] + 1], w.nrm[3 * (int64_t)vid[i] + 2]);
     }
     auto mix = [](F3 a, F3 b, float t) { return a * (1.f - t) + b * t; };
     int inner[4];
@@ -162,8 +162,8 @@ __global__ void kSubdivide(int n, SplitWork w, uint32_t* status) {
         const F3 nn = mix(mix(N[0], N[1], u), mix(N[3], N[2], u), v);
         const int c = 4 * n + 4 * k + i;
         w.origV[c] = w.vC2O[vid[i]];  // the differentiable path's parent: corner i
-        w.pos[3 * c] = pp.x; w.pos[3 * c + 1] = pp.y; w.pos[3 * c + 2] = pp.z;
-        w.nrm[3 * c] = nn.x; w.nrm[3 * c + 1] = nn.y; w.nrm[3 * c + 2] = nn.z;
+        w.pos[3 * (int64_t)c] = pp.x; w.pos[3 * (int64_t)c + 1] = pp.y; w.pos[3 * (int64_t)c + 2] = pp.z;
+        w.nrm[3 * (int64_t)c] = nn.x; w.nrm[3 * (int64_t)c + 1] = nn.y; w.nrm[3 * (int64_t)c + 2] = nn.z;
         inner[i] = c;
     }
     const int hb = 4 * n + 16 * k;
@@ -215,7 +215,7 @@ __device__ __forceinline__ void markPartner(int* num, int* slots, int count, int
         return;
     }
     const int idx = atomicAdd(&num[a], 1);
-    if (idx - 1 < 4) slots[4 * a + idx - 1] = b;
+    if (idx - 1 < 4) slots[4 * (int64_t)a + idx - 1] = b;
     if (idx > 2) atomicOr(status, kStatusPartnerOverflow);
 }
 
@@ -285,13 +285,13 @@ __global__ void kSortPartners(int* num, int* slots, int count) {
     const int n = min(num[a] - 1, 4);
     if (n < 2) return;
     int s[4];
-    for (int i = 0; i < n; ++i) s[i] = slots[4 * a + i];
+    for (int i = 0; i < n; ++i) s[i] = slots[4 * (int64_t)a + i];
     for (int i = 1; i < n; ++i) {
         int v = s[i], j = i - 1;
         while (j >= 0 && s[j] > v) { s[j + 1] = s[j]; --j; }
         s[j + 1] = v;
     }
-    for (int i = 0; i < n; ++i) slots[4 * a + i] = s[i];
+    for (int i = 0; i < n; ++i) slots[4 * (int64_t)a + i] = s[i];
 }
 
 // DeviceMergeList::getAllPartnersOf (:25-62): breadth-first closure, at most
@@ -300,12 +300,12 @@ __device__ int closure(const int* num, const int* slots, int v, int out[12], uin
     auto cnt = [&](int x) { return min(num[x], 5); };
     int np = cnt(v);
     if (np <= 1) return np;
-    for (int i = 0; i < np - 1; ++i) out[i] = slots[4 * v + i];
+    for (int i = 0; i < np - 1; ++i) out[i] = slots[4 * (int64_t)v + i];
     for (int i = 0; i < np - 1; ++i) {
         const int p = out[i];
         const int npp = cnt(p);
         for (int k = 0; k < npp - 1; ++k) {
-            const int pp = slots[4 * p + k];
+            const int pp = slots[4 * (int64_t)p + k];
             bool contained = (pp == v);
             for (int z = 0; z < np - 1; ++z) contained = contained || out[z] == pp;
             if (!contained) {
@@ -334,11 +334,11 @@ __global__ void kMergeVertices(SplitWork w, uint32_t* status) {
         return;
     }
     int smallest = v;
-    F3 p = f3(w.pos[3 * v], w.pos[3 * v + 1], w.pos[3 * v + 2]);
+    F3 p = f3(w.pos[3 * (int64_t)v], w.pos[3 * (int64_t)v + 1], w.pos[3 * (int64_t)v + 2]);
     bool obsolete = false;
     for (int i = 0; i < np - 1; ++i) {
         const int q = part[i];
-        p = p + f3(w.pos[3 * q], w.pos[3 * q + 1], w.pos[3 * q + 2]);
+        p = p + f3(w.pos[3 * (int64_t)q], w.pos[3 * (int64_t)q + 1], w.pos[3 * (int64_t)q + 2]);
         if (q < smallest) {
             obsolete = true;
             smallest = q;
@@ -349,8 +349,8 @@ __global__ void kMergeVertices(SplitWork w, uint32_t* status) {
         return;
     }
     p = p / (float)np;
-    w.pos[3 * smallest] = p.x; w.pos[3 * smallest + 1] = p.y; w.pos[3 * smallest + 2] = p.z;
-    w.nrm[3 * smallest] = p.x; w.nrm[3 * smallest + 1] = p.y; w.nrm[3 * smallest + 2] = p.z;
+    w.pos[3 * (int64_t)smallest] = p.x; w.pos[3 * (int64_t)smallest + 1] = p.y; w.pos[3 * (int64_t)smallest + 2] = p.z;
+    w.nrm[3 * (int64_t)smallest] = p.x; w.nrm[3 * (int64_t)smallest + 1] = p.y; w.nrm[3 * (int64_t)smallest + 2] = p.z;
 }
 
 // updateHalfedgeVertexIDs (:992-1019)
@@ -396,7 +396,7 @@ __global__ void kMoveVertices(View g, float iso, SplitWork w) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= w.nv) return;
     if (w.vfl[v] & kRemove) return;
-    const F3 p = f3(w.pos[3 * v], w.pos[3 * v + 1], w.pos[3 * v + 2]);
+    const F3 p = f3(w.pos[3 * (int64_t)v], w.pos[3 * (int64_t)v + 1], w.pos[3 * (int64_t)v + 2]);
     int idx[3];
     g.cellOf(p, idx);
     float s[8];
@@ -409,7 +409,7 @@ __global__ void kMoveVertices(View g, float iso, SplitWork w) {
     SurfaceIterator it{s, iso};
     it.move(local);
     const F3 q = g.origin() + (fi + local) * g.deltas();
-    w.pos[3 * v] = q.x; w.pos[3 * v + 1] = q.y; w.pos[3 * v + 2] = q.z;
+    w.pos[3 * (int64_t)v] = q.x; w.pos[3 * (int64_t)v + 1] = q.y; w.pos[3 * (int64_t)v + 2] = q.z;
 }
 
 // copy-back selection: elements kept and without an original get appended
@@ -440,8 +440,8 @@ __global__ void kCopyBackVertices(SplitWork w, const int* __restrict__ app, int 
         return;
     }
     for (int a = 0; a < 3; ++a) {
-        pos[3 * (int64_t)o + a] = w.pos[3 * v + a];
-        nrm[3 * (int64_t)o + a] = w.nrm[3 * v + a];
+        pos[3 * (int64_t)o + a] = w.pos[3 * (int64_t)v + a];
+        nrm[3 * (int64_t)o + a] = w.nrm[3 * (int64_t)v + a];
     }
 }
 __global__ void kAssignHalfedges(SplitWork w, const int* __restrict__ app) {

@@ -91,6 +91,8 @@ CONFIGS = {
     "blobs129_refine4": ("129^3 fp32 grid, 64 Gaussian blobs (sigma 3-12), trilinearly refined x4 "
                          "to 513^3 samples = 512^3 cells, iso 0.4",
                          lambda seed=2: gaussian_blobs(129, 64, (3.0, 12.0), seed), 0.4, 3, False),
+    "noise513": ("513^3 fp32 iid uniform[0,1] noise (512^3 cells), iso 0.5: the noise grid at the headline size",
+                 lambda seed=5: uniform_noise(513, seed), 0.5, 0, False),
     "sphere128_sdf": ("128^3 fp32 signed distance to a sphere of radius 40 cells, iso 0, surface iteration off "
                       "(the differentiable form)",
                       lambda seed=0: sphere_sdf(128, 40.0, seed), 0.0, 0, False),

@@ -74,3 +74,30 @@ def test_noise_256_deterministic_and_consistent():
     dest = he[he[:, 2], 0]
     sym = ok & (he[np.where(ok, t, 0), 3] == np.arange(H))
     assert np.all(he[t[sym], 0] == dest[sym])
+
+
+def test_noise513_same_mesh_on_a_reused_context():
+    """The 512^3-cell noise grid (26 M non-manifold faces in the splitter's
+    working copies, whose partner slots then pass 2^31 entries): a second run
+    on the same context, whose buffers hold the first run's data, gives the
+    same mesh, and the repair ends without device-side anomalies."""
+    import torch
+    free, total = torch.cuda.mem_get_info()
+    if total < 200e9:
+        pytest.skip("needs a device with 200 GB or more")
+    from manifolddmc_gb300.workloads import CONFIGS
+    desc, gen, iso, r, pad = CONFIGS["noise513"]
+    grid = mdmc.UniformGrid(gen(), [513, 513, 513])
+    dmc = mdmc.DualMarchingCubes()
+    dmc.run(iso, grid)
+    first = {k: v.clone() for k, v in dmc.device_arrays().items()}
+    s0 = (dmc.stats.num_non_manifold_vertices, int(dmc.mesh.num_vertices), int(dmc.mesh.num_faces))
+    assert dmc.stats.anomalies == 0 and dmc.stats.split_iterations >= 1
+    dmc.run(iso, grid)
+    s1 = (dmc.stats.num_non_manifold_vertices, int(dmc.mesh.num_vertices), int(dmc.mesh.num_faces))
+    assert s0 == s1 and dmc.stats.anomalies == 0
+    second = dmc.device_arrays()
+    for k in first:
+        assert torch.equal(first[k], second[k]), k
+    del first, second, dmc
+    torch.cuda.empty_cache()
