@@ -82,9 +82,12 @@ __global__ void __launch_bounds__(256) kCoarseMayCross(const float* __restrict__
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool may = false;
     if (i < numCells) {
-        const int x = (int)(i % (cX - 1));
-        const int y = (int)((i / (cX - 1)) % (cY - 1));
-        const int z = (int)(i / ((int64_t)(cX - 1) * (cY - 1)));
+        // fewer than 2^32 coarse cells: 32-bit division
+        const uint32_t iu = (uint32_t)i, ncx = (uint32_t)(cX - 1), ncy = (uint32_t)(cY - 1);
+        const uint32_t row = iu / ncx;
+        const int x = (int)(iu - row * ncx);
+        const int y = (int)(row % ncy);
+        const int z = (int)(row / ncy);
         float lo = INFINITY, hi = -INFINITY, mag = 0.f;
         bool nan = false;
 #pragma unroll
@@ -415,9 +418,12 @@ __global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g
             if (lane == 0) atomicOr(status, kStatusBadIndex);
             continue;
         }
-        const int mx = (int)(ci % (g.cX - 1));
-        const int my = (int)((ci / (g.cX - 1)) % (g.cY - 1));
-        const int mz = (int)(ci / ((int64_t)(g.cX - 1) * (g.cY - 1)));
+        // coarse cells number fewer than 2^32 (refined grids have fewer samples)
+        const uint32_t cu = (uint32_t)ci, ncx = (uint32_t)(g.cX - 1), ncy = (uint32_t)(g.cY - 1);
+        const uint32_t crow = cu / ncx;
+        const int mx = (int)(cu - crow * ncx);
+        const int my = (int)(crow % ncy);
+        const int mz = (int)(crow / ncy);
         const int xs = blockStart(g, mx), xe = blockEnd(g, mx, g.X, g.cX);
         const int ys = blockStart(g, my), ye = blockEnd(g, my, g.Y, g.cY);
         const int zs = blockStart(g, mz), ze = blockEnd(g, mz, g.Z, g.cZ);
@@ -693,8 +699,8 @@ __global__ void kScatterCells(const uint32_t* __restrict__ mask, const int* __re
     if (w >= numWords) return;
     uint32_t m = mask[w];
     if (!m) return;
-    const int row = (int)(w / W);
-    const int x0 = (int)(w - (int64_t)row * W) * 32;
+    const uint32_t row = (uint32_t)w / (uint32_t)W;  // fewer than 2^32 words
+    const int x0 = (int)((uint32_t)w - row * (uint32_t)W) * 32;
     const int y = row % (Y - 1), z = row / (Y - 1);
     const uint32_t base = (uint32_t)(((size_t)z * Y + y) * X + x0);
     int j = first[w];
@@ -718,8 +724,8 @@ struct CellScatter {
     __device__ __forceinline__ void operator()(int64_t w, int first) const {
         uint32_t m = mask[w];
         if (!m) return;
-        const int row = (int)(w / W);
-        const int x0 = (int)(w - (int64_t)row * W) * 32;
+        const uint32_t row = (uint32_t)w / (uint32_t)W;  // fewer than 2^32 words
+        const int x0 = (int)((uint32_t)w - row * (uint32_t)W) * 32;
         const int y = row % (Y - 1), z = row / (Y - 1);
         const uint32_t base = (uint32_t)(((size_t)z * Y + y) * X + x0);
         int64_t j = first;

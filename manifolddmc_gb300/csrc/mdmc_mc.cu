@@ -94,7 +94,7 @@ __global__ void kMCScatterEdges(const uint32_t* __restrict__ edgeMask, const int
     if (w >= numWords) return;
     uint32_t m = edgeMask[w];
     if (!m) return;
-    const int64_t row = w / W3;
+    const int64_t row = (uint32_t)w / (uint32_t)W3;  // fewer than 2^32 words
     const int b0 = (int)(w - row * W3) * 32;
     int j = first[w];
     while (m) {
