@@ -344,8 +344,33 @@ __device__ __forceinline__ void orActive(uint32_t* mask, int W, int Y, bool acti
 // 75 distinct y-lerps are computed once and the 125 z-lerps finish them, each
 // with the operations and operands at() uses.  Returns false (nothing
 // written) when the block's coarse indices do not lie within a 3x3x3 range.
-__device__ bool blockSamples5(const RefinedView& g, int xs, int ys, int zs, int lane, float* __restrict__ buf,
-                              float* __restrict__ sc, int* __restrict__ ax, float* __restrict__ ad) {
+// the lane's element coordinates in the three stages (the same for every
+// block): x-lerp i = lane + 32u -> (kx, ry, rz); y-lerp -> (kx, ky, rz);
+// sample -> (kx, ky, kz); packed 4 bits each, 0xFFF past the end
+struct SeparableLanes {
+    uint16_t xl[2], yl[3], s[4];
+    __device__ __forceinline__ explicit SeparableLanes(int lane) {
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+            const int i = lane + 32 * u;
+            xl[u] = i < 45 ? (uint16_t)((i % 5) | (((i / 5) % 3) << 4) | ((i / 15) << 8)) : 0xFFF;
+        }
+#pragma unroll
+        for (int u = 0; u < 3; ++u) {
+            const int i = lane + 32 * u;
+            yl[u] = i < 75 ? (uint16_t)((i % 5) | (((i / 5) % 5) << 4) | ((i / 25) << 8)) : 0xFFF;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int i = lane + 32 * u;
+            s[u] = i < 125 ? (uint16_t)((i % 5) | (((i / 5) % 5) << 4) | ((i / 25) << 8)) : 0xFFF;
+        }
+    }
+};
+
+__device__ bool blockSamples5(const RefinedView& g, int xs, int ys, int zs, int lane, const SeparableLanes& sl,
+                              float* __restrict__ buf, float* __restrict__ sc, int* __restrict__ ax,
+                              float* __restrict__ ad) {
     int i0 = 0, i1 = 0;
     float d = 0.f;
     if (lane < 15) {
@@ -377,30 +402,39 @@ __device__ bool blockSamples5(const RefinedView& g, int xs, int ys, int zs, int 
     __syncwarp();
     float* xl = sc + 27;  // [rz][ry][kx], 45
     float* yl = sc + 72;  // [rz][ky][kx], 75
-    for (int i = lane; i < 45; i += 32) {
-        const int kx = i % 5, ry = (i / 5) % 3, rz = i / 15;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+        const int c = sl.xl[u];
+        if (c == 0xFFF) continue;
+        const int kx = c & 15, ry = (c >> 4) & 15, rz = c >> 8;
         const float s0 = sc[rz * 9 + ry * 3 + ax[kx]], s1 = sc[rz * 9 + ry * 3 + ax[15 + kx]];
-        xl[i] = s0 + ad[kx] * (s1 - s0);
+        xl[lane + 32 * u] = s0 + ad[kx] * (s1 - s0);
     }
     __syncwarp();
-    for (int i = lane; i < 75; i += 32) {
-        const int kx = i % 5, ky = (i / 5) % 5, rz = i / 25;
+#pragma unroll
+    for (int u = 0; u < 3; ++u) {
+        const int c = sl.yl[u];
+        if (c == 0xFFF) continue;
+        const int kx = c & 15, ky = (c >> 4) & 15, rz = c >> 8;
         const float dy = ad[5 + ky];
         const float a = xl[rz * 15 + ax[5 + ky] * 5 + kx], bb = xl[rz * 15 + ax[20 + ky] * 5 + kx];
-        yl[i] = (1.f - dy) * a + dy * bb;
+        yl[lane + 32 * u] = (1.f - dy) * a + dy * bb;
     }
     __syncwarp();
-    for (int i = lane; i < 125; i += 32) {
-        const int kx = i % 5, ky = (i / 5) % 5, kz = i / 25;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int c = sl.s[u];
+        if (c == 0xFFF) continue;
+        const int kx = c & 15, ky = (c >> 4) & 15, kz = c >> 8;
         const float dz = ad[10 + kz];
         const float lo = yl[ax[10 + kz] * 25 + ky * 5 + kx], hi = yl[ax[25 + kz] * 25 + ky * 5 + kx];
-        buf[i] = (1.f - dz) * lo + dz * hi;
+        buf[lane + 32 * u] = (1.f - dz) * lo + dz * hi;
     }
     __syncwarp();
     return true;
 }
 
-__global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g, float iso, const uint32_t* __restrict__ list,
+__global__ void __launch_bounds__(32 * kBlockMaskWarps, 4) kBlockMask(RefinedView g, float iso, const uint32_t* __restrict__ list,
                                                                  const unsigned long long* listCount,
                                                                  uint32_t* __restrict__ mask, int W, uint32_t* status) {
     __shared__ float samples[kBlockMaskWarps][kBlockSamplesMax];
@@ -409,6 +443,7 @@ __global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g
     __shared__ float sepFrac[kBlockMaskWarps][15];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     float* buf = samples[warp];
+    const SeparableLanes sl(lane);
     const int64_t count = (int64_t)*listCount;
     const int64_t nc = (int64_t)(g.cX - 1) * (g.cY - 1) * (g.cZ - 1);
     for (int64_t li = (int64_t)blockIdx.x * kBlockMaskWarps + warp; li < count;
@@ -437,7 +472,7 @@ __global__ void __launch_bounds__(32 * kBlockMaskWarps) kBlockMask(RefinedView g
             // the standard block of a x4 refinement: 125 samples and 64 cells
             // with compile-time strides; the 4 cells of a row lie in one mask
             // word and occupy 4 aligned lanes, OR-ed by two shuffles
-            if (!blockSamples5(g, xs, ys, zs, lane, buf, sepSamples[warp], sepIndex[warp], sepFrac[warp])) {
+            if (!blockSamples5(g, xs, ys, zs, lane, sl, buf, sepSamples[warp], sepIndex[warp], sepFrac[warp])) {
                 float v[4];
 #pragma unroll
                 for (int u = 0; u < 4; ++u) {
