@@ -434,22 +434,25 @@ __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restri
 // (the reference's sort + unique) equals "halfedges named as key by some
 // halfedge, per origin".  No sort is needed.  Only the halfedges of vertices
 // the single walk did not settle.
+// (a grid-stride loop over a fixed grid: when no vertex is unsettled, which
+// is the common case, each block reads the counter once and leaves)
 __global__ void kFanKeys(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ slow,
                          const unsigned long long* slowCount, uint8_t* __restrict__ isKey, uint32_t* status) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= md.H || *slowCount == 0) return;
-    const int v = he[h].x;
-    if (!inb(v, md.V) || !slow[v]) return;
-    const int k = min(h, min(fanWalk(he, h, true, md.H, status), fanWalk(he, h, false, md.H, status)));
-    isKey[k] = 1;
+    if (*slowCount == 0) return;
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < md.H; h += gridDim.x * blockDim.x) {
+        const int v = he[h].x;
+        if (!inb(v, md.V) || !slow[v]) continue;
+        const int k = min(h, min(fanWalk(he, h, true, md.H, status), fanWalk(he, h, false, md.H, status)));
+        isKey[k] = 1;
+    }
 }
 
 __global__ void kFanCount(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ slow,
                           const unsigned long long* slowCount, const uint8_t* __restrict__ isKey,
                           int* __restrict__ fans, uint32_t* status) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= md.H || *slowCount == 0) return;
-    if (isKey[h]) {
+    if (*slowCount == 0) return;
+    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < md.H; h += gridDim.x * blockDim.x) {
+        if (!isKey[h]) continue;
         const int v = he[h].x;
         if (inb(v, md.V)) {
             if (slow[v]) atomicAdd(&fans[v], 1);
@@ -494,9 +497,10 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
     }
     if (md.H > 0) {
         countLaunch();
-        kFanKeys<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, slow, &ctr->slowFans, isKey, status);
+        const int blocks = std::min((md.H + 255) / 256, 152 * 8);
+        kFanKeys<<<blocks, 256, 0, s>>>(he, md, slow, &ctr->slowFans, isKey, status);
         countLaunch();
-        kFanCount<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, slow, &ctr->slowFans, isKey, fans, status);
+        kFanCount<<<blocks, 256, 0, s>>>(he, md, slow, &ctr->slowFans, isKey, fans, status);
     }
     if (md.V > 0) {
         countLaunch();
