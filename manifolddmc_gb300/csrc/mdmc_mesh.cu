@@ -360,7 +360,7 @@ __global__ void kVertexStar(const int4* __restrict__ he, MeshDims md, int* __res
 // per-halfedge walks and is counted.  Also turns "no outgoing halfedge" into -1.
 __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restrict__ vertexHE,
                          const int* __restrict__ deg, int* __restrict__ fans, uint8_t* __restrict__ slow,
-                         unsigned long long* slowCount) {
+                         uint8_t* __restrict__ vflags, unsigned long long* slowCount) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     bool isSlow = false;
     if (v < md.V) {
@@ -369,6 +369,7 @@ __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restri
             vertexHE[v] = -1;
             fans[v] = 0;
             slow[v] = 0;
+            vflags[v] &= (uint8_t)~MDMC_VERTEX_MULTIPLE_FANS;
         } else {
             const int start = vertexHE[v];
             bool ok = inb(start, md.H) && d <= 1024;
@@ -423,6 +424,8 @@ __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restri
             fans[v] = ok ? 1 : 0;
             slow[v] = ok ? 0 : 1;
             isSlow = !ok;
+            // one fan: not a non-manifold vertex (the slow ones are flagged by kFanFlags)
+            if (ok) vflags[v] &= (uint8_t)~MDMC_VERTEX_MULTIPLE_FANS;
         }
     }
     const unsigned b = __ballot_sync(0xffffffffu, isSlow);
@@ -462,14 +465,18 @@ __global__ void kFanCount(const int4* __restrict__ he, MeshDims md, const uint8_
     }
 }
 
-__global__ void kFanFlags(const int* __restrict__ fans, uint8_t* __restrict__ vflags, int numVertices, DevCounters* ctr) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+// the vertices the single walk did not settle (kFanFast flagged the others;
+// a grid-stride loop that leaves at once when there are none)
+__global__ void kFanFlags(const int* __restrict__ fans, const uint8_t* __restrict__ slow, uint8_t* __restrict__ vflags,
+                          int numVertices, DevCounters* ctr) {
+    if (ctr->slowFans == 0) return;
     int nm = 0;
-    if (v < numVertices) {
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < numVertices; v += gridDim.x * blockDim.x) {
+        if (!slow[v]) continue;
         uint8_t f = vflags[v];
         if (fans[v] > 1) {
             f |= MDMC_VERTEX_MULTIPLE_FANS;
-            nm = 1;
+            ++nm;
         } else {
             f &= (uint8_t)~MDMC_VERTEX_MULTIPLE_FANS;
         }
@@ -493,7 +500,7 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
                       int* fans, uint8_t* vflags, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
     if (md.V > 0) {
         countLaunch();
-        kFanFast<<<(md.V + 255) / 256, 256, 0, s>>>(he, md, vertexHE, deg, fans, slow, &ctr->slowFans);
+        kFanFast<<<(md.V + 255) / 256, 256, 0, s>>>(he, md, vertexHE, deg, fans, slow, vflags, &ctr->slowFans);
     }
     if (md.H > 0) {
         countLaunch();
@@ -504,7 +511,7 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
     }
     if (md.V > 0) {
         countLaunch();
-        kFanFlags<<<(md.V + 255) / 256, 256, 0, s>>>(fans, vflags, md.V, ctr);
+        kFanFlags<<<std::min((md.V + 255) / 256, 152 * 8), 256, 0, s>>>(fans, slow, vflags, md.V, ctr);
     }
 }
 
