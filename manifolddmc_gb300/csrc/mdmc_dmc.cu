@@ -1322,10 +1322,25 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
             }
         }
     }
-    blockAddTo(&ctr->edges, nE);
-    blockAddTo(&ctr->edges3, nE3);
-    blockAddTo(&ctr->edges4, nE4);
-    for (int k = 1; k <= 4; ++k) blockAddTo(&ctr->quadsNM[k], nmEdges == k ? 1 : 0);
+    // the seven counters packed into one word for one warp reduction: edges
+    // (<= 4 per quad) in 16 bits, the others (<= 4, <= 1 per quad) in 8 bits
+    unsigned long long packed = (unsigned long long)nE | ((unsigned long long)nE3 << 16) |
+                                ((unsigned long long)nE4 << 24);
+#pragma unroll
+    for (int k = 1; k <= 4; ++k) packed |= (unsigned long long)(nmEdges == k ? 1 : 0) << (24 + 8 * k);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) packed += __shfl_down_sync(0xffffffffu, packed, o);
+    if ((threadIdx.x & 31) == 0 && packed) {
+        const unsigned long long e = packed & 0xFFFFu, e3 = (packed >> 16) & 0xFFu, e4 = (packed >> 24) & 0xFFu;
+        if (e) atomicAdd(&ctr->edges, e);
+        if (e3) atomicAdd(&ctr->edges3, e3);
+        if (e4) atomicAdd(&ctr->edges4, e4);
+#pragma unroll
+        for (int k = 1; k <= 4; ++k) {
+            const unsigned long long qk = (packed >> (24 + 8 * k)) & 0xFFu;
+            if (qk) atomicAdd(&ctr->quadsNM[k], qk);
+        }
+    }
 }
 
 void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, const uint32_t* cellMask,

@@ -25,6 +25,17 @@ __device__ __forceinline__ void orVertexFlag(uint8_t* flags, int v, uint32_t bit
     atomicOr(reinterpret_cast<uint32_t*>(flags) + (v >> 2), bits << ((v & 3) * 8));
 }
 
+// warp-wide sum added to *dst by lane 0 when non-zero (every lane of the warp
+// must call it); no block barrier, so warps of uneven length do not wait for
+// one another
+template <typename T>
+__device__ __forceinline__ void warpAddTo(unsigned long long* dst, T v) {
+    unsigned long long w = (unsigned long long)v;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+    if ((threadIdx.x & 31) == 0 && w) atomicAdd(dst, w);
+}
+
 template <typename T>
 __device__ __forceinline__ void blockAddTo(unsigned long long* dst, T v) {
     __shared__ unsigned long long acc;

@@ -136,9 +136,9 @@ __global__ void kEdgeBuckets(int4* __restrict__ he, MeshDims md, const int* __re
             }
         }
     }
-    blockAddTo(&ctr->edges, nE);
-    blockAddTo(&ctr->edges3, nE3);
-    blockAddTo(&ctr->edges4, nE4);
+    warpAddTo(&ctr->edges, nE);
+    warpAddTo(&ctr->edges3, nE3);
+    warpAddTo(&ctr->edges4, nE4);
 }
 
 void launchDegree(const int4* he, MeshDims md, int* deg, uint32_t* status, cudaStream_t s) {
@@ -545,7 +545,8 @@ __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__
             atomicOr(&ctr->status, kStatusBadIndex);
         }
     }
-    for (int k = 1; k <= 4; ++k) blockAddTo(&ctr->quadsNM[k], cnt == k ? 1 : 0);
+#pragma unroll
+    for (int k = 1; k <= 4; ++k) warpAddTo(&ctr->quadsNM[k], cnt == k ? 1 : 0);
 }
 
 __global__ void kVertexHalfedgeFix(int* vertexHE, int numVertices) {
