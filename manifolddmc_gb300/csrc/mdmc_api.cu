@@ -968,7 +968,6 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)Vd));
     MDMC_CHECK(c, c->degree.ensure(sizeof(int) * (size_t)Vd));
     MDMC_CHECK(c, cudaMemsetAsync(c->vertexHE.p, 0x7F, sizeof(int) * (size_t)Vd, s));
-    MDMC_CHECK(c, cudaMemsetAsync(c->degree.p, 0, sizeof(int) * (size_t)Vd, s));
 
     // mapQuadrilaterals + collectHalfedgeElements, and the halfedge mesh's
     // twins and flags (HalfedgeMesh::initialize) in the same pass
@@ -985,7 +984,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
                     c->cellFirst.as<int>(), X, Y, Z, W, c->he.as<int4>(), c->faceFirst.as<int>(),
                     c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(),
                     c->nmList.as<int4>(), (int)(Q + 1), (int)Q, (int)Vd, c->quads.as<int4>(), c->vertexHE.as<int>(),
-                    c->degree.as<int>(), ctr, (int)q0, (int)q1, s);
+                    ctr, (int)q0, (int)q1, s);
         if (early && (st = earlyCopyFaces(c, q0, q1, s)) != MDMC_OK) return st;
     }
     c->earlyFaces = early;
@@ -993,7 +992,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     // vertex positions and normals (sliceP's vertex part)
     cudaEventRecord(c->kev[10], s);
     launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), (int)A, (int)Vd,
-                   c->pos.as<float>(), c->nrm.as<float>(), status, s);
+                   c->pos.as<float>(), c->nrm.as<float>(), c->degree.as<int>(), status, s);
     cudaEventRecord(c->kev[11], s);
     if (early && (st = earlyCopyVertices(c, s)) != MDMC_OK) return st;
     MDMC_CHECK(c, cudaGetLastError());

@@ -907,7 +907,8 @@ template <class View>
 __global__ void __launch_bounds__(128, MDMC_VERTICES_MIN_BLOCKS) kVertices(View g, float iso, int surfaceIteration,
                                                  const ActiveCell* __restrict__ act, int numActive,
                                                  int numVertices, float* __restrict__ pos,
-                                                 float* __restrict__ nrm, uint32_t* status) {
+                                                 float* __restrict__ nrm, int* __restrict__ degree,
+                                                 uint32_t* status) {
     __shared__ uint64_t table[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kContourTable[i];
     __syncthreads();
@@ -934,9 +935,20 @@ __global__ void __launch_bounds__(128, MDMC_VERTICES_MIN_BLOCKS) kVertices(View 
     for (int t = 0; t < n; ++t) {
         const int csz = nib(c, t);
         F3 q = f3(0.f, 0.f, 0.f);
+        int deg = 0;  // quads around the vertex: contour edges inside the grid's interior
         for (int k = 0; k < csz; ++k) {
             const int e = (int)((c >> (16 + 4 * (before + k))) & 0xF);
             const int a0 = edgeV0(e), a1 = edgeV1(e);
+            {
+                // the edge's start point; its quad exists when all four cells
+                // around the edge do (the owner test of the quad pass)
+                const int ea = edgeAxis(e);
+                const int gx = x + (a0 & 1), gy = y + ((a0 >> 1) & 1), gz = z + ((a0 >> 2) & 1);
+                deg += ((ea == 0 || (gx >= 1 && gx <= g.X - 2)) && (ea == 1 || (gy >= 1 && gy <= g.Y - 2)) &&
+                        (ea == 2 || (gz >= 1 && gz <= g.Z - 2)))
+                           ? 1
+                           : 0;
+            }
             const float w = (iso - s[a0]) / (s[a1] - s[a0]);
             // computeLocalCoordinateOffset (:176-200): the edge's axis gets the
             // crossing, the other two axes corner a0's coordinate
@@ -959,20 +971,21 @@ __global__ void __launch_bounds__(128, MDMC_VERTICES_MIN_BLOCKS) kVertices(View 
         nrm[3 * vi] = nm.x;
         nrm[3 * vi + 1] = nm.y;
         nrm[3 * vi + 2] = nm.z;
+        degree[vi] = deg;
     }
 }
 
 void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, int numActive,
-                    int numVertices, float* pos, float* nrm, uint32_t* status, cudaStream_t s) {
+                    int numVertices, float* pos, float* nrm, int* degree, uint32_t* status, cudaStream_t s) {
     if (numActive <= 0) return;
     countLaunch();
     const unsigned blocks = (unsigned)((numActive + 127) / 128);
     if (g.refined)
         kVertices<RefinedView><<<blocks, 128, 0, s>>>(g.ref, iso, surfaceIteration, act, numActive, numVertices, pos, nrm,
-                                                      status);
+                                                      degree, status);
     else
         kVertices<PlainView><<<blocks, 128, 0, s>>>(g.plain, iso, surfaceIteration, act, numActive, numVertices, pos, nrm,
-                                                    status);
+                                                    degree, status);
 }
 
 // ---------------------------------------------------------------------------
@@ -1040,7 +1053,7 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
                                               int* __restrict__ faceFirst, uint16_t* __restrict__ faceAttr,
                                               uint8_t* vflags, uint32_t* __restrict__ heValence4,
                                               int4* __restrict__ nmList, int nmCapacity, int numQuads, int numVertices,
-                                              int4* __restrict__ quadsOut, int* vertexHE, int* degree,
+                                              int4* __restrict__ quadsOut, int* vertexHE,
                                               DevCounters* ctr, int qBegin, int qEnd) {
     const int q = qBegin + blockIdx.x * blockDim.x + threadIdx.x;
     int nE = 0, nE3 = 0, nE4 = 0;
@@ -1317,7 +1330,6 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
                 for (int hi = 0; hi < 4; ++hi) {
                     nmEdges += ((valences >> (8 * hi)) & 0xFFu) > 2 ? 1 : 0;
                     atomicMin(&vertexHE[quadV[hi]], h0 + hi);
-                    atomicAdd(&degree[quadV[hi]], 1);
                 }
             }
         }
@@ -1346,7 +1358,7 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
 void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, const uint32_t* cellMask,
                  const int* cellFirst, int X, int Y, int Z, int W, int4* he, int* faceFirst, uint16_t* faceAttr,
                  uint8_t* vflags, uint8_t* heValence, int4* nmList, int nmCapacity, int numQuads, int numVertices,
-                 int4* quadsOut, int* vertexHE, int* degree, DevCounters* ctr, int qBegin, int qEnd, cudaStream_t s) {
+                 int4* quadsOut, int* vertexHE, DevCounters* ctr, int qBegin, int qEnd, cudaStream_t s) {
     if (qEnd <= qBegin) return;
     countLaunch();
     CellIndex ix;
@@ -1358,7 +1370,7 @@ void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, con
     ix.W = W;
     kQuads<<<(qEnd - qBegin + 255) / 256, 256, 0, s>>>(act, quadOwner, numActive, ix, he, faceFirst, faceAttr, vflags,
                                                         reinterpret_cast<uint32_t*>(heValence), nmList, nmCapacity,
-                                                        numQuads, numVertices, quadsOut, vertexHE, degree, ctr, qBegin,
+                                                        numQuads, numVertices, quadsOut, vertexHE, ctr, qBegin,
                                                         qEnd);
 }
 

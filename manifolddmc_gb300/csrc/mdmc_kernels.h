@@ -132,11 +132,11 @@ void launchMCTriangles(const uint32_t* cellIds, const uint8_t* cases, const int*
 void launchFinishCells(ActiveCell* act, const int2* offsets, int numActive, int X, int Y, int* quadOwner, int numQuads,
                        uint32_t* status, cudaStream_t s);
 void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, int numActive,
-                    int numVertices, float* pos, float* nrm, uint32_t* status, cudaStream_t s);
+                    int numVertices, float* pos, float* nrm, int* degree, uint32_t* status, cudaStream_t s);
 void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, const uint32_t* cellMask,
                  const int* cellFirst, int X, int Y, int Z, int W, int4* he, int* faceFirst, uint16_t* faceAttr,
                  uint8_t* vflags, uint8_t* heValence, int4* nmList, int nmCapacity, int numQuads, int numVertices,
-                 int4* quadsOut, int* vertexHE, int* degree, DevCounters* ctr, int qBegin, int qEnd,
+                 int4* quadsOut, int* vertexHE, DevCounters* ctr, int qBegin, int qEnd,
                  cudaStream_t s);
 void launchVertexHalfedgeFix(int* vertexHE, int numVertices, cudaStream_t s);
 
