@@ -36,6 +36,21 @@ __device__ __forceinline__ void warpAddTo(unsigned long long* dst, T v) {
     if ((threadIdx.x & 31) == 0 && w) atomicAdd(dst, w);
 }
 
+// Counters packed into one word (16 bits each, sums per block below 2^16),
+// added over the block with two barriers; thread 0 then passes the block's
+// packed total to add(total).  Every thread of the block must call it.
+template <class Add>
+__device__ __forceinline__ void blockAddPacked(unsigned long long packed, Add add) {
+    __shared__ unsigned long long acc;
+    if (threadIdx.x == 0) acc = 0;
+    __syncthreads();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) packed += __shfl_down_sync(0xffffffffu, packed, o);
+    if ((threadIdx.x & 31) == 0 && packed) atomicAdd(&acc, packed);
+    __syncthreads();
+    if (threadIdx.x == 0 && acc) add(acc);
+}
+
 template <typename T>
 __device__ __forceinline__ void blockAddTo(unsigned long long* dst, T v) {
     __shared__ unsigned long long acc;

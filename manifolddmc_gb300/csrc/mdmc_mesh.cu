@@ -136,9 +136,13 @@ __global__ void kEdgeBuckets(int4* __restrict__ he, MeshDims md, const int* __re
             }
         }
     }
-    warpAddTo(&ctr->edges, nE);
-    warpAddTo(&ctr->edges3, nE3);
-    warpAddTo(&ctr->edges4, nE4);
+    // one block reduction for the three counters (each <= 1 per halfedge)
+    blockAddPacked((unsigned long long)nE | ((unsigned long long)nE3 << 16) | ((unsigned long long)nE4 << 32),
+                   [&](unsigned long long t) {
+                       if (t & 0xFFFFu) atomicAdd(&ctr->edges, t & 0xFFFFu);
+                       if ((t >> 16) & 0xFFFFu) atomicAdd(&ctr->edges3, (t >> 16) & 0xFFFFu);
+                       if ((t >> 32) & 0xFFFFu) atomicAdd(&ctr->edges4, (t >> 32) & 0xFFFFu);
+                   });
 }
 
 void launchDegree(const int4* he, MeshDims md, int* deg, uint32_t* status, cudaStream_t s) {
@@ -545,8 +549,12 @@ __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__
             atomicOr(&ctr->status, kStatusBadIndex);
         }
     }
+    // quads with 1..4 edges of more than two faces, 16 bits each
+    blockAddPacked(cnt >= 1 && cnt <= 4 ? 1ull << (16 * (cnt - 1)) : 0ull, [&](unsigned long long t) {
 #pragma unroll
-    for (int k = 1; k <= 4; ++k) warpAddTo(&ctr->quadsNM[k], cnt == k ? 1 : 0);
+        for (int k = 1; k <= 4; ++k)
+            if ((t >> (16 * (k - 1))) & 0xFFFFu) atomicAdd(&ctr->quadsNM[k], (t >> (16 * (k - 1))) & 0xFFFFu);
+    });
 }
 
 __global__ void kVertexHalfedgeFix(int* vertexHE, int numVertices) {
