@@ -549,7 +549,7 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         MDMC_CHECK(c, c->nrm.grow(sizeof(float) * 3 * (size_t)V2, sizeof(float) * 3 * (size_t)c->V, s));
         MDMC_CHECK(c, c->vflags.grow(roundUp((size_t)V2, 4), (size_t)c->V, s));
         MDMC_CHECK(c, c->appParent.grow(sizeof(int) * (size_t)std::max<int64_t>(V2 - c->dmcV, 1),
-                                        sizeof(int) * (size_t)(c->V - c->dmcV), s));
+                                        sizeof(int) * (size_t)std::max<int64_t>(c->V - c->dmcV, 0), s));
         SplitWork wb = w;
         wb.appParent = c->appParent.as<int>();
         MDMC_CHECK(c, c->he.grow(sizeof(int4) * (size_t)H2, sizeof(int4) * (size_t)c->H, s));

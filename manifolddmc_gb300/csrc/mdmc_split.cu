@@ -433,7 +433,9 @@ __global__ void kCopyBackVertices(SplitWork w, const int* __restrict__ app, int 
         // the DMC vertex it descends from (parents of earlier appends resolved)
         const int p = w.origV[v];
         const int parent = !inb(p, w.V) ? -1 : (p < w.dmcV ? p : w.appParent[p - w.dmcV]);
-        if (inb(o - w.dmcV, V2 - w.dmcV)) w.appParent[o - w.dmcV] = parent;
+        // (after a simplification the mesh has fewer vertices than the DMC
+        // produced and no appended vertex has a slot here)
+        if (o >= w.dmcV && o < V2) w.appParent[o - w.dmcV] = parent;
     }
     if (!inb(o, V2)) {
         atomicOr(status, kStatusBadIndex);

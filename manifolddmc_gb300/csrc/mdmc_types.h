@@ -26,7 +26,10 @@ enum : uint32_t {
 };
 
 // unsigned range check used before every data-dependent access
-__host__ __device__ __forceinline__ bool inb(long long i, long long n) { return (unsigned long long)i < (unsigned long long)n; }
+// 0 <= i < n (false for every i when n <= 0)
+__host__ __device__ __forceinline__ bool inb(long long i, long long n) {
+    return (unsigned long long)i < (unsigned long long)(n > 0 ? n : 0);
+}
 
 // current element counts of the mesh arrays
 struct MeshDims {
