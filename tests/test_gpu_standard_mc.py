@@ -9,6 +9,7 @@ import pytest
 
 import manifolddmc_gb300 as mdmc
 from _support import golden_grid, oracle_refine, oracle_standard_mc, reference_goldens, sphere_sdf
+from test_gpu_parity import same_floats
 
 pytestmark = pytest.mark.gpu
 
@@ -42,8 +43,8 @@ def _compare(vol, dims, origin, spacing, iso, refinement, pad):
     rpos, rnrm, rtri = oracle_standard_mc(g, d, o, s, iso)
     assert pos.shape == rpos.shape and tri.shape == rtri.shape
     assert len(tri) > 0
-    assert np.array_equal(pos.view(np.uint32), rpos.view(np.uint32))
-    assert np.array_equal(nrm.view(np.uint32), rnrm.view(np.uint32))
+    assert same_floats(pos, rpos)
+    assert same_floats(nrm, rnrm)
     assert np.array_equal(tri, rtri)
     return dmc, pos, nrm, tri
 

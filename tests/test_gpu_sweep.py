@@ -34,12 +34,12 @@ def _field(rng, kind, dims):
     raise ValueError(kind)
 
 
-def _cases(n=36, seed=20261203):
+def _cases(n=160, seed=20261203):
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n):
         kind = ["noise", "quantised", "blobs", "sdf"][i % 4]
-        dims = [int(rng.integers(2, 19)) for _ in range(3)]
+        dims = [int(rng.integers(2, 19 if i < 120 else 31)) for _ in range(3)]
         if i % 9 == 0:
             dims[int(rng.integers(0, 3))] = 2
         refinement = int(rng.choice([0, 0, 1, 2, 3]))
@@ -49,6 +49,8 @@ def _cases(n=36, seed=20261203):
         if i % 6 == 5:
             opts.update(simplify_3x3y_color=int(rng.integers(0, 2)), simplify_3x3y_old=int(rng.integers(0, 2)),
                         simplify_3333=int(rng.integers(0, 2)))
+        if i % 7 == 3:
+            opts["splitting_step"] = int(rng.choice([0, 1, 2, 3, 4, 5, 6, 100]))
         iso = {"noise": 0.5, "quantised": 0.5, "blobs": float(rng.uniform(0.2, 0.7)), "sdf": 0.0}[kind]
         out.append(("%02d_%s_%dx%dx%d_r%d%s" % (i, kind, dims[0], dims[1], dims[2], refinement, "_pad" if pad else ""),
                     kind, dims, int(rng.integers(0, 2**31)), iso, refinement, pad, opts))
