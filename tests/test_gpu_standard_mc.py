@@ -34,7 +34,7 @@ CASES = [
 ]
 
 
-def _compare(vol, dims, origin, spacing, iso, refinement, pad):
+def _compare(vol, dims, origin, spacing, iso, refinement, pad, nonempty=True):
     grid = mdmc.UniformGrid(np.ascontiguousarray(vol, np.float32).reshape(dims[2], dims[1], dims[0]), dims, origin,
                             spacing, refinement, pad)
     dmc = mdmc.DualMarchingCubes()
@@ -42,7 +42,7 @@ def _compare(vol, dims, origin, spacing, iso, refinement, pad):
     g, d, o, s = oracle_refine(vol.reshape(-1), dims, origin, spacing, refinement, pad)
     rpos, rnrm, rtri = oracle_standard_mc(g, d, o, s, iso)
     assert pos.shape == rpos.shape and tri.shape == rtri.shape
-    assert len(tri) > 0
+    assert len(tri) > 0 or not nonempty
     assert same_floats(pos, rpos)
     assert same_floats(nrm, rnrm)
     assert np.array_equal(tri, rtri)
@@ -93,3 +93,31 @@ def test_standard_mc_without_crossing_is_empty():
     dmc = mdmc.DualMarchingCubes()
     pos, nrm, tri = dmc.run_standard_mc(0.5, grid)
     assert pos.shape == (0, 3) and tri.shape == (0, 3)
+
+
+def _sweep_cases(n=40, seed=77):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        dims = [int(rng.integers(2, 24)) for _ in range(3)]
+        kind = ["noise", "quantised", "blobs"][i % 3]
+        out.append(("%02d_%s_%dx%dx%d" % (i, kind, *dims), kind, dims, int(rng.integers(0, 2**31)),
+                    int(rng.choice([0, 0, 1, 3])), bool(rng.integers(0, 2))))
+    return out
+
+
+SWEEP = _sweep_cases()
+
+
+@pytest.mark.parametrize("name,kind,dims,seed,refinement,pad", SWEEP, ids=[c[0] for c in SWEEP])
+def test_standard_mc_sweep(name, kind, dims, seed, refinement, pad):
+    rng = np.random.default_rng(seed)
+    shape = (dims[2], dims[1], dims[0])
+    if kind == "noise":
+        vol = rng.random(shape, dtype=np.float32)
+    elif kind == "quantised":
+        vol = (rng.integers(0, 5, shape) * 0.25).astype(np.float32)
+    else:
+        vol = _blobs(max(dims), 3, seed % 1000)[:dims[2], :dims[1], :dims[0]].copy()
+    _compare(vol, dims, np.array([-0.5, 1.0, 0.25], np.float32), np.array([0.75, 0.5, 1.25], np.float32),
+             0.5 if kind != "blobs" else 0.3, refinement, pad, nonempty=False)
