@@ -677,6 +677,7 @@ mdmc_status finishActive(mdmc_context* c, const GridDesc& g, int W, int64_t numW
     const int X = geom.X, Y = geom.Y, Z = geom.Z;
     const int64_t cells = (X > 1 && Y > 1 && Z > 1) ? (int64_t)(X - 1) * (Y - 1) * (Z - 1) : 0;
     if (A < 0 || A > cells) return fail(c, MDMC_ERROR_CUDA, "inconsistent cell count from the mask pass");
+    if (A > 0x7FFFFFFF) return fail(c, MDMC_ERROR_LIMIT, "more than 2^31 active cells");
     if (A > idsCapacity) {
         MDMC_CHECK(c, c->cellIds.ensure(sizeof(uint32_t) * (size_t)A));
         launchScatterCells(c->cellMask.as<uint32_t>(), c->cellFirst.as<int>(), numWords, W, X, Y,
