@@ -73,3 +73,25 @@ def test_run_to_host_rejects_small_host_arrays_and_keeps_the_device_mesh():
     ref = mdmc.DualMarchingCubes()
     ref.run(0.5, grid)
     _equal(dmc.get_halfedge_mesh(), ref.get_halfedge_mesh())
+
+
+def test_run_to_host_with_pageable_arrays_and_null_fields():
+    """Plain (pageable) numpy arrays work too, and a NULL array is skipped."""
+    import ctypes
+    vol = _blobs(20, 4, 56)
+    grid = mdmc.UniformGrid(vol, [20, 20, 20], refinement=1)
+    ref = mdmc.DualMarchingCubes()
+    ref.run(0.4, grid)
+    expect = ref.get_halfedge_mesh()
+    V, F = len(expect.positions), len(expect.quads)
+    arrays = {"positions": np.zeros((V, 3), np.float32), "normals": None, "quads": np.zeros((F, 4), np.int32),
+              "halfedges": np.zeros((4 * F, 4), np.int32), "face_first_halfedge": np.zeros(F, np.int32),
+              "face_attributes": None, "vertex_halfedge": np.zeros(V, np.int32), "vertex_flags": np.zeros(V, np.uint8)}
+    host = mdmc.HostMeshArrays(V, F, *[a.ctypes.data if a is not None else None for a in arrays.values()])
+    dmc = mdmc.DualMarchingCubes()
+    st = dmc._ctx.lib.mdmc_run_to_host(dmc._ctx.handle, ctypes.byref(grid.grid), ctypes.c_float(0.4),
+                                       ctypes.byref(host), ctypes.byref(dmc.mesh), ctypes.byref(dmc.stats), None)
+    assert st == 0
+    for k, a in arrays.items():
+        if a is not None:
+            assert np.array_equal(a, getattr(expect, k)), k
