@@ -327,8 +327,9 @@ MDMC_API mdmc_status mdmc_backward(mdmc_context* context, const float* dl_dposit
  * stats[i], either array may be NULL) stay valid until the next batch run, and
  * mdmc_batch_context(batch, i) gives its context for the other getters.  The
  * pipelines run concurrently on `streams` worker streams; streams = 0 lets the
- * first mdmc_run_batch time 1, 2, 4, 8 and 16 workers on its grids and keep the
- * fastest (mdmc_batch_streams reports the choice).  The call waits for the
+ * first mdmc_run_batch time 1, 2, 4, 8, 16 and 32 workers on its grids and keep the
+ * fastest (mdmc_batch_streams reports the choice); the largest grids start
+ * first.  The call waits for the
  * caller's stream (the grids' inputs) first and returns when every mesh is
  * complete.  Grids keep the options given at creation. */
 typedef struct mdmc_batch mdmc_batch;

@@ -4,7 +4,8 @@
 // the grids' pipelines concurrently: one context per grid slot (its buffers,
 // and the mesh it returns) and S worker threads, each with its own stream,
 // taking grids in turn.  S is chosen by timing the first batch with
-// S = 1, 2, 4, 8, 16 when the batch is created with streams = 0.
+// S = 1, 2, 4, 8, 16, 32 when the batch is created with streams = 0; the
+// largest grids are started first.
 // No counterpart in the reference (DualMarchingCubes::run takes one grid).
 #include <cuda_runtime.h>
 
@@ -57,11 +58,21 @@ mdmc_status runWith(mdmc_batch* b, int S, const mdmc_grid* grids, const float* i
                     mdmc_stats* stats) {
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return batchFail(b, MDMC_ERROR_NO_DEVICE, "no current device");
+    // largest grids first (cells as the work estimate), so that no large
+    // grid starts last and runs alone
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    auto cells = [&](int i) {
+        const int32_t* d = grids[i].dims;
+        return (d[0] > 1 && d[1] > 1 && d[2] > 1) ? (int64_t)(d[0] - 1) * (d[1] - 1) * (d[2] - 1) : (int64_t)0;
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return cells(a) > cells(c); });
     std::atomic<int> next{0};
     std::vector<mdmc_status> result(n, MDMC_OK);
     auto worker = [&](int w) {
         cudaSetDevice(device);
-        for (int i = next.fetch_add(1); i < n; i = next.fetch_add(1)) {
+        for (int k = next.fetch_add(1); k < n; k = next.fetch_add(1)) {
+            const int i = order[k];
             result[i] = mdmc_run(b->ctx[i], &grids[i], isos[i], meshes ? &meshes[i] : nullptr,
                                  stats ? &stats[i] : nullptr, b->stream[w]);
         }
@@ -121,10 +132,10 @@ mdmc_status mdmc_run_batch(mdmc_batch* b, const mdmc_grid* grids, const float* i
     }
     if (b->streams == 0) {
         // pick the worker count by timing this batch once per candidate
-        const int candidates[] = {1, 2, 4, 8, 16};
+        const int candidates[] = {1, 2, 4, 8, 16, 32};
         double best = 1e30;
         int bestS = 1;
-        if ((st = ensureStreams(b, 16)) != MDMC_OK) return st;
+        if ((st = ensureStreams(b, 32)) != MDMC_OK) return st;
         for (int S : candidates) {
             if (S > std::max(n, 1)) break;
             const auto t0 = std::chrono::steady_clock::now();
