@@ -424,6 +424,89 @@ struct CellStencil<RefinedView> {
     }
 };
 
+// The stencil of a refined grid whose refinement factor f is at least 3,
+// evaluated separably.  Along an axis the four stencil positions span at most
+// three refined steps, so their coarse index pairs are (b + e, b + e + 1)
+// with e in {0, 1} for one base b: the stencil reads a 3x3x3 block of coarse
+// samples.  RefinedView::at's trilinear interpolation takes x-lerps along
+// coarse rows, then y-lerps of two x-lerps, then the z-lerp of two y-lerps;
+// here each x-lerp (position i, coarse row) and y-lerp (positions i, j,
+// coarse layer) is computed once from the 27 loaded samples, with the
+// operands and operations at() uses, and the 32 samples the corners and
+// gradients read are finished by their z-lerps.  Valid when e stays in
+// {0, 1}: f >= 3 and the rounding of i / f never reaches the next integer,
+// which holds for f and the refined dims up to 2^20 (sepStencilApplies).
+struct SepStencil {
+    float v[4][4][4];  // [k][j][i]; only samples with at most one index outside 1..2 are set
+    __device__ __forceinline__ float at(int i, int j, int k) const { return v[k][j][i]; }
+
+    // the axis's coarse rows (element offsets) and per-position fraction and row step
+    __device__ __forceinline__ static void axis(const RefinedView& g, int p, int n, int cn, uint32_t stride,
+                                                uint32_t o[3], float d[4], bool up[4]) {
+        int b = 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int u = g.unpad(min(max(p - 1 + j, 0), n - 1), n);
+            const float q = g.divf(u);
+            const int m = (int)floorf(q);
+            d[j] = q - (float)m;
+            if (j == 0) b = m;
+            up[j] = m != b;
+        }
+#pragma unroll
+        for (int r = 0; r < 3; ++r) o[r] = (uint32_t)min(max(b + r, 0), cn - 1) * stride;
+    }
+
+    __device__ __forceinline__ SepStencil(const RefinedView& g, int x, int y, int z) {
+        uint32_t ox[3], oy[3], oz[3];
+        float dx[4], dy[4], dz[4];
+        bool ux[4], uy[4], uz[4];
+        axis(g, x, g.X, g.cX, 1u, ox, dx, ux);
+        axis(g, y, g.Y, g.cY, (uint32_t)g.cX, oy, dy, uy);
+        axis(g, z, g.Z, g.cZ, (uint32_t)g.cX * (uint32_t)g.cY, oz, dz, uz);
+        float yl[3][4][4];  // [coarse layer][j][i]
+#pragma unroll
+        for (int rz = 0; rz < 3; ++rz) {
+            float xl[3][4];  // [coarse row][i]
+#pragma unroll
+            for (int ry = 0; ry < 3; ++ry) {
+                const float* row = g.c + (oz[rz] + oy[ry]);
+                const float c0 = __ldg(row + ox[0]), c1 = __ldg(row + ox[1]), c2 = __ldg(row + ox[2]);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float s0 = ux[i] ? c1 : c0, s1 = ux[i] ? c2 : c1;
+                    xl[ry][i] = s0 + dx[i] * (s1 - s0);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    if ((i == 0 || i == 3) && (j == 0 || j == 3)) continue;
+                    const float a = uy[j] ? xl[1][i] : xl[0][i], b = uy[j] ? xl[2][i] : xl[1][i];
+                    yl[rz][j][i] = (1.f - dy[j]) * a + dy[j] * b;
+                }
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int outside = (i == 0 || i == 3) + (j == 0 || j == 3) + (k == 0 || k == 3);
+                    if (outside > 1) continue;
+                    const float lo = uz[k] ? yl[1][j][i] : yl[0][j][i], hi = uz[k] ? yl[2][j][i] : yl[1][j][i];
+                    v[k][j][i] = (1.f - dz[k]) * lo + dz[k] * hi;
+                }
+    }
+};
+
+// host-side test of SepStencil's condition for a refined grid
+__host__ __device__ __forceinline__ bool sepStencilApplies(int refinement, int X, int Y, int Z) {
+    const int lim = 1 << 20;
+    return refinement >= 2 && refinement < lim && X <= lim && Y <= lim && Z <= lim;
+}
+
 // the cell's corner values (corner i at stencil (1 + bit0, 1 + bit1, 1 + bit2))
 template <class St>
 __device__ __forceinline__ void stencilCorners(const St& st, float s[8]) {
@@ -431,10 +514,22 @@ __device__ __forceinline__ void stencilCorners(const St& st, float s[8]) {
     for (int i = 0; i < 8; ++i) s[i] = st.at(1 + (i & 1), 1 + ((i >> 1) & 1), 1 + ((i >> 2) & 1));
 }
 
+// 1 / d when d is a power of two whose reciprocal is a normal float.  Then
+// x / d and x * (1 / d) are the correctly rounded values of the same real
+// number and agree bit for bit.
+__device__ __forceinline__ bool pow2Reciprocal(float d, float& inv) {
+    const uint32_t b = __float_as_uint(d);
+    const uint32_t e = (b >> 23) & 0xFFu;
+    inv = __uint_as_float((b & 0x80000000u) | (((254u - e) & 0xFFu) << 23));
+    return (b & 0x7FFFFFu) == 0u && e >= 1u && e <= 253u;
+}
+
 // cornerGradients from the stencil: along axis a, corner i's neighbour is
-// the stencil sample one step outside the cell (index 0 below, 3 above)
+// the stencil sample one step outside the cell (index 0 below, 3 above).
+// The division by the spacing is a multiplication when that is exact.
 template <class St>
 __device__ __forceinline__ void stencilGradients(const St& st, const float s[8], F3 dl, F3 out[8]) {
+    F3 half[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         const int bx = i & 1, by = (i >> 1) & 1, bz = (i >> 2) & 1;
@@ -443,7 +538,16 @@ __device__ __forceinline__ void stencilGradients(const St& st, const float s[8],
         const float nz = st.at(1 + bx, 1 + by, bz ? 3 : 0);
         const F3 gr = f3(bx ? nx - s[i ^ 1] : s[i ^ 1] - nx, by ? ny - s[i ^ 2] : s[i ^ 2] - ny,
                          bz ? nz - s[i ^ 4] : s[i ^ 4] - nz);
-        out[i] = (0.5f * gr) / dl;
+        half[i] = 0.5f * gr;
+    }
+    F3 inv;
+    const bool exact = pow2Reciprocal(dl.x, inv.x) & pow2Reciprocal(dl.y, inv.y) & pow2Reciprocal(dl.z, inv.z);
+    if (exact) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) out[i] = half[i] * inv;
+    } else {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) out[i] = half[i] / dl;
     }
 }
 

@@ -903,7 +903,7 @@ void launchFinishCells(ActiveCell* act, const int2* offsets, int numActive, int 
 #ifndef MDMC_VERTICES_MIN_BLOCKS
 #define MDMC_VERTICES_MIN_BLOCKS 5  // 96 registers: 0.19 ms instead of 0.22 ms at 114 on the 512^3-cell blobs
 #endif
-template <class View>
+template <class View, class Stencil>
 __global__ void __launch_bounds__(128, MDMC_VERTICES_MIN_BLOCKS) kVertices(View g, float iso, int surfaceIteration,
                                                  const ActiveCell* __restrict__ act, int numActive,
                                                  int numVertices, float* __restrict__ pos,
@@ -920,7 +920,7 @@ __global__ void __launch_bounds__(128, MDMC_VERTICES_MIN_BLOCKS) kVertices(View 
     const int z = (int)(rec.cell / ((uint32_t)g.X * (uint32_t)g.Y));
     const int vb = rec.pad;  // first vertex id
     const int cs = (int)(rec.info & 255u);
-    const CellStencil<View> st(g, x, y, z);
+    const Stencil st(g, x, y, z);
     float s[8];
     stencilCorners(st, s);
     const uint64_t c = cellContours(cs, s, iso, table);
@@ -980,12 +980,15 @@ void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const Ac
     if (numActive <= 0) return;
     countLaunch();
     const unsigned blocks = (unsigned)((numActive + 127) / 128);
-    if (g.refined)
-        kVertices<RefinedView><<<blocks, 128, 0, s>>>(g.ref, iso, surfaceIteration, act, numActive, numVertices, pos, nrm,
-                                                      degree, status);
+    if (g.refined && sepStencilApplies(g.ref.r, g.ref.X, g.ref.Y, g.ref.Z))
+        kVertices<RefinedView, SepStencil><<<blocks, 128, 0, s>>>(g.ref, iso, surfaceIteration, act, numActive,
+                                                                  numVertices, pos, nrm, degree, status);
+    else if (g.refined)
+        kVertices<RefinedView, CellStencil<RefinedView>><<<blocks, 128, 0, s>>>(
+            g.ref, iso, surfaceIteration, act, numActive, numVertices, pos, nrm, degree, status);
     else
-        kVertices<PlainView><<<blocks, 128, 0, s>>>(g.plain, iso, surfaceIteration, act, numActive, numVertices, pos, nrm,
-                                                    degree, status);
+        kVertices<PlainView, CellStencil<PlainView>><<<blocks, 128, 0, s>>>(
+            g.plain, iso, surfaceIteration, act, numActive, numVertices, pos, nrm, degree, status);
 }
 
 // ---------------------------------------------------------------------------
