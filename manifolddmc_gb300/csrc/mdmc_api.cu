@@ -132,6 +132,7 @@ struct mdmc_context {
     cudaEvent_t ev[6] = {};
     // per-kernel events: refine, count, emit, quads, table, vertices (begin/end each)
     cudaEvent_t kev[12] = {};
+    cudaEvent_t countsEv = nullptr;  // the DMC counts have reached the host
     float msRefine = 0.f;
     bool haveMesh = false;
     mdmc_stats stats;
@@ -724,7 +725,8 @@ mdmc_status mdmc_create(mdmc_context** context, const mdmc_options* options) {
     for (auto& e : c->ev) cudaEventCreate(&e);
     for (auto& e : c->kev) cudaEventCreate(&e);
     for (auto& e : c->copyEv) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
-    if (cudaStreamCreateWithFlags(&c->copyStream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaEventCreateWithFlags(&c->countsEv, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->copyStream, cudaStreamNonBlocking) != cudaSuccess) {
         mdmc_destroy(c);
         return MDMC_ERROR_CUDA;
     }
@@ -748,6 +750,7 @@ void mdmc_destroy(mdmc_context* c) {
         if (e) cudaEventDestroy(e);
     for (auto& e : c->copyEv)
         if (e) cudaEventDestroy(e);
+    if (c->countsEv) cudaEventDestroy(c->countsEv);
     if (c->copyStream) cudaStreamDestroy(c->copyStream);
     if (c->hostCounters) cudaFreeHost(c->hostCounters);
     if (c->hostInts) cudaFreeHost(c->hostInts);
@@ -917,10 +920,37 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     launchGatherCounts(numActiveDev, capA > 0 ? c->cellCounts.as<int2>() : nullptr, capA > 0 ? (int)capA : -1,
                        ctr->gathered, s);
     cudaEventRecord(c->kev[5], s);
+    MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, ctr->gathered, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    MDMC_CHECK(c, cudaEventRecord(c->countsEv, s));
+    // Before the counts reach the host: when the arrays of an earlier run are
+    // large enough, the cell offsets and the vertex pass run on the device's
+    // counts, so that the device works while the host waits for them.  Not for
+    // runs into host arrays, whose quad pass goes first to start the copies.
+    DeviceCounts spec{ctr->gathered, 0, 0, 0};
+    bool speculated = false;
+    if (!c->hostOut && capA > 0) {
+        const int64_t capV = std::min<int64_t>(std::min(c->pos.bytes, c->nrm.bytes) / (3 * sizeof(float)),
+                                               (int64_t)(c->degree.bytes / sizeof(int)));
+        const int64_t capQ = (int64_t)(c->quadOwner.bytes / sizeof(int));
+        if (capV > 0 && capQ > 0) {
+            spec.capA = (int)capA;
+            spec.capV = (int)std::min<int64_t>(capV, 0x7FFFFFFF);
+            spec.capQ = (int)std::min<int64_t>(capQ, 0x7FFFFFFF);
+            launchFinishCells(c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), spec.capA, X, Y,
+                              c->quadOwner.as<int>(), spec.capQ, status, s, &spec);
+            cudaEventRecord(c->kev[10], s);
+            launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), spec.capA,
+                           spec.capV, c->pos.as<float>(), c->nrm.as<float>(), c->degree.as<int>(), status, s, &spec);
+            cudaEventRecord(c->kev[11], s);
+            speculated = true;
+        }
+    }
     MDMC_CHECK(c, cudaGetLastError());
-    if ((st = readInts(c, ctr->gathered, 3, s)) != MDMC_OK) return st;
+    MDMC_CHECK(c, cudaEventSynchronize(c->countsEv));  // the counts, not the passes behind them
     const int64_t A = c->hostInts[0];
     int64_t Vd = c->hostInts[1], Q = c->hostInts[2];
+    // the passes above did their work exactly when the counts fit
+    const bool aheadDone = speculated && spec.fits(A, Vd, Q);
     if ((st = finishActive(c, g, W, numWords, A, idsCapacity, s)) != MDMC_OK) return st;
     c->stats.num_active_cells = A;
     if (A > capA || capA == 0) {
@@ -973,8 +1003,9 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     // mapQuadrilaterals + collectHalfedgeElements, and the halfedge mesh's
     // twins and flags (HalfedgeMesh::initialize) in the same pass
     cudaEventRecord(c->kev[6], s);
-    launchFinishCells(c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A, X, Y, c->quadOwner.as<int>(), (int)Q,
-                      status, s);
+    if (!aheadDone)
+        launchFinishCells(c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A, X, Y, c->quadOwner.as<int>(),
+                          (int)Q, status, s);
     // with host arrays to fill, the quads go in ranges, each copied out as
     // soon as it is written, so that the copies start early
     const bool early = earlyFits(c);
@@ -991,10 +1022,12 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->earlyFaces = early;
     cudaEventRecord(c->kev[7], s);
     // vertex positions and normals (sliceP's vertex part)
-    cudaEventRecord(c->kev[10], s);
-    launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), (int)A, (int)Vd,
-                   c->pos.as<float>(), c->nrm.as<float>(), c->degree.as<int>(), status, s);
-    cudaEventRecord(c->kev[11], s);
+    if (!aheadDone) {
+        cudaEventRecord(c->kev[10], s);
+        launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), (int)A, (int)Vd,
+                       c->pos.as<float>(), c->nrm.as<float>(), c->degree.as<int>(), status, s);
+        cudaEventRecord(c->kev[11], s);
+    }
     if (early && (st = earlyCopyVertices(c, s)) != MDMC_OK) return st;
     MDMC_CHECK(c, cudaGetLastError());
     cudaEventRecord(c->ev[1], s);

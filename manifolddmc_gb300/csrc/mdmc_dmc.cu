@@ -873,7 +873,13 @@ void launchGatherCounts(const int* numActiveDev, const int2* counts, int capacit
 // Each active cell's first vertex id (kept in its record's spare word) and
 // first quad id, and the owner of every quad.
 __global__ void kFinishCells(ActiveCell* __restrict__ act, const int2* __restrict__ offsets, int numActive, int X, int Y,
-                             int* __restrict__ quadOwner, int numQuads, uint32_t* status) {
+                             int* __restrict__ quadOwner, int numQuads, uint32_t* status, DeviceCounts counts) {
+    if (counts.dev) {
+        int a, v, q;
+        if (!counts.fits(a, v, q)) return;
+        numActive = a;
+        numQuads = q;
+    }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= numActive) return;
     const ActiveCell rec = act[i];
@@ -890,10 +896,11 @@ __global__ void kFinishCells(ActiveCell* __restrict__ act, const int2* __restric
 }
 
 void launchFinishCells(ActiveCell* act, const int2* offsets, int numActive, int X, int Y, int* quadOwner, int numQuads,
-                       uint32_t* status, cudaStream_t s) {
+                       uint32_t* status, cudaStream_t s, const DeviceCounts* counts) {
     if (numActive <= 0) return;
     countLaunch();
-    kFinishCells<<<(numActive + 255) / 256, 256, 0, s>>>(act, offsets, numActive, X, Y, quadOwner, numQuads, status);
+    kFinishCells<<<(numActive + 255) / 256, 256, 0, s>>>(act, offsets, numActive, X, Y, quadOwner, numQuads, status,
+                                                         counts ? *counts : DeviceCounts{nullptr, 0, 0, 0});
 }
 
 // ---------------------------------------------------------------------------
@@ -908,7 +915,13 @@ __global__ void __launch_bounds__(128, MDMC_VERTICES_MIN_BLOCKS) kVertices(View 
                                                  const ActiveCell* __restrict__ act, int numActive,
                                                  int numVertices, float* __restrict__ pos,
                                                  float* __restrict__ nrm, int* __restrict__ degree,
-                                                 uint32_t* status) {
+                                                 uint32_t* status, DeviceCounts counts) {
+    if (counts.dev) {
+        int a, v, q;
+        if (!counts.fits(a, v, q)) return;
+        numActive = a;
+        numVertices = v;
+    }
     __shared__ uint64_t table[256];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kContourTable[i];
     __syncthreads();
@@ -976,19 +989,21 @@ __global__ void __launch_bounds__(128, MDMC_VERTICES_MIN_BLOCKS) kVertices(View 
 }
 
 void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, int numActive,
-                    int numVertices, float* pos, float* nrm, int* degree, uint32_t* status, cudaStream_t s) {
+                    int numVertices, float* pos, float* nrm, int* degree, uint32_t* status, cudaStream_t s,
+                    const DeviceCounts* counts) {
     if (numActive <= 0) return;
     countLaunch();
     const unsigned blocks = (unsigned)((numActive + 127) / 128);
+    const DeviceCounts dc = counts ? *counts : DeviceCounts{nullptr, 0, 0, 0};
     if (g.refined && sepStencilApplies(g.ref.r, g.ref.X, g.ref.Y, g.ref.Z))
         kVertices<RefinedView, SepStencil><<<blocks, 128, 0, s>>>(g.ref, iso, surfaceIteration, act, numActive,
-                                                                  numVertices, pos, nrm, degree, status);
+                                                                  numVertices, pos, nrm, degree, status, dc);
     else if (g.refined)
         kVertices<RefinedView, CellStencil<RefinedView>><<<blocks, 128, 0, s>>>(
-            g.ref, iso, surfaceIteration, act, numActive, numVertices, pos, nrm, degree, status);
+            g.ref, iso, surfaceIteration, act, numActive, numVertices, pos, nrm, degree, status, dc);
     else
         kVertices<PlainView, CellStencil<PlainView>><<<blocks, 128, 0, s>>>(
-            g.plain, iso, surfaceIteration, act, numActive, numVertices, pos, nrm, degree, status);
+            g.plain, iso, surfaceIteration, act, numActive, numVertices, pos, nrm, degree, status, dc);
 }
 
 // ---------------------------------------------------------------------------

@@ -144,10 +144,30 @@ void launchMCVertices(const GridDesc& g, float iso, const uint32_t* edgeIds, int
 void launchMCTriangles(const uint32_t* cellIds, const uint8_t* cases, const int* triOffset, int numActive, int X, int Y,
                        int W3, const uint32_t* edgeMask, const int* edgeFirst, int64_t numWords, int* tris,
                        int numTriangles, uint32_t* status, cudaStream_t s);
+// Counts a pass reads on the device, for launches made before the host has
+// read them back: dev -> {active cells, vertices, quads} (the gathered
+// counts), valid only when all three fit the capacities the launch covers.
+// The passes given one do nothing when the counts do not fit; the host, which
+// reads the same counts, then launches them again at the right size.
+struct DeviceCounts {
+    const int* dev;
+    int capA, capV, capQ;
+    __device__ __forceinline__ bool fits(int& a, int& v, int& q) const {
+        a = dev[0];
+        v = dev[1];
+        q = dev[2];
+        return a >= 0 && a <= capA && v >= 0 && v <= capV && q >= 0 && q <= capQ;
+    }
+    bool fits(int64_t a, int64_t v, int64_t q) const {
+        return a >= 0 && a <= capA && v >= 0 && v <= capV && q >= 0 && q <= capQ;
+    }
+};
+
 void launchFinishCells(ActiveCell* act, const int2* offsets, int numActive, int X, int Y, int* quadOwner, int numQuads,
-                       uint32_t* status, cudaStream_t s);
+                       uint32_t* status, cudaStream_t s, const DeviceCounts* counts = nullptr);
 void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, int numActive,
-                    int numVertices, float* pos, float* nrm, int* degree, uint32_t* status, cudaStream_t s);
+                    int numVertices, float* pos, float* nrm, int* degree, uint32_t* status, cudaStream_t s,
+                    const DeviceCounts* counts = nullptr);
 void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, const uint32_t* cellMask,
                  const int* cellFirst, int X, int Y, int Z, int W, int4* he, int* faceFirst, uint16_t* faceAttr,
                  uint8_t* vflags, uint8_t* heValence, int4* nmList, int nmCapacity, int numQuads, int numVertices,
