@@ -372,8 +372,9 @@ mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaSt
         MDMC_CHECK(c, cudaMemsetAsync(c->isKey.p, 0, (size_t)c->H, s));
         MDMC_CHECK(c, cudaMemsetAsync(&ctr->slowFans, 0, sizeof(unsigned long long), s));
         if (!starsDone) launchVertexStar(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), s);
-        launchDetectFans(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), c->slowFan.as<uint8_t>(),
-                         c->isKey.as<uint8_t>(), c->fans.as<int>(), c->vflags.as<uint8_t>(), ctr, status, s);
+        launchDetectFans(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), starsDone,
+                         c->slowFan.as<uint8_t>(), c->isKey.as<uint8_t>(), c->fans.as<int>(), c->vflags.as<uint8_t>(),
+                         ctr, status, s);
     }
     cudaEventRecord(c->ev[4], s);
     if (!starsDone)

@@ -89,17 +89,22 @@ __device__ __forceinline__ int faceCorner(int f, int i) {
     return (fc[f] >> (4 * i)) & 0xF;
 }
 
-// The reference takes the asymptotic-decider path for a case
-// (s_triangleAmbiguities == MC_AMBIGUOUS, D/DualMarchingCubes.cpp:301) exactly
-// when a face of the cell has the diagonal sign pattern, or when the inside
-// corners are just the two ends of one cell diagonal (or all but those two).
-__host__ __device__ inline bool caseIsAmbiguous(int c) {
+// a face of the cell has the diagonal sign pattern (four crossing edges)
+__host__ __device__ inline bool caseHasDiagonalFace(int c) {
     const unsigned short fc[6] = {0x3120, 0x6475, 0x1504, 0x7362, 0x2064, 0x7531};
     for (int f = 0; f < 6; ++f) {
         int m = 0;
         for (int i = 0; i < 4; ++i) m |= ((c >> ((fc[f] >> (4 * i)) & 0xF)) & 1) << i;
         if (m == 6 || m == 9) return true;
     }
+    return false;
+}
+// The reference takes the asymptotic-decider path for a case
+// (s_triangleAmbiguities == MC_AMBIGUOUS, D/DualMarchingCubes.cpp:301) exactly
+// when a face of the cell has the diagonal sign pattern, or when the inside
+// corners are just the two ends of one cell diagonal (or all but those two).
+__host__ __device__ inline bool caseIsAmbiguous(int c) {
+    if (caseHasDiagonalFace(c)) return true;
     for (int i = 0; i < 4; ++i) {
         int pair = (1 << i) | (1 << (7 - i));
         if (c == pair || c == (255 ^ pair)) return true;

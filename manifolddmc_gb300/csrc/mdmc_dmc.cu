@@ -944,11 +944,12 @@ __global__ void __launch_bounds__(128, MDMC_VERTICES_MIN_BLOCKS) kVertices(View 
     }
     F3 normals[8];
     stencilGradients(st, s, g.deltas(), normals);
+    const bool diagonalFace = caseHasDiagonalFace(cs);
     int before = 0;
     for (int t = 0; t < n; ++t) {
-        const int csz = nib(c, t);
         F3 q = f3(0.f, 0.f, 0.f);
         int deg = 0;  // quads around the vertex: contour edges inside the grid's interior
+        const int csz = nib(c, t);
         for (int k = 0; k < csz; ++k) {
             const int e = (int)((c >> (16 + 4 * (before + k))) & 0xF);
             const int a0 = edgeV0(e), a1 = edgeV1(e);
@@ -984,7 +985,7 @@ __global__ void __launch_bounds__(128, MDMC_VERTICES_MIN_BLOCKS) kVertices(View 
         nrm[3 * vi] = nm.x;
         nrm[3 * vi + 1] = nm.y;
         nrm[3 * vi + 2] = nm.z;
-        degree[vi] = deg;
+        degree[vi] = deg == csz && !diagonalFace ? deg : -deg;
     }
 }
 

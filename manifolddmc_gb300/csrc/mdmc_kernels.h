@@ -165,6 +165,9 @@ struct DeviceCounts {
 
 void launchFinishCells(ActiveCell* act, const int2* offsets, int numActive, int X, int Y, int* quadOwner, int numQuads,
                        uint32_t* status, cudaStream_t s, const DeviceCounts* counts = nullptr);
+// degree[v] = the number of quads around DMC vertex v, negated unless every
+// edge of its contour has a quad and no face of its cell has four crossing
+// edges (then its faces are known to form one fan; see kFanFast)
 void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, int numActive,
                     int numVertices, float* pos, float* nrm, int* degree, uint32_t* status, cudaStream_t s,
                     const DeviceCounts* counts = nullptr);
@@ -183,8 +186,10 @@ void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s);
 void launchReconnect(const GridDesc& g, float iso, const int4* nmList, const DevCounters* ctr,
                      int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s);
 void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cudaStream_t s);
-void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, uint8_t* slow, uint8_t* isKey,
-                      int* fans, uint8_t* vflags, DevCounters* ctr,
+// vertexPassDegrees: deg is the vertex pass's signed degree of the DMC mesh
+// (only the twin repair has run since); otherwise non-negative degrees
+void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, bool vertexPassDegrees,
+                      uint8_t* slow, uint8_t* isKey, int* fans, uint8_t* vflags, DevCounters* ctr,
                       uint32_t* status, cudaStream_t s);
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, int4* quads,
                   int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s);

@@ -362,16 +362,31 @@ __global__ void kVertexStar(const int4* __restrict__ he, MeshDims md, int* __res
 // same fan, its key is the fan's smallest id, and the vertex has one fan with
 // no limit hit.  Every other vertex (non-manifold, asymmetric twins) takes the
 // per-halfedge walks and is counted.  Also turns "no outgoing halfedge" into -1.
+//
+// With the vertex pass's degrees (the DMC mesh after the twin repair), a
+// positive degree needs no walk.  It says that every edge of the vertex's
+// contour has a quad and that no face of its cell has four crossing edges.
+// The vertex's faces are then the quads of its contour's edges; two
+// consecutive ones share the mesh edge to the vertex of the neighbour across
+// the cell face of their contour segment, that face has no other crossing
+// edge, so exactly these two halfedges hold the vertex pair (the pairs the
+// twin repair changes have four) and they are twins: the faces form one
+// closed fan.
 __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restrict__ vertexHE,
-                         const int* __restrict__ deg, int* __restrict__ fans, uint8_t* __restrict__ slow,
-                         uint8_t* __restrict__ vflags, unsigned long long* slowCount) {
+                         const int* __restrict__ deg, bool vertexPassDegrees, int* __restrict__ fans,
+                         uint8_t* __restrict__ slow, uint8_t* __restrict__ vflags, unsigned long long* slowCount) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     bool isSlow = false;
     if (v < md.V) {
-        const int d = deg[v];
+        const int ds = deg[v];
+        const int d = ds < 0 ? -ds : ds;
         if (d == 0) {
             vertexHE[v] = -1;
             fans[v] = 0;
+            slow[v] = 0;
+            vflags[v] &= (uint8_t)~MDMC_VERTEX_MULTIPLE_FANS;
+        } else if (vertexPassDegrees && ds > 0) {
+            fans[v] = 1;
             slow[v] = 0;
             vflags[v] &= (uint8_t)~MDMC_VERTEX_MULTIPLE_FANS;
         } else {
@@ -500,11 +515,13 @@ void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cuda
     }
 }
 
-void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, uint8_t* slow, uint8_t* isKey,
-                      int* fans, uint8_t* vflags, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
+void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, bool vertexPassDegrees,
+                      uint8_t* slow, uint8_t* isKey, int* fans, uint8_t* vflags, DevCounters* ctr, uint32_t* status,
+                      cudaStream_t s) {
     if (md.V > 0) {
         countLaunch();
-        kFanFast<<<(md.V + 255) / 256, 256, 0, s>>>(he, md, vertexHE, deg, fans, slow, vflags, &ctr->slowFans);
+        kFanFast<<<(md.V + 255) / 256, 256, 0, s>>>(he, md, vertexHE, deg, vertexPassDegrees, fans, slow, vflags,
+                                                    &ctr->slowFans);
     }
     if (md.H > 0) {
         countLaunch();
