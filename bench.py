@@ -42,7 +42,8 @@ L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 100 for this library, 10 CPU runs for --impl reference)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", default="blobs129_refine4")
@@ -52,7 +53,11 @@ def parse():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--fit", action="store_true",
                     help="also time 200 Adam steps of the sphere-to-torus fit (brute-force Chamfer in torch)")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:
+        # ~0.1 s of timed GPU work, long enough for the clock samples to land in it
+        args.steps = 100 if args.impl == "ours" else 10
+    return args
 
 
 def dist_env():
@@ -82,13 +87,20 @@ class ClockSampler:
         self.proc = None
         self.lines = []
 
+    INTERVAL_MS = 20
+
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.INTERVAL_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the timed steps start once the sampler is delivering
+            t0 = time.time()
+            while not self.lines and time.time() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.005)
+            self.first = len(self.lines)
         except Exception:
             self.proc = None
         return self
@@ -99,6 +111,10 @@ class ClockSampler:
 
     def __exit__(self, *exc):
         if self.proc is not None:
+            # one sample after the timed steps, so that they lie between samples
+            n, t0 = len(self.lines), time.time()
+            while len(self.lines) <= n and time.time() - t0 < 1.0 and self.proc.poll() is None:
+                time.sleep(0.002)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -122,7 +138,8 @@ class ClockSampler:
                     reasons.add(n)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm),
+                "window": "nvidia-smi every %d ms from just before to just after the timed steps" % self.INTERVAL_MS}
 
 
 def algorithmic_bytes(kernel, s):
@@ -200,13 +217,26 @@ def run_ours(args, rank, world, local):
             check(st)
 
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    for _ in range(max(args.warmup, 3)):
+    # warm-up: every kernel timed (two event records per kernel and run), for
+    # the per-kernel breakdown; the timed steps record only the dominant
+    # kernel's pair, for the roofline
+    kernels = ("refine", "count", "emit", "vertices", "quads")
+    check(lib.mdmc_set_kernel_timing(ctx, mdmc.TIME_ALL))
+    warm_ms = {k: [] for k in kernels}
+    for i in range(max(args.warmup, 3)):
+        flush.zero_()
         step()
-    torch.cuda.synchronize(dev)
+        torch.cuda.synchronize(dev)
+        if i:
+            for k in kernels:
+                warm_ms[k].append(getattr(stats, mdmc.KERNEL_TIMING[k][1]))
+    breakdown = {k: float(np.mean(v)) for k, v in warm_ms.items()}
+    dominant = max(breakdown, key=breakdown.get)
+    check(lib.mdmc_set_kernel_timing(ctx, mdmc.KERNEL_TIMING[dominant][0]))
     cells = (grid.dims[0] - 1) * (grid.dims[1] - 1) * (grid.dims[2] - 1)
     samples = grid.dims[0] * grid.dims[1] * grid.dims[2]
 
-    per_step, kernel_ms, launches = [], {k: [] for k in ("refine", "count", "emit", "vertices", "quads")}, 0
+    per_step, kernel_ms, launches = [], {dominant: []}, 0
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
@@ -220,9 +250,7 @@ def run_ours(args, rank, world, local):
             e1.record(stream)
             e1.synchronize()
             per_step.append(e0.elapsed_time(e1))
-            for k, f in (("refine", "ms_refine"), ("count", "ms_count"), ("emit", "ms_emit"),
-                         ("vertices", "ms_vertices"), ("quads", "ms_quads")):
-                kernel_ms[k].append(getattr(stats, f))
+            kernel_ms[dominant].append(getattr(stats, mdmc.KERNEL_TIMING[dominant][1]))
             launches += int(stats.kernel_launches)
     torch.cuda.synchronize(dev)
     if world > 1:
@@ -239,11 +267,10 @@ def run_ours(args, rank, world, local):
              "refined": bool(refine or pad),
              "active": int(stats.num_active_cells), "dmc_vertices": int(stats.num_dmc_vertices),
              "dmc_quads": int(stats.num_dmc_quads)}
-    kavg = {k: float(np.mean(v)) for k, v in kernel_ms.items()}
-    dominant = max(kavg, key=kavg.get)
+    dominant_ms = float(np.mean(kernel_ms[dominant]))
     peak, peak_kind = peaks()
     ab = algorithmic_bytes(dominant, sizes)
-    achieved = ab / (kavg[dominant] / 1e3) / 1e9
+    achieved = ab / (dominant_ms / 1e3) / 1e9
     traffic = None
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
@@ -253,13 +280,16 @@ def run_ours(args, rank, world, local):
             traffic = None
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "peak_kind": peak_kind, "traffic": traffic,
-                "algorithmic_bytes": ab, "kernel_ms": {k: round(v, 4) for k, v in kavg.items()},
+                "algorithmic_bytes": ab, "kernel_ms_timed": round(dominant_ms, 4),
+                "kernel_ms": {k: round(v, 4) for k, v in breakdown.items()},
+                "kernel_ms_source": "warm-up steps with every kernel timed (the timed steps time only the dominant one)",
                 "whole_step_bytes": survey_bytes(sizes),
                 "whole_step_gbs": round(survey_bytes(sizes) / (ms / 1e3) / 1e9, 1),
                 "whole_step_frac": round(survey_bytes(sizes) / (ms / 1e3) / 1e9 / peak, 4)}
 
     e2e = None
     if not args.no_e2e:
+        check(lib.mdmc_set_kernel_timing(ctx, 0))  # the user's call: no kernel timing
         host_in = torch.from_numpy(vol).pin_memory()
         V, F, H = int(mesh.num_vertices), int(mesh.num_faces), int(mesh.num_halfedges)
         bufs = {"positions": torch.empty((V, 3), dtype=torch.float32).pin_memory(),

@@ -135,7 +135,8 @@ typedef struct mdmc_stats {
     float ms_repair;
     float ms_detect;
     float ms_total;
-    /* per-kernel GPU times of the last run (CUDA events on the run's stream) */
+    /* per-kernel GPU times of the last run (CUDA events on the run's stream),
+     * for the kernels mdmc_set_kernel_timing selects; 0 for the others */
     float ms_refine;               /* grid refinement of the last mdmc_prepare_grid */
     float ms_count;                /* per-row counting pass over the grid */
     float ms_emit;                 /* active-cell compaction pass */
@@ -155,6 +156,20 @@ MDMC_API void mdmc_destroy(mdmc_context* context);
 /* the flag setters of DualMarchingCubes (renderImGui, DualMarchingCubes.cu:150-182;
  * setSplittingStep, DualMarchingCubes.h:143-145) */
 MDMC_API mdmc_status mdmc_set_options(mdmc_context* context, const mdmc_options* options);
+
+/* Per-kernel timing (no reference counterpart; the reference times stages).
+ * Each timed kernel costs its run two CUDA event records on the stream, about
+ * 3.5 us of GPU time on a GB300, so kernels are timed only when their bit is
+ * set: MDMC_TIME_* bits, default 0.  The stage times (ms_dmc .. ms_total) are
+ * always taken. */
+#define MDMC_TIME_REFINE 1u   /* ms_refine */
+#define MDMC_TIME_COUNT 2u    /* ms_count */
+#define MDMC_TIME_EMIT 4u     /* ms_emit */
+#define MDMC_TIME_QUADS 8u    /* ms_quads */
+#define MDMC_TIME_TABLE 16u   /* ms_table */
+#define MDMC_TIME_VERTICES 32u /* ms_vertices */
+#define MDMC_TIME_ALL 63u
+MDMC_API mdmc_status mdmc_set_kernel_timing(mdmc_context* context, uint32_t kernels);
 MDMC_API mdmc_status mdmc_get_options(const mdmc_context* context, mdmc_options* options);
 
 /* Reads a .bin volume (int32 dims[3], float32 spacing[3], uint16 samples)

@@ -126,6 +126,11 @@ class Stats(ctypes.Structure):
 STATUS = {0: "ok", 1: "invalid argument", 2: "cuda error", 3: "out of memory", 4: "device limit hit",
           5: "io error", 6: "no cuda device"}
 
+# kernels mdmc_set_kernel_timing can time (MDMC_TIME_* of mdmc.h) -> Stats field
+KERNEL_TIMING = {"refine": (1, "ms_refine"), "count": (2, "ms_count"), "emit": (4, "ms_emit"),
+                 "quads": (8, "ms_quads"), "table": (16, "ms_table"), "vertices": (32, "ms_vertices")}
+TIME_ALL = 63
+
 
 class MDMCError(RuntimeError):
     def __init__(self, status, message):
@@ -154,6 +159,7 @@ def library():
             "mdmc_create": (ctypes.c_int, [P, P]),
             "mdmc_destroy": (None, [P]),
             "mdmc_set_options": (ctypes.c_int, [P, P]),
+            "mdmc_set_kernel_timing": (ctypes.c_int, [P, ctypes.c_uint32]),
             "mdmc_get_options": (ctypes.c_int, [P, P]),
             "mdmc_read_bin": (ctypes.c_int, [ctypes.c_char_p, P, P, P, P]),
             "mdmc_prepare_grid": (ctypes.c_int, [P, P, ctypes.c_int, P, P, P, ctypes.c_int32, ctypes.c_int32, P, P]),
@@ -353,6 +359,12 @@ class DualMarchingCubes:
 
     def set_option(self, name, value):
         self._set(name, value)
+
+    def set_kernel_timing(self, kernels):
+        """Times the named kernels (keys of KERNEL_TIMING, or an MDMC_TIME_*
+        mask) in the following runs' stats; each costs two event records."""
+        mask = kernels if isinstance(kernels, int) else sum(KERNEL_TIMING[k][0] for k in kernels)
+        self._ctx.check(self._ctx.lib.mdmc_set_kernel_timing(self._ctx.handle, mask))
 
     def run(self, iso_value, grid, stream=None):
         """DualMarchingCubes::run, DualMarchingCubes.cu:220-289.  Returns the

@@ -132,6 +132,7 @@ struct mdmc_context {
     cudaEvent_t ev[6] = {};
     // per-kernel events: refine, count, emit, quads, table, vertices (begin/end each)
     cudaEvent_t kev[12] = {};
+    uint32_t kernelTiming = 0;  // MDMC_TIME_* bits: kernels whose event pairs are recorded
     cudaEvent_t countsEv = nullptr;  // the DMC counts have reached the host
     float msRefine = 0.f;
     bool haveMesh = false;
@@ -139,6 +140,12 @@ struct mdmc_context {
 };
 
 namespace {
+
+// kev[2k], kev[2k + 1] bracket timed kernel k (bit k of MDMC_TIME_*): an
+// event record costs the stream about 1.7 us, so only requested pairs are made
+inline void markKernel(mdmc_context* c, int e, cudaStream_t s) {
+    if ((c->kernelTiming >> (e >> 1)) & 1u) cudaEventRecord(c->kev[e], s);
+}
 
 mdmc_status fail(mdmc_context* c, mdmc_status st, const std::string& msg) {
     if (c) c->err = msg;
@@ -257,10 +264,10 @@ mdmc_status makeGridDesc(mdmc_context* c, const mdmc_grid* grid, float iso, Grid
         MDMC_CHECK(c, c->mayCross.ensure(sizeof(uint32_t) * (size_t)((cells + 31) / 32 + 1)));
         MDMC_CHECK(c, c->candidates.ensure(sizeof(uint32_t) * (size_t)cells));
         d.ref.mayCross = c->mayCross.as<uint32_t>();
-        cudaEventRecord(c->kev[0], s);
+        markKernel(c, 0, s);
         launchCoarseMayCross(d.ref, iso, c->mayCross.as<uint32_t>(), c->candidates.as<uint32_t>(),
                              &c->counters.as<DevCounters>()->candidates, s);
-        cudaEventRecord(c->kev[1], s);
+        markKernel(c, 1, s);
     }
     return MDMC_OK;
 }
@@ -653,7 +660,7 @@ mdmc_status markActive(mdmc_context* c, const GridDesc& g, float iso, int& W, in
     numWords = numRows * (int64_t)W;
     MDMC_CHECK(c, c->cellMask.ensure(sizeof(uint32_t) * (size_t)std::max<int64_t>(numWords, 1)));
     MDMC_CHECK(c, c->cellFirst.ensure(sizeof(int) * (size_t)(numWords + 1)));
-    cudaEventRecord(c->kev[2], s);
+    markKernel(c, 2, s);
     if (g.refined && numWords > 0) MDMC_CHECK(c, cudaMemsetAsync(c->cellMask.p, 0, sizeof(uint32_t) * (size_t)numWords, s));
     if (g.refined && g.ref.mayCross && 2 * (g.ref.r + 4) * (g.ref.r + 4) <= 512 && numWords > 0)
         launchBlockMask(g.ref, iso, c->candidates.as<uint32_t>(), &c->counters.as<DevCounters>()->candidates,
@@ -667,7 +674,7 @@ mdmc_status markActive(mdmc_context* c, const GridDesc& g, float iso, int& W, in
     if (!scanMaskScatter(c->cellMask.as<uint32_t>(), c->cellFirst.as<int>(), numWords, W, X, Y,
                          c->cellIds.as<uint32_t>(), idsCapacity, c->scanScratch.as<int>(), s))
         return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
-    cudaEventRecord(c->kev[3], s);
+    markKernel(c, 3, s);
     MDMC_CHECK(c, cudaGetLastError());
     return MDMC_OK;
 }
@@ -756,6 +763,12 @@ void mdmc_destroy(mdmc_context* c) {
     if (c->hostCounters) cudaFreeHost(c->hostCounters);
     if (c->hostInts) cudaFreeHost(c->hostInts);
     delete c;
+}
+
+mdmc_status mdmc_set_kernel_timing(mdmc_context* c, uint32_t kernels) {
+    if (!c || (kernels & ~(uint32_t)MDMC_TIME_ALL)) return MDMC_ERROR_INVALID_ARGUMENT;
+    c->kernelTiming = kernels;
+    return MDMC_OK;
 }
 
 mdmc_status mdmc_set_options(mdmc_context* c, const mdmc_options* options) {
@@ -887,8 +900,8 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, cudaMemsetAsync(ctr, 0, sizeof(DevCounters), s));
     const long long launches0 = g_kernelLaunches.load();
     cudaEventRecord(c->ev[0], s);
-    cudaEventRecord(c->kev[0], s);
-    cudaEventRecord(c->kev[1], s);
+    markKernel(c, 0, s);
+    markKernel(c, 1, s);
     GridDesc g;
     mdmc_status st0 = makeGridDesc(c, grid, iso, g, s);
     if (st0 != MDMC_OK) return st0;
@@ -909,7 +922,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     int64_t capA = std::min<int64_t>(idsCapacity, (int64_t)(c->act.bytes / sizeof(ActiveCell)));
     capA = std::min<int64_t>(capA, (int64_t)(c->cellCounts.bytes / sizeof(int2)) - 1);
     capA = std::max<int64_t>(std::min<int64_t>(capA, 0x7FFFFFFF), 0);
-    cudaEventRecord(c->kev[4], s);
+    markKernel(c, 4, s);
     if (capA > 0) {
         MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(capA)));
         launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)capA,
@@ -920,7 +933,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     }
     launchGatherCounts(numActiveDev, capA > 0 ? c->cellCounts.as<int2>() : nullptr, capA > 0 ? (int)capA : -1,
                        ctr->gathered, s);
-    cudaEventRecord(c->kev[5], s);
+    markKernel(c, 5, s);
     MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, ctr->gathered, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
     MDMC_CHECK(c, cudaEventRecord(c->countsEv, s));
     // Before the counts reach the host: when the arrays of an earlier run are
@@ -939,10 +952,10 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
             spec.capQ = (int)std::min<int64_t>(capQ, 0x7FFFFFFF);
             launchFinishCells(c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), spec.capA, X, Y,
                               c->quadOwner.as<int>(), spec.capQ, status, s, &spec);
-            cudaEventRecord(c->kev[10], s);
+            markKernel(c, 10, s);
             launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), spec.capA,
                            spec.capV, c->pos.as<float>(), c->nrm.as<float>(), c->degree.as<int>(), status, s, &spec);
-            cudaEventRecord(c->kev[11], s);
+            markKernel(c, 11, s);
             speculated = true;
         }
     }
@@ -1003,7 +1016,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
 
     // mapQuadrilaterals + collectHalfedgeElements, and the halfedge mesh's
     // twins and flags (HalfedgeMesh::initialize) in the same pass
-    cudaEventRecord(c->kev[6], s);
+    markKernel(c, 6, s);
     if (!aheadDone)
         launchFinishCells(c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A, X, Y, c->quadOwner.as<int>(),
                           (int)Q, status, s);
@@ -1021,24 +1034,24 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
         if (early && (st = earlyCopyFaces(c, q0, q1, s)) != MDMC_OK) return st;
     }
     c->earlyFaces = early;
-    cudaEventRecord(c->kev[7], s);
+    markKernel(c, 7, s);
     // vertex positions and normals (sliceP's vertex part)
     if (!aheadDone) {
-        cudaEventRecord(c->kev[10], s);
+        markKernel(c, 10, s);
         launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), (int)A, (int)Vd,
                        c->pos.as<float>(), c->nrm.as<float>(), c->degree.as<int>(), status, s);
-        cudaEventRecord(c->kev[11], s);
+        markKernel(c, 11, s);
     }
     if (early && (st = earlyCopyVertices(c, s)) != MDMC_OK) return st;
     MDMC_CHECK(c, cudaGetLastError());
     cudaEventRecord(c->ev[1], s);
-    cudaEventRecord(c->kev[8], s);
+    markKernel(c, 8, s);
     // runPostProcesses, D/DualMarchingCubes.cu:335-380: simplifications first
     if (c->opt.simplify_p3x3y_color && (st = runSimplification(c, 0, s)) != MDMC_OK) return st;
     if (c->opt.simplify_p3x3y_old && (st = runSimplification(c, 1, s)) != MDMC_OK) return st;
     if (c->opt.simplify_p3333 && (st = runSimplification(c, 2, s)) != MDMC_OK) return st;
     const MeshDims md0{(int)c->V, (int)c->F, (int)c->H};
-    cudaEventRecord(c->kev[9], s);
+    markKernel(c, 9, s);
     cudaEventRecord(c->ev[2], s);
 
     // ---- repair: fixManifoldTwins, then the splitter ---------------------------
@@ -1096,7 +1109,9 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->stats.ms_total = ms[4];
     float km[6] = {0, 0, 0, 0, 0, 0};
     for (int k = 0; k < 6; ++k)
-        if (cudaEventElapsedTime(&km[k], c->kev[2 * k], c->kev[2 * k + 1]) != cudaSuccess) km[k] = 0.f;
+        if (((c->kernelTiming >> k) & 1u) &&
+            cudaEventElapsedTime(&km[k], c->kev[2 * k], c->kev[2 * k + 1]) != cudaSuccess)
+            km[k] = 0.f;
     (void)cudaGetLastError();  // elapsed-time queries leave no error behind
     c->stats.ms_refine = km[0];
     c->stats.ms_count = km[1];

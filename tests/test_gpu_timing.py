@@ -1,0 +1,46 @@
+"""Per-kernel timing is opt-in (mdmc_set_kernel_timing): selected kernels get
+positive times, the others read 0, the stage times are always taken, and
+timing changes no result."""
+import numpy as np
+import pytest
+
+import manifolddmc_gb300 as mdmc
+from manifolddmc_gb300.workloads import CONFIGS
+
+pytestmark = pytest.mark.gpu
+
+
+def _grid():
+    desc, gen, iso, refine, pad = CONFIGS["blobs64_pad"]
+    vol = gen()
+    dims = [vol.shape[2], vol.shape[1], vol.shape[0]]
+    return mdmc.UniformGrid(vol, dims, refinement=refine, add_zero_boundary=pad), iso
+
+
+def test_kernel_timing_mask_selects_fields():
+    grid, iso = _grid()
+    dmc = mdmc.DualMarchingCubes()
+    stages = dmc.run(iso, grid)
+    assert stages["Total"] > 0 and stages["DMC"] > 0
+    for _, field in mdmc.KERNEL_TIMING.values():
+        assert getattr(dmc.stats, field) == 0.0
+    base = dmc.get_halfedge_mesh()
+
+    dmc.set_kernel_timing(["quads", "vertices"])
+    dmc.run(iso, grid)
+    assert dmc.stats.ms_quads > 0 and dmc.stats.ms_vertices > 0
+    assert dmc.stats.ms_count == 0.0 and dmc.stats.ms_emit == 0.0
+
+    dmc.set_kernel_timing(mdmc.TIME_ALL)
+    dmc.run(iso, grid)
+    for k in ("count", "emit", "quads", "vertices"):
+        assert getattr(dmc.stats, mdmc.KERNEL_TIMING[k][1]) > 0, k
+    timed = dmc.get_halfedge_mesh()
+    for name in ("positions", "quads", "halfedges", "vertex_flags"):
+        assert np.array_equal(np.asarray(getattr(base, name)).view(np.uint8), np.asarray(getattr(timed, name)).view(np.uint8)), name
+
+
+def test_kernel_timing_rejects_unknown_bits():
+    dmc = mdmc.DualMarchingCubes()
+    with pytest.raises(mdmc.MDMCError):
+        dmc.set_kernel_timing(64)
