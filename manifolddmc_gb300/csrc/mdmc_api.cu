@@ -912,46 +912,42 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     mdmc_status st = markActive(c, g, iso, W, numWords, idsCapacity, s);
     if (st != MDMC_OK) return st;
 
-    // the active cells' records, their contour and quad counts and offsets.
-    // Without reading the active-cell count back first: the records are
-    // made for as many cells as the lists hold (all of them when the grid is
-    // like the last one), the count read on the device, and one read-back
-    // brings the cell, vertex and quad counts; only when the lists were too
-    // short is the pass repeated at the right size.
+    // The active cells' records, their contour and quad counts, and in the
+    // scan of the counts their offsets and the quad owners.  Without reading
+    // the active-cell count back first: the records are made for as many cells
+    // as the lists hold (all of them when the grid is like the last one), the
+    // count read on the device, and one read-back brings the cell, vertex and
+    // quad counts; only when the lists were too short is the pass repeated at
+    // the right size.
     const int* numActiveDev = c->cellFirst.as<int>() + numWords;
+    MDMC_CHECK(c, c->cellCounts.ensure(sizeof(int2)));
     int64_t capA = std::min<int64_t>(idsCapacity, (int64_t)(c->act.bytes / sizeof(ActiveCell)));
     capA = std::min<int64_t>(capA, (int64_t)(c->cellCounts.bytes / sizeof(int2)) - 1);
     capA = std::max<int64_t>(std::min<int64_t>(capA, 0x7FFFFFFF), 0);
+    const int64_t capQ = std::min<int64_t>((int64_t)(c->quadOwner.bytes / sizeof(int)), 0x7FFFFFFF);
     markKernel(c, 4, s);
-    if (capA > 0) {
-        MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(capA)));
-        launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)capA,
-                         status, s, numActiveDev);
-        if (!exclusiveScanOf<int2>(ArrayRead<int2>{c->cellCounts.as<int2>()}, c->cellCounts.as<int2>(), capA,
-                                   c->scanScratch.as<int2>(), s, NoPost(), numActiveDev))
-            return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
-    }
-    launchGatherCounts(numActiveDev, capA > 0 ? c->cellCounts.as<int2>() : nullptr, capA > 0 ? (int)capA : -1,
-                       ctr->gathered, s);
+    MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(capA)));
+    launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)capA,
+                     status, s, numActiveDev);
+    if (!scanCellCounts(c->cellCounts.as<int2>(), capA, numActiveDev, c->act.as<ActiveCell>(), c->quadOwner.as<int>(),
+                        capQ, ctr->gathered, c->scanScratch.as<int2>(), s))
+        return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
     markKernel(c, 5, s);
     MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, ctr->gathered, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
     MDMC_CHECK(c, cudaEventRecord(c->countsEv, s));
     // Before the counts reach the host: when the arrays of an earlier run are
-    // large enough, the cell offsets and the vertex pass run on the device's
-    // counts, so that the device works while the host waits for them.  Not for
-    // runs into host arrays, whose quad pass goes first to start the copies.
+    // large enough, the vertex pass runs on the device's counts, so that the
+    // device works while the host waits for them.  Not for runs into host
+    // arrays, whose quad pass goes first to start the copies.
     DeviceCounts spec{ctr->gathered, 0, 0, 0};
     bool speculated = false;
-    if (!c->hostOut && capA > 0) {
+    if (!c->hostOut && capA > 0 && capQ > 0) {
         const int64_t capV = std::min<int64_t>(std::min(c->pos.bytes, c->nrm.bytes) / (3 * sizeof(float)),
                                                (int64_t)(c->degree.bytes / sizeof(int)));
-        const int64_t capQ = (int64_t)(c->quadOwner.bytes / sizeof(int));
-        if (capV > 0 && capQ > 0) {
+        if (capV > 0) {
             spec.capA = (int)capA;
             spec.capV = (int)std::min<int64_t>(capV, 0x7FFFFFFF);
-            spec.capQ = (int)std::min<int64_t>(capQ, 0x7FFFFFFF);
-            launchFinishCells(c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), spec.capA, X, Y,
-                              c->quadOwner.as<int>(), spec.capQ, status, s, &spec);
+            spec.capQ = (int)capQ;
             markKernel(c, 10, s);
             launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), spec.capA,
                            spec.capV, c->pos.as<float>(), c->nrm.as<float>(), c->degree.as<int>(), status, s, &spec);
@@ -963,20 +959,32 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, cudaEventSynchronize(c->countsEv));  // the counts, not the passes behind them
     const int64_t A = c->hostInts[0];
     int64_t Vd = c->hostInts[1], Q = c->hostInts[2];
-    // the passes above did their work exactly when the counts fit
+    // the records and quad owners, and the vertex pass's vertices, are
+    // complete exactly when the counts fit what the passes covered
+    const bool emitDone = A >= 0 && A <= capA && Q >= 0 && Q <= capQ;
     const bool aheadDone = speculated && spec.fits(A, Vd, Q);
     if ((st = finishActive(c, g, W, numWords, A, idsCapacity, s)) != MDMC_OK) return st;
     c->stats.num_active_cells = A;
-    if (A > capA || capA == 0) {
+    if (!emitDone) {
         MDMC_CHECK(c, c->act.ensure(sizeof(ActiveCell) * (size_t)std::max<int64_t>(A, 1)));
         MDMC_CHECK(c, c->cellCounts.ensure(sizeof(int2) * (size_t)(A + 1)));
+        const int64_t needQ = A <= capA && Q >= 0 ? Q : 3 * A;  // a cell owns at most three quads
+        if (needQ >= (int64_t)0x7FFFFFFF) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "more than 2^31 quads");
+        MDMC_CHECK(c, c->quadOwner.ensure(sizeof(int) * (size_t)std::max<int64_t>(needQ, 1)));
+        MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(A)));
         launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A,
                          status, s);
-        if ((st = scan<int2>(c, c->cellCounts.as<int2>(), c->cellCounts.as<int2>(), A, s)) != MDMC_OK) return st;
+        if (!scanCellCounts(c->cellCounts.as<int2>(), A, nullptr, c->act.as<ActiveCell>(), c->quadOwner.as<int>(),
+                            needQ, ctr->gathered, c->scanScratch.as<int2>(), s))
+            return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
         MDMC_CHECK(c, cudaGetLastError());
-        if ((st = readInts(c, c->cellCounts.as<int2>() + A, 2, s)) != MDMC_OK) return st;
-        Vd = c->hostInts[0];
-        Q = c->hostInts[1];
+        if (A > 0) {
+            if ((st = readInts(c, ctr->gathered, 3, s)) != MDMC_OK) return st;
+            Vd = c->hostInts[1];
+            Q = c->hostInts[2];
+        } else {
+            Vd = Q = 0;
+        }
     }
     if (Vd < A || Vd > 4 * A || Q < 0 || Q > 3 * A)
         return fail(c, MDMC_ERROR_CUDA, "inconsistent vertex or quad count from the emit pass");
@@ -1017,9 +1025,6 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     // mapQuadrilaterals + collectHalfedgeElements, and the halfedge mesh's
     // twins and flags (HalfedgeMesh::initialize) in the same pass
     markKernel(c, 6, s);
-    if (!aheadDone)
-        launchFinishCells(c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A, X, Y, c->quadOwner.as<int>(),
-                          (int)Q, status, s);
     // with host arrays to fill, the quads go in ranges, each copied out as
     // soon as it is written, so that the copies start early
     const bool early = earlyFits(c);

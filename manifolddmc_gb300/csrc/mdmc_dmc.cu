@@ -756,9 +756,9 @@ struct CellScatter {
     uint32_t* __restrict__ cellIds;
     int64_t capacity;
     int W, X, Y;
-    __device__ __forceinline__ void operator()(int64_t w, int first) const {
+    __device__ __forceinline__ void operator()(int64_t w, int first, int count) const {
+        if (!count) return;
         uint32_t m = mask[w];
-        if (!m) return;
         const uint32_t row = (uint32_t)w / (uint32_t)W;  // fewer than 2^32 words
         const int x0 = (int)((uint32_t)w - row * (uint32_t)W) * 32;
         const int y = row % (Y - 1), z = row / (Y - 1);
@@ -771,12 +771,48 @@ struct CellScatter {
             ++j;
         }
     }
+    __device__ __forceinline__ void total(int64_t, int) const {}
 };
 
 bool scanMaskScatter(const uint32_t* mask, int* first, int64_t numWords, int W, int X, int Y, uint32_t* cellIds,
                      int64_t capacity, int* scratch, cudaStream_t s) {
     return exclusiveScanOf<int>(PopcRead{mask}, first, numWords, scratch, s,
                                 CellScatter{mask, cellIds, capacity, W, X, Y});
+}
+
+// The apply hook of the scan of the active cells' (vertex, quad) counts:
+// each cell's first vertex and quad id into its record, the owner of each of
+// its quads (the first capQ), and at the end the counts for the one read-back
+// (gathered: active cells, vertices, quads; -1, -1 for the last two when
+// there were more active cells than the scan covered).
+struct FinishPost {
+    ActiveCell* __restrict__ act;
+    int* __restrict__ quadOwner;
+    int capQ;
+    const int* numActiveDev;  // the uncapped active-cell count (nullptr: the scan's n)
+    int capA;
+    int* gathered;
+    __device__ __forceinline__ void operator()(int64_t i, int2 first, int2 count) const {
+        act[i].pad = first.x;
+        act[i].qbase = first.y;
+        for (int r = 0; r < count.y; ++r)
+            if (inb(first.y + r, capQ)) quadOwner[first.y + r] = (int)i;
+    }
+    __device__ __forceinline__ void total(int64_t n, int2 t) const {
+        const int raw = numActiveDev ? *numActiveDev : (int)n;
+        const bool all = raw >= 0 && raw <= capA;
+        gathered[0] = raw;
+        gathered[1] = all ? t.x : -1;
+        gathered[2] = all ? t.y : -1;
+    }
+};
+
+bool scanCellCounts(int2* counts, int64_t capA, const int* numActiveDev, ActiveCell* act, int* quadOwner, int64_t capQ,
+                    int* gathered, int2* scratch, cudaStream_t s) {
+    return exclusiveScanOf<int2>(ArrayRead<int2>{counts}, counts, capA, scratch, s,
+                                 FinishPost{act, quadOwner, (int)std::min<int64_t>(capQ, 0x7FFFFFFF), numActiveDev,
+                                            (int)capA, gathered},
+                                 numActiveDev);
 }
 
 void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords, int W, int X, int Y, uint32_t* cellIds,
@@ -852,55 +888,6 @@ void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, Act
     else
         kEmitActive<PlainView><<<blocks, 128, 0, s>>>(g.plain, iso, cellIds, act, counts, numActive, numActiveDev,
                                                       status);
-}
-
-// the active-cell count and, when the emit pass covered them all, the
-// vertex and quad totals of its scan, into one place for one read-back
-__global__ void kGatherCounts(const int* numActiveDev, const int2* counts, int capacity, int* out) {
-    const int a = *numActiveDev;
-    out[0] = a;
-    const bool all = a >= 0 && a <= capacity;
-    const int2 t = all ? counts[a] : make_int2(-1, -1);
-    out[1] = t.x;
-    out[2] = t.y;
-}
-
-void launchGatherCounts(const int* numActiveDev, const int2* counts, int capacity, int* out, cudaStream_t s) {
-    countLaunch();
-    kGatherCounts<<<1, 1, 0, s>>>(numActiveDev, counts, capacity, out);
-}
-
-// Each active cell's first vertex id (kept in its record's spare word) and
-// first quad id, and the owner of every quad.
-__global__ void kFinishCells(ActiveCell* __restrict__ act, const int2* __restrict__ offsets, int numActive, int X, int Y,
-                             int* __restrict__ quadOwner, int numQuads, uint32_t* status, DeviceCounts counts) {
-    if (counts.dev) {
-        int a, v, q;
-        if (!counts.fits(a, v, q)) return;
-        numActive = a;
-        numQuads = q;
-    }
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= numActive) return;
-    const ActiveCell rec = act[i];
-    const int2 off = offsets[i];
-    const uint32_t line = rec.cell / (uint32_t)X;
-    const int x = (int)(rec.cell - line * (uint32_t)X), y = (int)(line % (uint32_t)Y), z = (int)(line / (uint32_t)Y);
-    const int nq = ownedQuads((int)(rec.info & 255u), x, y, z);
-    act[i].qbase = off.y;
-    act[i].pad = off.x;
-    for (int r = 0; r < nq; ++r) {
-        if (inb(off.y + r, numQuads)) quadOwner[off.y + r] = i;
-        else atomicOr(status, kStatusCountMismatch);
-    }
-}
-
-void launchFinishCells(ActiveCell* act, const int2* offsets, int numActive, int X, int Y, int* quadOwner, int numQuads,
-                       uint32_t* status, cudaStream_t s, const DeviceCounts* counts) {
-    if (numActive <= 0) return;
-    countLaunch();
-    kFinishCells<<<(numActive + 255) / 256, 256, 0, s>>>(act, offsets, numActive, X, Y, quadOwner, numQuads, status,
-                                                         counts ? *counts : DeviceCounts{nullptr, 0, 0, 0});
 }
 
 // ---------------------------------------------------------------------------

@@ -132,7 +132,13 @@ void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords
 // numActiveDev != nullptr: the count is read on the device, at most numActive
 void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, ActiveCell* act, int2* counts,
                       int numActive, uint32_t* status, cudaStream_t s, const int* numActiveDev = nullptr);
-void launchGatherCounts(const int* numActiveDev, const int2* counts, int capacity, int* out, cudaStream_t s);
+// exclusive scan of the active cells' (vertex, quad) counts in place
+// (capA + 1 entries, the count read from numActiveDev when given) that also
+// writes each record's first vertex and quad id, the quad owners (the first
+// capQ) and gathered[0..2] = active cells, vertices, quads (-1, -1 for the
+// last two when the active cells exceed capA)
+bool scanCellCounts(int2* counts, int64_t capA, const int* numActiveDev, ActiveCell* act, int* quadOwner, int64_t capQ,
+                    int* gathered, int2* scratch, cudaStream_t s);
 // standard Marching Cubes (edge mask over global edge ids 3 * sample + axis,
 // W3 words per sample row)
 void launchMCMarkEdges(const GridDesc& g, float iso, const uint32_t* cellIds, int numActive, int W3, uint32_t* edgeMask,
@@ -147,8 +153,8 @@ void launchMCTriangles(const uint32_t* cellIds, const uint8_t* cases, const int*
 // Counts a pass reads on the device, for launches made before the host has
 // read them back: dev -> {active cells, vertices, quads} (the gathered
 // counts), valid only when all three fit the capacities the launch covers.
-// The passes given one do nothing when the counts do not fit; the host, which
-// reads the same counts, then launches them again at the right size.
+// A pass given one does nothing when the counts do not fit; the host, which
+// reads the same counts, then launches it again at the right size.
 struct DeviceCounts {
     const int* dev;
     int capA, capV, capQ;
@@ -163,8 +169,6 @@ struct DeviceCounts {
     }
 };
 
-void launchFinishCells(ActiveCell* act, const int2* offsets, int numActive, int X, int Y, int* quadOwner, int numQuads,
-                       uint32_t* status, cudaStream_t s, const DeviceCounts* counts = nullptr);
 // degree[v] = the number of quads around DMC vertex v, negated unless every
 // edge of its contour has a quad and no face of its cell has four crossing
 // edges (then its faces are known to form one fan; see kFanFast)

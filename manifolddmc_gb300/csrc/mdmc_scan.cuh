@@ -91,10 +91,13 @@ struct PopcRead {
     __device__ __forceinline__ int operator[](int64_t i) const { return __popc(p[i]); }
 };
 
-// called by the apply pass with every element's exclusive prefix
+// called by the apply pass with every element's exclusive prefix and value,
+// and once with the element count and the total
 struct NoPost {
     template <typename T>
-    __device__ __forceinline__ void operator()(int64_t, T) const {}
+    __device__ __forceinline__ void operator()(int64_t, T, T) const {}
+    template <typename T>
+    __device__ __forceinline__ void total(int64_t, T) const {}
 };
 
 // the element count: known on the host (dev == nullptr), or read on the
@@ -175,11 +178,14 @@ __global__ void __launch_bounds__(kScanThreads) kScanApply(In in, ScanCount cnt,
         int64_t i = base + (int64_t)threadIdx.x * kScanItems + k;
         if (i < n) {
             out[i] = run;
-            post(i, run);
+            post(i, run, vals[k]);
         }
         run = ScanOps<T>::add(run, vals[k]);
     }
-    if ((int)blockIdx.x == lastBlock && threadIdx.x == 0) out[n] = tileSums[nTiles];
+    if ((int)blockIdx.x == lastBlock && threadIdx.x == 0) {
+        out[n] = tileSums[nTiles];
+        post.total(n, tileSums[nTiles]);
+    }
 }
 
 // in and out may alias only if the caller accepts in being overwritten after
