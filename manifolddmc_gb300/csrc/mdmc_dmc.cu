@@ -1207,20 +1207,31 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
                     int ids[4], org[4];
                     ids[0] = h0 + hi;
                     org[0] = quadV[hi];
+                    ids[1] = ids[2] = ids[3] = 0x7FFFFFFF;
+                    org[1] = org[2] = org[3] = -1;
+                    // cand 0: parallel to the quad's edge on the face's other side;
+                    // cand 1, 2: across the face at the edge's lower / upper end.
+                    // The candidates that cross iso are found first and then gone
+                    // through with one body of code, so that lanes whose crossing
+                    // edge is a different candidate run it together.
+                    uint32_t crossing = 0;
 #pragma unroll
                     for (int cand = 0; cand < 3; ++cand) {
-                        ids[cand + 1] = 0x7FFFFFFF;
-                        org[cand + 1] = -1;
-                        // cand 0: parallel to the quad's edge on the face's other side;
-                        // cand 1, 2: across the face at the edge's lower / upper end
+                        const int al = cand == 0 ? axis : u;
+                        const int offU = cand == 0 ? (aMinusU ? 0 : 1) : 0;
+                        const int offA = cand == 2 ? 1 : 0;
+                        const int eA = localEdge((cT << t) | (offU << u) | (offA << axis), al);
+                        crossing |= (((csA >> edgeV0(eA)) ^ (csA >> edgeV1(eA))) & 1u) << cand;
+                    }
+                    while (crossing) {
+                        const int cand = __ffs(crossing) - 1;
+                        crossing &= crossing - 1;
                         const int al = cand == 0 ? axis : u;
                         const int offU = cand == 0 ? (aMinusU ? 0 : 1) : 0;
                         const int offA = cand == 2 ? 1 : 0;
                         const int ca = (cT << t) | (offU << u) | (offA << axis);
                         const int cb = (cTB << t) | (offU << u) | (offA << axis);
                         const int eA = localEdge(ca, al), eB = localEdge(cb, al);
-                        const bool cross = ((csA >> edgeV0(eA)) ^ (csA >> edgeV1(eA))) & 1u;
-                        if (!cross) continue;
                         if ((int)((infoA >> (8 + 2 * eA)) & 3u) != tA) continue;
                         if ((int)((infoB >> (8 + 2 * eB)) & 3u) != tB) continue;
                         // the grid edge's origin and the quad its owner holds
@@ -1259,14 +1270,25 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
                         const int q2 = oqbase + r;
                         const int edgyO = ((csA >> edgeV0(eA)) & 1u) ? 0 : 1;
                         const int sA = quadSlot(eA, edgyO), sB = quadSlot(eB, edgyO);
+                        int id = 0x7FFFFFFF, o = -1;
                         if (((sA + 1) & 3) == sB) {
-                            ids[cand + 1] = 4 * q2 + sA;
-                            org[cand + 1] = vbA + tA;
+                            id = 4 * q2 + sA;
+                            o = vbA + tA;
                         } else if (((sB + 1) & 3) == sA) {
-                            ids[cand + 1] = 4 * q2 + sB;
-                            org[cand + 1] = vbB + tB;
+                            id = 4 * q2 + sB;
+                            o = vbB + tB;
                         } else {
                             atomicOr(&ctr->status, kStatusBadIndex);
+                        }
+                        if (cand == 0) {
+                            ids[1] = id;
+                            org[1] = o;
+                        } else if (cand == 1) {
+                            ids[2] = id;
+                            org[2] = o;
+                        } else {
+                            ids[3] = id;
+                            org[3] = o;
                         }
                     }
                     // sort the bucket (absent entries last) with its origins
