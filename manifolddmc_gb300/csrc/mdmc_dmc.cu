@@ -1240,27 +1240,24 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
                         const int oy = py + (u == 1 ? du : 0) + (axis == 1 ? offA : 0);
                         const int oz = pz + (u == 2 ? du : 0) + (axis == 2 ? offA : 0);
                         if (((al != 0 && ox < 1) || (al != 1 && oy < 1) || (al != 2 && oz < 1))) continue;
-                        // the owner is often a cell around the quad's edge (p, p - e_u),
-                        // whose record is loaded already
-                        uint32_t oinfo;
-                        int oqbase;
+                        // the owner is a cell around the quad's edge (p, p - e_u), or
+                        // p + e_u (du = 1), p + e_a (du = 0) or p - e_u + e_a (du = -1);
+                        // every record is loaded already (both picks are made, one kept)
+                        const int ko = du == 0 ? 0 : (u == b ? 1 : 2);
+                        const int kx = offA == 0 ? (u == b ? 0 : 1) : (du == 0 ? 2 : (u == b ? 3 : 4));
+                        uint32_t oinfo = 0;
+                        int oqbase = -1;
+#pragma unroll
+                        for (int k = 0; k < 5; ++k)
+                            if (kx == k) {
+                                oinfo = xinfo[k];
+                                oqbase = xqbase[k];
+                            }
                         if (offA == 0 && du <= 0) {
-                            const int ko = du == 0 ? 0 : (u == b ? 1 : 2);
                             oinfo = ko == 0 ? cell[0].info : (ko == 1 ? cell[1].info : cell[2].info);
                             oqbase = ko == 0 ? cell[0].qbase : (ko == 1 ? cell[1].qbase : cell[2].qbase);
-                        } else {
-                            // p + e_u (du = 1), p + e_a (du = 0) or p - e_u + e_a (du = -1)
-                            const int kx = offA == 0 ? (u == b ? 0 : 1) : (du == 0 ? 2 : (u == b ? 3 : 4));
-                            oinfo = 0;
-                            oqbase = -1;
-#pragma unroll
-                            for (int k = 0; k < 5; ++k)
-                                if (kx == k) {
-                                    oinfo = xinfo[k];
-                                    oqbase = xqbase[k];
-                                }
-                            if (oqbase < 0) continue;
                         }
+                        if (oqbase < 0) continue;
                         const int cso = (int)(oinfo & 255u);
                         if (!ownsAxis(cso, al, ox, oy, oz)) continue;
                         int r = 0;
