@@ -752,6 +752,7 @@ __global__ void kScatterCells(const uint32_t* __restrict__ mask, const int* __re
 // first index: ids beyond `capacity` are not written (the caller then runs
 // kScatterCells once it knows the count and has the room).
 struct CellScatter {
+    static constexpr bool kStaged = false;
     const uint32_t* __restrict__ mask;
     uint32_t* __restrict__ cellIds;
     int64_t capacity;
@@ -786,6 +787,7 @@ bool scanMaskScatter(const uint32_t* mask, int* first, int64_t numWords, int W, 
 // (gathered: active cells, vertices, quads; -1, -1 for the last two when
 // there were more active cells than the scan covered).
 struct FinishPost {
+    static constexpr bool kStaged = true;
     ActiveCell* __restrict__ act;
     int* __restrict__ quadOwner;
     int capQ;
@@ -894,11 +896,20 @@ void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, Act
 // vertices of the active cells (sliceP's vertex part, D/CellIntersection.inl:
 // 368-439), one thread per active cell
 // ---------------------------------------------------------------------------
-#ifndef MDMC_VERTICES_MIN_BLOCKS
-#define MDMC_VERTICES_MIN_BLOCKS 5  // 96 registers: 0.19 ms instead of 0.22 ms at 114 on the 512^3-cell blobs
-#endif
+// resident blocks per SM the register allocation aims at: 5 (96 registers)
+// for the per-sample stencils (0.19 ms instead of 0.22 ms at 114 registers on
+// the 512^3-cell blobs), 6 (80 registers, no spills) for the separable one
+// (0.116 ms instead of 0.121 ms at 5)
+template <class Stencil>
+struct VerticesBlocks {
+    static constexpr int value = 5;
+};
+template <>
+struct VerticesBlocks<SepStencil> {
+    static constexpr int value = 6;
+};
 template <class View, class Stencil>
-__global__ void __launch_bounds__(128, MDMC_VERTICES_MIN_BLOCKS) kVertices(View g, float iso, int surfaceIteration,
+__global__ void __launch_bounds__(128, VerticesBlocks<Stencil>::value) kVertices(View g, float iso, int surfaceIteration,
                                                  const ActiveCell* __restrict__ act, int numActive,
                                                  int numVertices, float* __restrict__ pos,
                                                  float* __restrict__ nrm, int* __restrict__ degree,

@@ -94,6 +94,7 @@ struct PopcRead {
 // called by the apply pass with every element's exclusive prefix and value,
 // and once with the element count and the total
 struct NoPost {
+    static constexpr bool kStaged = false;
     template <typename T>
     __device__ __forceinline__ void operator()(int64_t, T, T) const {}
     template <typename T>
@@ -154,6 +155,7 @@ __global__ void __launch_bounds__(1024) kScanTiles(T* tileSums, ScanCount cnt) {
     if (threadIdx.x == 0) tileSums[numTiles] = carryShared;
 }
 
+// Each thread scans kScanItems consecutive elements straight from memory.
 template <typename T, class In, class Post>
 __global__ void __launch_bounds__(kScanThreads) kScanApply(In in, ScanCount cnt, const T* __restrict__ tileSums,
                            T* __restrict__ out, Post post) {
@@ -188,6 +190,59 @@ __global__ void __launch_bounds__(kScanThreads) kScanApply(In in, ScanCount cnt,
     }
 }
 
+// The same with the tile going through shared memory twice: loaded and
+// stored by consecutive threads (coalesced), scanned by each thread over
+// kScanItems consecutive elements; post gets each element's value as the
+// difference of consecutive prefixes.  For posts that write per-element
+// records (Post::kStaged), whose stores the direct kernel would stride.
+template <typename T, class In, class Post>
+__global__ void __launch_bounds__(kScanThreads) kScanApplyStaged(In in, ScanCount cnt, const T* __restrict__ tileSums,
+                                 T* __restrict__ out, Post post) {
+    __shared__ T stage[kScanTile];
+    const int64_t n = cnt.get();
+    const int nTiles = (int)scanTiles(n);
+    const int lastBlock = nTiles > 0 ? nTiles - 1 : 0;
+    if ((int)blockIdx.x > lastBlock) return;
+    const int64_t base = (int64_t)blockIdx.x * kScanTile;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t i = base + (int64_t)k * kScanThreads + threadIdx.x;
+        stage[k * kScanThreads + threadIdx.x] = i < n ? in[i] : ScanOps<T>::zero();
+    }
+    __syncthreads();
+    T vals[kScanItems];
+    T acc = ScanOps<T>::zero();
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        vals[k] = stage[threadIdx.x * kScanItems + k];
+        acc = ScanOps<T>::add(acc, vals[k]);
+    }
+    T total;
+    const T tileBase = tileSums[blockIdx.x];
+    T run = ScanOps<T>::add(tileBase, blockExclusive(acc, total));  // (ends with a barrier: stage is read)
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        stage[threadIdx.x * kScanItems + k] = run;
+        run = ScanOps<T>::add(run, vals[k]);
+    }
+    __syncthreads();
+    const T tileEnd = ScanOps<T>::add(tileBase, total);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        const int idx = k * kScanThreads + threadIdx.x;
+        const int64_t i = base + idx;
+        if (i < n) {
+            const T r = stage[idx];
+            out[i] = r;
+            post(i, r, minus(idx + 1 < kScanTile ? stage[idx + 1] : tileEnd, r));
+        }
+    }
+    if ((int)blockIdx.x == lastBlock && threadIdx.x == 0) {
+        out[n] = tileSums[nTiles];
+        post.total(n, tileSums[nTiles]);
+    }
+}
+
 // in and out may alias only if the caller accepts in being overwritten after
 // the reduction (kScanApply reads in[i] before writing out[i] of the same i).
 // scratch needs numTiles + 1 elements.  Returns false if n is too large.
@@ -210,7 +265,10 @@ bool exclusiveScanOf(In in, T* out, int64_t n, T* scratch, cudaStream_t s, Post 
     kScanTiles<T><<<1, 1024, 0, s>>>(scratch, cnt);
     if (n > 0 || nDev) {
         countLaunch();
-        kScanApply<T, In, Post><<<nt, kScanThreads, 0, s>>>(in, cnt, scratch, out, post);
+        if constexpr (Post::kStaged)
+            kScanApplyStaged<T, In, Post><<<nt, kScanThreads, 0, s>>>(in, cnt, scratch, out, post);
+        else
+            kScanApply<T, In, Post><<<nt, kScanThreads, 0, s>>>(in, cnt, scratch, out, post);
     } else {
         cudaMemcpyAsync(out, scratch, sizeof(T), cudaMemcpyDeviceToDevice, s);
     }
