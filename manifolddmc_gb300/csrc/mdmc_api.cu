@@ -130,6 +130,7 @@ struct mdmc_context {
     int64_t mcV = 0, mcT = 0;
     // events: start, dmc, halfedge, repair, detect, end
     cudaEvent_t ev[6] = {};
+    int evAt[6] = {0, 1, 2, 3, 4, 5};  // the event that marks stage boundary k
     // per-kernel events: refine, count, emit, quads, table, vertices (begin/end each)
     cudaEvent_t kev[12] = {};
     uint32_t kernelTiming = 0;  // MDMC_TIME_* bits: kernels whose event pairs are recorded
@@ -140,6 +141,17 @@ struct mdmc_context {
 };
 
 namespace {
+
+// stage boundary k (ev[k]); when nothing ran since boundary k - 1 the
+// previous boundary's event stands for it (an event record costs ~1.7 us)
+inline void markStage(mdmc_context* c, int k, bool ran, cudaStream_t s) {
+    if (ran || k == 0) {
+        cudaEventRecord(c->ev[k], s);
+        c->evAt[k] = k;
+    } else {
+        c->evAt[k] = c->evAt[k - 1];
+    }
+}
 
 // kev[2k], kev[2k + 1] bracket timed kernel k (bit k of MDMC_TIME_*): an
 // event record costs the stream about 1.7 us, so only requested pairs are made
@@ -383,13 +395,13 @@ mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaSt
                          c->slowFan.as<uint8_t>(), c->isKey.as<uint8_t>(), c->fans.as<int>(), c->vflags.as<uint8_t>(),
                          ctr, status, s);
     }
-    cudaEventRecord(c->ev[4], s);
+    markStage(c, 4, detect, s);
     if (!starsDone)
         launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), mdF, c->heValence.as<uint8_t>(), c->quads.as<int4>(),
                      c->vertexHE.as<int>(), detect, ctr, status, s);
     else if (!detect)
         launchVertexHalfedgeFix(c->vertexHE.as<int>(), (int)c->V, s);
-    cudaEventRecord(c->ev[5], s);
+    markStage(c, 5, !starsDone || !detect, s);
     MDMC_CHECK(c, cudaGetLastError());
     return MDMC_OK;
 }
@@ -899,7 +911,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     uint32_t* status = &ctr->status;
     MDMC_CHECK(c, cudaMemsetAsync(ctr, 0, sizeof(DevCounters), s));
     const long long launches0 = g_kernelLaunches.load();
-    cudaEventRecord(c->ev[0], s);
+    markStage(c, 0, true, s);
     markKernel(c, 0, s);
     markKernel(c, 1, s);
     GridDesc g;
@@ -1049,7 +1061,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     }
     if (early && (st = earlyCopyVertices(c, s)) != MDMC_OK) return st;
     MDMC_CHECK(c, cudaGetLastError());
-    cudaEventRecord(c->ev[1], s);
+    markStage(c, 1, true, s);
     markKernel(c, 8, s);
     // runPostProcesses, D/DualMarchingCubes.cu:335-380: simplifications first
     if (c->opt.simplify_p3x3y_color && (st = runSimplification(c, 0, s)) != MDMC_OK) return st;
@@ -1057,7 +1069,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     if (c->opt.simplify_p3333 && (st = runSimplification(c, 2, s)) != MDMC_OK) return st;
     const MeshDims md0{(int)c->V, (int)c->F, (int)c->H};
     markKernel(c, 9, s);
-    cudaEventRecord(c->ev[2], s);
+    markStage(c, 2, c->opt.simplify_p3x3y_color || c->opt.simplify_p3x3y_old || c->opt.simplify_p3333, s);
 
     // ---- repair: fixManifoldTwins, then the splitter ---------------------------
     launchReconnect(g, iso, c->nmList.as<int4>(), ctr, c->he.as<int4>(), c->pos.as<float>(), md0,
@@ -1071,7 +1083,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     // the splitter turns out not to run.
     bool finished = false;
     if (!c->simplified) {
-        cudaEventRecord(c->ev[3], s);
+        markStage(c, 3, true, s);
         if ((st = finishMesh(c, true, &ctr->specStatus, s)) != MDMC_OK) return st;
         if (early && (st = earlyCopyVertexMaps(c, s)) != MDMC_OK) return st;
         MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
@@ -1085,7 +1097,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
         if (c->opt.split_non_manifold_halfedges) {
             if ((st = runSplitter(c, g, iso, iterations, s)) != MDMC_OK) return st;
         }
-        cudaEventRecord(c->ev[3], s);
+        markStage(c, 3, true, s);
         // the splitter's refresh reset the edge counters; detection and the
         // face statistics start from zero again
         MDMC_CHECK(c, cudaMemsetAsync(&ctr->nmVertices, 0, sizeof(unsigned long long), s));
@@ -1105,8 +1117,8 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->stats.anomalies = (int64_t)hc.status;
     float ms[5] = {0, 0, 0, 0, 0};
     for (int k = 0; k < 4; ++k)
-        if (cudaEventElapsedTime(&ms[k], c->ev[k], c->ev[k + 1]) != cudaSuccess) ms[k] = 0.f;
-    if (cudaEventElapsedTime(&ms[4], c->ev[0], c->ev[5]) != cudaSuccess) ms[4] = 0.f;
+        if (cudaEventElapsedTime(&ms[k], c->ev[c->evAt[k]], c->ev[c->evAt[k + 1]]) != cudaSuccess) ms[k] = 0.f;
+    if (cudaEventElapsedTime(&ms[4], c->ev[c->evAt[0]], c->ev[c->evAt[5]]) != cudaSuccess) ms[4] = 0.f;
     c->stats.ms_dmc = ms[0];
     c->stats.ms_halfedge = ms[1];
     c->stats.ms_repair = ms[2];
