@@ -105,6 +105,7 @@ struct mdmc_context {
     DevBuf counters;
     DevCounters* hostCounters = nullptr;  // pinned
     int32_t* hostInts = nullptr;          // pinned scratch for small reads
+    int32_t* hostIntsDev = nullptr;       // hostInts as kernels address it (nullptr: not mapped)
     // splitter
     DevBuf nmFlags, nmOffsets, nmFaces;
     DevBuf wPos, wNrm, wVfl, wHfl, wFfl, wVC2O, wHC2O, wFC2O, wOrigV, wOrigH, wHe, wFirst, wAttr, wVNum, wVSlots,
@@ -742,6 +743,9 @@ mdmc_status mdmc_create(mdmc_context** context, const mdmc_options* options) {
         mdmc_destroy(c);
         return MDMC_ERROR_OUT_OF_MEMORY;
     }
+    void* mapped = nullptr;
+    if (cudaHostGetDevicePointer(&mapped, c->hostInts, 0) == cudaSuccess) c->hostIntsDev = static_cast<int32_t*>(mapped);
+    else (void)cudaGetLastError();
     for (auto& e : c->ev) cudaEventCreate(&e);
     for (auto& e : c->kev) cudaEventCreate(&e);
     for (auto& e : c->copyEv) cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
@@ -941,11 +945,14 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(capA)));
     launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)capA,
                      status, s, numActiveDev);
+    // the scan's last block writes the counts straight into the pinned host
+    // scratch when the device can address it (no copy on the stream)
     if (!scanCellCounts(c->cellCounts.as<int2>(), capA, numActiveDev, c->act.as<ActiveCell>(), c->quadOwner.as<int>(),
-                        capQ, ctr->gathered, c->scanScratch.as<int2>(), s))
+                        capQ, ctr->gathered, c->hostIntsDev, c->scanScratch.as<int2>(), s))
         return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
     markKernel(c, 5, s);
-    MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, ctr->gathered, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (!c->hostIntsDev)
+        MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, ctr->gathered, 3 * sizeof(int), cudaMemcpyDeviceToHost, s));
     MDMC_CHECK(c, cudaEventRecord(c->countsEv, s));
     // Before the counts reach the host: when the arrays of an earlier run are
     // large enough, the vertex pass runs on the device's counts, so that the
@@ -954,15 +961,18 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     DeviceCounts spec{ctr->gathered, 0, 0, 0};
     bool speculated = false;
     if (!c->hostOut && capA > 0 && capQ > 0) {
-        const int64_t capV = std::min<int64_t>(std::min(c->pos.bytes, c->nrm.bytes) / (3 * sizeof(float)),
-                                               (int64_t)(c->degree.bytes / sizeof(int)));
+        const int64_t capV = std::min<int64_t>(
+            std::min<int64_t>(std::min(c->pos.bytes, c->nrm.bytes) / (3 * sizeof(float)),
+                              (int64_t)(std::min(c->degree.bytes, c->vertexHE.bytes) / sizeof(int))),
+            (int64_t)(c->vflags.bytes & ~(size_t)3));  // (the flags are kept in whole words)
         if (capV > 0) {
             spec.capA = (int)capA;
             spec.capV = (int)std::min<int64_t>(capV, 0x7FFFFFFF);
             spec.capQ = (int)capQ;
             markKernel(c, 10, s);
             launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), spec.capA,
-                           spec.capV, c->pos.as<float>(), c->nrm.as<float>(), c->degree.as<int>(), status, s, &spec);
+                           spec.capV, c->pos.as<float>(), c->nrm.as<float>(), c->degree.as<int>(),
+                           c->vflags.as<uint8_t>(), c->vertexHE.as<int>(), status, s, &spec);
             markKernel(c, 11, s);
             speculated = true;
         }
@@ -987,7 +997,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
         launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A,
                          status, s);
         if (!scanCellCounts(c->cellCounts.as<int2>(), A, nullptr, c->act.as<ActiveCell>(), c->quadOwner.as<int>(),
-                            needQ, ctr->gathered, c->scanScratch.as<int2>(), s))
+                            needQ, ctr->gathered, nullptr, c->scanScratch.as<int2>(), s))
             return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
         MDMC_CHECK(c, cudaGetLastError());
         if (A > 0) {
@@ -1028,11 +1038,12 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     MDMC_CHECK(c, c->faceAttr.ensure(roundUp(sizeof(uint16_t) * (size_t)std::max<int64_t>(Q, 1), 4)));
     MDMC_CHECK(c, c->nmList.ensure(sizeof(int4) * (size_t)(Q + 1)));
     MDMC_CHECK(c, c->heValence.ensure((size_t)std::max<int64_t>(4 * Q, 1)));
-    MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)Vd, 4), s));
+    // (the vertex pass run ahead set the flags and stars' starting values)
+    if (!aheadDone) MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)Vd, 4), s));
     MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)std::max<int64_t>(Q, 1)));
     MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)Vd));
     MDMC_CHECK(c, c->degree.ensure(sizeof(int) * (size_t)Vd));
-    MDMC_CHECK(c, cudaMemsetAsync(c->vertexHE.p, 0x7F, sizeof(int) * (size_t)Vd, s));
+    if (!aheadDone) MDMC_CHECK(c, cudaMemsetAsync(c->vertexHE.p, 0x7F, sizeof(int) * (size_t)Vd, s));
 
     // mapQuadrilaterals + collectHalfedgeElements, and the halfedge mesh's
     // twins and flags (HalfedgeMesh::initialize) in the same pass
@@ -1056,7 +1067,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     if (!aheadDone) {
         markKernel(c, 10, s);
         launchVertices(g, iso, c->opt.enable_surface_to_vertex_iteration, c->act.as<ActiveCell>(), (int)A, (int)Vd,
-                       c->pos.as<float>(), c->nrm.as<float>(), c->degree.as<int>(), status, s);
+                       c->pos.as<float>(), c->nrm.as<float>(), c->degree.as<int>(), nullptr, nullptr, status, s);
         markKernel(c, 11, s);
     }
     if (early && (st = earlyCopyVertices(c, s)) != MDMC_OK) return st;

@@ -794,6 +794,7 @@ struct FinishPost {
     const int* numActiveDev;  // the uncapped active-cell count (nullptr: the scan's n)
     int capA;
     int* gathered;
+    int* gatheredHost;  // the same three counts into mapped host memory (optional)
     __device__ __forceinline__ void operator()(int64_t i, int2 first, int2 count) const {
         act[i].pad = first.x;
         act[i].qbase = first.y;
@@ -806,14 +807,20 @@ struct FinishPost {
         gathered[0] = raw;
         gathered[1] = all ? t.x : -1;
         gathered[2] = all ? t.y : -1;
+        if (gatheredHost) {
+            gatheredHost[0] = raw;
+            gatheredHost[1] = all ? t.x : -1;
+            gatheredHost[2] = all ? t.y : -1;
+            __threadfence_system();
+        }
     }
 };
 
 bool scanCellCounts(int2* counts, int64_t capA, const int* numActiveDev, ActiveCell* act, int* quadOwner, int64_t capQ,
-                    int* gathered, int2* scratch, cudaStream_t s) {
+                    int* gathered, int* gatheredHost, int2* scratch, cudaStream_t s) {
     return exclusiveScanOf<int2>(ArrayRead<int2>{counts}, counts, capA, scratch, s,
                                  FinishPost{act, quadOwner, (int)std::min<int64_t>(capQ, 0x7FFFFFFF), numActiveDev,
-                                            (int)capA, gathered},
+                                            (int)capA, gathered, gatheredHost},
                                  numActiveDev);
 }
 
@@ -913,6 +920,7 @@ __global__ void __launch_bounds__(128, VerticesBlocks<Stencil>::value) kVertices
                                                  const ActiveCell* __restrict__ act, int numActive,
                                                  int numVertices, float* __restrict__ pos,
                                                  float* __restrict__ nrm, int* __restrict__ degree,
+                                                 uint8_t* __restrict__ flagsInit, int* __restrict__ starInit,
                                                  uint32_t* status, DeviceCounts counts) {
     if (counts.dev) {
         int a, v, q;
@@ -984,25 +992,29 @@ __global__ void __launch_bounds__(128, VerticesBlocks<Stencil>::value) kVertices
         nrm[3 * vi + 1] = nm.y;
         nrm[3 * vi + 2] = nm.z;
         degree[vi] = deg == csz && !diagonalFace ? deg : -deg;
+        if (flagsInit) {  // what the quad pass starts from (no flags, no outgoing halfedge yet)
+            flagsInit[vi] = 0;
+            starInit[vi] = 0x7F7F7F7F;
+        }
     }
 }
 
 void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, int numActive,
-                    int numVertices, float* pos, float* nrm, int* degree, uint32_t* status, cudaStream_t s,
-                    const DeviceCounts* counts) {
+                    int numVertices, float* pos, float* nrm, int* degree, uint8_t* flagsInit, int* starInit,
+                    uint32_t* status, cudaStream_t s, const DeviceCounts* counts) {
     if (numActive <= 0) return;
     countLaunch();
     const unsigned blocks = (unsigned)((numActive + 127) / 128);
     const DeviceCounts dc = counts ? *counts : DeviceCounts{nullptr, 0, 0, 0};
     if (g.refined && sepStencilApplies(g.ref.r, g.ref.X, g.ref.Y, g.ref.Z))
         kVertices<RefinedView, SepStencil><<<blocks, 128, 0, s>>>(g.ref, iso, surfaceIteration, act, numActive,
-                                                                  numVertices, pos, nrm, degree, status, dc);
+                                                                  numVertices, pos, nrm, degree, flagsInit, starInit, status, dc);
     else if (g.refined)
         kVertices<RefinedView, CellStencil<RefinedView>><<<blocks, 128, 0, s>>>(
-            g.ref, iso, surfaceIteration, act, numActive, numVertices, pos, nrm, degree, status, dc);
+            g.ref, iso, surfaceIteration, act, numActive, numVertices, pos, nrm, degree, flagsInit, starInit, status, dc);
     else
         kVertices<PlainView, CellStencil<PlainView>><<<blocks, 128, 0, s>>>(
-            g.plain, iso, surfaceIteration, act, numActive, numVertices, pos, nrm, degree, status, dc);
+            g.plain, iso, surfaceIteration, act, numActive, numVertices, pos, nrm, degree, flagsInit, starInit, status, dc);
 }
 
 // ---------------------------------------------------------------------------

@@ -138,7 +138,7 @@ void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, Act
 // capQ) and gathered[0..2] = active cells, vertices, quads (-1, -1 for the
 // last two when the active cells exceed capA)
 bool scanCellCounts(int2* counts, int64_t capA, const int* numActiveDev, ActiveCell* act, int* quadOwner, int64_t capQ,
-                    int* gathered, int2* scratch, cudaStream_t s);
+                    int* gathered, int* gatheredHost, int2* scratch, cudaStream_t s);
 // standard Marching Cubes (edge mask over global edge ids 3 * sample + axis,
 // W3 words per sample row)
 void launchMCMarkEdges(const GridDesc& g, float iso, const uint32_t* cellIds, int numActive, int W3, uint32_t* edgeMask,
@@ -172,9 +172,11 @@ struct DeviceCounts {
 // degree[v] = the number of quads around DMC vertex v, negated unless every
 // edge of its contour has a quad and no face of its cell has four crossing
 // edges (then its faces are known to form one fan; see kFanFast)
+// flagsInit, starInit (optional): vertex flags set to 0 and smallest
+// outgoing halfedges to "none" (0x7F7F7F7F), the quad pass's starting values
 void launchVertices(const GridDesc& g, float iso, int surfaceIteration, const ActiveCell* act, int numActive,
-                    int numVertices, float* pos, float* nrm, int* degree, uint32_t* status, cudaStream_t s,
-                    const DeviceCounts* counts = nullptr);
+                    int numVertices, float* pos, float* nrm, int* degree, uint8_t* flagsInit, int* starInit,
+                    uint32_t* status, cudaStream_t s, const DeviceCounts* counts = nullptr);
 void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, const uint32_t* cellMask,
                  const int* cellFirst, int X, int Y, int Z, int W, int4* he, int* faceFirst, uint16_t* faceAttr,
                  uint8_t* vflags, uint8_t* heValence, int4* nmList, int nmCapacity, int numQuads, int numVertices,
