@@ -115,6 +115,7 @@ struct mdmc_context {
     DevBuf appV, appH, appF;
     // fan detection
     DevBuf isKey, fans, degree, slowFan;
+    uint8_t keyMark = 0;  // the last detection pass's fan-key mark (1..255, 0 = none yet)
     // standard Marching Cubes: edge mask and the index of each word's first
     // edge, per active cell its case and triangle offset, the vertices' edge
     // ids, and the triangle mesh
@@ -386,14 +387,23 @@ mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaSt
     const MeshDims mdF{(int)c->V, (int)c->F, (int)c->H};
     const bool detect = c->opt.detect_non_manifold_vertices != 0;
     if (detect) {
+        // fan keys are marked with this pass's number (1..255); the array is
+        // cleared only when it is new or the numbers wrap around
+        const void* keys = c->isKey.p;
         MDMC_CHECK(c, c->isKey.ensure((size_t)std::max<int64_t>(c->H, 1)));
+        if (c->isKey.p != keys || c->keyMark == 255) {
+            MDMC_CHECK(c, cudaMemsetAsync(c->isKey.p, 0, c->isKey.bytes, s));
+            c->keyMark = 0;
+        }
+        ++c->keyMark;
         MDMC_CHECK(c, c->fans.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
         MDMC_CHECK(c, c->slowFan.ensure((size_t)std::max<int64_t>(c->V, 1)));
-        MDMC_CHECK(c, cudaMemsetAsync(c->isKey.p, 0, (size_t)c->H, s));
-        MDMC_CHECK(c, cudaMemsetAsync(&ctr->slowFans, 0, sizeof(unsigned long long), s));
+        // (the first pass of a run finds the count zeroed with the counters)
+        if (!starsDone) MDMC_CHECK(c, cudaMemsetAsync(&ctr->slowFans, 0, sizeof(unsigned long long), s));
         if (!starsDone) launchVertexStar(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), s);
         launchDetectFans(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), starsDone,
-                         c->slowFan.as<uint8_t>(), c->isKey.as<uint8_t>(), c->fans.as<int>(), c->vflags.as<uint8_t>(),
+                         c->slowFan.as<uint8_t>(), c->isKey.as<uint8_t>(), c->keyMark, c->fans.as<int>(),
+                         c->vflags.as<uint8_t>(),
                          ctr, status, s);
     }
     markStage(c, 4, detect, s);

@@ -185,7 +185,7 @@ struct RowWalker<RefinedView> {
     int ySecond[2];      // per sample row y, y+1: 0 -> rows (J0, J1), 1 -> rows (J1, J2)
     int zSecond[2];
     float dy[2], dz[2];  // in-cell weights of y, y+1 and z, z+1
-    const float* rowPtr[3][3];
+    uint32_t rowOff[3][3];  // element offsets of the coarse rows (coarse grids have fewer than 2^32 samples)
     __device__ RowWalker(const RefinedView& view, int y, int z) : g(view) {
         int myy[2], mzz[2];
         for (int t = 0; t < 2; ++t) {
@@ -205,7 +205,7 @@ struct RowWalker<RefinedView> {
             zSecond[t] = mzz[t] != mzz[0] ? 1 : 0;
         }
         for (int a = 0; a < 3; ++a)
-            for (int b = 0; b < 3; ++b) rowPtr[a][b] = g.c + ((size_t)K[b] * g.cY + J[a]) * g.cX;
+            for (int b = 0; b < 3; ++b) rowOff[a][b] = ((uint32_t)K[b] * (uint32_t)g.cY + (uint32_t)J[a]) * (uint32_t)g.cX;
         my = g.coarseCell(y, g.Y, g.cY);
         mz = g.coarseCell(z, g.Z, g.cZ);
     }
@@ -220,8 +220,8 @@ struct RowWalker<RefinedView> {
         const float dx = qx - (float)mx;
         const int x0 = min(max(mx, 0), g.cX - 1), x1 = min(max(mx + 1, 0), g.cX - 1);
         auto lerpX = [&](int a, int b) {
-            const float* p = rowPtr[a][b];
-            const float s0 = __ldg(p + x0), s1 = __ldg(p + x1);
+            const uint32_t o = rowOff[a][b];
+            const float s0 = __ldg(g.c + (o + (uint32_t)x0)), s1 = __ldg(g.c + (o + (uint32_t)x1));
             return s0 + dx * (s1 - s0);
         };
         const bool y2 = ySecond[1], z2 = zSecond[1];
@@ -1030,7 +1030,8 @@ struct CellIndex {
     __device__ __forceinline__ int find(int x, int y, int z) const {
         if ((unsigned)x > (unsigned)(X - 2) || (unsigned)y > (unsigned)(Y - 2) || (unsigned)z > (unsigned)(Z - 2))
             return -1;
-        const int64_t w = ((int64_t)z * (Y - 1) + y) * W + (x >> 5);
+        // (mask words number fewer than 2^27: grids have fewer than 2^32 samples)
+        const uint32_t w = ((uint32_t)z * (uint32_t)(Y - 1) + (uint32_t)y) * (uint32_t)W + (uint32_t)(x >> 5);
         const uint32_t m = __ldg(mask + w);
         const int f = __ldg(first + w);
         const uint32_t bit = 1u << (x & 31);

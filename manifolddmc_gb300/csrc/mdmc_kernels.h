@@ -193,9 +193,10 @@ void launchReconnect(const GridDesc& g, float iso, const int4* nmList, const Dev
                      int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s);
 void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cudaStream_t s);
 // vertexPassDegrees: deg is the vertex pass's signed degree of the DMC mesh
-// (only the twin repair has run since); otherwise non-negative degrees
+// (only the twin repair has run since); otherwise non-negative degrees.
+// isKey[h] == keyMark marks this pass's fan keys (no other entry may hold it)
 void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, bool vertexPassDegrees,
-                      uint8_t* slow, uint8_t* isKey, int* fans, uint8_t* vflags, DevCounters* ctr,
+                      uint8_t* slow, uint8_t* isKey, uint8_t keyMark, int* fans, uint8_t* vflags, DevCounters* ctr,
                       uint32_t* status, cudaStream_t s);
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, int4* quads,
                   int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s);

@@ -458,23 +458,26 @@ __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restri
 // the single walk did not settle.
 // (a grid-stride loop over a fixed grid: when no vertex is unsettled, which
 // is the common case, each block reads the counter once and leaves)
+// isKey[h] == mark: h is a fan key in this detection pass (the caller gives
+// every pass its own mark, so that the marks of earlier passes need no clearing)
 __global__ void kFanKeys(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ slow,
-                         const unsigned long long* slowCount, uint8_t* __restrict__ isKey, uint32_t* status) {
+                         const unsigned long long* slowCount, uint8_t* __restrict__ isKey, uint8_t mark,
+                         uint32_t* status) {
     if (*slowCount == 0) return;
     for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < md.H; h += gridDim.x * blockDim.x) {
         const int v = he[h].x;
         if (!inb(v, md.V) || !slow[v]) continue;
         const int k = min(h, min(fanWalk(he, h, true, md.H, status), fanWalk(he, h, false, md.H, status)));
-        isKey[k] = 1;
+        isKey[k] = mark;
     }
 }
 
 __global__ void kFanCount(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ slow,
-                          const unsigned long long* slowCount, const uint8_t* __restrict__ isKey,
+                          const unsigned long long* slowCount, const uint8_t* __restrict__ isKey, uint8_t mark,
                           int* __restrict__ fans, uint32_t* status) {
     if (*slowCount == 0) return;
     for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < md.H; h += gridDim.x * blockDim.x) {
-        if (!isKey[h]) continue;
+        if (isKey[h] != mark) continue;
         const int v = he[h].x;
         if (inb(v, md.V)) {
             if (slow[v]) atomicAdd(&fans[v], 1);
@@ -516,7 +519,8 @@ void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cuda
 }
 
 void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, bool vertexPassDegrees,
-                      uint8_t* slow, uint8_t* isKey, int* fans, uint8_t* vflags, DevCounters* ctr, uint32_t* status,
+                      uint8_t* slow, uint8_t* isKey, uint8_t keyMark, int* fans, uint8_t* vflags, DevCounters* ctr,
+                      uint32_t* status,
                       cudaStream_t s) {
     if (md.V > 0) {
         countLaunch();
@@ -526,9 +530,9 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
     if (md.H > 0) {
         countLaunch();
         const int blocks = std::min((md.H + 255) / 256, 152 * 8);
-        kFanKeys<<<blocks, 256, 0, s>>>(he, md, slow, &ctr->slowFans, isKey, status);
+        kFanKeys<<<blocks, 256, 0, s>>>(he, md, slow, &ctr->slowFans, isKey, keyMark, status);
         countLaunch();
-        kFanCount<<<blocks, 256, 0, s>>>(he, md, slow, &ctr->slowFans, isKey, fans, status);
+        kFanCount<<<blocks, 256, 0, s>>>(he, md, slow, &ctr->slowFans, isKey, keyMark, fans, status);
     }
     if (md.V > 0) {
         countLaunch();
