@@ -157,18 +157,20 @@ MDMC_API void mdmc_destroy(mdmc_context* context);
  * setSplittingStep, DualMarchingCubes.h:143-145) */
 MDMC_API mdmc_status mdmc_set_options(mdmc_context* context, const mdmc_options* options);
 
-/* Per-kernel timing (no reference counterpart; the reference times stages).
- * Each timed kernel costs its run two CUDA event records on the stream, about
- * 3.5 us of GPU time on a GB300, so kernels are timed only when their bit is
- * set: MDMC_TIME_* bits, default 0.  The stage times (ms_dmc .. ms_total) are
- * always taken. */
+/* Timing.  Every CUDA event record costs the run's stream about 1.7 us of GPU
+ * time on a GB300, so the times are taken only for what the MDMC_TIME_* bits
+ * select.  MDMC_TIME_STAGES: the stage times ms_dmc .. ms_total (the
+ * reference's Performance result; on by default).  The kernel bits time one
+ * kernel each (two records per run; no reference counterpart; off by
+ * default).  Fields not timed read 0. */
 #define MDMC_TIME_REFINE 1u   /* ms_refine */
 #define MDMC_TIME_COUNT 2u    /* ms_count */
 #define MDMC_TIME_EMIT 4u     /* ms_emit */
 #define MDMC_TIME_QUADS 8u    /* ms_quads */
 #define MDMC_TIME_TABLE 16u   /* ms_table */
 #define MDMC_TIME_VERTICES 32u /* ms_vertices */
-#define MDMC_TIME_ALL 63u
+#define MDMC_TIME_STAGES 64u /* ms_dmc, ms_halfedge, ms_repair, ms_detect, ms_total */
+#define MDMC_TIME_ALL 127u
 MDMC_API mdmc_status mdmc_set_kernel_timing(mdmc_context* context, uint32_t kernels);
 MDMC_API mdmc_status mdmc_get_options(const mdmc_context* context, mdmc_options* options);
 

@@ -129,7 +129,8 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "cuda error", 3: "out of memory", 4
 # kernels mdmc_set_kernel_timing can time (MDMC_TIME_* of mdmc.h) -> Stats field
 KERNEL_TIMING = {"refine": (1, "ms_refine"), "count": (2, "ms_count"), "emit": (4, "ms_emit"),
                  "quads": (8, "ms_quads"), "table": (16, "ms_table"), "vertices": (32, "ms_vertices")}
-TIME_ALL = 63
+TIME_STAGES = 64  # the stage times (on by default)
+TIME_ALL = 127
 
 
 class MDMCError(RuntimeError):
@@ -360,10 +361,14 @@ class DualMarchingCubes:
     def set_option(self, name, value):
         self._set(name, value)
 
-    def set_kernel_timing(self, kernels):
-        """Times the named kernels (keys of KERNEL_TIMING, or an MDMC_TIME_*
-        mask) in the following runs' stats; each costs two event records."""
-        mask = kernels if isinstance(kernels, int) else sum(KERNEL_TIMING[k][0] for k in kernels)
+    def set_kernel_timing(self, kernels, stages=True):
+        """Times the named kernels (keys of KERNEL_TIMING; or an MDMC_TIME_*
+        mask, used as given) and, with stages, the stage times in the following
+        runs' stats; every timed item costs event records on the stream."""
+        if isinstance(kernels, int):
+            mask = kernels
+        else:
+            mask = sum(KERNEL_TIMING[k][0] for k in kernels) | (TIME_STAGES if stages else 0)
         self._ctx.check(self._ctx.lib.mdmc_set_kernel_timing(self._ctx.handle, mask))
 
     def run(self, iso_value, grid, stream=None):

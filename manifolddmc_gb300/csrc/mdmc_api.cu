@@ -135,7 +135,7 @@ struct mdmc_context {
     int evAt[6] = {0, 1, 2, 3, 4, 5};  // the event that marks stage boundary k
     // per-kernel events: refine, count, emit, quads, table, vertices (begin/end each)
     cudaEvent_t kev[12] = {};
-    uint32_t kernelTiming = 0;  // MDMC_TIME_* bits: kernels whose event pairs are recorded
+    uint32_t kernelTiming = MDMC_TIME_STAGES;  // MDMC_TIME_* bits: what gets event records
     cudaEvent_t countsEv = nullptr;  // the DMC counts have reached the host
     float msRefine = 0.f;
     bool haveMesh = false;
@@ -147,6 +147,7 @@ namespace {
 // stage boundary k (ev[k]); when nothing ran since boundary k - 1 the
 // previous boundary's event stands for it (an event record costs ~1.7 us)
 inline void markStage(mdmc_context* c, int k, bool ran, cudaStream_t s) {
+    if (!(c->kernelTiming & MDMC_TIME_STAGES)) return;
     if (ran || k == 0) {
         cudaEventRecord(c->ev[k], s);
         c->evAt[k] = k;
@@ -1137,9 +1138,11 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->stats.split_iterations = iterations;
     c->stats.anomalies = (int64_t)hc.status;
     float ms[5] = {0, 0, 0, 0, 0};
-    for (int k = 0; k < 4; ++k)
-        if (cudaEventElapsedTime(&ms[k], c->ev[c->evAt[k]], c->ev[c->evAt[k + 1]]) != cudaSuccess) ms[k] = 0.f;
-    if (cudaEventElapsedTime(&ms[4], c->ev[c->evAt[0]], c->ev[c->evAt[5]]) != cudaSuccess) ms[4] = 0.f;
+    if (c->kernelTiming & MDMC_TIME_STAGES) {
+        for (int k = 0; k < 4; ++k)
+            if (cudaEventElapsedTime(&ms[k], c->ev[c->evAt[k]], c->ev[c->evAt[k + 1]]) != cudaSuccess) ms[k] = 0.f;
+        if (cudaEventElapsedTime(&ms[4], c->ev[c->evAt[0]], c->ev[c->evAt[5]]) != cudaSuccess) ms[4] = 0.f;
+    }
     c->stats.ms_dmc = ms[0];
     c->stats.ms_halfedge = ms[1];
     c->stats.ms_repair = ms[2];

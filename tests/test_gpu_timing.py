@@ -1,6 +1,6 @@
-"""Per-kernel timing is opt-in (mdmc_set_kernel_timing): selected kernels get
-positive times, the others read 0, the stage times are always taken, and
-timing changes no result."""
+"""Timing is selected per item (mdmc_set_kernel_timing): selected kernels get
+positive times, the others read 0, the stage times are on by default and can
+be switched off, and timing changes no result."""
 import numpy as np
 import pytest
 
@@ -40,7 +40,18 @@ def test_kernel_timing_mask_selects_fields():
         assert np.array_equal(np.asarray(getattr(base, name)).view(np.uint8), np.asarray(getattr(timed, name)).view(np.uint8)), name
 
 
+def test_stage_timing_can_be_switched_off():
+    grid, iso = _grid()
+    dmc = mdmc.DualMarchingCubes()
+    dmc.set_kernel_timing(["quads"], stages=False)
+    stages = dmc.run(iso, grid)
+    assert all(v == 0.0 for v in stages.values()), stages
+    assert dmc.stats.ms_quads > 0
+    dmc.set_kernel_timing([])
+    assert dmc.run(iso, grid)["Total"] > 0 and dmc.stats.ms_quads == 0.0
+
+
 def test_kernel_timing_rejects_unknown_bits():
     dmc = mdmc.DualMarchingCubes()
     with pytest.raises(mdmc.MDMCError):
-        dmc.set_kernel_timing(64)
+        dmc.set_kernel_timing(128)
