@@ -197,6 +197,33 @@ __device__ inline uint64_t asymptoticContours(const float s[8], float iso) {
     return c;
 }
 
+// edge -> contour map of a packed contour word (2 bits per edge, contour t
+// of every edge of contour t) and, in bits 24-26, the number of contours
+__host__ __device__ constexpr uint32_t contourEdgeMap(uint64_t c) {
+    int n = 0;
+    for (int t = 0; t < 4; ++t) n += ((c >> (4 * t)) & 0xF) != 0 ? 1 : 0;
+    uint32_t emap = 0;
+    int before = 0;
+    for (int t = 0; t < n; ++t) {
+        const int sz = (int)((c >> (4 * t)) & 0xF);
+        for (int i = 0; i < sz; ++i) emap |= (uint32_t)t << (2 * (int)((c >> (16 + 4 * (before + i))) & 0xF));
+        before += sz;
+    }
+    return emap | ((uint32_t)n << 24);
+}
+
+// contourEdgeMap of every case's table word, made at compile time
+struct EdgeMapTable {
+    uint32_t v[256];
+};
+constexpr unsigned long long kContourWordsConst[256] = {MDMC_CONTOUR_WORDS};
+constexpr EdgeMapTable makeEdgeMapTable() {
+    EdgeMapTable t{};
+    for (int i = 0; i < 256; ++i) t.v[i] = contourEdgeMap(kContourWordsConst[i]);
+    return t;
+}
+__device__ const EdgeMapTable kEdgeMapTable = makeEdgeMapTable();
+
 // contours of an active cell: table word or asymptotic decider
 __device__ __forceinline__ uint64_t cellContours(int cs, const float s[8], float iso, const uint64_t* table) {
     if (caseIsAmbiguous(cs)) return asymptoticContours(s, iso);

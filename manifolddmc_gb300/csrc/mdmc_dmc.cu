@@ -90,9 +90,12 @@ __global__ void __launch_bounds__(256) kCoarseMayCross(const float* __restrict__
         const int z = (int)(row / ncy);
         float lo = INFINITY, hi = -INFINITY, mag = 0.f;
         bool nan = false;
+        // (coarse grids have fewer than 2^32 samples: 32-bit offsets)
+        const uint32_t sy = (uint32_t)cX, sz = (uint32_t)cX * (uint32_t)cY;
+        const uint32_t base = (uint32_t)z * sz + (uint32_t)y * sy + (uint32_t)x;
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
-            const float v = __ldg(c + ((int64_t)(z + ((k >> 2) & 1)) * cY + (y + ((k >> 1) & 1))) * cX + (x + (k & 1)));
+            const float v = __ldg(c + (base + ((k >> 2) & 1) * sz + ((k >> 1) & 1) * sy + (k & 1)));
             nan = nan || (v != v);
             lo = fminf(lo, v);
             hi = fmaxf(hi, v);
@@ -840,8 +843,8 @@ template <class View>
 __global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint32_t* __restrict__ cellIds,
                                                    ActiveCell* __restrict__ act, int2* __restrict__ counts,
                                                    int numActive, const int* numActiveDev, uint32_t* status) {
-    __shared__ uint64_t table[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kContourTable[i];
+    __shared__ uint32_t edgeMaps[256];  // per case: edge -> contour map | contours << 24
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) edgeMaps[i] = kEdgeMapTable.v[i];
     __syncthreads();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (numActiveDev) numActive = min(max(*numActiveDev, 0), numActive);
@@ -868,15 +871,11 @@ __global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint
         atomicOr(status, kStatusCountMismatch);
         return;
     }
-    const uint64_t c = cellContours(cs, s, iso, table);
-    uint32_t emap = 0;
-    int before = 0;
-    const int n = numContours(c);
-    for (int t = 0; t < n; ++t) {
-        const int sz = nib(c, t);
-        for (int i = 0; i < sz; ++i) emap |= (uint32_t)t << (2 * (int)((c >> (16 + 4 * (before + i))) & 0xF));
-        before += sz;
-    }
+    // the contours' edge map: the case's table entry, or from the asymptotic
+    // decider's contours for the ambiguous cases
+    const uint32_t em = caseIsAmbiguous(cs) ? contourEdgeMap(asymptoticContours(s, iso)) : edgeMaps[cs];
+    const int n = (int)(em >> 24);
+    const uint32_t emap = em & 0xFFFFFFu;
     ActiveCell rec;
     rec.cell = cell;
     rec.qbase = 0;
