@@ -90,7 +90,7 @@ __device__ __forceinline__ int faceCorner(int f, int i) {
 }
 
 // a face of the cell has the diagonal sign pattern (four crossing edges)
-__host__ __device__ inline bool caseHasDiagonalFace(int c) {
+__host__ __device__ constexpr bool caseHasDiagonalFace(int c) {
     const unsigned short fc[6] = {0x3120, 0x6475, 0x1504, 0x7362, 0x2064, 0x7531};
     for (int f = 0; f < 6; ++f) {
         int m = 0;
@@ -103,7 +103,7 @@ __host__ __device__ inline bool caseHasDiagonalFace(int c) {
 // (s_triangleAmbiguities == MC_AMBIGUOUS, D/DualMarchingCubes.cpp:301) exactly
 // when a face of the cell has the diagonal sign pattern, or when the inside
 // corners are just the two ends of one cell diagonal (or all but those two).
-__host__ __device__ inline bool caseIsAmbiguous(int c) {
+__host__ __device__ constexpr bool caseIsAmbiguous(int c) {
     if (caseHasDiagonalFace(c)) return true;
     for (int i = 0; i < 4; ++i) {
         int pair = (1 << i) | (1 << (7 - i));
@@ -212,17 +212,32 @@ __host__ __device__ constexpr uint32_t contourEdgeMap(uint64_t c) {
     return emap | ((uint32_t)n << 24);
 }
 
-// contourEdgeMap of every case's table word, made at compile time
-struct EdgeMapTable {
-    uint32_t v[256];
+// Per-case tables made at compile time, with the ambiguous cases (which take
+// the asymptotic decider instead) tagged so that one shared-memory read both
+// classifies a cell and gives its table entry:
+// - contour words: 0 = ambiguous with a diagonal face, 1 = ambiguous without
+//   (a real word's first contour size is at least 3);
+// - edge maps (contourEdgeMap of the word): 0xFFFFFFFF = ambiguous.
+struct CaseTables {
+    unsigned long long words[256];
+    uint32_t edgeMaps[256];
 };
 constexpr unsigned long long kContourWordsConst[256] = {MDMC_CONTOUR_WORDS};
-constexpr EdgeMapTable makeEdgeMapTable() {
-    EdgeMapTable t{};
-    for (int i = 0; i < 256; ++i) t.v[i] = contourEdgeMap(kContourWordsConst[i]);
+constexpr CaseTables makeCaseTables() {
+    CaseTables t{};
+    for (int i = 0; i < 256; ++i) {
+        const bool amb = caseIsAmbiguous(i);
+        t.words[i] = amb ? (caseHasDiagonalFace(i) ? 0ull : 1ull) : kContourWordsConst[i];
+        t.edgeMaps[i] = amb ? 0xFFFFFFFFu : contourEdgeMap(kContourWordsConst[i]);
+    }
     return t;
 }
-__device__ const EdgeMapTable kEdgeMapTable = makeEdgeMapTable();
+__device__ const CaseTables kCaseTables = makeCaseTables();
+
+// contours of an active cell from a tagged word table (above)
+__device__ __forceinline__ uint64_t taggedContours(uint64_t word, const float s[8], float iso) {
+    return word <= 1 ? asymptoticContours(s, iso) : word;
+}
 
 // contours of an active cell: table word or asymptotic decider
 __device__ __forceinline__ uint64_t cellContours(int cs, const float s[8], float iso, const uint64_t* table) {

@@ -844,7 +844,7 @@ __global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint
                                                    ActiveCell* __restrict__ act, int2* __restrict__ counts,
                                                    int numActive, const int* numActiveDev, uint32_t* status) {
     __shared__ uint32_t edgeMaps[256];  // per case: edge -> contour map | contours << 24
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) edgeMaps[i] = kEdgeMapTable.v[i];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) edgeMaps[i] = kCaseTables.edgeMaps[i];
     __syncthreads();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (numActiveDev) numActive = min(max(*numActiveDev, 0), numActive);
@@ -873,7 +873,8 @@ __global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint
     }
     // the contours' edge map: the case's table entry, or from the asymptotic
     // decider's contours for the ambiguous cases
-    const uint32_t em = caseIsAmbiguous(cs) ? contourEdgeMap(asymptoticContours(s, iso)) : edgeMaps[cs];
+    uint32_t em = edgeMaps[cs];
+    if (em == 0xFFFFFFFFu) em = contourEdgeMap(asymptoticContours(s, iso));
     const int n = (int)(em >> 24);
     const uint32_t emap = em & 0xFFFFFFu;
     ActiveCell rec;
@@ -928,7 +929,7 @@ __global__ void __launch_bounds__(128, VerticesBlocks<Stencil>::value) kVertices
         numVertices = v;
     }
     __shared__ uint64_t table[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kContourTable[i];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) table[i] = kCaseTables.words[i];  // ambiguous ones tagged
     __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= numActive) return;
@@ -941,7 +942,8 @@ __global__ void __launch_bounds__(128, VerticesBlocks<Stencil>::value) kVertices
     const Stencil st(g, x, y, z);
     float s[8];
     stencilCorners(st, s);
-    const uint64_t c = cellContours(cs, s, iso, table);
+    const uint64_t word = table[cs];
+    const uint64_t c = taggedContours(word, s, iso);
     const int n = numContours(c);
     if (vb < 0 || vb + n > numVertices) {
         atomicOr(status, kStatusCountMismatch);
@@ -949,7 +951,7 @@ __global__ void __launch_bounds__(128, VerticesBlocks<Stencil>::value) kVertices
     }
     F3 normals[8];
     stencilGradients(st, s, g.deltas(), normals);
-    const bool diagonalFace = caseHasDiagonalFace(cs);
+    const bool diagonalFace = word == 0;  // (the tag of ambiguous cases with a diagonal face)
     int before = 0;
     for (int t = 0; t < n; ++t) {
         F3 q = f3(0.f, 0.f, 0.f);
