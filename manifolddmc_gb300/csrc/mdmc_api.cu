@@ -262,6 +262,7 @@ mdmc_status makeGridDesc(mdmc_context* c, const mdmc_grid* grid, float iso, Grid
         d.ref.fPow2 = (f & (f - 1)) == 0 ? 1 : 0;
         d.ref.invf = 1.0f / (float)f;
     }
+    setDivisors(d);
     d.ref.mayCross = nullptr;
     if (!d.refined) {
         if (!grid->samples) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "grid has no samples");

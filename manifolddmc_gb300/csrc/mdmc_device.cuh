@@ -307,7 +307,30 @@ struct SurfaceIterator {
 // float operations, so it returns exactly the values the dense refined grid
 // would hold without that grid ever being written.
 // ---------------------------------------------------------------------------
+// Unsigned division by a divisor fixed for a launch, as a multiply-high and
+// two shifts (Granlund and Montgomery, "Division by Invariant Integers using
+// Multiplication", PLDI 1994, section 4): for 1 <= d < 2^31 and every 32-bit
+// n, n / d = (t + ((n - t) >> s1)) >> s2 with t = umulhi(m, n),
+// l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, s1 = min(l, 1),
+// s2 = max(l - 1, 0).  Exact; made on the host.
+struct FastDiv {
+    uint32_t d = 1, m = 1, s1 = 0, s2 = 0;
+    FastDiv() = default;
+    __host__ explicit FastDiv(uint32_t div) : d(div < 1 ? 1 : div) {
+        uint32_t l = 0;
+        while ((1ull << l) < d) ++l;
+        m = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+        s1 = l > 0 ? 1 : 0;
+        s2 = l > 0 ? l - 1 : 0;
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t n) const {
+        const uint32_t t = __umulhi(m, n);
+        return (t + ((n - t) >> s1)) >> s2;
+    }
+};
+
 struct GridGeom {
+    FastDiv divX, divY;  // by X and Y (decoding linear sample ids; set by setDivisors)
     int X, Y, Z;       // samples of the (refined) grid
     float ox, oy, oz;  // origin
     float dx, dy, dz;  // spacing
@@ -338,6 +361,7 @@ struct RefinedView : GridGeom {
 
     float invf;                // 1 / f when f is a power of two (then i * invf == i / f exactly)
     int fPow2;
+    FastDiv divCX1, divCY1;    // by the coarse cells per row and per layer (set by setDivisors)
 
     // sample index of the unpadded refined grid (refineGrid's clamp and shift)
     __device__ __forceinline__ int unpad(int i, int n) const { return pad ? min(max(i, 1), n - 2) - 1 : i; }

@@ -76,7 +76,8 @@ void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int p
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) kCoarseMayCross(const float* __restrict__ c, int cX, int cY, int cZ, float iso,
                                                        uint32_t* __restrict__ bits, int64_t numCells,
-                                                       uint32_t* __restrict__ list, unsigned long long* listCount) {
+                                                       uint32_t* __restrict__ list, unsigned long long* listCount,
+                                                       FastDiv divCX1, FastDiv divCY1) {
     __shared__ unsigned warpCount[8];
     __shared__ unsigned long long blockBase;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -84,10 +85,10 @@ __global__ void __launch_bounds__(256) kCoarseMayCross(const float* __restrict__
     if (i < numCells) {
         // fewer than 2^32 coarse cells: 32-bit division
         const uint32_t iu = (uint32_t)i, ncx = (uint32_t)(cX - 1), ncy = (uint32_t)(cY - 1);
-        const uint32_t row = iu / ncx;
+        const uint32_t row = divCX1.div(iu), layer = divCY1.div(row);
         const int x = (int)(iu - row * ncx);
-        const int y = (int)(row % ncy);
-        const int z = (int)(row / ncy);
+        const int y = (int)(row - layer * ncy);
+        const int z = (int)layer;
         float lo = INFINITY, hi = -INFINITY, mag = 0.f;
         bool nan = false;
         // (coarse grids have fewer than 2^32 samples: 32-bit offsets)
@@ -136,7 +137,8 @@ void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, uint3
     const int64_t n = (int64_t)(g.cX - 1) * (g.cY - 1) * (g.cZ - 1);
     if (n <= 0) return;
     countLaunch();
-    kCoarseMayCross<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g.c, g.cX, g.cY, g.cZ, iso, bits, n, list, listCount);
+    kCoarseMayCross<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(g.c, g.cX, g.cY, g.cZ, iso, bits, n, list, listCount,
+                                                                g.divCX1, g.divCY1);
 }
 
 
@@ -458,10 +460,10 @@ __global__ void __launch_bounds__(32 * kBlockMaskWarps, 4) kBlockMask(RefinedVie
         }
         // coarse cells number fewer than 2^32 (refined grids have fewer samples)
         const uint32_t cu = (uint32_t)ci, ncx = (uint32_t)(g.cX - 1), ncy = (uint32_t)(g.cY - 1);
-        const uint32_t crow = cu / ncx;
+        const uint32_t crow = g.divCX1.div(cu), clayer = g.divCY1.div(crow);
         const int mx = (int)(cu - crow * ncx);
-        const int my = (int)(crow % ncy);
-        const int mz = (int)(crow / ncy);
+        const int my = (int)(crow - clayer * ncy);
+        const int mz = (int)clayer;
         const int xs = blockStart(g, mx), xe = blockEnd(g, mx, g.X, g.cX);
         const int ys = blockStart(g, my), ye = blockEnd(g, my, g.Y, g.cY);
         const int zs = blockStart(g, mz), ze = blockEnd(g, mz, g.Z, g.cZ);
@@ -850,8 +852,8 @@ __global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint
     if (numActiveDev) numActive = min(max(*numActiveDev, 0), numActive);
     if (j >= numActive) return;
     const uint32_t cell = cellIds[j];
-    const uint32_t line = cell / (uint32_t)g.X;
-    const int x = (int)(cell - line * (uint32_t)g.X), y = (int)(line % (uint32_t)g.Y), z = (int)(line / (uint32_t)g.Y);
+    const uint32_t line = g.divX.div(cell), layer = g.divY.div(line);
+    const int x = (int)(cell - line * (uint32_t)g.X), y = (int)(line - layer * (uint32_t)g.Y), z = (int)layer;
     if (x >= g.X - 1 || y >= g.Y - 1 || z >= g.Z - 1) {
         atomicOr(status, kStatusCountMismatch);
         return;
@@ -934,9 +936,10 @@ __global__ void __launch_bounds__(128, VerticesBlocks<Stencil>::value) kVertices
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= numActive) return;
     const ActiveCell rec = act[i];
-    const int x = (int)(rec.cell % (uint32_t)g.X);
-    const int y = (int)((rec.cell / (uint32_t)g.X) % (uint32_t)g.Y);
-    const int z = (int)(rec.cell / ((uint32_t)g.X * (uint32_t)g.Y));
+    const uint32_t line = g.divX.div(rec.cell), layer = g.divY.div(line);
+    const int x = (int)(rec.cell - line * (uint32_t)g.X);
+    const int y = (int)(line - layer * (uint32_t)g.Y);
+    const int z = (int)layer;
     const int vb = rec.pad;  // first vertex id
     const int cs = (int)(rec.info & 255u);
     const Stencil st(g, x, y, z);
@@ -1027,6 +1030,7 @@ struct CellIndex {
     const uint32_t* mask;
     const int* first;
     int X, Y, Z, W;
+    FastDiv divX, divY;  // by X and Y (decoding linear cell ids)
     // index of cell (x,y,z) in the active-cell list, -1 if inactive or outside
     __device__ __forceinline__ int find(int x, int y, int z) const {
         if ((unsigned)x > (unsigned)(X - 2) || (unsigned)y > (unsigned)(Y - 2) || (unsigned)z > (unsigned)(Z - 2))
@@ -1098,9 +1102,9 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
     if (ok) {
         const ActiveCell rec = act[j];
         const int cs = (int)(rec.info & 255u);
-        const uint32_t line = rec.cell / (uint32_t)ix.X;
-        const int px = (int)(rec.cell - line * (uint32_t)ix.X), py = (int)(line % (uint32_t)ix.Y),
-                  pz = (int)(line / (uint32_t)ix.Y);
+        const uint32_t line = ix.divX.div(rec.cell), layer = ix.divY.div(line);
+        const int px = (int)(rec.cell - line * (uint32_t)ix.X), py = (int)(line - layer * (uint32_t)ix.Y),
+                  pz = (int)layer;
         // the rank-th owned axis of the owner
         int axis = -1, rank = q - rec.qbase;
 #pragma unroll
@@ -1418,6 +1422,8 @@ void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, con
     ix.Y = Y;
     ix.Z = Z;
     ix.W = W;
+    ix.divX = FastDiv((uint32_t)X);
+    ix.divY = FastDiv((uint32_t)Y);
     kQuads<<<(qEnd - qBegin + 255) / 256, 256, 0, s>>>(act, quadOwner, numActive, ix, he, faceFirst, faceAttr, vflags,
                                                         reinterpret_cast<uint32_t*>(heValence), nmList, nmCapacity,
                                                         numQuads, numVertices, quadsOut, vertexHE, ctr, qBegin,

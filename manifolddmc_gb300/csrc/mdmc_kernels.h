@@ -72,6 +72,15 @@ struct GridDesc {
     const GridGeom& geom() const { return refined ? static_cast<const GridGeom&>(ref) : static_cast<const GridGeom&>(plain); }
 };
 
+// the divisors of both views, once their dims are set
+inline void setDivisors(GridDesc& d) {
+    const FastDiv dx((uint32_t)d.plain.X), dy((uint32_t)d.plain.Y);
+    d.plain.divX = d.ref.divX = dx;
+    d.plain.divY = d.ref.divY = dy;
+    d.ref.divCX1 = FastDiv((uint32_t)(d.ref.cX > 1 ? d.ref.cX - 1 : 1));
+    d.ref.divCY1 = FastDiv((uint32_t)(d.ref.cY > 1 ? d.ref.cY - 1 : 1));
+}
+
 // the (sorted) ids of one edge bucket with four or more halfedges, as listed
 // in the non-manifold edge list
 struct NMIds {

@@ -174,6 +174,7 @@ extern "C" MDMC_API mdmc_status mdmc_count_cells_noalloc(const mdmc_grid* grid, 
         d.ref.fPow2 = (f & (f - 1)) == 0 ? 1 : 0;
         d.ref.invf = 1.0f / (float)f;
     }
+    setDivisors(d);
     d.ref.mayCross = nullptr;
     int64_t coarseCells = 0;
     if (!d.refined) {
