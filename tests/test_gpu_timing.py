@@ -55,3 +55,26 @@ def test_kernel_timing_rejects_unknown_bits():
     dmc = mdmc.DualMarchingCubes()
     with pytest.raises(mdmc.MDMCError):
         dmc.set_kernel_timing(128)
+
+
+def test_fan_key_marks_wrap_around():
+    """Fan detection marks its keys with a per-pass number (1..255) instead of
+    clearing them every run; 300 runs on one context pass the wrap-around and
+    must keep giving the first run's non-manifold vertices."""
+    seen_nm = False
+    for which in (0, 1):
+        for pad in (False, True):
+            vol, dims, origin, spacing = mdmc.generate_edge_case(which)
+            grid = mdmc.UniformGrid(vol, dims, origin=origin, spacing=spacing, add_zero_boundary=pad)
+            dmc = mdmc.DualMarchingCubes()
+            dmc.run(900.0, grid)
+            first = dmc.get_halfedge_mesh()
+            nm = dmc.get_num_non_manifold_vertices()
+            seen_nm = seen_nm or nm > 0
+            for i in range(300):
+                dmc.run(900.0, grid)
+                assert dmc.get_num_non_manifold_vertices() == nm, (which, pad, i)
+                if i % 50 == 49:
+                    m = dmc.get_halfedge_mesh()
+                    assert np.array_equal(m.vertex_flags, first.vertex_flags), (which, pad, i)
+    assert seen_nm  # the path that marks fan keys ran
