@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-noise", action="store_true")
     ap.add_argument("--fit", action="store_true",
                     help="also time 200 Adam steps of the sphere-to-torus fit (brute-force Chamfer in torch)")
     args = ap.parse_args()
@@ -323,6 +324,9 @@ def run_ours(args, rank, world, local):
         e2e = {"value": round(world * cells / (m / 1e3) / 1e6, 2), "unit": "Mcells/s", "ms_per_step": round(m, 4),
                "h2d_bytes_per_step": int(host_in.numel() * 4), "d2h_bytes_per_step": int(d2h)}
 
+    noise = None
+    if rank == 0 and not args.no_noise:
+        noise = measure_noise(args, dev, stream, flush)
     batched = None
     if rank == 0 and not args.no_batch:
         batched = measure_batch(args, dev)
@@ -351,6 +355,7 @@ def run_ours(args, rank, world, local):
             "e2e": e2e,
             "adjoint": adjoint,
             "batch": batched,
+            "noise": noise,
             "gpu_launches": launches,
             "clocks": clocks.summary(),
         }
@@ -410,6 +415,68 @@ def measure_adjoint(args, dev, stream, flush):
             "fwd_adjoint_ms": round(b, 4), "ratio": round(b / f, 3),
             "gradient_check": "max |gpu - FP64 oracle| <= 1e-5 * max |FP64| (tests/test_gpu_adjoint.py); "
                               "FP64 oracle vs FP64 central differences h=1e-4 (tests/test_adjoint_oracle.py)"}
+
+
+def measure_noise(args, dev, stream, flush):
+    """The uniform-noise workloads, the worst case for ambiguous cells and
+    non-manifold edges (every non-manifold edge goes through the splitter):
+    256^3 samples (iso 0.5) and 513^3 samples = 512^3 cells, the headline cell
+    count.  Grid resident in HBM, one mdmc_run per step with the stage times
+    (CUDA events inside the library) and the step time (CUDA events around
+    the call), L2 flushed before every step; the 512^3 grid needs about 150 GB
+    of device memory and is skipped on smaller devices."""
+    import torch
+
+    import manifolddmc_gb300 as mdmc
+    from manifolddmc_gb300.workloads import CONFIGS
+    peak, peak_kind = peaks()
+    out = {}
+    for name, steps in (("noise256", 5), ("noise513", 3)):
+        desc, gen, iso, refine, pad = CONFIGS[name]
+        free, total = torch.cuda.mem_get_info(dev)
+        if name == "noise513" and total < 200e9:
+            out[name] = {"skipped": "needs a device with 200 GB or more"}
+            continue
+        vol = gen()
+        d_in = torch.from_numpy(vol).to(dev)
+        del vol
+        dims = [d_in.shape[2], d_in.shape[1], d_in.shape[0]]
+        dmc = mdmc.DualMarchingCubes()
+        grid = mdmc.UniformGrid(d_in, dims, stream=stream)
+        ms, stages = [], {"dmc": [], "halfedge": [], "repair": [], "detect": []}
+        for i in range(1 + steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            dmc.run(iso, grid, stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            if i:
+                ms.append(e0.elapsed_time(e1))
+                st = dmc.stats
+                for k, f in (("dmc", "ms_dmc"), ("halfedge", "ms_halfedge"), ("repair", "ms_repair"),
+                             ("detect", "ms_detect")):
+                    stages[k].append(float(getattr(st, f)))
+        st = dmc.stats
+        cells = (dims[0] - 1) * (dims[1] - 1) * (dims[2] - 1)
+        t = float(np.mean(ms))
+        sizes = {"samples_in": dims[0] * dims[1] * dims[2], "samples": dims[0] * dims[1] * dims[2],
+                 "dmc_vertices": int(st.num_dmc_vertices), "dmc_quads": int(st.num_dmc_quads)}
+        b = survey_bytes(sizes)
+        out[name] = {"description": desc, "steps": steps, "ms_per_step": round(t, 3),
+                     "mcells_s": round(cells / (t / 1e3) / 1e6, 1),
+                     "stage_ms": {k: round(float(np.mean(v)), 3) for k, v in stages.items()},
+                     "whole_step_bytes": b, "whole_step_gbs": round(b / (t / 1e3) / 1e9, 1),
+                     "whole_step_frac": round(b / (t / 1e3) / 1e9 / peak, 4), "peak_kind": peak_kind,
+                     "dmc_vertices": int(st.num_dmc_vertices), "dmc_quads": int(st.num_dmc_quads),
+                     "final_vertices": int(dmc.mesh.num_vertices), "final_faces": int(dmc.mesh.num_faces),
+                     "split_iterations": int(st.split_iterations), "edges4": int(st.num_edges4),
+                     "non_manifold_vertices": int(st.num_non_manifold_vertices)}
+        del dmc, grid, d_in
+        torch.cuda.synchronize(dev)
+        torch.cuda.empty_cache()
+    return out
 
 
 def measure_batch(args, dev):

@@ -401,7 +401,9 @@ MDMC_API void mdmc_case_tables(uint64_t contour_words[256], uint8_t ambiguous[25
  * any work.  Calls that overlap on the GPU race on the scratch: serialize
  * them.  The first call on a device (with that device current) looks up the
  * scratch there, which loads this code onto the device; make it before any
- * stream capture.  message (may be NULL) receives an error description of at
+ * stream capture.  After a cudaDeviceReset the next call on that device finds
+ * a new context and looks the scratch up again (a set-up call once more).
+ * message (may be NULL) receives an error description of at
  * most message_len bytes. */
 MDMC_API mdmc_status mdmc_count_cells_noalloc(const mdmc_grid* grid, float iso_value, int64_t* totals, void* stream,
                                               char* message, int message_len);

@@ -13,7 +13,10 @@
 // on a device and keeping the last call's contents:
 //   g_rowScratch     one int4 per x-row of cells, kMaxRows rows (4 MiB);
 //   g_mayCrossScratch one bit per coarse cell of a refined grid,
-//                    kMaxCoarseCells cells (2 MiB).
+//                    kMaxCoarseCells cells (2 MiB), plus one spare word: the
+//                    refined row walker loads the word after a row's first
+//                    word too (its bits are masked off), as mdmc_run's own
+//                    bit mask allows for.
 // Every call rewrites all the words it reads (the count kernel writes each
 // row's record, the coarse pre-pass each word of its bit mask, the reduction
 // writes the caller's totals outright), so nothing has to start at zero.
@@ -23,7 +26,10 @@
 // Device set-up: the first call on a device, with that device current, looks
 // up the arrays' addresses (cudaGetSymbolAddress), which also makes the CUDA
 // runtime load this file's module (and with it the arrays) on that device.
-// Make that first call before any stream capture begins.
+// Make that first call before any stream capture begins.  The addresses are
+// kept per device together with the id of the context they belong to; when
+// the caller has reset the device (cudaDeviceReset) the next call finds a new
+// context and looks them up again, which is then again a set-up call.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -42,13 +48,18 @@ constexpr int64_t kMaxMayCrossWords = kMaxCoarseCells / 32;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) int4 g_rowScratch[kMaxRows];
-static __device__ __align__(256) uint32_t g_mayCrossScratch[kMaxMayCrossWords];
+static __device__ __align__(256) uint32_t g_mayCrossScratch[kMaxMayCrossWords + 1];
 
 struct DeviceScratch {
     bool ready = false;
+    unsigned long long context = 0;  // cuCtxGetId of the context the addresses belong to
     int4* rows = nullptr;
     uint32_t* mayCross = nullptr;
 };
+
+// the driver's context id calls, reached through the runtime (no link to libcuda)
+typedef int (*CtxGetCurrentFn)(void** ctx);
+typedef int (*CtxGetIdFn)(void* ctx, unsigned long long* id);
 
 std::mutex g_setupLock;
 DeviceScratch g_scratch[kMaxDevices];
@@ -57,11 +68,36 @@ void setMessage(char* message, int len, const char* text) {
     if (message && len > 0) std::snprintf(message, (size_t)len, "%s", text);
 }
 
-// once per device, with that device current
+// id of the current context, 0 when there is none yet (or the driver lacks the calls)
+unsigned long long currentContextId() {
+    static CtxGetCurrentFn getCurrent = nullptr;
+    static CtxGetIdFn getId = nullptr;
+    static bool looked = false;
+    if (!looked) {
+        looked = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            getCurrent = reinterpret_cast<CtxGetCurrentFn>(f);
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            getId = reinterpret_cast<CtxGetIdFn>(f);
+        (void)cudaGetLastError();
+    }
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (!getCurrent || !getId || getCurrent(&ctx) != 0 || !ctx || getId(ctx, &id) != 0) return 0;
+    return id;
+}
+
+// once per device and context, with that device current
 cudaError_t scratchFor(int device, DeviceScratch& out) {
     std::lock_guard<std::mutex> lock(g_setupLock);
     DeviceScratch& d = g_scratch[device];
-    if (!d.ready) {
+    const unsigned long long ctx = currentContextId();
+    if (!d.ready || ctx == 0 || ctx != d.context) {
         void* rows = nullptr;
         void* may = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&rows, g_rowScratch);
@@ -70,6 +106,7 @@ cudaError_t scratchFor(int device, DeviceScratch& out) {
         if (e != cudaSuccess) return e;
         d.rows = static_cast<int4*>(rows);
         d.mayCross = static_cast<uint32_t*>(may);
+        d.context = currentContextId();  // the lookup has made the context current
         d.ready = true;
     }
     out = d;

@@ -21,7 +21,8 @@ with its intersected-edge masks (``e_pattern``, :123).  Each case's triangles
 are packed into one 64-bit word: bits 0-3 the triangle count, then the cell
 edges of the triangles, three per triangle, one nibble each, in table order.
 
-Run from the repository root:  python3 oracle/gen_mc_tables.py [reference_root]
+Run from the repository root:  python3 oracle/gen_mc_tables.py <reference_root>
+(or with the reference checkout named by the environment variable MDMC_REFERENCE).
 """
 import hashlib
 import json
@@ -29,7 +30,9 @@ import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MDMC_REFERENCE")
+if not REF:
+    sys.exit("usage: %s <reference_root>  (or set MDMC_REFERENCE)" % sys.argv[0])
 SRC = os.path.join(REF, "MarchingCubes/VisualDMC/src/DMC/DualMarchingCubes.cpp")
 SRC_MC = os.path.join(REF, "MarchingCubes/OriginalDMC/src/DualMarchingCubes.h")
 HERE = os.path.dirname(os.path.abspath(__file__))

@@ -339,3 +339,88 @@ def oracle_mean_ratio(positions, triangles):
     q = np.zeros(len(tri), np.float32)
     oracle().mdmc_oracle_mean_ratio(_p(pos), _p(tri), len(tri), _p(q))
     return q
+
+
+# ---------------------------------------------------------------------------
+# an independent manifold check (no oracle, no library code)
+# ---------------------------------------------------------------------------
+def manifold_report(halfedges, num_vertices, vertex_flags):
+    """Recomputes, from the halfedge array alone, what the reference's
+    statistics getters and fan detection report, with torch on whatever device
+    the arrays are on (they are converted to torch tensors).
+
+    - Edge valences: halfedges per undirected edge (min, max vertex), the
+      edge table's count (D/Halfedges/HalfedgeMesh.cu:1164-1239).
+    - Quads with k edges of valence > 2.
+    - Face fans: the fans around a vertex are the connected components of its
+      outgoing halfedges under h -> next(twin(h)) (one step of the cw walk of
+      D/PostProcesses/ManifoldCreator.cu:393-465; the ccw step is its inverse
+      where twins pair two opposite halfedges).  Found by pointer doubling
+      forwards and backwards, so no walk is repeated.  Compared with the
+      multi-fan flag only at "clean" vertices, whose incident edges all have 1
+      or 2 halfedges (where a 3-halfedge edge's cyclic twins make the walk
+      direction-dependent, the walk itself is the definition).
+
+    Returns a dict of counts and the tensors the assertions use."""
+    import torch
+
+    he = torch.as_tensor(halfedges)
+    dev = he.device
+    H = he.shape[0]
+    V = int(num_vertices)
+    flags = torch.as_tensor(vertex_flags).to(dev)
+    origin = he[:, 0].long()
+    nxt = he[:, 2].long()
+    twin = he[:, 3].long()
+    dest = origin[nxt]
+    lo = torch.minimum(origin, dest)
+    hi = torch.maximum(origin, dest)
+    key = lo * V + hi
+    uniq, inv, counts = torch.unique(key, return_inverse=True, return_counts=True)
+    valence = counts[inv]  # per halfedge
+    # quads with k edges of valence > 2 (each halfedge names its face; after
+    # the split a face's halfedges are no longer 4f..4f+3)
+    face = he[:, 1].long()
+    per_face = torch.bincount(face[valence > 2], minlength=int(face.max()) + 1 if H else 0)
+    qk = [int((per_face == k).sum()) for k in range(1, 5)]
+    # clean vertices: every incident edge has 1 or 2 halfedges
+    bad = valence > 2
+    unclean = torch.zeros(V, dtype=torch.bool, device=dev)
+    unclean[origin[bad]] = True
+    unclean[dest[bad]] = True
+    # fan components: successor s(h) = next(twin(h)) when it leaves the same vertex
+    idx = torch.arange(H, device=dev)
+    has = twin >= 0
+    cand = torch.where(has, nxt[torch.where(has, twin, 0)], idx)
+    succ = torch.where(has & (origin[cand] == origin), cand, idx)
+    pred = idx.clone()
+    moved = succ != idx
+    pred[succ[moved]] = idx[moved]
+
+    def path_min(step):
+        m = idx.clone()
+        p = step.clone()
+        for _ in range(40):  # 2^40 steps: any fan
+            m2 = torch.minimum(m, m[p])
+            p2 = p[p]
+            if torch.equal(m2, m) and torch.equal(p2, p):
+                break
+            m, p = m2, p2
+        return m
+
+    fan_key = torch.minimum(path_min(succ), path_min(pred))
+    is_key = fan_key == idx
+    fans = torch.bincount(origin[is_key], minlength=V)
+    multi = (flags & 8) != 0
+    clean = ~unclean
+    return {
+        "num_edges": int(uniq.numel()),
+        "edges_by_valence": {int(k): int(c) for k, c in zip(*torch.unique(counts, return_counts=True))},
+        "quads_with_non_manifold_edges": qk,
+        "num_flagged": int(multi.sum()),
+        "clean_vertices": int(clean.sum()),
+        "clean_mismatch": int(((fans > 1) != multi)[clean].sum()),
+        "clean_multi_fan": int(((fans > 1) & clean).sum()),
+        "twins_not_opposite_at_valence2": int(((valence == 2) & has & (origin[torch.where(has, twin, 0)] != dest)).sum()),
+        "twins_not_involutive_at_valence2": int(((valence == 2) & has & (twin[torch.where(has, twin, 0)] != idx)).sum()),
+    }

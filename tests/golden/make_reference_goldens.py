@@ -13,14 +13,17 @@ MarchingCubes/VisualDMC/src/LayerCUDA.cpp:575-636):
   0 = no padding, no split; 1 = padding, no split;
   2 = padding, one splitter iteration; 3 = padding, full splitter.
 
-Run from the repository root:  python3 tests/golden/make_reference_goldens.py [reference_root]
+Run from the repository root:  python3 tests/golden/make_reference_goldens.py <reference_root>
+(or with the reference checkout named by the environment variable MDMC_REFERENCE).
 """
 import json
 import os
 import struct
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MDMC_REFERENCE")
+if not REF:
+    sys.exit("usage: %s <reference_root>  (or set MDMC_REFERENCE)" % sys.argv[0])
 DR = os.path.join(REF, "Data-and-Results")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_goldens.json")
 

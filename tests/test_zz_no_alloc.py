@@ -78,6 +78,46 @@ def test_noalloc_count_matches_run_on_consecutive_calls():
         totals.fill_(-7)
 
 
+def _smooth_field(dims, torch):
+    """A smooth field on the device with many iso-crossings (dims x, y, z)."""
+    X, Y, Z = dims
+    z = torch.arange(Z, device="cuda", dtype=torch.float32).view(Z, 1, 1)
+    y = torch.arange(Y, device="cuda", dtype=torch.float32).view(1, Y, 1)
+    x = torch.arange(X, device="cuda", dtype=torch.float32).view(1, 1, X)
+    return (torch.sin(0.21 * x + 0.3) * torch.cos(0.17 * y) + torch.sin(0.13 * z + 0.05 * x)).contiguous()
+
+
+def test_noalloc_count_at_exactly_its_limits():
+    """Grids at exactly the scratch's limits are accepted and count like mdmc_run.
+
+    The refined limit case ends its last row of coarse cells on the last word
+    of the bit mask, where the row walker also loads the word after it."""
+    torch = pytest.importorskip("torch")
+    totals = torch.full((2,), -7, dtype=torch.int64, device="cuda")
+    cases = [
+        # (512 * 512) = 2^18 x-rows of cells, dense
+        ("rows_2^18", [3, 513, 513], 0, False),
+        # 256^3 = 2^24 coarse cells, padded on demand (259^3 samples)
+        ("coarse_2^24_pad", [257, 257, 257], 0, True),
+        # 2^24 coarse cells refined x2 (coarse 257^3, 513^3 samples)
+        ("coarse_2^24_refine1", [257, 257, 257], 1, False),
+    ]
+    for name, cdims, r, pad in cases:
+        field = _smooth_field(cdims, torch)
+        grid = mdmc.UniformGrid(field, cdims, refinement=r, add_zero_boundary=pad)
+        dmc = mdmc.DualMarchingCubes(split_non_manifold_halfedges=False, detect_non_manifold_vertices=False)
+        dmc.run(0.1, grid)
+        expect = (int(dmc.stats.num_active_cells), int(dmc.stats.num_dmc_quads))
+        assert expect[0] > 0 and expect[1] > 0, name
+        del dmc
+        for _ in range(2):
+            st, msg = _count(grid, 0.1, totals)
+            assert st == MDMC_OK, (name, msg)
+            torch.cuda.synchronize()
+            assert tuple(int(t) for t in totals.cpu()) == expect, name
+            totals.fill_(-7)
+
+
 def test_noalloc_count_rejects_grids_beyond_its_scratch():
     torch = pytest.importorskip("torch")
     totals = torch.full((2,), -7, dtype=torch.int64, device="cuda")
