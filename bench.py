@@ -52,8 +52,8 @@ def parse():
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-noise", action="store_true")
-    ap.add_argument("--fit", action="store_true",
-                    help="also time 200 Adam steps of the sphere-to-torus fit (brute-force Chamfer in torch)")
+    ap.add_argument("--no-fit", action="store_true",
+                    help="skip the 200 Adam steps of the sphere-to-torus fit (the differentiable workload)")
     args = ap.parse_args()
     if args.steps is None:
         # ~0.1 s of timed GPU work, long enough for the clock samples to land in it
@@ -342,14 +342,13 @@ def run_ours(args, rank, world, local):
             "metric": "Mcells/s (DMC + manifold repair, 512^3-cell refined grid)",
             "value": round(value, 2), "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian blobs)",
-            "config": {"workload": args.config, "description": desc, "cells": cells,
-                       "grid_in": dims_in, "grid_processed": list(grid.dims), "iso": iso, "refinement": refine,
-                       "pad": bool(pad), "l2": "flushed between timed steps (256 MB write)",
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "dmc_vertices": int(stats.num_dmc_vertices), "dmc_quads": int(stats.num_dmc_quads),
-                       "final_vertices": int(mesh.num_vertices), "final_faces": int(mesh.num_faces),
-                       "split_iterations": int(stats.split_iterations), "edges4": int(stats.num_edges4)},
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded numpy default_rng fields of the workload's shape; no dataset)",
+            "config": workload_config(args.config),
+            "parallelism": "replicas" if world > 1 else "single GPU",
+            "l2": "flushed between timed steps (256 MB write)",
+            "mesh": {"dmc_vertices": int(stats.num_dmc_vertices), "dmc_quads": int(stats.num_dmc_quads),
+                     "final_vertices": int(mesh.num_vertices), "final_faces": int(mesh.num_faces),
+                     "split_iterations": int(stats.split_iterations), "edges4": int(stats.num_edges4)},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
@@ -401,16 +400,22 @@ def measure_adjoint(args, dev, stream, flush):
                 (both if with_adjoint else fwd).append(e0.elapsed_time(e1))
     f, b = float(np.mean(fwd)), float(np.mean(both))
     fit = None
-    if args.fit:
+    if not args.no_fit:
         # 200 Adam steps of forward + adjoint + one-sided Chamfer to 200k points
-        # on a torus (R = 40, r = 15 cells) around the grid's centre
+        # on a torus (R = 40, r = 15 cells) around the grid's centre; the
+        # nearest points come from the library's point index
         from manifolddmc_gb300.optimize import fit_to_points
         from manifolddmc_gb300.workloads import torus_points
         c = (vol.shape[0] - 1) / 2.0
         pts = torch.from_numpy(torus_points(200000, 40.0, 15.0, (c, c, c), seed=5)).to(dev)
-        _, losses, seconds = fit_to_points(d_in, pts, iso, steps=200, lr=0.1)
+        fit_to_points(d_in, pts, iso, steps=5, lr=0.1)  # warm-up (buffers, index build path)
+        split = {}
+        _, losses, seconds = fit_to_points(d_in, pts, iso, steps=200, lr=0.1, timing=split)
         fit = {"steps": 200, "points": 200000, "seconds": round(seconds, 3), "ms_per_step": round(1e3 * seconds / 200, 3),
-               "loss_first": round(losses[0], 4), "loss_last": round(losses[-1], 4)}
+               "loss_first": round(losses[0], 4), "loss_last": round(losses[-1], 4),
+               "step_split_ms": {k: round(v, 4) for k, v in split.items()},
+               "note": "wall clock of the whole loop (Python, autograd and Adam included); step_split_ms from CUDA "
+                       "events: DMC forward, nearest points + loss, adjoint backward + Adam"}
     return {"workload": name, "description": desc, "vertices": V, "fwd_ms": round(f, 4), "fit": fit,
             "fwd_adjoint_ms": round(b, 4), "ratio": round(b / f, 3),
             "gradient_check": "max |gpu - FP64 oracle| <= 1e-5 * max |FP64| (tests/test_gpu_adjoint.py); "
@@ -500,6 +505,12 @@ def measure_batch(args, dev):
     single = mdmc.DualMarchingCubes()
     for g, iso in zip(grids, isos):
         single.run(iso, g)
+    # each grid's stream time (the run's first to last CUDA event inside the
+    # library, gaps while the host reads counts back included), summed
+    busy = 0.0
+    for g, iso in zip(grids, isos):
+        single.run(iso, g)
+        busy += float(single.stats.ms_total)
     seq, bat = [], []
     for _ in range(max(1, min(args.steps, 3))):
         torch.cuda.synchronize(dev)
@@ -516,8 +527,21 @@ def measure_batch(args, dev):
     return {"workload": "96 grids, dims uniform in [24,192] per axis, 4-32 Gaussian blobs or uniform noise (50/50), "
                         "iso uniform in [0.3,0.7], seed 4",
             "cells": int(cells), "streams": batch.streams, "sequential_ms": round(1e3 * s, 3),
-            "batch_ms": round(1e3 * b, 3), "speedup": round(s / b, 3),
+            "batch_ms": round(1e3 * b, 3), "speedup": round(s / b, 3), "gpu_busy_ms": round(busy, 3),
+            "gpu_busy_note": "sum over the 96 grids of each run's stream time (ms_total: first to last CUDA event "
+                             "of the run, including the short gaps while the host reads counts back)",
             "batch_mcells_s": round(cells / b / 1e6, 1), "sequential_mcells_s": round(cells / s / 1e6, 1)}
+
+
+def workload_config(config):
+    """The workload descriptor both arms print (inputs only, no results)."""
+    from manifolddmc_gb300.workloads import CONFIGS
+    desc, gen, iso, refine, pad = CONFIGS[config]
+    shape = {"blobs64_pad": [64] * 3, "noise128": [128] * 3, "noise256": [256] * 3, "blobs129_refine4": [129] * 3, "blobs65_refine4": [65] * 3,
+             "noise513": [513] * 3, "sphere128_sdf": [128] * 3}[config]
+    proc = [d + (d - 1) * refine + (2 if pad else 0) for d in shape]
+    return {"workload": config, "description": desc, "cells": (proc[0] - 1) * (proc[1] - 1) * (proc[2] - 1),
+            "grid_in": shape, "grid_processed": proc, "iso": iso, "refinement": refine, "pad": bool(pad)}
 
 
 def cpu_sample(config, fraction=1):
@@ -538,25 +562,40 @@ def cpu_threads():
 
 
 def time_oracle(sub, dims, iso, refine, pad):
+    """One run of the FP64 build of the oracle (refinement and the whole
+    path in double) on the sample; returns (cells, seconds, result)."""
     sys.path.insert(0, str(ROOT / "tests"))
-    from _support import oracle_refine, oracle_run
+    from _support import oracle_run_refined
     o = np.zeros(3, np.float32)
     s = np.ones(3, np.float32)
     t0 = time.perf_counter()
-    g, d, oo, ss = oracle_refine(sub.reshape(-1), dims, o, s, refine, pad)
-    r = oracle_run(g, d, oo, ss, iso)
+    r = oracle_run_refined(sub.reshape(-1), dims, o, s, refine, pad, iso, f64=True)
     dt = time.perf_counter() - t0
+    d = [x + (x - 1) * refine + (2 if pad else 0) for x in dims]
     cells = (d[0] - 1) * (d[1] - 1) * (d[2] - 1)
     return cells, dt, r
 
 
+CPU_BASELINE_WHAT = ("the FP64 build of the CPU oracle (the C++ restatement of the reference's algorithm compiled "
+                     "with double arithmetic; the reference has no CPU path): refinement and the DMC cell loop run "
+                     "with OpenMP over z-slabs on %d host threads, the halfedge build, the repair and the fan "
+                     "detection are serial")
+
+
 def cpu_baseline(config):
+    """Median of 5 runs after 1 warm-up, on the whole workload."""
     sub, dims, iso, refine, pad = cpu_sample(config)
-    cells, dt, _ = time_oracle(sub, dims, iso, refine, pad)
+    times = []
+    cells = 0
+    for i in range(6):
+        cells, dt, _ = time_oracle(sub, dims, iso, refine, pad)
+        if i:
+            times.append(dt)
+    dt = float(np.median(times))
     return {"value": round(cells / dt / 1e6, 3), "unit": "Mcells/s", "cores": cpu_threads(), "kind": "port",
-            "sample": "CPU oracle (C++ restatement; OpenMP over z-slabs for refinement and DMC, the halfedge build and "
-                      "repair serial) on the whole workload: %d of %d input z-planes, %d cells, one run, %.2f s"
-                      % (dims[2], dims[0], cells, dt)}
+            "sample": (CPU_BASELINE_WHAT % cpu_threads()) + "; the whole workload (%d of %d input z-planes, %d "
+                      "cells), median of 5 runs after 1 warm-up: %.2f s (runs %s s)"
+                      % (dims[2], dims[2], cells, dt, ", ".join("%.2f" % t for t in times))}
 
 
 def run_reference(args, rank, world):
@@ -569,18 +608,15 @@ def run_reference(args, rank, world):
         cells, dt, _ = time_oracle(sub, dims, iso, refine, pad)
         if i >= max(args.warmup, 3):
             times.append(dt)
-    ms = float(np.mean(times)) * 1e3
+    ms = float(np.median(times)) * 1e3
     value = cells / (ms / 1e3) / 1e6
-    sample = ("the reference's path has no CPU implementation and does not build on this image (CUDA-only, "
-              "MSVC/OpenGL dependencies); its C++ restatement (oracle/) runs with OpenMP on %d host threads "
-              "(refinement and DMC in z-slabs, halfedge build and repair serial) over the whole workload, %d of %d "
-              "input z-planes (%d cells per step)" % (cpu_threads(), dims[2], dims[0], cells))
-    from manifolddmc_gb300.workloads import CONFIGS
+    sample = ((CPU_BASELINE_WHAT % cpu_threads()) + "; each step one run over the whole workload (%d input z-planes, "
+              "%d cells); value from the median step" % (dims[2], cells))
     line = {"impl": "reference", "metric": "Mcells/s (DMC + manifold repair, 512^3-cell refined grid)",
             "value": round(value, 3), "unit": "Mcells/s", "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": round(ms, 2), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian blobs)",
-            "config": {"workload": args.config, "description": CONFIGS[args.config][0]},
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded numpy default_rng fields of the workload's shape; no dataset)",
+            "config": workload_config(args.config), "parallelism": "%d host threads" % cpu_threads(),
             "cpu_baseline": {"value": round(value, 3), "unit": "Mcells/s", "cores": cpu_threads(), "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 3), "unit": "Mcells/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}

@@ -387,6 +387,26 @@ MDMC_API mdmc_status mdmc_write_bin(const char* path, const int32_t dims[3], con
  * s_triangleAmbiguities, DualMarchingCubes.cpp:301,564). */
 MDMC_API void mdmc_case_tables(uint64_t contour_words[256], uint8_t ambiguous[256]);
 
+/* Nearest points for the differentiable form's Chamfer loss (no
+ * counterpart in the reference).  mdmc_point_index_create copies `count`
+ * points (device memory, 3 floats each) into device memory the index owns
+ * until mdmc_point_index_destroy.  Synchronous. */
+typedef struct mdmc_point_index mdmc_point_index;
+MDMC_API mdmc_status mdmc_point_index_create(mdmc_point_index** index, const float* points, int64_t count,
+                                             void* stream);
+MDMC_API void mdmc_point_index_destroy(mdmc_point_index* index);
+/* For each of `count` query points (device, 3 floats each): the index of the
+ * nearest indexed point (its position in the array given to create) and,
+ * when dist2 is not NULL, the squared distance (dx*dx + dy*dy) + dz*dz in
+ * float.  Exact and exhaustive (every point is compared; the cost does not
+ * depend on where the queries lie): equal distances go to the smaller index.
+ * scratch: device memory of `count` uint64 the call overwrites.
+ * Asynchronous on the stream. */
+MDMC_API mdmc_status mdmc_point_index_nearest(const mdmc_point_index* index, const float* queries, int64_t count,
+                                              int32_t* nearest, float* dist2, uint64_t* scratch, void* stream);
+/* The number of indexed points. */
+MDMC_API int64_t mdmc_point_index_count(const mdmc_point_index* index);
+
 /* The count pass of mdmc_run without a context and without allocating:
  * writes {active cells, DMC quads} of the grid at iso_value to totals, two
  * int64 in DEVICE memory, asynchronously on the stream (equal to

@@ -189,6 +189,10 @@ def library():
             "mdmc_batch_streams": (ctypes.c_int, [P]),
             "mdmc_batch_context": (P, [P, ctypes.c_int]),
             "mdmc_batch_last_error": (ctypes.c_char_p, [P]),
+            "mdmc_point_index_create": (ctypes.c_int, [P, P, ctypes.c_int64, P]),
+            "mdmc_point_index_destroy": (None, [P]),
+            "mdmc_point_index_nearest": (ctypes.c_int, [P, P, ctypes.c_int64, P, P, P, P]),
+            "mdmc_point_index_count": (ctypes.c_int64, [P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(lib, name)
@@ -639,3 +643,50 @@ def mean_ratio(positions, triangles, stream=None):
     if int(bad.item()):
         raise MDMCError(1, "triangle vertex id outside the vertex array")
     return q
+
+
+class PointIndex:
+    """Exact nearest-point queries against a fixed set of CUDA float32 points
+    [P, 3] (mdmc_point_index_*; no counterpart in the reference): an
+    exhaustive tiled search on the GPU, whose cost does not depend on where
+    the queries lie."""
+
+    def __init__(self, points, stream=None):
+        import torch
+        if not points.is_cuda or points.dtype != torch.float32 or points.dim() != 2 or points.shape[1] != 3:
+            raise ValueError("points must be a CUDA float32 tensor [P, 3]")
+        self.lib = library()
+        self.points = points.contiguous()
+        self.handle = P()
+        st = self.lib.mdmc_point_index_create(ctypes.byref(self.handle), self.points.data_ptr(), len(self.points),
+                                              _stream_handle(stream if stream is not None
+                                                             else torch.cuda.current_stream()))
+        if st != 0:
+            raise MDMCError(st, "mdmc_point_index_create failed")
+        self._scratch = None
+
+    def __len__(self):
+        return int(self.lib.mdmc_point_index_count(self.handle))
+
+    def nearest(self, queries, stream=None):
+        """(index int64 [Q], squared distance float32 [Q]) of the nearest point to each CUDA float32 query [Q, 3]."""
+        import torch
+        q = queries.detach().contiguous().float()
+        idx = torch.empty(len(q), dtype=torch.int32, device=q.device)
+        d2 = torch.empty(len(q), dtype=torch.float32, device=q.device)
+        if self._scratch is None or len(self._scratch) < len(q):
+            self._scratch = torch.empty(max(len(q), 1), dtype=torch.int64, device=q.device)
+        st = self.lib.mdmc_point_index_nearest(self.handle, q.data_ptr(), len(q), idx.data_ptr(), d2.data_ptr(),
+                                               self._scratch.data_ptr(),
+                                               _stream_handle(stream if stream is not None
+                                                              else torch.cuda.current_stream()))
+        if st != 0:
+            raise MDMCError(st, "mdmc_point_index_nearest failed")
+        return idx.long(), d2
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h:
+            self.lib.mdmc_point_index_destroy(h)
+            self.handle = None
+

@@ -17,7 +17,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT_DIR = PKG / "_build"
 LIB = OUT_DIR / "libmdmc.so"
-SOURCES = ["mdmc_api.cu", "mdmc_dmc.cu", "mdmc_mesh.cu", "mdmc_split.cu", "mdmc_noalloc.cu", "mdmc_adjoint.cu", "mdmc_simplify.cu", "mdmc_batch.cu", "mdmc_generate.cu", "mdmc_mc.cu", "mdmc_quality.cu"]
+SOURCES = ["mdmc_api.cu", "mdmc_dmc.cu", "mdmc_mesh.cu", "mdmc_split.cu", "mdmc_noalloc.cu", "mdmc_adjoint.cu", "mdmc_simplify.cu", "mdmc_batch.cu", "mdmc_generate.cu", "mdmc_mc.cu", "mdmc_quality.cu", "mdmc_points.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "--expt-relaxed-constexpr",
          "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",

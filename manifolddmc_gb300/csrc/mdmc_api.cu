@@ -97,7 +97,10 @@ struct mdmc_context {
     DevBuf sVal, sCount, sType, sTarget, sClaimA, sClaimC, sMerge, sKeepV, sKeepF, sPos, sNrm, sQuads, sAttr;
     // edge buckets: per-vertex adjacency rows (destination, halfedge), the
     // 4-face edge list, per-halfedge valence
-    DevBuf adjRow, adjCursor, adj, nmList, heValence;
+    DevBuf adjRow, adjRank, adj, nmList, heValence, faceNM;
+    DevBuf caseBytes;  // the mask pass's per-cell cases for the emit pass
+    int caseMode = 0;  // CaseBytes::mode of the last mask pass
+    bool faceNMValid = false;  // faceNM holds the current mesh's per-face counts (else heValence)
     // quad -> owner cell; per-row active-cell mask (32 cells per word) and the
     // index of each word's first active cell; per active cell {contours, quads}
     DevBuf quadOwner, cellMask, cellFirst, cellCounts, cellIds;
@@ -351,20 +354,21 @@ mdmc_status edgeBuckets(mdmc_context* c, int connect, cudaStream_t s) {
     DevCounters* ctr = c->counters.as<DevCounters>();
     const MeshDims md{(int)c->V, (int)c->F, (int)c->H};
     MDMC_CHECK(c, c->nmList.ensure(sizeof(int4) * (size_t)(c->H / 4 + 1)));
-    MDMC_CHECK(c, c->heValence.ensure((size_t)std::max<int64_t>(c->H, 1)));
+    MDMC_CHECK(c, c->faceNM.ensure(roundUp((size_t)std::max<int64_t>(c->F, 1), 4)));
     MDMC_CHECK(c, c->adjRow.ensure(sizeof(int) * (size_t)(c->V + 1)));
-    MDMC_CHECK(c, c->adjCursor.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
+    MDMC_CHECK(c, c->adjRank.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->H, 1)));
     MDMC_CHECK(c, c->adj.ensure(sizeof(int2) * (size_t)std::max<int64_t>(c->H, 1)));
     MDMC_CHECK(c, cudaMemsetAsync(c->adjRow.p, 0, sizeof(int) * (size_t)c->V, s));
-    launchDegree(c->he.as<int4>(), md, c->adjRow.as<int>(), &ctr->status, s);
+    launchEdgeRowDegree(c->he.as<int4>(), md, c->adjRow.as<int>(), c->adjRank.as<int>(), &ctr->status, s);
     mdmc_status st = scan<int>(c, c->adjRow.as<int>(), c->adjRow.as<int>(), c->V, s);
     if (st != MDMC_OK) return st;
-    MDMC_CHECK(c, cudaMemsetAsync(c->adjCursor.p, 0, sizeof(int) * (size_t)c->V, s));
     MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)std::max<int64_t>(c->V, 1), 4), s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->faceNM.p, 0, roundUp((size_t)std::max<int64_t>(c->F, 1), 4), s));
     MDMC_CHECK(c, cudaMemsetAsync((char*)c->counters.p + 8, 0, sizeof(DevCounters) - 8, s));
-    launchEdgeBuckets(c->he.as<int4>(), md, c->adjRow.as<int>(), c->adjCursor.as<int>(), c->adj.as<int2>(), connect,
-                      c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(),
+    launchEdgeBuckets(c->he.as<int4>(), md, c->adjRow.as<int>(), c->adjRank.as<int>(), c->adj.as<int2>(), connect,
+                      c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), c->faceNM.as<uint8_t>(),
                       c->nmList.as<int4>(), ctr, s);
+    c->faceNMValid = true;
     return MDMC_OK;
 }
 
@@ -410,7 +414,8 @@ mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaSt
     }
     markStage(c, 4, detect, s);
     if (!starsDone)
-        launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), mdF, c->heValence.as<uint8_t>(), c->quads.as<int4>(),
+        launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), mdF, c->heValence.as<uint8_t>(),
+                     c->faceNMValid ? c->faceNM.as<uint8_t>() : nullptr, c->quads.as<int4>(),
                      c->vertexHE.as<int>(), detect, ctr, status, s);
     else if (!detect)
         launchVertexHalfedgeFix(c->vertexHE.as<int>(), (int)c->V, s);
@@ -687,11 +692,24 @@ mdmc_status markActive(mdmc_context* c, const GridDesc& g, float iso, int& W, in
     MDMC_CHECK(c, c->cellFirst.ensure(sizeof(int) * (size_t)(numWords + 1)));
     markKernel(c, 2, s);
     if (g.refined && numWords > 0) MDMC_CHECK(c, cudaMemsetAsync(c->cellMask.p, 0, sizeof(uint32_t) * (size_t)numWords, s));
-    if (g.refined && g.ref.mayCross && 2 * (g.ref.r + 4) * (g.ref.r + 4) <= 512 && numWords > 0)
+    const bool blockMask = g.refined && g.ref.mayCross && 2 * (g.ref.r + 4) * (g.ref.r + 4) <= 512 && numWords > 0;
+    // per-cell cases for the emit pass: every cell of a plain grid, the
+    // standard blocks of a x4 refinement without padding
+    CaseBytes cases;
+    if (!g.refined && numWords > 0) {
+        MDMC_CHECK(c, c->caseBytes.ensure((size_t)X * Y * Z));
+        cases = CaseBytes{c->caseBytes.as<uint8_t>(), 1};
+    } else if (blockMask && g.ref.r == 3 && !g.ref.pad) {
+        const int64_t coarseCells = (int64_t)(g.ref.cX - 1) * (g.ref.cY - 1) * (g.ref.cZ - 1);
+        MDMC_CHECK(c, c->caseBytes.ensure((size_t)coarseCells * 64));
+        cases = CaseBytes{c->caseBytes.as<uint8_t>(), 2};
+    }
+    c->caseMode = cases.mode;
+    if (blockMask)
         launchBlockMask(g.ref, iso, c->candidates.as<uint32_t>(), &c->counters.as<DevCounters>()->candidates,
-                        c->cellMask.as<uint32_t>(), W, status, s);
+                        c->cellMask.as<uint32_t>(), W, cases, status, s);
     else
-        launchRowMask(g, iso, c->cellMask.as<uint32_t>(), (int)numRows, W, s);
+        launchRowMask(g, iso, c->cellMask.as<uint32_t>(), (int)numRows, W, cases, s);
     // the scan also lists the active cells' ids, as many as the list holds
     // already (all of them when the grid is like the last one)
     MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(numWords)));
@@ -956,7 +974,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     markKernel(c, 4, s);
     MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(capA)));
     launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)capA,
-                     status, s, numActiveDev);
+                     CaseBytes{c->caseBytes.as<uint8_t>(), c->caseMode}, status, s, numActiveDev);
     // the scan's last block writes the counts straight into the pinned host
     // scratch when the device can address it (no copy on the stream)
     if (!scanCellCounts(c->cellCounts.as<int2>(), capA, numActiveDev, c->act.as<ActiveCell>(), c->quadOwner.as<int>(),
@@ -1007,7 +1025,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
         MDMC_CHECK(c, c->quadOwner.ensure(sizeof(int) * (size_t)std::max<int64_t>(needQ, 1)));
         MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(A)));
         launchEmitActive(g, iso, c->cellIds.as<uint32_t>(), c->act.as<ActiveCell>(), c->cellCounts.as<int2>(), (int)A,
-                         status, s);
+                         CaseBytes{c->caseBytes.as<uint8_t>(), c->caseMode}, status, s);
         if (!scanCellCounts(c->cellCounts.as<int2>(), A, nullptr, c->act.as<ActiveCell>(), c->quadOwner.as<int>(),
                             needQ, ctr->gathered, nullptr, c->scanScratch.as<int2>(), s))
             return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
@@ -1074,6 +1092,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
         if (early && (st = earlyCopyFaces(c, q0, q1, s)) != MDMC_OK) return st;
     }
     c->earlyFaces = early;
+    c->faceNMValid = false;  // the quad pass wrote heValence
     markKernel(c, 7, s);
     // vertex positions and normals (sliceP's vertex part)
     if (!aheadDone) {

@@ -441,7 +441,8 @@ __device__ bool blockSamples5(const RefinedView& g, int xs, int ys, int zs, int 
 
 __global__ void __launch_bounds__(32 * kBlockMaskWarps, 4) kBlockMask(RefinedView g, float iso, const uint32_t* __restrict__ list,
                                                                  const unsigned long long* listCount,
-                                                                 uint32_t* __restrict__ mask, int W, uint32_t* status) {
+                                                                 uint32_t* __restrict__ mask, int W, CaseBytes cases,
+                                                                 uint32_t* status) {
     __shared__ float samples[kBlockMaskWarps][kBlockSamplesMax];
     __shared__ float sepSamples[kBlockMaskWarps][27 + 45 + 75];
     __shared__ int sepIndex[kBlockMaskWarps][30];
@@ -498,6 +499,7 @@ __global__ void __launch_bounds__(32 * kBlockMaskWarps, 4) kBlockMask(RefinedVie
                 const float s[8] = {buf[o],      buf[o + 1],      buf[o + 5],      buf[o + 6],
                                     buf[o + 25], buf[o + 26], buf[o + 30], buf[o + 31]};
                 const int cs = caseOf(s, iso);
+                if (cases.mode == 2) cases.p[(size_t)ci * 64 + k] = (uint8_t)cs;
                 const int x = xs + lx;
                 unsigned bitv = (cs != 0 && cs != 255) ? (1u << (x & 31)) : 0u;
                 bitv |= __shfl_xor_sync(0xffffffffu, bitv, 1);
@@ -579,9 +581,9 @@ __global__ void __launch_bounds__(32 * kBlockMaskWarps, 4) kBlockMask(RefinedVie
 }
 
 void launchBlockMask(const RefinedView& g, float iso, const uint32_t* list, const unsigned long long* listCount,
-                     uint32_t* mask, int W, uint32_t* status, cudaStream_t s) {
+                     uint32_t* mask, int W, CaseBytes cases, uint32_t* status, cudaStream_t s) {
     countLaunch();
-    kBlockMask<<<152 * 8, 32 * kBlockMaskWarps, 0, s>>>(g, iso, list, listCount, mask, W, status);
+    kBlockMask<<<152 * 8, 32 * kBlockMaskWarps, 0, s>>>(g, iso, list, listCount, mask, W, cases, status);
 }
 
 // Visits the cells of one row and calls f(x, s[8]) once per lane and step
@@ -702,17 +704,20 @@ void launchRowCount(const GridDesc& g, float iso, int4* rowCounts, int numRows, 
 // refined rows visit only candidate cells and OR their bits into words
 // cleared beforehand.
 template <class View>
-__global__ void __launch_bounds__(256) kRowMask(View g, float iso, uint32_t* __restrict__ mask, int numRows, int W) {
+__global__ void __launch_bounds__(256) kRowMask(View g, float iso, uint32_t* __restrict__ mask, int numRows, int W,
+                                                CaseBytes cases) {
     const int lane = threadIdx.x & 31;
     const int row = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (row >= numRows) return;
     const int y = row % (g.Y - 1), z = row / (g.Y - 1);
     uint32_t* words = mask + (int64_t)row * W;
+    uint8_t* rowCases = cases.mode == 1 ? cases.p + ((size_t)z * g.Y + y) * g.X : nullptr;
     walkRow(g, y, z, lane, [&](int x, const float s[8]) {
         bool active = false;
         if (x < g.X - 1) {
             const int cs = caseOf(s, iso);
             active = cs != 0 && cs != 255;
+            if (rowCases) rowCases[x] = (uint8_t)cs;
         }
         if constexpr (View::kRefined) {
             if (active) atomicOr(&words[x >> 5], 1u << (x & 31));
@@ -723,11 +728,11 @@ __global__ void __launch_bounds__(256) kRowMask(View g, float iso, uint32_t* __r
     });
 }
 
-void launchRowMask(const GridDesc& g, float iso, uint32_t* mask, int numRows, int W, cudaStream_t s) {
+void launchRowMask(const GridDesc& g, float iso, uint32_t* mask, int numRows, int W, CaseBytes cases, cudaStream_t s) {
     if (numRows <= 0) return;
     countLaunch();
-    if (g.refined) kRowMask<RefinedView><<<(numRows + 7) / 8, 256, 0, s>>>(g.ref, iso, mask, numRows, W);
-    else kRowMask<PlainView><<<(numRows + 7) / 8, 256, 0, s>>>(g.plain, iso, mask, numRows, W);
+    if (g.refined) kRowMask<RefinedView><<<(numRows + 7) / 8, 256, 0, s>>>(g.ref, iso, mask, numRows, W, CaseBytes{});
+    else kRowMask<PlainView><<<(numRows + 7) / 8, 256, 0, s>>>(g.plain, iso, mask, numRows, W, cases);
 }
 
 // The linear cell id of every active cell, in row-major order: one thread
@@ -844,7 +849,8 @@ void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords
 template <class View>
 __global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint32_t* __restrict__ cellIds,
                                                    ActiveCell* __restrict__ act, int2* __restrict__ counts,
-                                                   int numActive, const int* numActiveDev, uint32_t* status) {
+                                                   int numActive, const int* numActiveDev, CaseBytes cases,
+                                                   uint32_t* status) {
     __shared__ uint32_t edgeMaps[256];  // per case: edge -> contour map | contours << 24
     for (int i = threadIdx.x; i < 256; i += blockDim.x) edgeMaps[i] = kCaseTables.edgeMaps[i];
     __syncthreads();
@@ -858,25 +864,41 @@ __global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint
         atomicOr(status, kStatusCountMismatch);
         return;
     }
-    const RowWalker<View> walker(g, y, z);
-    float cur[4], nxt[4];
-    walker.load(x, cur);
-    walker.load(x + 1, nxt);
-    float s[8];
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        s[2 * k] = cur[k];
-        s[2 * k + 1] = nxt[k];
+    // the case the mask pass found, when it left one
+    int cs = -1;
+    if constexpr (View::kRefined) {
+        if (cases.mode == 2) {
+            const uint32_t coarse = ((uint32_t)(z >> 2) * (uint32_t)(g.cY - 1) + (uint32_t)(y >> 2)) *
+                                        (uint32_t)(g.cX - 1) + (uint32_t)(x >> 2);
+            cs = cases.p[(size_t)coarse * 64 + ((z & 3) << 4) + ((y & 3) << 2) + (x & 3)];
+        }
+    } else {
+        if (cases.mode == 1) cs = cases.p[cell];
     }
-    const int cs = caseOf(s, iso);
+    // the contours' edge map: the case's table entry, or from the asymptotic
+    // decider's contours for the ambiguous cases (which need the corners)
+    uint32_t em = cs >= 0 ? edgeMaps[cs] : 0xFFFFFFFFu;
+    if (em == 0xFFFFFFFFu) {
+        const RowWalker<View> walker(g, y, z);
+        float cur[4], nxt[4];
+        walker.load(x, cur);
+        walker.load(x + 1, nxt);
+        float s[8];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            s[2 * k] = cur[k];
+            s[2 * k + 1] = nxt[k];
+        }
+        const int c2 = caseOf(s, iso);
+        if (cs >= 0 && c2 != cs) atomicOr(status, kStatusCountMismatch);
+        cs = c2;
+        em = edgeMaps[cs];
+        if (em == 0xFFFFFFFFu) em = contourEdgeMap(asymptoticContours(s, iso));
+    }
     if (cs == 0 || cs == 255) {
         atomicOr(status, kStatusCountMismatch);
         return;
     }
-    // the contours' edge map: the case's table entry, or from the asymptotic
-    // decider's contours for the ambiguous cases
-    uint32_t em = edgeMaps[cs];
-    if (em == 0xFFFFFFFFu) em = contourEdgeMap(asymptoticContours(s, iso));
     const int n = (int)(em >> 24);
     const uint32_t emap = em & 0xFFFFFFu;
     ActiveCell rec;
@@ -889,16 +911,16 @@ __global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint
 }
 
 void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, ActiveCell* act, int2* counts,
-                      int numActive, uint32_t* status, cudaStream_t s, const int* numActiveDev) {
+                      int numActive, CaseBytes cases, uint32_t* status, cudaStream_t s, const int* numActiveDev) {
     if (numActive <= 0) return;
     countLaunch();
     const unsigned blocks = (unsigned)((numActive + 127) / 128);
     if (g.refined)
         kEmitActive<RefinedView><<<blocks, 128, 0, s>>>(g.ref, iso, cellIds, act, counts, numActive, numActiveDev,
-                                                        status);
+                                                        cases, status);
     else
         kEmitActive<PlainView><<<blocks, 128, 0, s>>>(g.plain, iso, cellIds, act, counts, numActive, numActiveDev,
-                                                      status);
+                                                      cases, status);
 }
 
 // ---------------------------------------------------------------------------

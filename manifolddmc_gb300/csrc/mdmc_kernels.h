@@ -128,10 +128,19 @@ void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, cudaS
 // also appends the candidate coarse cells to list (count in *listCount)
 void launchCoarseMayCross(const RefinedView& g, float iso, uint32_t* bits, uint32_t* list, unsigned long long* listCount,
                           cudaStream_t s);
+// The case byte of every cell the mask pass classifies, left for the emit
+// pass so that it need not evaluate the corners of cells whose case has a
+// table entry.  mode 0: none; 1: a plain grid, p[linear id of the cell's
+// corner-0 sample]; 2: a grid refined x4 without padding (standard 4x4x4
+// blocks of the block mask), p[coarse cell * 64 + (z & 3) * 16 + (y & 3) * 4 + (x & 3)].
+struct CaseBytes {
+    uint8_t* p = nullptr;
+    int mode = 0;
+};
 void launchBlockMask(const RefinedView& g, float iso, const uint32_t* list, const unsigned long long* listCount,
-                     uint32_t* mask, int W, uint32_t* status, cudaStream_t s);
+                     uint32_t* mask, int W, CaseBytes cases, uint32_t* status, cudaStream_t s);
 void launchRowCount(const GridDesc& g, float iso, int4* rowCounts, int numRows, cudaStream_t s);
-void launchRowMask(const GridDesc& g, float iso, uint32_t* mask, int numRows, int W, cudaStream_t s);
+void launchRowMask(const GridDesc& g, float iso, uint32_t* mask, int numRows, int W, CaseBytes cases, cudaStream_t s);
 // exclusive scan of the mask words' popcounts into first (numWords + 1
 // entries) that also writes the active cells' ids, the first `capacity` of them
 bool scanMaskScatter(const uint32_t* mask, int* first, int64_t numWords, int W, int X, int Y, uint32_t* cellIds,
@@ -140,7 +149,8 @@ void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords
                         int numActive, uint32_t* status, cudaStream_t s);
 // numActiveDev != nullptr: the count is read on the device, at most numActive
 void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, ActiveCell* act, int2* counts,
-                      int numActive, uint32_t* status, cudaStream_t s, const int* numActiveDev = nullptr);
+                      int numActive, CaseBytes cases, uint32_t* status, cudaStream_t s,
+                      const int* numActiveDev = nullptr);
 // exclusive scan of the active cells' (vertex, quad) counts in place
 // (capA + 1 entries, the count read from numActiveDev when given) that also
 // writes each record's first vertex and quad id, the quad owners (the first
@@ -193,9 +203,11 @@ void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, con
                  cudaStream_t s);
 void launchVertexHalfedgeFix(int* vertexHE, int numVertices, cudaStream_t s);
 
-void launchDegree(const int4* he, MeshDims md, int* deg, uint32_t* status, cudaStream_t s);
-void launchEdgeBuckets(int4* he, MeshDims md, const int* rowStart, int* cursor, int2* adj, int connectTwins,
-                       uint16_t* faceAttr, uint8_t* vflags, uint8_t* heValence, int4* nmList, DevCounters* ctr,
+// edge buckets: rows of halfedges keyed by their smaller end vertex
+// (deg: per vertex, the halfedges whose smaller end it is)
+void launchEdgeRowDegree(const int4* he, MeshDims md, int* deg, int* rank, uint32_t* status, cudaStream_t s);
+void launchEdgeBuckets(int4* he, MeshDims md, const int* rowStart, const int* rank, int2* adj, int connectTwins,
+                       uint16_t* faceAttr, uint8_t* vflags, uint8_t* faceNM, int4* nmList, DevCounters* ctr,
                        cudaStream_t s);
 void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s);
 void launchReconnect(const GridDesc& g, float iso, const int4* nmList, const DevCounters* ctr,
@@ -207,8 +219,8 @@ void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cuda
 void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, bool vertexPassDegrees,
                       uint8_t* slow, uint8_t* isKey, uint8_t keyMark, int* fans, uint8_t* vflags, DevCounters* ctr,
                       uint32_t* status, cudaStream_t s);
-void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, int4* quads,
-                  int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s);
+void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, const uint8_t* faceNM,
+                  int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s);
 
 // valence-pattern simplifications
 void launchValence(const int4* he, MeshDims md, int* val, cudaStream_t s);

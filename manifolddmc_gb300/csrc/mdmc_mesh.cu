@@ -12,6 +12,8 @@
 // pairing of 3- and 4-face edges, wall-side ties in the repair) deterministic.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "mdmc_device.cuh"
 #include "mdmc_kernels.h"
 
@@ -32,133 +34,236 @@ void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s) {
 }
 
 // ---------------------------------------------------------------------------
-// Edge buckets without a hash table: the halfedges of the vertex pair {a, b}
-// all leave a or b, so with every vertex's outgoing halfedges listed as
-// (destination, id) rows, a halfedge finds its bucket by scanning two short
-// rows.  Same buckets, counts and flags as the edge table of
-// refreshHashTable / connectHalfedgeTwins (D/Halfedges/HalfedgeMesh.cu:62-291,
-// :1063-1100); a bucket keeps its 4 smallest ids.
+// Edge buckets without a hash table.  Every halfedge is listed in the row of
+// the smaller of its two end vertices as (larger end, id), the larger end
+// stored as ~end when the halfedge leaves it; all halfedges of the vertex
+// pair {a, b} then sit in one row.  A warp takes 32 consecutive vertices,
+// whose rows are one contiguous span: it stages the span in shared memory
+// with coalesced loads and each lane settles the buckets of its own row.
+// Same buckets, counts and flags as the edge table of refreshHashTable /
+// connectHalfedgeTwins (D/Halfedges/HalfedgeMesh.cu:62-291, :1063-1100); a
+// bucket keeps its 4 smallest ids.
 // ---------------------------------------------------------------------------
-__global__ void kDegree(const int4* __restrict__ he, MeshDims md, int* __restrict__ deg, uint32_t* status) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= md.H) return;
-    const int v = he[h].x;
-    if (inb(v, md.V)) atomicAdd(&deg[v], 1);
-    else atomicOr(status, kStatusBadIndex);
-}
 
-__global__ void kAdjScatter(const int4* __restrict__ he, MeshDims md, const int* __restrict__ rowStart,
-                            int* __restrict__ cursor, int2* __restrict__ adj, uint32_t* status) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h >= md.H) return;
+// the end vertices of halfedge h, false (and a status bit) when an id is out of range
+__device__ __forceinline__ bool edgeEnds(const int4* __restrict__ he, MeshDims md, int h, int& a, int& b,
+                                         uint32_t* status) {
     const int4 e = he[h];
-    if (!inb(e.x, md.V)) return;
-    const int dest = inb(e.z, md.H) ? he[e.z].x : -1;
-    const int pos = rowStart[e.x] + atomicAdd(&cursor[e.x], 1);
-    if (pos < rowStart[e.x + 1]) adj[pos] = make_int2(dest, h);
-    else atomicOr(status, kStatusBadIndex);
+    a = e.x;
+    b = (inb(e.z, md.H) && inb(a, md.V)) ? he[e.z].x : -1;
+    if (!inb(b, md.V)) {
+        atomicOr(status, kStatusBadIndex);
+        return false;
+    }
+    return true;
 }
 
-__device__ __forceinline__ void keepSmallest(int ids[4], int g) {
+// row sizes; rank[h] = the halfedge's place in its row (the count before it,
+// in atomic order), -1 for a halfedge with an id out of range
+__global__ void kEdgeRowDegree(const int4* __restrict__ he, MeshDims md, int* __restrict__ deg, int* __restrict__ rank,
+                               uint32_t* status) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= md.H) return;
+    int a, b;
+    rank[h] = edgeEnds(he, md, h, a, b, status) ? atomicAdd(&deg[min(a, b)], 1) : -1;
+}
+
+__global__ void kEdgeRowScatter(const int4* __restrict__ he, MeshDims md, const int* __restrict__ rowStart,
+                                const int* __restrict__ rank, int2* __restrict__ adj) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= md.H) return;
+    const int k = rank[h];
+    if (k < 0) return;
+    const int a = he[h].x, b = he[he[h].z].x;  // in range (checked by the degree pass)
+    const int m = min(a, b), o = max(a, b);
+    adj[rowStart[m] + k] = make_int2(a == m ? o : ~o, h);
+}
+
+// the 4 smallest ids of a bucket, ascending, with their origins
+__device__ __forceinline__ void keepSmallest(int ids[4], int org[4], int g, int go) {
     if (g >= ids[3]) return;
     int k = 3;
     while (k > 0 && ids[k - 1] > g) {
         ids[k] = ids[k - 1];
+        org[k] = org[k - 1];
         --k;
     }
     ids[k] = g;
+    org[k] = go;
 }
 
-__global__ void kEdgeBuckets(int4* __restrict__ he, MeshDims md, const int* __restrict__ rowStart,
-                             const int2* __restrict__ adj, int connectTwins, uint16_t* faceAttr, uint8_t* vflags,
-                             uint8_t* __restrict__ heValence, int4* __restrict__ nmList, DevCounters* ctr) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    int nE = 0, nE3 = 0, nE4 = 0;
-    if (h < md.H) {
-        const int4 e = he[h];
-        const int a = e.x;
-        const int b = (inb(e.z, md.H) && inb(a, md.V)) ? he[e.z].x : -1;
-        if (!inb(b, md.V)) {
-            atomicOr(&ctr->status, kStatusBadIndex);
-        } else {
-            int ids[4] = {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF};
-            int cnt = 0;
-            for (int j = rowStart[a], je = rowStart[a + 1]; j < je; ++j) {
-                const int2 r = adj[j];
-                if (r.x == b) {
-                    ++cnt;
-                    keepSmallest(ids, r.y);
+constexpr int kBucketWarps = 8;
+constexpr int kBucketStage = 512;  // row entries of 32 vertices staged per warp (longer spans: global memory)
+
+// One warp per tile of 32 consecutive vertices (grid-stride over tiles).  The
+// tile's rows form one contiguous span of the row array; it is staged in
+// shared memory, each entry's larger end vertex and row (lane) beside it.
+// Then one lane per entry counts the entries of its own row with the same
+// end vertex (its bucket) and those before it: the bucket's first entry
+// counts the bucket.  Only an entry of a bucket of other than two halfedges
+// (or, with connectTwins, any entry) goes on: it collects the bucket's four
+// smallest ids and acts for its own halfedge: the vertex flag of its origin
+// (non-manifold / weird / boundary by the bucket's size), the non-manifold
+// face flag and the per-face count of edges with more than two halfedges
+// (faceNM, zeroed by the caller), its twin by the rules of
+// connectHalfedgeTwins (with connectTwins), and the first entry of a 4-face
+// bucket lists it.  The counters take one addition per block.
+__global__ void __launch_bounds__(32 * kBucketWarps) kEdgeBuckets(int4* __restrict__ he, MeshDims md,
+                                                                  const int* __restrict__ rowStart,
+                                                                  const int2* __restrict__ adj, int connectTwins,
+                                                                  uint16_t* faceAttr, uint8_t* vflags, uint8_t* faceNM,
+                                                                  int4* __restrict__ nmList, DevCounters* ctr) {
+    __shared__ int2 stage[kBucketWarps][kBucketStage];
+    __shared__ int stageEnd[kBucketWarps][kBucketStage];
+    __shared__ uint8_t stageRow[kBucketWarps][kBucketStage];
+    __shared__ int rowBegin[kBucketWarps][33];
+    __shared__ unsigned long long part[3][kBucketWarps];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    unsigned long long nE = 0, nE3 = 0, nE4 = 0;
+    const int tiles = (md.V + 31) / 32;
+    for (int tile = blockIdx.x * kBucketWarps + warp; tile < tiles; tile += gridDim.x * kBucketWarps) {
+        const int m0 = tile * 32;
+        const int myStart = rowStart[min(m0 + lane, md.V)];
+        const int s0 = __shfl_sync(0xffffffffu, myStart, 0);
+        const int s1 = rowStart[min(m0 + 32, md.V)];
+        const int span = s1 - s0;
+        const bool staged = span <= kBucketStage;
+        __syncwarp();
+        rowBegin[warp][lane] = myStart - s0;
+        if (lane == 0) rowBegin[warp][32] = span;
+        if (staged)
+            for (int k = lane; k < span; k += 32) {
+                const int2 r = adj[s0 + k];
+                stage[warp][k] = r;
+                stageEnd[warp][k] = r.x >= 0 ? r.x : ~r.x;
+            }
+        __syncwarp();
+        if (staged) {  // each lane tags its row's entries
+            const int b = rowBegin[warp][lane], e = rowBegin[warp][lane + 1];
+            for (int k = b; k < e; ++k) stageRow[warp][k] = (uint8_t)lane;
+        }
+        __syncwarp();
+        for (int k = lane; k < span; k += 32) {
+            int row;
+            int2 mine;
+            if (staged) {
+                row = stageRow[warp][k];
+                mine = stage[warp][k];
+            } else {  // a long span: the row by bisection over the 33 bounds
+                int lo = 0, hi = 32;
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (rowBegin[warp][mid] <= k) lo = mid;
+                    else hi = mid;
+                }
+                row = lo;
+                mine = adj[s0 + k];
+            }
+            const int r0 = rowBegin[warp][row], r1 = rowBegin[warp][row + 1];
+            const int oe = mine.x >= 0 ? mine.x : ~mine.x;
+            int cnt = 0, before = 0;
+            if (staged) {
+                for (int j = r0; j < r1; ++j) {
+                    const int same = stageEnd[warp][j] == oe ? 1 : 0;
+                    cnt += same;
+                    before += j < k ? same : 0;
+                }
+            } else {
+                for (int j = r0; j < r1; ++j) {
+                    const int x = adj[s0 + j].x;
+                    const int same = (x >= 0 ? x : ~x) == oe ? 1 : 0;
+                    cnt += same;
+                    before += j < k ? same : 0;
                 }
             }
-            if (a != b)
-                for (int j = rowStart[b], je = rowStart[b + 1]; j < je; ++j) {
-                    const int2 r = adj[j];
-                    if (r.x == a) {
-                        ++cnt;
-                        keepSmallest(ids, r.y);
-                    }
-                }
-            int me = 4;
-            for (int k = 3; k >= 0; --k)
-                if (ids[k] == h) me = k;
-            heValence[h] = (uint8_t)(cnt < 255 ? cnt : 255);
-            if (connectTwins && me < 4) {
-                int twin = -1;
-                if (cnt == 2) {
-                    twin = ids[1 - me];
-                } else if (cnt == 3) {
-                    twin = ids[me == 2 ? 0 : me + 1];
-                } else if (cnt == 4) {  // "HACKY_OLD_WAY", HalfedgeMesh.cu:250-281
-                    const int v0 = he[ids[0]].x, v1 = he[ids[1]].x, v2 = he[ids[2]].x;
-                    const int partner = v0 != v1 ? (me ^ 1) : (v0 != v2 ? (me ^ 2) : 3 - me);
-                    twin = ids[partner];
-                }
-                if (cnt >= 2 && cnt <= 4) setTwin(he, h, twin);
-            }
-            if (cnt == 4) {
-                orFaceAttr(faceAttr, e.y, MDMC_FACE_NON_MANIFOLD);
-                orVertexFlag(vflags, a, MDMC_VERTEX_NON_MANIFOLD);
-            } else if (cnt == 3) {
-                orVertexFlag(vflags, a, MDMC_VERTEX_WEIRD);
-            } else if (cnt == 1) {
-                orVertexFlag(vflags, a, MDMC_VERTEX_BOUNDARY);
-            }
-            if (me == 0) {  // the bucket's smallest halfedge counts it
+            if (before == 0) {
                 ++nE;
-                if (cnt == 3) ++nE3;
-                if (cnt == 4) ++nE4;
+                nE3 += cnt == 3 ? 1 : 0;
+                nE4 += cnt == 4 ? 1 : 0;
+            }
+            if (cnt == 2 && !connectTwins) continue;
+            // the rare path: the bucket's four smallest ids and their origins
+            const int m = m0 + row;
+            int ids[4] = {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF}, org[4] = {-1, -1, -1, -1};
+            for (int j = r0; j < r1; ++j) {
+                const int2 r = staged ? stage[warp][j] : adj[s0 + j];
+                if ((r.x >= 0 ? r.x : ~r.x) == oe) keepSmallest(ids, org, r.y, r.x >= 0 ? m : oe);
+            }
+            if (before == 0) {
                 if (cnt > 4) atomicOr(&ctr->status, kStatusBucketOverflow);
                 if (cnt >= 4) {
                     const unsigned long long slot = atomicAdd(&ctr->nmBuckets, 1ULL);
-                    if (slot < (unsigned long long)(md.H / 4 + 1)) nmList[slot] = make_int4(ids[0], ids[1], ids[2], ids[3]);
+                    if (slot < (unsigned long long)(md.H / 4 + 1))
+                        nmList[slot] = make_int4(ids[0], ids[1], ids[2], ids[3]);
                     else atomicOr(&ctr->status, kStatusBadIndex);
+                }
+            }
+            const int h = mine.y, origin = mine.x >= 0 ? m : oe;
+            if (connectTwins && cnt >= 2 && cnt <= 4) {
+                int kk = 4;
+#pragma unroll
+                for (int t = 3; t >= 0; --t)
+                    if (ids[t] == h) kk = t;
+                if (kk < 4) {
+                    int twin;
+                    if (cnt == 2) twin = ids[1 - kk];
+                    else if (cnt == 3) twin = ids[kk == 2 ? 0 : kk + 1];
+                    else  // "HACKY_OLD_WAY", HalfedgeMesh.cu:250-281
+                        twin = ids[org[0] != org[1] ? (kk ^ 1) : (org[0] != org[2] ? (kk ^ 2) : 3 - kk)];
+                    setTwin(he, h, twin);
+                }
+            }
+            if (cnt == 2) continue;
+            if (cnt == 4) orVertexFlag(vflags, origin, MDMC_VERTEX_NON_MANIFOLD);
+            else if (cnt == 3) orVertexFlag(vflags, origin, MDMC_VERTEX_WEIRD);
+            else if (cnt == 1) orVertexFlag(vflags, origin, MDMC_VERTEX_BOUNDARY);
+            if (cnt > 2) {
+                const int f = he[h].y;
+                if (inb(f, md.F)) {
+                    atomicAdd(reinterpret_cast<uint32_t*>(faceNM) + (f >> 2), 1u << ((f & 3) * 8));
+                    if (cnt == 4) orFaceAttr(faceAttr, f, MDMC_FACE_NON_MANIFOLD);
+                } else {
+                    atomicOr(&ctr->status, kStatusBadIndex);
                 }
             }
         }
     }
-    // one block reduction for the three counters (each <= 1 per halfedge)
-    blockAddPacked((unsigned long long)nE | ((unsigned long long)nE3 << 16) | ((unsigned long long)nE4 << 32),
-                   [&](unsigned long long t) {
-                       if (t & 0xFFFFu) atomicAdd(&ctr->edges, t & 0xFFFFu);
-                       if ((t >> 16) & 0xFFFFu) atomicAdd(&ctr->edges3, (t >> 16) & 0xFFFFu);
-                       if ((t >> 32) & 0xFFFFu) atomicAdd(&ctr->edges4, (t >> 32) & 0xFFFFu);
-                   });
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        nE += __shfl_down_sync(0xffffffffu, nE, o);
+        nE3 += __shfl_down_sync(0xffffffffu, nE3, o);
+        nE4 += __shfl_down_sync(0xffffffffu, nE4, o);
+    }
+    if (lane == 0) {
+        part[0][warp] = nE;
+        part[1][warp] = nE3;
+        part[2][warp] = nE4;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        unsigned long long t = 0;
+#pragma unroll
+        for (int w = 0; w < kBucketWarps; ++w) t += part[threadIdx.x][w];
+        if (t) atomicAdd(threadIdx.x == 0 ? &ctr->edges : (threadIdx.x == 1 ? &ctr->edges3 : &ctr->edges4), t);
+    }
 }
 
-void launchDegree(const int4* he, MeshDims md, int* deg, uint32_t* status, cudaStream_t s) {
+void launchEdgeRowDegree(const int4* he, MeshDims md, int* deg, int* rank, uint32_t* status, cudaStream_t s) {
     if (md.H <= 0) return;
     countLaunch();
-    kDegree<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, deg, status);
+    kEdgeRowDegree<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, deg, rank, status);
 }
 
-void launchEdgeBuckets(int4* he, MeshDims md, const int* rowStart, int* cursor, int2* adj, int connectTwins,
-                       uint16_t* faceAttr, uint8_t* vflags, uint8_t* heValence, int4* nmList, DevCounters* ctr,
+void launchEdgeBuckets(int4* he, MeshDims md, const int* rowStart, const int* rank, int2* adj, int connectTwins,
+                       uint16_t* faceAttr, uint8_t* vflags, uint8_t* faceNM, int4* nmList, DevCounters* ctr,
                        cudaStream_t s) {
     if (md.H <= 0) return;
     countLaunch(2);
-    kAdjScatter<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, rowStart, cursor, adj, &ctr->status);
-    kEdgeBuckets<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, rowStart, adj, connectTwins, faceAttr, vflags, heValence,
-                                                    nmList, ctr);
+    kEdgeRowScatter<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, rowStart, rank, adj);
+    const int64_t tiles = ((int64_t)md.V + 31) / 32;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((tiles + kBucketWarps - 1) / kBucketWarps, 152 * 8));
+    kEdgeBuckets<<<blocks, 32 * kBucketWarps, 0, s>>>(he, md, rowStart, adj, connectTwins, faceAttr, vflags, faceNM,
+                                                      nmList, ctr);
 }
 
 // ---------------------------------------------------------------------------
@@ -544,8 +649,11 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
 // output pass: face vertex quads, getNumQuadsWithNonManifoldEdges, and the
 // smallest outgoing halfedge of every vertex
 // ---------------------------------------------------------------------------
+// (edge sizes: faceNM, one count per face, when given; else heValence, the
+// quad pass's size of every halfedge's bucket)
 __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__ faceFirst, MeshDims md,
-                            const uint8_t* __restrict__ heValence, int4* __restrict__ quads, DevCounters* ctr) {
+                            const uint8_t* __restrict__ heValence, const uint8_t* __restrict__ faceNM,
+                            int4* __restrict__ quads, DevCounters* ctr) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     int cnt = -1;
     if (f < md.F) {
@@ -564,8 +672,10 @@ __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__
         quads[f] = make_int4(q[0], q[1], q[2], q[3]);
         if (ok) {
             cnt = 0;
-            for (int i = 0; i < 4; ++i)
-                if (heValence[hs[i]] > 2) ++cnt;
+            if (faceNM) cnt = faceNM[f];
+            else
+                for (int i = 0; i < 4; ++i)
+                    if (heValence[hs[i]] > 2) ++cnt;
         } else {
             atomicOr(&ctr->status, kStatusBadIndex);
         }
@@ -589,12 +699,12 @@ void launchVertexHalfedgeFix(int* vertexHE, int numVertices, cudaStream_t s) {
     kVertexHalfedgeFix<<<(numVertices + 255) / 256, 256, 0, s>>>(vertexHE, numVertices);
 }
 
-void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, int4* quads,
-                  int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
+void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, const uint8_t* faceNM,
+                  int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
     (void)status;
     if (md.F > 0) {
         countLaunch();
-        kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, heValence, quads, ctr);
+        kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, heValence, faceNM, quads, ctr);
     }
     if (md.V > 0 && !vertexHEDone) {
         launchVertexStar(he, md, vertexHE, nullptr, s);

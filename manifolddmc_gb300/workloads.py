@@ -86,11 +86,16 @@ def torus_points(count, major, minor, centre, seed):
 CONFIGS = {
     "blobs64_pad": ("64^3 fp32 grid, 8 Gaussian blobs (sigma 4-10), padded by 1, iso 0.5",
                     lambda seed=0: gaussian_blobs(64, 8, (4.0, 10.0), seed), 0.5, 0, True),
+    "noise128": ("128^3 fp32 iid uniform[0,1] noise, iso 0.5 (the noise workload at 1/8 size, for profiling)",
+                 lambda seed=1: uniform_noise(128, seed), 0.5, 0, False),
     "noise256": ("256^3 fp32 iid uniform[0,1] noise, iso 0.5",
                  lambda seed=1: uniform_noise(256, seed), 0.5, 0, False),
     "blobs129_refine4": ("129^3 fp32 grid, 64 Gaussian blobs (sigma 3-12), trilinearly refined x4 "
                          "to 513^3 samples = 512^3 cells, iso 0.4",
                          lambda seed=2: gaussian_blobs(129, 64, (3.0, 12.0), seed), 0.4, 3, False),
+    "blobs65_refine4": ("65^3 fp32 grid, 16 Gaussian blobs (sigma 3-12), trilinearly refined x4 to 257^3 samples = "
+                        "256^3 cells, iso 0.4 (the refined workload at 1/8 size, for profiling)",
+                        lambda seed=2: gaussian_blobs(65, 16, (3.0, 12.0), seed), 0.4, 3, False),
     "noise513": ("513^3 fp32 iid uniform[0,1] noise (512^3 cells), iso 0.5: the noise grid at the headline size",
                  lambda seed=5: uniform_noise(513, seed), 0.5, 0, False),
     "sphere128_sdf": ("128^3 fp32 signed distance to a sphere of radius 40 cells, iso 0, surface iteration off "

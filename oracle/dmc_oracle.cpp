@@ -20,6 +20,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <unordered_map>
 #ifdef _OPENMP
 #include <omp.h>
@@ -28,45 +29,54 @@
 
 namespace oracle {
 
+// The arithmetic type of the restatement: float (the default, bit for bit
+// the CUDA path's operations) or, with -DMDMC_ORACLE_REAL=double, the FP64
+// form of the same algorithm that is timed as the CPU baseline.  Input
+// samples and the C API stay float in both.
+#ifndef MDMC_ORACLE_REAL
+#define MDMC_ORACLE_REAL float
+#endif
+typedef MDMC_ORACLE_REAL Real;
+
 // ------------------------------------------------------------------------ //
 // small float vector helpers, each operation rounded once (glm semantics)
 // ------------------------------------------------------------------------ //
 struct V3 {
-    float x, y, z;
+    Real x, y, z;
 };
-static inline V3 v3(float x, float y, float z) { return {x, y, z}; }
+static inline V3 v3(Real x, Real y, Real z) { return {x, y, z}; }
 static inline V3 add(V3 a, V3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
 static inline V3 sub(V3 a, V3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 static inline V3 mul(V3 a, V3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
-static inline V3 muls(V3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
-static inline V3 smul(float s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
+static inline V3 muls(V3 a, Real s) { return {a.x * s, a.y * s, a.z * s}; }
+static inline V3 smul(Real s, V3 a) { return {s * a.x, s * a.y, s * a.z}; }
 static inline V3 divv(V3 a, V3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
-static inline V3 divs(V3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
-static inline float gmin(float x, float y) { return (y < x) ? y : x; }  // glm::min
-static inline float gmax(float x, float y) { return (x < y) ? y : x; }  // glm::max
-static inline float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+static inline V3 divs(V3 a, Real s) { return {a.x / s, a.y / s, a.z / s}; }
+static inline Real gmin(Real x, Real y) { return (y < x) ? y : x; }  // glm::min
+static inline Real gmax(Real x, Real y) { return (x < y) ? y : x; }  // glm::max
+static inline Real gclamp(Real x, Real lo, Real hi) { return gmin(gmax(x, lo), hi); }
 // glm::normalize: v * (1 / sqrt(dot(v, v))), dot = (x*x + y*y) + z*z
 static inline V3 normalize(V3 v) {
-    float d = v.x * v.x + v.y * v.y;
+    Real d = v.x * v.x + v.y * v.y;
     d = d + v.z * v.z;
-    float inv = 1.0f / std::sqrt(d);
+    Real inv = 1.0f / std::sqrt(d);
     return muls(v, inv);
 }
 
-static const float kEpsilon = 0.0001f;  // LazyEngine::Constants::EPSILON
+static const Real kEpsilon = 0.0001f;  // LazyEngine::Constants::EPSILON
 
 // ------------------------------------------------------------------------ //
 // Grid, D/UniformGrid.h:44-130
 // ------------------------------------------------------------------------ //
 struct Grid {
     int d[3];
-    float origin[3];
-    float deltas[3];
-    const float* v;
-    inline float at(int x, int y, int z) const {
+    Real origin[3];
+    Real deltas[3];
+    const Real* v;
+    inline Real at(int x, int y, int z) const {
         return v[(size_t)z * d[0] * d[1] + (size_t)y * d[0] + x];
     }
-    inline float atClamped(int x, int y, int z) const {
+    inline Real atClamped(int x, int y, int z) const {
         x = x < 0 ? 0 : (x > d[0] - 1 ? d[0] - 1 : x);
         y = y < 0 ? 0 : (y > d[1] - 1 ? d[1] - 1 : y);
         z = z < 0 ? 0 : (z > d[2] - 1 ? d[2] - 1 : z);
@@ -77,39 +87,39 @@ struct Grid {
 };
 
 // Interpolation<float>::interpolateTrilinearly, D/Utils/Interpolation.inl:76-84
-static inline float trilinear(const float s[8], V3 p) {
-    float a = s[0] + p.x * (s[1] - s[0]);
-    float b = s[2] + p.x * (s[3] - s[2]);
-    float c = s[4] + p.x * (s[5] - s[4]);
-    float e = s[6] + p.x * (s[7] - s[6]);
-    float lo = (1.f - p.y) * a + p.y * b;
-    float hi = (1.f - p.y) * c + p.y * e;
+static inline Real trilinear(const Real s[8], V3 p) {
+    Real a = s[0] + p.x * (s[1] - s[0]);
+    Real b = s[2] + p.x * (s[3] - s[2]);
+    Real c = s[4] + p.x * (s[5] - s[4]);
+    Real e = s[6] + p.x * (s[7] - s[6]);
+    Real lo = (1.f - p.y) * a + p.y * b;
+    Real hi = (1.f - p.y) * c + p.y * e;
     return (1.f - p.z) * lo + p.z * hi;
 }
 static inline V3 trilinear3(const V3 s[8], V3 p) {
-    float xs[8], ys[8], zs[8];
+    Real xs[8], ys[8], zs[8];
     for (int i = 0; i < 8; ++i) { xs[i] = s[i].x; ys[i] = s[i].y; zs[i] = s[i].z; }
     return v3(trilinear(xs, p), trilinear(ys, p), trilinear(zs, p));
 }
 
 // UniformGrid::evaluateCellCornerValues, D/UniformGrid.inl:414-427
-static inline void cornerValues(const Grid& g, int x, int y, int z, float s[8]) {
+static inline void cornerValues(const Grid& g, int x, int y, int z, Real s[8]) {
     for (int i = 0; i < 8; ++i) s[i] = g.atClamped(x + (i & 1), y + ((i >> 1) & 1), z + ((i >> 2) & 1));
 }
 
 // ------------------------------------------------------------------------ //
 // refineGrid, D/UniformGrid.inl:279-319 (+ host geometry :575-608)
 // ------------------------------------------------------------------------ //
-static void refine(const Grid& in, int r, bool pad, std::vector<float>& out, int od[3], float oo[3],
-                   float odl[3]) {
+static void refine(const Grid& in, int r, bool pad, std::vector<Real>& out, int od[3], Real oo[3],
+                   Real odl[3]) {
     for (int a = 0; a < 3; ++a) {
         od[a] = in.d[a] + (in.d[a] - 1) * r + (pad ? 2 : 0);
-        odl[a] = (in.deltas[a] * 1.f) / ((float)r + 1.f);
+        odl[a] = (in.deltas[a] * 1.f) / ((Real)r + 1.f);
         oo[a] = in.origin[a];
         if (pad) oo[a] = oo[a] - odl[a];
     }
     out.assign((size_t)od[0] * od[1] * od[2], 0.f);
-    const float f = (float)(r + 1);
+    const Real f = (Real)(r + 1);
 #pragma omp parallel for schedule(static)
     for (int z = 0; z < od[2]; ++z)
         for (int y = 0; y < od[1]; ++y)
@@ -120,10 +130,10 @@ static void refine(const Grid& in, int r, bool pad, std::vector<float>& out, int
                     iy = std::min(std::max(iy, 1), od[1] - 2) - 1;
                     iz = std::min(std::max(iz, 1), od[2] - 2) - 1;
                 }
-                float qx = (float)ix / f, qy = (float)iy / f, qz = (float)iz / f;
+                Real qx = (Real)ix / f, qy = (Real)iy / f, qz = (Real)iz / f;
                 int mx = (int)std::floor(qx), my = (int)std::floor(qy), mz = (int)std::floor(qz);
-                V3 diff = v3(qx - (float)mx, qy - (float)my, qz - (float)mz);
-                float s[8];
+                V3 diff = v3(qx - (Real)mx, qy - (Real)my, qz - (Real)mz);
+                Real s[8];
                 cornerValues(in, mx, my, mz, s);
                 out[(size_t)z * od[0] * od[1] + (size_t)y * od[0] + x] = trilinear(s, diff);
             }
@@ -181,7 +191,7 @@ bool caseIsAmbiguous(int c) {
 }
 
 // marchingCubesAsymptoticPolygon, D/CellIntersection.inl:202-338
-static uint64_t asymptoticContours(const float s[8], float iso, int& numContours) {
+static uint64_t asymptoticContours(const Real s[8], Real iso, int& numContours) {
     unsigned char seg[12];
     for (int i = 0; i < 12; ++i) seg[i] = 0xFF;
     auto connect = [&](int in, int out) {
@@ -190,7 +200,7 @@ static uint64_t asymptoticContours(const float s[8], float iso, int& numContours
     };
     for (int f = 0; f < 6; ++f) {
         int e[4];
-        float val[4];
+        Real val[4];
         unsigned fc = 0;
         for (int i = 0; i < 4; ++i) {
             int v = nib(kFaceCorners[f], i);
@@ -214,11 +224,11 @@ static uint64_t asymptoticContours(const float s[8], float iso, int& numContours
             case 6:
             case 9: {
                 // (a*d - b*c) / (a + d - b - c)
-                float num = val[0] * val[3] - val[1] * val[2];
-                float den = val[0] + val[3];
+                Real num = val[0] * val[3] - val[1] * val[2];
+                Real den = val[0] + val[3];
                 den = den - val[1];
                 den = den - val[2];
-                float decision = num / den;
+                Real decision = num / den;
                 if (fc == 6) {
                     if (decision >= iso) { connect(e[3], e[0]); connect(e[1], e[2]); }
                     else { connect(e[1], e[0]); connect(e[3], e[2]); }
@@ -254,7 +264,7 @@ static uint64_t asymptoticContours(const float s[8], float iso, int& numContours
     return c;
 }
 
-static uint64_t cellContours(int cs, const float s[8], float iso, int& n) {
+static uint64_t cellContours(int cs, const Real s[8], Real iso, int& n) {
     if (caseIsAmbiguous(cs)) return asymptoticContours(s, iso, n);
     uint64_t c = kContourTable[cs];
     n = 0;
@@ -263,7 +273,7 @@ static uint64_t cellContours(int cs, const float s[8], float iso, int& n) {
 }
 
 // UniformGrid::computeGradients, D/UniformGrid.inl:325-379
-static void cornerGradients(const Grid& g, int x, int y, int z, const float s[8], V3 out[8]) {
+static void cornerGradients(const Grid& g, int x, int y, int z, const Real s[8], V3 out[8]) {
     auto cl = [](int dim, int ii) { return ii < 0 ? 0 : (ii >= dim ? dim - 1 : ii); };
     const int X = g.d[0], Y = g.d[1], Z = g.d[2];
     V3 gr[8];
@@ -288,22 +298,22 @@ static void cornerGradients(const Grid& g, int x, int y, int z, const float s[8]
 
 // VertexToSurfaceIterator, D/CellIntersection.inl:12-122
 struct SurfaceIterator {
-    const float* s;
-    float iso;
-    float step = 0.05f;
+    const Real* s;
+    Real iso;
+    Real step = 0.05f;
     int maxIter = 30;
 
     V3 gradient(V3 p) const {
-        float gx = (1 - p.z) * ((1 - p.y) * (s[1] - s[0]) + p.y * (s[3] - s[2])) +
+        Real gx = (1 - p.z) * ((1 - p.y) * (s[1] - s[0]) + p.y * (s[3] - s[2])) +
                    p.z * ((1 - p.y) * (s[5] - s[4]) + p.y * (s[7] - s[6]));
-        float gy = (1 - p.z) * ((1 - p.x) * (s[2] - s[0]) + p.x * (s[3] - s[1])) +
+        Real gy = (1 - p.z) * ((1 - p.x) * (s[2] - s[0]) + p.x * (s[3] - s[1])) +
                    p.z * ((1 - p.x) * (s[6] - s[4]) + p.x * (s[7] - s[5]));
-        float gz = (1 - p.y) * ((1 - p.x) * (s[4] - s[0]) + p.x * (s[5] - s[1])) +
+        Real gz = (1 - p.y) * ((1 - p.x) * (s[4] - s[0]) + p.x * (s[5] - s[1])) +
                    p.y * ((1 - p.x) * (s[6] - s[2]) + p.x * (s[7] - s[3]));
         return v3(gx, gy, gz);
     }
     // updateGradient, :83-122; returns breakNow, sets clamp flags
-    bool update(V3& point, V3& grad, const V3& in1, V3& in2, float v1, float& v2, bool clamped[3]) const {
+    bool update(V3& point, V3& grad, const V3& in1, V3& in2, Real v1, Real& v2, bool clamped[3]) const {
         grad = normalize(grad);
         in2 = add(in1, smul(step, grad));
         clamped[0] = in2.x <= 0.f || in2.x >= 1.f;
@@ -312,7 +322,7 @@ struct SurfaceIterator {
         in2 = v3(gclamp(in2.x, 0.f, 1.f), gclamp(in2.y, 0.f, 1.f), gclamp(in2.z, 0.f, 1.f));
         v2 = trilinear(s, in2);
         if ((v1 <= iso && iso <= v2) || (v2 <= iso && iso <= v1)) {
-            float e = v1;
+            Real e = v1;
             if (v1 != v2) e = (iso - v1) / (v2 - v1);
             point = add(in1, smul(e, sub(in2, in1)));
             return true;
@@ -321,8 +331,8 @@ struct SurfaceIterator {
     }
     void move(V3& point) const {
         V3 in1 = point;
-        float v1 = trilinear(s, in1);
-        float v2 = 0.f;
+        Real v1 = trilinear(s, in1);
+        Real v2 = 0.f;
         for (int i = 0; i < maxIter; ++i) {
             V3 g = gradient(in1);
             if (v1 > iso) g = v3(-g.x, -g.y, -g.z);
@@ -339,7 +349,7 @@ struct SurfaceIterator {
             in1 = in2;
             v1 = v2;
         }
-        const float lo = kEpsilon, hi = 1.f - kEpsilon;
+        const Real lo = kEpsilon, hi = 1.f - kEpsilon;
         point = v3(gclamp(point.x, lo, hi), gclamp(point.y, lo, hi), gclamp(point.z, lo, hi));
     }
 };
@@ -383,7 +393,7 @@ static inline uint64_t edgeKey(int a, int b) {
 
 struct Result {
     // DMC stage
-    std::vector<float> dmcPos, dmcNrm;
+    std::vector<Real> dmcPos, dmcNrm;
     std::vector<int> dmcQuads;
     std::vector<uint16_t> dmcAttr;
     // per DMC vertex: its cell (3 ints) and the cell edges of its contour (12-bit mask)
@@ -392,7 +402,7 @@ struct Result {
     // per final vertex: the DMC vertex it descends from (-1: none)
     std::vector<int> parent;
     // final mesh
-    std::vector<float> pos, nrm;  // 3 per vertex
+    std::vector<Real> pos, nrm;  // 3 per vertex
     std::vector<HE> he;
     std::vector<int> faceFirst;
     std::vector<uint16_t> faceAttr;
@@ -430,7 +440,7 @@ struct EdgeTable {
 };
 
 struct Mesh {
-    std::vector<float> pos, nrm;
+    std::vector<Real> pos, nrm;
     std::vector<HE> he;
     std::vector<int> faceFirst;
     std::vector<uint16_t> faceAttr;
@@ -532,20 +542,20 @@ struct QuadEntry {
 // One z-slab of cells [z0, z1): vertices numbered from 0 within the slab,
 // quad slots keyed by the global edge key.
 struct SlabDMC {
-    std::vector<float> pos, nrm;
+    std::vector<Real> pos, nrm;
     std::vector<int> cells;
     std::vector<uint16_t> edgeMasks;
     std::unordered_map<uint64_t, QuadEntry> table;
     uint32_t anomalies = 0;
 };
 
-static void runDMCSlab(const Grid& g, float iso, bool surfaceIteration, int z0, int z1, SlabDMC& out) {
+static void runDMCSlab(const Grid& g, Real iso, bool surfaceIteration, int z0, int z1, SlabDMC& out) {
     const int X = g.d[0], Y = g.d[1];
     V3 origin = g.o(), dl = g.dl();
     for (int z = z0; z < z1; ++z)
         for (int y = 0; y + 1 < Y; ++y)
             for (int x = 0; x + 1 < X; ++x) {
-                float s[8];
+                Real s[8];
                 cornerValues(g, x, y, z, s);
                 int cs = 0;
                 for (int i = 0; i < 8; ++i) cs |= (s[i] >= iso ? 1 : 0) << i;
@@ -561,21 +571,21 @@ static void runDMCSlab(const Grid& g, float iso, bool surfaceIteration, int z0, 
                     for (int i = 0; i < sz; ++i) {
                         int e = contourEdge(c, t, i);
                         int a0 = kEdgeV0[e], a1 = kEdgeV1[e];
-                        float w = (iso - s[a0]) / (s[a1] - s[a0]);
+                        Real w = (iso - s[a0]) / (s[a1] - s[a0]);
                         // computeLocalCoordinateOffset, :176-200: the edge's own
                         // axis gets the crossing, the others corner a0's coordinate
-                        float c0[3] = {(float)(a0 & 1), (float)((a0 >> 1) & 1), (float)((a0 >> 2) & 1)};
+                        Real c0[3] = {(Real)(a0 & 1), (Real)((a0 >> 1) & 1), (Real)((a0 >> 2) & 1)};
                         c0[kEdgeAxis[e]] = w;
                         p = add(p, v3(c0[0], c0[1], c0[2]));
                         if (s[a0] < iso) edgy |= 1u << e;
                     }
-                    p = divs(p, (float)sz);
+                    p = divs(p, (Real)sz);
                     if (surfaceIteration) {
                         SurfaceIterator it{s, iso};
                         it.move(p);
                     }
                     V3 nm = normalize(trilinear3(normals, p));
-                    V3 wp = add(origin, mul(add(v3((float)x, (float)y, (float)z), p), dl));
+                    V3 wp = add(origin, mul(add(v3((Real)x, (Real)y, (Real)z), p), dl));
                     int vid = (int)(out.pos.size() / 3);
                     out.pos.push_back(wp.x); out.pos.push_back(wp.y); out.pos.push_back(wp.z);
                     out.nrm.push_back(nm.x); out.nrm.push_back(nm.y); out.nrm.push_back(nm.z);
@@ -604,8 +614,8 @@ static void runDMCSlab(const Grid& g, float iso, bool surfaceIteration, int z0, 
 // performDualMarchingCubes + mapQuadrilaterals (D/DualMarchingCubes.cu:38-85):
 // z-slabs in parallel (OpenMP), joined in slab order, so vertex ids follow
 // the cells' (z, y, x) order as in a single pass
-static void runDMC(const Grid& g, float iso, bool surfaceIteration, std::vector<float>& pos,
-                   std::vector<float>& nrm, std::vector<int>& quads, std::vector<uint16_t>& attr,
+static void runDMC(const Grid& g, Real iso, bool surfaceIteration, std::vector<Real>& pos,
+                   std::vector<Real>& nrm, std::vector<int>& quads, std::vector<uint16_t>& attr,
                    std::vector<int>& cells, std::vector<uint16_t>& edgeMasks, uint32_t& anomalies) {
     const int Zc = std::max(g.d[2] - 1, 0);
     int slabs = 1;
@@ -671,7 +681,7 @@ static inline int gridIndex(const Grid& g, const int c[3]) {
     return c[2] * g.d[0] * g.d[1] + c[1] * g.d[0] + c[0];
 }
 
-static void reconnect(Mesh& m, const Grid& g, float iso) {
+static void reconnect(Mesh& m, const Grid& g, Real iso) {
     for (auto& kv : m.table.map) {
         const Bucket& b = kv.second;
         if (b.count < 4) continue;  // isHashTableEntryNonManifold: all 4 ids set
@@ -724,31 +734,31 @@ static void reconnect(Mesh& m, const Grid& g, float iso) {
         if (mn[0] < 0 || mn[1] < 0 || mn[2] < 0 || mn[0] + 1 >= g.d[0] || mn[1] + 1 >= g.d[1] ||
             mn[2] + 1 >= g.d[2])
             m.anomalies |= kSWall;
-        float w[4];
+        Real w[4];
         w[0] = g.atClamped(mn[0], mn[1], mn[2]);
         w[1] = g.atClamped(mn[0] + xo[0], mn[1] + xo[1], mn[2] + xo[2]);
         w[2] = g.atClamped(mn[0] + xo[0] + yo[0], mn[1] + xo[1] + yo[1], mn[2] + xo[2] + yo[2]);
         w[3] = g.atClamped(mn[0] + yo[0], mn[1] + yo[1], mn[2] + yo[2]);
-        V3 corner0 = add(g.o(), mul(g.dl(), v3((float)mn[0], (float)mn[1], (float)mn[2])));
-        V3 corner2 = add(g.o(), mul(g.dl(), v3((float)(mn[0] + xo[0] + yo[0]), (float)(mn[1] + xo[1] + yo[1]),
-                                              (float)(mn[2] + xo[2] + yo[2]))));
+        V3 corner0 = add(g.o(), mul(g.dl(), v3((Real)mn[0], (Real)mn[1], (Real)mn[2])));
+        V3 corner2 = add(g.o(), mul(g.dl(), v3((Real)(mn[0] + xo[0] + yo[0]), (Real)(mn[1] + xo[1] + yo[1]),
+                                              (Real)(mn[2] + xo[2] + yo[2]))));
         bool omitX = xo[0] == 0 && yo[0] == 0;
         bool omitY = xo[1] == 0 && yo[1] == 0;
-        auto down = [&](V3 p, float& u, float& v) {
+        auto down = [&](V3 p, Real& u, Real& v) {
             if (omitX) { u = p.y; v = p.z; }
             else if (omitY) { u = p.x; v = p.z; }
             else { u = p.x; v = p.y; }
         };
-        float minU, minV, maxU, maxV;
+        Real minU, minV, maxU, maxV;
         down(corner0, minU, minV);
         down(corner2, maxU, maxV);
         int sorted[4] = {-1, -1, -1, -1};
         for (int i = 0; i < 4; ++i) {
             int hid = b.ids[i];
             int opp = m.he[m.he[m.he[hid].next].next].origin;
-            float u, v;
+            Real u, v;
             down(m.P(opp), u, v);
-            float mnU = u - minU, mnV = v - minV, mxU = u - maxU, mxV = v - maxV;
+            Real mnU = u - minU, mnV = v - minV, mxU = u - maxU, mxV = v - maxV;
             if (mnV < 0.f) sorted[0] = hid;
             if (mxU > 0.f) sorted[1] = hid;
             if (mxV > 0.f) sorted[2] = hid;
@@ -758,11 +768,11 @@ static void reconnect(Mesh& m, const Grid& g, float iso) {
         for (int i = 0; i < 4; ++i) ok = ok && sorted[i] != -1;
         if (!ok) continue;
         // AsymptoticDecider2D::quadrant0BelongsTogether, D/Utils/AsymptoticDecider.h:119-164
-        float m00 = w[0], m10 = w[1], m11 = w[2], m01 = w[3];
-        float C = m00 - m10;
+        Real m00 = w[0], m10 = w[1], m11 = w[2], m01 = w[3];
+        Real C = m00 - m10;
         C = C - m01;
         C = C + m11;
-        float delta = (m00 * m11 - m10 * m01) / C;
+        Real delta = (m00 * m11 - m10 * m01) / C;
         bool together = (m00 < iso && delta >= iso) || (m00 >= iso && delta < iso);
         bool connect01 = !together;
         if (connect01) {
@@ -832,7 +842,7 @@ struct MergeList {
     }
 };
 
-static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
+static int runSplitter(Mesh& m, const Grid& g, Real iso, int step) {
     int iterations = 0;
     while (true) {
         std::vector<int> nm;
@@ -846,7 +856,7 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
         const int nh = 4 * n + (doSub ? 16 * n : 0);
         const int nf = n + (doSub ? 4 * n : 0);
         // working copies
-        std::vector<float> cpos(3 * (size_t)nv, 0.f), cnrm(3 * (size_t)nv, 0.f);
+        std::vector<Real> cpos(3 * (size_t)nv, 0.f), cnrm(3 * (size_t)nv, 0.f);
         std::vector<uint8_t> vfl(nv, 0), hfl(nh, 0), ffl(nf, 0);
         std::vector<int> vC2O(nv, -1), hC2O(nh, -1), fC2O(nf, -1);
         std::vector<int> cparent(nv, -1);  // mesh vertex each working vertex comes from
@@ -910,7 +920,7 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
         }
         // performSubdivideQuads :650-731
         if (doSub) {
-            const float uvs[4][2] = {{0.33f, 0.33f}, {0.67f, 0.33f}, {0.67f, 0.67f}, {0.33f, 0.67f}};
+            const Real uvs[4][2] = {{0.33f, 0.33f}, {0.67f, 0.33f}, {0.67f, 0.67f}, {0.33f, 0.67f}};
             for (int k = 0; k < n; ++k) {
                 int hid[4], vid[4];
                 int h = cfirst[k];
@@ -922,9 +932,9 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
                 }
                 int inner[4];
                 for (int i = 0; i < 4; ++i) {
-                    float u = uvs[i][0], v = uvs[i][1];
+                    Real u = uvs[i][0], v = uvs[i][1];
                     // Interpolation<Vertex>::interpolateBilinearly with glm::mix
-                    auto mix = [](V3 a, V3 b, float f) { return add(muls(a, 1.f - f), muls(b, f)); };
+                    auto mix = [](V3 a, V3 b, Real f) { return add(muls(a, 1.f - f), muls(b, f)); };
                     V3 pa = mix(P[0], P[1], u), pb = mix(P[3], P[2], u), pp = mix(pa, pb, v);
                     V3 na = mix(N[0], N[1], u), nb = mix(N[3], N[2], u), nn = mix(na, nb, v);
                     int c = 4 * n + 4 * k + i;
@@ -1026,7 +1036,7 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
                         if (q < smallest) { obsolete = true; smallest = q; }
                     }
                     if (obsolete) { vfl[v] |= kFlagRemove; continue; }
-                    p = divs(p, (float)np);
+                    p = divs(p, (Real)np);
                     cpos[3 * smallest] = p.x; cpos[3 * smallest + 1] = p.y; cpos[3 * smallest + 2] = p.z;
                     // the reference stores the averaged position as the normal (:989)
                     cnrm[3 * smallest] = p.x; cnrm[3 * smallest + 1] = p.y; cnrm[3 * smallest + 2] = p.z;
@@ -1070,10 +1080,10 @@ static int runSplitter(Mesh& m, const Grid& g, float iso, int step) {
                 V3 p = v3(cpos[3 * v], cpos[3 * v + 1], cpos[3 * v + 2]);
                 int idx[3];
                 cellOf(g, p, idx);
-                float s[8];
+                Real s[8];
                 cornerValues(g, idx[0], idx[1], idx[2], s);
-                V3 fi = v3((float)idx[0], (float)idx[1], (float)idx[2]);
-                V3 fi1 = v3((float)(idx[0] + 1), (float)(idx[1] + 1), (float)(idx[2] + 1));
+                V3 fi = v3((Real)idx[0], (Real)idx[1], (Real)idx[2]);
+                V3 fi1 = v3((Real)(idx[0] + 1), (Real)(idx[1] + 1), (Real)(idx[2] + 1));
                 V3 mn = add(g.o(), mul(fi, g.dl()));
                 V3 mx = add(g.o(), mul(fi1, g.dl()));
                 V3 local = divv(sub(p, mn), sub(mx, mn));
@@ -1202,7 +1212,7 @@ static void detectNonManifoldVertices(Mesh& m) {
 // 3 * sample + axis and triangles the cells' (z, y, x) order, then the table.
 // ------------------------------------------------------------------------ //
 struct MCMesh {
-    std::vector<float> pos, nrm;
+    std::vector<Real> pos, nrm;
     std::vector<int> tris;
 };
 
@@ -1210,13 +1220,13 @@ struct MCMesh {
 // (UniformGrid::gradient, O/UniformGrid.h:278-330: each corner's entry)
 static V3 pointGradient(const Grid& g, int x, int y, int z) {
     V3 d = g.dl();
-    float gx = 0.5f * (g.atClamped(x + 1, y, z) - g.atClamped(x - 1, y, z)) / d.x;
-    float gy = 0.5f * (g.atClamped(x, y + 1, z) - g.atClamped(x, y - 1, z)) / d.y;
-    float gz = 0.5f * (g.atClamped(x, y, z + 1) - g.atClamped(x, y, z - 1)) / d.z;
+    Real gx = 0.5f * (g.atClamped(x + 1, y, z) - g.atClamped(x - 1, y, z)) / d.x;
+    Real gy = 0.5f * (g.atClamped(x, y + 1, z) - g.atClamped(x, y - 1, z)) / d.y;
+    Real gz = 0.5f * (g.atClamped(x, y, z + 1) - g.atClamped(x, y, z - 1)) / d.z;
     return v3(gx, gy, gz);
 }
 
-static MCMesh* standardMC(const Grid& g, float iso) {
+static MCMesh* standardMC(const Grid& g, Real iso) {
     MCMesh* m = new MCMesh();
     const int X = g.d[0], Y = g.d[1], Z = g.d[2];
     if (X < 2 || Y < 2 || Z < 2) return m;  // no cells
@@ -1229,16 +1239,16 @@ static MCMesh* standardMC(const Grid& g, float iso) {
                 for (int a = 0; a < 3; ++a) {
                     const int x1 = x + (a == 0), y1 = y + (a == 1), z1 = z + (a == 2);
                     if (x1 >= X || y1 >= Y || z1 >= Z) continue;
-                    const float u0 = g.at(x, y, z), u1 = g.at(x1, y1, z1);
+                    const Real u0 = g.at(x, y, z), u1 = g.at(x1, y1, z1);
                     if ((u0 >= iso) == (u1 >= iso)) continue;
                     const size_t e = 3 * (((size_t)z * Y + y) * X + x) + a;
                     vid[e] = (int)(m->pos.size() / 3);
-                    const float l = (iso - u0) / (u1 - u0);
-                    const float p0[3] = {o.x + (float)x * dl.x, o.y + (float)y * dl.y, o.z + (float)z * dl.z};
-                    const float p1[3] = {o.x + (float)x1 * dl.x, o.y + (float)y1 * dl.y, o.z + (float)z1 * dl.z};
+                    const Real l = (iso - u0) / (u1 - u0);
+                    const Real p0[3] = {o.x + (Real)x * dl.x, o.y + (Real)y * dl.y, o.z + (Real)z * dl.z};
+                    const Real p1[3] = {o.x + (Real)x1 * dl.x, o.y + (Real)y1 * dl.y, o.z + (Real)z1 * dl.z};
                     const V3 n0 = pointGradient(g, x, y, z), n1 = pointGradient(g, x1, y1, z1);
                     V3 ni = v3(n0.x + l * (n1.x - n0.x), n0.y + l * (n1.y - n0.y), n0.z + l * (n1.z - n0.z));
-                    const float f = std::sqrt(ni.x * ni.x + ni.y * ni.y + ni.z * ni.z);
+                    const Real f = std::sqrt(ni.x * ni.x + ni.y * ni.y + ni.z * ni.z);
                     ni = v3(ni.x / f, ni.y / f, ni.z / f);
                     for (int k = 0; k < 3; ++k) m->pos.push_back(p0[k] + l * (p1[k] - p0[k]));
                     m->nrm.push_back(ni.x);
@@ -1248,7 +1258,7 @@ static MCMesh* standardMC(const Grid& g, float iso) {
     for (int z = 0; z + 1 < Z; ++z)
         for (int y = 0; y + 1 < Y; ++y)
             for (int x = 0; x + 1 < X; ++x) {
-                float sv[8];
+                Real sv[8];
                 cornerValues(g, x, y, z, sv);
                 int cs = 0;
                 for (int i = 0; i < 8; ++i) cs |= (sv[i] >= iso ? 1 : 0) << i;
@@ -1327,7 +1337,7 @@ static void compactAndRebuild(Mesh& m, const std::vector<int>& type, int removed
                               bool remapPatternQuads) {
     const int V = m.numV(), F = (int)m.faceFirst.size();
     std::vector<int> addr(V, -1);
-    std::vector<float> pos, nrm;
+    std::vector<Real> pos, nrm;
     std::vector<int> parent;
     for (int v = 0; v < V; ++v) {
         if (type[v] == removedType) continue;
@@ -1473,7 +1483,7 @@ static void simplify3333(Mesh& m) {
     compactAndRebuild(m, type, kTypePattern, target, true);
 }
 
-static Result* run(const Grid& g, float iso, const mdmc_oracle_options& opt) {
+static Result* run(const Grid& g, Real iso, const mdmc_oracle_options& opt) {
     Result* r = new Result();
     std::memset(r->stats, 0, sizeof r->stats);
     uint32_t anomalies = 0;
@@ -1554,6 +1564,39 @@ static Result* run(const Grid& g, float iso, const mdmc_oracle_options& opt) {
 // ------------------------------------------------------------------------ //
 // C API
 // ------------------------------------------------------------------------ //
+namespace {
+// float input as the restatement's arithmetic type (a copy unless that is float)
+struct RealInput {
+    std::vector<oracle::Real> copy;
+    const oracle::Real* p = nullptr;
+    RealInput(const float* v, size_t n) {
+        if (std::is_same<oracle::Real, float>::value) {
+            p = reinterpret_cast<const oracle::Real*>(v);
+        } else {
+            copy.assign(v, v + n);
+            p = copy.data();
+        }
+    }
+};
+template <class T>
+void copyFloats(float* dst, const std::vector<T>& v) {
+    if (std::is_same<T, float>::value) std::memcpy(dst, v.data(), v.size() * sizeof(float));
+    else
+        for (size_t i = 0; i < v.size(); ++i) dst[i] = (float)v[i];
+}
+oracle::Grid gridOf(const RealInput& in, const int dims[3], const float origin[3], const float spacing[3]) {
+    oracle::Grid g;
+    for (int a = 0; a < 3; ++a) {
+        g.d[a] = dims[a];
+        g.origin[a] = origin[a];
+        g.deltas[a] = spacing[a];
+    }
+    g.v = in.p;
+    return g;
+}
+size_t samplesOf(const int dims[3]) { return (size_t)dims[0] * dims[1] * dims[2]; }
+}  // namespace
+
 extern "C" {
 
 void mdmc_oracle_default_options(mdmc_oracle_options* o) {
@@ -1585,19 +1628,36 @@ int mdmc_oracle_read_bin(const char* path, int dims[3], float spacing[3], float 
 void mdmc_oracle_refine(const float* in, const int dims[3], const float origin[3], const float spacing[3],
                         int refinement, int pad, float* out, int out_dims[3], float out_origin[3],
                         float out_spacing[3]) {
+    const RealInput input(in, samplesOf(dims));
+    const oracle::Grid g = gridOf(input, dims, origin, spacing);
+    std::vector<oracle::Real> res;
+    oracle::Real oo[3], os[3];
+    oracle::refine(g, refinement, pad != 0, res, out_dims, oo, os);
+    for (int a = 0; a < 3; ++a) {
+        out_origin[a] = (float)oo[a];
+        out_spacing[a] = (float)os[a];
+    }
+    if (out) copyFloats(out, res);
+}
+
+// refine + run in one call, the refined grid kept in the arithmetic type
+void* mdmc_oracle_run_refined(const float* coarse, const int dims[3], const float origin[3], const float spacing[3],
+                              int refinement, int pad, float iso, const mdmc_oracle_options* opt) {
+    const RealInput input(coarse, samplesOf(dims));
+    const oracle::Grid cg = gridOf(input, dims, origin, spacing);
+    std::vector<oracle::Real> res;
     oracle::Grid g;
-    for (int a = 0; a < 3; ++a) { g.d[a] = dims[a]; g.origin[a] = origin[a]; g.deltas[a] = spacing[a]; }
-    g.v = in;
-    std::vector<float> res;
-    oracle::refine(g, refinement, pad != 0, res, out_dims, out_origin, out_spacing);
-    if (out) std::memcpy(out, res.data(), res.size() * sizeof(float));
+    oracle::refine(cg, refinement, pad != 0, res, g.d, g.origin, g.deltas);
+    g.v = res.data();
+    mdmc_oracle_options o;
+    if (opt) o = *opt; else mdmc_oracle_default_options(&o);
+    return oracle::run(g, iso, o);
 }
 
 void* mdmc_oracle_run(const float* grid, const int dims[3], const float origin[3], const float spacing[3],
                       float iso, const mdmc_oracle_options* opt) {
-    oracle::Grid g;
-    for (int a = 0; a < 3; ++a) { g.d[a] = dims[a]; g.origin[a] = origin[a]; g.deltas[a] = spacing[a]; }
-    g.v = grid;
+    const RealInput input(grid, samplesOf(dims));
+    const oracle::Grid g = gridOf(input, dims, origin, spacing);
     mdmc_oracle_options o;
     if (opt) o = *opt; else mdmc_oracle_default_options(&o);
     return oracle::run(g, iso, o);
@@ -1620,8 +1680,8 @@ void mdmc_oracle_stats(const void* res, int64_t stats[MDMC_ORC_NUM_STATS]) {
 void mdmc_oracle_get(const void* res, float* positions, float* normals, int* halfedges, int* face_first,
                      uint16_t* face_attr, uint8_t* vertex_flags, int* vertex_he) {
     const oracle::Result* r = (const oracle::Result*)res;
-    if (positions) std::memcpy(positions, r->pos.data(), r->pos.size() * sizeof(float));
-    if (normals) std::memcpy(normals, r->nrm.data(), r->nrm.size() * sizeof(float));
+    if (positions) copyFloats(positions, r->pos);
+    if (normals) copyFloats(normals, r->nrm);
     if (halfedges) std::memcpy(halfedges, r->he.data(), r->he.size() * sizeof(oracle::HE));
     if (face_first) std::memcpy(face_first, r->faceFirst.data(), r->faceFirst.size() * sizeof(int));
     if (face_attr) std::memcpy(face_attr, r->faceAttr.data(), r->faceAttr.size() * sizeof(uint16_t));
@@ -1631,8 +1691,8 @@ void mdmc_oracle_get(const void* res, float* positions, float* normals, int* hal
 
 void mdmc_oracle_get_dmc(const void* res, float* positions, float* normals, int* quads, uint16_t* quad_attr) {
     const oracle::Result* r = (const oracle::Result*)res;
-    if (positions) std::memcpy(positions, r->dmcPos.data(), r->dmcPos.size() * sizeof(float));
-    if (normals) std::memcpy(normals, r->dmcNrm.data(), r->dmcNrm.size() * sizeof(float));
+    if (positions) copyFloats(positions, r->dmcPos);
+    if (normals) copyFloats(normals, r->dmcNrm);
     if (quads) std::memcpy(quads, r->dmcQuads.data(), r->dmcQuads.size() * sizeof(int));
     if (quad_attr) std::memcpy(quad_attr, r->dmcAttr.data(), r->dmcAttr.size() * sizeof(uint16_t));
 }
@@ -1641,9 +1701,8 @@ void mdmc_oracle_free(void* res) { delete (oracle::Result*)res; }
 
 void* mdmc_oracle_standard_mc(const float* grid, const int dims[3], const float origin[3], const float spacing[3],
                               float iso, int64_t counts[2]) {
-    oracle::Grid g;
-    for (int a = 0; a < 3; ++a) { g.d[a] = dims[a]; g.origin[a] = origin[a]; g.deltas[a] = spacing[a]; }
-    g.v = grid;
+    const RealInput input(grid, samplesOf(dims));
+    const oracle::Grid g = gridOf(input, dims, origin, spacing);
     oracle::MCMesh* m = oracle::standardMC(g, iso);
     counts[0] = (int64_t)(m->pos.size() / 3);
     counts[1] = (int64_t)(m->tris.size() / 3);
@@ -1652,8 +1711,8 @@ void* mdmc_oracle_standard_mc(const float* grid, const int dims[3], const float 
 
 void mdmc_oracle_get_standard_mc(const void* mesh, float* positions, float* normals, int* triangles) {
     const oracle::MCMesh* m = (const oracle::MCMesh*)mesh;
-    if (positions) std::memcpy(positions, m->pos.data(), m->pos.size() * sizeof(float));
-    if (normals) std::memcpy(normals, m->nrm.data(), m->nrm.size() * sizeof(float));
+    if (positions) copyFloats(positions, m->pos);
+    if (normals) copyFloats(normals, m->nrm);
     if (triangles) std::memcpy(triangles, m->tris.data(), m->tris.size() * sizeof(int));
 }
 

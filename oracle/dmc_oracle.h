@@ -79,6 +79,11 @@ void mdmc_oracle_refine(const float* in, const int dims[3], const float origin[3
 
 void* mdmc_oracle_run(const float* grid, const int dims[3], const float origin[3],
                       const float spacing[3], float iso, const mdmc_oracle_options* opt);
+/* mdmc_oracle_refine followed by mdmc_oracle_run, the refined grid kept in
+ * the arithmetic type (float, or double in the FP64 build). */
+void* mdmc_oracle_run_refined(const float* coarse, const int dims[3], const float origin[3],
+                              const float spacing[3], int refinement, int pad, float iso,
+                              const mdmc_oracle_options* opt);
 void mdmc_oracle_counts(const void* result, int64_t counts[MDMC_ORC_NUM_COUNTS]);
 void mdmc_oracle_stats(const void* result, int64_t stats[MDMC_ORC_NUM_STATS]);
 /* Any pointer may be NULL.  halfedges: 4 ints per halfedge (origin, face, next, twin). */

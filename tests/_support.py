@@ -13,10 +13,12 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[1]
 ORACLE_DIR = ROOT / "oracle"
 ORACLE_SO = ORACLE_DIR / "_build" / "libmdmc_oracle.so"
+ORACLE_F64_SO = ORACLE_DIR / "_build" / "libmdmc_oracle_f64.so"
 GOLDEN_DIR = ROOT / "tests" / "golden"
 
 _lock = threading.Lock()
 _lib = None
+_lib64 = None
 
 # SplittingStep, MarchingCubes/VisualDMC/src/DMC/PostProcesses/ManifoldSplitter.h:155-166
 STEP_NONE, STEP_SUBDIVIDE, STEP_COLLAPSE, STEP_MERGE, STEP_TWINS, STEP_MOVE, STEP_ITERATE = range(7)
@@ -37,50 +39,70 @@ class OracleOptions(ctypes.Structure):
 
 
 def build_oracle():
-    """Builds oracle/_build/libmdmc_oracle.so when it is missing or stale."""
+    """Builds oracle/_build/libmdmc_oracle.so (and its FP64 build
+    libmdmc_oracle_f64.so) when missing or stale."""
     srcs = [ORACLE_DIR / n for n in ("dmc_oracle.cpp", "dmc_oracle.h", "mc_contour_table_oracle.h",
-                                     "mc_triangle_table_oracle.h")]
-    if ORACLE_SO.exists() and all(ORACLE_SO.stat().st_mtime >= s.stat().st_mtime for s in srcs):
+                                     "mc_triangle_table_oracle.h", "Makefile")]
+    if all(so.exists() and all(so.stat().st_mtime >= s.stat().st_mtime for s in srcs)
+           for so in (ORACLE_SO, ORACLE_F64_SO)):
         return
-    subprocess.run(["make", "-s", "-C", str(ORACLE_DIR)], check=True)
+    subprocess.run(["make", "-s", "-j2", "-C", str(ORACLE_DIR)], check=True)
 
 
 def oracle():
+    """The float restatement (bit for bit the CUDA path's arithmetic)."""
     global _lib
     with _lock:
         if _lib is None:
             build_oracle()
-            lib = ctypes.CDLL(str(ORACLE_SO))
-            lib.mdmc_oracle_run.restype = ctypes.c_void_p
-            lib.mdmc_oracle_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                                            ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p]
-            for name in ("mdmc_oracle_counts", "mdmc_oracle_stats", "mdmc_oracle_free"):
-                getattr(lib, name).argtypes = [ctypes.c_void_p] + ([ctypes.c_void_p] if name != "mdmc_oracle_free" else [])
-            lib.mdmc_oracle_get.argtypes = [ctypes.c_void_p] * 8
-            lib.mdmc_oracle_get_dmc.argtypes = [ctypes.c_void_p] * 5
-            lib.mdmc_oracle_refine.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                                               ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
-                                               ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
-                                               ctypes.c_void_p]
-            lib.mdmc_oracle_read_bin.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 4
-            lib.mdmc_oracle_get_topology.argtypes = [ctypes.c_void_p] * 4
-            lib.mdmc_oracle_standard_mc.restype = ctypes.c_void_p
-            lib.mdmc_oracle_standard_mc.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_float, ctypes.c_void_p]
-            lib.mdmc_oracle_get_standard_mc.argtypes = [ctypes.c_void_p] * 4
-            lib.mdmc_oracle_free_standard_mc.argtypes = [ctypes.c_void_p]
-            lib.mdmc_oracle_color_faces.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
-                                                    ctypes.c_int64]
-            lib.mdmc_oracle_quads_to_triangles.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
-            lib.mdmc_oracle_mean_ratio.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
-            lib.mdmc_oracle_positions_f64.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_double, ctypes.c_void_p]
-            lib.mdmc_oracle_backward.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_double, ctypes.c_void_p,
-                                                                         ctypes.c_void_p]
-            lib.mdmc_oracle_refine_f64.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
-                                                   ctypes.c_void_p]
-            lib.mdmc_oracle_refine_backward.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
-                                                        ctypes.c_int, ctypes.c_void_p]
-            _lib = lib
+            _lib = _bind(ctypes.CDLL(str(ORACLE_SO)))
     return _lib
+
+
+def oracle_f64():
+    """The same restatement computing in double (the timed FP64 CPU baseline)."""
+    global _lib64
+    with _lock:
+        if _lib64 is None:
+            build_oracle()
+            _lib64 = _bind(ctypes.CDLL(str(ORACLE_F64_SO)))
+    return _lib64
+
+
+def _bind(lib):
+    """Declares the argument and result types of the oracle library's C API."""
+    lib.mdmc_oracle_run.restype = ctypes.c_void_p
+    lib.mdmc_oracle_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_float, ctypes.c_void_p]
+    for name in ("mdmc_oracle_counts", "mdmc_oracle_stats", "mdmc_oracle_free"):
+        getattr(lib, name).argtypes = [ctypes.c_void_p] + ([ctypes.c_void_p] if name != "mdmc_oracle_free" else [])
+    lib.mdmc_oracle_get.argtypes = [ctypes.c_void_p] * 8
+    lib.mdmc_oracle_get_dmc.argtypes = [ctypes.c_void_p] * 5
+    lib.mdmc_oracle_refine.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p]
+    lib.mdmc_oracle_read_bin.argtypes = [ctypes.c_char_p] + [ctypes.c_void_p] * 4
+    lib.mdmc_oracle_get_topology.argtypes = [ctypes.c_void_p] * 4
+    lib.mdmc_oracle_standard_mc.restype = ctypes.c_void_p
+    lib.mdmc_oracle_standard_mc.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_float, ctypes.c_void_p]
+    lib.mdmc_oracle_get_standard_mc.argtypes = [ctypes.c_void_p] * 4
+    lib.mdmc_oracle_free_standard_mc.argtypes = [ctypes.c_void_p]
+    lib.mdmc_oracle_color_faces.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_int64]
+    lib.mdmc_oracle_quads_to_triangles.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+    lib.mdmc_oracle_mean_ratio.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
+    lib.mdmc_oracle_positions_f64.argtypes = [ctypes.c_void_p] * 5 + [ctypes.c_double, ctypes.c_void_p]
+    lib.mdmc_oracle_backward.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_double, ctypes.c_void_p,
+                                                                 ctypes.c_void_p]
+    lib.mdmc_oracle_refine_f64.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_void_p]
+    lib.mdmc_oracle_refine_backward.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                                ctypes.c_int, ctypes.c_void_p]
+    lib.mdmc_oracle_run_refined.restype = ctypes.c_void_p
+    lib.mdmc_oracle_run_refined.argtypes = [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                                                    ctypes.c_void_p]
+    return lib
 
 
 def _p(a):
@@ -129,6 +151,23 @@ def oracle_run(grid, dims, origin, spacing, iso, **opts):
     res = lib.mdmc_oracle_run(_p(grid), _p(np.asarray(dims, np.int32)),
                               _p(np.asarray(origin, np.float32)), _p(np.asarray(spacing, np.float32)),
                               ctypes.c_float(iso), ctypes.byref(o))
+    return _collect(lib, res)
+
+
+def oracle_run_refined(coarse, dims, origin, spacing, refinement, pad, iso, f64=False, **opts):
+    """Refinement and run in one oracle call (the refined grid stays in the
+    oracle's arithmetic type: float, or double with f64)."""
+    lib = oracle_f64() if f64 else oracle()
+    coarse = np.ascontiguousarray(coarse, np.float32).reshape(-1)
+    assert coarse.size == int(np.prod(dims))
+    o = default_options(**opts)
+    res = lib.mdmc_oracle_run_refined(_p(coarse), _p(np.asarray(dims, np.int32)), _p(np.asarray(origin, np.float32)),
+                                      _p(np.asarray(spacing, np.float32)), int(refinement), int(pad),
+                                      ctypes.c_float(iso), ctypes.byref(o))
+    return _collect(lib, res)
+
+
+def _collect(lib, res):
     try:
         counts = np.zeros(5, np.int64)
         stats = np.zeros(10, np.int64)
