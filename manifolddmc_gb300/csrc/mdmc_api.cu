@@ -101,6 +101,12 @@ struct mdmc_context {
     DevBuf caseBytes;  // the mask pass's per-cell cases for the emit pass
     int caseMode = 0;  // CaseBytes::mode of the last mask pass
     bool faceNMValid = false;  // faceNM holds the current mesh's per-face counts (else heValence)
+    // per-vertex member counts (vcount) and rows that a full refresh left for
+    // the current mesh; the splitter's local refresh needs both
+    DevBuf vcount;
+    bool rowsValid = false;
+    // local refresh: records of the old and new edge sets and their tables
+    DevBuf censusFill, censusOld, censusNew, censusTabOld, censusTabNew;
     // quad -> owner cell; per-row active-cell mask (32 cells per word) and the
     // index of each word's first active cell; per active cell {contours, quads}
     DevBuf quadOwner, cellMask, cellFirst, cellCounts, cellIds;
@@ -207,6 +213,8 @@ std::string statusText(uint32_t s) {
     add(kStatusMissingCell, "quad neighbour cell missing");
     add(kStatusMappingSwap, "unexpected working-copy mapping");
     add(kStatusCountMismatch, "emit pass disagreed with the count pass");
+    add(kStatusBadIndex, "element id out of range");
+    add(kStatusCountOverflow, "vertex edge-count field overflow");
     return t;
 }
 
@@ -350,7 +358,7 @@ mdmc_status ensureMaps(mdmc_context* c, cudaStream_t s) {
 // Edge buckets of the current mesh from per-vertex adjacency rows: valences,
 // vertex and face flags, edge counters, the 4-face edge list, and (connect)
 // the twins of connectHalfedgeTwins (D/Halfedges/HalfedgeMesh.cu:92-291)
-mdmc_status edgeBuckets(mdmc_context* c, int connect, cudaStream_t s) {
+mdmc_status edgeBuckets(mdmc_context* c, int connect, cudaStream_t s, bool trackCounts = false) {
     DevCounters* ctr = c->counters.as<DevCounters>();
     const MeshDims md{(int)c->V, (int)c->F, (int)c->H};
     MDMC_CHECK(c, c->nmList.ensure(sizeof(int4) * (size_t)(c->H / 4 + 1)));
@@ -365,10 +373,15 @@ mdmc_status edgeBuckets(mdmc_context* c, int connect, cudaStream_t s) {
     MDMC_CHECK(c, cudaMemsetAsync(c->vflags.p, 0, roundUp((size_t)std::max<int64_t>(c->V, 1), 4), s));
     MDMC_CHECK(c, cudaMemsetAsync(c->faceNM.p, 0, roundUp((size_t)std::max<int64_t>(c->F, 1), 4), s));
     MDMC_CHECK(c, cudaMemsetAsync((char*)c->counters.p + 8, 0, sizeof(DevCounters) - 8, s));
+    if (trackCounts) {
+        MDMC_CHECK(c, c->vcount.ensure(sizeof(uint32_t) * (size_t)std::max<int64_t>(c->V, 1)));
+        MDMC_CHECK(c, cudaMemsetAsync(c->vcount.p, 0, sizeof(uint32_t) * (size_t)c->V, s));
+    }
     launchEdgeBuckets(c->he.as<int4>(), md, c->adjRow.as<int>(), c->adjRank.as<int>(), c->adj.as<int2>(), connect,
                       c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), c->faceNM.as<uint8_t>(),
-                      c->nmList.as<int4>(), ctr, s);
+                      trackCounts ? c->vcount.as<uint32_t>() : nullptr, c->nmList.as<int4>(), ctr, s);
     c->faceNMValid = true;
+    c->rowsValid = trackCounts;
     return MDMC_OK;
 }
 
@@ -377,7 +390,7 @@ mdmc_status edgeBuckets(mdmc_context* c, int connect, cudaStream_t s) {
 mdmc_status refreshTable(mdmc_context* c, uint32_t* status, cudaStream_t s) {
     (void)status;
     launchResetFaceFlags(c->faceAttr.as<uint16_t>(), (int)c->F, s);
-    return edgeBuckets(c, 0, s);
+    return edgeBuckets(c, 0, s, true);
 }
 
 // Non-manifold vertex detection (detectNonManifoldVertices,
@@ -493,6 +506,91 @@ mdmc_status runSimplification(mdmc_context* c, int kind, cudaStream_t s) {
     return MDMC_OK;
 }
 
+// The splitter's local refresh (kCensus* in csrc/mdmc_split.cu): record
+// buffers and tables sized from the old edge set (nOld records) and the
+// kept one (at most capNew); the old records are taken before the copy-back
+// overwrites the old halfedges.
+struct Census {
+    int capOld = 0, capNew = 0;
+    CensusTable tOld{}, tNew{};
+};
+
+static int censusTableSize(int records) {
+    int p = 1024;
+    while (p < 2 * records) p *= 2;
+    return p;
+}
+
+static CensusTable censusTable(DevBuf& b, int capacity) {
+    CensusTable t;
+    char* p = (char*)b.p;
+    t.capacity = capacity;
+    t.keys = (unsigned long long*)p;
+    t.count = (int*)(p + 8 * (size_t)capacity);
+    t.claim = (int*)(p + 12 * (size_t)capacity);
+    t.members = (int*)(p + 16 * (size_t)capacity);
+    return t;
+}
+
+mdmc_status censusBegin(mdmc_context* c, const SplitWork& w, int n, int nOld, int capNew, Census& k, cudaStream_t s) {
+    if (nOld > 0x3FFFFFFF || capNew > 0x3FFFFFFF) return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "local refresh too large");
+    k.capOld = nOld;
+    k.capNew = capNew;
+    const int pOld = censusTableSize(nOld), pNew = censusTableSize(capNew);
+    MDMC_CHECK(c, c->censusOld.ensure(sizeof(CensusRec) * (size_t)std::max(nOld, 1)));
+    MDMC_CHECK(c, c->censusNew.ensure(sizeof(CensusRec) * (size_t)std::max(capNew, 1)));
+    MDMC_CHECK(c, c->censusTabOld.ensure(32 * (size_t)pOld));
+    MDMC_CHECK(c, c->censusTabNew.ensure(32 * (size_t)pNew));
+    k.tOld = censusTable(c->censusTabOld, pOld);
+    k.tNew = censusTable(c->censusTabNew, pNew);
+    for (const CensusTable* t : {&k.tOld, &k.tNew}) {
+        MDMC_CHECK(c, cudaMemsetAsync(t->keys, 0xFF, 8 * (size_t)t->capacity, s));
+        MDMC_CHECK(c, cudaMemsetAsync(t->count, 0, 8 * (size_t)t->capacity, s));  // count and claim
+    }
+    MDMC_CHECK(c, cudaMemsetAsync(c->censusFill.p, 0, sizeof(int) * 4, s));
+    launchCensusCollectOld(w, n, c->adjRow.as<int>(), c->adj.as<int2>(), c->he.as<int4>(), c->censusOld.as<CensusRec>(),
+                           c->censusNew.as<CensusRec>(), c->censusFill.as<int>(), k.capOld, k.capNew,
+                           &c->counters.as<DevCounters>()->status, s);
+    return MDMC_OK;
+}
+
+// after the copy-back (c->V/H/F already the new sizes; V1, F1 the old ones):
+// the kept halfedges' records, the old edge sets counted out and the new ones
+// in, then the flags of every vertex and face the records name
+mdmc_status censusFinish(mdmc_context* c, const SplitWork& w, const Census& k, int64_t V1, int64_t F1, cudaStream_t s) {
+    DevCounters* ctr = c->counters.as<DevCounters>();
+    const MeshDims md{(int)c->V, (int)c->F, (int)c->H};
+    // the appended vertices and faces start from zero counts and flags
+    MDMC_CHECK(c, c->vcount.grow(sizeof(uint32_t) * (size_t)c->V, sizeof(uint32_t) * (size_t)V1, s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->vcount.as<uint32_t>() + V1, 0, sizeof(uint32_t) * (size_t)(c->V - V1), s));
+    MDMC_CHECK(c, c->faceNM.grow(roundUp((size_t)c->F, 4), (size_t)F1, s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->faceNM.as<uint8_t>() + F1, 0, roundUp((size_t)c->F, 4) - (size_t)F1, s));
+    MDMC_CHECK(c, cudaMemsetAsync(c->vflags.as<uint8_t>() + V1, 0, roundUp((size_t)c->V, 4) - (size_t)V1, s));
+    MDMC_CHECK(c, c->nmList.grow(sizeof(int4) * (size_t)(c->H / 4 + 1), 0, s));
+    // the refresh's other counters start from zero, as after a full refresh
+    MDMC_CHECK(c, cudaMemsetAsync(&ctr->nmVertices, 0, sizeof(DevCounters) - offsetof(DevCounters, nmVertices), s));
+    launchCensusCollectNew(w, c->he.as<int4>(), md, c->censusNew.as<CensusRec>(), c->censusFill.as<int>(), k.capNew,
+                           &ctr->status, s);
+    const int* fill = c->censusFill.as<int>();
+    launchCensusApply(c->censusOld.as<CensusRec>(), fill, k.capOld, k.tOld, -1, c->vcount.as<uint32_t>(),
+                      c->faceNM.as<uint8_t>(), c->nmList.as<int4>(), (int)(c->H / 4 + 1), ctr, s);
+    launchCensusApply(c->censusNew.as<CensusRec>(), fill + 1, k.capNew, k.tNew, 1, c->vcount.as<uint32_t>(),
+                      c->faceNM.as<uint8_t>(), c->nmList.as<int4>(), (int)(c->H / 4 + 1), ctr, s);
+    launchCensusFinish(c->censusOld.as<CensusRec>(), fill, k.capOld, c->vcount.as<uint32_t>(), c->faceNM.as<uint8_t>(),
+                       c->vflags.as<uint8_t>(), c->faceAttr.as<uint16_t>(), s);
+    launchCensusFinish(c->censusNew.as<CensusRec>(), fill + 1, k.capNew, c->vcount.as<uint32_t>(),
+                       c->faceNM.as<uint8_t>(), c->vflags.as<uint8_t>(), c->faceAttr.as<uint16_t>(), s);
+    // the new record count must fit what was reserved
+    MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, c->censusFill.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    MDMC_CHECK(c, cudaStreamSynchronize(s));
+    if (c->hostInts[0] != k.capOld || c->hostInts[1] < 0 || c->hostInts[1] > k.capNew)
+        return fail(c, MDMC_ERROR_CUDA, "local refresh record counts disagree with their sizes");
+    MDMC_CHECK(c, cudaGetLastError());
+    c->faceNMValid = true;
+    c->rowsValid = false;
+    return MDMC_OK;
+}
+
 // ManifoldSplitter::run, D/PostProcesses/ManifoldSplitter.cu:96-208
 mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& iterations, cudaStream_t s) {
     DevCounters* ctr = c->counters.as<DevCounters>();
@@ -575,6 +673,16 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         if ((st = scan<int>(c, c->appV.as<int>(), c->appV.as<int>(), nv, s)) != MDMC_OK) return st;
         if ((st = scan<int>(c, c->appH.as<int>(), c->appH.as<int>(), nh, s)) != MDMC_OK) return st;
         if ((st = scan<int>(c, c->appF.as<int>(), c->appF.as<int>(), nf, s)) != MDMC_OK) return st;
+        // a small iteration after a full refresh gets the local refresh: the
+        // sizes of its old and kept edge sets come back with the append counts
+        const bool local = c->rowsValid && doSub && (int64_t)nh * 16 <= c->H;
+        if (local) {
+            MDMC_CHECK(c, c->censusFill.ensure(sizeof(int) * 4));
+            MDMC_CHECK(c, cudaMemsetAsync(c->censusFill.p, 0, sizeof(int) * 4, s));
+            launchCensusCountOld(w, n, c->adjRow.as<int>(), c->adj.as<int2>(), c->he.as<int4>(), c->censusFill.as<int>(),
+                                 s);
+            MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts + 3, c->censusFill.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+        }
         MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts, c->appV.as<int>() + nv, sizeof(int), cudaMemcpyDeviceToHost, s));
         MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts + 1, c->appH.as<int>() + nh, sizeof(int), cudaMemcpyDeviceToHost, s));
         MDMC_CHECK(c, cudaMemcpyAsync(c->hostInts + 2, c->appF.as<int>() + nf, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -584,6 +692,13 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         if (addV < 0 || addV > nv || addH < 0 || addH > nh || addF < 0 || addF > nf)
             return fail(c, MDMC_ERROR_CUDA, "inconsistent working-copy append counts");
         const int64_t V2 = c->V + addV, H2 = c->H + addH, F2 = c->F + addF;
+        Census census;
+        if (local) {
+            const int64_t nOld = c->hostInts[3], nSame = c->hostInts[4];
+            if (nOld < 0 || nSame < 0 || nSame > nOld || nOld > c->H)
+                return fail(c, MDMC_ERROR_CUDA, "inconsistent local-refresh sizes");
+            if ((st = censusBegin(c, w, n, (int)nOld, (int)(nSame + nh), census, s)) != MDMC_OK) return st;
+        }
         MDMC_CHECK(c, c->pos.grow(sizeof(float) * 3 * (size_t)V2, sizeof(float) * 3 * (size_t)c->V, s));
         MDMC_CHECK(c, c->nrm.grow(sizeof(float) * 3 * (size_t)V2, sizeof(float) * 3 * (size_t)c->V, s));
         MDMC_CHECK(c, c->vflags.grow(roundUp((size_t)V2, 4), (size_t)c->V, s));
@@ -598,10 +713,13 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
                             c->pos.as<float>(), c->nrm.as<float>(), c->he.as<int4>(), c->faceFirst.as<int>(),
                             c->faceAttr.as<uint16_t>(), status, s);
         launchSplitResetMaps(n, c->nmFaces.as<int>(), w, s);
+        const int64_t V1 = c->V, F1 = c->F;
         c->V = V2;
         c->H = H2;
         c->F = F2;
-        if ((st = refreshTable(c, status, s)) != MDMC_OK) return st;
+        if (local) st = censusFinish(c, wb, census, V1, F1, s);
+        else st = refreshTable(c, status, s);
+        if (st != MDMC_OK) return st;
         MDMC_CHECK(c, cudaGetLastError());
         ++iterations;
         if (step < MDMC_STEP_ENABLE_ITERATIVE_REFINEMENT) break;
@@ -940,6 +1058,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->dmcV = c->activeCells = 0;
     c->simplified = false;
     c->earlyFaces = c->earlyVertices = c->earlyVertexMaps = c->lateChange = false;
+    c->rowsValid = false;
     std::memset(&c->stats, 0, sizeof c->stats);
     DevCounters* ctr = c->counters.as<DevCounters>();
     uint32_t* status = &ctr->status;

@@ -206,9 +206,15 @@ void launchVertexHalfedgeFix(int* vertexHE, int numVertices, cudaStream_t s);
 // edge buckets: rows of halfedges keyed by their smaller end vertex
 // (deg: per vertex, the halfedges whose smaller end it is)
 void launchEdgeRowDegree(const int4* he, MeshDims md, int* deg, int* rank, uint32_t* status, cudaStream_t s);
+// faceNM (one byte per face): the face's edges with more than two halfedges
+// (low nibble) and with exactly four (high nibble).  vcount (optional, one
+// word per vertex): how many of the vertex's outgoing halfedges lie on edges
+// of one (bits 0-9), three (10-19) and four (20-29) halfedges.
+constexpr uint32_t kFaceNMCount = 0x0Fu;
+constexpr int kVCountShiftBoundary = 0, kVCountShiftWeird = 10, kVCountShiftNM = 20;
 void launchEdgeBuckets(int4* he, MeshDims md, const int* rowStart, const int* rank, int2* adj, int connectTwins,
-                       uint16_t* faceAttr, uint8_t* vflags, uint8_t* faceNM, int4* nmList, DevCounters* ctr,
-                       cudaStream_t s);
+                       uint16_t* faceAttr, uint8_t* vflags, uint8_t* faceNM, uint32_t* vcount, int4* nmList,
+                       DevCounters* ctr, cudaStream_t s);
 void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s);
 void launchReconnect(const GridDesc& g, float iso, const int4* nmList, const DevCounters* ctr,
                      int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s);
@@ -267,5 +273,40 @@ void launchSplitCopyBack(const SplitWork& w, const int* appV, const int* appH, c
                          float* pos, float* nrm, int4* he, int* faceFirst, uint16_t* faceAttr, uint32_t* status,
                          cudaStream_t s);
 void launchSplitResetMaps(int n, const int* nmFaces, const SplitWork& w, cudaStream_t s);
+
+// Local refresh after a splitter iteration (see mdmc_split.cu).  One record
+// per halfedge of an edge whose two ends are in the iteration's vertex set.
+struct CensusRec {
+    int lo, hi;      // the edge's end vertices, lo < hi
+    int h;           // halfedge id
+    int origin;      // its origin vertex
+    int face;        // its face
+    int slot;        // its edge's slot in the census table
+};
+struct CensusTable {
+    unsigned long long* keys;  // lo << 32 | hi, ~0 = empty
+    int* count;                // halfedges of the edge
+    int* claim;                // set by the record that settles the edge
+    int* members;              // the edge's first four halfedge ids
+    int capacity;              // a power of two
+};
+// over the iteration's distinct corners: out[0] += halfedges of the old
+// mesh between two vertices of the set, out[1] += those the copy-back keeps
+void launchCensusCountOld(const SplitWork& w, int n, const int* rowStart, const int2* adj, const int4* he, int* out,
+                          cudaStream_t s);
+// their records, into oldRecs and (the kept ones) newRecs; fill[0], fill[1]
+// count them (records past a capacity are dropped, the count still grows)
+void launchCensusCollectOld(const SplitWork& w, int n, const int* rowStart, const int2* adj, const int4* he,
+                            CensusRec* oldRecs, CensusRec* newRecs, int* fill, int capOld, int capNew, uint32_t* status,
+                            cudaStream_t s);
+// the written-back halfedges' records (after the copy-back), counted by fill[1]
+void launchCensusCollectNew(const SplitWork& w, const int4* he, MeshDims md, CensusRec* newRecs, int* fill, int capNew,
+                            uint32_t* status, cudaStream_t s);
+// counts out (sign -1) or in (+1) the edges of the first min(*fill, cap) records
+void launchCensusApply(CensusRec* recs, const int* fill, int cap, const CensusTable& t, int sign, uint32_t* vcount,
+                       uint8_t* faceNM, int4* nmList, int nmCapacity, DevCounters* ctr, cudaStream_t s);
+// vertex flags and face flags of the records' vertices and faces from their counts
+void launchCensusFinish(const CensusRec* recs, const int* fill, int cap, const uint32_t* vcount, const uint8_t* faceNM,
+                        uint8_t* vflags, uint16_t* faceAttr, cudaStream_t s);
 
 }  // namespace mdmc

@@ -103,16 +103,18 @@ constexpr int kBucketStage = 512;  // row entries of 32 vertices staged per warp
 // counts the bucket.  Only an entry of a bucket of other than two halfedges
 // (or, with connectTwins, any entry) goes on: it collects the bucket's four
 // smallest ids and acts for its own halfedge: the vertex flag of its origin
-// (non-manifold / weird / boundary by the bucket's size), the non-manifold
-// face flag and the per-face count of edges with more than two halfedges
-// (faceNM, zeroed by the caller), its twin by the rules of
+// (non-manifold / weird / boundary by the bucket's size; with vcount, also
+// counted per vertex), the non-manifold face flag and the per-face counts of
+// edges with more than two and with four halfedges (faceNM, zeroed by the
+// caller), its twin by the rules of
 // connectHalfedgeTwins (with connectTwins), and the first entry of a 4-face
 // bucket lists it.  The counters take one addition per block.
 __global__ void __launch_bounds__(32 * kBucketWarps) kEdgeBuckets(int4* __restrict__ he, MeshDims md,
                                                                   const int* __restrict__ rowStart,
                                                                   const int2* __restrict__ adj, int connectTwins,
                                                                   uint16_t* faceAttr, uint8_t* vflags, uint8_t* faceNM,
-                                                                  int4* __restrict__ nmList, DevCounters* ctr) {
+                                                                  uint32_t* vcount, int4* __restrict__ nmList,
+                                                                  DevCounters* ctr) {
     __shared__ int2 stage[kBucketWarps][kBucketStage];
     __shared__ int stageEnd[kBucketWarps][kBucketStage];
     __shared__ uint8_t stageRow[kBucketWarps][kBucketStage];
@@ -217,10 +219,15 @@ __global__ void __launch_bounds__(32 * kBucketWarps) kEdgeBuckets(int4* __restri
             if (cnt == 4) orVertexFlag(vflags, origin, MDMC_VERTEX_NON_MANIFOLD);
             else if (cnt == 3) orVertexFlag(vflags, origin, MDMC_VERTEX_WEIRD);
             else if (cnt == 1) orVertexFlag(vflags, origin, MDMC_VERTEX_BOUNDARY);
+            if (vcount && cnt <= 4) {
+                const int sh = cnt == 1 ? kVCountShiftBoundary : (cnt == 3 ? kVCountShiftWeird : kVCountShiftNM);
+                const uint32_t old = atomicAdd(vcount + origin, 1u << sh);
+                if (((old >> sh) & 0x3FFu) >= 1000u) atomicOr(&ctr->status, kStatusCountOverflow);
+            }
             if (cnt > 2) {
                 const int f = he[h].y;
                 if (inb(f, md.F)) {
-                    atomicAdd(reinterpret_cast<uint32_t*>(faceNM) + (f >> 2), 1u << ((f & 3) * 8));
+                    atomicAdd(reinterpret_cast<uint32_t*>(faceNM) + (f >> 2), (cnt == 4 ? 0x11u : 0x01u) << ((f & 3) * 8));
                     if (cnt == 4) orFaceAttr(faceAttr, f, MDMC_FACE_NON_MANIFOLD);
                 } else {
                     atomicOr(&ctr->status, kStatusBadIndex);
@@ -255,15 +262,15 @@ void launchEdgeRowDegree(const int4* he, MeshDims md, int* deg, int* rank, uint3
 }
 
 void launchEdgeBuckets(int4* he, MeshDims md, const int* rowStart, const int* rank, int2* adj, int connectTwins,
-                       uint16_t* faceAttr, uint8_t* vflags, uint8_t* faceNM, int4* nmList, DevCounters* ctr,
-                       cudaStream_t s) {
+                       uint16_t* faceAttr, uint8_t* vflags, uint8_t* faceNM, uint32_t* vcount, int4* nmList,
+                       DevCounters* ctr, cudaStream_t s) {
     if (md.H <= 0) return;
     countLaunch(2);
     kEdgeRowScatter<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, rowStart, rank, adj);
     const int64_t tiles = ((int64_t)md.V + 31) / 32;
     const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((tiles + kBucketWarps - 1) / kBucketWarps, 152 * 8));
     kEdgeBuckets<<<blocks, 32 * kBucketWarps, 0, s>>>(he, md, rowStart, adj, connectTwins, faceAttr, vflags, faceNM,
-                                                      nmList, ctr);
+                                                      vcount, nmList, ctr);
 }
 
 // ---------------------------------------------------------------------------
@@ -672,7 +679,7 @@ __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__
         quads[f] = make_int4(q[0], q[1], q[2], q[3]);
         if (ok) {
             cnt = 0;
-            if (faceNM) cnt = faceNM[f];
+            if (faceNM) cnt = faceNM[f] & kFaceNMCount;
             else
                 for (int i = 0; i < 4; ++i)
                     if (heValence[hs[i]] > 2) ++cnt;

@@ -508,6 +508,191 @@ __global__ void kResetMaps(int n, const int* __restrict__ nmFaces, SplitWork w) 
 }
 
 // ---------------------------------------------------------------------------
+// Local refresh (refreshHashTable, D/Halfedges/HalfedgeMesh.cu:1063-1100,
+// restricted to what an iteration can change).  Let D be the corners of the
+// iteration's non-manifold faces plus the vertices it appends.  Every
+// halfedge the copy-back writes runs between two vertices of D, and every
+// other halfedge keeps its ends, its next and its face.  So only edges with
+// both ends in D change their halfedge sets: their old sets (from the rows
+// of the last full refresh, before the copy-back) are counted out and their
+// new sets counted in.  Vertex flags follow from per-vertex member counts,
+// face flags from per-face edge counts, and the edge counters from the
+// per-edge differences; the result equals a full refresh of the new mesh.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool inD(const SplitWork& w, int v) { return inb(v, w.V) && w.vO2C[v] != 0x7FFFFFFF; }
+
+// the corner copy that stands for original vertex d (its smallest copy), or -1
+__device__ __forceinline__ int distinctCorner(const SplitWork& w, int c) {
+    const int d = w.origV[c];
+    return (inb(d, w.V) && w.vO2C[d] == c) ? d : -1;
+}
+
+__global__ void kCensusCountOld(SplitWork w, int n, const int* __restrict__ rowStart, const int2* __restrict__ adj,
+                                const int4* __restrict__ he, int* out) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    int nOld = 0, nSame = 0;
+    if (c < 4 * n) {
+        const int d = distinctCorner(w, c);
+        if (d >= 0)
+            for (int k = rowStart[d]; k < rowStart[d + 1]; ++k) {
+                const int2 r = adj[k];
+                if (!inD(w, r.x >= 0 ? r.x : ~r.x) || !inb(r.y, w.H) || !inb(he[r.y].y, w.F)) continue;
+                ++nOld;
+                if (w.hO2C[r.y] == kNone) ++nSame;
+            }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        nOld += __shfl_down_sync(0xffffffffu, nOld, o);
+        nSame += __shfl_down_sync(0xffffffffu, nSame, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (nOld) atomicAdd(out, nOld);
+        if (nSame) atomicAdd(out + 1, nSame);
+    }
+}
+
+__global__ void kCensusCollectOld(SplitWork w, int n, const int* __restrict__ rowStart, const int2* __restrict__ adj,
+                                  const int4* __restrict__ he, CensusRec* oldRecs, CensusRec* newRecs, int* fill,
+                                  int2 caps, uint32_t* status) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= 4 * n) return;
+    const int d = distinctCorner(w, c);
+    if (d < 0) return;
+    for (int k = rowStart[d]; k < rowStart[d + 1]; ++k) {
+        const int2 r = adj[k];
+        const int o = r.x >= 0 ? r.x : ~r.x;
+        if (!inD(w, o)) continue;
+        const int f = inb(r.y, w.H) ? he[r.y].y : -1;
+        if (!inb(f, w.F)) {
+            atomicOr(status, kStatusBadIndex);
+            continue;
+        }
+        CensusRec rec;
+        rec.lo = d;
+        rec.hi = o;
+        rec.h = r.y;
+        rec.origin = r.x >= 0 ? d : o;
+        rec.face = f;
+        rec.slot = -1;
+        const int a = atomicAdd(fill, 1);
+        if (a < caps.x) oldRecs[a] = rec;
+        if (w.hO2C[r.y] == kNone) {
+            const int b = atomicAdd(fill + 1, 1);
+            if (b < caps.y) newRecs[b] = rec;
+        }
+    }
+}
+
+__global__ void kCensusCollectNew(SplitWork w, const int4* __restrict__ he, MeshDims md, CensusRec* newRecs, int* fill,
+                                  int cap, uint32_t* status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= w.nh || (w.hfl[t] & kRemove)) return;
+    const int self = w.hC2O[t];
+    if (!inb(self, md.H)) {
+        atomicOr(status, kStatusBadIndex);
+        return;
+    }
+    const int4 e = he[self];
+    if (!inb(e.z, md.H) || !inb(e.x, md.V) || !inb(e.y, md.F)) {
+        atomicOr(status, kStatusBadIndex);
+        return;
+    }
+    const int b = he[e.z].x;
+    if (!inb(b, md.V)) {
+        atomicOr(status, kStatusBadIndex);
+        return;
+    }
+    CensusRec rec;
+    rec.lo = min(e.x, b);
+    rec.hi = max(e.x, b);
+    rec.h = self;
+    rec.origin = e.x;
+    rec.face = e.y;
+    rec.slot = -1;
+    const int at = atomicAdd(fill + 1, 1);
+    if (at < cap) newRecs[at] = rec;
+}
+
+// each record finds (or opens) its edge's slot and counts itself in
+__global__ void kCensusInsert(CensusRec* recs, const int* fill, int cap, CensusTable t, uint32_t* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= min(*fill, cap)) return;
+    CensusRec& r = recs[i];
+    const unsigned long long key = ((unsigned long long)(uint32_t)r.lo << 32) | (uint32_t)r.hi;
+    const uint32_t mask = (uint32_t)t.capacity - 1u;
+    uint32_t slot = (uint32_t)((key * 0x9E3779B97F4A7C15ull) >> 32) & mask;
+    for (int probe = 0; probe < t.capacity; ++probe) {
+        const unsigned long long k = atomicCAS(t.keys + slot, ~0ull, key);
+        if (k == ~0ull || k == key) {
+            const int idx = atomicAdd(t.count + slot, 1);
+            if (idx < 4) t.members[4 * (int64_t)slot + idx] = r.h;
+            r.slot = (int)slot;
+            return;
+        }
+        slot = (slot + 1u) & mask;
+    }
+    atomicOr(status, kStatusBadIndex);  // table full (sized to twice the records: not reached)
+}
+
+// each record counts itself out (sign < 0) or in (sign > 0); the edge's
+// first record to claim it settles the edge-level counters
+__global__ void kCensusApply(const CensusRec* __restrict__ recs, const int* fill, int cap, CensusTable t, int sign,
+                             uint32_t* vcount, uint8_t* faceNM, int4* nmList, int nmCapacity, DevCounters* ctr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= min(*fill, cap)) return;
+    const CensusRec r = recs[i];
+    if (r.slot < 0) return;
+    const int cnt = t.count[r.slot];
+    const unsigned long long one = sign > 0 ? 1ull : ~0ull;
+    if (atomicExch(t.claim + r.slot, 1) == 0) {
+        atomicAdd(&ctr->edges, one);
+        if (cnt == 3) atomicAdd(&ctr->edges3, one);
+        if (cnt == 4) atomicAdd(&ctr->edges4, one);
+        if (sign > 0 && cnt > 4) atomicOr(&ctr->status, kStatusBucketOverflow);
+        if (sign > 0 && cnt == 4) {  // the new mesh's 4-face edges, ascending ids
+            int m[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) m[k] = t.members[4 * (int64_t)r.slot + k];
+#define MDMC_CX(a, b)          \
+    if (m[b] < m[a]) {          \
+        const int x = m[a];     \
+        m[a] = m[b];            \
+        m[b] = x;               \
+    }
+            MDMC_CX(0, 1) MDMC_CX(2, 3) MDMC_CX(0, 2) MDMC_CX(1, 3) MDMC_CX(1, 2)
+#undef MDMC_CX
+            const unsigned long long at = atomicAdd(&ctr->nmBuckets, 1ull);
+            if (at < (unsigned long long)nmCapacity) nmList[at] = make_int4(m[0], m[1], m[2], m[3]);
+            else atomicOr(&ctr->status, kStatusBadIndex);
+        }
+    }
+    if (cnt != 2 && cnt <= 4) {
+        const int sh = cnt == 1 ? kVCountShiftBoundary : (cnt == 3 ? kVCountShiftWeird : kVCountShiftNM);
+        const uint32_t old = atomicAdd(vcount + r.origin, sign > 0 ? (1u << sh) : (0u - (1u << sh)));
+        if (sign > 0 && ((old >> sh) & 0x3FFu) >= 1000u) atomicOr(&ctr->status, kStatusCountOverflow);
+    }
+    if (cnt > 2) {
+        const uint32_t add = (cnt == 4 ? 0x11u : 0x01u) << ((r.face & 3) * 8);
+        atomicAdd(reinterpret_cast<uint32_t*>(faceNM) + (r.face >> 2), sign > 0 ? add : 0u - add);
+    }
+}
+
+// flags of every vertex and face a record names, from the final counts
+__global__ void kCensusFinish(const CensusRec* __restrict__ recs, const int* fill, int cap,
+                              const uint32_t* __restrict__ vcount, const uint8_t* __restrict__ faceNM, uint8_t* vflags,
+                              uint16_t* faceAttr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= min(*fill, cap)) return;
+    const CensusRec r = recs[i];
+    const uint32_t vc = vcount[r.origin];
+    vflags[r.origin] = (uint8_t)((((vc >> kVCountShiftBoundary) & 0x3FFu) ? MDMC_VERTEX_BOUNDARY : 0u) |
+                                 (((vc >> kVCountShiftWeird) & 0x3FFu) ? MDMC_VERTEX_WEIRD : 0u) |
+                                 (((vc >> kVCountShiftNM) & 0x3FFu) ? MDMC_VERTEX_NON_MANIFOLD : 0u));
+    faceAttr[r.face] = (uint16_t)((faceAttr[r.face] & 0x1Fu) | ((faceNM[r.face] >> 4) ? MDMC_FACE_NON_MANIFOLD : 0u));
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 // blocks of `bs` threads covering n elements
@@ -565,6 +750,40 @@ void launchSplitCopyBack(const SplitWork& w, const int* appV, const int* appH, c
 void launchSplitResetMaps(int n, const int* nmFaces, const SplitWork& w, cudaStream_t s) {
     countLaunch();
     kResetMaps<<<nb(4 * (int64_t)n, 256), 256, 0, s>>>(n, nmFaces, w);
+}
+
+void launchCensusCountOld(const SplitWork& w, int n, const int* rowStart, const int2* adj, const int4* he, int* out,
+                          cudaStream_t s) {
+    if (n <= 0) return;
+    countLaunch();
+    kCensusCountOld<<<nb(4 * (int64_t)n, 256), 256, 0, s>>>(w, n, rowStart, adj, he, out);
+}
+void launchCensusCollectOld(const SplitWork& w, int n, const int* rowStart, const int2* adj, const int4* he,
+                            CensusRec* oldRecs, CensusRec* newRecs, int* fill, int capOld, int capNew, uint32_t* status,
+                            cudaStream_t s) {
+    if (n <= 0) return;
+    countLaunch();
+    kCensusCollectOld<<<nb(4 * (int64_t)n, 256), 256, 0, s>>>(w, n, rowStart, adj, he, oldRecs, newRecs, fill,
+                                                               make_int2(capOld, capNew), status);
+}
+void launchCensusCollectNew(const SplitWork& w, const int4* he, MeshDims md, CensusRec* newRecs, int* fill, int capNew,
+                            uint32_t* status, cudaStream_t s) {
+    if (w.nh <= 0) return;
+    countLaunch();
+    kCensusCollectNew<<<nb(w.nh, 256), 256, 0, s>>>(w, he, md, newRecs, fill, capNew, status);
+}
+void launchCensusApply(CensusRec* recs, const int* fill, int cap, const CensusTable& t, int sign, uint32_t* vcount,
+                       uint8_t* faceNM, int4* nmList, int nmCapacity, DevCounters* ctr, cudaStream_t s) {
+    if (cap <= 0) return;
+    countLaunch(2);
+    kCensusInsert<<<nb(cap, 256), 256, 0, s>>>(recs, fill, cap, t, &ctr->status);
+    kCensusApply<<<nb(cap, 256), 256, 0, s>>>(recs, fill, cap, t, sign, vcount, faceNM, nmList, nmCapacity, ctr);
+}
+void launchCensusFinish(const CensusRec* recs, const int* fill, int cap, const uint32_t* vcount, const uint8_t* faceNM,
+                        uint8_t* vflags, uint16_t* faceAttr, cudaStream_t s) {
+    if (cap <= 0) return;
+    countLaunch();
+    kCensusFinish<<<nb(cap, 256), 256, 0, s>>>(recs, fill, cap, vcount, faceNM, vflags, faceAttr);
 }
 
 }  // namespace mdmc

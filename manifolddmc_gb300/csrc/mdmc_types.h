@@ -23,6 +23,7 @@ enum : uint32_t {
     kStatusMappingSwap = 1u << 9,      // unexpected working-copy mapping swap
     kStatusCountMismatch = 1u << 10,   // a write outside the sizes the count pass gave
     kStatusBadIndex = 1u << 11,        // an element id outside its array (skipped)
+    kStatusCountOverflow = 1u << 12,   // a vertex's count of non-two-halfedge edges past its field
 };
 
 // unsigned range check used before every data-dependent access
