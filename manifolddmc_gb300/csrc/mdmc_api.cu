@@ -119,7 +119,7 @@ struct mdmc_context {
     DevBuf nmFlags, nmOffsets, nmFaces;
     DevBuf wPos, wNrm, wVfl, wHfl, wFfl, wVC2O, wHC2O, wFC2O, wOrigV, wOrigH, wHe, wFirst, wAttr, wVNum, wVSlots,
         wHNum, wHSlots;
-    DevBuf vO2C, hO2C, fO2C;
+    DevBuf vO2C, hO2C, fO2C, splitFlags;
     size_t vO2CCount = 0, hO2CCount = 0, fO2CCount = 0;
     DevBuf appV, appH, appF;
     // fan detection
@@ -321,6 +321,8 @@ SplitWork splitWork(mdmc_context* c, int nv, int nh, int nf) {
     w.origV = c->wOrigV.as<int>();
     w.appParent = c->appParent.as<int>();
     w.dmcV = (int)c->dmcV;
+    w.cornerLimit = nv;
+    w.flags = c->splitFlags.as<int>();
     w.origH = c->wOrigH.as<int>();
     w.he = c->wHe.as<int4>();
     w.first = c->wFirst.as<int>();
@@ -397,8 +399,10 @@ mdmc_status refreshTable(mdmc_context* c, uint32_t* status, cudaStream_t s) {
 // D/PostProcesses/ManifoldCreator.cu:488-536) and the outputs (quads by face
 // walk, getNumQuadsWithNonManifoldEdges, smallest outgoing halfedge per
 // vertex).  starsDone: the quad pass already wrote the vertex stars, quads and
-// face statistics of this mesh.
-mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaStream_t s) {
+// face statistics of this mesh.  gate: a device counter; when it is non-zero
+// the detection does nothing (a speculative pass on a mesh about to change).
+mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaStream_t s,
+                       const unsigned long long* gate = nullptr) {
     DevCounters* ctr = c->counters.as<DevCounters>();
     MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
     MDMC_CHECK(c, c->degree.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
@@ -422,8 +426,7 @@ mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaSt
         if (!starsDone) launchVertexStar(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), s);
         launchDetectFans(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), starsDone,
                          c->slowFan.as<uint8_t>(), c->isKey.as<uint8_t>(), c->keyMark, c->fans.as<int>(),
-                         c->vflags.as<uint8_t>(),
-                         ctr, status, s);
+                         c->vflags.as<uint8_t>(), ctr, status, gate, s);
     }
     markStage(c, 4, detect, s);
     if (!starsDone)
@@ -648,7 +651,10 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         MDMC_CHECK(c, cudaMemsetAsync(c->wHSlots.p, 0xFF, sizeof(int) * 4 * (size_t)nh, s));
         launchFillInt(c->wVNum.as<int>(), nv, 1, s);
         launchFillInt(c->wHNum.as<int>(), nh, 1, s);
-        const SplitWork w = splitWork(c, nv, nh, nf);
+        MDMC_CHECK(c, c->splitFlags.ensure(sizeof(int) * 4));
+        MDMC_CHECK(c, cudaMemsetAsync(c->splitFlags.p, 0, sizeof(int) * 4, s));
+        SplitWork w = splitWork(c, nv, nh, nf);
+        if (doSub) w.cornerLimit = 4 * n;
 
         // createWorkingCopies (:273-301)
         launchSplitCopy(c->nmFaces.as<int>(), n, c->he.as<int4>(), c->faceFirst.as<int>(), c->faceAttr.as<uint16_t>(),
@@ -1245,7 +1251,10 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     bool finished = false;
     if (!c->simplified) {
         markStage(c, 3, true, s);
-        if ((st = finishMesh(c, true, &ctr->specStatus, s)) != MDMC_OK) return st;
+        // (on the device the detection is skipped when the splitter will run)
+        if ((st = finishMesh(c, true, &ctr->specStatus, s, c->opt.split_non_manifold_halfedges ? &ctr->nmBuckets : nullptr)) !=
+            MDMC_OK)
+            return st;
         if (early && (st = earlyCopyVertexMaps(c, s)) != MDMC_OK) return st;
         MDMC_CHECK(c, cudaMemcpyAsync(c->hostCounters, ctr, sizeof(DevCounters), cudaMemcpyDeviceToHost, s));
         MDMC_CHECK(c, cudaStreamSynchronize(s));

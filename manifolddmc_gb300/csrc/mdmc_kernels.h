@@ -121,6 +121,10 @@ struct SplitWork {
     // DMC vertex each appended mesh vertex descends from (index o - dmcV)
     int* appParent;
     int dmcV;
+    // copies below this id are the faces' corners (4n with subdivision, nv
+    // without); flags[0] is set when a merge partner is a corner
+    int cornerLimit;
+    int* flags;
 };
 
 void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int pad, cudaStream_t s);
@@ -222,9 +226,11 @@ void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cuda
 // vertexPassDegrees: deg is the vertex pass's signed degree of the DMC mesh
 // (only the twin repair has run since); otherwise non-negative degrees.
 // isKey[h] == keyMark marks this pass's fan keys (no other entry may hold it)
+// (gate: when given and non-zero, the pass does nothing: the fan-slow count
+// stays zero, so the later fan passes do nothing either)
 void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, bool vertexPassDegrees,
                       uint8_t* slow, uint8_t* isKey, uint8_t keyMark, int* fans, uint8_t* vflags, DevCounters* ctr,
-                      uint32_t* status, cudaStream_t s);
+                      uint32_t* status, const unsigned long long* gate, cudaStream_t s);
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, const uint8_t* faceNM,
                   int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s);
 

@@ -486,7 +486,9 @@ __global__ void kVertexStar(const int4* __restrict__ he, MeshDims md, int* __res
 // closed fan.
 __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restrict__ vertexHE,
                          const int* __restrict__ deg, bool vertexPassDegrees, int* __restrict__ fans,
-                         uint8_t* __restrict__ slow, uint8_t* __restrict__ vflags, unsigned long long* slowCount) {
+                         uint8_t* __restrict__ slow, uint8_t* __restrict__ vflags, unsigned long long* slowCount,
+                         const unsigned long long* gate) {
+    if (gate && *gate != 0) return;  // a speculative pass whose mesh the splitter will change
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     bool isSlow = false;
     if (v < md.V) {
@@ -632,12 +634,11 @@ void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cuda
 
 void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, bool vertexPassDegrees,
                       uint8_t* slow, uint8_t* isKey, uint8_t keyMark, int* fans, uint8_t* vflags, DevCounters* ctr,
-                      uint32_t* status,
-                      cudaStream_t s) {
+                      uint32_t* status, const unsigned long long* gate, cudaStream_t s) {
     if (md.V > 0) {
         countLaunch();
         kFanFast<<<(md.V + 255) / 256, 256, 0, s>>>(he, md, vertexHE, deg, vertexPassDegrees, fans, slow, vflags,
-                                                    &ctr->slowFans);
+                                                    &ctr->slowFans, gate);
     }
     if (md.H > 0) {
         countLaunch();

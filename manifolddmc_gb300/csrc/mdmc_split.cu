@@ -64,12 +64,22 @@ __global__ void kCopyOut(const int* __restrict__ nmFaces, int n, const int4* __r
         return;
     }
     int h = faceFirst[f];
+    // a face of the DMC mesh holds halfedges 4f'..4f'+3 in walk order: load
+    // them together (and check the order), else walk
+    int4 e4[4];
+    bool direct = (h & 3) == 0 && inb(h + 3, w.H);
+    if (direct) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) e4[i] = he[h + i];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) direct = direct && e4[i].z == h + ((i + 1) & 3);
+    }
     for (int i = 0; i < 4; ++i) {
-        if (!inb(h, w.H) || !inb(he[h].x, w.V)) {
+        if (!inb(h, w.H) || !inb(direct ? e4[i].x : he[h].x, w.V)) {
             atomicOr(status, kStatusBadIndex);
             return;
         }
-        const int4 e = he[h];
+        const int4 e = direct ? e4[i] : he[h];
         const int c = 4 * k + i;
         const int v = e.x;
         for (int a = 0; a < 3; ++a) {
@@ -138,16 +148,36 @@ __global__ void kSubdivide(int n, SplitWork w, uint32_t* status) {
     if (k >= n) return;
     const float uvs[4][2] = {{0.33f, 0.33f}, {0.67f, 0.33f}, {0.67f, 0.67f}, {0.33f, 0.67f}};
     int hid[4], vid[4];
-    int h = w.first[k];
+    int4 orig[4];  // the face's halfedge records
+    // the copy of face k holds halfedges 4k..4k+3 in walk order (kCopyOut,
+    // kUpdateRefs): load them together, walk only if that does not hold
+#pragma unroll
+    for (int i = 0; i < 4; ++i) orig[i] = w.he[4 * k + i];
+    bool direct = w.first[k] == 4 * k;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) direct = direct && orig[i].z == 4 * k + ((i + 1) & 3);
+    if (direct) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) hid[i] = 4 * k + i;
+    } else {
+        int h = w.first[k];
+        for (int i = 0; i < 4; ++i) {
+            if (!inb(h, w.nh)) {
+                atomicOr(status, kStatusBadIndex);
+                return;
+            }
+            hid[i] = h;
+            orig[i] = w.he[h];
+            h = orig[i].z;
+        }
+    }
+#pragma unroll
     for (int i = 0; i < 4; ++i) {
-        if (!inb(h, w.nh) || !inb(w.he[h].x, w.nv)) {
+        if (!inb(orig[i].x, w.nv)) {
             atomicOr(status, kStatusBadIndex);
             return;
         }
-        hid[i] = h;
-        const int4 e = w.he[h];
-        vid[i] = e.x;
-        h = e.z;
+        vid[i] = orig[i].x;
     }
     F3 P[4], N[4];
     for (int i = 0; i < 4; ++i) {
@@ -155,46 +185,54 @@ __global__ void kSubdivide(int n, SplitWork w, uint32_t* status) {
         N[i] = f3(w.nrm[3 * (int64_t)vid[i]], w.nrm[3 * (int64_t)vid[i] + 1], w.nrm[3 * (int64_t)vid[i] + 2]);
     }
     auto mix = [](F3 a, F3 b, float t) { return a * (1.f - t) + b * t; };
+    // inner vertices 4n+4k..4n+4k+3: positions and normals as three float4 each
+    float pq[12], nq[12];
     int inner[4];
     for (int i = 0; i < 4; ++i) {
         const float u = uvs[i][0], v = uvs[i][1];
         const F3 pp = mix(mix(P[0], P[1], u), mix(P[3], P[2], u), v);
         const F3 nn = mix(mix(N[0], N[1], u), mix(N[3], N[2], u), v);
-        const int c = 4 * n + 4 * k + i;
-        w.origV[c] = w.vC2O[vid[i]];  // the differentiable path's parent: corner i
-        w.pos[3 * (int64_t)c] = pp.x; w.pos[3 * (int64_t)c + 1] = pp.y; w.pos[3 * (int64_t)c + 2] = pp.z;
-        w.nrm[3 * (int64_t)c] = nn.x; w.nrm[3 * (int64_t)c + 1] = nn.y; w.nrm[3 * (int64_t)c + 2] = nn.z;
-        inner[i] = c;
+        pq[3 * i] = pp.x; pq[3 * i + 1] = pp.y; pq[3 * i + 2] = pp.z;
+        nq[3 * i] = nn.x; nq[3 * i + 1] = nn.y; nq[3 * i + 2] = nn.z;
+        inner[i] = 4 * n + 4 * k + i;
     }
+    {
+        const int64_t c0 = 4 * (int64_t)n + 4 * (int64_t)k;
+        float4* pd = reinterpret_cast<float4*>(w.pos + 3 * c0);
+        float4* nd = reinterpret_cast<float4*>(w.nrm + 3 * c0);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            pd[q] = make_float4(pq[4 * q], pq[4 * q + 1], pq[4 * q + 2], pq[4 * q + 3]);
+            nd[q] = make_float4(nq[4 * q], nq[4 * q + 1], nq[4 * q + 2], nq[4 * q + 3]);
+        }
+        // the differentiable path's parent of inner vertex i: corner i
+        *reinterpret_cast<int4*>(w.origV + c0) =
+            make_int4(w.vC2O[vid[0]], w.vC2O[vid[1]], w.vC2O[vid[2]], w.vC2O[vid[3]]);
+    }
+    // halfedges 4n+16k..+15, each written once with its twin: the inner ring
+    // (i -> i+1, twin: the second halfedge of boundary quad i+1), then three
+    // per boundary quad j (corner j -> inner j -> inner j-1 -> the original
+    // edge j-1, which closes it)
     const int hb = 4 * n + 16 * k;
     int ih[4];
+#pragma unroll
     for (int i = 0; i < 4; ++i) ih[i] = hb + i;
-    for (int i = 0; i < 4; ++i) w.he[ih[i]] = make_int4(inner[i], k, ih[(i + 1) & 3], -1);
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+        w.he[ih[i]] = make_int4(inner[i], k, ih[(i + 1) & 3], hb + 4 + 3 * ((i + 1) & 3) + 1);
     w.first[k] = ih[0];
-    int of[4][4];
-    int prev = 3;
+#pragma unroll
     for (int j = 0; j < 4; ++j) {
-        const int qv[3] = {vid[j], inner[j], inner[prev]};
-        for (int t = 0; t < 3; ++t) of[j][t] = hb + 4 + 3 * j + t;
-        of[j][3] = hid[prev];
+        const int prev = (j + 3) & 3;
+        const int q = hb + 4 + 3 * j;
         const int nf = n + 4 * k + j;
-        for (int t = 0; t < 3; ++t) w.he[of[j][t]] = make_int4(qv[t], nf, of[j][(t + 1) & 3], -1);
+        w.he[q] = make_int4(vid[j], nf, q + 1, hb + 4 + 3 * ((j + 1) & 3) + 2);
+        w.he[q + 1] = make_int4(inner[j], nf, q + 2, ih[prev]);
+        w.he[q + 2] = make_int4(inner[prev], nf, hid[prev], hb + 4 + 3 * prev);
         // the original edge keeps origin and twin, joins the boundary quad
-        int4 o = w.he[hid[prev]];
-        o.y = nf;
-        o.z = of[j][0];
-        w.he[hid[prev]] = o;
-        w.first[nf] = of[j][0];
+        w.he[hid[prev]] = make_int4(orig[prev].x, nf, q, orig[prev].w);
+        w.first[nf] = q;
         w.attr[nf] = 0x1F;  // HalfedgeFace(): INVALID_COLOR
-        prev = j;
-    }
-    prev = 3;
-    for (int j = 0; j < 4; ++j) {
-        w.he[of[j][2]].w = of[prev][0];
-        w.he[of[prev][0]].w = of[j][2];
-        w.he[of[j][1]].w = ih[prev];
-        w.he[ih[prev]].w = of[j][1];
-        prev = j;
     }
     // swapHalfedgeMappings (:629-648): the inner ring takes over the original
     // halfedge slots, the original edges become new halfedges
@@ -231,9 +269,12 @@ __global__ void kCollapse(SplitWork w, uint32_t* status) {
     }
     if (tw < t) return;
     int f0[4], f1[4];
-    int4 cur = w.he[t], ctw = w.he[tw];
+    int4 E0[4], E1[4];  // the records of f0 and f1
+    E0[0] = w.he[t];
+    E1[0] = w.he[tw];
     f0[0] = t;
     f1[0] = tw;
+    int4 cur = E0[0], ctw = E1[0];
     for (int i = 1; i < 4; ++i) {
         if (!inb(cur.z, w.nh) || !inb(ctw.z, w.nh)) {
             atomicOr(status, kStatusBadIndex);
@@ -243,31 +284,38 @@ __global__ void kCollapse(SplitWork w, uint32_t* status) {
         f1[4 - i] = ctw.z;
         cur = w.he[cur.z];
         ctw = w.he[ctw.z];
+        E0[i] = cur;
+        E1[4 - i] = ctw;
     }
-    const int fa = w.he[f0[0]].y, fb = w.he[f1[0]].y;
+    const int fa = E0[0].y, fb = E1[0].y;
     if (!inb(fa, w.nf) || !inb(fb, w.nf)) {
         atomicOr(status, kStatusBadIndex);
         return;
     }
+    // a boundary quad holds one original edge, so one thread removes it and
+    // its halfedges: plain read-modify-writes (others only read the
+    // non-manifold bit of these words, which does not change)
     for (int i = 0; i < 4; ++i) {
-        atomicOr(&w.hfl[f0[i]], kRemove);
-        atomicOr(&w.hfl[f1[i]], kRemove);
+        w.hfl[f0[i]] |= kRemove;
+        w.hfl[f1[i]] |= kRemove;
     }
-    atomicOr(&w.ffl[fa], kRemove);
-    atomicOr(&w.ffl[fb], kRemove);
+    w.ffl[fa] |= kRemove;
+    w.ffl[fb] |= kRemove;
     {
-        const int a = w.he[f0[2]].x, b = w.he[f1[1]].x;
+        const int a = E0[2].x, b = E1[1].x;
         markPartner(w.vNum, w.vSlots, w.nv, a, b, status);
         markPartner(w.vNum, w.vSlots, w.nv, b, a, status);
+        if (a < w.cornerLimit || b < w.cornerLimit) w.flags[0] = 1;
     }
     {
-        const int a = w.he[f0[3]].x, b = w.he[f1[2]].x;
+        const int a = E0[3].x, b = E1[2].x;
         markPartner(w.vNum, w.vSlots, w.nv, a, b, status);
         markPartner(w.vNum, w.vSlots, w.nv, b, a, status);
+        if (a < w.cornerLimit || b < w.cornerLimit) w.flags[0] = 1;
     }
     for (int i = 1; i < 4; ++i) {
         const int a = f0[i], b = f1[i];
-        const int at = w.he[a].w, bt = w.he[b].w;
+        const int at = E0[i].w, bt = E1[i].w;
         if (at < 0 || bt < 0) {
             atomicOr(status, kStatusBadTwin);
             continue;
@@ -353,18 +401,44 @@ __global__ void kMergeVertices(SplitWork w, uint32_t* status) {
     w.nrm[3 * (int64_t)smallest] = p.x; w.nrm[3 * (int64_t)smallest + 1] = p.y; w.nrm[3 * (int64_t)smallest + 2] = p.z;
 }
 
-// updateHalfedgeVertexIDs (:992-1019)
+// updateHalfedgeVertexIDs (:992-1019), grid-stride over the halfedges; only
+// when a corner copy has merge partners (flags[0]) or without subdivision
 __global__ void kUpdateOrigins(SplitWork w, uint32_t* status) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= w.nh) return;
-    const int v = w.he[t].x;
-    if (!inb(v, w.nv)) return;
+    if (w.cornerLimit < w.nv && w.flags[0] == 0) return;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < w.nh; t += gridDim.x * blockDim.x) {
+        const int v = w.he[t].x;
+        if (!inb(v, w.nv)) continue;
+        int part[12];
+        const int np = closure(w.vNum, w.vSlots, v, part, status);
+        if (np <= 1) continue;
+        int s = v;
+        for (int i = 0; i < np - 1; ++i) s = min(s, part[i]);
+        w.he[t].x = s;
+    }
+}
+
+// The same for the subdivision's inner vertices, one thread per vertex: inner
+// vertex i of face k is the origin of exactly three halfedges (its inner-ring
+// halfedge, and the second and third halfedge of two boundary quads; see
+// kSubdivide), so a vertex with merge partners rewrites those three.
+__global__ void kUpdateInnerOrigins(SplitWork w, int n, uint32_t* status) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= 4 * n) return;
+    const int v = 4 * n + j;
     int part[12];
     const int np = closure(w.vNum, w.vSlots, v, part, status);
     if (np <= 1) return;
-    int s = v;
-    for (int i = 0; i < np - 1; ++i) s = min(s, part[i]);
-    w.he[t].x = s;
+    int sm = v;
+    for (int i = 0; i < np - 1; ++i) sm = min(sm, part[i]);
+    const int k = j >> 2, i = j & 3;
+    const int hb = 4 * n + 16 * k;
+    const int hs[3] = {hb + i, hb + 4 + 3 * i + 1, hb + 4 + 3 * ((i + 1) & 3) + 2};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        int* x = reinterpret_cast<int*>(w.he) + 4 * (int64_t)hs[q];
+        if (*x == v) *x = sm;
+        else atomicOr(status, kStatusMappingSwap);
+    }
 }
 
 // mergeHalfedges (:1021-1067): reads only removed partners' twins, which no
@@ -722,7 +796,11 @@ void launchSplitCollapse(const SplitWork& w, uint32_t* status, cudaStream_t s) {
 void launchSplitMerge(const SplitWork& w, uint32_t* status, cudaStream_t s) {
     countLaunch(2);
     kMergeVertices<<<nb(w.nv, 128), 128, 0, s>>>(w, status);
-    kUpdateOrigins<<<nb(w.nh, 128), 128, 0, s>>>(w, status);
+    if (w.cornerLimit < w.nv) {  // subdivided: nv = 8n, corners below 4n
+        countLaunch();
+        kUpdateInnerOrigins<<<nb(w.cornerLimit, 128), 128, 0, s>>>(w, w.cornerLimit / 4, status);
+    }
+    kUpdateOrigins<<<std::min(nb(w.nh, 128), 152 * 16), 128, 0, s>>>(w, status);
 }
 void launchSplitMergeHalfedges(const SplitWork& w, uint32_t* status, cudaStream_t s) {
     countLaunch();
