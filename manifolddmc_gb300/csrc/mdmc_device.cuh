@@ -79,16 +79,6 @@ __host__ __device__ __forceinline__ int quadSlot(int e, int edgyBit) {
     return (int)((240177437832960ULL >> (4 * e + 2 * edgyBit)) & 3);
 }
 
-// cell faces in the flattened orientation (D/CellIntersection.inl:290-292)
-__device__ __forceinline__ int faceEdge(int f, int i) {
-    const unsigned short fe[6] = {0x0123, 0x4765, 0x4908, 0x2A6B, 0x83B7, 0x95A1};
-    return (fe[f] >> (4 * i)) & 0xF;
-}
-__device__ __forceinline__ int faceCorner(int f, int i) {
-    const unsigned short fc[6] = {0x3120, 0x6475, 0x1504, 0x7362, 0x2064, 0x7531};
-    return (fc[f] >> (4 * i)) & 0xF;
-}
-
 // a face of the cell has the diagonal sign pattern (four crossing edges)
 __host__ __device__ constexpr bool caseHasDiagonalFace(int c) {
     const unsigned short fc[6] = {0x3120, 0x6475, 0x1504, 0x7362, 0x2064, 0x7531};
@@ -116,53 +106,55 @@ __host__ __device__ constexpr bool caseIsAmbiguous(int c) {
 // classified, their oriented segments connected, ambiguous faces decided by
 // the bilinear saddle value, and the segments chained into contours starting
 // from the lowest unused edge.
-__device__ inline uint64_t asymptoticContours(const float s[8], float iso) {
-    uint32_t seg[12];
-#pragma unroll
-    for (int i = 0; i < 12; ++i) seg[i] = 0xFF;
-    auto connect = [&](int in, int out) {
+// The procedure depends on the cell's values only through its case and, for
+// each face with the diagonal pattern, one bit: the decider's value >= iso.
+// contoursFromDecisions runs it on those bits (bit f of `hi` for face f), so
+// every (case, decisions) pair can be tabulated at compile time below.
+// cell faces in the flattened orientation (D/CellIntersection.inl:290-292)
+__host__ __device__ constexpr int faceEdgeC(int f, int i) {
+    const unsigned short fe[6] = {0x0123, 0x4765, 0x4908, 0x2A6B, 0x83B7, 0x95A1};
+    return (fe[f] >> (4 * i)) & 0xF;
+}
+__host__ __device__ constexpr int faceCornerC(int f, int i) {
+    const unsigned short fc[6] = {0x3120, 0x6475, 0x1504, 0x7362, 0x2064, 0x7531};
+    return (fc[f] >> (4 * i)) & 0xF;
+}
+__host__ __device__ constexpr unsigned faceSigns(int cs, int f) {
+    unsigned fc = 0;
+    for (int i = 0; i < 4; ++i) fc |= (unsigned)((cs >> faceCornerC(f, i)) & 1) << i;
+    return fc;
+}
+__host__ __device__ constexpr uint64_t contoursFromDecisions(int cs, unsigned hi) {
+    uint32_t seg[12] = {0xFF, 0xFF, 0xFF, 0xFF, 0xFF, 0xFF, 0xFF, 0xFF, 0xFF, 0xFF, 0xFF, 0xFF};
+    auto connect = [&seg](int in, int out) {
         seg[in] = (seg[in] & 0xF0u) | (uint32_t)(out & 0xF);
         seg[out] = (seg[out] & 0x0Fu) | (uint32_t)(in << 4);
     };
     for (int f = 0; f < 6; ++f) {
-        int e[4];
-        float val[4];
-        unsigned fc = 0;
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            e[i] = faceEdge(f, i);
-            val[i] = s[faceCorner(f, i)];
-            fc |= (unsigned)(val[i] >= iso) << i;
-        }
+        const int e0 = faceEdgeC(f, 0), e1 = faceEdgeC(f, 1), e2 = faceEdgeC(f, 2), e3 = faceEdgeC(f, 3);
+        const unsigned fc = faceSigns(cs, f);
+        const bool h = ((hi >> f) & 1u) != 0;
         switch (fc) {
-            case 1: connect(e[0], e[3]); break;
-            case 2: connect(e[1], e[0]); break;
-            case 3: connect(e[1], e[3]); break;
-            case 4: connect(e[3], e[2]); break;
-            case 5: connect(e[0], e[2]); break;
-            case 7: connect(e[1], e[2]); break;
-            case 8: connect(e[2], e[1]); break;
-            case 10: connect(e[2], e[0]); break;
-            case 11: connect(e[2], e[3]); break;
-            case 12: connect(e[3], e[1]); break;
-            case 13: connect(e[0], e[1]); break;
-            case 14: connect(e[3], e[0]); break;
+            case 1: connect(e0, e3); break;
+            case 2: connect(e1, e0); break;
+            case 3: connect(e1, e3); break;
+            case 4: connect(e3, e2); break;
+            case 5: connect(e0, e2); break;
+            case 7: connect(e1, e2); break;
+            case 8: connect(e2, e1); break;
+            case 10: connect(e2, e0); break;
+            case 11: connect(e2, e3); break;
+            case 12: connect(e3, e1); break;
+            case 13: connect(e0, e1); break;
+            case 14: connect(e3, e0); break;
             case 6:
-            case 9: {
-                float num = val[0] * val[3] - val[1] * val[2];
-                float den = val[0] + val[3];
-                den = den - val[1];
-                den = den - val[2];
-                float decision = num / den;
-                bool hi = decision >= iso;
-                if (fc == 6) {
-                    if (hi) { connect(e[3], e[0]); connect(e[1], e[2]); }
-                    else { connect(e[1], e[0]); connect(e[3], e[2]); }
-                } else {
-                    if (hi) { connect(e[0], e[1]); connect(e[2], e[3]); }
-                    else { connect(e[0], e[3]); connect(e[2], e[1]); }
-                }
-            } break;
+                if (h) { connect(e3, e0); connect(e1, e2); }
+                else { connect(e1, e0); connect(e3, e2); }
+                break;
+            case 9:
+                if (h) { connect(e0, e1); connect(e2, e3); }
+                else { connect(e0, e3); connect(e2, e1); }
+                break;
             default: break;
         }
     }
@@ -181,7 +173,7 @@ __device__ inline uint64_t asymptoticContours(const float s[8], float iso) {
             ++pos;
             bit = 16 + 4 * (used + pos);
             if (bit <= 60) c = (c & ~(0xFULL << bit)) | ((uint64_t)out << bit);
-            int in = out;
+            const int in = out;
             if (in < 12) {
                 out = (int)(seg[in] & 0xF);
                 seg[in] = 0xFF;
@@ -233,6 +225,88 @@ constexpr CaseTables makeCaseTables() {
     return t;
 }
 __device__ const CaseTables kCaseTables = makeCaseTables();
+
+// Every case with every combination of decisions on its diagonal faces:
+// info[cs] = first entry (bits 0-15) | the case's diagonal-face mask << 16;
+// entry first + b holds the contour word and edge map for decision bits b
+// (bit j: the j-th diagonal face in face order).  656 entries.
+__host__ __device__ constexpr unsigned diagonalFaces(int cs) {
+    unsigned m = 0;
+    for (int f = 0; f < 6; ++f) {
+        const unsigned fc = faceSigns(cs, f);
+        if (fc == 6 || fc == 9) m |= 1u << f;
+    }
+    return m;
+}
+__host__ __device__ constexpr int popcount6(unsigned m) {
+    int n = 0;
+    for (int f = 0; f < 6; ++f) n += (m >> f) & 1u;
+    return n;
+}
+constexpr int countDecisionEntries() {
+    int n = 0;
+    for (int cs = 0; cs < 256; ++cs) n += 1 << popcount6(diagonalFaces(cs));
+    return n;
+}
+constexpr int kDecisionEntries = countDecisionEntries();
+static_assert(kDecisionEntries == 656, "decision table size");
+struct DecisionTables {
+    uint32_t info[256];
+    unsigned long long words[kDecisionEntries];
+    uint32_t edgeMaps[kDecisionEntries];
+};
+constexpr DecisionTables makeDecisionTables() {
+    DecisionTables t{};
+    int at = 0;
+    for (int cs = 0; cs < 256; ++cs) {
+        const unsigned m = diagonalFaces(cs);
+        const int k = popcount6(m);
+        t.info[cs] = (uint32_t)at | (m << 16);
+        for (unsigned b = 0; b < (1u << k); ++b) {
+            // spread decision bits b over the diagonal faces
+            unsigned hi = 0;
+            int j = 0;
+            for (int f = 0; f < 6; ++f)
+                if ((m >> f) & 1u) hi |= ((b >> j++) & 1u) << f;
+            t.words[at + (int)b] = contoursFromDecisions(cs, hi);
+            t.edgeMaps[at + (int)b] = contourEdgeMap(t.words[at + (int)b]);
+        }
+        at += 1 << k;
+    }
+    return t;
+}
+__device__ const DecisionTables kDecisionTables = makeDecisionTables();
+
+// marchingCubesAsymptoticPolygon on the cell's values: the case, the
+// decider's bit for each diagonal face (the bilinear saddle value
+// (v0 v3 - v1 v2) / (v0 + v3 - v1 - v2) against iso, D/CellIntersection.inl:
+// 248-252), and the entry of that combination
+__device__ __forceinline__ int asymptoticEntry(const float s[8], float iso) {
+    int cs = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) cs |= (s[i] >= iso ? 1 : 0) << i;
+    const uint32_t info = kDecisionTables.info[cs];
+    const unsigned m = info >> 16;
+    unsigned bits = 0;
+    int j = 0;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+        if (!((m >> f) & 1u)) continue;
+        const float v0 = s[faceCornerC(f, 0)], v1 = s[faceCornerC(f, 1)], v2 = s[faceCornerC(f, 2)],
+                    v3 = s[faceCornerC(f, 3)];
+        const float num = v0 * v3 - v1 * v2;
+        float den = v0 + v3;
+        den = den - v1;
+        den = den - v2;
+        const float decision = num / den;
+        bits |= (decision >= iso ? 1u : 0u) << j;
+        ++j;
+    }
+    return (int)(info & 0xFFFFu) + (int)bits;
+}
+__device__ __forceinline__ uint64_t asymptoticContours(const float s[8], float iso) {
+    return kDecisionTables.words[asymptoticEntry(s, iso)];
+}
 
 // contours of an active cell from a tagged word table (above)
 __device__ __forceinline__ uint64_t taggedContours(uint64_t word, const float s[8], float iso) {

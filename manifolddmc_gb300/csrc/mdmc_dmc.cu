@@ -893,7 +893,7 @@ __global__ void __launch_bounds__(128) kEmitActive(View g, float iso, const uint
         if (cs >= 0 && c2 != cs) atomicOr(status, kStatusCountMismatch);
         cs = c2;
         em = edgeMaps[cs];
-        if (em == 0xFFFFFFFFu) em = contourEdgeMap(asymptoticContours(s, iso));
+        if (em == 0xFFFFFFFFu) em = kDecisionTables.edgeMaps[asymptoticEntry(s, iso)];
     }
     if (cs == 0 || cs == 255) {
         atomicOr(status, kStatusCountMismatch);

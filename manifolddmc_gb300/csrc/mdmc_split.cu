@@ -269,12 +269,9 @@ __global__ void kCollapse(SplitWork w, uint32_t* status) {
     }
     if (tw < t) return;
     int f0[4], f1[4];
-    int4 E0[4], E1[4];  // the records of f0 and f1
-    E0[0] = w.he[t];
-    E1[0] = w.he[tw];
+    int4 cur = w.he[t], ctw = w.he[tw];
     f0[0] = t;
     f1[0] = tw;
-    int4 cur = E0[0], ctw = E1[0];
     for (int i = 1; i < 4; ++i) {
         if (!inb(cur.z, w.nh) || !inb(ctw.z, w.nh)) {
             atomicOr(status, kStatusBadIndex);
@@ -284,38 +281,33 @@ __global__ void kCollapse(SplitWork w, uint32_t* status) {
         f1[4 - i] = ctw.z;
         cur = w.he[cur.z];
         ctw = w.he[ctw.z];
-        E0[i] = cur;
-        E1[4 - i] = ctw;
     }
-    const int fa = E0[0].y, fb = E1[0].y;
+    const int fa = w.he[f0[0]].y, fb = w.he[f1[0]].y;
     if (!inb(fa, w.nf) || !inb(fb, w.nf)) {
         atomicOr(status, kStatusBadIndex);
         return;
     }
-    // a boundary quad holds one original edge, so one thread removes it and
-    // its halfedges: plain read-modify-writes (others only read the
-    // non-manifold bit of these words, which does not change)
     for (int i = 0; i < 4; ++i) {
-        w.hfl[f0[i]] |= kRemove;
-        w.hfl[f1[i]] |= kRemove;
+        atomicOr(&w.hfl[f0[i]], kRemove);
+        atomicOr(&w.hfl[f1[i]], kRemove);
     }
-    w.ffl[fa] |= kRemove;
-    w.ffl[fb] |= kRemove;
+    atomicOr(&w.ffl[fa], kRemove);
+    atomicOr(&w.ffl[fb], kRemove);
     {
-        const int a = E0[2].x, b = E1[1].x;
+        const int a = w.he[f0[2]].x, b = w.he[f1[1]].x;
         markPartner(w.vNum, w.vSlots, w.nv, a, b, status);
         markPartner(w.vNum, w.vSlots, w.nv, b, a, status);
         if (a < w.cornerLimit || b < w.cornerLimit) w.flags[0] = 1;
     }
     {
-        const int a = E0[3].x, b = E1[2].x;
+        const int a = w.he[f0[3]].x, b = w.he[f1[2]].x;
         markPartner(w.vNum, w.vSlots, w.nv, a, b, status);
         markPartner(w.vNum, w.vSlots, w.nv, b, a, status);
         if (a < w.cornerLimit || b < w.cornerLimit) w.flags[0] = 1;
     }
     for (int i = 1; i < 4; ++i) {
         const int a = f0[i], b = f1[i];
-        const int at = E0[i].w, bt = E1[i].w;
+        const int at = w.he[a].w, bt = w.he[b].w;
         if (at < 0 || bt < 0) {
             atomicOr(status, kStatusBadTwin);
             continue;
