@@ -668,7 +668,24 @@ __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__
         int h = faceFirst[f];
         int q[4] = {-1, -1, -1, -1}, hs[4] = {-1, -1, -1, -1};
         bool ok = true;
-        for (int i = 0; i < 4 && ok; ++i) {
+        // most faces (DMC quads, and the inner quads the splitter leaves in
+        // their slots) hold halfedges h..h+3 in walk order: load those four
+        // together and walk only when the links say otherwise
+        bool direct = (h & 3) == 0 && inb(h + 3, md.H);
+        if (direct) {
+            int4 e[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) e[i] = he[h + i];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) direct = direct && e[i].z == h + ((i + 1) & 3);
+            if (direct)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    q[i] = e[i].x;
+                    hs[i] = h + i;
+                }
+        }
+        for (int i = 0; i < 4 && ok && !direct; ++i) {
             ok = inb(h, md.H);
             if (ok) {
                 const int4 e = he[h];

@@ -74,6 +74,9 @@ __global__ void kCopyOut(const int* __restrict__ nmFaces, int n, const int4* __r
 #pragma unroll
         for (int i = 0; i < 4; ++i) direct = direct && e4[i].z == h + ((i + 1) & 3);
     }
+    // copies 4k..4k+3: gathered in registers, written as whole vectors
+    int vs[4], hs[4];
+    float pq[12], nq[12];
     for (int i = 0; i < 4; ++i) {
         if (!inb(h, w.H) || !inb(direct ? e4[i].x : he[h].x, w.V)) {
             atomicOr(status, kStatusBadIndex);
@@ -83,18 +86,28 @@ __global__ void kCopyOut(const int* __restrict__ nmFaces, int n, const int4* __r
         const int c = 4 * k + i;
         const int v = e.x;
         for (int a = 0; a < 3; ++a) {
-            w.pos[3 * (int64_t)c + a] = pos[3 * (int64_t)v + a];
-            w.nrm[3 * (int64_t)c + a] = nrm[3 * (int64_t)v + a];
+            pq[3 * i + a] = pos[3 * (int64_t)v + a];
+            nq[3 * i + a] = nrm[3 * (int64_t)v + a];
         }
-        w.vC2O[c] = v;
-        w.origV[c] = v;
+        vs[i] = v;
+        hs[i] = h;
         atomicMin(&w.vO2C[v], c);
         w.he[c] = e;
-        w.hC2O[c] = h;
-        w.origH[c] = h;
         w.hO2C[h] = c;
         h = e.z;
     }
+    float4* pd = reinterpret_cast<float4*>(w.pos + 12 * (int64_t)k);
+    float4* nd = reinterpret_cast<float4*>(w.nrm + 12 * (int64_t)k);
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        pd[q] = make_float4(pq[4 * q], pq[4 * q + 1], pq[4 * q + 2], pq[4 * q + 3]);
+        nd[q] = make_float4(nq[4 * q], nq[4 * q + 1], nq[4 * q + 2], nq[4 * q + 3]);
+    }
+    const int4 v4 = make_int4(vs[0], vs[1], vs[2], vs[3]), h4 = make_int4(hs[0], hs[1], hs[2], hs[3]);
+    *reinterpret_cast<int4*>(w.vC2O + 4 * (int64_t)k) = v4;
+    *reinterpret_cast<int4*>(w.origV + 4 * (int64_t)k) = v4;
+    *reinterpret_cast<int4*>(w.hC2O + 4 * (int64_t)k) = h4;
+    *reinterpret_cast<int4*>(w.origH + 4 * (int64_t)k) = h4;
     w.first[k] = 4 * k;  // hO2C of the face's first halfedge
     w.attr[k] = faceAttr[f];
     w.fC2O[k] = f;
