@@ -124,6 +124,10 @@ struct mdmc_context {
     DevBuf appV, appH, appF;
     // fan detection
     DevBuf isKey, fans, degree, slowFan;
+    // the vertex pass's degrees kept through the splitter, and its marks of
+    // the DMC vertices whose fans it may change (fastFans: both valid)
+    DevBuf dmcDegree, splitTouched;
+    bool fastFans = false;
     uint8_t keyMark = 0;  // the last detection pass's fan-key mark (1..255, 0 = none yet)
     // standard Marching Cubes: edge mask and the index of each word's first
     // edge, per active cell its case and triangle offset, the vertices' edge
@@ -323,6 +327,7 @@ SplitWork splitWork(mdmc_context* c, int nv, int nh, int nf) {
     w.dmcV = (int)c->dmcV;
     w.cornerLimit = nv;
     w.flags = c->splitFlags.as<int>();
+    w.touched = c->fastFans ? c->splitTouched.as<uint8_t>() : nullptr;
     w.origH = c->wOrigH.as<int>();
     w.he = c->wHe.as<int4>();
     w.first = c->wFirst.as<int>();
@@ -426,7 +431,9 @@ mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaSt
         if (!starsDone) launchVertexStar(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), s);
         launchDetectFans(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), starsDone,
                          c->slowFan.as<uint8_t>(), c->isKey.as<uint8_t>(), c->keyMark, c->fans.as<int>(),
-                         c->vflags.as<uint8_t>(), ctr, status, gate, s);
+                         c->vflags.as<uint8_t>(), ctr, status, gate,
+                         (!starsDone && c->fastFans) ? c->dmcDegree.as<int>() : nullptr, c->splitTouched.as<uint8_t>(),
+                         (int)c->dmcV, s);
     }
     markStage(c, 4, detect, s);
     if (!starsDone)
@@ -600,6 +607,16 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
     uint32_t* status = &ctr->status;
     const int step = c->opt.splitting_step;
     iterations = 0;
+    // keep the vertex pass's degrees for the fan detection after the splitter
+    // (valid for the DMC mesh as the twin repair left it; not after a
+    // simplification renumbered it)
+    if (c->opt.detect_non_manifold_vertices && !c->simplified && c->dmcV == c->V) {
+        std::swap(c->degree.p, c->dmcDegree.p);
+        std::swap(c->degree.bytes, c->dmcDegree.bytes);
+        MDMC_CHECK(c, c->splitTouched.ensure((size_t)std::max<int64_t>(c->dmcV, 1)));
+        MDMC_CHECK(c, cudaMemsetAsync(c->splitTouched.p, 0, (size_t)c->dmcV, s));
+        c->fastFans = c->dmcDegree.bytes >= sizeof(int) * (size_t)c->dmcV;
+    }
     while (true) {
         // countNonManifoldFaces + the list of non-manifold faces
         MDMC_CHECK(c, c->nmFlags.ensure(sizeof(int) * (size_t)(c->F + 1)));
@@ -1065,6 +1082,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
     c->simplified = false;
     c->earlyFaces = c->earlyVertices = c->earlyVertexMaps = c->lateChange = false;
     c->rowsValid = false;
+    c->fastFans = false;
     std::memset(&c->stats, 0, sizeof c->stats);
     DevCounters* ctr = c->counters.as<DevCounters>();
     uint32_t* status = &ctr->status;

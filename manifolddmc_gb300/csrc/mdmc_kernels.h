@@ -125,6 +125,9 @@ struct SplitWork {
     // without); flags[0] is set when a merge partner is a corner
     int cornerLimit;
     int* flags;
+    // optional: marks the DMC vertices (ids below dmcV) that are corners of
+    // a copied face, i.e. whose fans the splitter may change
+    uint8_t* touched;
 };
 
 void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int pad, cudaStream_t s);
@@ -228,9 +231,12 @@ void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cuda
 // isKey[h] == keyMark marks this pass's fan keys (no other entry may hold it)
 // (gate: when given and non-zero, the pass does nothing: the fan-slow count
 // stays zero, so the later fan passes do nothing either)
+// (dmcDeg, touched, dmcV: optional; after the splitter, a DMC vertex it did
+// not touch whose vertex-pass degree was positive still has one closed fan)
 void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, bool vertexPassDegrees,
                       uint8_t* slow, uint8_t* isKey, uint8_t keyMark, int* fans, uint8_t* vflags, DevCounters* ctr,
-                      uint32_t* status, const unsigned long long* gate, cudaStream_t s);
+                      uint32_t* status, const unsigned long long* gate, const int* dmcDeg, const uint8_t* touched,
+                      int dmcV, cudaStream_t s);
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, const uint8_t* faceNM,
                   int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s);
 

@@ -483,11 +483,14 @@ __global__ void kVertexStar(const int4* __restrict__ he, MeshDims md, int* __res
 // the cell face of their contour segment, that face has no other crossing
 // edge, so exactly these two halfedges hold the vertex pair (the pairs the
 // twin repair changes have four) and they are twins: the faces form one
-// closed fan.
+// closed fan.  After the splitter the same holds for every DMC vertex it
+// did not touch (no corner of a copied face): its faces, and the twins of
+// their halfedges at it, are those the vertex pass saw.
 __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restrict__ vertexHE,
                          const int* __restrict__ deg, bool vertexPassDegrees, int* __restrict__ fans,
                          uint8_t* __restrict__ slow, uint8_t* __restrict__ vflags, unsigned long long* slowCount,
-                         const unsigned long long* gate) {
+                         const unsigned long long* gate, const int* __restrict__ dmcDeg,
+                         const uint8_t* __restrict__ touched, int dmcV) {
     if (gate && *gate != 0) return;  // a speculative pass whose mesh the splitter will change
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     bool isSlow = false;
@@ -499,7 +502,7 @@ __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restri
             fans[v] = 0;
             slow[v] = 0;
             vflags[v] &= (uint8_t)~MDMC_VERTEX_MULTIPLE_FANS;
-        } else if (vertexPassDegrees && ds > 0) {
+        } else if ((vertexPassDegrees && ds > 0) || (dmcDeg && v < dmcV && !touched[v] && dmcDeg[v] > 0)) {
             fans[v] = 1;
             slow[v] = 0;
             vflags[v] &= (uint8_t)~MDMC_VERTEX_MULTIPLE_FANS;
@@ -634,11 +637,12 @@ void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cuda
 
 void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, bool vertexPassDegrees,
                       uint8_t* slow, uint8_t* isKey, uint8_t keyMark, int* fans, uint8_t* vflags, DevCounters* ctr,
-                      uint32_t* status, const unsigned long long* gate, cudaStream_t s) {
+                      uint32_t* status, const unsigned long long* gate, const int* dmcDeg, const uint8_t* touched,
+                      int dmcV, cudaStream_t s) {
     if (md.V > 0) {
         countLaunch();
         kFanFast<<<(md.V + 255) / 256, 256, 0, s>>>(he, md, vertexHE, deg, vertexPassDegrees, fans, slow, vflags,
-                                                    &ctr->slowFans, gate);
+                                                    &ctr->slowFans, gate, dmcDeg, touched, dmcV);
     }
     if (md.H > 0) {
         countLaunch();

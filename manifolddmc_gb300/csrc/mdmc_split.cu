@@ -91,6 +91,7 @@ __global__ void kCopyOut(const int* __restrict__ nmFaces, int n, const int4* __r
         }
         vs[i] = v;
         hs[i] = h;
+        if (w.touched && v < w.dmcV) w.touched[v] = 1;
         atomicMin(&w.vO2C[v], c);
         w.he[c] = e;
         w.hO2C[h] = c;
@@ -374,17 +375,16 @@ __device__ int closure(const int* num, const int* slots, int v, int out[12], uin
     return np;
 }
 
-// mergeVertices (:936-990); the survivor's normal receives the averaged
-// position, as in the reference (:989)
-__global__ void kMergeVertices(SplitWork w, uint32_t* status) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= w.nv) return;
+// mergeVertices (:936-990) for vertex v; the survivor's normal receives the
+// averaged position, as in the reference (:989).  Returns the survivor (v
+// itself, or the smaller partner that replaces it), or v with np <= 1.
+__device__ __forceinline__ int mergeVertex(const SplitWork& w, int v, uint32_t* status) {
     int part[12];
     const int np = closure(w.vNum, w.vSlots, v, part, status);
-    if (np <= 1) return;
+    if (np <= 1) return v;
     if (np > 12) {
         atomicOr(status, kStatusPartnerOverflow);
-        return;
+        return v;
     }
     int smallest = v;
     F3 p = f3(w.pos[3 * (int64_t)v], w.pos[3 * (int64_t)v + 1], w.pos[3 * (int64_t)v + 2]);
@@ -399,11 +399,19 @@ __global__ void kMergeVertices(SplitWork w, uint32_t* status) {
     }
     if (obsolete) {
         atomicOr(&w.vfl[v], kRemove);
-        return;
+        return smallest;
     }
     p = p / (float)np;
     w.pos[3 * (int64_t)smallest] = p.x; w.pos[3 * (int64_t)smallest + 1] = p.y; w.pos[3 * (int64_t)smallest + 2] = p.z;
     w.nrm[3 * (int64_t)smallest] = p.x; w.nrm[3 * (int64_t)smallest + 1] = p.y; w.nrm[3 * (int64_t)smallest + 2] = p.z;
+    return smallest;
+}
+
+// every copy vertex, grid-stride; only when a corner copy has merge partners
+// (flags[0]) or without subdivision (else kMergeInner does the work)
+__global__ void kMergeVertices(SplitWork w, uint32_t* status) {
+    if (w.cornerLimit < w.nv && w.flags[0] == 0) return;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < w.nv; v += gridDim.x * blockDim.x) mergeVertex(w, v, status);
 }
 
 // updateHalfedgeVertexIDs (:992-1019), grid-stride over the halfedges; only
@@ -422,19 +430,19 @@ __global__ void kUpdateOrigins(SplitWork w, uint32_t* status) {
     }
 }
 
-// The same for the subdivision's inner vertices, one thread per vertex: inner
-// vertex i of face k is the origin of exactly three halfedges (its inner-ring
-// halfedge, and the second and third halfedge of two boundary quads; see
-// kSubdivide), so a vertex with merge partners rewrites those three.
-__global__ void kUpdateInnerOrigins(SplitWork w, int n, uint32_t* status) {
+// Subdivided copies whose merge partners are all inner vertices (no corner
+// has partners): one thread per inner vertex merges it (mergeVertex) and
+// points its halfedges at the survivor (updateHalfedgeVertexIDs).  Inner
+// vertex i of face k is the origin of exactly three halfedges: its
+// inner-ring halfedge and the second and third halfedge of two boundary
+// quads (kSubdivide's numbering).
+__global__ void kMergeInner(SplitWork w, int n, uint32_t* status) {
+    if (w.flags[0] != 0) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= 4 * n) return;
     const int v = 4 * n + j;
-    int part[12];
-    const int np = closure(w.vNum, w.vSlots, v, part, status);
-    if (np <= 1) return;
-    int sm = v;
-    for (int i = 0; i < np - 1; ++i) sm = min(sm, part[i]);
+    const int sm = mergeVertex(w, v, status);
+    if (sm == v) return;
     const int k = j >> 2, i = j & 3;
     const int hb = 4 * n + 16 * k;
     const int hs[3] = {hb + i, hb + 4 + 3 * i + 1, hb + 4 + 3 * ((i + 1) & 3) + 2};
@@ -799,12 +807,13 @@ void launchSplitCollapse(const SplitWork& w, uint32_t* status, cudaStream_t s) {
     kSortPartners<<<nb(w.nh, 256), 256, 0, s>>>(w.hNum, w.hSlots, w.nh);
 }
 void launchSplitMerge(const SplitWork& w, uint32_t* status, cudaStream_t s) {
-    countLaunch(2);
-    kMergeVertices<<<nb(w.nv, 128), 128, 0, s>>>(w, status);
     if (w.cornerLimit < w.nv) {  // subdivided: nv = 8n, corners below 4n
         countLaunch();
-        kUpdateInnerOrigins<<<nb(w.cornerLimit, 128), 128, 0, s>>>(w, w.cornerLimit / 4, status);
+        kMergeInner<<<nb(w.cornerLimit, 128), 128, 0, s>>>(w, w.cornerLimit / 4, status);
     }
+    // the general passes (they return at once after kMergeInner did the work)
+    countLaunch(2);
+    kMergeVertices<<<std::min(nb(w.nv, 128), 152 * 16), 128, 0, s>>>(w, status);
     kUpdateOrigins<<<std::min(nb(w.nh, 128), 152 * 16), 128, 0, s>>>(w, status);
 }
 void launchSplitMergeHalfedges(const SplitWork& w, uint32_t* status, cudaStream_t s) {
