@@ -116,7 +116,7 @@ struct mdmc_context {
     int32_t* hostInts = nullptr;          // pinned scratch for small reads
     int32_t* hostIntsDev = nullptr;       // hostInts as kernels address it (nullptr: not mapped)
     // splitter
-    DevBuf nmFlags, nmOffsets, nmFaces;
+    DevBuf nmOffsets, nmFaces;
     DevBuf wPos, wNrm, wVfl, wHfl, wFfl, wVC2O, wHC2O, wFC2O, wOrigV, wOrigH, wHe, wFirst, wAttr, wVNum, wVSlots,
         wHNum, wHSlots;
     DevBuf vO2C, hO2C, fO2C, splitFlags;
@@ -618,12 +618,14 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         c->fastFans = c->dmcDegree.bytes >= sizeof(int) * (size_t)c->dmcV;
     }
     while (true) {
-        // countNonManifoldFaces + the list of non-manifold faces
-        MDMC_CHECK(c, c->nmFlags.ensure(sizeof(int) * (size_t)(c->F + 1)));
+        // countNonManifoldFaces + the list of non-manifold faces (one scan)
         MDMC_CHECK(c, c->nmOffsets.ensure(sizeof(int) * (size_t)(c->F + 1)));
-        launchFlagNMFaces(c->faceAttr.as<uint16_t>(), (int)c->F, c->nmFlags.as<int>(), s);
-        mdmc_status st = scan<int>(c, c->nmFlags.as<int>(), c->nmOffsets.as<int>(), c->F, s);
-        if (st != MDMC_OK) return st;
+        MDMC_CHECK(c, c->nmFaces.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->F, 1)));
+        MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(c->F)));
+        if (!scanNMFaces(c->faceAttr.as<uint16_t>(), (int)c->F, c->nmOffsets.as<int>(), c->nmFaces.as<int>(),
+                         c->scanScratch.as<int>(), s))
+            return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
+        mdmc_status st = MDMC_OK;
         MDMC_CHECK(c, cudaGetLastError());
         if ((st = readInts(c, c->nmOffsets.as<int>() + c->F, 1, s)) != MDMC_OK) return st;
         const int n = (int)c->hostInts[0];
@@ -631,8 +633,6 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         if (n == 0) break;
         if ((int64_t)c->H + 20 * (int64_t)n >= (int64_t)0x7FFFFFFF)
             return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "splitting would exceed 2^31 halfedges");
-        MDMC_CHECK(c, c->nmFaces.ensure(sizeof(int) * (size_t)n));
-        launchCompactNMFaces(c->nmFlags.as<int>(), c->nmOffsets.as<int>(), (int)c->F, c->nmFaces.as<int>(), s);
 
         const bool doSub = step >= MDMC_STEP_SUBDIVIDE_QUADS;
         const int nv = 4 * n + (doSub ? 4 * n : 0);
@@ -690,12 +690,11 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         MDMC_CHECK(c, c->appV.ensure(sizeof(int) * (size_t)(nv + 1)));
         MDMC_CHECK(c, c->appH.ensure(sizeof(int) * (size_t)(nh + 1)));
         MDMC_CHECK(c, c->appF.ensure(sizeof(int) * (size_t)(nf + 1)));
-        launchSplitFlagAppends(nv, w.vfl, w.vC2O, c->appV.as<int>(), s);
-        launchSplitFlagAppends(nh, w.hfl, w.hC2O, c->appH.as<int>(), s);
-        launchSplitFlagAppends(nf, w.ffl, w.fC2O, c->appF.as<int>(), s);
-        if ((st = scan<int>(c, c->appV.as<int>(), c->appV.as<int>(), nv, s)) != MDMC_OK) return st;
-        if ((st = scan<int>(c, c->appH.as<int>(), c->appH.as<int>(), nh, s)) != MDMC_OK) return st;
-        if ((st = scan<int>(c, c->appF.as<int>(), c->appF.as<int>(), nf, s)) != MDMC_OK) return st;
+        MDMC_CHECK(c, c->scanScratch.ensure(sizeof(int4) * (size_t)scanScratchElems(nh)));
+        if (!scanAppends(w.vfl, w.vC2O, nv, c->appV.as<int>(), c->scanScratch.as<int>(), s) ||
+            !scanAppends(w.hfl, w.hC2O, nh, c->appH.as<int>(), c->scanScratch.as<int>(), s, (int)c->H) ||
+            !scanAppends(w.ffl, w.fC2O, nf, c->appF.as<int>(), c->scanScratch.as<int>(), s))
+            return fail(c, MDMC_ERROR_INVALID_ARGUMENT, "prefix sum input too large");
         // a small iteration after a full refresh gets the local refresh: the
         // sizes of its old and kept edge sets come back with the append counts
         const bool local = c->rowsValid && doSub && (int64_t)nh * 16 <= c->H;

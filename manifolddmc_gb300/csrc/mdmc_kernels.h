@@ -268,8 +268,15 @@ void launchRenderBuffers(const float* pos, const float* nrm, const uint8_t* vfla
 // face coloring 24 -> 5 colors in place (orig: one byte per face of scratch)
 void launchColorFaces(const int4* he, const int* faceFirst, uint16_t* attr, uint8_t* orig, int numFaces, int numHalfedges,
                       cudaStream_t s);
-void launchFlagNMFaces(const uint16_t* attr, int numFaces, int* flags, cudaStream_t s);
-void launchCompactNMFaces(const int* flags, const int* offsets, int numFaces, int* nmFaces, cudaStream_t s);
+// exclusive prefix of the non-manifold face flags into offsets (numFaces + 1
+// entries) and the flagged face ids into nmFaces (capacity numFaces); false
+// when numFaces is beyond the scan's size
+bool scanNMFaces(const uint16_t* attr, int numFaces, int* offsets, int* nmFaces, int* scratch, cudaStream_t s);
+// exclusive prefix of "kept and without an original" over count copy
+// elements; with assignBase >= 0 each such element's c2o entry becomes
+// assignBase + its number (the halfedges' new ids, before the copy-back)
+bool scanAppends(const uint32_t* fl, int* c2o, int count, int* offsets, int* scratch, cudaStream_t s,
+                 int assignBase = -1);
 void launchFillInt(int* p, int64_t n, int v, cudaStream_t s);
 void launchSplitCopy(const int* nmFaces, int n, const int4* he, const int* faceFirst, const uint16_t* faceAttr,
                      const float* pos, const float* nrm, const SplitWork& w, uint32_t* status, cudaStream_t s);
@@ -280,7 +287,6 @@ void launchSplitCollapse(const SplitWork& w, uint32_t* status, cudaStream_t s);
 void launchSplitMerge(const SplitWork& w, uint32_t* status, cudaStream_t s);
 void launchSplitMergeHalfedges(const SplitWork& w, uint32_t* status, cudaStream_t s);
 void launchSplitMove(const GridDesc& g, float iso, const SplitWork& w, cudaStream_t s);
-void launchSplitFlagAppends(int count, const uint32_t* fl, const int* c2o, int* out, cudaStream_t s);
 void launchSplitCopyBack(const SplitWork& w, const int* appV, const int* appH, const int* appF, int V2, int H2, int F2,
                          float* pos, float* nrm, int4* he, int* faceFirst, uint16_t* faceAttr, uint32_t* status,
                          cudaStream_t s);

@@ -11,6 +11,7 @@
 
 #include "mdmc_device.cuh"
 #include "mdmc_kernels.h"
+#include "mdmc_scan.cuh"
 
 namespace mdmc {
 
@@ -18,26 +19,50 @@ constexpr uint32_t kRemove = 16;      // Flags::setRemoveFlag
 constexpr uint32_t kNonManifold = 1;  // Flags::setNonManifoldFlag
 constexpr int kNone = -1;
 
-__global__ void kFlagNMFaces(const uint16_t* __restrict__ attr, int numFaces, int* __restrict__ flags) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f < numFaces) flags[f] = (attr[f] & MDMC_FACE_NON_MANIFOLD) ? 1 : 0;
-}
-__global__ void kCompactNMFaces(const int* __restrict__ flags, const int* __restrict__ offsets, int numFaces,
-                                int* __restrict__ nmFaces) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f < numFaces && flags[f]) nmFaces[offsets[f]] = f;
-}
-void launchFlagNMFaces(const uint16_t* attr, int numFaces, int* flags, cudaStream_t s) {
-    if (numFaces > 0) {
-        countLaunch();
-        kFlagNMFaces<<<(numFaces + 255) / 256, 256, 0, s>>>(attr, numFaces, flags);
+// countNonManifoldFaces + the list of those faces in one prefix sum: the scan
+// reads each face's flag from its attributes, and its apply pass writes every
+// flagged face id to its place (no flag array, no compaction pass)
+struct FaceNMRead {
+    const uint16_t* __restrict__ attr;
+    __device__ __forceinline__ int operator[](int64_t f) const {
+        return (attr[f] & MDMC_FACE_NON_MANIFOLD) ? 1 : 0;
     }
-}
-void launchCompactNMFaces(const int* flags, const int* offsets, int numFaces, int* nmFaces, cudaStream_t s) {
-    if (numFaces > 0) {
-        countLaunch();
-        kCompactNMFaces<<<(numFaces + 255) / 256, 256, 0, s>>>(flags, offsets, numFaces, nmFaces);
+};
+struct CompactPost {
+    static constexpr bool kStaged = false;
+    int* out;
+    __device__ __forceinline__ void operator()(int64_t i, int at, int v) const {
+        if (v) out[at] = (int)i;
     }
+    __device__ __forceinline__ void total(int64_t, int) const {}
+};
+bool scanNMFaces(const uint16_t* attr, int numFaces, int* offsets, int* nmFaces, int* scratch, cudaStream_t s) {
+    return exclusiveScanOf<int>(FaceNMRead{attr}, offsets, numFaces, scratch, s, CompactPost{nmFaces});
+}
+
+// copy-back selection (kept elements without an original are appended), read
+// by the scan that numbers them
+struct AppendRead {
+    const uint32_t* __restrict__ fl;
+    const int* __restrict__ c2o;
+    __device__ __forceinline__ int operator[](int64_t i) const {
+        return (!(fl[i] & 16u) && c2o[i] == -1) ? 1 : 0;  // kRemove, kNone
+    }
+};
+// (assignHalfedgeIDs: an appended element's mesh id, base + its number,
+// written by the apply pass into its copy -> original map)
+struct AssignPost {
+    static constexpr bool kStaged = false;
+    int* c2o;
+    int base;
+    __device__ __forceinline__ void operator()(int64_t i, int at, int v) const {
+        if (v && c2o) c2o[i] = base + at;
+    }
+    __device__ __forceinline__ void total(int64_t, int) const {}
+};
+bool scanAppends(const uint32_t* fl, int* c2o, int count, int* offsets, int* scratch, cudaStream_t s, int assignBase) {
+    return exclusiveScanOf<int>(AppendRead{fl, c2o}, offsets, count, scratch, s,
+                                AssignPost{assignBase >= 0 ? c2o : nullptr, assignBase});
 }
 
 __global__ void kFillInt(int* p, int64_t n, int v) {
@@ -477,12 +502,22 @@ __global__ void kMergeHalfedges(SplitWork w, uint32_t* status) {
     w.he[valid].w = t;
 }
 
+// A corner copy other than the smallest copy of its original vertex: after
+// kUpdateRefs no halfedge names it, it holds the same data as the smallest
+// copy and would move and be written back identically, so the moving and
+// copy-back passes leave it to that copy.
+__device__ __forceinline__ bool spareCorner(const SplitWork& w, int v) {
+    if (v >= w.cornerLimit) return false;
+    const int o = w.vC2O[v];
+    return inb(o, w.V) && w.vO2C[o] != v;
+}
+
 // performMoveVerticesToSurface (:1130-1160)
 template <class View>
 __global__ void kMoveVertices(View g, float iso, SplitWork w) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= w.nv) return;
-    if (w.vfl[v] & kRemove) return;
+    if ((w.vfl[v] & kRemove) || spareCorner(w, v)) return;
     const F3 p = f3(w.pos[3 * (int64_t)v], w.pos[3 * (int64_t)v + 1], w.pos[3 * (int64_t)v + 2]);
     int idx[3];
     g.cellOf(p, idx);
@@ -499,20 +534,13 @@ __global__ void kMoveVertices(View g, float iso, SplitWork w) {
     w.pos[3 * (int64_t)v] = q.x; w.pos[3 * (int64_t)v + 1] = q.y; w.pos[3 * (int64_t)v + 2] = q.z;
 }
 
-// copy-back selection: elements kept and without an original get appended
-__global__ void kFlagAppends(int count, const uint32_t* __restrict__ fl, const int* __restrict__ c2o,
-                             int* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count) out[i] = (!(fl[i] & kRemove) && c2o[i] == kNone) ? 1 : 0;
-}
-
 // copyVerticesBack / copyHalfedgesBack / copyFacesBack (:1176-1260); V2, H2
 // and F2 are the mesh sizes after the appends
 __global__ void kCopyBackVertices(SplitWork w, const int* __restrict__ app, int V2, float* pos, float* nrm,
                                   uint32_t* status) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= w.nv) return;
-    if (w.vfl[v] & kRemove) return;
+    if ((w.vfl[v] & kRemove) || spareCorner(w, v)) return;
     int o = w.vC2O[v];
     if (o == kNone) {
         o = w.V + app[v];
@@ -532,12 +560,6 @@ __global__ void kCopyBackVertices(SplitWork w, const int* __restrict__ app, int 
         pos[3 * (int64_t)o + a] = w.pos[3 * (int64_t)v + a];
         nrm[3 * (int64_t)o + a] = w.nrm[3 * (int64_t)v + a];
     }
-}
-__global__ void kAssignHalfedges(SplitWork w, const int* __restrict__ app) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= w.nh) return;
-    if (w.hfl[t] & kRemove) return;
-    if (w.hC2O[t] == kNone) w.hC2O[t] = w.H + app[t];
 }
 __global__ void kCopyBackFaces(SplitWork w, const int* __restrict__ app, int H2, int F2, int* faceFirst,
                                uint16_t* faceAttr, uint32_t* status) {
@@ -794,7 +816,7 @@ void launchSplitCopy(const int* nmFaces, int n, const int4* he, const int* faceF
 void launchSplitMarkNM(const int4* nmList, const DevCounters* ctr, const SplitWork& w,
                        uint32_t* status, cudaStream_t s) {
     countLaunch();
-    kMarkNM<<<152, 256, 0, s>>>(nmList, ctr, w, status);
+    kMarkNM<<<152 * 8, 256, 0, s>>>(nmList, ctr, w, status);
 }
 void launchSplitSubdivide(int n, const SplitWork& w, uint32_t* status, cudaStream_t s) {
     countLaunch();
@@ -825,17 +847,11 @@ void launchSplitMove(const GridDesc& g, float iso, const SplitWork& w, cudaStrea
     if (g.refined) kMoveVertices<RefinedView><<<nb(w.nv, 128), 128, 0, s>>>(g.ref, iso, w);
     else kMoveVertices<PlainView><<<nb(w.nv, 128), 128, 0, s>>>(g.plain, iso, w);
 }
-void launchSplitFlagAppends(int count, const uint32_t* fl, const int* c2o, int* out, cudaStream_t s) {
-    if (count <= 0) return;
-    countLaunch();
-    kFlagAppends<<<nb(count, 256), 256, 0, s>>>(count, fl, c2o, out);
-}
 void launchSplitCopyBack(const SplitWork& w, const int* appV, const int* appH, const int* appF, int V2, int H2, int F2,
                          float* pos, float* nrm, int4* he, int* faceFirst, uint16_t* faceAttr, uint32_t* status,
                          cudaStream_t s) {
-    countLaunch(4);
+    countLaunch(3);
     kCopyBackVertices<<<nb(w.nv, 256), 256, 0, s>>>(w, appV, V2, pos, nrm, status);
-    kAssignHalfedges<<<nb(w.nh, 256), 256, 0, s>>>(w, appH);
     kCopyBackFaces<<<nb(w.nf, 256), 256, 0, s>>>(w, appF, H2, F2, faceFirst, faceAttr, status);
     kCopyBackHalfedges<<<nb(w.nh, 256), 256, 0, s>>>(w, V2, H2, F2, he, status);
 }
