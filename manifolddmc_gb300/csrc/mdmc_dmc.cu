@@ -930,11 +930,13 @@ void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, Act
 // resident blocks per SM the register allocation aims at: 5 (96 registers)
 // for the per-sample stencils (0.19 ms instead of 0.22 ms at 114 registers on
 // the 512^3-cell blobs), 6 (80 registers, no spills) for the separable one
-// (0.116 ms instead of 0.121 ms at 5)
+// (0.116 ms instead of 0.121 ms at 5); the pooled pass below: 7 (72
+// registers, no spills; 256^3 noise 2.15 -> 2.0 ms against 5)
 template <class Stencil>
 struct VerticesBlocks {
-    static constexpr int value = 7;  // 72 registers, no spills (256^3 noise: pooled pass 2.15 -> 2.0 ms)
+    static constexpr int value = 5;
 };
+constexpr int kPooledVerticesBlocks = 7;
 template <>
 struct VerticesBlocks<SepStencil> {
     static constexpr int value = 6;
@@ -1038,7 +1040,7 @@ __global__ void __launch_bounds__(128, VerticesBlocks<Stencil>::value) kVertices
 // the shared-memory round trip only costs (106 -> 127 us on the 512^3-cell
 // blobs), so they keep kVertices, one thread per cell.
 template <class View, class Stencil>
-__global__ void __launch_bounds__(128, VerticesBlocks<Stencil>::value) kVerticesPooled(View g, float iso, int surfaceIteration,
+__global__ void __launch_bounds__(128, kPooledVerticesBlocks) kVerticesPooled(View g, float iso, int surfaceIteration,
                                                  const ActiveCell* __restrict__ act, int numActive,
                                                  int numVertices, float* __restrict__ pos,
                                                  float* __restrict__ nrm, int* __restrict__ degree,
