@@ -159,9 +159,11 @@ def algorithmic_bytes(kernel, s):
         return 8 * words + 16 * A + 8 * A + 16 * A
     if kernel == "vertices":  # records read, positions + normals written
         return 16 * A + 24 * V
-    if kernel == "quads":  # offsets -> records + quad owners; records + owners read, halfedges (with twins),
-        # faces, attributes, valences written
-        return (8 * A + 8 * A + 4 * Q) + (4 * Q + 16 * A + 64 * Q + 4 * Q + 2 * Q + 4 * Q)
+    if kernel == "quads":  # read: each active cell's record (16 B) and the mask word and first-cell offset
+        # that find it (8 B), each quad's owner (4 B); written: halfedges with twins (64 B), valences (4 B),
+        # face first halfedge (4 B), attributes (2 B), output quad (16 B) per quad, and each vertex's
+        # smallest outgoing halfedge (4 B)
+        return (16 + 8) * A + 4 * Q + (64 + 4 + 4 + 2 + 16) * Q + 4 * V
     raise KeyError(kernel)
 
 
