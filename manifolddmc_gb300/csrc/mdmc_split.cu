@@ -503,9 +503,10 @@ __global__ void kMergeHalfedges(SplitWork w, uint32_t* status) {
 }
 
 // A corner copy other than the smallest copy of its original vertex: after
-// kUpdateRefs no halfedge names it, it holds the same data as the smallest
-// copy and would move and be written back identically, so the moving and
-// copy-back passes leave it to that copy.
+// kUpdateRefs no halfedge names it, and it holds the same data as the
+// smallest copy (both move identically), so the copy-back leaves it to that
+// copy.  (The moving pass moves it anyway: the check costs it more than the
+// skipped moves save.)
 __device__ __forceinline__ bool spareCorner(const SplitWork& w, int v) {
     if (v >= w.cornerLimit) return false;
     const int o = w.vC2O[v];
@@ -517,7 +518,7 @@ template <class View>
 __global__ void kMoveVertices(View g, float iso, SplitWork w) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= w.nv) return;
-    if ((w.vfl[v] & kRemove) || spareCorner(w, v)) return;
+    if (w.vfl[v] & kRemove) return;
     const F3 p = f3(w.pos[3 * (int64_t)v], w.pos[3 * (int64_t)v + 1], w.pos[3 * (int64_t)v + 2]);
     int idx[3];
     g.cellOf(p, idx);
