@@ -119,7 +119,7 @@ struct mdmc_context {
     DevBuf nmOffsets, nmFaces;
     DevBuf wPos, wNrm, wVfl, wHfl, wFfl, wVC2O, wHC2O, wFC2O, wOrigV, wOrigH, wHe, wFirst, wAttr, wVNum, wVSlots,
         wHNum, wHSlots;
-    DevBuf vO2C, hO2C, fO2C, splitFlags;
+    DevBuf vO2C, hO2C, fO2C, splitFlags, wHTwin;
     size_t vO2CCount = 0, hO2CCount = 0, fO2CCount = 0;
     DevBuf appV, appH, appF;
     // fan detection
@@ -328,6 +328,7 @@ SplitWork splitWork(mdmc_context* c, int nv, int nh, int nf) {
     w.cornerLimit = nv;
     w.flags = c->splitFlags.as<int>();
     w.touched = c->fastFans ? c->splitTouched.as<uint8_t>() : nullptr;
+    w.hTwinBest = c->wHTwin.as<unsigned long long>();
     w.origH = c->wOrigH.as<int>();
     w.he = c->wHe.as<int4>();
     w.first = c->wFirst.as<int>();
@@ -655,6 +656,7 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         MDMC_CHECK(c, c->wVSlots.ensure(sizeof(int) * 4 * (size_t)nv));
         MDMC_CHECK(c, c->wHNum.ensure(sizeof(int) * (size_t)nh));
         MDMC_CHECK(c, c->wHSlots.ensure(sizeof(int) * 4 * (size_t)nh));
+        MDMC_CHECK(c, c->wHTwin.ensure(sizeof(unsigned long long) * (size_t)nh));
         if ((st = ensureMaps(c, s)) != MDMC_OK) return st;
         MDMC_CHECK(c, cudaMemsetAsync(c->wVfl.p, 0, sizeof(uint32_t) * (size_t)nv, s));
         MDMC_CHECK(c, cudaMemsetAsync(c->wOrigV.p, 0xFF, sizeof(int) * (size_t)nv, s));

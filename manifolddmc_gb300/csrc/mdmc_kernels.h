@@ -128,6 +128,8 @@ struct SplitWork {
     // optional: marks the DMC vertices (ids below dmcV) that are corners of
     // a copied face, i.e. whose fans the splitter may change
     uint8_t* touched;
+    // per copy halfedge: the last merge pair's twin offer (kMergeHalfedges)
+    unsigned long long* hTwinBest;
 };
 
 void launchRefine(const float* in, int3 din, float* out, int3 dout, int r, int pad, cudaStream_t s);

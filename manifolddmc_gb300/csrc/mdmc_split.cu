@@ -479,8 +479,16 @@ __global__ void kMergeInner(SplitWork w, int n, uint32_t* status) {
     }
 }
 
-// mergeHalfedges (:1021-1067): reads only removed partners' twins, which no
-// thread writes, so one pass is race-free
+// mergeHalfedges (:1021-1067) as the oracle states it: every decision reads
+// the twins as they were before the pass, and the pairs (t, valid) are then
+// applied in increasing t, a later pair overwriting an earlier one.  Here
+// the decisions write nothing into the halfedges: each pair offers
+// ((t + 1) << 32 | value) to both of its halfedges by a 64-bit atomicMax,
+// so that every halfedge keeps the value of its last pair, and
+// kApplyMergedTwins writes those values afterwards.  (Writing the twins in
+// the deciding pass raced with decisions that read a kept partner's twin:
+// on one grid of 96 a batch run once gave 1243 non-manifold vertices instead
+// of 1242.)
 __global__ void kMergeHalfedges(SplitWork w, uint32_t* status) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= w.nh) return;
@@ -498,8 +506,16 @@ __global__ void kMergeHalfedges(SplitWork w, uint32_t* status) {
         }
     }
     if (valid == -1 || valid < t) return;
-    w.he[t].w = valid;
-    w.he[valid].w = t;
+    const unsigned long long tag = (unsigned long long)(t + 1) << 32;
+    atomicMax(w.hTwinBest + t, tag | (uint32_t)valid);
+    atomicMax(w.hTwinBest + valid, tag | (uint32_t)t);
+}
+
+__global__ void kApplyMergedTwins(SplitWork w) {
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < w.nh; x += gridDim.x * blockDim.x) {
+        const unsigned long long b = w.hTwinBest[x];
+        if (b) reinterpret_cast<int*>(w.he)[4 * (int64_t)x + 3] = (int)(uint32_t)b;
+    }
 }
 
 // A corner copy other than the smallest copy of its original vertex: after
@@ -840,8 +856,10 @@ void launchSplitMerge(const SplitWork& w, uint32_t* status, cudaStream_t s) {
     kUpdateOrigins<<<std::min(nb(w.nh, 128), 152 * 16), 128, 0, s>>>(w, status);
 }
 void launchSplitMergeHalfedges(const SplitWork& w, uint32_t* status, cudaStream_t s) {
-    countLaunch();
+    countLaunch(2);
+    cudaMemsetAsync(w.hTwinBest, 0, sizeof(unsigned long long) * (size_t)w.nh, s);
     kMergeHalfedges<<<nb(w.nh, 128), 128, 0, s>>>(w, status);
+    kApplyMergedTwins<<<std::min(nb(w.nh, 256), 152 * 16), 256, 0, s>>>(w);
 }
 void launchSplitMove(const GridDesc& g, float iso, const SplitWork& w, cudaStream_t s) {
     countLaunch();

@@ -36,3 +36,25 @@ def test_batch_matches_single_runs(streams):
     stats2 = batch.run(grids[:4], isos[:4])
     for i in range(4):
         assert int(stats2[i].num_dmc_vertices) == int(stats[i].num_dmc_vertices)
+
+
+def test_full_batch_workload_matches_single_runs():
+    """The bench's batch workload (96 grids, dims uniform in [24, 192], half
+    Gaussian blobs and half uniform noise, iso in [0.3, 0.7]): every grid's
+    mesh from one batch call equals a single mdmc_run's, bit for bit."""
+    items = batch_grids()
+    assert len(items) == 96
+    grids = [mdmc.UniformGrid(vol) for vol, _ in items]
+    isos = [iso for _, iso in items]
+    batch = mdmc.BatchedDualMarchingCubes(streams=8)
+    stats = batch.run(grids, isos)
+    single = mdmc.DualMarchingCubes()
+    splits = 0
+    for i, (g, iso) in enumerate(zip(grids, isos)):
+        single.run(iso, g)
+        assert int(stats[i].num_dmc_quads) == single.get_num_quads()
+        assert int(stats[i].num_non_manifold_vertices) == single.get_num_non_manifold_vertices()
+        assert int(stats[i].split_iterations) == int(single.stats.split_iterations)
+        splits += int(stats[i].split_iterations) > 0
+        _same(batch.get_halfedge_mesh(i), single.get_halfedge_mesh())
+    assert splits > 0  # the noise grids go through the splitter
