@@ -415,6 +415,13 @@ mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaSt
     MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)std::max<int64_t>(c->F, 1)));
     const MeshDims mdF{(int)c->V, (int)c->F, (int)c->H};
     const bool detect = c->opt.detect_non_manifold_vertices != 0;
+    // a changed mesh: output quads, face statistics and vertex stars in one
+    // pass over the faces, before the detection that reads the stars (so the
+    // stage times count this pass with the detection)
+    if (!starsDone)
+        launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), mdF, c->heValence.as<uint8_t>(),
+                     c->faceNMValid ? c->faceNM.as<uint8_t>() : nullptr, c->quads.as<int4>(), c->vertexHE.as<int>(),
+                     detect ? c->degree.as<int>() : nullptr, ctr, status, s);
     if (detect) {
         // fan keys are marked with this pass's number (1..255); the array is
         // cleared only when it is new or the numbers wrap around
@@ -429,7 +436,6 @@ mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaSt
         MDMC_CHECK(c, c->slowFan.ensure((size_t)std::max<int64_t>(c->V, 1)));
         // (the first pass of a run finds the count zeroed with the counters)
         if (!starsDone) MDMC_CHECK(c, cudaMemsetAsync(&ctr->slowFans, 0, sizeof(unsigned long long), s));
-        if (!starsDone) launchVertexStar(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), s);
         launchDetectFans(c->he.as<int4>(), mdF, c->vertexHE.as<int>(), c->degree.as<int>(), starsDone,
                          c->slowFan.as<uint8_t>(), c->isKey.as<uint8_t>(), c->keyMark, c->fans.as<int>(),
                          c->vflags.as<uint8_t>(), ctr, status, gate,
@@ -437,13 +443,8 @@ mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaSt
                          (int)c->dmcV, s);
     }
     markStage(c, 4, detect, s);
-    if (!starsDone)
-        launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), mdF, c->heValence.as<uint8_t>(),
-                     c->faceNMValid ? c->faceNM.as<uint8_t>() : nullptr, c->quads.as<int4>(),
-                     c->vertexHE.as<int>(), detect, ctr, status, s);
-    else if (!detect)
-        launchVertexHalfedgeFix(c->vertexHE.as<int>(), (int)c->V, s);
-    markStage(c, 5, !starsDone || !detect, s);
+    if (!detect) launchVertexHalfedgeFix(c->vertexHE.as<int>(), (int)c->V, s);  // "none" -> -1
+    markStage(c, 5, !detect, s);
     MDMC_CHECK(c, cudaGetLastError());
     return MDMC_OK;
 }

@@ -227,7 +227,6 @@ void launchEdgeBuckets(int4* he, MeshDims md, const int* rowStart, const int* ra
 void launchResetFaceFlags(uint16_t* attr, int numFaces, cudaStream_t s);
 void launchReconnect(const GridDesc& g, float iso, const int4* nmList, const DevCounters* ctr,
                      int4* he, const float* pos, MeshDims md, uint32_t* status, cudaStream_t s);
-void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cudaStream_t s);
 // vertexPassDegrees: deg is the vertex pass's signed degree of the DMC mesh
 // (only the twin repair has run since); otherwise non-negative degrees.
 // isKey[h] == keyMark marks this pass's fan keys (no other entry may hold it)
@@ -239,8 +238,11 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
                       uint8_t* slow, uint8_t* isKey, uint8_t keyMark, int* fans, uint8_t* vflags, DevCounters* ctr,
                       uint32_t* status, const unsigned long long* gate, const int* dmcDeg, const uint8_t* touched,
                       int dmcV, cudaStream_t s);
+// output quads, quads_with_non_manifold_edges and the vertex stars
+// (smallest outgoing halfedge into vertexHE, 0x7F7F7F7F for none; the
+// out-degree into deg when given) from one walk per face
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, const uint8_t* faceNM,
-                  int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s);
+                  int4* quads, int* vertexHE, int* deg, DevCounters* ctr, uint32_t* status, cudaStream_t s);
 
 // valence-pattern simplifications
 void launchValence(const int4* he, MeshDims md, int* val, cudaStream_t s);

@@ -452,19 +452,6 @@ __device__ __forceinline__ int fanWalk(const int4* he, int start, bool cw, int H
     return result;
 }
 
-// The smallest outgoing halfedge (0x7F7F7F7F: none yet) and the number of
-// outgoing halfedges of every vertex.
-__global__ void kVertexStar(const int4* __restrict__ he, MeshDims md, int* __restrict__ vertexHE, int* __restrict__ deg) {
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
-    if (h < md.H) {
-        const int v = he[h].x;
-        if (inb(v, md.V)) {
-            atomicMin(&vertexHE[v], h);
-            if (deg) atomicAdd(&deg[v], 1);
-        }
-    }
-}
-
 // One walk per vertex.  When the walks from the vertex's smallest outgoing
 // halfedge visit exactly all of the vertex's outgoing halfedges through
 // symmetric twin pairs (faces are 4-cycles) -- clockwise back to the start
@@ -624,17 +611,6 @@ __global__ void kFanFlags(const int* __restrict__ fans, const uint8_t* __restric
     blockAddTo(&ctr->nmVertices, nm);
 }
 
-void launchVertexStar(const int4* he, MeshDims md, int* vertexHE, int* deg, cudaStream_t s) {
-    if (md.V <= 0) return;
-    // 0x7F7F7F7F marks "none"; atomicMin lowers it
-    cudaMemsetAsync(vertexHE, 0x7F, sizeof(int) * (size_t)md.V, s);
-    if (deg) cudaMemsetAsync(deg, 0, sizeof(int) * (size_t)md.V, s);
-    if (md.H > 0) {
-        countLaunch();
-        kVertexStar<<<(md.H + 255) / 256, 256, 0, s>>>(he, md, vertexHE, deg);
-    }
-}
-
 void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg, bool vertexPassDegrees,
                       uint8_t* slow, uint8_t* isKey, uint8_t keyMark, int* fans, uint8_t* vflags, DevCounters* ctr,
                       uint32_t* status, const unsigned long long* gate, const int* dmcDeg, const uint8_t* touched,
@@ -665,7 +641,7 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
 // quad pass's size of every halfedge's bucket)
 __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__ faceFirst, MeshDims md,
                             const uint8_t* __restrict__ heValence, const uint8_t* __restrict__ faceNM,
-                            int4* __restrict__ quads, DevCounters* ctr) {
+                            int4* __restrict__ quads, int* vertexHE, int* deg, DevCounters* ctr) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     int cnt = -1;
     if (f < md.F) {
@@ -699,6 +675,15 @@ __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__
             }
         }
         quads[f] = make_int4(q[0], q[1], q[2], q[3]);
+        // the vertex stars (smallest outgoing halfedge, out-degree) from the
+        // same four records: every halfedge lies in exactly one face
+        if (ok && vertexHE)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (inb(q[i], md.V)) {
+                    atomicMin(&vertexHE[q[i]], hs[i]);
+                    if (deg) atomicAdd(&deg[q[i]], 1);
+                }
         if (ok) {
             cnt = 0;
             if (faceNM) cnt = faceNM[f] & kFaceNMCount;
@@ -729,16 +714,16 @@ void launchVertexHalfedgeFix(int* vertexHE, int numVertices, cudaStream_t s) {
 }
 
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, const uint8_t* faceNM,
-                  int4* quads, int* vertexHE, bool vertexHEDone, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
+                  int4* quads, int* vertexHE, int* deg, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
     (void)status;
+    if (md.V > 0) {
+        // 0x7F7F7F7F marks "none"; atomicMin lowers it
+        cudaMemsetAsync(vertexHE, 0x7F, sizeof(int) * (size_t)md.V, s);
+        if (deg) cudaMemsetAsync(deg, 0, sizeof(int) * (size_t)md.V, s);
+    }
     if (md.F > 0) {
         countLaunch();
-        kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, heValence, faceNM, quads, ctr);
-    }
-    if (md.V > 0 && !vertexHEDone) {
-        launchVertexStar(he, md, vertexHE, nullptr, s);
-        countLaunch();
-        kVertexHalfedgeFix<<<(md.V + 255) / 256, 256, 0, s>>>(vertexHE, md.V);
+        kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, heValence, faceNM, quads, vertexHE, deg, ctr);
     }
 }
 

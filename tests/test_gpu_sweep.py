@@ -5,6 +5,8 @@ thin grids (2 samples along an axis), uneven dims, values with ties at the
 iso-value, negative and large-magnitude fields, and every flag combination
 the reference exposes, so that index arithmetic, boundary handling and the
 repair paths meet inputs the hand-written cases do not."""
+import zlib
+
 import numpy as np
 import pytest
 
@@ -67,4 +69,29 @@ def test_sweep_bit_exact(name, kind, dims, seed, iso, refinement, pad, opts):
     spacing = np.array([0.5, 1.25, 0.75], np.float32)
     dmc, m, _ = gpu_run(vol.reshape(-1), dims, origin, spacing, iso, refinement, pad, **opts)
     ref, _ = oracle_for(vol.reshape(-1), dims, origin, spacing, iso, refinement, pad, **opts)
+    assert_parity(dmc, m, ref)
+
+
+# Larger noise grids: several splitter iterations, the local edge-bucket
+# refresh of the later ones, the decider table on many ambiguous cells, and
+# detection after the splitter with and without the vertex pass's fan degrees
+# (a simplification before the splitter renumbers vertices and turns them off).
+NOISE_CASES = [
+    ("noise48_iso045", 48, 0.45, {}),
+    ("noise56_iso055_nodetect", 56, 0.55, {"detect_non_manifold_vertices": 0}),
+    ("noise64_iso05", 64, 0.5, {}),
+    ("noise64_iso03_nosurf", 64, 0.3, {"surface_iteration": 0}),
+    ("noise40_iso05_simplify", 40, 0.5, {"simplify_3333": 1}),
+    ("noise44_iso06_steps", 44, 0.6, {"splitting_step": 5}),
+]
+
+
+@pytest.mark.parametrize("name,n,iso,opts", NOISE_CASES, ids=[c[0] for c in NOISE_CASES])
+def test_noise_repair_bit_exact(name, n, iso, opts):
+    vol = np.random.default_rng(zlib.crc32(name.encode())).random((n, n + 3, n - 2), dtype=np.float32)
+    dims = [n - 2, n + 3, n]
+    origin = np.zeros(3, np.float32)
+    spacing = np.ones(3, np.float32)
+    dmc, m, _ = gpu_run(vol.reshape(-1), dims, origin, spacing, iso, **opts)
+    ref, _ = oracle_for(vol.reshape(-1), dims, origin, spacing, iso, **opts)
     assert_parity(dmc, m, ref)
