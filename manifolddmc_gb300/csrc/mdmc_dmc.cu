@@ -767,12 +767,14 @@ struct CellScatter {
     uint32_t* __restrict__ cellIds;
     int64_t capacity;
     int W, X, Y;
+    FastDiv divW, divRows;  // by W and by Y - 1 (multiplications instead of divisions)
     __device__ __forceinline__ void operator()(int64_t w, int first, int count) const {
         if (!count) return;
         uint32_t m = mask[w];
-        const uint32_t row = (uint32_t)w / (uint32_t)W;  // fewer than 2^32 words
+        const uint32_t row = divW.div((uint32_t)w);  // fewer than 2^32 words
         const int x0 = (int)((uint32_t)w - row * (uint32_t)W) * 32;
-        const int y = row % (Y - 1), z = row / (Y - 1);
+        const uint32_t zq = divRows.div(row);
+        const int y = (int)(row - zq * (uint32_t)(Y - 1)), z = (int)zq;
         const uint32_t base = (uint32_t)(((size_t)z * Y + y) * X + x0);
         int64_t j = first;
         while (m) {
@@ -788,7 +790,8 @@ struct CellScatter {
 bool scanMaskScatter(const uint32_t* mask, int* first, int64_t numWords, int W, int X, int Y, uint32_t* cellIds,
                      int64_t capacity, int* scratch, cudaStream_t s) {
     return exclusiveScanOf<int>(PopcRead{mask}, first, numWords, scratch, s,
-                                CellScatter{mask, cellIds, capacity, W, X, Y});
+                                CellScatter{mask, cellIds, capacity, W, X, Y, FastDiv((uint32_t)W),
+                                            FastDiv((uint32_t)(Y - 1))});
 }
 
 // The apply hook of the scan of the active cells' (vertex, quad) counts:
