@@ -389,8 +389,9 @@ MDMC_API void mdmc_case_tables(uint64_t contour_words[256], uint8_t ambiguous[25
 
 /* Nearest points for the differentiable form's Chamfer loss (no
  * counterpart in the reference).  mdmc_point_index_create copies `count`
- * points (device memory, 3 floats each) into device memory the index owns
- * until mdmc_point_index_destroy.  Synchronous. */
+ * points (device memory, 3 floats each), sorts them along a Morton curve on
+ * the host and keeps them in device memory the index owns until
+ * mdmc_point_index_destroy.  Synchronous. */
 typedef struct mdmc_point_index mdmc_point_index;
 MDMC_API mdmc_status mdmc_point_index_create(mdmc_point_index** index, const float* points, int64_t count,
                                              void* stream);
@@ -398,8 +399,10 @@ MDMC_API void mdmc_point_index_destroy(mdmc_point_index* index);
 /* For each of `count` query points (device, 3 floats each): the index of the
  * nearest indexed point (its position in the array given to create) and,
  * when dist2 is not NULL, the squared distance (dx*dx + dy*dy) + dz*dz in
- * float.  Exact and exhaustive (every point is compared; the cost does not
- * depend on where the queries lie): equal distances go to the smaller index.
+ * float.  Exact: equal distances go to the smaller index.  The points are
+ * kept in tiles along a Morton curve; a tile whose bounding box is farther
+ * from a query than the query's best distance so far (strictly) is not
+ * compared, which never skips the nearest point or a tie.
  * scratch: device memory of `count` uint64 the call overwrites.
  * Asynchronous on the stream. */
 MDMC_API mdmc_status mdmc_point_index_nearest(const mdmc_point_index* index, const float* queries, int64_t count,

@@ -647,9 +647,9 @@ def mean_ratio(positions, triangles, stream=None):
 
 class PointIndex:
     """Exact nearest-point queries against a fixed set of CUDA float32 points
-    [P, 3] (mdmc_point_index_*; no counterpart in the reference): an
-    exhaustive tiled search on the GPU, whose cost does not depend on where
-    the queries lie."""
+    [P, 3] (mdmc_point_index_*; no counterpart in the reference): a tiled
+    search on the GPU over the points in Morton order, skipping the tiles
+    whose bounding box is farther than a query's best distance so far."""
 
     def __init__(self, points, stream=None):
         import torch

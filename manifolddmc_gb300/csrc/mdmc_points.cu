@@ -2,79 +2,121 @@
 // the differentiable workload (fitting a grid's iso-surface to points).  No
 // counterpart in the reference, which is not differentiable.
 //
-// Exhaustive and tiled: the queries of a block (one per thread) meet every
-// point of one slice of the point set, staged tile by tile in shared memory;
-// the slices of the set go to different blocks, so a few thousand queries
-// still fill every SM.  Each thread keeps its best (distance, index) and
-// merges it into the query's result with one 64-bit atomicMin on
-// (float bits of the squared distance << 32 | index): squared distances are
-// non-negative, whose float bits order like their values, so the minimum is
-// the smallest distance and, among equal distances, the smallest index.  The
-// distance is (dx*dx + dy*dy) + dz*dz in float, each operation rounded.
-// The cost does not depend on where the queries lie (a tree or grid search
-// degrades when many points are nearly equidistant from far queries, as
-// points on a torus are from a sphere's vertices around its axis).
+// Tiled, exact, with pruning that cannot change the answer.  The index keeps
+// the points sorted along a Morton curve in tiles of 256 (nearby points share
+// a tile) with each tile's bounding box.  A query first takes the nearest of
+// the tiles' first points as an upper bound; then the queries of a block (one
+// per thread) go through one slice of the tiles, staging in shared memory
+// only the tiles some query of the block still needs: a tile whose box is
+// farther from every query than that query's bound cannot hold its nearest
+// point.  Each thread keeps its best (distance, index) and merges it into the
+// query's result with one 64-bit atomicMin on (float bits of the squared
+// distance << 32 | index): squared distances are non-negative, whose float
+// bits order like their values, so the minimum is the smallest distance and,
+// among equal distances, the smallest index.  The distance is
+// (dx*dx + dy*dy) + dz*dz in float, each operation rounded.
+//
+// Why the pruning is exact: for the point c of a box nearest to q (q clamped
+// to the box), |q - c| <= |q - p| per axis for every p in the box, and every
+// float operation of the distance is monotonic, so the box's float distance is
+// at most the float distance of each of its points.  A tile is skipped only
+// when that bound exceeds the query's current best distance strictly, so no
+// point at the best distance (a tie included) is ever skipped.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
+#include <numeric>
 #include <vector>
 
 #include "mdmc.h"
 #include "mdmc_kernels.h"
 
+namespace mdmc {
+constexpr int kPointTile = 256;  // points per tile (and staged per round)
+}
+
 struct mdmc_point_index {
     int64_t count = 0;
-    float4* points = nullptr;  // x, y, z, original index (int bits)
+    int tiles = 0;
+    float4* points = nullptr;   // x, y, z, original index (int bits); Morton order
+    float4* boxes = nullptr;    // per tile: min x, y, z, -, max x, y, z, - (two float4)
 };
 
 namespace mdmc {
 namespace {
 
 constexpr int kNearestThreads = 256;
-constexpr int kNearestTile = 256;  // points staged per round
 
-__global__ void kPackPoints(const float* __restrict__ p, int n, float4* __restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = make_float4(p[3 * (int64_t)i], p[3 * (int64_t)i + 1], p[3 * (int64_t)i + 2], __int_as_float(i));
+__device__ __forceinline__ float dist2(float qx, float qy, float qz, float px, float py, float pz) {
+    const float dx = qx - px, dy = qy - py, dz = qz - pz;
+    return __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
 }
 
-__global__ void kNearestInit(unsigned long long* best, int64_t count) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < count) best[i] = ~0ull;
+// (distance, index) packed for atomicMin; ~0 (no candidate) for a distance
+// that is not finite (a NaN coordinate, or an overflow): such a point never
+// wins, as no strictly smaller distance than the initial infinity is found
+__device__ __forceinline__ unsigned long long packBest(float d, int index) {
+    return d < INFINITY ? ((unsigned long long)__float_as_uint(d) << 32) | (uint32_t)index : ~0ull;
 }
 
-// blockIdx.x: a group of kNearestThreads queries; blockIdx.y: a slice of the points
-__global__ void __launch_bounds__(kNearestThreads) kNearestSlice(const float4* __restrict__ pts, int n, int sliceLen,
-                                                                 const float* __restrict__ q, int64_t count,
-                                                                 unsigned long long* __restrict__ best) {
-    __shared__ float4 tile[kNearestTile];
+// the upper bound: the nearest of the tiles' first points (a real candidate)
+__global__ void __launch_bounds__(kNearestThreads) kNearestSeed(const float4* __restrict__ pts, int tiles,
+                                                                const float* __restrict__ q, int64_t count,
+                                                                unsigned long long* __restrict__ best) {
+    __shared__ float4 rep[kNearestThreads];
     const int64_t i = (int64_t)blockIdx.x * kNearestThreads + threadIdx.x;
     const bool active = i < count;
     const float qx = active ? q[3 * i] : 0.f, qy = active ? q[3 * i + 1] : 0.f, qz = active ? q[3 * i + 2] : 0.f;
-    const int p0 = blockIdx.y * sliceLen, p1 = min(n, p0 + sliceLen);
-    float bd = INFINITY;
-    int bi = 0x7FFFFFFF;
-    for (int t0 = p0; t0 < p1; t0 += kNearestTile) {
-        const int len = min(kNearestTile, p1 - t0);
+    unsigned long long b = ~0ull;
+    for (int t0 = 0; t0 < tiles; t0 += kNearestThreads) {
+        const int len = min(kNearestThreads, tiles - t0);
         __syncthreads();
-        if ((int)threadIdx.x < len) tile[threadIdx.x] = pts[t0 + threadIdx.x];
+        if ((int)threadIdx.x < len) rep[threadIdx.x] = pts[(int64_t)(t0 + threadIdx.x) * kPointTile];
         __syncthreads();
-#pragma unroll 8
         for (int k = 0; k < len; ++k) {
-            const float4 p = tile[k];
-            const float dx = qx - p.x, dy = qy - p.y, dz = qz - p.z;
-            const float d = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-            // points are visited in increasing index: a strictly smaller distance wins
-            if (d < bd) {
-                bd = d;
-                bi = t0 + k;
+            const float4 p = rep[k];
+            const unsigned long long c = packBest(dist2(qx, qy, qz, p.x, p.y, p.z), __float_as_int(p.w));
+            b = c < b ? c : b;
+        }
+    }
+    if (active) best[i] = b;
+}
+
+// blockIdx.x: a group of kNearestThreads queries; blockIdx.y: a slice of the tiles
+__global__ void __launch_bounds__(kNearestThreads) kNearestSlice(const float4* __restrict__ pts, int n,
+                                                                 const float4* __restrict__ boxes, int tiles,
+                                                                 int tilesPerSlice, const float* __restrict__ q,
+                                                                 int64_t count, unsigned long long* __restrict__ best) {
+    __shared__ float4 tile[kPointTile];
+    const int64_t i = (int64_t)blockIdx.x * kNearestThreads + threadIdx.x;
+    const bool active = i < count;
+    const float qx = active ? q[3 * i] : 0.f, qy = active ? q[3 * i + 1] : 0.f, qz = active ? q[3 * i + 2] : 0.f;
+    unsigned long long bk = active ? best[i] : ~0ull;  // the seed: (distance, index) of a real point
+    const int s0 = blockIdx.y * tilesPerSlice, s1 = min(tiles, s0 + tilesPerSlice);
+    for (int t = s0; t < s1; ++t) {
+        const float4 lo = boxes[2 * t], hi = boxes[2 * t + 1];
+        const float cx = fminf(fmaxf(qx, lo.x), hi.x), cy = fminf(fmaxf(qy, lo.y), hi.y),
+                    cz = fminf(fmaxf(qz, lo.z), hi.z);
+        const float bound = dist2(qx, qy, qz, cx, cy, cz);
+        // (no candidate yet: no bound to prune with)
+        const bool need = active && (bk == ~0ull || !(bound > __uint_as_float((uint32_t)(bk >> 32))));
+        if (!__syncthreads_or(need)) continue;  // (the barrier also ends the last tile's reads)
+        const int base = t * kPointTile, len = min(kPointTile, n - base);
+        if ((int)threadIdx.x < len) tile[threadIdx.x] = pts[base + threadIdx.x];
+        __syncthreads();
+        if (need) {
+#pragma unroll 8
+            for (int k = 0; k < len; ++k) {
+                const float4 p = tile[k];
+                const unsigned long long c = packBest(dist2(qx, qy, qz, p.x, p.y, p.z), __float_as_int(p.w));
+                bk = c < bk ? c : bk;
             }
         }
     }
-    if (active && bi != 0x7FFFFFFF)
-        atomicMin(best + i, ((unsigned long long)__float_as_uint(bd) << 32) | (unsigned)bi);
+    if (active) atomicMin(best + i, bk);
 }
 
 __global__ void kNearestFinish(const unsigned long long* __restrict__ best, int64_t count, int32_t* __restrict__ nearest,
@@ -84,6 +126,19 @@ __global__ void kNearestFinish(const unsigned long long* __restrict__ best, int6
     const unsigned long long b = best[i];
     nearest[i] = (int32_t)(uint32_t)(b & 0xFFFFFFFFull);
     if (d2) d2[i] = __uint_as_float((uint32_t)(b >> 32));
+}
+
+// 10 bits per axis of the point's place in the set's bounding box, interleaved
+uint32_t morton30(float x, float y, float z, const float lo[3], const float scale[3]) {
+    const float v[3] = {x, y, z};
+    uint32_t code = 0;
+    for (int a = 0; a < 3; ++a) {
+        float f = (v[a] - lo[a]) * scale[a];
+        f = f < 0.f ? 0.f : (f > 1023.f ? 1023.f : f);  // (NaN coordinates land at 0)
+        const uint32_t u = (uint32_t)f;
+        for (int b = 0; b < 10; ++b) code |= ((u >> b) & 1u) << (3 * b + a);
+    }
+    return code;
 }
 
 }  // namespace
@@ -97,15 +152,68 @@ extern "C" MDMC_API mdmc_status mdmc_point_index_create(mdmc_point_index** out, 
     *out = nullptr;
     if (!points || count < 1 || count > 0x7FFFFFFF) return MDMC_ERROR_INVALID_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
+    // the points on the host: Morton order, tiles and their boxes (a one-time build)
+    std::vector<float> host(3 * (size_t)count);
+    cudaError_t e = cudaMemcpyAsync(host.data(), points, sizeof(float) * host.size(), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return MDMC_ERROR_CUDA;
+    }
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY}, scale[3];
+    for (int64_t i = 0; i < count; ++i)
+        for (int a = 0; a < 3; ++a) {
+            const float v = host[3 * i + a];
+            if (v < lo[a]) lo[a] = v;
+            if (v > hi[a]) hi[a] = v;
+        }
+    for (int a = 0; a < 3; ++a) {
+        if (!(hi[a] >= lo[a])) lo[a] = hi[a] = 0.f;  // no finite coordinate
+        scale[a] = hi[a] > lo[a] ? 1023.f / (hi[a] - lo[a]) : 0.f;
+    }
+    std::vector<uint32_t> code((size_t)count);
+    for (int64_t i = 0; i < count; ++i) code[i] = morton30(host[3 * i], host[3 * i + 1], host[3 * i + 2], lo, scale);
+    std::vector<int> order((size_t)count);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return code[a] < code[b]; });
+    const int tiles = (int)((count + kPointTile - 1) / kPointTile);
+    std::vector<float4> sorted((size_t)count), boxes(2 * (size_t)tiles);
+    for (int64_t k = 0; k < count; ++k) {
+        const int i = order[k];
+        float4 p;
+        p.x = host[3 * (size_t)i];
+        p.y = host[3 * (size_t)i + 1];
+        p.z = host[3 * (size_t)i + 2];
+        int iw = i;
+        std::memcpy(&p.w, &iw, sizeof(int));
+        sorted[k] = p;
+    }
+    for (int t = 0; t < tiles; ++t) {
+        float4 bl, bh;
+        bl.x = bl.y = bl.z = INFINITY;
+        bh.x = bh.y = bh.z = -INFINITY;
+        bl.w = bh.w = 0.f;
+        bool nan = false;
+        for (int64_t k = (int64_t)t * kPointTile; k < std::min<int64_t>(count, (int64_t)(t + 1) * kPointTile); ++k) {
+            const float4 p = sorted[k];
+            nan = nan || p.x != p.x || p.y != p.y || p.z != p.z;
+            bl.x = std::min(bl.x, p.x); bl.y = std::min(bl.y, p.y); bl.z = std::min(bl.z, p.z);
+            bh.x = std::max(bh.x, p.x); bh.y = std::max(bh.y, p.y); bh.z = std::max(bh.z, p.z);
+        }
+        if (nan) {  // a NaN point: a box no query can rule out
+            bl.x = bl.y = bl.z = -INFINITY;
+            bh.x = bh.y = bh.z = INFINITY;
+        }
+        boxes[2 * (size_t)t] = bl;
+        boxes[2 * (size_t)t + 1] = bh;
+    }
     mdmc_point_index* ix = new mdmc_point_index();
     ix->count = count;
-    cudaError_t e = cudaMalloc(&ix->points, sizeof(float4) * (size_t)count);
-    if (e == cudaSuccess) {
-        countLaunch();
-        kPackPoints<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(points, (int)count, ix->points);
-        e = cudaGetLastError();
-    }
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    ix->tiles = tiles;
+    e = cudaMalloc(&ix->points, sizeof(float4) * (size_t)count);
+    if (e == cudaSuccess) e = cudaMalloc(&ix->boxes, sizeof(float4) * boxes.size());
+    if (e == cudaSuccess) e = cudaMemcpy(ix->points, sorted.data(), sizeof(float4) * sorted.size(), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(ix->boxes, boxes.data(), sizeof(float4) * boxes.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
         mdmc_point_index_destroy(ix);
@@ -118,6 +226,7 @@ extern "C" MDMC_API mdmc_status mdmc_point_index_create(mdmc_point_index** out, 
 extern "C" MDMC_API void mdmc_point_index_destroy(mdmc_point_index* ix) {
     if (!ix) return;
     cudaFree(ix->points);
+    cudaFree(ix->boxes);
     delete ix;
 }
 
@@ -128,18 +237,18 @@ extern "C" MDMC_API mdmc_status mdmc_point_index_nearest(const mdmc_point_index*
         return MDMC_ERROR_INVALID_ARGUMENT;
     if (count == 0) return MDMC_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    const int n = (int)ix->count;
-    // enough slices of the points for about four blocks per SM
+    const int n = (int)ix->count, tiles = ix->tiles;
+    // enough slices of the tiles for about four blocks per SM
     const int64_t groups = (count + kNearestThreads - 1) / kNearestThreads;
-    int slices = (int)std::max<int64_t>(1, std::min<int64_t>((152 * 4 + groups - 1) / groups,
-                                                             ((int64_t)n + kNearestTile - 1) / kNearestTile));
+    int slices = (int)std::max<int64_t>(1, std::min<int64_t>((152 * 4 + groups - 1) / groups, tiles));
     slices = std::min(slices, 65535);
-    const int sliceLen = (int)(((int64_t)n + slices - 1) / slices);
+    const int tilesPerSlice = (tiles + slices - 1) / slices;
+    slices = (tiles + tilesPerSlice - 1) / tilesPerSlice;
     countLaunch(3);
     unsigned long long* best = reinterpret_cast<unsigned long long*>(scratch);
-    kNearestInit<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(best, count);
-    kNearestSlice<<<dim3((unsigned)groups, (unsigned)slices), kNearestThreads, 0, s>>>(ix->points, n, sliceLen, queries,
-                                                                                        count, best);
+    kNearestSeed<<<(unsigned)groups, kNearestThreads, 0, s>>>(ix->points, tiles, queries, count, best);
+    kNearestSlice<<<dim3((unsigned)groups, (unsigned)slices), kNearestThreads, 0, s>>>(
+        ix->points, n, ix->boxes, tiles, tilesPerSlice, queries, count, best);
     kNearestFinish<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(best, count, nearest, dist2);
     return cudaGetLastError() == cudaSuccess ? MDMC_OK : MDMC_ERROR_CUDA;
 }
