@@ -403,7 +403,7 @@ MDMC_API void mdmc_point_index_destroy(mdmc_point_index* index);
  * kept in tiles along a Morton curve; a tile whose bounding box is farther
  * from a query than the query's best distance so far (strictly) is not
  * compared, which never skips the nearest point or a tie.
- * scratch: device memory of `count` uint64 the call overwrites.
+ * scratch: device memory of 2 * count + 2056 uint64 the call overwrites.
  * Asynchronous on the stream. */
 MDMC_API mdmc_status mdmc_point_index_nearest(const mdmc_point_index* index, const float* queries, int64_t count,
                                               int32_t* nearest, float* dist2, uint64_t* scratch, void* stream);

@@ -674,8 +674,9 @@ class PointIndex:
         q = queries.detach().contiguous().float()
         idx = torch.empty(len(q), dtype=torch.int32, device=q.device)
         d2 = torch.empty(len(q), dtype=torch.float32, device=q.device)
-        if self._scratch is None or len(self._scratch) < len(q):
-            self._scratch = torch.empty(max(len(q), 1), dtype=torch.int64, device=q.device)
+        need = 2 * len(q) + 2056  # mdmc_point_index_nearest's scratch
+        if self._scratch is None or len(self._scratch) < need:
+            self._scratch = torch.empty(need, dtype=torch.int64, device=q.device)
         st = self.lib.mdmc_point_index_nearest(self.handle, q.data_ptr(), len(q), idx.data_ptr(), d2.data_ptr(),
                                                self._scratch.data_ptr(),
                                                _stream_handle(stream if stream is not None

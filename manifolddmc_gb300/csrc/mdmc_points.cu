@@ -4,12 +4,13 @@
 //
 // Tiled, exact, with pruning that cannot change the answer.  The index keeps
 // the points sorted along a Morton curve in tiles of 256 (nearby points share
-// a tile) with each tile's bounding box.  A query first takes the nearest of
-// the tiles' first points as an upper bound; then the queries of a block (one
-// per thread) go through one slice of the tiles, staging in shared memory
-// only the tiles some query of the block still needs: a tile whose box is
-// farther from every query than that query's bound cannot hold its nearest
-// point.  Each thread keeps its best (distance, index) and merges it into the
+// a tile) with each tile's bounding box.  The queries are grouped by a coarse
+// Morton key, so that a block's queries lie close together.  A query first
+// takes the nearest of the tiles' first points as an upper bound; then the
+// queries of a block (one per thread) go through one slice of the tiles,
+// staging in shared memory only the tiles some query of the block still
+// needs: a tile whose box is farther from every query than that query's bound
+// cannot hold its nearest point.  Each thread keeps its best (distance, index) and merges it into the
 // query's result with one 64-bit atomicMin on (float bits of the squared
 // distance << 32 | index): squared distances are non-negative, whose float
 // bits order like their values, so the minimum is the smallest distance and,
@@ -43,6 +44,7 @@ struct mdmc_point_index {
     int tiles = 0;
     float4* points = nullptr;   // x, y, z, original index (int bits); Morton order
     float4* boxes = nullptr;    // per tile: min x, y, z, -, max x, y, z, - (two float4)
+    float lo[3] = {0, 0, 0}, scale[3] = {0, 0, 0};  // the points' box, for the queries' bucket keys
 };
 
 namespace mdmc {
@@ -62,13 +64,62 @@ __device__ __forceinline__ unsigned long long packBest(float d, int index) {
     return d < INFINITY ? ((unsigned long long)__float_as_uint(d) << 32) | (uint32_t)index : ~0ull;
 }
 
+// Queries go to blocks in the order of a 12-bit Morton key (4 bits per axis
+// of their place in the points' box), so that a block's queries lie close
+// together and need fewer tiles; a counting sort (the order inside a bucket
+// does not matter: every query's result is exact wherever it is computed).
+constexpr int kQueryBuckets = 4096;
+struct QueryKey {
+    float lo[3], scale[3];  // scale maps the box to [0, 16)
+    __device__ __forceinline__ int operator()(float x, float y, float z) const {
+        const float v[3] = {x, y, z};
+        int code = 0;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            float f = (v[a] - lo[a]) * scale[a];
+            f = f >= 0.f ? (f < 15.f ? f : 15.f) : 0.f;  // (NaN lands at 0)
+            const int u = (int)f;
+#pragma unroll
+            for (int b = 0; b < 4; ++b) code |= ((u >> b) & 1) << (3 * b + a);
+        }
+        return code;
+    }
+};
+__global__ void kQueryHistogram(const float* __restrict__ q, int64_t count, QueryKey key, int* __restrict__ hist) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) atomicAdd(hist + key(q[3 * i], q[3 * i + 1], q[3 * i + 2]), 1);
+}
+// one block of 1024 threads: exclusive prefix of the 4096 bucket counts, in place
+__global__ void __launch_bounds__(1024) kQueryBucketScan(int* __restrict__ hist) {
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    const int4 v = reinterpret_cast<int4*>(hist)[t];
+    const int sum = v.x + v.y + v.z + v.w;
+    part[t] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele scan
+        const int add = t >= o ? part[t - o] : 0;
+        __syncthreads();
+        part[t] += add;
+        __syncthreads();
+    }
+    const int base = part[t] - sum;
+    reinterpret_cast<int4*>(hist)[t] = make_int4(base, base + v.x, base + v.x + v.y, base + v.x + v.y + v.z);
+}
+__global__ void kQueryScatter(const float* __restrict__ q, int64_t count, QueryKey key, int* __restrict__ offsets,
+                              int* __restrict__ perm) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < count) perm[atomicAdd(offsets + key(q[3 * i], q[3 * i + 1], q[3 * i + 2]), 1)] = (int)i;
+}
+
 // the upper bound: the nearest of the tiles' first points (a real candidate)
 __global__ void __launch_bounds__(kNearestThreads) kNearestSeed(const float4* __restrict__ pts, int tiles,
-                                                                const float* __restrict__ q, int64_t count,
-                                                                unsigned long long* __restrict__ best) {
+                                                                const float* __restrict__ q, const int* __restrict__ perm,
+                                                                int64_t count, unsigned long long* __restrict__ best) {
     __shared__ float4 rep[kNearestThreads];
-    const int64_t i = (int64_t)blockIdx.x * kNearestThreads + threadIdx.x;
-    const bool active = i < count;
+    const int64_t j = (int64_t)blockIdx.x * kNearestThreads + threadIdx.x;
+    const bool active = j < count;
+    const int64_t i = active ? (perm ? perm[j] : j) : 0;
     const float qx = active ? q[3 * i] : 0.f, qy = active ? q[3 * i + 1] : 0.f, qz = active ? q[3 * i + 2] : 0.f;
     unsigned long long b = ~0ull;
     for (int t0 = 0; t0 < tiles; t0 += kNearestThreads) {
@@ -89,10 +140,12 @@ __global__ void __launch_bounds__(kNearestThreads) kNearestSeed(const float4* __
 __global__ void __launch_bounds__(kNearestThreads) kNearestSlice(const float4* __restrict__ pts, int n,
                                                                  const float4* __restrict__ boxes, int tiles,
                                                                  int tilesPerSlice, const float* __restrict__ q,
-                                                                 int64_t count, unsigned long long* __restrict__ best) {
+                                                                 const int* __restrict__ perm, int64_t count,
+                                                                 unsigned long long* __restrict__ best) {
     __shared__ float4 tile[kPointTile];
-    const int64_t i = (int64_t)blockIdx.x * kNearestThreads + threadIdx.x;
-    const bool active = i < count;
+    const int64_t j = (int64_t)blockIdx.x * kNearestThreads + threadIdx.x;
+    const bool active = j < count;
+    const int64_t i = active ? (perm ? perm[j] : j) : 0;
     const float qx = active ? q[3 * i] : 0.f, qy = active ? q[3 * i + 1] : 0.f, qz = active ? q[3 * i + 2] : 0.f;
     unsigned long long bk = active ? best[i] : ~0ull;  // the seed: (distance, index) of a real point
     const int s0 = blockIdx.y * tilesPerSlice, s1 = min(tiles, s0 + tilesPerSlice);
@@ -210,6 +263,10 @@ extern "C" MDMC_API mdmc_status mdmc_point_index_create(mdmc_point_index** out, 
     mdmc_point_index* ix = new mdmc_point_index();
     ix->count = count;
     ix->tiles = tiles;
+    for (int a = 0; a < 3; ++a) {
+        ix->lo[a] = lo[a];
+        ix->scale[a] = hi[a] > lo[a] ? 16.f / (hi[a] - lo[a]) : 0.f;
+    }
     e = cudaMalloc(&ix->points, sizeof(float4) * (size_t)count);
     if (e == cudaSuccess) e = cudaMalloc(&ix->boxes, sizeof(float4) * boxes.size());
     if (e == cudaSuccess) e = cudaMemcpy(ix->points, sorted.data(), sizeof(float4) * sorted.size(), cudaMemcpyHostToDevice);
@@ -244,11 +301,26 @@ extern "C" MDMC_API mdmc_status mdmc_point_index_nearest(const mdmc_point_index*
     slices = std::min(slices, 65535);
     const int tilesPerSlice = (tiles + slices - 1) / slices;
     slices = (tiles + tilesPerSlice - 1) / tilesPerSlice;
-    countLaunch(3);
     unsigned long long* best = reinterpret_cast<unsigned long long*>(scratch);
-    kNearestSeed<<<(unsigned)groups, kNearestThreads, 0, s>>>(ix->points, tiles, queries, count, best);
+    // scratch: best (count words), the permutation (count ints), the bucket
+    // counts (4096 ints, from a 16-byte boundary)
+    int* perm = reinterpret_cast<int*>(scratch + count);
+    int* hist = reinterpret_cast<int*>(scratch + count + (count + 1) / 2 + 1);
+    hist = reinterpret_cast<int*>((reinterpret_cast<uintptr_t>(hist) + 15) & ~(uintptr_t)15);
+    QueryKey key;
+    for (int a = 0; a < 3; ++a) {
+        key.lo[a] = ix->lo[a];
+        key.scale[a] = ix->scale[a];
+    }
+    if (cudaMemsetAsync(hist, 0, sizeof(int) * kQueryBuckets, s) != cudaSuccess) return MDMC_ERROR_CUDA;
+    countLaunch(6);
+    const unsigned qb = (unsigned)((count + 255) / 256);
+    kQueryHistogram<<<qb, 256, 0, s>>>(queries, count, key, hist);
+    kQueryBucketScan<<<1, 1024, 0, s>>>(hist);
+    kQueryScatter<<<qb, 256, 0, s>>>(queries, count, key, hist, perm);
+    kNearestSeed<<<(unsigned)groups, kNearestThreads, 0, s>>>(ix->points, tiles, queries, perm, count, best);
     kNearestSlice<<<dim3((unsigned)groups, (unsigned)slices), kNearestThreads, 0, s>>>(
-        ix->points, n, ix->boxes, tiles, tilesPerSlice, queries, count, best);
+        ix->points, n, ix->boxes, tiles, tilesPerSlice, queries, perm, count, best);
     kNearestFinish<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(best, count, nearest, dist2);
     return cudaGetLastError() == cudaSuccess ? MDMC_OK : MDMC_ERROR_CUDA;
 }
