@@ -20,7 +20,18 @@ class _DMCFunction(torch.autograd.Function):
         samples = samples.detach().contiguous()
         dims = [samples.shape[2], samples.shape[1], samples.shape[0]]
         stream = torch.cuda.current_stream()
-        grid = UniformGrid(samples, dims, origin, spacing, refinement, pad, stream=stream)
+        # A grid on the device only describes the samples' memory (refinement
+        # and padding are evaluated from it on demand): the description of the
+        # last call is reused when the samples sit at the same address with the
+        # same layout (an optimiser updating them in place), which saves a
+        # library context per step.
+        key = (samples.data_ptr(), tuple(dims), tuple(origin), tuple(spacing), int(refinement), bool(pad))
+        cached = getattr(dmc, "_grid_cache", None)
+        if cached is not None and cached[0] == key:
+            grid = cached[1]
+        else:
+            grid = UniformGrid(samples, dims, origin, spacing, refinement, pad, stream=stream)
+            dmc._grid_cache = (key, grid)
         dmc.run(iso, grid, stream=stream)
         arrays = dmc.device_arrays()
         positions = arrays["positions"].clone()
