@@ -401,6 +401,16 @@ def measure_adjoint(args, dev, stream, flush):
             if i >= max(args.warmup, 3):
                 (both if with_adjoint else fwd).append(e0.elapsed_time(e1))
     f, b = float(np.mean(fwd)), float(np.mean(both))
+    # the adjoint accumulates with float atomics: the spread between two
+    # backward passes of the same run, relative to the gradient's scale
+    dmc.run(iso, grid, stream=stream)
+    g1 = torch.empty_like(d_in)
+    g2 = torch.empty_like(d_in)
+    dmc.backward(dl, g1, stream=stream)
+    dmc.backward(dl, g2, stream=stream)
+    stream.synchronize()
+    scale = float(g1.abs().max())
+    spread = float((g1 - g2).abs().max()) / scale if scale > 0 else 0.0
     fit = None
     if not args.no_fit:
         # 200 Adam steps of forward + adjoint + one-sided Chamfer to 200k points
@@ -420,6 +430,8 @@ def measure_adjoint(args, dev, stream, flush):
                        "events: DMC forward, nearest points + loss, adjoint backward + Adam"}
     return {"workload": name, "description": desc, "vertices": V, "fwd_ms": round(f, 4), "fit": fit,
             "fwd_adjoint_ms": round(b, 4), "ratio": round(b / f, 3),
+            "run_to_run_spread": spread,
+            "run_to_run_note": "max |g1 - g2| / max |g1| over two backward passes of one run (float atomics)",
             "gradient_check": "max |gpu - FP64 oracle| <= 1e-5 * max |FP64| (tests/test_gpu_adjoint.py); "
                               "FP64 oracle vs FP64 central differences h=1e-4 (tests/test_adjoint_oracle.py)"}
 
