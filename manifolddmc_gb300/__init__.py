@@ -436,9 +436,10 @@ class DualMarchingCubes:
             _ptr(out.vertex_flags), None))
         return out
 
-    def device_arrays(self):
+    def device_arrays(self, names=None):
         """The last run's mesh as CUDA torch tensors viewing the library's
-        buffers (valid until the next run on this object)."""
+        buffers (valid until the next run on this object); `names` picks a
+        subset (all by default)."""
         import torch
         m = self.mesh
         V, F, H = int(m.num_vertices), int(m.num_faces), int(m.num_halfedges)
@@ -446,6 +447,8 @@ class DualMarchingCubes:
                  "quads": (m.quads, (F, 4), "<i4"), "halfedges": (m.halfedges, (H, 4), "<i4"),
                  "face_first_halfedge": (m.face_first_halfedge, (F,), "<i4"),
                  "vertex_halfedge": (m.vertex_halfedge, (V,), "<i4"), "vertex_flags": (m.vertex_flags, (V,), "|u1")}
+        if names is not None:
+            views = {k: views[k] for k in names}
         out = {}
         for k, (ptr, shape, ts) in views.items():
             addr = int(ptr) if ptr else 0

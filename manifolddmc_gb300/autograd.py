@@ -33,7 +33,7 @@ class _DMCFunction(torch.autograd.Function):
             grid = UniformGrid(samples, dims, origin, spacing, refinement, pad, stream=stream)
             dmc._grid_cache = (key, grid)
         dmc.run(iso, grid, stream=stream)
-        arrays = dmc.device_arrays()
+        arrays = dmc.device_arrays(("positions", "quads"))
         positions = arrays["positions"].clone()
         quads = arrays["quads"].clone()
         ctx.mark_non_differentiable(quads)
