@@ -424,10 +424,12 @@ mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaSt
                      detect ? c->degree.as<int>() : nullptr, ctr, status, s);
     if (detect) {
         // fan keys are marked with this pass's number (1..255); the array is
-        // cleared only when it is new or the numbers wrap around
-        const void* keys = c->isKey.p;
+        // cleared only when it is new or the numbers wrap around.  (A new
+        // array is told by its capacity: a reallocation can return the
+        // address just freed, holding another array's old marks.)
+        const size_t keyBytes = c->isKey.bytes;
         MDMC_CHECK(c, c->isKey.ensure((size_t)std::max<int64_t>(c->H, 1)));
-        if (c->isKey.p != keys || c->keyMark == 255) {
+        if (c->isKey.bytes != keyBytes || c->keyMark == 255) {
             MDMC_CHECK(c, cudaMemsetAsync(c->isKey.p, 0, c->isKey.bytes, s));
             c->keyMark = 0;
         }
