@@ -669,8 +669,8 @@ mdmc_status runSplitter(mdmc_context* c, const GridDesc& g, float iso, int64_t& 
         MDMC_CHECK(c, cudaMemsetAsync(c->wHC2O.p, 0xFF, sizeof(int) * (size_t)nh, s));
         MDMC_CHECK(c, cudaMemsetAsync(c->wFC2O.p, 0xFF, sizeof(int) * (size_t)nf, s));
         MDMC_CHECK(c, cudaMemsetAsync(c->wHe.p, 0xFF, sizeof(int4) * (size_t)nh, s));
-        MDMC_CHECK(c, cudaMemsetAsync(c->wVSlots.p, 0xFF, sizeof(int) * 4 * (size_t)nv, s));
-        MDMC_CHECK(c, cudaMemsetAsync(c->wHSlots.p, 0xFF, sizeof(int) * 4 * (size_t)nh, s));
+        // (the partner slots need no clearing: an element's count says how
+        // many of its slots the collapse wrote, and nothing reads beyond)
         launchFillInt(c->wVNum.as<int>(), nv, 1, s);
         launchFillInt(c->wHNum.as<int>(), nh, 1, s);
         MDMC_CHECK(c, c->splitFlags.ensure(sizeof(int) * 4));

@@ -55,10 +55,10 @@ __device__ __forceinline__ float trilinear(const float s[8], F3 p) {
 // cell edges and the packed contour word (D/CellIntersection.h:28-137)
 // ---------------------------------------------------------------------------
 // corner pair of every cell edge; corner i sits at (i&1, (i>>1)&1, (i>>2)&1)
-__host__ __device__ __forceinline__ int edgeV0(int e) { return (int)((0x231046540210ULL >> (4 * e)) & 0xF); }
-__host__ __device__ __forceinline__ int edgeV1(int e) { return (int)((0x675467752331ULL >> (4 * e)) & 0xF); }
+__host__ __device__ constexpr int edgeV0(int e) { return (int)((0x231046540210ULL >> (4 * e)) & 0xF); }
+__host__ __device__ constexpr int edgeV1(int e) { return (int)((0x675467752331ULL >> (4 * e)) & 0xF); }
 // axis of every edge (0 = x, 1 = y, 2 = z)
-__host__ __device__ __forceinline__ int edgeAxis(int e) { return (int)((0xAA4444u >> (2 * e)) & 0x3); }
+__host__ __device__ constexpr int edgeAxis(int e) { return (int)((0xAA4444u >> (2 * e)) & 0x3); }
 
 __host__ __device__ __forceinline__ int nib(uint64_t w, int i) { return (int)((w >> (4 * i)) & 0xF); }
 __device__ __forceinline__ int contourSize(uint64_t c, int t) { return nib(c, t); }
@@ -75,7 +75,7 @@ __device__ __forceinline__ int numContours(uint64_t c) {
 }
 
 // quad slot of an edge (computeVertexPosition, D/CellIntersection.inl:361-366)
-__host__ __device__ __forceinline__ int quadSlot(int e, int edgyBit) {
+__host__ __device__ constexpr int quadSlot(int e, int edgyBit) {
     return (int)((240177437832960ULL >> (4 * e + 2 * edgyBit)) & 3);
 }
 

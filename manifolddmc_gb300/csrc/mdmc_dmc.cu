@@ -1236,7 +1236,7 @@ __device__ __forceinline__ bool ownsAxis(int cs, int axis, int x, int y, int z) 
 
 // local index of the cell edge leaving corner `corner` (bit 0 x, 1 y, 2 z)
 // along `axis`; the corner's bit for that axis is 0
-__device__ __forceinline__ int localEdge(int corner, int axis) {
+__host__ __device__ constexpr int localEdge(int corner, int axis) {
     if (axis == 0) return corner;                                                        // 0, 2, 4, 6
     if (axis == 1) return (0x5713 >> (4 * ((corner & 1) | ((corner >> 1) & 2)))) & 0xF;  // 3, 1, 7, 5
     return (0xAB98 >> (4 * corner)) & 0xF;                                               // 8, 9, 11, 10
@@ -1244,14 +1244,89 @@ __device__ __forceinline__ int localEdge(int corner, int axis) {
 
 __device__ __forceinline__ int axisBit(int a) { return 1 << a; }
 
-// one cell around a quad's grid edge, in registers
-struct AroundCell {
-    uint32_t info;  // case | edge -> contour map << 8
-    int vbase;      // first vertex id
-    int qbase;      // first quad id
-    int le;         // local index of the quad's edge in this cell
-    int contour;    // contour of that edge in this cell
+// The fixed geometry of a quad's halfedges, by the quad's axis a, the sign of
+// its owner cell's corner 0 (edgy: the slot order of the four cells around the
+// quad's edge) and the halfedge's slot hi.  Cell k around the edge is
+// p - (k & 1) e_b - (k >> 1) e_c (b < c the other axes); halfedge hi runs from
+// the vertex of cell A (slot hi) to that of cell B (slot hi + 1), which share a
+// face.  The only quads that can hold the same vertex pair are those of the
+// face's three other grid edges: cand 0 parallel to the quad's edge on the
+// face's far side, cand 1 and 2 across the face at the edge's lower and upper
+// end.
+//   head[6 * hi + 2 * a + edgy]: cell A's k (2 bits) and A's local index of
+//     the quad's edge (4), then per candidate the two corners (3 + 3) of its
+//     edge in A (the edge crosses iso when their signs differ);
+//   cand[6 * (3 * hi + cand) + 2 * a + edgy]: the candidate edge's local index
+//     in A and in B (4 + 4), its axis (2), which loaded record holds its owner
+//     cell (4: 0..2 cells around the quad's edge, 4..8 the five others), the
+//     owner's offset from p plus one along x, y, z (2 + 2 + 2), and for each
+//     sign of A's corner at the edge's start the shared halfedge's slot in the
+//     candidate quad (2), "its origin is A's vertex" (1) and "valid" (1).
+// Built at compile time from the same index arithmetic a per-halfedge
+// evaluation would run.
+struct QuadGeom {
+    uint32_t head[24];
+    uint32_t cand[72];
 };
+
+constexpr QuadGeom makeQuadGeom() {
+    QuadGeom g{};
+    for (int axis = 0; axis < 3; ++axis)
+        for (int edgy = 0; edgy < 2; ++edgy) {
+            const int ae = 2 * axis + edgy;
+            const int b = axis == 0 ? 1 : 0, c = axis == 2 ? 1 : 2;
+            const int leWord = axis == 0 ? 0x6420 : (axis == 1 ? 0x5713 : 0xAB98);
+            int le[4] = {0, 0, 0, 0}, quadK[4] = {0, 0, 0, 0};
+            for (int k = 0; k < 4; ++k) le[k] = (leWord >> (4 * k)) & 0xF;
+            // slot -> cell: edges with v0 inside take the reverse cycle
+            // (quadSlot, computeVertexPosition, D/CellIntersection.inl:361-366)
+            for (int k = 0; k < 4; ++k) quadK[quadSlot(le[k], edgy)] = k;
+            for (int hi = 0; hi < 4; ++hi) {
+                const int kA = quadK[hi], kB = quadK[(hi + 1) & 3];
+                // A and B differ along t (bit 0 of k: along b, bit 1: along c);
+                // u is the remaining axis of the face
+                const bool alongB = ((kA ^ kB) & 1) != 0;
+                const int t = alongB ? b : c, u = alongB ? c : b;
+                const int aMinusT = alongB ? (kA & 1) : (kA >> 1);  // A = p - e_t ?
+                const int aMinusU = alongB ? (kA >> 1) : (kA & 1);  // A = p - e_u ?
+                // A's corner offsets of the face's grid edges: the t offset is 1
+                // where A lies below the face
+                const int cT = aMinusT, cTB = 1 - aMinusT;
+                uint32_t head = (uint32_t)kA | ((uint32_t)le[kA] << 2);
+                for (int cand = 0; cand < 3; ++cand) {
+                    const int al = cand == 0 ? axis : u;
+                    const int offU = cand == 0 ? (aMinusU ? 0 : 1) : 0;
+                    const int offA = cand == 2 ? 1 : 0;
+                    const int ca = (cT << t) | (offU << u) | (offA << axis);
+                    const int cb = (cTB << t) | (offU << u) | (offA << axis);
+                    const int eA = localEdge(ca, al), eB = localEdge(cb, al);
+                    head |= (uint32_t)(edgeV0(eA) | (edgeV1(eA) << 3)) << (6 + 6 * cand);
+                    // the grid edge's origin: p + du e_u + offA e_a; its owner is a
+                    // cell around the quad's edge (p, p - e_u) or p + e_u (du = 1),
+                    // p + e_a (du = 0) or p - e_u + e_a (du = -1)
+                    const int du = offU - aMinusU;
+                    int d[3] = {0, 0, 0};
+                    for (int x = 0; x < 3; ++x) d[x] = (u == x ? du : 0) + (axis == x ? offA : 0);
+                    const int ko = du == 0 ? 0 : (u == b ? 1 : 2);
+                    const int kx = offA == 0 ? (u == b ? 0 : 1) : (du == 0 ? 2 : (u == b ? 3 : 4));
+                    const int slot = (offA == 0 && du <= 0) ? ko : 4 + kx;
+                    uint32_t code[2] = {0, 0};
+                    for (int eo = 0; eo < 2; ++eo) {
+                        const int sA = quadSlot(eA, eo), sB = quadSlot(eB, eo);
+                        if (((sA + 1) & 3) == sB) code[eo] = (uint32_t)sA | 4u | 8u;
+                        else if (((sB + 1) & 3) == sA) code[eo] = (uint32_t)sB | 8u;
+                    }
+                    g.cand[6 * (3 * hi + cand) + ae] =
+                        (uint32_t)eA | ((uint32_t)eB << 4) | ((uint32_t)al << 8) | ((uint32_t)slot << 10) |
+                        ((uint32_t)(d[0] + 1) << 14) | ((uint32_t)(d[1] + 1) << 16) | ((uint32_t)(d[2] + 1) << 18) |
+                        (code[0] << 20) | (code[1] << 24);
+                }
+                g.head[6 * hi + ae] = head;
+            }
+        }
+    return g;
+}
+__device__ const QuadGeom kQuadGeom = makeQuadGeom();
 
 // The quads (mapQuadrilaterals, D/DualMarchingCubes.cu:72-85), their halfedges
 // (collectHalfedgeElements, D/Halfedges/HalfedgeMesh.cu:14-60) and the twins
@@ -1261,17 +1336,31 @@ struct AroundCell {
 // can hold the same vertex pair are those of the four grid edges of the A|B
 // face, and each of them does exactly when its edge lies in the same contours
 // of A and of B.  That set is the reference's edge-table bucket; sorted, it
-// gives the twins by the reference's rules.
+// gives the twins by the reference's rules.  The nine cell records a quad
+// needs sit in the thread's own column of shared memory, so that a record
+// picked by a table entry is one load, not a chain of selects.
 #ifndef MDMC_QUADS_MIN_BLOCKS
-#define MDMC_QUADS_MIN_BLOCKS 3
+#define MDMC_QUADS_MIN_BLOCKS 4
 #endif
-__global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const ActiveCell* __restrict__ act, const int* __restrict__ quadOwner,
+constexpr int kQuadThreads = 256;
+__global__ void __launch_bounds__(kQuadThreads, MDMC_QUADS_MIN_BLOCKS) kQuads(const ActiveCell* __restrict__ act, const int* __restrict__ quadOwner,
                                               int numActive, CellIndex ix, int4* __restrict__ he,
                                               int* __restrict__ faceFirst, uint16_t* __restrict__ faceAttr,
                                               uint8_t* vflags, uint32_t* __restrict__ heValence4,
                                               int4* __restrict__ nmList, int nmCapacity, int numQuads, int numVertices,
                                               int4* __restrict__ quadsOut, int* vertexHE,
                                               DevCounters* ctr, int qBegin, int qEnd) {
+    __shared__ uint32_t sHead[24], sCand[72];
+    // records: 0..3 the cells around the quad's edge (k), 4..8 the five others
+    __shared__ uint32_t sInfo[9][kQuadThreads];
+    __shared__ int sQbase[9][kQuadThreads];
+    __shared__ int sVbase[4][kQuadThreads];
+    for (int i = threadIdx.x; i < 96; i += blockDim.x) {
+        if (i < 24) sHead[i] = kQuadGeom.head[i];
+        else sCand[i - 24] = kQuadGeom.cand[i - 24];
+    }
+    __syncthreads();
+    const int tid = threadIdx.x;
     const int q = qBegin + blockIdx.x * blockDim.x + threadIdx.x;
     int nE = 0, nE3 = 0, nE4 = 0;
     int nmEdges = -1;  // halfedges of this quad on edges of more than two faces
@@ -1299,11 +1388,6 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
         if (ok) {
             // the other axes b < c; cell k = p - (k&1) e_b - (k>>1) e_c
             const int b = axis == 0 ? 1 : 0, c = axis == 2 ? 1 : 2;
-            const uint32_t leWord = axis == 0 ? 0x6420u : (axis == 1 ? 0x5713u : 0xAB98u);
-            AroundCell cell[4];
-            cell[0].info = rec.info;
-            cell[0].vbase = rec.pad;
-            cell[0].qbase = rec.qbase;
             // the cells around the quad's edge (k = 1..3), and the five other
             // cells that can own a quad of one of the face buckets:
             // p + e_b, p + e_c, p + e_a, p - e_b + e_a, p - e_c + e_a.  All
@@ -1325,59 +1409,51 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
                                 py + (axis == 1 ? dA : 0) + (b == 1 ? dB : 0) + (c == 1 ? dC : 0),
                                 pz + (axis == 2 ? dA : 0) + (c == 2 ? dC : 0));
             }
+            sInfo[0][tid] = rec.info;
+            sQbase[0][tid] = rec.qbase;
+            sVbase[0][tid] = rec.pad;
 #pragma unroll
             for (int k = 1; k < 4; ++k) {
+                uint32_t info = 0;
+                int qbase = 0, vbase = 0;
                 if (jk[k] < 0 || jk[k] >= numActive) {
                     ok = false;
-                    cell[k].info = 0;
-                    cell[k].vbase = 0;
-                    cell[k].qbase = 0;
                 } else {
                     const ActiveCell r2 = act[jk[k]];
-                    cell[k].info = r2.info;
-                    cell[k].vbase = r2.pad;
-                    cell[k].qbase = r2.qbase;
+                    info = r2.info;
+                    qbase = r2.qbase;
+                    vbase = r2.pad;
                 }
+                sInfo[k][tid] = info;
+                sQbase[k][tid] = qbase;
+                sVbase[k][tid] = vbase;
             }
-            uint32_t xinfo[5];
-            int xqbase[5];
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
-                xinfo[k] = 0;
-                xqbase[k] = -1;  // no such active cell
+                uint32_t info = 0;
+                int qbase = -1;  // no such active cell
                 if (inb(jx[k], numActive)) {
                     const ActiveCell r2 = act[jx[k]];
-                    xinfo[k] = r2.info;
-                    xqbase[k] = r2.qbase;
+                    info = r2.info;
+                    qbase = r2.qbase;
                 }
-            }
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                cell[k].le = (int)((leWord >> (4 * k)) & 0xF);
-                cell[k].contour = (int)((cell[k].info >> (8 + 2 * cell[k].le)) & 3u);
+                sInfo[4 + k][tid] = info;
+                sQbase[4 + k][tid] = qbase;
             }
             if (!ok) atomicOr(&ctr->status, kStatusMissingCell);
-            // slot -> cell: edges with v0 inside take the reverse cycle
-            // (quadSlot, computeVertexPosition, D/CellIntersection.inl:361-366)
-            const int edgy = (cs & 1) ? 0 : 1;
-            int quadK[4] = {0, 0, 0, 0};
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int sl = quadSlot(cell[k].le, edgy);
-#pragma unroll
-                for (int t = 0; t < 4; ++t)
-                    if (sl == t) quadK[t] = k;
-            }
-            int quadV[4];
+            const int ae = 2 * axis + ((cs & 1) ? 0 : 1);
+            // per slot: its cell's record, the contour of the quad's edge in
+            // that cell, and the vertex (the slot's halfedge's origin)
+            uint32_t head[4], info[4];
+            int contour[4], quadV[4];
 #pragma unroll
             for (int sl = 0; sl < 4; ++sl) {
-                const int k = quadK[sl];
-                int v = 0;
-#pragma unroll
-                for (int t = 0; t < 4; ++t)
-                    if (k == t) v = cell[t].vbase + cell[t].contour;
-                quadV[sl] = v;
-                if (!inb(v, numVertices)) ok = false;
+                head[sl] = sHead[6 * sl + ae];
+                const int k = (int)(head[sl] & 3u);
+                info[sl] = sInfo[k][tid];
+                contour[sl] = (int)((info[sl] >> (8 + 2 * ((head[sl] >> 2) & 15u))) & 3u);
+                quadV[sl] = sVbase[k][tid] + contour[sl];
+                if (!inb(quadV[sl], numVertices)) ok = false;
             }
             if (!ok) {
                 atomicOr(&ctr->status, kStatusCountMismatch);
@@ -1389,85 +1465,45 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
                 int4 out[4];
 #pragma unroll
                 for (int hi = 0; hi < 4; ++hi) {
-                    const int kA = quadK[hi], kB = quadK[(hi + 1) & 3];
-                    uint32_t infoA = 0, infoB = 0;
-                    int vbA = 0, vbB = 0;
-#pragma unroll
-                    for (int t = 0; t < 4; ++t) {
-                        if (kA == t) {
-                            infoA = cell[t].info;
-                            vbA = cell[t].vbase;
-                        }
-                        if (kB == t) {
-                            infoB = cell[t].info;
-                            vbB = cell[t].vbase;
-                        }
-                    }
-                    const int tA = (int)((infoA >> (8 + 2 * ((leWord >> (4 * kA)) & 0xF))) & 3u);
-                    const int tB = (int)((infoB >> (8 + 2 * ((leWord >> (4 * kB)) & 0xF))) & 3u);
-                    // A and B differ along t; u is the remaining axis.  diffB:
-                    // A and B differ in bit 0 of k (along b) or bit 1 (along c)
-                    const bool alongB = ((kA ^ kB) & 1) != 0;
-                    const int t = alongB ? b : c, u = alongB ? c : b;
-                    const int aMinusT = alongB ? (kA & 1) : (kA >> 1);   // A = p - e_t ?
-                    const int aMinusU = alongB ? (kA >> 1) : (kA & 1);   // A = p - e_u ?
-                    // A's corner offsets (relative to A) of the face's grid edges:
-                    // the t offset is 1 where A lies below the face
-                    const int cT = aMinusT, cTB = 1 - aMinusT;
+                    const uint32_t infoA = info[hi], infoB = info[(hi + 1) & 3];
+                    const int tA = contour[hi], tB = contour[(hi + 1) & 3];
                     const uint32_t csA = infoA & 255u;
+                    const uint32_t hd = head[hi];
+                    const int self = h0 + hi;
                     int ids[4], org[4];
-                    ids[0] = h0 + hi;
+                    ids[0] = self;
                     org[0] = quadV[hi];
                     ids[1] = ids[2] = ids[3] = 0x7FFFFFFF;
                     org[1] = org[2] = org[3] = -1;
-                    // cand 0: parallel to the quad's edge on the face's other side;
-                    // cand 1, 2: across the face at the edge's lower / upper end.
                     // The candidates that cross iso are found first and then gone
                     // through with one body of code, so that lanes whose crossing
                     // edge is a different candidate run it together.
                     uint32_t crossing = 0;
 #pragma unroll
-                    for (int cand = 0; cand < 3; ++cand) {
-                        const int al = cand == 0 ? axis : u;
-                        const int offU = cand == 0 ? (aMinusU ? 0 : 1) : 0;
-                        const int offA = cand == 2 ? 1 : 0;
-                        const int eA = localEdge((cT << t) | (offU << u) | (offA << axis), al);
-                        crossing |= (((csA >> edgeV0(eA)) ^ (csA >> edgeV1(eA))) & 1u) << cand;
-                    }
+                    for (int cand = 0; cand < 3; ++cand)
+                        crossing |= (((csA >> ((hd >> (6 + 6 * cand)) & 7u)) ^ (csA >> ((hd >> (9 + 6 * cand)) & 7u))) &
+                                     1u) << cand;
+                    // (the three table entries are loaded before the loop, and the
+                    // owner record of a candidate before its tests, so that each
+                    // iteration waits on one shared load at most)
+                    const uint32_t en0 = sCand[6 * (3 * hi) + ae], en1 = sCand[6 * (3 * hi + 1) + ae],
+                                   en2 = sCand[6 * (3 * hi + 2) + ae];
+                    int found = 0;
                     while (crossing) {
                         const int cand = __ffs(crossing) - 1;
                         crossing &= crossing - 1;
-                        const int al = cand == 0 ? axis : u;
-                        const int offU = cand == 0 ? (aMinusU ? 0 : 1) : 0;
-                        const int offA = cand == 2 ? 1 : 0;
-                        const int ca = (cT << t) | (offU << u) | (offA << axis);
-                        const int cb = (cTB << t) | (offU << u) | (offA << axis);
-                        const int eA = localEdge(ca, al), eB = localEdge(cb, al);
-                        if ((int)((infoA >> (8 + 2 * eA)) & 3u) != tA) continue;
-                        if ((int)((infoB >> (8 + 2 * eB)) & 3u) != tB) continue;
+                        const uint32_t en = cand == 0 ? en0 : (cand == 1 ? en1 : en2);
+                        const int slot = (int)((en >> 10) & 15u);
+                        const int oqbase = sQbase[slot][tid];
+                        const uint32_t oinfo = sInfo[slot][tid];
+                        if ((int)((infoA >> (8 + 2 * (en & 15u))) & 3u) != tA) continue;
+                        if ((int)((infoB >> (8 + 2 * ((en >> 4) & 15u))) & 3u) != tB) continue;
                         // the grid edge's origin and the quad its owner holds
-                        const int du = offU - aMinusU;
-                        const int ox = px + (u == 0 ? du : 0) + (axis == 0 ? offA : 0);
-                        const int oy = py + (u == 1 ? du : 0) + (axis == 1 ? offA : 0);
-                        const int oz = pz + (u == 2 ? du : 0) + (axis == 2 ? offA : 0);
+                        const int al = (int)((en >> 8) & 3u);
+                        const int ox = px + (int)((en >> 14) & 3u) - 1;
+                        const int oy = py + (int)((en >> 16) & 3u) - 1;
+                        const int oz = pz + (int)((en >> 18) & 3u) - 1;
                         if (((al != 0 && ox < 1) || (al != 1 && oy < 1) || (al != 2 && oz < 1))) continue;
-                        // the owner is a cell around the quad's edge (p, p - e_u), or
-                        // p + e_u (du = 1), p + e_a (du = 0) or p - e_u + e_a (du = -1);
-                        // every record is loaded already (both picks are made, one kept)
-                        const int ko = du == 0 ? 0 : (u == b ? 1 : 2);
-                        const int kx = offA == 0 ? (u == b ? 0 : 1) : (du == 0 ? 2 : (u == b ? 3 : 4));
-                        uint32_t oinfo = 0;
-                        int oqbase = -1;
-#pragma unroll
-                        for (int k = 0; k < 5; ++k)
-                            if (kx == k) {
-                                oinfo = xinfo[k];
-                                oqbase = xqbase[k];
-                            }
-                        if (offA == 0 && du <= 0) {
-                            oinfo = ko == 0 ? cell[0].info : (ko == 1 ? cell[1].info : cell[2].info);
-                            oqbase = ko == 0 ? cell[0].qbase : (ko == 1 ? cell[1].qbase : cell[2].qbase);
-                        }
                         if (oqbase < 0) continue;
                         const int cso = (int)(oinfo & 255u);
                         if (!ownsAxis(cso, al, ox, oy, oz)) continue;
@@ -1476,15 +1512,15 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
                         for (int a2 = 0; a2 < 2; ++a2)
                             if (a2 < al && ownsAxis(cso, a2, ox, oy, oz)) ++r;
                         const int q2 = oqbase + r;
-                        const int edgyO = ((csA >> edgeV0(eA)) & 1u) ? 0 : 1;
-                        const int sA = quadSlot(eA, edgyO), sB = quadSlot(eB, edgyO);
+                        // the shared halfedge's slot in that quad, by the sign of
+                        // A's corner at the candidate edge's start
+                        const uint32_t v0 = (hd >> (6 + 6 * cand)) & 7u;
+                        const uint32_t code = (en >> (((csA >> v0) & 1u) ? 20 : 24)) & 15u;
                         int id = 0x7FFFFFFF, o = -1;
-                        if (((sA + 1) & 3) == sB) {
-                            id = 4 * q2 + sA;
-                            o = vbA + tA;
-                        } else if (((sB + 1) & 3) == sA) {
-                            id = 4 * q2 + sB;
-                            o = vbB + tB;
+                        if (code & 8u) {
+                            id = 4 * q2 + (int)(code & 3u);
+                            o = (code & 4u) ? quadV[hi] : quadV[(hi + 1) & 3];
+                            ++found;
                         } else {
                             atomicOr(&ctr->status, kStatusBadIndex);
                         }
@@ -1499,7 +1535,16 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
                             org[3] = o;
                         }
                     }
-                    // sort the bucket (absent entries last) with its origins
+                    const int n = 1 + found;
+                    int me = 0, twin = -1;
+                    if (found <= 1) {  // at most one other halfedge: the pair needs no sorting
+                        const int other = min(ids[1], min(ids[2], ids[3]));
+                        if (found == 1) {
+                            twin = other;
+                            me = other < self ? 1 : 0;
+                        }
+                    } else {
+                        // sort the bucket (absent entries last) with its origins
 #define MDMC_CX(i0, i1)                                   \
     if (ids[i1] < ids[i0]) {                              \
         const int ti = ids[i0], to = org[i0];             \
@@ -1508,25 +1553,21 @@ __global__ void __launch_bounds__(256, MDMC_QUADS_MIN_BLOCKS) kQuads(const Activ
         ids[i1] = ti;                                     \
         org[i1] = to;                                     \
     }
-                    MDMC_CX(0, 1) MDMC_CX(2, 3) MDMC_CX(0, 2) MDMC_CX(1, 3) MDMC_CX(1, 2)
+                        MDMC_CX(0, 1) MDMC_CX(2, 3) MDMC_CX(0, 2) MDMC_CX(1, 3) MDMC_CX(1, 2)
 #undef MDMC_CX
-                    const int self = h0 + hi;
-                    const int n = 1 + (ids[1] != 0x7FFFFFFF) + (ids[2] != 0x7FFFFFFF) + (ids[3] != 0x7FFFFFFF);
-                    const int me = (ids[1] == self) ? 1 : (ids[2] == self) ? 2 : (ids[3] == self) ? 3 : 0;
-                    int partner = -1;
-                    if (n == 2) {
-                        partner = 1 - me;
-                    } else if (n == 3) {
-                        partner = me == 2 ? 0 : me + 1;
-                    } else if (n == 4) {  // "HACKY_OLD_WAY", HalfedgeMesh.cu:250-281
-                        if (org[0] != org[1]) partner = me ^ 1;       // (0,1) (2,3)
-                        else if (org[0] != org[2]) partner = me ^ 2;  // (0,2) (1,3)
-                        else partner = 3 - me;                        // (0,3) (1,2)
-                    }
-                    int twin = -1;
+                        me = (ids[1] == self) ? 1 : (ids[2] == self) ? 2 : (ids[3] == self) ? 3 : 0;
+                        int partner = -1;
+                        if (n == 3) {
+                            partner = me == 2 ? 0 : me + 1;
+                        } else if (n == 4) {  // "HACKY_OLD_WAY", HalfedgeMesh.cu:250-281
+                            if (org[0] != org[1]) partner = me ^ 1;       // (0,1) (2,3)
+                            else if (org[0] != org[2]) partner = me ^ 2;  // (0,2) (1,3)
+                            else partner = 3 - me;                        // (0,3) (1,2)
+                        }
 #pragma unroll
-                    for (int t2 = 0; t2 < 4; ++t2)
-                        if (partner == t2) twin = ids[t2];
+                        for (int t2 = 0; t2 < 4; ++t2)
+                            if (partner == t2) twin = ids[t2];
+                    }
                     out[hi] = make_int4(quadV[hi], q, h0 + ((hi + 1) & 3), twin);
                     valences |= (uint32_t)n << (8 * hi);
                     const int origin = quadV[hi];
@@ -1606,7 +1647,7 @@ void launchQuads(const ActiveCell* act, const int* quadOwner, int numActive, con
     ix.W = W;
     ix.divX = FastDiv((uint32_t)X);
     ix.divY = FastDiv((uint32_t)Y);
-    kQuads<<<(qEnd - qBegin + 255) / 256, 256, 0, s>>>(act, quadOwner, numActive, ix, he, faceFirst, faceAttr, vflags,
+    kQuads<<<(qEnd - qBegin + kQuadThreads - 1) / kQuadThreads, kQuadThreads, 0, s>>>(act, quadOwner, numActive, ix, he, faceFirst, faceAttr, vflags,
                                                         reinterpret_cast<uint32_t*>(heValence), nmList, nmCapacity,
                                                         numQuads, numVertices, quadsOut, vertexHE, ctr, qBegin,
                                                         qEnd);
