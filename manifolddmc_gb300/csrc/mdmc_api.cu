@@ -410,18 +410,23 @@ mdmc_status refreshTable(mdmc_context* c, uint32_t* status, cudaStream_t s) {
 mdmc_status finishMesh(mdmc_context* c, bool starsDone, uint32_t* status, cudaStream_t s,
                        const unsigned long long* gate = nullptr) {
     DevCounters* ctr = c->counters.as<DevCounters>();
-    MDMC_CHECK(c, c->vertexHE.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
+    const bool detect = c->opt.detect_non_manifold_vertices != 0;
+    // after the splitter, with the vertex pass's degrees kept: the DMC
+    // vertices it did not touch keep the stars the quad pass wrote
+    const bool keepStars = !starsDone && c->fastFans && detect;
+    MDMC_CHECK(c, c->vertexHE.grow(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1),
+                                   keepStars ? sizeof(int) * (size_t)c->dmcV : 0, s));
     MDMC_CHECK(c, c->degree.ensure(sizeof(int) * (size_t)std::max<int64_t>(c->V, 1)));
     MDMC_CHECK(c, c->quads.ensure(sizeof(int4) * (size_t)std::max<int64_t>(c->F, 1)));
     const MeshDims mdF{(int)c->V, (int)c->F, (int)c->H};
-    const bool detect = c->opt.detect_non_manifold_vertices != 0;
     // a changed mesh: output quads, face statistics and vertex stars in one
     // pass over the faces, before the detection that reads the stars (so the
     // stage times count this pass with the detection)
     if (!starsDone)
         launchOutput(c->he.as<int4>(), c->faceFirst.as<int>(), mdF, c->heValence.as<uint8_t>(),
                      c->faceNMValid ? c->faceNM.as<uint8_t>() : nullptr, c->quads.as<int4>(), c->vertexHE.as<int>(),
-                     detect ? c->degree.as<int>() : nullptr, ctr, status, s);
+                     detect ? c->degree.as<int>() : nullptr, keepStars ? c->splitTouched.as<uint8_t>() : nullptr,
+                     (int)c->dmcV, ctr, status, s);
     if (detect) {
         // fan keys are marked with this pass's number (1..255); the array is
         // cleared only when it is new or the numbers wrap around.  (A new

@@ -240,9 +240,12 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
                       int dmcV, cudaStream_t s);
 // output quads, quads_with_non_manifold_edges and the vertex stars
 // (smallest outgoing halfedge into vertexHE, 0x7F7F7F7F for none; the
-// out-degree into deg when given) from one walk per face
+// out-degree into deg when given) from one walk per face.  With touched
+// (after the splitter): the stars of DMC vertices (below dmcV) it did not
+// touch are left as the quad pass wrote them, and their deg is not written.
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, const uint8_t* faceNM,
-                  int4* quads, int* vertexHE, int* deg, DevCounters* ctr, uint32_t* status, cudaStream_t s);
+                  int4* quads, int* vertexHE, int* deg, const uint8_t* touched, int dmcV, DevCounters* ctr,
+                  uint32_t* status, cudaStream_t s);
 
 // valence-pattern simplifications
 void launchValence(const int4* he, MeshDims md, int* val, cudaStream_t s);

@@ -482,14 +482,17 @@ __global__ void kFanFast(const int4* __restrict__ he, MeshDims md, int* __restri
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     bool isSlow = false;
     if (v < md.V) {
-        const int ds = deg[v];
+        // a DMC vertex the splitter did not touch has the out-degree the vertex
+        // pass counted (the output pass left its star alone)
+        const bool kept = dmcDeg && v < dmcV && !touched[v];
+        const int ds = kept ? dmcDeg[v] : deg[v];
         const int d = ds < 0 ? -ds : ds;
         if (d == 0) {
             vertexHE[v] = -1;
             fans[v] = 0;
             slow[v] = 0;
             vflags[v] &= (uint8_t)~MDMC_VERTEX_MULTIPLE_FANS;
-        } else if ((vertexPassDegrees && ds > 0) || (dmcDeg && v < dmcV && !touched[v] && dmcDeg[v] > 0)) {
+        } else if ((vertexPassDegrees || kept) && ds > 0) {
             fans[v] = 1;
             slow[v] = 0;
             vflags[v] &= (uint8_t)~MDMC_VERTEX_MULTIPLE_FANS;
@@ -641,7 +644,8 @@ void launchDetectFans(const int4* he, MeshDims md, int* vertexHE, const int* deg
 // quad pass's size of every halfedge's bucket)
 __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__ faceFirst, MeshDims md,
                             const uint8_t* __restrict__ heValence, const uint8_t* __restrict__ faceNM,
-                            int4* __restrict__ quads, int* vertexHE, int* deg, DevCounters* ctr) {
+                            int4* __restrict__ quads, int* vertexHE, int* deg, const uint8_t* __restrict__ touched,
+                            int dmcV, DevCounters* ctr) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     int cnt = -1;
     if (f < md.F) {
@@ -676,11 +680,13 @@ __global__ void kFaceOutput(const int4* __restrict__ he, const int* __restrict__
         }
         quads[f] = make_int4(q[0], q[1], q[2], q[3]);
         // the vertex stars (smallest outgoing halfedge, out-degree) from the
-        // same four records: every halfedge lies in exactly one face
+        // same four records: every halfedge lies in exactly one face.  (With
+        // touched: a DMC vertex the splitter did not touch keeps the star the
+        // quad pass gave it, since none of its outgoing halfedges changed.)
         if (ok && vertexHE)
 #pragma unroll
             for (int i = 0; i < 4; ++i)
-                if (inb(q[i], md.V)) {
+                if (inb(q[i], md.V) && !(touched && q[i] < dmcV && !touched[q[i]])) {
                     atomicMin(&vertexHE[q[i]], hs[i]);
                     if (deg) atomicAdd(&deg[q[i]], 1);
                 }
@@ -713,17 +719,35 @@ void launchVertexHalfedgeFix(int* vertexHE, int numVertices, cudaStream_t s) {
     kVertexHalfedgeFix<<<(numVertices + 255) / 256, 256, 0, s>>>(vertexHE, numVertices);
 }
 
+// the stars the output pass recomputes start from "none" (0x7F7F7F7F; atomicMin
+// lowers it) and degree 0: every vertex's, or with touched only those of the
+// touched DMC vertices and of the vertices appended after them
+__global__ void kResetStars(int* vertexHE, int* deg, const uint8_t* __restrict__ touched, int dmcV, int numVertices) {
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < numVertices; v += gridDim.x * blockDim.x) {
+        if (v < dmcV && !touched[v]) continue;
+        vertexHE[v] = 0x7F7F7F7F;
+        if (deg) deg[v] = 0;
+    }
+}
+
 void launchOutput(const int4* he, const int* faceFirst, MeshDims md, const uint8_t* heValence, const uint8_t* faceNM,
-                  int4* quads, int* vertexHE, int* deg, DevCounters* ctr, uint32_t* status, cudaStream_t s) {
+                  int4* quads, int* vertexHE, int* deg, const uint8_t* touched, int dmcV, DevCounters* ctr,
+                  uint32_t* status, cudaStream_t s) {
     (void)status;
-    if (md.V > 0) {
-        // 0x7F7F7F7F marks "none"; atomicMin lowers it
-        cudaMemsetAsync(vertexHE, 0x7F, sizeof(int) * (size_t)md.V, s);
-        if (deg) cudaMemsetAsync(deg, 0, sizeof(int) * (size_t)md.V, s);
+    if (!touched) dmcV = 0;
+    if (md.V > 0 && vertexHE) {
+        if (touched) {
+            countLaunch();
+            kResetStars<<<std::min((md.V + 255) / 256, 152 * 8), 256, 0, s>>>(vertexHE, deg, touched, dmcV, md.V);
+        } else {
+            cudaMemsetAsync(vertexHE, 0x7F, sizeof(int) * (size_t)md.V, s);
+            if (deg) cudaMemsetAsync(deg, 0, sizeof(int) * (size_t)md.V, s);
+        }
     }
     if (md.F > 0) {
         countLaunch();
-        kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, heValence, faceNM, quads, vertexHE, deg, ctr);
+        kFaceOutput<<<(md.F + 255) / 256, 256, 0, s>>>(he, faceFirst, md, heValence, faceNM, quads, vertexHE, deg,
+                                                        touched, dmcV, ctr);
     }
 }
 
