@@ -1213,16 +1213,18 @@ struct CellIndex {
     const int* first;
     int X, Y, Z, W;
     FastDiv divX, divY;  // by X and Y (decoding linear cell ids)
-    // index of cell (x,y,z) in the active-cell list, -1 if inactive or outside
+    // index of cell (x,y,z) in the active-cell list, -1 if inactive or outside.
+    // Without a branch: a cell outside reads word 0 and is then rejected, so
+    // that a caller's lookups can all be in flight together.
     __device__ __forceinline__ int find(int x, int y, int z) const {
-        if ((unsigned)x > (unsigned)(X - 2) || (unsigned)y > (unsigned)(Y - 2) || (unsigned)z > (unsigned)(Z - 2))
-            return -1;
+        const bool in =
+            (unsigned)x <= (unsigned)(X - 2) && (unsigned)y <= (unsigned)(Y - 2) && (unsigned)z <= (unsigned)(Z - 2);
         // (mask words number fewer than 2^27: grids have fewer than 2^32 samples)
-        const uint32_t w = ((uint32_t)z * (uint32_t)(Y - 1) + (uint32_t)y) * (uint32_t)W + (uint32_t)(x >> 5);
+        const uint32_t w = in ? ((uint32_t)z * (uint32_t)(Y - 1) + (uint32_t)y) * (uint32_t)W + (uint32_t)(x >> 5) : 0u;
         const uint32_t m = __ldg(mask + w);
         const int f = __ldg(first + w);
         const uint32_t bit = 1u << (x & 31);
-        return (m & bit) ? f + __popc(m & (bit - 1u)) : -1;
+        return (in && (m & bit)) ? f + __popc(m & (bit - 1u)) : -1;
     }
 };
 
@@ -1409,36 +1411,29 @@ __global__ void __launch_bounds__(kQuadThreads, MDMC_QUADS_MIN_BLOCKS) kQuads(co
                                 py + (axis == 1 ? dA : 0) + (b == 1 ? dB : 0) + (c == 1 ? dC : 0),
                                 pz + (axis == 2 ? dA : 0) + (c == 2 ? dC : 0));
             }
+            // the eight records, all loads issued before any is used (a
+            // missing cell loads record j and is then replaced)
+            ActiveCell r2[8];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) r2[k] = act[inb(jk[k + 1], numActive) ? jk[k + 1] : j];
+#pragma unroll
+            for (int k = 0; k < 5; ++k) r2[3 + k] = act[inb(jx[k], numActive) ? jx[k] : j];
             sInfo[0][tid] = rec.info;
             sQbase[0][tid] = rec.qbase;
             sVbase[0][tid] = rec.pad;
 #pragma unroll
             for (int k = 1; k < 4; ++k) {
-                uint32_t info = 0;
-                int qbase = 0, vbase = 0;
-                if (jk[k] < 0 || jk[k] >= numActive) {
-                    ok = false;
-                } else {
-                    const ActiveCell r2 = act[jk[k]];
-                    info = r2.info;
-                    qbase = r2.qbase;
-                    vbase = r2.pad;
-                }
-                sInfo[k][tid] = info;
-                sQbase[k][tid] = qbase;
-                sVbase[k][tid] = vbase;
+                const bool have = inb(jk[k], numActive);
+                if (!have) ok = false;
+                sInfo[k][tid] = have ? r2[k - 1].info : 0u;
+                sQbase[k][tid] = have ? r2[k - 1].qbase : 0;
+                sVbase[k][tid] = have ? r2[k - 1].pad : 0;
             }
 #pragma unroll
             for (int k = 0; k < 5; ++k) {
-                uint32_t info = 0;
-                int qbase = -1;  // no such active cell
-                if (inb(jx[k], numActive)) {
-                    const ActiveCell r2 = act[jx[k]];
-                    info = r2.info;
-                    qbase = r2.qbase;
-                }
-                sInfo[4 + k][tid] = info;
-                sQbase[4 + k][tid] = qbase;
+                const bool have = inb(jx[k], numActive);
+                sInfo[4 + k][tid] = have ? r2[3 + k].info : 0u;
+                sQbase[4 + k][tid] = have ? r2[3 + k].qbase : -1;  // -1: no such active cell
             }
             if (!ok) atomicOr(&ctr->status, kStatusMissingCell);
             const int ae = 2 * axis + ((cs & 1) ? 0 : 1);
