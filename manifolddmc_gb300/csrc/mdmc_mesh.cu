@@ -579,19 +579,39 @@ __global__ void kFanKeys(const int4* __restrict__ he, MeshDims md, const uint8_t
     }
 }
 
+// (the marks are read 16 at a time and compared four at a time; few match)
+__device__ __forceinline__ void countFanKey(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ slow,
+                                            int h, int* __restrict__ fans, uint32_t* status) {
+    const int v = he[h].x;
+    if (inb(v, md.V)) {
+        if (slow[v]) atomicAdd(&fans[v], 1);
+    } else {
+        atomicOr(status, kStatusBadIndex);
+    }
+}
 __global__ void kFanCount(const int4* __restrict__ he, MeshDims md, const uint8_t* __restrict__ slow,
                           const unsigned long long* slowCount, const uint8_t* __restrict__ isKey, uint8_t mark,
                           int* __restrict__ fans, uint32_t* status) {
     if (*slowCount == 0) return;
-    for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < md.H; h += gridDim.x * blockDim.x) {
-        if (isKey[h] != mark) continue;
-        const int v = he[h].x;
-        if (inb(v, md.V)) {
-            if (slow[v]) atomicAdd(&fans[v], 1);
-        } else {
-            atomicOr(status, kStatusBadIndex);
+    const uint32_t marks = 0x01010101u * mark;
+    const int chunks = md.H >> 4;  // whole 16-byte chunks (isKey is 256-byte aligned)
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < chunks; c += gridDim.x * blockDim.x) {
+        const uint4 k = reinterpret_cast<const uint4*>(isKey)[c];
+        const uint32_t words[4] = {k.x, k.y, k.z, k.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            uint32_t eq = __vcmpeq4(words[q], marks);  // 0xFF in every byte that holds the mark
+            while (eq) {
+                const int b = (__ffs(eq) - 1) >> 3;
+                eq &= ~(0xFFu << (8 * b));
+                countFanKey(he, md, slow, 16 * c + 4 * q + b, fans, status);
+            }
         }
     }
+    // the last H mod 16 marks, one each
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int h = 16 * chunks + t;
+    if (t < 16 && h < md.H && isKey[h] == mark) countFanKey(he, md, slow, h, fans, status);
 }
 
 // the vertices the single walk did not settle (kFanFast flagged the others;
