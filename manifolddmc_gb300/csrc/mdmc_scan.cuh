@@ -80,16 +80,51 @@ __device__ T blockExclusive(T v, T& total) {
 }
 
 // element readers: an array, or the popcounts of a bit-mask's words (the
-// per-word counts are then never stored)
+// per-word counts are then never stored).  A reader of 4-byte elements may
+// also read four at once (four(i, v): elements i..i+3, i a multiple of 4,
+// one 16-byte load per array); vectorOk() says on the host whether its
+// arrays are 16-byte aligned, which that needs.
 template <typename T>
 struct ArrayRead {
+    static constexpr bool kFour = sizeof(T) == 4;
     const T* __restrict__ p;
     __device__ __forceinline__ T operator[](int64_t i) const { return p[i]; }
+    __device__ __forceinline__ void four(int64_t i, T v[4]) const {
+        const int4 q = *reinterpret_cast<const int4*>(p + i);
+        v[0] = (T)q.x;
+        v[1] = (T)q.y;
+        v[2] = (T)q.z;
+        v[3] = (T)q.w;
+    }
+    bool vectorOk() const { return kFour && (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 };
 struct PopcRead {
+    static constexpr bool kFour = true;
     const uint32_t* __restrict__ p;
     __device__ __forceinline__ int operator[](int64_t i) const { return __popc(p[i]); }
+    __device__ __forceinline__ void four(int64_t i, int v[4]) const {
+        const uint4 q = *reinterpret_cast<const uint4*>(p + i);
+        v[0] = __popc(q.x);
+        v[1] = __popc(q.y);
+        v[2] = __popc(q.z);
+        v[3] = __popc(q.w);
+    }
+    bool vectorOk() const { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 };
+
+// elements i..i+3 (i a multiple of 4) into v, zero past n: one vector load
+// per array when the reader has one and all four lie below n
+template <typename T, class In>
+__device__ __forceinline__ void loadFour(const In& in, bool vec, int64_t i, int64_t n, T v[4]) {
+    if constexpr (In::kFour) {
+        if (vec && i + 3 < n) {
+            in.four(i, v);
+            return;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = i + k < n ? in[i + k] : ScanOps<T>::zero();
+}
 
 // called by the apply pass with every element's exclusive prefix and value,
 // and once with the element count and the total
@@ -116,15 +151,22 @@ struct ScanCount {
 __device__ __forceinline__ int64_t scanTiles(int64_t n) { return (n + kScanTile - 1) / kScanTile; }
 
 template <typename T, class In>
-__global__ void __launch_bounds__(kScanThreads) kScanReduce(In in, ScanCount cnt, T* __restrict__ tileSums) {
+__global__ void __launch_bounds__(kScanThreads) kScanReduce(In in, ScanCount cnt, T* __restrict__ tileSums, bool vec) {
     const int64_t n = cnt.get();
     if (blockIdx.x > 0 && blockIdx.x >= scanTiles(n)) return;
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
     T acc = ScanOps<T>::zero();
+    if (vec) {  // each thread its four consecutive elements (kScanItems == 4)
+        T v[4];
+        loadFour<T>(in, vec, base + (int64_t)threadIdx.x * kScanItems, n, v);
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        int64_t i = base + (int64_t)k * kScanThreads + threadIdx.x;
-        if (i < n) acc = ScanOps<T>::add(acc, in[i]);
+        for (int k = 0; k < 4; ++k) acc = ScanOps<T>::add(acc, v[k]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            int64_t i = base + (int64_t)k * kScanThreads + threadIdx.x;
+            if (i < n) acc = ScanOps<T>::add(acc, in[i]);
+        }
     }
     T total;
     blockExclusive(acc, total);
@@ -158,21 +200,19 @@ __global__ void __launch_bounds__(1024) kScanTiles(T* tileSums, ScanCount cnt) {
 // Each thread scans kScanItems consecutive elements straight from memory.
 template <typename T, class In, class Post>
 __global__ void __launch_bounds__(kScanThreads) kScanApply(In in, ScanCount cnt, const T* __restrict__ tileSums,
-                           T* __restrict__ out, Post post) {
+                           T* __restrict__ out, Post post, bool vec) {
     const int64_t n = cnt.get();
     const int nTiles = (int)scanTiles(n);
     const int lastBlock = nTiles > 0 ? nTiles - 1 : 0;
     if ((int)blockIdx.x > lastBlock) return;
     const int64_t base = (int64_t)blockIdx.x * kScanTile;
-    // each thread owns kScanItems consecutive elements
+    // each thread owns kScanItems (= 4) consecutive elements
+    static_assert(kScanItems == 4, "loadFour reads four elements");
     T vals[kScanItems];
+    loadFour<T>(in, vec, base + (int64_t)threadIdx.x * kScanItems, n, vals);
     T acc = ScanOps<T>::zero();
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        int64_t i = base + (int64_t)threadIdx.x * kScanItems + k;
-        vals[k] = i < n ? in[i] : ScanOps<T>::zero();
-        acc = ScanOps<T>::add(acc, vals[k]);
-    }
+    for (int k = 0; k < kScanItems; ++k) acc = ScanOps<T>::add(acc, vals[k]);
     T total;
     T run = ScanOps<T>::add(tileSums[blockIdx.x], blockExclusive(acc, total));
 #pragma unroll
@@ -255,9 +295,12 @@ bool exclusiveScanOf(In in, T* out, int64_t n, T* scratch, cudaStream_t s, Post 
     if (tiles > kScanMaxTiles) return false;
     const int nt = tiles > 0 ? (int)tiles : 1;
     const ScanCount cnt{n, nDev};
+    // (four elements per load only from 16-byte aligned arrays)
+    bool vec = false;
+    if constexpr (In::kFour) vec = in.vectorOk();
     if (n > 0 || nDev) {
         countLaunch();
-        kScanReduce<T, In><<<nt, kScanThreads, 0, s>>>(in, cnt, scratch);
+        kScanReduce<T, In><<<nt, kScanThreads, 0, s>>>(in, cnt, scratch, vec);
     } else {
         cudaMemsetAsync(scratch, 0, sizeof(T), s);
     }
@@ -268,7 +311,7 @@ bool exclusiveScanOf(In in, T* out, int64_t n, T* scratch, cudaStream_t s, Post 
         if constexpr (Post::kStaged)
             kScanApplyStaged<T, In, Post><<<nt, kScanThreads, 0, s>>>(in, cnt, scratch, out, post);
         else
-            kScanApply<T, In, Post><<<nt, kScanThreads, 0, s>>>(in, cnt, scratch, out, post);
+            kScanApply<T, In, Post><<<nt, kScanThreads, 0, s>>>(in, cnt, scratch, out, post, vec);
     } else {
         cudaMemcpyAsync(out, scratch, sizeof(T), cudaMemcpyDeviceToDevice, s);
     }

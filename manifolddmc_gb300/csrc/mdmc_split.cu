@@ -23,10 +23,18 @@ constexpr int kNone = -1;
 // reads each face's flag from its attributes, and its apply pass writes every
 // flagged face id to its place (no flag array, no compaction pass)
 struct FaceNMRead {
+    static constexpr bool kFour = true;
     const uint16_t* __restrict__ attr;
     __device__ __forceinline__ int operator[](int64_t f) const {
         return (attr[f] & MDMC_FACE_NON_MANIFOLD) ? 1 : 0;
     }
+    __device__ __forceinline__ void four(int64_t f, int v[4]) const {  // (8 bytes: four attributes)
+        const uint2 q = *reinterpret_cast<const uint2*>(attr + f);
+        const uint32_t w[2] = {q.x, q.y};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) v[k] = ((w[k >> 1] >> (16 * (k & 1))) & MDMC_FACE_NON_MANIFOLD) ? 1 : 0;
+    }
+    bool vectorOk() const { return (reinterpret_cast<uintptr_t>(attr) & 15u) == 0; }
 };
 struct CompactPost {
     static constexpr bool kStaged = false;
@@ -43,10 +51,22 @@ bool scanNMFaces(const uint16_t* attr, int numFaces, int* offsets, int* nmFaces,
 // copy-back selection (kept elements without an original are appended), read
 // by the scan that numbers them
 struct AppendRead {
+    static constexpr bool kFour = true;
     const uint32_t* __restrict__ fl;
     const int* __restrict__ c2o;
     __device__ __forceinline__ int operator[](int64_t i) const {
         return (!(fl[i] & 16u) && c2o[i] == -1) ? 1 : 0;  // kRemove, kNone
+    }
+    __device__ __forceinline__ void four(int64_t i, int v[4]) const {
+        const uint4 f = *reinterpret_cast<const uint4*>(fl + i);
+        const int4 c = *reinterpret_cast<const int4*>(c2o + i);
+        v[0] = (!(f.x & 16u) && c.x == -1) ? 1 : 0;
+        v[1] = (!(f.y & 16u) && c.y == -1) ? 1 : 0;
+        v[2] = (!(f.z & 16u) && c.z == -1) ? 1 : 0;
+        v[3] = (!(f.w & 16u) && c.w == -1) ? 1 : 0;
+    }
+    bool vectorOk() const {
+        return ((reinterpret_cast<uintptr_t>(fl) | reinterpret_cast<uintptr_t>(c2o)) & 15u) == 0;
     }
 };
 // (assignHalfedgeIDs: an appended element's mesh id, base + its number,
