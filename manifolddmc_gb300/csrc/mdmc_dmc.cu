@@ -763,6 +763,7 @@ __global__ void kScatterCells(const uint32_t* __restrict__ mask, const int* __re
 // kScatterCells once it knows the count and has the room).
 struct CellScatter {
     static constexpr bool kStaged = false;
+    static constexpr bool kPrefixes = true;
     const uint32_t* __restrict__ mask;
     uint32_t* __restrict__ cellIds;
     int64_t capacity;
@@ -801,6 +802,7 @@ bool scanMaskScatter(const uint32_t* mask, int* first, int64_t numWords, int W, 
 // there were more active cells than the scan covered).
 struct FinishPost {
     static constexpr bool kStaged = true;
+    static constexpr bool kPrefixes = false;  // (the records get the offsets; the counts array is not read)
     ActiveCell* __restrict__ act;
     int* __restrict__ quadOwner;
     int capQ;

@@ -160,11 +160,12 @@ void launchScatterCells(const uint32_t* mask, const int* first, int64_t numWords
 void launchEmitActive(const GridDesc& g, float iso, const uint32_t* cellIds, ActiveCell* act, int2* counts,
                       int numActive, CaseBytes cases, uint32_t* status, cudaStream_t s,
                       const int* numActiveDev = nullptr);
-// exclusive scan of the active cells' (vertex, quad) counts in place
-// (capA + 1 entries, the count read from numActiveDev when given) that also
-// writes each record's first vertex and quad id, the quad owners (the first
-// capQ) and gathered[0..2] = active cells, vertices, quads (-1, -1 for the
-// last two when the active cells exceed capA)
+// exclusive scan of the active cells' (vertex, quad) counts (capA + 1
+// entries, the count read from numActiveDev when given) into each record's
+// first vertex and quad id, the quad owners (the first capQ) and
+// gathered[0..2] = active cells, vertices, quads (-1, -1 for the last two
+// when the active cells exceed capA); of counts only counts[n], the total,
+// is rewritten
 bool scanCellCounts(int2* counts, int64_t capA, const int* numActiveDev, ActiveCell* act, int* quadOwner, int64_t capQ,
                     int* gathered, int* gatheredHost, int2* scratch, cudaStream_t s);
 // standard Marching Cubes (edge mask over global edge ids 3 * sample + axis,
@@ -275,13 +276,15 @@ void launchRenderBuffers(const float* pos, const float* nrm, const uint8_t* vfla
 // face coloring 24 -> 5 colors in place (orig: one byte per face of scratch)
 void launchColorFaces(const int4* he, const int* faceFirst, uint16_t* attr, uint8_t* orig, int numFaces, int numHalfedges,
                       cudaStream_t s);
-// exclusive prefix of the non-manifold face flags into offsets (numFaces + 1
-// entries) and the flagged face ids into nmFaces (capacity numFaces); false
-// when numFaces is beyond the scan's size
+// the number of non-manifold faces into offsets[numFaces] (the per-face
+// prefixes are not written) and the flagged face ids, ascending, into nmFaces
+// (capacity numFaces); false when numFaces is beyond the scan's size
 bool scanNMFaces(const uint16_t* attr, int numFaces, int* offsets, int* nmFaces, int* scratch, cudaStream_t s);
 // exclusive prefix of "kept and without an original" over count copy
-// elements; with assignBase >= 0 each such element's c2o entry becomes
-// assignBase + its number (the halfedges' new ids, before the copy-back)
+// elements into offsets (count + 1 entries); with assignBase >= 0 instead
+// each such element's c2o entry becomes assignBase + its number (the
+// halfedges' new ids, before the copy-back) and only offsets[count], the
+// total, is written
 bool scanAppends(const uint32_t* fl, int* c2o, int count, int* offsets, int* scratch, cudaStream_t s,
                  int assignBase = -1);
 void launchFillInt(int* p, int64_t n, int v, cudaStream_t s);

@@ -127,9 +127,11 @@ __device__ __forceinline__ void loadFour(const In& in, bool vec, int64_t i, int6
 }
 
 // called by the apply pass with every element's exclusive prefix and value,
-// and once with the element count and the total
+// and once with the element count and the total; kPrefixes false: the apply
+// pass writes only out[n], the total
 struct NoPost {
     static constexpr bool kStaged = false;
+    static constexpr bool kPrefixes = true;
     template <typename T>
     __device__ __forceinline__ void operator()(int64_t, T, T) const {}
     template <typename T>
@@ -219,7 +221,7 @@ __global__ void __launch_bounds__(kScanThreads) kScanApply(In in, ScanCount cnt,
     for (int k = 0; k < kScanItems; ++k) {
         int64_t i = base + (int64_t)threadIdx.x * kScanItems + k;
         if (i < n) {
-            out[i] = run;
+            if constexpr (Post::kPrefixes) out[i] = run;
             post(i, run, vals[k]);
         }
         run = ScanOps<T>::add(run, vals[k]);
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__(kScanThreads) kScanApplyStaged(In in, ScanCoun
         const int64_t i = base + idx;
         if (i < n) {
             const T r = stage[idx];
-            out[i] = r;
+            if constexpr (Post::kPrefixes) out[i] = r;
             post(i, r, minus(idx + 1 < kScanTile ? stage[idx + 1] : tileEnd, r));
         }
     }

@@ -38,6 +38,7 @@ struct FaceNMRead {
 };
 struct CompactPost {
     static constexpr bool kStaged = false;
+    static constexpr bool kPrefixes = false;  // (only the total and the compacted list are read)
     int* out;
     __device__ __forceinline__ void operator()(int64_t i, int at, int v) const {
         if (v) out[at] = (int)i;
@@ -70,19 +71,22 @@ struct AppendRead {
     }
 };
 // (assignHalfedgeIDs: an appended element's mesh id, base + its number,
-// written by the apply pass into its copy -> original map)
+// written by the apply pass into its copy -> original map; the per-element
+// numbers are then not written, only their total)
 struct AssignPost {
     static constexpr bool kStaged = false;
+    static constexpr bool kPrefixes = false;
     int* c2o;
     int base;
     __device__ __forceinline__ void operator()(int64_t i, int at, int v) const {
-        if (v && c2o) c2o[i] = base + at;
+        if (v) c2o[i] = base + at;
     }
     __device__ __forceinline__ void total(int64_t, int) const {}
 };
 bool scanAppends(const uint32_t* fl, int* c2o, int count, int* offsets, int* scratch, cudaStream_t s, int assignBase) {
-    return exclusiveScanOf<int>(AppendRead{fl, c2o}, offsets, count, scratch, s,
-                                AssignPost{assignBase >= 0 ? c2o : nullptr, assignBase});
+    if (assignBase >= 0)
+        return exclusiveScanOf<int>(AppendRead{fl, c2o}, offsets, count, scratch, s, AssignPost{c2o, assignBase});
+    return exclusiveScanOf<int>(AppendRead{fl, c2o}, offsets, count, scratch, s);
 }
 
 __global__ void kFillInt(int* p, int64_t n, int v) {
