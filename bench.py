@@ -157,8 +157,9 @@ def algorithmic_bytes(kernel, s):
         return 4 * S + 8 * words
     if kernel == "emit":  # mask + offsets read; records and {contours, quads} counts written, counts scanned in place
         return 8 * words + 16 * A + 8 * A + 16 * A
-    if kernel == "vertices":  # records read, positions + normals written
-        return 16 * A + 24 * V
+    if kernel == "vertices":  # records read; positions + normals (24 B), the vertex pass's degree (4 B) and the
+        # quad pass's starting flags (1 B) and smallest-outgoing-halfedge seed (4 B) written per vertex
+        return 16 * A + (24 + 4 + 1 + 4) * V
     if kernel == "quads":  # read: each active cell's record (16 B) and the mask word and first-cell offset
         # that find it (8 B), each quad's owner (4 B); written: halfedges with twins (64 B), valences (4 B),
         # face first halfedge (4 B), attributes (2 B), output quad (16 B) per quad, and each vertex's
@@ -286,6 +287,10 @@ def run_ours(args, rank, world, local):
                 "algorithmic_bytes": ab, "kernel_ms_timed": round(dominant_ms, 4),
                 "kernel_ms": {k: round(v, 4) for k, v in breakdown.items()},
                 "kernel_ms_source": "warm-up steps with every kernel timed (the timed steps time only the dominant one)",
+                "by_kernel": {k: {"ms": round(v, 4), "algorithmic_bytes": algorithmic_bytes(k, sizes),
+                                  "achieved": round(algorithmic_bytes(k, sizes) / (v / 1e3) / 1e9, 1) if v > 0 else None,
+                                  "frac": round(algorithmic_bytes(k, sizes) / (v / 1e3) / 1e9 / peak, 4) if v > 0 else None}
+                              for k, v in breakdown.items()},
                 "whole_step_bytes": survey_bytes(sizes),
                 "whole_step_gbs": round(survey_bytes(sizes) / (ms / 1e3) / 1e9, 1),
                 "whole_step_frac": round(survey_bytes(sizes) / (ms / 1e3) / 1e9 / peak, 4)}
