@@ -140,3 +140,37 @@ def test_noise513_same_mesh_on_a_reused_context():
         assert torch.equal(first[k], second[k]), k
     del first, second, dmc
     torch.cuda.empty_cache()
+
+
+def test_detection_when_growing_into_reused_device_memory():
+    """A context that grows its arrays for a larger grid can be handed memory
+    just freed by another array, still holding that array's bytes.  The fan
+    detection marks keys with the pass's number and clears its key array only
+    when the array is new, so "new" has to be told by the capacity, not the
+    address (a freed address can come back).  Freed memory holding every byte
+    value before each growth, one context through grids of growing size gives
+    the meshes fresh contexts give."""
+    import torch
+    sizes = (20, 36, 52, 68, 84)
+    grids = [mdmc.UniformGrid(uniform_noise(n, seed=40 + n)) for n in sizes]
+    expect = []
+    for g in grids:
+        fresh = mdmc.DualMarchingCubes()
+        fresh.run(0.5, g)
+        expect.append((fresh.get_num_non_manifold_vertices(), fresh.get_halfedge_mesh()))
+        del fresh
+    dmc = mdmc.DualMarchingCubes()
+    for (nm, ref), g in zip(expect, grids):
+        # memory holding every byte value, returned to the driver before the run grows its arrays
+        junk = (torch.arange(16 << 20, device="cuda", dtype=torch.int32) % 256).to(torch.uint8)
+        del junk
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        dmc.run(0.5, g)
+        assert dmc.get_num_non_manifold_vertices() == nm
+        m = dmc.get_halfedge_mesh()
+        assert np.array_equal(m.vertex_flags, ref.vertex_flags)
+        assert np.array_equal(m.halfedges, ref.halfedges)
+        assert np.array_equal(m.vertex_halfedge, ref.vertex_halfedge)
+    del dmc
+    torch.cuda.empty_cache()
