@@ -791,17 +791,20 @@ cudaError_t copyOut(mdmc_context* c, void* dst, const void* src, size_t bytes) {
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->copyStream);
 }
 
-mdmc_status earlyCopyFaces(mdmc_context* c, int64_t q0, int64_t q1, cudaStream_t s) {
+// the halfedges and output quads of quads [q0, q1); with faces also the face
+// first halfedges and attributes of quads [0, q1) (small arrays, copied once
+// after the last range: every copy costs the link time of its own)
+mdmc_status earlyCopyFaces(mdmc_context* c, int64_t q0, int64_t q1, bool faces, cudaStream_t s) {
     const mdmc_host_mesh* h = c->hostOut;
     mdmc_status st = copyAfter(c, 0, s);
     if (st != MDMC_OK) return st;
     const size_t n = (size_t)(q1 - q0);
     MDMC_CHECK(c, copyOut(c, h->halfedges ? h->halfedges + 16 * q0 : nullptr, c->he.as<int4>() + 4 * q0, 4 * sizeof(int4) * n));
     MDMC_CHECK(c, copyOut(c, h->quads ? h->quads + 4 * q0 : nullptr, c->quads.as<int4>() + q0, sizeof(int4) * n));
-    MDMC_CHECK(c, copyOut(c, h->face_first_halfedge ? h->face_first_halfedge + q0 : nullptr, c->faceFirst.as<int>() + q0,
-                          sizeof(int) * n));
-    MDMC_CHECK(c, copyOut(c, h->face_attributes ? h->face_attributes + q0 : nullptr, c->faceAttr.as<uint16_t>() + q0,
-                          sizeof(uint16_t) * n));
+    if (faces) {
+        MDMC_CHECK(c, copyOut(c, h->face_first_halfedge, c->faceFirst.as<int>(), sizeof(int) * (size_t)q1));
+        MDMC_CHECK(c, copyOut(c, h->face_attributes, c->faceAttr.as<uint16_t>(), sizeof(uint16_t) * (size_t)q1));
+    }
     return MDMC_OK;
 }
 
@@ -1243,7 +1246,7 @@ mdmc_status mdmc_run(mdmc_context* c, const mdmc_grid* grid, float iso, mdmc_mes
                     c->faceAttr.as<uint16_t>(), c->vflags.as<uint8_t>(), c->heValence.as<uint8_t>(),
                     c->nmList.as<int4>(), (int)(Q + 1), (int)Q, (int)Vd, c->quads.as<int4>(), c->vertexHE.as<int>(),
                     ctr, (int)q0, (int)q1, s);
-        if (early && (st = earlyCopyFaces(c, q0, q1, s)) != MDMC_OK) return st;
+        if (early && (st = earlyCopyFaces(c, q0, q1, k == ranges - 1, s)) != MDMC_OK) return st;
     }
     c->earlyFaces = early;
     c->faceNMValid = false;  // the quad pass wrote heValence
